@@ -1,0 +1,321 @@
+"""Benchmark: detected coincidences/s of the plain Monte Carlo on one GB300.
+
+Workload (one step = one full acquisition, simulated and digitized):
+  F-18 uniform in a 3 cm-radius cylinder (positron range on), 128^3 voxels of
+  0.5 mm (water, four bone rods, lung sphere), 1e8 decays in [0, 120] s,
+  8-panel LYSO ring at 8 cm (8x8 crystals of 3x3x20 mm), energy blur 12%,
+  paralyzable dead time 300 ns per block, window 350-650 keV, coincidence
+  window 4 ns. Seeded synthetic inputs written in gPET's own file formats.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0). `value` = coincidences / device time with the
+scene resident on the GPU (CUDA events on the library's stream); `e2e` = the
+same metric through the C ABI with host buffers (phantom upload, run, singles
+and coincidence copy-out) timed on the host clock. The reference arm
+(--impl reference) times the CPU oracle, the restatement of the reference's
+algorithm, on all host cores (the reference's own GPU build does not compile
+with CUDA 13).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "detected coincidences/s on 1 GB300 (plain MC)"
+UNIT = "coincidences/s"
+WORKLOAD = ("positron: F-18 cylinder r=3 cm (positron range on), 128^3 x 0.5 mm water/bone/lung phantom, "
+            "1e8 decays per step, 8-panel LYSO ring at 8 cm (8x8 crystals 3x3x20 mm), blur 12%, "
+            "paralyzable dead time 0.3 us per block, window 350-650 keV, coincidence window 4 ns")
+
+# Algorithmic bytes of the source+phantom kernel, per decay (the model of the
+# gPET path's data movement: per photon 44 B source state written, 88 B phantom
+# state read+written, 5 B per Woodcock step for the voxel (u8 material + f32
+# density), 44 B per photon handed to the detector).
+def algorithmic_bytes_source_phantom(n_decays, ph_steps, entered):
+    return 2 * n_decays * (44 + 88) + 5 * ph_steps + 44 * entered
+
+
+# DRAM bytes per decay of k_source_phantom measured by ncu (dram__bytes_read.sum
+# + dram__bytes_write.sum of one launch on a 2^22-decay case of this workload);
+# None until a capture exists.
+MEASURED_DRAM_BYTES_PER_DECAY = None
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_scene(directory, n_decays):
+    from gpet_gb300 import scenes
+    return scenes.positron(directory, n_decays=n_decays)
+
+
+def cpu_baseline(scene, seconds, threads=0, max_decays=200_000_000):
+    """The oracle (FP64, OpenMP over decays) on a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import bridge
+    bridge.build()
+    o = bridge.OracleScene(scene.config_path, scene.options, os.path.join(ROOT, "data"), base_dir=scene.directory)
+    n0 = 200_000
+    t0 = time.perf_counter()
+    o.run(0, n0, precision="fp64", threads=threads)
+    rate = n0 / max(time.perf_counter() - t0, 1e-6)
+    n = int(min(max(n0, rate * seconds), max_decays, o.n_decays))
+    t0 = time.perf_counter()
+    r = o.run(0, n, precision="fp64", threads=threads)
+    dt = time.perf_counter() - t0
+    cores = threads if threads > 0 else (os.cpu_count() or 1)
+    return {"value": r["n_coinc"] / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d of the %d decays (oracle FP64, %d threads, %.1f s)" % (n, o.n_decays, cores, dt),
+            "decays_per_s": n / dt, "coincidences": r["n_coinc"]}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory() as d:
+        sc = make_scene(d, args.decays)
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import bridge
+        bridge.build()
+        o = bridge.OracleScene(sc.config_path, sc.options, os.path.join(ROOT, "data"), base_dir=d)
+        n0 = 200_000
+        t0 = time.perf_counter()
+        o.run(0, n0, precision="fp64")
+        rate = n0 / max(time.perf_counter() - t0, 1e-6)
+        n = int(min(o.n_decays, max(n0, rate * args.ref_step_seconds)))
+        for w in range(args.warmup):
+            o.run(0, min(n, 200_000), precision="fp64")
+        tot_c, tot_t, tot_d = 0, 0.0, 0
+        for k in range(args.steps):
+            b = (k * n) % max(1, o.n_decays - n + 1)
+            t0 = time.perf_counter()
+            r = o.run(b, b + n, precision="fp64")
+            tot_t += time.perf_counter() - t0
+            tot_c += r["n_coinc"]
+            tot_d += n
+        value = tot_c / tot_t
+        cores = os.cpu_count() or 1
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": WORKLOAD, "decays_per_step": n, "sample_of": o.n_decays},
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                                 "sample": "%d decays per step of the %d-decay workload, oracle FP64, %d threads"
+                                           % (n, o.n_decays, cores)},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "decays_per_s": tot_d / tot_t}
+        print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if not args.gloo else "gloo")
+    import torch
+    from gpet_gb300 import api, formats as F
+    torch.cuda.set_device(local)
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda:%d" % local)   # 512 MB > L2
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    with tempfile.TemporaryDirectory() as d:
+        sc = make_scene(d, args.decays)
+        data = os.path.join(ROOT, "data")
+        ctx = api.Context(local)
+        opts = dict(sc.options, data_dir=data, base_dir=d, sim_id=rank)
+        ctx.set_options(opts)
+        ctx.load_config(sc.config_path)
+        for w in range(args.warmup):
+            ctx.set_option("seed", 1000 + w)
+            ctx.run()
+        sampler = ClockSampler(local)
+        barrier()
+        sampler.start()
+        t_wall0 = time.perf_counter()
+        tot = {"coinc": 0, "ms": 0.0, "ms_sp": 0.0, "ms_det": 0.0, "ms_dig": 0.0, "launches": 0, "ph_steps": 0,
+               "entered": 0, "decays": 0, "singles": 0, "true": 0, "scatter": 0, "random": 0, "chunks": 0}
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ctx.set_option("seed", 20261203 + k)
+            st = ctx.run()
+            tot["coinc"] += st["n_coinc"]; tot["ms"] += st["ms_total"]; tot["ms_sp"] += st["ms_source_phantom"]
+            tot["ms_det"] += st["ms_detector"]; tot["ms_dig"] += st["ms_digitizer"]
+            tot["launches"] += st["kernel_launches"]; tot["ph_steps"] += st["phantom_steps"]
+            tot["entered"] += st["n_entered"]; tot["decays"] += st["n_decays"]; tot["singles"] += st["n_singles"]
+            tot["true"] += st["n_true"]; tot["scatter"] += st["n_scatter"]; tot["random"] += st["n_random"]
+            tot["chunks"] += -(-st["n_decays"] // (1 << 24))
+        barrier()
+        wall = time.perf_counter() - t_wall0
+        clocks = sampler.stop()
+        ms = tot["ms"]
+        if dist:
+            t = torch.tensor([ms, float(tot["coinc"])], dtype=torch.float64, device="cuda:%d" % local)
+            mx = t[:1].clone(); dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+            sm = t[1:].clone(); dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+            ms_max, coinc_all = float(mx.item()), float(sm.item())
+        else:
+            ms_max, coinc_all = ms, float(tot["coinc"])
+        value = coinc_all / (ms_max * 1e-3)
+        # e2e through the C ABI with host buffers
+        mat, den = F.read_phantom(os.path.join(d, "phantom_mat.dat"), os.path.join(d, "phantom_den.dat"),
+                                  (128, 128, 128))
+        cfg = F.read_config(sc.config_path)
+        e2e_steps = max(2, args.steps // 2)
+        barrier()
+        t0 = time.perf_counter()
+        e_coinc, h2d, d2h = 0, 0, 0
+        for k in range(e2e_steps):
+            ctx.set_option("seed", 777 + k)
+            ctx.set_phantom(mat, den, cfg.pdim, cfg.poffset, cfg.psize)
+            st = ctx.run()
+            singles, scat = ctx.singles()
+            pairs, cls = ctx.coincidences()
+            e_coinc += len(pairs)
+            h2d += mat.nbytes + den.nbytes
+            d2h += singles.nbytes + scat.nbytes + pairs.nbytes + cls.nbytes
+        barrier()
+        e_wall = time.perf_counter() - t0
+        ctx.close()
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peak, peak_kind = _peaks()
+    n_launch_sp = max(1, tot["chunks"])
+    bytes_sp = algorithmic_bytes_source_phantom(tot["decays"], tot["ph_steps"], tot["entered"])
+    dur_sp = tot["ms_sp"] * 1e-3 / n_launch_sp
+    achieved = (bytes_sp / n_launch_sp) / dur_sp / 1e9
+    traffic = None
+    if MEASURED_DRAM_BYTES_PER_DECAY is not None:
+        traffic = MEASURED_DRAM_BYTES_PER_DECAY * tot["decays"] / n_launch_sp
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded, written in gPET input formats)",
+        "config": {"workload": WORKLOAD, "decays_per_step": args.decays, "l2": "flushed between steps (512 MB write)",
+                   "per_rank": "independent acquisitions (disjoint Philox keys)"},
+        "gpu_launches": tot["launches"],
+        "breakdown_ms_per_step": {"source_phantom": tot["ms_sp"] / args.steps, "detector": tot["ms_det"] / args.steps,
+                                  "digitizer_and_coincidences": tot["ms_dig"] / args.steps},
+        "counts_per_step": {"decays": tot["decays"] / args.steps, "singles": tot["singles"] / args.steps,
+                            "coincidences": tot["coinc"] / args.steps, "true": tot["true"] / args.steps,
+                            "scatter": tot["scatter"] / args.steps, "random": tot["random"] / args.steps},
+        "decays_per_s": tot["decays"] * world / (ms_max * 1e-3),
+        "roofline": {"kernel": "k_source_phantom", "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": bytes_sp / n_launch_sp,
+                     "launch_ms": dur_sp * 1e3},
+        "e2e": {"value": e_coinc / e_wall, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
+                "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps},
+        "clocks": clocks,
+        "wall_s_timed_region": wall,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        with tempfile.TemporaryDirectory() as d2:
+            line["cpu_baseline"] = cpu_baseline(make_scene(d2, args.decays), args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--decays", type=int, default=100_000_000)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=4.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--gloo", action="store_true", help=argparse.SUPPRESS)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

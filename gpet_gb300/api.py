@@ -1,0 +1,255 @@
+"""Python mirror of the C ABI in include/gpet.h (ctypes over libgpet.so).
+
+The native library is the product: every call here goes to the CUDA
+implementation, and a missing or unloadable library raises GpetError instead
+of falling back to anything else.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .formats import EVENT_DTYPE
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgpet.so")
+
+GPET_OK = 0
+ERRORS = {-1: "bad argument or state", -2: "missing or malformed input file", -3: "CUDA runtime error",
+          -4: "a bounded buffer overflowed", -5: "no CUDA device or kernels not built for it"}
+
+EXIT_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("ux", "<f4"), ("uy", "<f4"), ("uz", "<f4"),
+                       ("E", "<f4"), ("nscat", "<i4"), ("t", "<f8"), ("status", "<i4"), ("panel", "<i4")])
+
+
+class GpetError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("gpet error %d (%s): %s" % (code, ERRORS.get(code, "?"), msg))
+        self.code = code
+
+
+class RunStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in (
+        "n_decays", "n_pairs", "n_entered", "n_pulses", "n_hits", "n_threshold", "n_deadtime", "n_singles",
+        "n_coinc", "n_true", "n_scatter", "n_random", "n_multiple", "n_overflow", "n_stepcap")] + [
+        (n, C.c_double) for n in ("ms_total", "ms_source_phantom", "ms_detector", "ms_digitizer",
+                                  "ms_coincidence")] + [
+        ("kernel_launches", C.c_int64), ("phantom_steps", C.c_int64), ("detector_steps", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_LIB = None
+
+
+def load_library(path=None):
+    """Load libgpet.so (built by gpet_gb300.build). Raises GpetError when absent."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise GpetError(-5, "%s is missing: run gpet_gb300.build.build() first" % p)
+    L = C.CDLL(p)
+    vp, i32, i64, u8p = C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_uint8)
+    L.gpet_create.argtypes = [C.c_int, C.POINTER(vp)]
+    L.gpet_destroy.argtypes = [vp]
+    L.gpet_destroy.restype = None
+    L.gpet_last_error.argtypes = [vp]
+    L.gpet_last_error.restype = C.c_char_p
+    L.gpet_set_option.argtypes = [vp, C.c_char_p, C.c_char_p]
+    L.gpet_load_config.argtypes = [vp, C.c_char_p]
+    L.gpet_load_tables.argtypes = [vp, C.c_char_p]
+    L.gpet_set_phantom.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.gpet_load_geometry.argtypes = [vp, C.c_char_p]
+    L.gpet_set_source_file.argtypes = [vp, C.c_char_p, C.c_float, C.c_float]
+    L.gpet_set_source_psf.argtypes = [vp, vp, i64, C.c_int]
+    L.gpet_run.argtypes = [vp, C.POINTER(RunStats)]
+    L.gpet_digitize.argtypes = [vp, vp, vp, vp, i64, C.POINTER(RunStats)]
+    L.gpet_get_singles.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
+    L.gpet_get_pulses.argtypes = [vp, vp, vp, vp, i64, C.POINTER(i64)]
+    L.gpet_get_coincidences.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
+    L.gpet_get_hits.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
+    L.gpet_get_exits.argtypes = [vp, vp, i64, C.POINTER(i64)]
+    L.gpet_write_outputs.argtypes = [vp, C.c_char_p]
+    L.gpet_get_panels.argtypes = [vp, vp, i32, C.POINTER(i32)]
+    L.gpet_get_counts.argtypes = [vp, vp]
+    L.gpet_get_source_layout.argtypes = [vp, vp, vp, i32, C.POINTER(i32)]
+    L.gpet_get_majorant.argtypes = [vp, C.c_int, vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.gpet_get_table.argtypes = [vp, C.c_int, vp, i64, C.POINTER(i64)]
+    if path is None:
+        _LIB = L
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class Context:
+    """One simulation context on one GPU (gpet_create / gpet_destroy)."""
+
+    def __init__(self, device=0, lib=None):
+        self.L = lib or load_library()
+        h = C.c_void_p()
+        rc = self.L.gpet_create(device, C.byref(h))
+        if rc != GPET_OK:
+            raise GpetError(rc, "gpet_create(device=%d) failed" % device)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gpet_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        if rc != GPET_OK:
+            raise GpetError(rc, self.L.gpet_last_error(self.h).decode(errors="replace"))
+
+    # ---- inputs
+    def set_option(self, key, value):
+        self._ck(self.L.gpet_set_option(self.h, str(key).encode(), str(value).encode()))
+
+    def set_options(self, opts):
+        for k, v in opts.items():
+            self.set_option(k, v)
+
+    def load_config(self, path):
+        self._ck(self.L.gpet_load_config(self.h, os.fspath(path).encode()))
+
+    def load_tables(self, data_dir):
+        self._ck(self.L.gpet_load_tables(self.h, os.fspath(data_dir).encode()))
+
+    def set_phantom(self, mat, den, dims, offset, size):
+        mat = np.ascontiguousarray(mat, np.int32)
+        den = np.ascontiguousarray(den, np.float32)
+        d = np.asarray(dims, np.int32)
+        o = np.asarray(offset, np.float32)
+        s = np.asarray(size, np.float32)
+        self._ck(self.L.gpet_set_phantom(self.h, _ptr(mat), _ptr(den), _ptr(d), _ptr(o), _ptr(s)))
+
+    def load_geometry(self, path):
+        self._ck(self.L.gpet_load_geometry(self.h, os.fspath(path).encode()))
+
+    def set_source_file(self, path, tstart, tend):
+        self._ck(self.L.gpet_set_source_file(self.h, os.fspath(path).encode(), tstart, tend))
+
+    def set_source_psf(self, records, ptype):
+        r = np.ascontiguousarray(records, np.float64).reshape(-1, 8)
+        self._ck(self.L.gpet_set_source_psf(self.h, _ptr(r), len(r), ptype))
+
+    # ---- run
+    def run(self):
+        st = RunStats()
+        self._ck(self.L.gpet_run(self.h, C.byref(st)))
+        return st.as_dict()
+
+    def digitize(self, pulses, scat, slot):
+        pulses = np.ascontiguousarray(pulses, EVENT_DTYPE)
+        scat = np.ascontiguousarray(scat, np.uint8)
+        slot = np.ascontiguousarray(slot, np.uint8)
+        st = RunStats()
+        self._ck(self.L.gpet_digitize(self.h, _ptr(pulses), _ptr(scat), _ptr(slot), len(pulses), C.byref(st)))
+        return st.as_dict()
+
+    # ---- outputs
+    def _count(self, fn, *nulls):
+        n = C.c_int64()
+        self._ck(fn(self.h, *nulls, 0, C.byref(n)))
+        return n.value
+
+    def singles(self):
+        n = self._count(self.L.gpet_get_singles, None, None)
+        ev = np.zeros(n, EVENT_DTYPE)
+        sc = np.zeros(n, np.uint8)
+        m = C.c_int64()
+        if n:
+            self._ck(self.L.gpet_get_singles(self.h, _ptr(ev), _ptr(sc), n, C.byref(m)))
+        return ev, sc
+
+    def pulses(self):
+        n = self._count(self.L.gpet_get_pulses, None, None, None)
+        ev = np.zeros(n, EVENT_DTYPE)
+        sc = np.zeros(n, np.uint8)
+        sl = np.zeros(n, np.uint8)
+        m = C.c_int64()
+        if n:
+            self._ck(self.L.gpet_get_pulses(self.h, _ptr(ev), _ptr(sc), _ptr(sl), n, C.byref(m)))
+        return ev, sc, sl
+
+    def coincidences(self):
+        n = self._count(self.L.gpet_get_coincidences, None, None)
+        pr = np.zeros((n, 2), np.int64)
+        cl = np.zeros(n, np.uint8)
+        m = C.c_int64()
+        if n:
+            self._ck(self.L.gpet_get_coincidences(self.h, _ptr(pr), _ptr(cl), n, C.byref(m)))
+        return pr, cl
+
+    def hits(self):
+        n = self._count(self.L.gpet_get_hits, None, None)
+        ids = np.zeros((n, 5), np.int32)
+        f = np.zeros((n, 5), np.float32)
+        m = C.c_int64()
+        if n:
+            self._ck(self.L.gpet_get_hits(self.h, _ptr(ids), _ptr(f), n, C.byref(m)))
+        return ids, f
+
+    def exits(self):
+        n = self._count(self.L.gpet_get_exits, None)
+        out = np.zeros(n, EXIT_DTYPE)
+        m = C.c_int64()
+        if n:
+            self._ck(self.L.gpet_get_exits(self.h, _ptr(out), n, C.byref(m)))
+        return out
+
+    def write_outputs(self, out_dir):
+        self._ck(self.L.gpet_write_outputs(self.h, os.fspath(out_dir).encode()))
+
+    # ---- introspection
+    def panels(self):
+        n = C.c_int32()
+        self._ck(self.L.gpet_get_panels(self.h, None, 0, C.byref(n)))
+        out = np.zeros((n.value, 32), np.float32)
+        self._ck(self.L.gpet_get_panels(self.h, _ptr(out), n.value, C.byref(n)))
+        return out
+
+    def counts(self):
+        out = np.zeros(4, np.int32)
+        self._ck(self.L.gpet_get_counts(self.h, _ptr(out)))
+        return tuple(int(v) for v in out)
+
+    def source_layout(self):
+        n = C.c_int32()
+        self._ck(self.L.gpet_get_source_layout(self.h, None, None, 0, C.byref(n)))
+        first = np.zeros(n.value, np.int64)
+        count = np.zeros(n.value, np.int64)
+        if n.value:
+            self._ck(self.L.gpet_get_source_layout(self.h, _ptr(first), _ptr(count), n.value, C.byref(n)))
+        return first, count
+
+    def majorant(self, which):
+        tab = np.zeros(4096, np.float32)
+        e0, ide = C.c_float(), C.c_float()
+        self._ck(self.L.gpet_get_majorant(self.h, which, _ptr(tab), C.byref(e0), C.byref(ide)))
+        return tab, e0.value, ide.value
+
+    def table(self, which):
+        n = C.c_int64()
+        self._ck(self.L.gpet_get_table(self.h, which, None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.float32)
+        self._ck(self.L.gpet_get_table(self.h, which, _ptr(out), n.value, C.byref(n)))
+        return out

@@ -1,0 +1,224 @@
+/* detmath.h - deterministic single/double precision math for the random-number
+ * transforms of the photon transport and the digitizer.
+ *
+ * Every function here is a fixed sequence of IEEE-754 operations that round the
+ * same way on the GPU (sm_103a, compiled with -fmad=false; fused steps are
+ * written as explicit fma) and on a CPU (gcc -ffp-contract=off): sqrt and
+ * division are correctly rounded on both, fma is a single rounding on both.
+ * The same source therefore yields bit-identical results in the CUDA kernels and
+ * in the FP32 build of the CPU oracle, which is what lets the transport be
+ * compared history by history.
+ *
+ * Methods (all from elementary series, coefficients are exact rationals):
+ *   log  : x = m 2^e, m in [sqrt(1/2), sqrt(2)); log m = 2 atanh(s),
+ *          s = (m-1)/(m+1), atanh series in s^2.
+ *   exp  : x = k ln2 + r, |r| <= ln2/2, Taylor series of e^r, scale by 2^k.
+ *   sin/cos of 2*pi*u : quadrant reduction on u (exact), Taylor series on
+ *          |x| <= pi/4.
+ * Accuracy is a few ulp, which the tests check against libm.
+ *
+ * This header is C99 and CUDA C++; it includes nothing from CUDA's math
+ * library beyond the rounding intrinsics. */
+#ifndef GPET_DETMATH_H
+#define GPET_DETMATH_H
+
+#include <stdint.h>
+#include <string.h>
+#include <math.h>
+
+#if defined(__CUDACC__)
+#define DM_FN __host__ __device__ __forceinline__
+#else
+#define DM_FN static inline
+#endif
+
+DM_FN float dm_fma(float a, float b, float c)
+{
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return fmaf(a, b, c);
+#endif
+}
+
+DM_FN double dm_fmad(double a, double b, double c)
+{
+#if defined(__CUDA_ARCH__)
+    return __fma_rn(a, b, c);
+#else
+    return fma(a, b, c);
+#endif
+}
+
+/* correctly rounded square root */
+DM_FN float dm_sqrt(float x)
+{
+#if defined(__CUDA_ARCH__)
+    return __fsqrt_rn(x);
+#else
+    return sqrtf(x);
+#endif
+}
+
+DM_FN uint32_t dm_f2u(float x)
+{
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(x);
+#else
+    uint32_t u; memcpy(&u, &x, 4); return u;
+#endif
+}
+
+DM_FN float dm_u2f(uint32_t u)
+{
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float x; memcpy(&x, &u, 4); return x;
+#endif
+}
+
+DM_FN uint64_t dm_d2u(double x)
+{
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t u; memcpy(&u, &x, 8); return u;
+#endif
+}
+
+DM_FN double dm_u2d(uint64_t u)
+{
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)u);
+#else
+    double x; memcpy(&x, &u, 8); return x;
+#endif
+}
+
+/* ln 2 split so that e*DM_LN2_HI is exact for |e| < 2^9 */
+#define DM_LN2_HI 0.693145751953125f
+#define DM_LN2_LO 1.428606765330187e-06f
+#define DM_INV_LN2 1.44269504088896341f
+#define DM_TWO_PI 6.28318530717958648f
+
+/* natural log of a positive normal float */
+DM_FN float dm_logf(float x)
+{
+    uint32_t b = dm_f2u(x);
+    int e = (int)((b >> 23) & 0xffu) - 127;
+    uint32_t mb = (b & 0x7fffffu) | 0x3f800000u;      /* m in [1,2) */
+    if (mb > 0x3fb504f3u) { mb -= 0x00800000u; e += 1; } /* m > sqrt(2): halve */
+    float m = dm_u2f(mb);
+    float s = (m - 1.0f) / (m + 1.0f);
+    float z = s * s;
+    /* 2 atanh(s) = s * (2 + z(2/3 + z(2/5 + z(2/7 + z 2/9)))) */
+    float p = dm_fma(z, 0.222222222f, 0.285714298f);
+    p = dm_fma(z, p, 0.400000006f);
+    p = dm_fma(z, p, 0.666666687f);
+    p = dm_fma(z, p, 2.0f);
+    float lm = s * p;
+    float fe = (float)e;
+    return dm_fma(fe, DM_LN2_HI, dm_fma(fe, DM_LN2_LO, lm));
+}
+
+/* e^x for |x| < 87 */
+DM_FN float dm_expf(float x)
+{
+    float kf = floorf(dm_fma(x, DM_INV_LN2, 0.5f));
+    float r = dm_fma(-kf, DM_LN2_HI, x);
+    r = dm_fma(-kf, DM_LN2_LO, r);
+    /* Taylor to r^8, |r| <= 0.347 */
+    float p = dm_fma(r, 2.48015873e-05f, 1.98412698e-04f);
+    p = dm_fma(r, p, 1.38888889e-03f);
+    p = dm_fma(r, p, 8.33333333e-03f);
+    p = dm_fma(r, p, 4.16666667e-02f);
+    p = dm_fma(r, p, 1.66666667e-01f);
+    p = dm_fma(r, p, 0.5f);
+    p = dm_fma(r, p, 1.0f);
+    p = dm_fma(r, p, 1.0f);
+    int k = (int)kf;
+    return p * dm_u2f((uint32_t)(k + 127) << 23);
+}
+
+/* sin and cos of 2*pi*u for any finite u (turns) */
+DM_FN void dm_sincos_turns(float u, float* s, float* c)
+{
+    float q = floorf(u * 4.0f + 0.5f);      /* nearest quarter turn */
+    float r = u - q * 0.25f;                /* exact, |r| <= 1/8 */
+    int qi = ((int)q) & 3;                  /* two's complement: mod 4 */
+    float x = r * DM_TWO_PI;                /* |x| <= pi/4 */
+    float z = x * x;
+    float sp = dm_fma(z, 2.75573192e-06f, -1.98412698e-04f);
+    sp = dm_fma(z, sp, 8.33333333e-03f);
+    sp = dm_fma(z, sp, -1.66666667e-01f);
+    float sn = dm_fma(x * z, sp, x);
+    float cp = dm_fma(z, -2.75573192e-07f, 2.48015873e-05f);
+    cp = dm_fma(z, cp, -1.38888889e-03f);
+    cp = dm_fma(z, cp, 4.16666667e-02f);
+    cp = dm_fma(z, cp, -0.5f);
+    float cs = dm_fma(z, cp, 1.0f);
+    switch (qi) {
+    case 0: *s = sn;  *c = cs;  break;
+    case 1: *s = cs;  *c = -sn; break;
+    case 2: *s = -sn; *c = -cs; break;
+    default: *s = -cs; *c = sn; break;
+    }
+}
+
+/* cube root of u in (0, 1] */
+DM_FN float dm_cbrtf(float u)
+{
+    float y = dm_expf(dm_logf(u) * 0.333333343f);
+    /* one Newton step on y^3 = u */
+    return y - (y * y * y - u) / (3.0f * y * y);
+}
+
+/* natural log of a positive normal double (decay-time sampling) */
+DM_FN double dm_log(double x)
+{
+    uint64_t b = dm_d2u(x);
+    int e = (int)((b >> 52) & 0x7ffu) - 1023;
+    uint64_t mb = (b & 0x000fffffffffffffull) | 0x3ff0000000000000ull;
+    if (mb > 0x3ff6a09e667f3bcdull) { mb -= 0x0010000000000000ull; e += 1; }
+    double m = dm_u2d(mb);
+    double s = (m - 1.0) / (m + 1.0);
+    double z = s * s;
+    /* 2 atanh(s) series to s^23 */
+    double p = 2.0 / 23.0;
+    p = dm_fmad(z, p, 2.0 / 21.0);
+    p = dm_fmad(z, p, 2.0 / 19.0);
+    p = dm_fmad(z, p, 2.0 / 17.0);
+    p = dm_fmad(z, p, 2.0 / 15.0);
+    p = dm_fmad(z, p, 2.0 / 13.0);
+    p = dm_fmad(z, p, 2.0 / 11.0);
+    p = dm_fmad(z, p, 2.0 / 9.0);
+    p = dm_fmad(z, p, 2.0 / 7.0);
+    p = dm_fmad(z, p, 2.0 / 5.0);
+    p = dm_fmad(z, p, 2.0 / 3.0);
+    p = dm_fmad(z, p, 2.0);
+    return dm_fmad((double)e, 0.69314718055994531, s * p);
+}
+
+/* uniform (0,1) float from 24 random bits: (k + 0.5) 2^-24, exact */
+DM_FN float dm_u01(uint32_t x)
+{
+    return ((float)(x >> 8) + 0.5f) * 5.9604644775390625e-08f;
+}
+
+/* uniform (0,1) double from 53 random bits */
+DM_FN double dm_u01d(uint32_t hi, uint32_t lo)
+{
+    uint64_t k = ((uint64_t)(hi >> 5) << 26) | (uint64_t)(lo >> 6);
+    return ((double)k + 0.5) * 1.1102230246251565e-16;
+}
+
+/* standard normal from two uniforms (Box-Muller, cosine branch) */
+DM_FN float dm_normal(float u1, float u2)
+{
+    float s, c;
+    dm_sincos_turns(u2, &s, &c);
+    return dm_sqrt(-2.0f * dm_logf(u1)) * c;
+}
+
+#endif /* GPET_DETMATH_H */

@@ -1,0 +1,597 @@
+// digitizer.cu - the digitizer chain and the coincidence sorter on the device
+// (the work gPET.cu:385-424 does with blur/energywindow/setSitenum/deadtime
+// kernels and four host std::sort round trips), for sm_103a.
+//
+//   blur + threshold      one pass, draws keyed by (parn, slot)
+//   time order            stable LSD radix sort on the IEEE bits of t
+//                         (8 passes of 8 bits), equal-t runs ordered by
+//                         (parn, slot): total order (t, parn, slot)
+//   site order            stable radix sort of the time order by site
+//   dead time             paralyzable: one comparison with the previous
+//                         pulse of the site; non-paralyzable: one thread per
+//                         cluster (a pulse >= tau after its predecessor starts
+//                         a cluster no earlier pulse can reach)
+//   energy window         ordered compaction of the time order
+//   coincidences          one thread per cluster of singles closer than the
+//                         window; pair counts, scan, write
+#include <algorithm>
+#include <vector>
+
+#include "kernels.h"
+#include "../../include/gpet.h"
+
+namespace gpet {
+
+constexpr int kTile = 4096;      // items per block in radix / scan kernels
+constexpr int kScanThreads = 1024;
+
+// ---------------------------------------------------------------- scan
+__global__ void k_scan_reduce(const uint32_t* __restrict__ in, int64_t n, uint32_t* __restrict__ aux)
+{
+    __shared__ uint32_t ws[32];
+    int64_t base = (int64_t)blockIdx.x * kTile;
+    uint32_t s = 0;
+    for (int k = threadIdx.x; k < kTile; k += blockDim.x) {
+        int64_t i = base + k;
+        if (i < n) s += in[i];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t v = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) aux[blockIdx.x] = v;
+    }
+}
+
+// block-wide exclusive scan of one value per thread (blockDim.x == 1024)
+__device__ __forceinline__ uint32_t block_exscan(uint32_t v, uint32_t* ws, uint32_t& total)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) ws[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t x = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0;
+        uint32_t xi = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, xi, o);
+            if (lane >= o) xi += t;
+        }
+        ws[lane] = xi - x;
+        if (lane == 31) ws[32] = xi;
+    }
+    __syncthreads();
+    uint32_t r = ws[w] + inc - v;
+    total = ws[32];
+    __syncthreads();
+    return r;
+}
+
+// exclusive scan of the per-block sums, single block
+__global__ void k_scan_aux(uint32_t* aux, int64_t nb, uint32_t* total)
+{
+    __shared__ uint32_t ws[33];
+    uint32_t carry = 0;
+    for (int64_t b0 = 0; b0 < nb; b0 += blockDim.x) {
+        int64_t i = b0 + threadIdx.x;
+        uint32_t v = i < nb ? aux[i] : 0;
+        uint32_t tot;
+        uint32_t e = block_exscan(v, ws, tot);
+        if (i < nb) aux[i] = carry + e;
+        carry += tot;
+    }
+    if (threadIdx.x == 0 && total) *total = carry;
+}
+
+__global__ void k_scan_down(const uint32_t* in, int64_t n, const uint32_t* __restrict__ aux, uint32_t* out)
+{
+    __shared__ uint32_t ws[33];
+    int64_t base = (int64_t)blockIdx.x * kTile;
+    uint32_t carry = aux[blockIdx.x];
+    constexpr int per = kTile / kScanThreads;   // 4 consecutive items per thread
+    uint32_t v[per];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < per; ++k) {
+        int64_t i = base + (int64_t)threadIdx.x * per + k;
+        v[k] = i < n ? in[i] : 0;
+        s += v[k];
+    }
+    uint32_t tot;
+    uint32_t e = block_exscan(s, ws, tot);
+    uint32_t run = carry + e;
+#pragma unroll
+    for (int k = 0; k < per; ++k) {
+        int64_t i = base + (int64_t)threadIdx.x * per + k;
+        if (i < n) out[i] = run;
+        run += v[k];
+    }
+}
+
+// exclusive scan in -> out (may alias), total written to *total (device)
+static void scan_exclusive(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* aux, uint32_t* total,
+                           cudaStream_t s, int64_t* launches)
+{
+    int64_t nb = (n + kTile - 1) / kTile;
+    if (nb == 0) {
+        cudaMemsetAsync(total, 0, sizeof(uint32_t), s);
+        return;
+    }
+    k_scan_reduce<<<(unsigned)nb, 256, 0, s>>>(in, n, aux);
+    k_scan_aux<<<1, kScanThreads, 0, s>>>(aux, nb, total);
+    k_scan_down<<<(unsigned)nb, kScanThreads, 0, s>>>(in, n, aux, out);
+    *launches += 3;
+}
+
+// ---------------------------------------------------------------- radix sort
+__global__ void __launch_bounds__(256) k_radix_hist(const uint64_t* __restrict__ keys, int64_t n, int shift,
+                                                    uint32_t* __restrict__ hist, int64_t nblocks)
+{
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    int64_t base = (int64_t)blockIdx.x * kTile;
+    for (int k = threadIdx.x; k < kTile; k += 256) {
+        int64_t i = base + k;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+// stable scatter: items of a tile keep their order within a digit
+__global__ void __launch_bounds__(256) k_radix_scatter(const uint64_t* __restrict__ kin,
+                                                       const uint32_t* __restrict__ vin, int64_t n, int shift,
+                                                       const uint32_t* __restrict__ off, int64_t nblocks,
+                                                       uint64_t* __restrict__ kout, uint32_t* __restrict__ vout)
+{
+    __shared__ uint32_t run[256];
+    __shared__ uint32_t wc[8][256];
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    run[tid] = 0;
+    const int64_t base = (int64_t)blockIdx.x * kTile;
+    const uint32_t goff = off[(int64_t)tid * nblocks + blockIdx.x];
+    __shared__ uint32_t soff[256];
+    soff[tid] = goff;
+    for (int r = 0; r < kTile / 256; ++r) {
+#pragma unroll
+        for (int ww = 0; ww < 8; ++ww) wc[ww][tid] = 0;
+        __syncthreads();
+        const int64_t i = base + (int64_t)r * 256 + tid;
+        const bool valid = i < n;
+        uint64_t key = valid ? kin[i] : 0ull;
+        uint32_t val = valid ? vin[i] : 0u;
+        uint32_t dig = valid ? (uint32_t)((key >> shift) & 255u) : 256u;
+        unsigned peers = __match_any_sync(0xffffffffu, dig);
+        uint32_t rank = __popc(peers & lt);
+        if (valid && rank == 0) wc[w][dig] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t pre = run[dig] + rank;
+            for (int ww = 0; ww < w; ++ww) pre += wc[ww][dig];
+            const uint32_t pos = soff[dig] + pre;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+        uint32_t add = 0;
+#pragma unroll
+        for (int ww = 0; ww < 8; ++ww) add += wc[ww][tid];
+        run[tid] += add;
+        __syncthreads();
+        (void)lane;
+    }
+}
+
+// sort (keys, vals) of length n by bits [0, nbits) of key, stably; result in
+// (ka, va) on return (the buffers are ping-ponged an even number of times)
+static void radix_sort(uint64_t*& ka, uint32_t*& va, uint64_t*& kb, uint32_t*& vb, int64_t n, int nbits,
+                       uint32_t* hist, uint32_t* aux, uint32_t* total, cudaStream_t s, int64_t* launches)
+{
+    if (n <= 1) return;
+    int64_t nb = (n + kTile - 1) / kTile;
+    for (int shift = 0; shift < nbits; shift += 8) {
+        k_radix_hist<<<(unsigned)nb, 256, 0, s>>>(ka, n, shift, hist, nb);
+        scan_exclusive(hist, hist, 256 * nb, aux, total, s, launches);
+        k_radix_scatter<<<(unsigned)nb, 256, 0, s>>>(ka, va, n, shift, hist, nb, kb, vb);
+        *launches += 2;
+        std::swap(ka, kb);
+        std::swap(va, vb);
+    }
+}
+
+// ---------------------------------------------------------------- stages
+// blur (gPET_kernals.cu:814-837) + threshold (energywindow :641-656 with
+// [Eth, 2 MeV]); survivors' pulse indices appended to sel, site stored
+__global__ void k_blur_threshold(PulseDev P, int64_t n, DigiParams prm, float* Eb, float* xb, float* yb, float* zb,
+                                 int32_t* site, uint32_t* sel, unsigned long long* nsel)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        bool keep = false;
+        if (i < n) {
+            const int32_t parn = P.parn[i];
+            const uint32_t slot = P.meta[i] & 0x7fu;
+            Stream st;
+            st_init(st, prm.key0, prm.key1, kTagBlur, ((uint64_t)(uint32_t)parn << 4) | slot);
+            float E = P.E[i], x = P.x[i], y = P.y[i], z = P.z[i];
+            float R = 0.0f;
+            if (prm.blurpolicy == 0) R = dm_sqrt(prm.Eref / E) * prm.Rref;
+            if (prm.blurpolicy == 1) R = prm.Rref + prm.Eslope * (E - prm.Eref) / 1.0e6f;
+            if (R < 0.0f) R = 0.0f;
+            float zn = st_normal(st);
+            E += zn * R * E / 2.35482f;
+            if (prm.Sblur > 0.0f) {
+                x += prm.Sblur * st_normal(st);
+                y += prm.Sblur * st_normal(st);
+                z += prm.Sblur * st_normal(st);
+            }
+            Eb[i] = E; xb[i] = x; yb[i] = y; zb[i] = z;
+            keep = !(E < prm.Eth || E > 2000000.0f);
+            // setSitenum, gPET_kernals.cu:607-640 (level 3 keeps the readout site)
+            int32_t sv;
+            switch (prm.dlevel) {
+            case 0: sv = 0; break;
+            case 1: sv = P.pann[i]; break;
+            case 2: sv = P.pann[i] * prm.moduleN + P.modn[i]; break;
+            default: sv = P.siten[i]; break;
+            }
+            site[i] = sv;
+        }
+        unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (m) {
+            unsigned long long b = 0;
+            int leader = __ffs(m) - 1;
+            if (lane == leader) b = atomicAdd(nsel, (unsigned long long)__popc(m));
+            b = __shfl_sync(0xffffffffu, b, leader);
+            if (keep) sel[b + __popc(m & lt)] = (uint32_t)i;
+        }
+    }
+}
+
+__global__ void k_time_keys(const uint32_t* __restrict__ sel, int64_t m, const double* __restrict__ t,
+                            uint64_t* key, uint32_t* val)
+{
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t p = sel[j];
+        key[j] = (uint64_t)__double_as_longlong(t[p]);
+        val[j] = p;
+    }
+}
+
+// order runs of equal t by (parn, slot)
+__global__ void k_tie_fix(const uint64_t* __restrict__ key, uint32_t* idx, int64_t m, const int32_t* __restrict__ parn,
+                          const uint8_t* __restrict__ meta)
+{
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        if (j > 0 && key[j] == key[j - 1]) continue;
+        if (j + 1 >= m || key[j + 1] != key[j]) continue;
+        int64_t e = j + 1;
+        while (e < m && key[e] == key[j]) e++;
+        for (int64_t a = j + 1; a < e; ++a) {
+            uint32_t v = idx[a];
+            uint64_t kv = ((uint64_t)(uint32_t)parn[v] << 8) | (meta[v] & 0x7fu);
+            int64_t b = a - 1;
+            while (b >= j) {
+                uint32_t u = idx[b];
+                uint64_t ku = ((uint64_t)(uint32_t)parn[u] << 8) | (meta[u] & 0x7fu);
+                if (ku <= kv) break;
+                idx[b + 1] = u;
+                b--;
+            }
+            idx[b + 1] = v;
+        }
+    }
+}
+
+__global__ void k_site_keys(const uint32_t* __restrict__ torder, int64_t m, const int32_t* __restrict__ site,
+                            uint64_t* key, uint32_t* val)
+{
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t p = torder[j];
+        key[j] = (uint64_t)(uint32_t)site[p];
+        val[j] = p;
+    }
+}
+
+// dead time (deadtime, gPET_kernals.cu:657-698, sequential semantics, FP64):
+// sorder is the (site, t, parn, slot) order
+__global__ void k_deadtime(const uint32_t* __restrict__ sorder, int64_t m, const int32_t* __restrict__ site,
+                           const double* __restrict__ t, double tau, int dtype, uint32_t* flags,
+                           unsigned long long* nalive)
+{
+    unsigned long long alive = 0;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t p = sorder[j];
+        if (dtype == 0) {
+            bool keep = true;
+            if (j > 0) {
+                const uint32_t q = sorder[j - 1];
+                keep = !(site[q] == site[p] && t[p] < t[q] + tau);
+            }
+            flags[p] = keep ? 1u : 0u;
+            alive += keep;
+        } else {
+            // anchors: first pulse of a site or >= tau after its predecessor
+            bool anchor = j == 0;
+            if (!anchor) {
+                const uint32_t q = sorder[j - 1];
+                anchor = site[q] != site[p] || !(t[p] < t[q] + tau);
+            }
+            if (!anchor) continue;
+            double tdead = t[p];
+            flags[p] = 1u;
+            alive++;
+            for (int64_t i = j + 1; i < m; ++i) {
+                const uint32_t a = sorder[i], b = sorder[i - 1];
+                if (site[a] != site[b] || !(t[a] < t[b] + tau)) break;   // next anchor
+                if (t[a] < tdead + tau) {
+                    flags[a] = 0u;
+                } else {
+                    flags[a] = 1u;
+                    alive++;
+                    tdead = t[a];
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) alive += __shfl_xor_sync(0xffffffffu, alive, o);
+    if ((threadIdx.x & 31) == 0 && alive) atomicAdd(nalive, alive);
+}
+
+// energy window (gPET.cu:418) predicate over the time order
+__global__ void k_window_pred(const uint32_t* __restrict__ torder, int64_t m, const uint32_t* __restrict__ flags,
+                              const float* __restrict__ Eb, float lo, float hi, uint32_t* pred)
+{
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t p = torder[j];
+        const float E = Eb[p];
+        pred[j] = (flags[p] && !(E < lo || E > hi)) ? 1u : 0u;
+    }
+}
+
+__global__ void k_compact(const uint32_t* __restrict__ torder, const uint32_t* __restrict__ pred,
+                          const uint32_t* __restrict__ off, int64_t m, uint32_t* out)
+{
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x)
+        if (pred[j]) out[off[j]] = torder[j];
+}
+
+// coincidence windows (no counterpart in the reference): a single not inside
+// an open window opens [t, t+W). One thread walks each cluster of singles
+// (a single >= W after its predecessor cannot be inside an earlier window).
+__global__ void k_coinc_count(const uint32_t* __restrict__ sidx, int64_t s, const double* __restrict__ t,
+                              const int32_t* __restrict__ pann, double W, int policy, uint32_t* wcount,
+                              uint32_t* wend, unsigned long long* nmult)
+{
+    unsigned long long mult = 0;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < s; j += (int64_t)gridDim.x * blockDim.x) {
+        bool anchor = j == 0 || !(t[sidx[j]] < t[sidx[j - 1]] + W);
+        if (!anchor) continue;
+        int64_t i = j;
+        while (i < s && (i == j || t[sidx[i]] < t[sidx[i - 1]] + W)) {
+            const double ti = t[sidx[i]];
+            int64_t e = i + 1;
+            while (e < s && t[sidx[e]] < ti + W) e++;
+            const int64_t cnt = e - i;
+            uint32_t pairs = 0;
+            if (policy == 0) {
+                if (cnt == 2 && pann[sidx[i]] != pann[sidx[i + 1]]) pairs = 1;
+            } else {
+                for (int64_t a = i; a < e; ++a)
+                    for (int64_t b = a + 1; b < e; ++b) pairs += pann[sidx[a]] != pann[sidx[b]];
+            }
+            if (cnt > 2) mult++;
+            wcount[i] = pairs;
+            wend[i] = (uint32_t)e;
+            i = e;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mult += __shfl_xor_sync(0xffffffffu, mult, o);
+    if ((threadIdx.x & 31) == 0 && mult) atomicAdd(nmult, mult);
+}
+
+__global__ void k_coinc_write(const uint32_t* __restrict__ sidx, int64_t s, const uint32_t* __restrict__ wend,
+                              const uint32_t* __restrict__ off, const int32_t* __restrict__ pann,
+                              const int32_t* __restrict__ eid, const uint8_t* __restrict__ meta, int policy,
+                              int64_t* pairs, uint8_t* klass, int64_t cap, unsigned long long* ncls)
+{
+    unsigned long long c0 = 0, c1 = 0, c2 = 0;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < s; j += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = wend[j];
+        if (e <= j) continue;
+        const int64_t cnt = e - j;
+        if (policy == 0 && cnt != 2) continue;
+        uint32_t o = off[j];
+        for (int64_t a = j; a < e; ++a) {
+            for (int64_t b = a + 1; b < e; ++b) {
+                const uint32_t pa = sidx[a], pb = sidx[b];
+                if (pann[pa] == pann[pb]) continue;
+                uint8_t k;
+                if (eid[pa] == eid[pb]) k = ((meta[pa] | meta[pb]) & 0x80u) ? 1 : 0;
+                else k = 2;
+                if (o < cap) {
+                    pairs[2 * (int64_t)o] = a;
+                    pairs[2 * (int64_t)o + 1] = b;
+                    klass[o] = k;
+                }
+                o++;
+                if (k == 0) c0++; else if (k == 1) c1++; else c2++;
+            }
+        }
+    }
+    if (c0) atomicAdd(&ncls[0], c0);
+    if (c1) atomicAdd(&ncls[1], c1);
+    if (c2) atomicAdd(&ncls[2], c2);
+}
+
+static unsigned grid_for_g(int64_t n)
+{
+    int64_t b = (n + 255) / 256;
+    return (unsigned)(b < 1 ? 1 : (b > 152 * 64 ? 152 * 64 : b));
+}
+
+// gather records (gPET.h:87-92 layout) for the pulses listed in idx (or
+// 0..n-1); blurred fields and the dead-time site when `blurred`
+__global__ void k_gather_events(PulseDev P, const uint32_t* __restrict__ idx, int64_t n, int blurred,
+                                const float* __restrict__ Eb, const float* __restrict__ xb,
+                                const float* __restrict__ yb, const float* __restrict__ zb,
+                                const int32_t* __restrict__ site, EventRec* out, uint8_t* meta)
+{
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = idx ? (int64_t)idx[j] : j;
+        EventRec e;
+        e.parn = P.parn[p]; e.pann = P.pann[p]; e.modn = P.modn[p]; e.cryn = P.cryn[p];
+        e.siten = blurred ? site[p] : P.siten[p];
+        e.eventid = P.eventid[p];
+        e.t = P.t[p];
+        if (blurred) { e.E = Eb[p]; e.x = xb[p]; e.y = yb[p]; e.z = zb[p]; }
+        else { e.E = P.E[p]; e.x = P.x[p]; e.y = P.y[p]; e.z = P.z[p]; }
+        out[j] = e;
+        meta[j] = P.meta[p];
+    }
+}
+
+int gather_events(const PulseDev& P, const uint32_t* idx, int64_t n, bool blurred, const DigiScratch& D,
+                  EventRec* out, uint8_t* meta, cudaStream_t s)
+{
+    if (n <= 0) return 0;
+    k_gather_events<<<grid_for_g(n), 256, 0, s>>>(P, idx, n, blurred ? 1 : 0, D.Eb, D.xb, D.yb, D.zb, D.site, out,
+                                                  meta);
+    return cudaGetLastError() == cudaSuccess ? 0 : GPET_ERR_CUDA;
+}
+
+static unsigned grid_for(int64_t n, int threads)
+{
+    int64_t b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > 152 * 64) b = 152 * 64;
+    return (unsigned)b;
+}
+
+static int ensure(void** p, size_t bytes, size_t* have)
+{
+    if (*have >= bytes && *p) return 0;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    if (cudaMalloc(p, bytes ? bytes : 16) != cudaSuccess) return GPET_ERR_CUDA;
+    *have = bytes;
+    return 0;
+}
+
+int digitize_device(const PulseDev& P, int64_t n, const DigiParams& prm, DigiScratch& D, Counters* cnt,
+                    cudaStream_t s, int64_t* launches, int64_t* n_singles_out, int64_t* n_coinc_out)
+{
+    unsigned long long hc[4] = {0, 0, 0, 0};
+    cudaMemsetAsync(D.dcount, 0, 8 * sizeof(unsigned long long), s);
+    if (n > 0) {
+        k_blur_threshold<<<grid_for(n, 256), 256, 0, s>>>(P, n, prm, D.Eb, D.xb, D.yb, D.zb, D.site, D.sel,
+                                                          D.dcount + 0);
+        ++*launches;
+    }
+    cudaMemcpyAsync(hc, D.dcount, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return GPET_ERR_CUDA;
+    const int64_t m = (int64_t)hc[0];
+    // dcount: [0] selected [1] alive after dead time [2] singles (uint32, scan
+    // total) [3] multiples [4] scratch scan total [5..7] true/scatter/random
+    uint32_t* total = reinterpret_cast<uint32_t*>(D.dcount + 4);
+    // time order
+    uint64_t *ka = D.key_a, *kb = D.key_b;
+    uint32_t *va = D.idx_a, *vb = D.idx_b;
+    if (m > 0) {
+        k_time_keys<<<grid_for(m, 256), 256, 0, s>>>(D.sel, m, P.t, ka, va);
+        ++*launches;
+        radix_sort(ka, va, kb, vb, m, 64, D.hist, D.scan_aux, total, s, launches);
+        k_tie_fix<<<grid_for(m, 256), 256, 0, s>>>(ka, va, m, P.parn, P.meta);
+        ++*launches;
+        cudaMemcpyAsync(D.torder, va, sizeof(uint32_t) * m, cudaMemcpyDeviceToDevice, s);
+        // site order
+        int site_bits = 8;
+        {
+            int64_t maxsite = (int64_t)prm.moduleN * prm.crystalN * kMaxPanels;
+            while (site_bits < 32 && (1ll << site_bits) <= maxsite) site_bits += 8;
+        }
+        k_site_keys<<<grid_for(m, 256), 256, 0, s>>>(D.torder, m, D.site, ka, va);
+        ++*launches;
+        radix_sort(ka, va, kb, vb, m, site_bits, D.hist, D.scan_aux, total, s, launches);
+        // dead time on the site order
+        k_deadtime<<<grid_for(m, 256), 256, 0, s>>>(va, m, D.site, P.t, prm.tau, prm.dtype, D.flags, D.dcount + 1);
+        // energy window over the time order, ordered compaction
+        k_window_pred<<<grid_for(m, 256), 256, 0, s>>>(D.torder, m, D.flags, D.Eb, prm.ewin_lo, prm.ewin_hi, D.sel);
+        *launches += 2;
+        scan_exclusive(D.sel, D.wcount, m, D.scan_aux, reinterpret_cast<uint32_t*>(D.dcount + 2), s, launches);
+        k_compact<<<grid_for(m, 256), 256, 0, s>>>(D.torder, D.sel, D.wcount, m, D.single_idx);
+        ++*launches;
+    }
+    cudaMemcpyAsync(hc, D.dcount, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return GPET_ERR_CUDA;
+    const int64_t ndead = m > 0 ? (int64_t)hc[1] : 0;
+    const int64_t ns = m > 0 ? (int64_t)(uint32_t)(hc[2] & 0xffffffffull) : 0;
+    // coincidences
+    int64_t nc = 0;
+    unsigned long long* ncls = D.dcount + 5;
+    if (ns > 0) {
+        cudaMemsetAsync(D.wcount, 0, sizeof(uint32_t) * ns, s);
+        cudaMemsetAsync(D.wend, 0, sizeof(uint32_t) * ns, s);
+        k_coinc_count<<<grid_for(ns, 256), 256, 0, s>>>(D.single_idx, ns, P.t, P.pann, prm.window, prm.coinc_policy,
+                                                        D.wcount, D.wend, D.dcount + 3);
+        ++*launches;
+        scan_exclusive(D.wcount, D.sel, ns, D.scan_aux, total, s, launches);
+        uint32_t hn = 0;
+        cudaMemcpyAsync(&hn, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return GPET_ERR_CUDA;
+        nc = hn;
+        if (nc > D.coinc_cap) {
+            cudaFree(D.coinc_pairs);
+            cudaFree(D.coinc_class);
+            D.coinc_pairs = nullptr; D.coinc_class = nullptr;
+            int64_t cap = nc + nc / 4 + 1024;
+            if (cudaMalloc(&D.coinc_pairs, sizeof(int64_t) * 2 * cap) != cudaSuccess ||
+                cudaMalloc(&D.coinc_class, cap) != cudaSuccess) {
+                D.coinc_cap = 0;
+                return GPET_ERR_CUDA;
+            }
+            D.coinc_cap = cap;
+        }
+        cudaMemsetAsync(ncls, 0, 3 * sizeof(unsigned long long), s);
+        k_coinc_write<<<grid_for(ns, 256), 256, 0, s>>>(D.single_idx, ns, D.wend, D.sel, P.pann, P.eventid, P.meta,
+                                                        prm.coinc_policy, D.coinc_pairs, D.coinc_class,
+                                                        D.coinc_cap, ncls);
+        ++*launches;
+    }
+    unsigned long long h8[8] = {0};
+    cudaMemcpyAsync(h8, D.dcount, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return GPET_ERR_CUDA;
+    if (cudaGetLastError() != cudaSuccess) return GPET_ERR_CUDA;
+    cnt->n_thr = (unsigned long long)m;
+    cnt->n_dead = (unsigned long long)ndead;
+    cnt->n_single = (unsigned long long)ns;
+    cnt->n_coinc = (unsigned long long)nc;
+    cnt->n_mult = ns > 0 ? h8[3] : 0;
+    cnt->n_true = ns > 0 ? h8[5] : 0;
+    cnt->n_scat = ns > 0 ? h8[6] : 0;
+    cnt->n_rand = ns > 0 ? h8[7] : 0;
+    *n_singles_out = ns;
+    *n_coinc_out = nc;
+    return 0;
+}
+
+}  // namespace gpet

@@ -1,0 +1,978 @@
+// gpet_api.cu - host runtime behind the C ABI of include/gpet.h: context,
+// options, scene upload, run orchestration (the role of main.cu, init and
+// sampleParticle/simulateParticle in gPET.cu), output copy-out and writers.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "loaders.hpp"
+#include "../../include/gpet.h"
+
+using namespace gpet;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() { if (p) cudaFree(p); }
+    cudaError_t ensure(size_t n)
+    {
+        if (n <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, n ? n : 16);
+        if (e == cudaSuccess) bytes = n;
+        return e;
+    }
+    template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+}  // namespace
+
+struct gpet_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    // options
+    uint64_t seed = 20261203ull;
+    uint32_t sim_id = 0;
+    int64_t n_decays_opt = -1;
+    double coinc_window_ns = 4.0;
+    int coinc_policy = 0;
+    int record_hits = 1;
+    int record_exits = 0;
+    int64_t chunk_decays = 1ll << 24;
+    std::string base_dir = ".";
+    std::string data_dir;
+    // host scene
+    Config cfg;
+    bool have_cfg = false, have_tables = false, have_phantom = false, have_geo = false, have_source = false;
+    Tables tab;
+    Geometry geo;
+    Sources src;
+    float tstart = 0.0f, tend = 1.0f;
+    std::vector<double> psf;
+    int psf_ptype = 0;
+    bool use_psf = false;
+    int pdim[3] = {0, 0, 0};
+    float poff[3] = {0, 0, 0}, psz[3] = {0, 0, 0};
+    float maxden_ph[10] = {0};
+    std::vector<float> wck_ph, wck_det;
+    float wck_e0 = 0, wck_ide = 0;
+    std::vector<int64_t> src_first, src_count;
+    // device scene
+    SimDesc sim{};
+    DevBuf d_sim, d_xs4, d_cmpsf, d_rayff, d_wck_ph, d_wck_det, d_vox, d_panels, d_psf;
+    // device work buffers
+    DevBuf q_f, q_t, q_i, cnt, qcount;
+    int64_t q_cap = 0;
+    DevBuf p_int, p_t, p_f, p_meta;       // pulses: 6 int32, 1 double, 4 float, 1 byte
+    int64_t p_cap = 0;
+    DevBuf h_id, h_f;
+    int64_t h_cap = 0;
+    DevBuf exits;
+    DevBuf g_ev, g_meta;                  // gathered Event records for copy-out
+    DigiScratch dg{};
+    DevBuf dg_idx_a, dg_idx_b, dg_key_a, dg_key_b, dg_torder, dg_flags, dg_site, dg_hist, dg_aux, dg_sel, dg_blur,
+        dg_single, dg_wcount, dg_wend, dg_dcount;
+    // results
+    int64_t n_pulses = 0, n_hits = 0, n_singles = 0, n_coinc = 0;
+    std::vector<ExitRec> host_exits;
+    gpet_run_stats last{};
+    bool have_results = false;
+    cudaEvent_t ev[8] = {};
+};
+
+static int fail(gpet_ctx* c, int code, const std::string& msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+static int cuda_fail(gpet_ctx* c, cudaError_t e, const char* what)
+{
+    return fail(c, GPET_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                            \
+    do {                                                    \
+        cudaError_t e__ = (call);                           \
+        if (e__ != cudaSuccess) return cuda_fail(c, e__, #call); \
+    } while (0)
+
+static std::string resolve(const gpet_ctx* c, const std::string& p)
+{
+    if (p.empty() || p[0] == '/') return p;
+    return c->base_dir + "/" + p;
+}
+
+extern "C" {
+
+int gpet_create(int device, gpet_ctx** out)
+{
+    if (!out) return GPET_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return GPET_ERR_NOGPU;
+    if (device < 0 || device >= n) return GPET_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return GPET_ERR_CUDA;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, k_source_phantom) != cudaSuccess) return GPET_ERR_NOGPU;
+    auto* c = new gpet_ctx();
+    c->device = device;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return GPET_ERR_CUDA;
+    }
+    for (auto& e : c->ev) cudaEventCreate(&e);
+    *out = c;
+    return GPET_OK;
+}
+
+void gpet_destroy(gpet_ctx* c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+    cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* gpet_last_error(gpet_ctx* c)
+{
+    return c ? c->err.c_str() : "null context";
+}
+
+int gpet_set_option(gpet_ctx* c, const char* key, const char* value)
+{
+    if (!c || !key || !value) return GPET_ERR_ARG;
+    std::string k(key), v(value);
+    char* end = nullptr;
+    if (k == "seed") c->seed = std::strtoull(value, &end, 10);
+    else if (k == "sim_id") c->sim_id = (uint32_t)std::strtoul(value, &end, 10);
+    else if (k == "n_decays") c->n_decays_opt = std::strtoll(value, &end, 10);
+    else if (k == "coinc_window_ns") c->coinc_window_ns = std::strtod(value, &end);
+    else if (k == "coinc_policy") c->coinc_policy = (int)std::strtol(value, &end, 10);
+    else if (k == "record_hits") c->record_hits = (int)std::strtol(value, &end, 10);
+    else if (k == "record_exits") c->record_exits = (int)std::strtol(value, &end, 10);
+    else if (k == "chunk_decays") c->chunk_decays = std::strtoll(value, &end, 10);
+    else if (k == "base_dir") { c->base_dir = v; return GPET_OK; }
+    else if (k == "data_dir") { c->data_dir = v; return GPET_OK; }
+    else return fail(c, GPET_ERR_ARG, "unknown option " + k);
+    if (end == value || (end && *end)) return fail(c, GPET_ERR_ARG, "bad value for " + k + ": " + v);
+    if (c->coinc_policy < 0 || c->coinc_policy > 1) return fail(c, GPET_ERR_ARG, "coinc_policy must be 0 or 1");
+    if (c->chunk_decays < 1024) return fail(c, GPET_ERR_ARG, "chunk_decays must be >= 1024");
+    return GPET_OK;
+}
+
+// ---------------------------------------------------------------- tables
+static double lerp_d(const Tables& t, const float* tab, double e, float idle)
+{
+    double x = (double)idle * (e - (double)t.energy[0]);
+    if (!(x > 0.0)) return tab[0];
+    if (x >= t.ne - 1) return tab[t.ne - 1];
+    int i = (int)x;
+    double f = x - i;
+    return tab[i] + f * ((double)tab[i + 1] - (double)tab[i]);
+}
+
+// Woodcock majorant (replaces iniwck, initialize.cu:773-829, 919-966): node i
+// holds 1/max_m rho_max(m) max(mu_m over [e_{i-1}, e_{i+1}]) of the linearly
+// interpolated tables, so the interpolated majorant bounds every material.
+static void build_wck(const Tables& t, float idle, const float* maxden, std::vector<float>& w, float& e0, float& ide)
+{
+    float de = (t.emax - t.eminph) / (float)kNwck;
+    e0 = t.eminph;
+    ide = 1.0f / de;
+    w.assign(kNwck, 0.0f);
+    for (int i = 0; i < kNwck; ++i) {
+        double lo = (double)t.eminph + (double)de * (double)(i > 0 ? i - 1 : 0);
+        double hi = (double)t.eminph + (double)de * (double)(i + 1);
+        double best = 0.0;
+        for (int m = 0; m < t.nmat; ++m) {
+            if (!(maxden[m] > 0.0f)) continue;
+            const float* tb = &t.lamph[(size_t)m * t.ne];
+            double mx = lerp_d(t, tb, lo, idle);
+            double v = lerp_d(t, tb, hi, idle);
+            if (v > mx) mx = v;
+            double xlo = (double)idle * (lo - (double)t.energy[0]);
+            double xhi = (double)idle * (hi - (double)t.energy[0]);
+            int k0 = (int)std::ceil(xlo), k1 = (int)std::floor(xhi);
+            if (k0 < 0) k0 = 0;
+            if (k1 > t.ne - 1) k1 = t.ne - 1;
+            for (int k = k0; k <= k1; ++k)
+                if (tb[k] > mx) mx = tb[k];
+            mx *= (double)maxden[m];
+            if (mx > best) best = mx;
+        }
+        w[i] = (float)(1.0 / best);
+    }
+}
+
+static float table_idle(const Tables& t) { return (float)(t.ne - 1) / (t.energy[t.ne - 1] - t.energy[0]); }
+
+int gpet_load_tables(gpet_ctx* c, const char* data_dir)
+{
+    if (!c || !data_dir) return GPET_ERR_ARG;
+    cudaSetDevice(c->device);
+    Tables t;
+    std::string e = read_tables(data_dir, t);
+    if (!e.empty()) return fail(c, GPET_ERR_IO, e);
+    c->tab = std::move(t);
+    const Tables& T = c->tab;
+    std::vector<float4> xs((size_t)T.nmat * T.ne);
+    for (int m = 0; m < T.nmat; ++m)
+        for (int i = 0; i < T.ne; ++i) {
+            size_t k = (size_t)m * T.ne + i;
+            xs[k] = make_float4(T.lamph[k], T.compt[k], T.rayle[k], T.phote[k]);
+        }
+    CK(c->d_xs4.ensure(xs.size() * sizeof(float4)));
+    CK(cudaMemcpy(c->d_xs4.p, xs.data(), xs.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(c->d_cmpsf.ensure(T.cmpsf.size() * 4));
+    CK(cudaMemcpy(c->d_cmpsf.p, T.cmpsf.data(), T.cmpsf.size() * 4, cudaMemcpyHostToDevice));
+    CK(c->d_rayff.ensure(T.rayff.size() * 4));
+    CK(cudaMemcpy(c->d_rayff.p, T.rayff.data(), T.rayff.size() * 4, cudaMemcpyHostToDevice));
+    c->have_tables = true;
+    return GPET_OK;
+}
+
+int gpet_set_phantom(gpet_ctx* c, const int32_t* mat, const float* den, const int32_t dims[3], const float offset[3],
+                     const float size[3])
+{
+    if (!c || !mat || !den || !dims || !offset || !size) return GPET_ERR_ARG;
+    if (!c->have_tables) return fail(c, GPET_ERR_ARG, "load the tables before the phantom");
+    if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1) return fail(c, GPET_ERR_ARG, "phantom dimensions must be >= 1");
+    cudaSetDevice(c->device);
+    const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
+    float maxden[10] = {0};
+    std::vector<uint2> vox((size_t)n);
+    for (int64_t v = 0; v < n; ++v) {
+        int m = mat[v];
+        if (m < 0 || m >= c->tab.nmat) return fail(c, GPET_ERR_ARG, "phantom material index out of range");
+        if (den[v] > maxden[m]) maxden[m] = den[v];
+        uint32_t bits;
+        std::memcpy(&bits, &den[v], 4);
+        vox[(size_t)v] = make_uint2(bits, (uint32_t)m);
+    }
+    CK(c->d_vox.ensure((size_t)n * sizeof(uint2)));
+    CK(cudaMemcpyAsync(c->d_vox.p, vox.data(), (size_t)n * sizeof(uint2), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < 3; ++k) { c->pdim[k] = dims[k]; c->poff[k] = offset[k]; c->psz[k] = size[k]; }
+    std::memcpy(c->maxden_ph, maxden, sizeof(maxden));
+    build_wck(c->tab, table_idle(c->tab), maxden, c->wck_ph, c->wck_e0, c->wck_ide);
+    CK(c->d_wck_ph.ensure(kNwck * 4));
+    CK(cudaMemcpy(c->d_wck_ph.p, c->wck_ph.data(), kNwck * 4, cudaMemcpyHostToDevice));
+    c->have_phantom = true;
+    return GPET_OK;
+}
+
+int gpet_load_geometry(gpet_ctx* c, const char* path)
+{
+    if (!c || !path) return GPET_ERR_ARG;
+    if (!c->have_tables) return fail(c, GPET_ERR_ARG, "load the tables before the geometry");
+    cudaSetDevice(c->device);
+    Geometry g;
+    std::string e = read_geometry(path, g);
+    if (!e.empty()) return fail(c, GPET_ERR_IO, e);
+    for (int k = 0; k < 2; ++k)
+        if (g.det_mat[k] < 0 || g.det_mat[k] >= c->tab.nmat) return fail(c, GPET_ERR_ARG, "detector material out of range");
+    c->geo = std::move(g);
+    float dmax[10] = {0};
+    for (int k = 0; k < 2; ++k)
+        if (c->geo.det_den[k] > dmax[c->geo.det_mat[k]]) dmax[c->geo.det_mat[k]] = c->geo.det_den[k];
+    float e0, ide;
+    build_wck(c->tab, table_idle(c->tab), dmax, c->wck_det, e0, ide);
+    CK(c->d_wck_det.ensure(kNwck * 4));
+    CK(cudaMemcpy(c->d_wck_det.p, c->wck_det.data(), kNwck * 4, cudaMemcpyHostToDevice));
+    CK(c->d_panels.ensure(c->geo.panels.size() * 4));
+    CK(cudaMemcpy(c->d_panels.p, c->geo.panels.data(), c->geo.panels.size() * 4, cudaMemcpyHostToDevice));
+    c->have_geo = true;
+    return GPET_OK;
+}
+
+int gpet_set_source_file(gpet_ctx* c, const char* path, float tstart, float tend)
+{
+    if (!c || !path) return GPET_ERR_ARG;
+    Sources s;
+    std::string e = read_sources(path, s);
+    if (!e.empty()) return fail(c, GPET_ERR_IO, e);
+    if ((int)s.natom.size() > kMaxSrc) return fail(c, GPET_ERR_ARG, "at most 64 sources");
+    for (auto t : s.type)
+        if (t < 0 || t >= (int)c->tab.iso_halftime.size()) return fail(c, GPET_ERR_ARG, "isotope type out of range");
+    c->src = std::move(s);
+    c->tstart = tstart;
+    c->tend = tend;
+    c->use_psf = false;
+    c->have_source = true;
+    return GPET_OK;
+}
+
+int gpet_set_source_psf(gpet_ctx* c, const double* rec8, int64_t n, int ptype)
+{
+    if (!c || (!rec8 && n > 0) || n < 0 || (ptype != 0 && ptype != 1)) return GPET_ERR_ARG;
+    c->psf.assign(rec8, rec8 + 8 * n);
+    c->psf_ptype = ptype;
+    c->use_psf = true;
+    c->have_source = true;
+    return GPET_OK;
+}
+
+int gpet_load_config(gpet_ctx* c, const char* path)
+{
+    if (!c || !path) return GPET_ERR_ARG;
+    Config cfg;
+    std::string e = read_config(path, cfg);
+    if (!e.empty()) return fail(c, GPET_ERR_IO, e);
+    c->cfg = cfg;
+    c->have_cfg = true;
+    std::string dd = c->data_dir.empty() ? c->base_dir + "/data" : c->data_dir;
+    int rc = gpet_load_tables(c, dd.c_str());
+    if (rc) return rc;
+    const int64_t n = (int64_t)cfg.pdim[0] * cfg.pdim[1] * cfg.pdim[2];
+    if (n <= 0) return fail(c, GPET_ERR_IO, "phantom dimension must be positive");
+    std::vector<int32_t> mat;
+    std::vector<float> den;
+    e = read_phantom(resolve(c, cfg.matfile), resolve(c, cfg.denfile), n, mat, den);
+    if (!e.empty()) return fail(c, GPET_ERR_IO, e);
+    rc = gpet_set_phantom(c, mat.data(), den.data(), cfg.pdim, cfg.poffset, cfg.psize);
+    if (rc) return rc;
+    rc = gpet_load_geometry(c, resolve(c, cfg.geofile).c_str());
+    if (rc) return rc;
+    if (cfg.usepsf) {
+        std::vector<double> rec;
+        e = read_psf(resolve(c, cfg.sourcefile), cfg.nparticle, rec);
+        if (!e.empty()) return fail(c, GPET_ERR_IO, e);
+        return gpet_set_source_psf(c, rec.data(), (int64_t)rec.size() / 8, cfg.ptype);
+    }
+    return gpet_set_source_file(c, resolve(c, cfg.sourcefile).c_str(), cfg.tstart, cfg.tend);
+}
+
+// ---------------------------------------------------------------- run
+// decays per source (gPET.cu:204-208, 264-272: floor(N_t (1 - 2^(-dt/T)))
+// with N_t = floor(natom 2^(-tstart/T))); an exact total is split over the
+// sources in proportion (largest remainder).
+static std::string source_layout(gpet_ctx* c)
+{
+    const Sources& s = c->src;
+    const double dt = (double)(c->tend - c->tstart);
+    std::vector<int64_t> ex(s.natom.size());
+    double tot = 0;
+    for (size_t i = 0; i < s.natom.size(); ++i) {
+        double th = (double)c->tab.iso_halftime[s.type[i]];
+        double nt = std::floor((double)s.natom[i] * std::pow(2.0, -(double)c->tstart / th));
+        ex[i] = (int64_t)std::floor(nt * (1.0 - std::pow(2.0, -dt / th)));
+        tot += (double)ex[i];
+    }
+    std::vector<int64_t> cnt = ex;
+    if (c->n_decays_opt >= 0) {
+        if (!(tot > 0)) return "no source decays in the acquisition window";
+        std::vector<double> quota(ex.size());
+        int64_t sum = 0;
+        for (size_t i = 0; i < ex.size(); ++i) {
+            quota[i] = (double)c->n_decays_opt * (double)ex[i] / tot;
+            cnt[i] = (int64_t)std::floor(quota[i]);
+            sum += cnt[i];
+        }
+        std::vector<size_t> order(ex.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+            return (quota[a] - (double)cnt[a]) > (quota[b] - (double)cnt[b]);
+        });
+        for (int64_t r = 0; r < c->n_decays_opt - sum; ++r) cnt[order[(size_t)r]]++;
+    }
+    c->src_first.assign(cnt.size(), 0);
+    c->src_count = cnt;
+    for (size_t i = 1; i < cnt.size(); ++i) c->src_first[i] = c->src_first[i - 1] + cnt[i - 1];
+    return "";
+}
+
+static int build_sim(gpet_ctx* c)
+{
+    SimDesc& S = c->sim;
+    std::memset(&S, 0, sizeof(S));
+    S.key0 = (uint32_t)c->seed;
+    S.key1 = (uint32_t)(c->seed >> 32) + c->sim_id;
+    const Tables& T = c->tab;
+    S.nmat = T.nmat; S.ne = T.ne; S.e0 = T.energy[0]; S.idle = table_idle(T);
+    S.xs4 = c->d_xs4.as<float4>();
+    S.ncp_c = T.ncp_c; S.ne_c = T.ne_c; S.idcp_c = 1.0f / T.dcp_c; S.ide_c = 1.0f / T.de_c;
+    S.cmpsf = c->d_cmpsf.as<float>();
+    S.ncp_r = T.ncp_r; S.ne_r = T.ne_r; S.idcp_r = 1.0f / T.dcp_r; S.ide_r = 1.0f / T.de_r;
+    S.rayff = c->d_rayff.as<float>();
+    S.wck_e0 = c->wck_e0; S.wck_ide = c->wck_ide;
+    S.wck_ph = c->d_wck_ph.as<float>(); S.wck_det = c->d_wck_det.as<float>();
+    S.nx = c->pdim[0]; S.ny = c->pdim[1]; S.nz = c->pdim[2];
+    S.dx = c->psz[0] / (float)c->pdim[0]; S.dy = c->psz[1] / (float)c->pdim[1]; S.dz = c->psz[2] / (float)c->pdim[2];
+    S.idx = 1.0f / S.dx; S.idy = 1.0f / S.dy; S.idz = 1.0f / S.dz;
+    S.offx = c->poff[0]; S.offy = c->poff[1]; S.offz = c->poff[2];
+    S.vox = c->d_vox.as<uint2>();
+    S.npanels = c->geo.npanels;
+    S.panels = c->d_panels.as<float>();
+    for (int k = 0; k < 2; ++k) { S.det_mat[k] = c->geo.det_mat[k]; S.det_den[k] = c->geo.det_den[k]; }
+    S.moduleN = c->geo.moduleN; S.crystalN = c->geo.crystalN; S.moduleNy = c->geo.moduleNy; S.crystalNy = c->geo.crystalNy;
+    const Config& cf = c->cfg;
+    S.nsurface = c->have_cfg ? (int)cf.surfaces.size() / 10 : 0;
+    for (int k = 0; k < 10 * S.nsurface; ++k) S.surface[k] = cf.surfaces[k];
+    S.noncol_sigma = c->have_cfg ? cf.noncol_sigma : 0.0037056f;
+    S.eabsph = c->have_cfg ? cf.eabsph : 1000.0f;
+    S.useprange = c->have_cfg ? cf.useprange : 0;
+    S.rdepth = c->have_cfg ? cf.rdepth : 2;
+    S.rpolicy = c->have_cfg ? cf.rpolicy : 1;
+    if (c->use_psf) {
+        S.npsf = (int64_t)c->psf.size() / 8;
+        S.psf_ptype = c->psf_ptype;
+        if (cudaSuccess != c->d_psf.ensure(c->psf.size() * 8)) return fail(c, GPET_ERR_CUDA, "psf upload");
+        cudaMemcpy(c->d_psf.p, c->psf.data(), c->psf.size() * 8, cudaMemcpyHostToDevice);
+        S.psf = c->d_psf.as<double>();
+        S.nsrc = 0;
+    } else {
+        std::string e = source_layout(c);
+        if (!e.empty()) return fail(c, GPET_ERR_ARG, e);
+        S.nsrc = (int)c->src.natom.size();
+        const double dt = (double)(c->tend - c->tstart);
+        for (int i = 0; i < S.nsrc; ++i) {
+            int ty = c->src.type[i];
+            S.src_end[i] = c->src_first[i] + c->src_count[i];
+            S.src_type[i] = ty;
+            S.src_shape[i] = c->src.shape[i];
+            for (int k = 0; k < 6; ++k) S.src_coef[i][k] = c->src.coef[6 * i + k];
+            double th = (double)c->tab.iso_halftime[ty];
+            double tau = th / 0.69314718055994530942;
+            S.src_tau[i] = tau;
+            S.src_cfac[i] = -std::expm1(-dt / tau);
+            S.iso_ratio[i] = c->tab.iso_ratio[ty];
+            for (int k = 0; k < 8; ++k) S.iso_coef[i][k] = c->tab.iso_coef[8 * ty + k];
+        }
+        S.tstart_s = (double)c->tstart;
+    }
+    if (cudaSuccess != c->d_sim.ensure(sizeof(SimDesc))) return fail(c, GPET_ERR_CUDA, "sim upload");
+    cudaMemcpyAsync(c->d_sim.p, &S, sizeof(SimDesc), cudaMemcpyHostToDevice, c->stream);
+    return GPET_OK;
+}
+
+static int64_t total_decays(const gpet_ctx* c)
+{
+    if (c->use_psf) return (int64_t)c->psf.size() / 8;
+    int64_t t = 0;
+    for (auto v : c->src_count) t += v;
+    return t;
+}
+
+// grow a structure-of-arrays pulse buffer, keeping the first `used` entries
+static int grow_pulses(gpet_ctx* c, int64_t need, int64_t used)
+{
+    if (need <= c->p_cap) return GPET_OK;
+    int64_t cap = std::max<int64_t>(need + need / 2, 1 << 20);
+    DevBuf ni, nt, nf, nm;
+    CK(ni.ensure((size_t)cap * 6 * 4));
+    CK(nt.ensure((size_t)cap * 8));
+    CK(nf.ensure((size_t)cap * 4 * 4));
+    CK(nm.ensure((size_t)cap));
+    if (used > 0) {
+        for (int a = 0; a < 6; ++a)
+            CK(cudaMemcpyAsync(ni.as<int32_t>() + a * cap, c->p_int.as<int32_t>() + a * c->p_cap, used * 4,
+                               cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(nt.p, c->p_t.p, used * 8, cudaMemcpyDeviceToDevice, c->stream));
+        for (int a = 0; a < 4; ++a)
+            CK(cudaMemcpyAsync(nf.as<float>() + a * cap, c->p_f.as<float>() + a * c->p_cap, used * 4,
+                               cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(nm.p, c->p_meta.p, used, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    std::swap(c->p_int.p, ni.p); std::swap(c->p_int.bytes, ni.bytes);
+    std::swap(c->p_t.p, nt.p); std::swap(c->p_t.bytes, nt.bytes);
+    std::swap(c->p_f.p, nf.p); std::swap(c->p_f.bytes, nf.bytes);
+    std::swap(c->p_meta.p, nm.p); std::swap(c->p_meta.bytes, nm.bytes);
+    c->p_cap = cap;
+    return GPET_OK;
+}
+
+static int grow_hits(gpet_ctx* c, int64_t need, int64_t used)
+{
+    if (need <= c->h_cap) return GPET_OK;
+    int64_t cap = std::max<int64_t>(need + need / 2, 1 << 20);
+    DevBuf ni, nf;
+    CK(ni.ensure((size_t)cap * 20));
+    CK(nf.ensure((size_t)cap * 20));
+    if (used > 0) {
+        CK(cudaMemcpyAsync(ni.p, c->h_id.p, used * 20, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(nf.p, c->h_f.p, used * 20, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    std::swap(c->h_id.p, ni.p); std::swap(c->h_id.bytes, ni.bytes);
+    std::swap(c->h_f.p, nf.p); std::swap(c->h_f.bytes, nf.bytes);
+    c->h_cap = cap;
+    return GPET_OK;
+}
+
+static PulseDev pulse_view(gpet_ctx* c)
+{
+    PulseDev P;
+    int32_t* I = c->p_int.as<int32_t>();
+    float* F = c->p_f.as<float>();
+    int64_t cap = c->p_cap;
+    P.parn = I; P.pann = I + cap; P.modn = I + 2 * cap; P.cryn = I + 3 * cap; P.siten = I + 4 * cap;
+    P.eventid = I + 5 * cap;
+    P.t = c->p_t.as<double>();
+    P.E = F; P.x = F + cap; P.y = F + 2 * cap; P.z = F + 3 * cap;
+    P.meta = c->p_meta.as<uint8_t>();
+    P.count = c->cnt.as<unsigned long long>() + 32;
+    P.cap = cap;
+    return P;
+}
+
+static int ensure_digi(gpet_ctx* c, int64_t n)
+{
+    int64_t cap = std::max<int64_t>(n, 1024);
+    if (cap > c->dg.cap) {
+        cap = cap + cap / 4;
+        CK(c->dg_idx_a.ensure(cap * 4)); CK(c->dg_idx_b.ensure(cap * 4));
+        CK(c->dg_key_a.ensure(cap * 8)); CK(c->dg_key_b.ensure(cap * 8));
+        CK(c->dg_torder.ensure(cap * 4)); CK(c->dg_flags.ensure(cap * 4)); CK(c->dg_site.ensure(cap * 4));
+        CK(c->dg_sel.ensure(cap * 4)); CK(c->dg_blur.ensure(cap * 16)); CK(c->dg_single.ensure(cap * 4));
+        CK(c->dg_wcount.ensure(cap * 4)); CK(c->dg_wend.ensure(cap * 4));
+        int64_t nb = (cap + 4095) / 4096;
+        CK(c->dg_hist.ensure((size_t)256 * nb * 4));
+        int64_t na = (256 * nb + 4095) / 4096 + (cap + 4095) / 4096 + 16;
+        CK(c->dg_aux.ensure((size_t)na * 4));
+        CK(c->dg_dcount.ensure(16 * 8));
+        DigiScratch& D = c->dg;
+        D.idx_a = c->dg_idx_a.as<uint32_t>(); D.idx_b = c->dg_idx_b.as<uint32_t>();
+        D.key_a = c->dg_key_a.as<uint64_t>(); D.key_b = c->dg_key_b.as<uint64_t>();
+        D.torder = c->dg_torder.as<uint32_t>(); D.flags = c->dg_flags.as<uint32_t>(); D.site = c->dg_site.as<int32_t>();
+        D.hist = c->dg_hist.as<uint32_t>(); D.scan_aux = c->dg_aux.as<uint32_t>(); D.sel = c->dg_sel.as<uint32_t>();
+        float* B = c->dg_blur.as<float>();
+        D.Eb = B; D.xb = B + cap; D.yb = B + 2 * cap; D.zb = B + 3 * cap;
+        D.single_idx = c->dg_single.as<uint32_t>();
+        D.wcount = c->dg_wcount.as<uint32_t>(); D.wend = c->dg_wend.as<uint32_t>();
+        D.dcount = c->dg_dcount.as<unsigned long long>();
+        D.cap = cap;
+        D.hist_cap = 256 * nb;
+    }
+    return GPET_OK;
+}
+
+static DigiParams digi_params(const gpet_ctx* c)
+{
+    DigiParams p{};
+    p.key0 = (uint32_t)c->seed;
+    p.key1 = (uint32_t)(c->seed >> 32) + c->sim_id;
+    const Config& f = c->cfg;
+    p.blurpolicy = f.blurpolicy; p.Eref = f.eref; p.Rref = f.rref; p.Eslope = f.eslope; p.Sblur = f.sblur;
+    p.Eth = f.eth; p.dlevel = f.dlevel; p.dtype = f.dtype; p.tau = (double)f.dtime;
+    p.ewin_lo = f.ewin_lo; p.ewin_hi = f.ewin_hi;
+    p.window = c->coinc_window_ns * 1e-3;
+    p.coinc_policy = c->coinc_policy;
+    p.moduleN = c->geo.moduleN; p.crystalN = c->geo.crystalN;
+    return p;
+}
+
+static void fill_stats(gpet_ctx* c, const Counters& h, gpet_run_stats* st)
+{
+    st->n_pairs = (int64_t)h.pairs;
+    st->n_entered = (int64_t)h.entered;
+    st->n_pulses = c->n_pulses;
+    st->n_hits = c->n_hits;
+    st->n_threshold = (int64_t)h.n_thr;
+    st->n_deadtime = (int64_t)h.n_dead;
+    st->n_singles = (int64_t)h.n_single;
+    st->n_coinc = (int64_t)h.n_coinc;
+    st->n_true = (int64_t)h.n_true;
+    st->n_scatter = (int64_t)h.n_scat;
+    st->n_random = (int64_t)h.n_rand;
+    st->n_multiple = (int64_t)h.n_mult;
+    st->n_overflow = (int64_t)h.overflow;
+    st->n_stepcap = (int64_t)h.stepcap;
+    st->phantom_steps = (int64_t)h.ph_steps;
+    st->detector_steps = (int64_t)h.det_steps;
+}
+
+static int digitize_and_finish(gpet_ctx* c, int64_t np, gpet_run_stats* st, Counters& h, float* ms_digi)
+{
+    int rc = ensure_digi(c, np);
+    if (rc) return rc;
+    PulseDev P = pulse_view(c);
+    DigiParams prm = digi_params(c);
+    Counters* dcnt = c->cnt.as<Counters>();
+    cudaEventRecord(c->ev[4], c->stream);
+    int64_t ns = 0, nc = 0;
+    rc = digitize_device(P, np, prm, c->dg, &h, c->stream, &st->kernel_launches, &ns, &nc);
+    if (rc) return fail(c, rc, std::string("digitizer failed: ") + cudaGetErrorString(cudaGetLastError()));
+    cudaEventRecord(c->ev[5], c->stream);
+    CK(cudaEventSynchronize(c->ev[5]));
+    cudaEventElapsedTime(ms_digi, c->ev[4], c->ev[5]);
+    (void)dcnt;
+    c->n_singles = ns;
+    c->n_coinc = nc;
+    c->have_results = true;
+    return GPET_OK;
+}
+
+int gpet_run(gpet_ctx* c, gpet_run_stats* st)
+{
+    if (!c) return GPET_ERR_ARG;
+    if (!c->have_tables || !c->have_phantom || !c->have_geo || !c->have_source)
+        return fail(c, GPET_ERR_ARG, "tables, phantom, geometry and source must be set before gpet_run");
+    CK(cudaSetDevice(c->device));
+    gpet_run_stats local{};
+    if (!st) st = &local;
+    std::memset(st, 0, sizeof(*st));
+    int rc = build_sim(c);
+    if (rc) return rc;
+    const int64_t nd = total_decays(c);
+    st->n_decays = nd;
+    const int64_t chunk = std::min<int64_t>(std::max<int64_t>(nd, 1), c->chunk_decays);
+    // queue sized so no photon of a chunk can be dropped
+    if (2 * chunk > c->q_cap) {
+        int64_t cap = 2 * chunk;
+        CK(c->q_f.ensure((size_t)cap * 7 * 4));
+        CK(c->q_t.ensure((size_t)cap * 8));
+        CK(c->q_i.ensure((size_t)cap * 4 * 4));
+        c->q_cap = cap;
+    }
+    CK(c->cnt.ensure(64 * 8));
+    CK(cudaMemsetAsync(c->cnt.p, 0, 64 * 8, c->stream));
+    rc = grow_pulses(c, 1 << 20, 0);
+    if (rc) return rc;
+    if (c->record_hits) { rc = grow_hits(c, 1 << 20, 0); if (rc) return rc; }
+    if (c->record_exits) {
+        CK(c->exits.ensure((size_t)2 * chunk * sizeof(ExitRec)));
+        c->host_exits.assign((size_t)2 * nd, ExitRec{});
+    }
+    Counters* dcnt = c->cnt.as<Counters>();
+    unsigned long long* qcount = c->cnt.as<unsigned long long>() + 31;
+    unsigned long long* pcount = c->cnt.as<unsigned long long>() + 32;
+    unsigned long long* hcount = c->cnt.as<unsigned long long>() + 33;
+    int nsm = 0;
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
+    const size_t smem = (size_t)c->geo.npanels * kPanelStride * 4;
+    float ms_sp = 0, ms_det = 0;
+    cudaEventRecord(c->ev[0], c->stream);
+    int64_t pulses_used = 0, hits_used = 0;
+    for (int64_t d0 = 0; d0 < nd; d0 += chunk) {
+        const int64_t d1 = std::min(nd, d0 + chunk);
+        CK(cudaMemsetAsync(qcount, 0, 8, c->stream));
+        QueueDev q;
+        q.f = c->q_f.as<float>(); q.t = c->q_t.as<double>(); q.i = c->q_i.as<int32_t>();
+        q.count = qcount; q.cap = c->q_cap;
+        int64_t blocks = std::min<int64_t>((d1 - d0 + 255) / 256, (int64_t)nsm * 8);
+        cudaEventRecord(c->ev[1], c->stream);
+        k_source_phantom<<<(unsigned)std::max<int64_t>(blocks, 1), 256, smem, c->stream>>>(
+            c->d_sim.as<SimDesc>(), d0, d1, q, c->record_exits ? c->exits.as<ExitRec>() : nullptr, dcnt);
+        cudaEventRecord(c->ev[2], c->stream);
+        st->kernel_launches++;
+        unsigned long long hq = 0;
+        CK(cudaMemcpyAsync(&hq, qcount, 8, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        CK(cudaGetLastError());
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
+        ms_sp += ms;
+        if (c->record_exits)
+            CK(cudaMemcpy(c->host_exits.data() + 2 * d0, c->exits.p, (size_t)2 * (d1 - d0) * sizeof(ExitRec),
+                          cudaMemcpyDeviceToHost));
+        // room for the worst case of this chunk's queue
+        rc = grow_pulses(c, pulses_used + (int64_t)hq * kMaxPulse, pulses_used);
+        if (rc) return rc;
+        if (c->record_hits) { rc = grow_hits(c, hits_used + (int64_t)hq * kMaxHits, hits_used); if (rc) return rc; }
+        PulseDev P = pulse_view(c);
+        HitDev H;
+        H.id = c->h_id.as<int32_t>(); H.f = c->h_f.as<float>(); H.count = hcount; H.cap = c->h_cap;
+        int64_t dblocks = std::min<int64_t>(((int64_t)hq + 255) / 256, (int64_t)nsm * 8);
+        cudaEventRecord(c->ev[1], c->stream);
+        if (hq > 0) {
+            k_detector<<<(unsigned)std::max<int64_t>(dblocks, 1), 256, smem, c->stream>>>(c->d_sim.as<SimDesc>(), q, P,
+                                                                                       H, c->record_hits, dcnt);
+            st->kernel_launches++;
+        }
+        cudaEventRecord(c->ev[2], c->stream);
+        unsigned long long hp[2] = {0, 0};
+        CK(cudaMemcpyAsync(hp, pcount, 16, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        CK(cudaGetLastError());
+        cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
+        ms_det += ms;
+        pulses_used = (int64_t)std::min<unsigned long long>(hp[0], (unsigned long long)c->p_cap);
+        hits_used = (int64_t)std::min<unsigned long long>(hp[1], (unsigned long long)c->h_cap);
+    }
+    Counters h{};
+    CK(cudaMemcpyAsync(&h, dcnt, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (h.queue_drop || h.pulse_drop || h.hit_drop)
+        return fail(c, GPET_ERR_CAPACITY, "a device buffer overflowed (queue/pulse/hit drops)");
+    c->n_pulses = pulses_used;
+    c->n_hits = c->record_hits ? hits_used : 0;
+    float ms_digi = 0;
+    rc = digitize_and_finish(c, c->n_pulses, st, h, &ms_digi);
+    if (rc) return rc;
+    cudaEventRecord(c->ev[3], c->stream);
+    CK(cudaEventSynchronize(c->ev[3]));
+    float ms_tot = 0;
+    cudaEventElapsedTime(&ms_tot, c->ev[0], c->ev[3]);
+    fill_stats(c, h, st);
+    st->n_decays = nd;
+    st->ms_total = ms_tot;
+    st->ms_source_phantom = ms_sp;
+    st->ms_detector = ms_det;
+    st->ms_digitizer = ms_digi;
+    st->ms_coincidence = 0;
+    c->last = *st;
+    return GPET_OK;
+}
+
+int gpet_digitize(gpet_ctx* c, const gpet_event* ev, const uint8_t* scat, const uint8_t* slot, int64_t n,
+                  gpet_run_stats* st)
+{
+    if (!c || n < 0 || (n > 0 && (!ev || !scat || !slot))) return GPET_ERR_ARG;
+    if (!c->have_geo) return fail(c, GPET_ERR_ARG, "load the geometry first (site numbering)");
+    CK(cudaSetDevice(c->device));
+    gpet_run_stats local{};
+    if (!st) st = &local;
+    std::memset(st, 0, sizeof(*st));
+    int rc = grow_pulses(c, std::max<int64_t>(n, 1), 0);
+    if (rc) return rc;
+    CK(c->cnt.ensure(64 * 8));
+    CK(cudaMemsetAsync(c->cnt.p, 0, 64 * 8, c->stream));
+    std::vector<int32_t> I((size_t)n * 6);
+    std::vector<double> T((size_t)n);
+    std::vector<float> F((size_t)n * 4);
+    std::vector<uint8_t> M((size_t)n);
+    for (int64_t i = 0; i < n; ++i) {
+        I[i] = ev[i].parn; I[n + i] = ev[i].pann; I[2 * n + i] = ev[i].modn; I[3 * n + i] = ev[i].cryn;
+        I[4 * n + i] = ev[i].siten; I[5 * n + i] = ev[i].eventid;
+        T[i] = ev[i].t;
+        F[i] = ev[i].E; F[n + i] = ev[i].x; F[2 * n + i] = ev[i].y; F[3 * n + i] = ev[i].z;
+        if (slot[i] > 0x7f) return fail(c, GPET_ERR_ARG, "slot must be < 128");
+        M[i] = (uint8_t)(slot[i] | (scat[i] ? 0x80 : 0));
+    }
+    PulseDev P = pulse_view(c);
+    for (int a = 0; a < 6; ++a)
+        CK(cudaMemcpyAsync(reinterpret_cast<int32_t*>(c->p_int.p) + a * c->p_cap, I.data() + a * n, n * 4,
+                           cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->p_t.p, T.data(), n * 8, cudaMemcpyHostToDevice, c->stream));
+    for (int a = 0; a < 4; ++a)
+        CK(cudaMemcpyAsync(reinterpret_cast<float*>(c->p_f.p) + a * c->p_cap, F.data() + a * n, n * 4,
+                           cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->p_meta.p, M.data(), n, cudaMemcpyHostToDevice, c->stream));
+    (void)P;
+    c->n_pulses = n;
+    c->n_hits = 0;
+    Counters h{};
+    float ms_digi = 0;
+    rc = digitize_and_finish(c, n, st, h, &ms_digi);
+    if (rc) return rc;
+    fill_stats(c, h, st);
+    st->ms_digitizer = ms_digi;
+    st->ms_total = ms_digi;
+    return GPET_OK;
+}
+
+// ---------------------------------------------------------------- outputs
+static int copy_pulse_fields(gpet_ctx* c, const uint32_t* d_idx, int64_t n, bool blurred, std::vector<gpet_event>& out,
+                             std::vector<uint8_t>& meta)
+{
+    out.resize((size_t)n);
+    meta.resize((size_t)n);
+    if (n == 0) return GPET_OK;
+    CK(c->g_ev.ensure((size_t)n * sizeof(EventRec)));
+    CK(c->g_meta.ensure((size_t)n));
+    PulseDev P = pulse_view(c);
+    if (gather_events(P, d_idx, n, blurred, c->dg, c->g_ev.as<EventRec>(), c->g_meta.as<uint8_t>(), c->stream))
+        return fail(c, GPET_ERR_CUDA, "gather of event records failed");
+    CK(cudaMemcpyAsync(out.data(), c->g_ev.p, (size_t)n * sizeof(EventRec), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(meta.data(), c->g_meta.p, (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return GPET_OK;
+}
+
+int gpet_get_singles(gpet_ctx* c, gpet_event* buf, uint8_t* scat, int64_t cap, int64_t* n)
+{
+    if (!c || !n) return GPET_ERR_ARG;
+    *n = c->have_results ? c->n_singles : 0;
+    if (!buf || *n == 0) return GPET_OK;
+    if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the singles");
+    std::vector<gpet_event> ev;
+    std::vector<uint8_t> m;
+    int rc = copy_pulse_fields(c, c->dg.single_idx, *n, true, ev, m);
+    if (rc) return rc;
+    std::memcpy(buf, ev.data(), sizeof(gpet_event) * (size_t)*n);
+    if (scat)
+        for (int64_t i = 0; i < *n; ++i) scat[i] = (m[i] & 0x80) ? 1 : 0;
+    return GPET_OK;
+}
+
+int gpet_get_pulses(gpet_ctx* c, gpet_event* buf, uint8_t* scat, uint8_t* slot, int64_t cap, int64_t* n)
+{
+    if (!c || !n) return GPET_ERR_ARG;
+    *n = c->have_results ? c->n_pulses : 0;
+    if (!buf || *n == 0) return GPET_OK;
+    if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the pulses");
+    std::vector<gpet_event> ev;
+    std::vector<uint8_t> m;
+    int rc = copy_pulse_fields(c, nullptr, *n, false, ev, m);
+    if (rc) return rc;
+    std::vector<int64_t> order((size_t)*n);
+    for (int64_t i = 0; i < *n; ++i) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+        if (ev[a].parn != ev[b].parn) return ev[a].parn < ev[b].parn;
+        return (m[a] & 0x7f) < (m[b] & 0x7f);
+    });
+    for (int64_t i = 0; i < *n; ++i) {
+        buf[i] = ev[order[i]];
+        if (scat) scat[i] = (m[order[i]] & 0x80) ? 1 : 0;
+        if (slot) slot[i] = m[order[i]] & 0x7f;
+    }
+    return GPET_OK;
+}
+
+int gpet_get_coincidences(gpet_ctx* c, int64_t* pairs, uint8_t* klass, int64_t cap, int64_t* n)
+{
+    if (!c || !n) return GPET_ERR_ARG;
+    *n = c->have_results ? c->n_coinc : 0;
+    if (!pairs || *n == 0) return GPET_OK;
+    if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the coincidences");
+    CK(cudaMemcpyAsync(pairs, c->dg.coinc_pairs, sizeof(int64_t) * 2 * (size_t)*n, cudaMemcpyDeviceToHost, c->stream));
+    if (klass) CK(cudaMemcpyAsync(klass, c->dg.coinc_class, (size_t)*n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return GPET_OK;
+}
+
+int gpet_get_hits(gpet_ctx* c, int32_t* ids, float* f, int64_t cap, int64_t* n)
+{
+    if (!c || !n) return GPET_ERR_ARG;
+    *n = c->have_results ? c->n_hits : 0;
+    if ((!ids && !f) || *n == 0) return GPET_OK;
+    if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the hits");
+    if (ids) CK(cudaMemcpyAsync(ids, c->h_id.p, (size_t)*n * 20, cudaMemcpyDeviceToHost, c->stream));
+    if (f) CK(cudaMemcpyAsync(f, c->h_f.p, (size_t)*n * 20, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return GPET_OK;
+}
+
+int gpet_get_exits(gpet_ctx* c, void* buf, int64_t cap, int64_t* n)
+{
+    if (!c || !n) return GPET_ERR_ARG;
+    *n = (int64_t)c->host_exits.size();
+    if (!buf || *n == 0) return GPET_OK;
+    if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the exits");
+    std::memcpy(buf, c->host_exits.data(), sizeof(ExitRec) * (size_t)*n);
+    return GPET_OK;
+}
+
+static int append_file(gpet_ctx* c, const std::string& path, const void* p, size_t bytes)
+{
+    FILE* f = std::fopen(path.c_str(), "ab");
+    if (!f) return fail(c, GPET_ERR_IO, "cannot open " + path);
+    if (bytes && std::fwrite(p, 1, bytes, f) != bytes) { std::fclose(f); return fail(c, GPET_ERR_IO, "short write " + path); }
+    std::fclose(f);
+    return GPET_OK;
+}
+
+int gpet_write_outputs(gpet_ctx* c, const char* dir)
+{
+    if (!c || !dir) return GPET_ERR_ARG;
+    if (!c->have_results) return fail(c, GPET_ERR_ARG, "no results to write");
+    std::string d(dir);
+    int64_t n = 0;
+    int rc;
+    // adder.dat: pulses after adder + readout (gPET.cu:383)
+    gpet_get_pulses(c, nullptr, nullptr, nullptr, 0, &n);
+    std::vector<gpet_event> ev((size_t)n);
+    if (n && (rc = gpet_get_pulses(c, ev.data(), nullptr, nullptr, n, &n))) return rc;
+    if ((rc = append_file(c, d + "/adder.dat", ev.data(), sizeof(gpet_event) * (size_t)n))) return rc;
+    // HitsID.dat / Hits.dat (gPET.cu:367-379)
+    gpet_get_hits(c, nullptr, nullptr, 0, &n);
+    std::vector<int32_t> hid((size_t)n * 5);
+    std::vector<float> hf((size_t)n * 5);
+    if (n && (rc = gpet_get_hits(c, hid.data(), hf.data(), n, &n))) return rc;
+    if ((rc = append_file(c, d + "/HitsID.dat", hid.data(), hid.size() * 4))) return rc;
+    if ((rc = append_file(c, d + "/Hits.dat", hf.data(), hf.size() * 4))) return rc;
+    // singles.dat (gPET.cu:424)
+    gpet_get_singles(c, nullptr, nullptr, 0, &n);
+    std::vector<gpet_event> sg((size_t)n);
+    if (n && (rc = gpet_get_singles(c, sg.data(), nullptr, n, &n))) return rc;
+    if ((rc = append_file(c, d + "/singles.dat", sg.data(), sizeof(gpet_event) * (size_t)n))) return rc;
+    // coincidences.dat: pairs of Event records; coincidences_class.dat: class bytes
+    int64_t nc = 0;
+    gpet_get_coincidences(c, nullptr, nullptr, 0, &nc);
+    std::vector<int64_t> pr((size_t)nc * 2);
+    std::vector<uint8_t> cl((size_t)nc);
+    if (nc && (rc = gpet_get_coincidences(c, pr.data(), cl.data(), nc, &nc))) return rc;
+    std::vector<gpet_event> ce((size_t)nc * 2);
+    for (int64_t i = 0; i < nc; ++i) { ce[2 * i] = sg[pr[2 * i]]; ce[2 * i + 1] = sg[pr[2 * i + 1]]; }
+    if ((rc = append_file(c, d + "/coincidences.dat", ce.data(), sizeof(gpet_event) * ce.size()))) return rc;
+    if ((rc = append_file(c, d + "/coincidences_class.dat", cl.data(), cl.size()))) return rc;
+    return GPET_OK;
+}
+
+// ---------------------------------------------------------------- introspection
+int gpet_get_panels(gpet_ctx* c, float* out, int32_t cap, int32_t* np)
+{
+    if (!c || !np) return GPET_ERR_ARG;
+    *np = c->geo.npanels;
+    if (!out) return GPET_OK;
+    if (cap < *np) return fail(c, GPET_ERR_ARG, "buffer too small for the panels");
+    std::memcpy(out, c->geo.panels.data(), sizeof(float) * 32 * (size_t)*np);
+    return GPET_OK;
+}
+
+int gpet_get_counts(gpet_ctx* c, int32_t out[4])
+{
+    if (!c || !out) return GPET_ERR_ARG;
+    out[0] = c->geo.moduleNy; out[1] = c->geo.moduleN; out[2] = c->geo.crystalNy; out[3] = c->geo.crystalN;
+    return GPET_OK;
+}
+
+int gpet_get_source_layout(gpet_ctx* c, int64_t* first, int64_t* count, int32_t cap, int32_t* nsrc)
+{
+    if (!c || !nsrc) return GPET_ERR_ARG;
+    if (c->use_psf) { *nsrc = 0; return GPET_OK; }
+    std::string e = source_layout(c);
+    if (!e.empty()) return fail(c, GPET_ERR_ARG, e);
+    *nsrc = (int32_t)c->src_first.size();
+    if (!first || !count) return GPET_OK;
+    if (cap < *nsrc) return fail(c, GPET_ERR_ARG, "buffer too small for the source layout");
+    for (int i = 0; i < *nsrc; ++i) { first[i] = c->src_first[i]; count[i] = c->src_count[i]; }
+    return GPET_OK;
+}
+
+int gpet_get_majorant(gpet_ctx* c, int which, float* tab, float* e0, float* ide)
+{
+    if (!c || !tab) return GPET_ERR_ARG;
+    const std::vector<float>& w = which == 0 ? c->wck_ph : c->wck_det;
+    if (w.size() != (size_t)kNwck) return fail(c, GPET_ERR_ARG, "majorant not built yet");
+    std::memcpy(tab, w.data(), 4 * kNwck);
+    if (e0) *e0 = c->wck_e0;
+    if (ide) *ide = c->wck_ide;
+    return GPET_OK;
+}
+
+int gpet_get_table(gpet_ctx* c, int which, float* out, int64_t cap, int64_t* n)
+{
+    if (!c || !n) return GPET_ERR_ARG;
+    const std::vector<float>* v = nullptr;
+    switch (which) {
+    case 0: v = &c->tab.lamph; break;
+    case 1: v = &c->tab.compt; break;
+    case 2: v = &c->tab.phote; break;
+    case 3: v = &c->tab.rayle; break;
+    case 4: v = &c->tab.cmpsf; break;
+    case 5: v = &c->tab.rayff; break;
+    default: return GPET_ERR_ARG;
+    }
+    *n = (int64_t)v->size();
+    if (!out) return GPET_OK;
+    if (cap < *n) return GPET_ERR_ARG;
+    std::memcpy(out, v->data(), 4 * (size_t)*n);
+    return GPET_OK;
+}
+
+}  // extern "C"

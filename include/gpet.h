@@ -1,0 +1,154 @@
+/* gpet.h - C ABI of libgpet, the GB300-native gPET hot path.
+ *
+ * The reference exposes no library API: its boundary is the process
+ * `./gPET input_PET.in` (main.cu:26-33) reading gPET's input files and writing
+ * its output records, and internally the two drivers
+ *     void sampleParticle(Source, Isotopes, float tstart, float tend, int nPanels)   gPET.h:155
+ *     void simulateParticle(Particle, int ptype, int nPanels)                         gPET.h:154
+ * that run on process-global device state set up by loadPhantom/init/
+ * read_file_ro/iniPanel/iniwck (gPET.h:129-160). This header replaces that
+ * seam with re-entrant calls on an opaque context: plain pointers and sizes,
+ * int status returns (0 = success), no global state, one CUDA stream per
+ * context. Each entry point names the reference code it replaces.
+ *
+ * Units as in the reference: energy eV, length cm, time microseconds. */
+#ifndef GPET_H
+#define GPET_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPET_OK 0
+#define GPET_ERR_ARG -1       /* bad argument or state */
+#define GPET_ERR_IO -2        /* missing or malformed input file */
+#define GPET_ERR_CUDA -3      /* CUDA runtime error */
+#define GPET_ERR_CAPACITY -4  /* a bounded buffer overflowed; see gpet_last_error */
+#define GPET_ERR_NOGPU -5     /* no CUDA device, or the kernels were not built for it */
+
+typedef struct gpet_ctx gpet_ctx;
+
+/* Event record of the reference (gPET.h:87-92): 48 bytes, t at offset 24.
+ * singles.dat / adder.dat are arrays of this record (detector.cu:287-307). */
+typedef struct {
+    int32_t parn, pann, modn, cryn, siten, eventid;
+    double t;
+    float E, x, y, z;
+} gpet_event;
+
+/* Panel record: 32 floats per panel, in this order (object_t, gPET.h:54-78):
+ * 0-2 length xyz, 3-5 module size, 6-8 module space, 9-11 crystal size,
+ * 12-14 crystal space, 15-17 offset, 18-20 expansion direction, 21-23 local x
+ * axis, 24-26 local y axis, 27-29 local z axis, 30 panel id, 31 unused. */
+#define GPET_PANEL_STRIDE 32
+
+typedef struct {
+    int64_t n_decays;     /* decays simulated */
+    int64_t n_pairs;      /* annihilation pairs emitted (beta+ branch) */
+    int64_t n_entered;    /* photons that entered a detector panel */
+    int64_t n_pulses;     /* pulses after the per-photon adder and readout */
+    int64_t n_hits;       /* energy deposits in crystals */
+    int64_t n_threshold;  /* pulses after blur and the threshold window */
+    int64_t n_deadtime;   /* after dead time */
+    int64_t n_singles;    /* after the energy window */
+    int64_t n_coinc, n_true, n_scatter, n_random, n_multiple;
+    int64_t n_overflow;   /* photons whose pulse or hit list overflowed */
+    int64_t n_stepcap;    /* histories stopped by the step cap */
+    double ms_total;             /* device time of the whole run (CUDA events) */
+    double ms_source_phantom;    /* source + phantom transport kernels */
+    double ms_detector;          /* detector transport kernels */
+    double ms_digitizer;         /* blur .. energy window, incl. sorts */
+    double ms_coincidence;       /* coincidence sorter */
+    int64_t kernel_launches;     /* kernels launched by this run */
+    int64_t phantom_steps;       /* Woodcock steps in the phantom (all photons) */
+    int64_t detector_steps;      /* Woodcock steps in the panels */
+} gpet_run_stats;
+
+/* ------------------------------------------------------------ lifetime */
+/* Create a context on CUDA device `device` (iniDevice, iniDevice.cu:1-60). */
+int gpet_create(int device, gpet_ctx** out);
+void gpet_destroy(gpet_ctx* ctx);
+/* Message of the last failing call on this context (never NULL). */
+const char* gpet_last_error(gpet_ctx* ctx);
+
+/* Options the reference has no input key for (key=value):
+ *   seed (uint64, default 20261203), sim_id, n_decays (exact decay count,
+ *   split over sources in proportion to their expected decays),
+ *   coinc_window_ns (4), coinc_policy (0 single window with exactly two
+ *   singles, 1 all pairs), record_hits (1), record_exits (0),
+ *   base_dir (directory relative paths in input_PET.in resolve against),
+ *   data_dir (table directory, default <base_dir>/data), chunk_decays. */
+int gpet_set_option(gpet_ctx* ctx, const char* key, const char* value);
+
+/* ------------------------------------------------------------ inputs */
+/* Parse input_PET.in (main.cu:50-182) and load everything it references:
+ * tables (init, initialize.cu:886-917), phantom (loadPhantom :32-74),
+ * detector (read_file_ro detector.cu:64-285, iniPanel initialize.cu:969),
+ * and the voxel source (loadIsotopes/readSource :10-31, :116-144) or the
+ * PSF (readParticle :76-115). */
+int gpet_load_config(gpet_ctx* ctx, const char* input_pet_in);
+/* data/input4gPET.{matter,lamph,compt,cmpsf,phote,rayle,rayff} + isotopes.txt
+ * (rmater..rrayff, initialize.cu:279-748; loadIsotopes :10-31). */
+int gpet_load_tables(gpet_ctx* ctx, const char* data_dir);
+/* Voxel phantom from caller buffers (copied): int32 material, float32
+ * density, x fastest (loadPhantom + initPhantom, initialize.cu:32-74, 831-884). */
+int gpet_set_phantom(gpet_ctx* ctx, const int32_t* mat, const float* den, const int32_t dims[3],
+                     const float offset[3], const float size[3]);
+/* Panel ring from a .geo file (read_file_ro detector.cu:64-285; iniPanel and
+ * iniwck for the detector, initialize.cu:919-1224). */
+int gpet_load_geometry(gpet_ctx* ctx, const char* geo_path);
+/* source.txt (readSource, initialize.cu:116-144) for the window [tstart, tend] s. */
+int gpet_set_source_file(gpet_ctx* ctx, const char* source_txt, float tstart, float tend);
+/* Phase-space source from caller buffers: n records of 8 doubles
+ * x,y,z,t,vx,vy,vz,E; ptype 0 positron, 1 photon (readParticle,
+ * initialize.cu:76-115; simulateParticle gPET.cu:13-199). */
+int gpet_set_source_psf(gpet_ctx* ctx, const double* rec8, int64_t n, int ptype);
+
+/* ------------------------------------------------------------ run */
+/* Simulate the configured source and digitize: sampleParticle (gPET.cu:201-437)
+ * or simulateParticle (gPET.cu:13-199) followed by the coincidence sorter. */
+int gpet_run(gpet_ctx* ctx, gpet_run_stats* stats);
+/* Digitizer + coincidence sorter alone on a caller pulse list (the digitizer
+ * chain of gPET.cu:385-424): scat[i] != 0 marks a photon that scattered in the
+ * phantom, slot[i] is the pulse's index within its photon's readout list. */
+int gpet_digitize(gpet_ctx* ctx, const gpet_event* pulses, const uint8_t* scat, const uint8_t* slot, int64_t n,
+                  gpet_run_stats* stats);
+
+/* ------------------------------------------------------------ outputs */
+/* Each copies into caller memory; with buf == NULL only *n is set. */
+int gpet_get_singles(gpet_ctx* ctx, gpet_event* buf, uint8_t* scat, int64_t cap, int64_t* n);
+/* Pulses after adder + readout, ordered by (parn, slot) (adder.dat content). */
+int gpet_get_pulses(gpet_ctx* ctx, gpet_event* buf, uint8_t* scat, uint8_t* slot, int64_t cap, int64_t* n);
+/* Coincidences: index pairs into the singles list and class (0 true,
+ * 1 scatter, 2 random). */
+int gpet_get_coincidences(gpet_ctx* ctx, int64_t* pairs, uint8_t* klass, int64_t cap, int64_t* n);
+/* Hits (HitsID.dat / Hits.dat records, gPET.cu:367-379): ids [n][5] = parn,
+ * panel, module, crystal, type (1/2 Compton, 4 photoelectric); f [n][5] = E,
+ * t, local x, y, z. Order within a photon is deposit order. */
+int gpet_get_hits(gpet_ctx* ctx, int32_t* ids, float* f, int64_t cap, int64_t* n);
+/* Phantom exit state of every photon (option record_exits=1): per photon 12
+ * words: x,y,z,ux,uy,uz,E (float), nscat (int32), t (double), status (int32:
+ * 0 absorbed, 1 escaped, 2 not emitted, 3 step cap), panel (int32, -1 none). */
+int gpet_get_exits(gpet_ctx* ctx, void* buf, int64_t cap, int64_t* n);
+/* Append the run's records to out_dir: singles.dat, adder.dat, HitsID.dat,
+ * Hits.dat (outevents/outputData, detector.cu:287-307, 387-408) and
+ * coincidences.dat (+ coincidences_class.dat). */
+int gpet_write_outputs(gpet_ctx* ctx, const char* out_dir);
+
+/* ------------------------------------------------------------ introspection */
+int gpet_get_panels(gpet_ctx* ctx, float* out, int32_t cap, int32_t* npanels);
+/* moduleNy, moduleN, crystalNy, crystalN (iniPanel, initialize.cu:1074-1086) */
+int gpet_get_counts(gpet_ctx* ctx, int32_t out[4]);
+/* decays per source: first index and count */
+int gpet_get_source_layout(gpet_ctx* ctx, int64_t* first, int64_t* count, int32_t cap, int32_t* nsrc);
+/* Woodcock majorant table (which 0 phantom, 1 detector): 4096 floats + e0, 1/de */
+int gpet_get_majorant(gpet_ctx* ctx, int which, float* tab4096, float* e0, float* ide);
+/* tables as parsed: which 0 lamph 1 compt 2 phote 3 rayle 4 cmpsf 5 rayff */
+int gpet_get_table(gpet_ctx* ctx, int which, float* out, int64_t cap, int64_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

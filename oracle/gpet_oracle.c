@@ -1,0 +1,1210 @@
+/* gpet_oracle.c - CPU oracle for the gPET hot path. TEST INFRASTRUCTURE ONLY:
+ * imported by the tests and by bench.py's CPU-baseline leg, never by the
+ * product. See gpet_oracle.h for what it restates and how it is built.
+ *
+ * Build: ORACLE_FP32 defined -> single-precision transport with detmath.h
+ * (operation-for-operation twin of the CUDA kernels); otherwise double
+ * precision transport with libm. Compile with -ffp-contract=off. */
+#include "gpet_oracle.h"
+#include "../gpet_gb300/csrc/detmath.h"
+
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifdef ORACLE_FP32
+typedef float real;
+#define R_LOG(x) dm_logf(x)
+#define R_EXP(x) dm_expf(x)
+#define R_SQRT(x) dm_sqrt(x)
+#define R_CBRT(x) dm_cbrtf(x)
+#define R_FLOOR(x) floorf(x)
+#define R_FABS(x) fabsf(x)
+#define D_LOG(x) dm_log(x)
+static inline void r_sincos_turns(real u, real* s, real* c) { dm_sincos_turns(u, s, c); }
+#else
+typedef double real;
+#define R_LOG(x) log(x)
+#define R_EXP(x) exp(x)
+#define R_SQRT(x) sqrt(x)
+#define R_CBRT(x) cbrt(x)
+#define R_FLOOR(x) floor(x)
+#define R_FABS(x) fabs(x)
+#define D_LOG(x) log(x)
+static inline void r_sincos_turns(real u, real* s, real* c)
+{
+    double a = 6.283185307179586476925 * u;
+    *s = sin(a);
+    *c = cos(a);
+}
+#endif
+
+#define C_MC2 ((real)510999.1)          /* constants.h:37 MC2 (eV) */
+#define C_IMC2 ((real)1.95695060911e-6) /* constants.h:38 */
+#define C_SPE 29979.2458                /* cm/us, gPET_kernals.cu:264 */
+#define MAX_STEPS 100000
+#define MAX_PULSE 8   /* distinct crystals per photon in the adder list */
+#define MAX_HITS 16   /* deposits recorded per photon */
+
+enum { TAG_DECAY = 1, TAG_PHANTOM = 2, TAG_DET = 4, TAG_BLUR = 8 };
+
+/* ------------------------------------------------------------------ RNG */
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), restated from the paper. */
+void oracle_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4])
+{
+    uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+    uint32_t k0 = key_in[0], k1 = key_in[1];
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+typedef struct { uint32_t key[2], ctr[4], buf[4]; int pos; } stream_t;
+
+static void st_init(stream_t* s, const or_scene* sc, uint32_t tag, uint64_t id)
+{
+    s->key[0] = (uint32_t)sc->seed;
+    s->key[1] = (uint32_t)(sc->seed >> 32) + sc->sim_id;
+    s->ctr[0] = 0; s->ctr[1] = tag; s->ctr[2] = (uint32_t)id; s->ctr[3] = (uint32_t)(id >> 32);
+    s->pos = 4;
+}
+
+static inline uint32_t st_next(stream_t* s)
+{
+    if (s->pos == 4) {
+        oracle_philox4x32_10(s->ctr, s->key, s->buf);
+        s->ctr[0]++;
+        s->pos = 0;
+    }
+    return s->buf[s->pos++];
+}
+
+static inline real st_u(stream_t* s) { return (real)dm_u01(st_next(s)); }
+
+static inline double st_ud(stream_t* s)
+{
+    uint32_t hi = st_next(s);
+    uint32_t lo = st_next(s);
+    return dm_u01d(hi, lo);
+}
+
+/* normal deviate: Box-Muller, two uniforms (replaces curand_normal) */
+static inline real st_normal(stream_t* s)
+{
+    real u1 = st_u(s), u2 = st_u(s);
+    real sn, cs;
+    r_sincos_turns(u2, &sn, &cs);
+    return R_SQRT((real)-2.0 * R_LOG(u1)) * cs;
+}
+
+/* the digitizer always computes in the Event record's float */
+static inline float st_normal_f(stream_t* s)
+{
+    float u1 = dm_u01(st_next(s)), u2 = dm_u01(st_next(s));
+    return dm_normal(u1, u2);
+}
+
+int oracle_real_bytes(void) { return (int)sizeof(real); }
+
+/* --------------------------------------------------------------- lookups */
+/* linear interpolation at fractional index x with edge clamping: the value the
+ * reference's linearly filtered 1-D textures return (gPET_kernals.cu:31-64) */
+static inline real lerp1(const float* tab, int n, real x)
+{
+    if (!(x > (real)0.0)) return (real)tab[0];
+    if (x >= (real)(n - 1)) return (real)tab[n - 1];
+    int i = (int)x;
+    real f = x - (real)i;
+    real a = (real)tab[i], b = (real)tab[i + 1];
+    return a + f * (b - a);
+}
+
+/* bilinear lookup of an inverse-CDF surface [ncp][ne] at (energy index xe,
+ * probability index ycp), clamped: tex3D(s_tex/f_tex) gPET_kernals.cu:82,142 */
+static inline real lerp2(const float* s, int ncp, int ne, real xe, real ycp)
+{
+    if (!(xe > (real)0.0)) xe = (real)0.0;
+    if (xe > (real)(ne - 1)) xe = (real)(ne - 1);
+    if (!(ycp > (real)0.0)) ycp = (real)0.0;
+    if (ycp > (real)(ncp - 1)) ycp = (real)(ncp - 1);
+    int ie = (int)xe; if (ie > ne - 2) ie = ne - 2;
+    int ic = (int)ycp; if (ic > ncp - 2) ic = ncp - 2;
+    real fe = xe - (real)ie, fc = ycp - (real)ic;
+    const float* r0 = s + (size_t)ic * ne;
+    const float* r1 = r0 + ne;
+    real a = (real)r0[ie] + fe * ((real)r0[ie + 1] - (real)r0[ie]);
+    real b = (real)r1[ie] + fe * ((real)r1[ie + 1] - (real)r1[ie]);
+    return a + fc * (b - a);
+}
+
+static inline real xs_at(const or_scene* sc, const float* tab, int m, real e)
+{
+    real x = (real)sc->idle * (e - (real)sc->e0);
+    return lerp1(tab + (size_t)m * sc->ne, sc->ne, x);
+}
+
+/* Woodcock majorant tables (replaces iniwck, initialize.cu:773-829, 919-966):
+ * node i at e_i = eminph + de*i, de = (emax - eminph)/4096 (the reference's
+ * (1-1e-10) factor is 1 in float). Each node stores 1/max over materials of
+ * rho_max(m) * max(mu_m over [e_{i-1}, e_{i+1}]) of the linearly interpolated
+ * table, so the interpolated majorant bounds every material everywhere. */
+#define NWCK 4096
+typedef struct { float e0, ide; float tab[NWCK]; } wck_t;
+
+static double xs_lerp_d(const or_scene* sc, const float* tab, double e)
+{
+    double x = (double)sc->idle * (e - (double)sc->e0);
+    if (!(x > 0.0)) return tab[0];
+    if (x >= sc->ne - 1) return tab[sc->ne - 1];
+    int i = (int)x;
+    double f = x - i;
+    return tab[i] + f * ((double)tab[i + 1] - (double)tab[i]);
+}
+
+static void build_wck(const or_scene* sc, const float* maxden, wck_t* w)
+{
+    float de = (sc->emax - sc->eminph) / (float)NWCK;
+    w->e0 = sc->eminph;
+    w->ide = 1.0f / de;
+    for (int i = 0; i < NWCK; ++i) {
+        double lo = (double)sc->eminph + (double)de * (double)(i > 0 ? i - 1 : 0);
+        double hi = (double)sc->eminph + (double)de * (double)(i + 1);
+        double best = 0.0;
+        for (int m = 0; m < sc->nmat; ++m) {
+            if (!(maxden[m] > 0.0f)) continue;
+            const float* tab = sc->lamph + (size_t)m * sc->ne;
+            double mx = xs_lerp_d(sc, tab, lo);
+            double v = xs_lerp_d(sc, tab, hi);
+            if (v > mx) mx = v;
+            double xlo = (double)sc->idle * (lo - (double)sc->e0);
+            double xhi = (double)sc->idle * (hi - (double)sc->e0);
+            int k0 = (int)ceil(xlo), k1 = (int)floor(xhi);
+            if (k0 < 0) k0 = 0;
+            if (k1 > sc->ne - 1) k1 = sc->ne - 1;
+            for (int k = k0; k <= k1; ++k)
+                if (tab[k] > mx) mx = tab[k];
+            mx *= (double)maxden[m];
+            if (mx > best) best = mx;
+        }
+        w->tab[i] = (float)(1.0 / best);
+    }
+}
+
+static inline real wck_at(const wck_t* w, real e)
+{
+    return lerp1(w->tab, NWCK, (real)w->ide * (e - (real)w->e0));
+}
+
+/* -------------------------------------------------------------- geometry */
+/* rotate(): gPET_kernals.cu:172-254 (direction change by polar cos and
+ * azimuth; the azimuth is given in turns, phi = 2*pi*u) */
+static void rotate(real* u, real* v, real* w, real costh, real phi_turns)
+{
+    real rho2 = (*u) * (*u) + (*v) * (*v);
+    real norm = rho2 + (*w) * (*w);
+    if (R_FABS(norm - (real)1.0) > (real)1.0e-4) {
+        norm = (real)1.0 / R_SQRT(norm);
+        *u = (*u) * norm; *v = (*v) * norm; *w = (*w) * norm;
+    }
+    real sinphi, cosphi;
+    r_sincos_turns(phi_turns, &sinphi, &cosphi);
+    real temp = costh * costh;
+    if (rho2 > (real)1.0e-20f) {
+        real sthrho = temp < (real)1.0 ? R_SQRT(((real)1.0 - temp) / rho2) : (real)0.0;
+        real urho = (*u) * sthrho, vrho = (*v) * sthrho;
+        real uu = (*u) * costh - vrho * sinphi + (*w) * urho * cosphi;
+        real vv = (*v) * costh + urho * sinphi + (*w) * vrho * cosphi;
+        real ww = (*w) * costh - rho2 * sthrho * cosphi;
+        *u = uu; *v = vv; *w = ww;
+    } else {
+        real sinth = temp < (real)1.0 ? R_SQRT((real)1.0 - temp) : (real)0.0;
+        *v = sinth * sinphi;
+        if (*w > (real)0.0) { *u = sinth * cosphi; *w = costh; }
+        else { *u = -sinth * cosphi; *w = -costh; }
+    }
+}
+
+/* getAbsVox, gPET_kernals.cu:19-29: index = trunc((x-off)*idx); an index of 0
+ * counts as outside (the reference tests `<= 0` on the truncated value), so
+ * inside means 1 <= (x-off)*idx < n in every axis. */
+static inline int abs_vox(const or_scene* sc, real idx, real idy, real idz,
+                          real x, real y, real z, int* ix, int* iy, int* iz)
+{
+    real vx = (x - (real)sc->offx) * idx;
+    real vy = (y - (real)sc->offy) * idy;
+    real vz = (z - (real)sc->offz) * idz;
+    int in = vx >= (real)1.0 && vx < (real)sc->nx && vy >= (real)1.0 && vy < (real)sc->ny &&
+             vz >= (real)1.0 && vz < (real)sc->nz;
+    if (in) { *ix = (int)vx; *iy = (int)vy; *iz = (int)vz; }
+    return in;
+}
+
+static inline float den_clamped(const or_scene* sc, int ix, int iy, int iz)
+{
+    if (ix < 0) ix = 0; if (ix > sc->nx - 1) ix = sc->nx - 1;
+    if (iy < 0) iy = 0; if (iy > sc->ny - 1) iy = sc->ny - 1;
+    if (iz < 0) iz = 0; if (iz > sc->nz - 1) iz = sc->nz - 1;
+    return sc->den[(size_t)ix + (size_t)sc->nx * ((size_t)iy + (size_t)sc->ny * iz)];
+}
+
+/* ---------------------------------------------------------------- source */
+/* getPositionFromShape, gPET_kernals.cu:445-482 */
+static void shape_position(const or_scene* sc, int si, stream_t* st, real p[3])
+{
+    const float* c = sc->src_coef + 6 * si;
+    int shape = sc->src_shape[si];
+    if (shape < 0 || shape > 2) shape = 0;
+    if (shape == 0) {
+        real a = st_u(st), b = st_u(st), d = st_u(st);
+        p[0] = (real)c[0] + (real)c[3] * ((real)-1.0 + (real)2.0 * a) * (real)0.5;
+        p[1] = (real)c[1] + (real)c[4] * ((real)-1.0 + (real)2.0 * b) * (real)0.5;
+        p[2] = (real)c[2] + (real)c[5] * ((real)-1.0 + (real)2.0 * d) * (real)0.5;
+    } else if (shape == 1) {
+        real phi = st_u(st);
+        real r = (real)c[3] * R_SQRT(st_u(st));
+        real zz = st_u(st);
+        real s, cs;
+        r_sincos_turns(phi, &s, &cs);
+        p[0] = (real)c[0] + r * cs;
+        p[1] = (real)c[1] + r * s;
+        p[2] = (real)c[2] + (real)c[4] * ((real)-1.0 + (real)2.0 * zz) * (real)0.5;
+    } else {
+        real phi = st_u(st);
+        real cost = (real)-1.0 + (real)2.0 * st_u(st);
+        real r = (real)c[3] * R_CBRT(st_u(st));
+        real s, cs;
+        r_sincos_turns(phi, &s, &cs);
+        real st2 = R_SQRT((real)1.0 - cost * cost);
+        p[0] = (real)c[0] + r * st2 * cs;
+        p[1] = (real)c[1] + r * st2 * s;
+        p[2] = (real)c[2] + r * cost;
+    }
+}
+
+/* sampleEkPositron, gPET_kernals.cu:420-443: rejection on the fitted
+ * spectrum polynomial (evaluated by Horner); returns kinetic energy in eV */
+static real sample_ek(const or_scene* sc, int type, stream_t* st)
+{
+    const float* cf = sc->iso_coef + 8 * type;
+    real e = (real)0.0;
+    for (int it = 0; it < 100000; ++it) {
+        e = st_u(st) * ((real)cf[0] - (real)0.511) + (real)0.511;
+        real u = (real)cf[1] * st_u(st);
+        real sum = (real)cf[2];
+        for (int k = 3; k < 8; ++k) sum = sum * e + (real)cf[k];
+        if (!(u > sum)) break;
+    }
+    return (e - (real)0.511) * (real)1.0e6;
+}
+
+/* setPositronRange, gPET_kernals.cu:347-418: Gaussian displacement with
+ * sigma = Rex/2 (Rex from a water fit), walked through voxels so that the
+ * density-weighted length equals r. The density is read from the voxel being
+ * entered (as the reference does). A positron that reaches outside the phantom
+ * finishes its remaining range in air (0.0012905 g/cm^3); the reference adds a
+ * spurious 1000 cm there (:383,405). */
+static void positron_range(const or_scene* sc, real x[3], real ek, const real* dir, stream_t* st)
+{
+    real ekin = ek / (real)1.0e6;
+    real b1 = (real)5.44040782, b2 = (real)0.369516529;
+    real rex = (real)0.1 * b1 * ekin * ekin / (b2 + ekin);
+    real sigma = rex / (real)2.0;
+    real d[3];
+    d[0] = sigma * st_normal(st);
+    d[1] = sigma * st_normal(st);
+    d[2] = sigma * st_normal(st);
+    real r = R_SQRT(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    if (dir) {
+        real tmp = R_SQRT(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+        d[0] = r * dir[0] / tmp; d[1] = r * dir[1] / tmp; d[2] = r * dir[2] / tmp;
+    }
+    real idx = (real)1.0 / (real)sc->dx, idy = (real)1.0 / (real)sc->dy, idz = (real)1.0 / (real)sc->dz;
+    int vx = 0, vy = 0, vz = 0;
+    int inside = abs_vox(sc, (real)(1.0f / sc->dx), (real)(1.0f / sc->dy), (real)(1.0f / sc->dz),
+                         x[0], x[1], x[2], &vx, &vy, &vz);
+    (void)idx; (void)idy; (void)idz;
+    if (!inside) {
+        /* the reference keeps the truncated indices even when outside; they
+         * are only used while inside, so any value will do */
+        vx = vy = vz = 0;
+    }
+    real s = (real)0.0, step;
+    const real xmax = (real)sc->offx + (real)sc->nx * (real)sc->dx;
+    const real ymax = (real)sc->offy + (real)sc->ny * (real)sc->dy;
+    const real zmax = (real)sc->offz + (real)sc->nz * (real)sc->dz;
+    for (int guard = 0; s < r && guard < 100000; ++guard) {
+        step = (real)1000.0;
+        if (inside) {
+            int ax = 0;
+            real bb = ((real)sc->offx + (real)(vx + (d[0] > (real)0.0)) * (real)sc->dx - x[0]) / d[0];
+            if (step > bb) { step = bb; ax = 1; }
+            bb = ((real)sc->offy + (real)(vy + (d[1] > (real)0.0)) * (real)sc->dy - x[1]) / d[1];
+            if (step > bb) { step = bb; ax = 2; }
+            bb = ((real)sc->offz + (real)(vz + (d[2] > (real)0.0)) * (real)sc->dz - x[2]) / d[2];
+            if (step > bb) { step = bb; ax = 3; }
+            if (ax == 1) vx += d[0] > (real)0.0 ? 1 : -1;
+            else if (ax == 2) vy += d[1] > (real)0.0 ? 1 : -1;
+            else vz += d[2] > (real)0.0 ? 1 : -1;
+            real rho = (real)den_clamped(sc, vx, vy, vz);
+            step = step * r;
+            s += step * rho;
+            if (s > r) step += (r - s) / rho;
+        } else {
+            step = (r - s) / (real)0.0012905;
+            s = r + (real)100.0;
+        }
+        x[0] += step * d[0] / r;
+        x[1] += step * d[1] / r;
+        x[2] += step * d[2] / r;
+        if (x[0] < (real)sc->offx || x[0] > xmax) inside = 0;
+        if (x[1] < (real)sc->offy || x[1] > ymax) inside = 0;
+        if (x[2] < (real)sc->offz || x[2] > zmax) inside = 0;
+    }
+}
+
+/* ------------------------------------------------------ phantom transport */
+typedef struct {
+    real x[3], u[3], E;
+    double t;
+    int nscat;
+} photon_t;
+
+/* comsam(matid), gPET_kernals.cu:66-88: cos(theta) from the Compton surface */
+static inline void compton_surface(const or_scene* sc, real e, int m, stream_t* st, real* efrac, real* cost)
+{
+    real indcp = st_u(st) * (real)sc->idcp_c;
+    real inde = e * (real)sc->ide_c;
+    real c = lerp2(sc->cmpsf + (size_t)m * sc->ncp_c * sc->ne_c, sc->ncp_c, sc->ne_c, inde, indcp);
+    if (c > (real)1.0) c = (real)1.0;
+    if (c < (real)-1.0) c = (real)-1.0;
+    *cost = c;
+    *efrac = (real)1.0 / ((real)1.0 + e * C_IMC2 * ((real)1.0 - c));
+}
+
+/* rylsam, gPET_kernals.cu:128-146 */
+static inline real rayleigh_surface(const or_scene* sc, real e, int m, stream_t* st)
+{
+    real indcp = st_u(st) * (real)sc->idcp_r;
+    real inde = e * (real)sc->ide_r;
+    real c = lerp2(sc->rayff + (size_t)m * sc->ncp_r * sc->ne_r, sc->ncp_r, sc->ne_r, inde, indcp);
+    if (c > (real)1.0) c = (real)1.0;
+    if (c < (real)-1.0) c = (real)-1.0;
+    return c;
+}
+
+/* photon(), gPET_kernals.cu:256-345. Returns status: 0 photoelectric,
+ * 1 escaped the phantom (or dropped below eabsph after a Compton event and
+ * leaves as-is, :318-320), 3 step cap */
+static int phantom_transport(const or_scene* sc, const wck_t* wck, photon_t* p, stream_t* st)
+{
+    const real idx = (real)(1.0f / sc->dx), idy = (real)(1.0f / sc->dy), idz = (real)(1.0f / sc->dz);
+    for (int step = 0; step < MAX_STEPS; ++step) {
+        real lammin = wck_at(wck, p->E);
+        real s = -lammin * R_LOG(st_u(st));
+        p->x[0] += s * p->u[0];
+        p->x[1] += s * p->u[1];
+        p->x[2] += s * p->u[2];
+        p->t += (double)s / C_SPE;
+        int ix, iy, iz;
+        if (!abs_vox(sc, idx, idy, idz, p->x[0], p->x[1], p->x[2], &ix, &iy, &iz)) return 1;
+        size_t v = (size_t)ix + (size_t)sc->nx * ((size_t)iy + (size_t)sc->ny * iz);
+        real voxden = (real)sc->den[v];
+        int m = sc->mat[v];
+        real lamden = lammin * voxden;
+        real prob = (real)1.0 - lamden * xs_at(sc, sc->lamph, m, p->E);
+        real rn = st_u(st);
+        if (rn < prob) continue;
+        prob += lamden * xs_at(sc, sc->compt, m, p->E);
+        if (rn < prob) {
+            real efrac, cost;
+            compton_surface(sc, p->E, m, st, &efrac, &cost);
+            real phi = st_u(st);
+            p->E *= efrac;
+            p->nscat++;
+            if (p->E < (real)sc->eabsph) return 1;
+            rotate(&p->u[0], &p->u[1], &p->u[2], cost, phi);
+            continue;
+        }
+        prob += lamden * xs_at(sc, sc->rayle, m, p->E);
+        if (rn < prob) {
+            real cost = rayleigh_surface(sc, p->E, m, st);
+            real phi = st_u(st);
+            rotate(&p->u[0], &p->u[1], &p->u[2], cost, phi);
+            p->nscat++;
+            continue;
+        }
+        return 0;
+    }
+    return 3;
+}
+
+/* ------------------------------------------------------ detector transport */
+typedef struct {
+    real x[3], u[3], E;
+    double t;
+    int panel;          /* index into the panel array */
+} local_t;
+
+/* panel search of photonde, gPET_kernals.cu:963-1009: first panel (in order)
+ * whose plane the photon crosses within the panel face while moving along the
+ * panel's depth direction; the photon is moved onto that plane */
+static int enter_panel(const or_scene* sc, const photon_t* p, local_t* q)
+{
+    for (int i = 0; i < sc->npanels; ++i) {
+        const float* P = sc->panels + (size_t)i * OR_PANEL_STRIDE;
+        real px = p->x[0] - (real)P[15], py = p->x[1] - (real)P[16], pz = p->x[2] - (real)P[17];
+        real tx = px * (real)P[21] + py * (real)P[22] + pz * (real)P[23];
+        real ty = px * (real)P[24] + py * (real)P[25] + pz * (real)P[26];
+        real tz = px * (real)P[27] + py * (real)P[28] + pz * (real)P[29];
+        real tvx = p->u[0] * (real)P[21] + p->u[1] * (real)P[22] + p->u[2] * (real)P[23];
+        real tvy = p->u[0] * (real)P[24] + p->u[1] * (real)P[25] + p->u[2] * (real)P[26];
+        real tvz = p->u[0] * (real)P[27] + p->u[1] * (real)P[28] + p->u[2] * (real)P[29];
+        if (tvx * (real)P[18] >= (real)0.0) {
+            real ty2 = ty - tx / tvx * tvy;
+            real tz2 = tz - tx / tvx * tvz;
+            if (R_FABS(ty2) < (real)P[1] / (real)2.0 && R_FABS(tz2) < (real)P[2] / (real)2.0) {
+                q->x[0] = (real)0.0; q->x[1] = ty2; q->x[2] = tz2;
+                q->u[0] = tvx; q->u[1] = tvy; q->u[2] = tvz;
+                q->E = p->E;
+                q->t = p->t + (double)(-tx) / (C_SPE * (double)tvx);
+                q->panel = i;
+                return 1;
+            }
+        }
+    }
+    return 0;
+}
+
+/* crystalSearch, gPET_kernals.cu:1236-1279: m_id 0 crystal, 1 gap */
+static void crystal_search(const or_scene* sc, const float* P, const real x[3], int* m_id, int* M_id, int* L_id)
+{
+    real xx = x[0], y = x[1], z = x[2];
+    for (int k = 0; k < sc->nsurface; ++k) {
+        const float* a = sc->surface + 10 * k;
+        real v = (real)a[0] * xx * xx + (real)a[1] * y * y + (real)a[2] * z * z + (real)a[3] * xx * y +
+                 (real)a[4] * xx * z + (real)a[5] * y * z + (real)a[6] * xx + (real)a[7] * y + (real)a[8] * z +
+                 (real)a[9];
+        if (v < (real)0.0) { *m_id = 1; return; }
+    }
+    y = (real)P[1] / (real)2.0 + x[1];
+    z = (real)P[2] / (real)2.0 + x[2];
+    real pmy = (real)P[4] + (real)P[7], pmz = (real)P[5] + (real)P[8];
+    int my = R_FLOOR(y / pmy) > (real)0.0 ? (int)(y / pmy) : 0;
+    int mz = R_FLOOR(z / pmz) > (real)0.0 ? (int)(z / pmz) : 0;
+    *M_id = mz * sc->moduleNy + my;
+    y = y - (real)my * pmy;
+    z = z - (real)mz * pmz;
+    if (y > (real)P[4] || z > (real)P[5]) { *m_id = 1; return; }
+    real pcy = (real)P[10] + (real)P[13], pcz = (real)P[11] + (real)P[14];
+    int ly = R_FLOOR(y / pcy) > (real)0.0 ? (int)(y / pcy) : 0;
+    int lz = R_FLOOR(z / pcz) > (real)0.0 ? (int)(z / pcz) : 0;
+    *L_id = lz * sc->crystalNy + ly;
+    y = y - (real)ly * pcy;
+    z = z - (real)lz * pcz;
+    if (y > (real)P[10] || z > (real)P[11]) { *m_id = 1; return; }
+    *m_id = 0;
+}
+
+/* comsam (free electron Klein-Nishina), gPET_kernals.cu:90-126 */
+static void kn_sample(real e, stream_t* st, real* efrac, real* cost)
+{
+    real e0 = e * C_IMC2;
+    real twoe = (real)2.0 * e0;
+    real kmin2 = (real)1.0 / (((real)1.0 + twoe) * ((real)1.0 + twoe));
+    real loge = R_LOG((real)1.0 + twoe);
+    real ef = (real)1.0;
+    for (int it = 0; it < 100000; ++it) {
+        if (st_u(st) * (loge + twoe * ((real)1.0 + e0) * kmin2) < loge)
+            ef = R_EXP(-st_u(st) * loge);
+        else
+            ef = R_SQRT(kmin2 + st_u(st) * ((real)1.0 - kmin2));
+        real mess = e0 * e0 * ef * ((real)1.0 + ef * ef);
+        if (st_u(st) * mess <= mess - ((real)1.0 - ef) * (((real)1.0 + twoe) * ef - (real)1.0)) break;
+    }
+    *efrac = ef;
+    *cost = (real)1.0 - ((real)1.0 - ef) / (ef * e0);
+}
+
+/* adder, gPET_kernals.cu:737-755: same crystal -> energy-weighted centroid
+ * and summed energy, first time kept */
+static int adder(or_event* ev, int* n, const or_event* e)
+{
+    for (int i = 0; i < *n; ++i) {
+        if (e->siten == ev[i].siten) {
+            float s = ev[i].E + e->E;
+            ev[i].x = (ev[i].x * ev[i].E + e->x * e->E) / s;
+            ev[i].y = (ev[i].y * ev[i].E + e->y * e->E) / s;
+            ev[i].z = (ev[i].z * ev[i].E + e->z * e->E) / s;
+            ev[i].E = ev[i].E + e->E;
+            return 1;
+        }
+    }
+    if (*n >= MAX_PULSE) return 0;
+    ev[(*n)++] = *e;
+    return 1;
+}
+
+/* readout, gPET_kernals.cu:756-813. Depth 3 leaves the pulses as they are
+ * (the reference returns early there and then copies a stale count of 4). */
+static int readout(const or_scene* sc, or_event* ev, int n, or_event* out)
+{
+    int depth = sc->rdepth, policy = sc->rpolicy;
+    if (depth == 3) {
+        for (int i = 0; i < n; ++i) out[i] = ev[i];
+        return n;
+    }
+    if (policy == 1) depth = 2;
+    for (int i = 0; i < n; ++i) {
+        if (depth == 0) ev[i].siten = 0;
+        else if (depth == 1) ev[i].siten = ev[i].pann;
+        else if (depth == 2) ev[i].siten = ev[i].pann * sc->moduleN + ev[i].modn;
+    }
+    uint8_t dead[MAX_PULSE];
+    memset(dead, 0, sizeof(dead));
+    int k = 0;
+    for (int i = 0; i < n; ++i) {
+        if (dead[i]) continue;
+        or_event e0 = ev[i];
+        for (int j = i + 1; j < n; ++j) {
+            const or_event* e = &ev[j];
+            if (e->parn == e0.parn && e->siten == e0.siten) {
+                if (policy == 1) {
+                    float s = e0.E + e->E;
+                    e0.x = (e0.x * e0.E + e->x * e->E) / s;
+                    e0.y = (e0.y * e0.E + e->y * e->E) / s;
+                    e0.z = (e0.z * e0.E + e->z * e->E) / s;
+                    e0.E = e0.E + e->E;
+                } else {
+                    e0 = (e0.E > e->E) ? e0 : *e;
+                }
+                dead[j] = 1;
+            }
+        }
+        out[k++] = e0;
+    }
+    return k;
+}
+
+typedef struct {
+    or_event* ev; uint8_t* scat; uint8_t* slot; int64_t n, cap;
+    int32_t* hid; float* hf; int64_t nh, caph;
+    int64_t n_entered, n_pairs, n_overflow, n_stepcap;
+} tbuf_t;
+
+static void tb_push_pulse(tbuf_t* b, const or_event* e, uint8_t scat, uint8_t slot)
+{
+    if (b->n == b->cap) {
+        b->cap = b->cap ? 2 * b->cap : 1024;
+        b->ev = (or_event*)realloc(b->ev, sizeof(or_event) * b->cap);
+        b->scat = (uint8_t*)realloc(b->scat, b->cap);
+        b->slot = (uint8_t*)realloc(b->slot, b->cap);
+    }
+    b->ev[b->n] = *e; b->scat[b->n] = scat; b->slot[b->n] = slot; b->n++;
+}
+
+static void tb_push_hit(tbuf_t* b, const int32_t id[5], const float f[5])
+{
+    if (b->nh == b->caph) {
+        b->caph = b->caph ? 2 * b->caph : 1024;
+        b->hid = (int32_t*)realloc(b->hid, sizeof(int32_t) * 5 * b->caph);
+        b->hf = (float*)realloc(b->hf, sizeof(float) * 5 * b->caph);
+    }
+    memcpy(b->hid + 5 * b->nh, id, 20);
+    memcpy(b->hf + 5 * b->nh, f, 20);
+    b->nh++;
+}
+
+/* photonde per photon, gPET_kernals.cu:1011-1200 */
+static void detector_transport(const or_scene* sc, const wck_t* wck, local_t* q, int32_t parn, int32_t eventid,
+                               int scat, stream_t* st, tbuf_t* tb, int rec_hits)
+{
+    const float* P = sc->panels + (size_t)q->panel * OR_PANEL_STRIDE;
+    const int32_t pann = (int32_t)P[30];
+    or_event ev[MAX_PULSE];
+    int nev = 0, overflow = 0, nh = 0;
+    int step;
+    for (step = 0; step < MAX_STEPS; ++step) {
+        real lammin = wck_at(wck, q->E);
+        real s = -lammin * R_LOG(st_u(st));
+        q->x[0] += s * q->u[0];
+        q->x[1] += s * q->u[1];
+        q->x[2] += s * q->u[2];
+        q->t += (double)s / C_SPE;
+        if (R_FABS(q->x[1]) > (real)P[1] * (real)0.5 || R_FABS(q->x[2]) > (real)P[2] * (real)0.5 ||
+            q->x[0] * (real)P[18] < (real)0.0 || q->x[0] * (real)P[18] > (real)P[0])
+            break;
+        int m_id = -1, M_id = -1, L_id = -1;
+        crystal_search(sc, P, q->x, &m_id, &M_id, &L_id);
+        real den = (real)sc->det_den[m_id];
+        int mat = sc->det_mat[m_id];
+        real lamden = lammin * den;
+        real prob = (real)1.0 - lamden * xs_at(sc, sc->lamph, mat, q->E);
+        if (prob < (real)0.0) prob = (real)0.0;
+        real rn = st_u(st);
+        if (rn < prob) continue;
+        prob += lamden * xs_at(sc, sc->compt, mat, q->E);
+        int type = 0;
+        real dep = (real)0.0;
+        int stop = 0;
+        if (rn < prob) {
+            real efrac, cost;
+            kn_sample(q->E, st, &efrac, &cost);
+            real de = q->E * ((real)1.0 - efrac);
+            real phi = st_u(st);
+            if (m_id == 0) {
+                or_event e;
+                e.parn = parn; e.cryn = L_id; e.modn = M_id; e.pann = pann;
+                e.siten = pann * sc->moduleN * sc->crystalN + M_id * sc->crystalN + L_id;
+                e.eventid = eventid;
+                e.E = (float)de; e.t = q->t;
+                e.x = (float)q->x[0]; e.y = (float)q->x[1]; e.z = (float)q->x[2];
+                if (rec_hits) {
+                    int32_t hid[5] = {parn, pann, M_id, L_id, 1};
+                    float hf[5] = {(float)de, (float)q->t, (float)q->x[0], (float)q->x[1], (float)q->x[2]};
+                    if (nh < MAX_HITS) { tb_push_hit(tb, hid, hf); nh++; } else overflow = 1;
+                }
+                if (!adder(ev, &nev, &e)) overflow = 1;
+            }
+            q->E -= de;
+            if (q->E < (real)sc->eabsph) {
+                type = 2; dep = q->E; stop = 1;
+            } else {
+                rotate(&q->u[0], &q->u[1], &q->u[2], cost, phi);
+                continue;
+            }
+        } else {
+            prob += lamden * xs_at(sc, sc->rayle, mat, q->E);
+            if (rn < prob) {
+                real cost = rayleigh_surface(sc, q->E, mat, st);
+                real phi = st_u(st);
+                rotate(&q->u[0], &q->u[1], &q->u[2], cost, phi);
+                continue;
+            }
+            type = 4; dep = q->E; stop = 1;
+        }
+        if (stop) {
+            if (m_id == 0) {
+                or_event e;
+                e.parn = parn; e.cryn = L_id; e.modn = M_id; e.pann = pann;
+                e.siten = pann * sc->moduleN * sc->crystalN + M_id * sc->crystalN + L_id;
+                e.eventid = eventid;
+                e.E = (float)dep; e.t = q->t;
+                e.x = (float)q->x[0]; e.y = (float)q->x[1]; e.z = (float)q->x[2];
+                if (rec_hits) {
+                    int32_t hid[5] = {parn, pann, M_id, L_id, type};
+                    float hf[5] = {(float)dep, (float)q->t, (float)q->x[0], (float)q->x[1], (float)q->x[2]};
+                    if (nh < MAX_HITS) { tb_push_hit(tb, hid, hf); nh++; } else overflow = 1;
+                }
+                if (!adder(ev, &nev, &e)) overflow = 1;
+            }
+            break;
+        }
+    }
+    if (step == MAX_STEPS) tb->n_stepcap++;
+    if (overflow) tb->n_overflow++;
+    if (nev) {
+        or_event out[MAX_PULSE];
+        int k = readout(sc, ev, nev, out);
+        for (int i = 0; i < k; ++i) tb_push_pulse(tb, &out[i], (uint8_t)(scat != 0), (uint8_t)i);
+    }
+}
+
+/* --------------------------------------------------------- one decay */
+typedef struct {
+    wck_t wph, wdet;
+    double tau[64], cfac[64];       /* per source: 1/lambda (s), 1 - exp(-dt/tau) */
+} prep_t;
+
+static void make_pair(const or_scene* sc, stream_t* st, const real pos[3], photon_t ph[2], double t_us)
+{
+    /* setPosition, gPET_kernals.cu:536-555 */
+    real cost = (real)-1.0 + (real)2.0 * st_u(st);
+    real phi = st_u(st);
+    real s, c;
+    r_sincos_turns(phi, &s, &c);
+    real sint = R_SQRT((real)1.0 - cost * cost);
+    real u0 = sint * c, u1 = sint * s, u2 = cost;
+    real phi2 = st_u(st);
+    real theta = st_normal(st) * (real)sc->noncol_sigma;
+    for (int k = 0; k < 2; ++k) {
+        ph[k].x[0] = pos[0]; ph[k].x[1] = pos[1]; ph[k].x[2] = pos[2];
+        ph[k].t = t_us; ph[k].nscat = 0;
+    }
+    ph[0].u[0] = u0; ph[0].u[1] = u1; ph[0].u[2] = u2;
+    ph[0].E = C_MC2 + theta * C_MC2 / (real)2.0;
+    real ts, tc;
+    r_sincos_turns(theta * (real)0.159154943091895335768883763, &ts, &tc);  /* cos(theta) */
+    (void)ts;
+    rotate(&u0, &u1, &u2, -tc, phi2);
+    ph[1].u[0] = u0; ph[1].u[1] = u1; ph[1].u[2] = u2;
+    ph[1].E = C_MC2 - theta * C_MC2 / (real)2.0;
+}
+
+static void record_exit(or_exit* ex, const photon_t* p, int status, int panel)
+{
+    ex->x = (float)p->x[0]; ex->y = (float)p->x[1]; ex->z = (float)p->x[2];
+    ex->ux = (float)p->u[0]; ex->uy = (float)p->u[1]; ex->uz = (float)p->u[2];
+    ex->E = (float)p->E; ex->t = p->t; ex->nscat = p->nscat; ex->status = status; ex->panel = panel;
+}
+
+static void transport_pair(const or_scene* sc, const prep_t* pp, int64_t d, photon_t ph[2], int have,
+                           or_exit* exits, tbuf_t* tb, int flags)
+{
+    for (int k = 0; k < 2; ++k) {
+        if (!have) {
+            if (exits) { photon_t z; memset(&z, 0, sizeof(z)); record_exit(&exits[k], &z, 2, -1); }
+            continue;
+        }
+        stream_t st;
+        st_init(&st, sc, TAG_PHANTOM + k, (uint64_t)d);
+        int status = phantom_transport(sc, &pp->wph, &ph[k], &st);
+        int panel = -1;
+        local_t q;
+        if (status == 3) tb->n_stepcap++;
+        if (status == 1 && enter_panel(sc, &ph[k], &q)) {
+            panel = q.panel;
+            tb->n_entered++;
+            stream_t sd;
+            st_init(&sd, sc, TAG_DET + k, (uint64_t)d);
+            detector_transport(sc, &pp->wdet, &q, (int32_t)(2 * d + k), (int32_t)d, ph[k].nscat, &sd, tb,
+                               flags & 2);
+        }
+        if (exits) record_exit(&exits[k], &ph[k], status, panel);
+    }
+}
+
+static void simulate_decay(const or_scene* sc, const prep_t* pp, int64_t d, or_exit* exits, tbuf_t* tb, int flags)
+{
+    stream_t st;
+    st_init(&st, sc, TAG_DECAY, (uint64_t)d);
+    photon_t ph[2];
+    int have = 0;
+    if (sc->npsf > 0) {
+        /* setPositionForPhoton / photon PSF, gPET.cu:13-199, gPET_kernals.cu:563-604 */
+        const double* r = sc->psf + 8 * d;
+        if (sc->psf_ptype == 1) {
+            ph[0].x[0] = (real)(float)r[0]; ph[0].x[1] = (real)(float)r[1]; ph[0].x[2] = (real)(float)r[2];
+            ph[0].u[0] = (real)(float)r[4]; ph[0].u[1] = (real)(float)r[5]; ph[0].u[2] = (real)(float)r[6];
+            ph[0].E = (real)(float)r[7]; ph[0].t = r[3]; ph[0].nscat = 0;
+            /* one photon per record: photon slot 1 carries nothing */
+            stream_t s0;
+            st_init(&s0, sc, TAG_PHANTOM, (uint64_t)d);
+            int status = r[3] > 0.0 && ph[0].E >= (real)0.0 ? phantom_transport(sc, &pp->wph, &ph[0], &s0) : 2;
+            int panel = -1;
+            local_t q;
+            if (status == 3) tb->n_stepcap++;
+            if (status == 1 && enter_panel(sc, &ph[0], &q)) {
+                panel = q.panel;
+                tb->n_entered++;
+                stream_t sd;
+                st_init(&sd, sc, TAG_DET, (uint64_t)d);
+                detector_transport(sc, &pp->wdet, &q, (int32_t)(2 * d), (int32_t)d, ph[0].nscat, &sd, tb, flags & 2);
+            }
+            if (exits) {
+                if (status == 2) { photon_t z; memset(&z, 0, sizeof(z)); record_exit(&exits[0], &z, 2, -1); }
+                else record_exit(&exits[0], &ph[0], status, panel);
+                photon_t z; memset(&z, 0, sizeof(z)); record_exit(&exits[1], &z, 2, -1);
+            }
+            return;
+        }
+        real pos[3] = {(real)(float)r[0], (real)(float)r[1], (real)(float)r[2]};
+        real dir[3] = {(real)(float)r[4], (real)(float)r[5], (real)(float)r[6]};
+        if (sc->useprange) positron_range(sc, pos, (real)(float)r[7], dir, &st);
+        make_pair(sc, &st, pos, ph, r[3]);
+        have = 1;
+        tb->n_pairs++;
+        transport_pair(sc, pp, d, ph, have, exits, tb, flags);
+        return;
+    }
+    /* source mode: decay d belongs to the source whose index range holds it */
+    int si = 0;
+    while (si < sc->nsrc - 1 && d >= sc->src_first[si] + sc->src_count[si]) si++;
+    int type = sc->src_type[si];
+    /* truncated exponential decay time in [0, dt) (the per-atom test of
+     * setPosition, gPET_kernals.cu:519-521, conditioned on decaying) */
+    double ud = st_ud(&st);
+    double tdec = -pp->tau[si] * D_LOG(1.0 - ud * pp->cfac[si]);
+    double t_us = (sc->tstart_s + tdec) * 1e6;
+    real br = st_u(&st);
+    if (br < (real)sc->iso_ratio[type]) {
+        real pos[3];
+        shape_position(sc, si, &st, pos);
+        if (sc->useprange) {
+            real ek = sample_ek(sc, type, &st);
+            positron_range(sc, pos, ek, NULL, &st);
+        }
+        make_pair(sc, &st, pos, ph, t_us);
+        have = 1;
+        tb->n_pairs++;
+    }
+    transport_pair(sc, pp, d, ph, have, exits, tb, flags);
+}
+
+/* ------------------------------------------------------------- digitizer */
+typedef struct { or_event e; uint8_t scat, slot; int32_t site; } dpulse_t;
+
+/* total order used for the per-site dead-time pass: (site, t, parn, slot) */
+static int cmp_site_t(const void* a, const void* b)
+{
+    const dpulse_t* x = (const dpulse_t*)a;
+    const dpulse_t* y = (const dpulse_t*)b;
+    if (x->site != y->site) return x->site < y->site ? -1 : 1;
+    if (x->e.t != y->e.t) return x->e.t < y->e.t ? -1 : 1;
+    if (x->e.parn != y->e.parn) return x->e.parn < y->e.parn ? -1 : 1;
+    return (int)x->slot - (int)y->slot;
+}
+
+/* total order of the singles list: (t, parn, slot) */
+static int cmp_t(const void* a, const void* b)
+{
+    const dpulse_t* x = (const dpulse_t*)a;
+    const dpulse_t* y = (const dpulse_t*)b;
+    if (x->e.t != y->e.t) return x->e.t < y->e.t ? -1 : 1;
+    if (x->e.parn != y->e.parn) return x->e.parn < y->e.parn ? -1 : 1;
+    return (int)x->slot - (int)y->slot;
+}
+
+static int cmp_parn_slot(const void* a, const void* b)
+{
+    const dpulse_t* x = (const dpulse_t*)a;
+    const dpulse_t* y = (const dpulse_t*)b;
+    if (x->e.parn != y->e.parn) return x->e.parn < y->e.parn ? -1 : 1;
+    return (int)x->slot - (int)y->slot;
+}
+
+/* blur, gPET_kernals.cu:814-837, with the normal deviates drawn from the
+ * pulse's own Philox stream (key (parn, slot)) so the result does not depend
+ * on the order pulses are processed in */
+static void blur_pulse(const or_scene* sc, dpulse_t* p)
+{
+    stream_t st;
+    st_init(&st, sc, TAG_BLUR, ((uint64_t)(uint32_t)p->e.parn << 4) | p->slot);
+    float R = 0.0f;
+    if (sc->blurpolicy == 0) R = dm_sqrt(sc->Eref / p->e.E) * sc->Rref;
+    if (sc->blurpolicy == 1) R = sc->Rref + sc->Eslope * (p->e.E - sc->Eref) / 1.0e6f;
+    if (R < 0.0f) R = 0.0f;
+    float z = st_normal_f(&st);
+    p->e.E += z * R * p->e.E / 2.35482f;
+    if (sc->Sblur > 0.0f) {
+        p->e.x += sc->Sblur * st_normal_f(&st);
+        p->e.y += sc->Sblur * st_normal_f(&st);
+        p->e.z += sc->Sblur * st_normal_f(&st);
+    }
+}
+
+/* setSitenum, gPET_kernals.cu:607-640 (applied only when dlevel != 3,
+ * gPET.cu:402-407; at level 3 the site set by readout is kept) */
+static int32_t dead_site(const or_scene* sc, const or_event* e)
+{
+    switch (sc->dlevel) {
+    case 0: return 0;
+    case 1: return e->pann;
+    case 2: return e->pann * sc->moduleN + e->modn;
+    default: return e->siten;
+    }
+}
+
+static void digitize(const or_scene* sc, dpulse_t* p, int64_t n, or_result* out)
+{
+    /* 1. blur; 2. threshold [Eth, 2 MeV] (gPET.cu:388-396, energywindow
+     * gPET_kernals.cu:641-656: dropped if E < lo or E > hi) */
+    int64_t k = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        blur_pulse(sc, &p[i]);
+        if (p[i].e.E < sc->Eth || p[i].e.E > 2000000.0f) continue;
+        /* setSitenum overwrites the record's site (gPET_kernals.cu:607-640) */
+        p[i].site = dead_site(sc, &p[i].e);
+        p[i].e.siten = p[i].site;
+        p[k++] = p[i];
+    }
+    out->n_threshold = k;
+    /* 3. dead time per site in time order (orderevents detector.cu:369-385,
+     * deadtime gPET_kernals.cu:657-698) with the sequential semantics the
+     * reference kernel intends, in double precision: an event is lost if it
+     * comes less than tau after the last event (paralyzable, type 0) or after
+     * the last surviving event (non-paralyzable, type 1) of its site. */
+    qsort(p, (size_t)k, sizeof(dpulse_t), cmp_site_t);
+    const double tau = (double)sc->dtime_us;
+    int64_t m = 0;
+    double tdead = 0.0;
+    for (int64_t i = 0; i < k; ++i) {
+        int keep;
+        if (i == 0 || p[i].site != p[i - 1].site) {
+            keep = 1;
+            tdead = p[i].e.t;
+        } else if (p[i].e.t < tdead + tau) {
+            keep = 0;
+            if (sc->dtype == 0) tdead = p[i].e.t;
+        } else {
+            keep = 1;
+            tdead = p[i].e.t;
+        }
+        if (keep) p[m++] = p[i];
+    }
+    out->n_deadtime = m;
+    /* 4. energy window (gPET.cu:418-424) */
+    int64_t s = 0;
+    for (int64_t i = 0; i < m; ++i) {
+        if (p[i].e.E < sc->ewin_lo || p[i].e.E > sc->ewin_hi) continue;
+        p[s++] = p[i];
+    }
+    qsort(p, (size_t)s, sizeof(dpulse_t), cmp_t);
+    out->n_singles = s;
+    out->singles = (or_event*)malloc(sizeof(or_event) * (s ? s : 1));
+    out->single_scat = (uint8_t*)malloc(s ? s : 1);
+    out->single_slot = (uint8_t*)malloc(s ? s : 1);
+    for (int64_t i = 0; i < s; ++i) {
+        out->singles[i] = p[i].e;
+        out->single_scat[i] = p[i].scat;
+        out->single_slot[i] = p[i].slot;
+    }
+    /* 5. coincidence sorter (no counterpart in the reference): a single that
+     * is not inside an open window opens [t, t+W); policy 0 keeps a window
+     * holding exactly two singles in different panels, policy 1 keeps every
+     * pair in different panels. Same event id and no phantom scatter -> true,
+     * same event id otherwise -> scatter, different event ids -> random. */
+    int64_t cap = 16, nc = 0;
+    int64_t* cc = (int64_t*)malloc(sizeof(int64_t) * 2 * cap);
+    uint8_t* cl = (uint8_t*)malloc(cap);
+    int64_t nmult = 0;
+    const double W = sc->coinc_window_us;
+    for (int64_t i = 0; i < s;) {
+        int64_t j = i + 1;
+        while (j < s && out->singles[j].t < out->singles[i].t + W) j++;
+        int64_t cnt = j - i;
+        for (int64_t a = i; a < j; ++a) {
+            for (int64_t b = a + 1; b < j; ++b) {
+                if (sc->coinc_policy == 0 && cnt != 2) continue;
+                if (out->singles[a].pann == out->singles[b].pann) continue;
+                if (nc == cap) {
+                    cap *= 2;
+                    cc = (int64_t*)realloc(cc, sizeof(int64_t) * 2 * cap);
+                    cl = (uint8_t*)realloc(cl, cap);
+                }
+                cc[2 * nc] = a; cc[2 * nc + 1] = b;
+                uint8_t klass;
+                if (out->singles[a].eventid == out->singles[b].eventid)
+                    klass = (out->single_scat[a] || out->single_scat[b]) ? 1 : 0;
+                else
+                    klass = 2;
+                cl[nc] = klass;
+                if (klass == 0) out->n_true++;
+                else if (klass == 1) out->n_scatter++;
+                else out->n_random++;
+                nc++;
+            }
+        }
+        if (cnt > 2) nmult++;
+        i = j;
+    }
+    out->n_coinc = nc;
+    out->n_multiple = nmult;
+    out->coinc = cc;
+    out->coinc_class = cl;
+}
+
+static int prepare(const or_scene* sc, prep_t* pp)
+{
+    if (sc->nmat < 1 || sc->nmat > 10 || sc->ne < 2) return -1;
+    float maxden[10] = {0};
+    int64_t nv = (int64_t)sc->nx * sc->ny * sc->nz;
+    for (int64_t v = 0; v < nv; ++v) {
+        int m = sc->mat[v];
+        if (m < 0 || m >= sc->nmat) return -2;
+        if (sc->den[v] > maxden[m]) maxden[m] = sc->den[v];
+    }
+    build_wck(sc, maxden, &pp->wph);
+    float dmax[10] = {0};
+    for (int i = 0; i < 2; ++i)
+        if (sc->det_den[i] > dmax[sc->det_mat[i]]) dmax[sc->det_mat[i]] = sc->det_den[i];
+    build_wck(sc, dmax, &pp->wdet);
+    if (sc->nsrc > 64) return -3;
+    for (int i = 0; i < sc->nsrc; ++i) {
+        double th = (double)sc->iso_halftime[sc->src_type[i]];
+        double tau = th / 0.69314718055994530942;
+        pp->tau[i] = tau;
+        pp->cfac[i] = -expm1(-sc->dt_s / tau);
+    }
+    return 0;
+}
+
+int oracle_run(const or_scene* sc, int64_t d_begin, int64_t d_end, int nthreads, int flags, or_result* out)
+{
+    memset(out, 0, sizeof(*out));
+    prep_t* pp = (prep_t*)malloc(sizeof(prep_t));
+    int rc = prepare(sc, pp);
+    if (rc) { free(pp); return rc; }
+    int64_t nd = d_end - d_begin;
+    if (nd < 0) { free(pp); return -4; }
+    out->n_decays = nd;
+    if (flags & 1) out->exits = (or_exit*)calloc((size_t)(2 * nd + 1), sizeof(or_exit));
+#ifdef _OPENMP
+    if (nthreads < 1) nthreads = omp_get_max_threads();
+#else
+    nthreads = 1;
+#endif
+    tbuf_t* tb = (tbuf_t*)calloc((size_t)nthreads, sizeof(tbuf_t));
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nthreads)
+#endif
+    {
+#ifdef _OPENMP
+        int tid = omp_get_thread_num();
+#else
+        int tid = 0;
+#endif
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 256)
+#endif
+        for (int64_t d = d_begin; d < d_end; ++d)
+            simulate_decay(sc, pp, d, out->exits ? out->exits + 2 * (d - d_begin) : NULL, &tb[tid], flags);
+    }
+    int64_t np = 0, nh = 0;
+    for (int t = 0; t < nthreads; ++t) {
+        np += tb[t].n; nh += tb[t].nh;
+        out->n_entered += tb[t].n_entered; out->n_pairs += tb[t].n_pairs;
+        out->n_overflow += tb[t].n_overflow; out->n_stepcap += tb[t].n_stepcap;
+    }
+    dpulse_t* p = (dpulse_t*)malloc(sizeof(dpulse_t) * (np ? np : 1));
+    out->hit_id = (int32_t*)malloc(sizeof(int32_t) * 5 * (nh ? nh : 1));
+    out->hit_f = (float*)malloc(sizeof(float) * 5 * (nh ? nh : 1));
+    int64_t o = 0, oh = 0;
+    for (int t = 0; t < nthreads; ++t) {
+        for (int64_t i = 0; i < tb[t].n; ++i, ++o) {
+            p[o].e = tb[t].ev[i]; p[o].scat = tb[t].scat[i]; p[o].slot = tb[t].slot[i]; p[o].site = 0;
+        }
+        if (tb[t].nh) {
+            memcpy(out->hit_id + 5 * oh, tb[t].hid, sizeof(int32_t) * 5 * tb[t].nh);
+            memcpy(out->hit_f + 5 * oh, tb[t].hf, sizeof(float) * 5 * tb[t].nh);
+            oh += tb[t].nh;
+        }
+        free(tb[t].ev); free(tb[t].scat); free(tb[t].slot); free(tb[t].hid); free(tb[t].hf);
+    }
+    free(tb);
+    out->n_hits = nh;
+    qsort(p, (size_t)np, sizeof(dpulse_t), cmp_parn_slot);
+    out->n_pulses = np;
+    out->pulses = (or_event*)malloc(sizeof(or_event) * (np ? np : 1));
+    out->pulse_scat = (uint8_t*)malloc(np ? np : 1);
+    out->pulse_slot = (uint8_t*)malloc(np ? np : 1);
+    for (int64_t i = 0; i < np; ++i) {
+        out->pulses[i] = p[i].e; out->pulse_scat[i] = p[i].scat; out->pulse_slot[i] = p[i].slot;
+    }
+    digitize(sc, p, np, out);
+    free(p);
+    free(pp);
+    return 0;
+}
+
+int oracle_digitize(const or_scene* sc, const or_event* pulses, const uint8_t* scat, const uint8_t* slot,
+                    int64_t n, or_result* out)
+{
+    memset(out, 0, sizeof(*out));
+    dpulse_t* p = (dpulse_t*)malloc(sizeof(dpulse_t) * (n ? n : 1));
+    for (int64_t i = 0; i < n; ++i) {
+        p[i].e = pulses[i]; p[i].scat = scat[i]; p[i].slot = slot[i]; p[i].site = 0;
+    }
+    out->n_pulses = n;
+    digitize(sc, p, n, out);
+    free(p);
+    return 0;
+}
+
+void oracle_free_result(or_result* r)
+{
+    free(r->exits); free(r->pulses); free(r->pulse_scat); free(r->pulse_slot);
+    free(r->hit_id); free(r->hit_f); free(r->singles); free(r->single_scat); free(r->single_slot);
+    free(r->coinc); free(r->coinc_class);
+    memset(r, 0, sizeof(*r));
+}
+
+/* ------------------------------------------------ known-answer test hooks */
+static void hook_scene(or_scene* sc, uint64_t seed)
+{
+    memset(sc, 0, sizeof(*sc));
+    sc->seed = seed;
+}
+
+/* positron kinetic energies (eV) from sampleEkPositron for one isotope row */
+void oracle_sample_ek(const float* coef8, uint64_t seed, int64_t n, double* out)
+{
+    or_scene sc;
+    hook_scene(&sc, seed);
+    for (int64_t i = 0; i < n; ++i) {
+        stream_t st;
+        st_init(&st, &sc, TAG_DECAY, (uint64_t)i);
+        or_scene s2 = sc;
+        s2.iso_coef = coef8;
+        out[i] = (double)sample_ek(&s2, 0, &st);
+    }
+}
+
+/* Klein-Nishina (free electron) samples: cos(theta) and energy fraction */
+void oracle_kn_sample(double energy, uint64_t seed, int64_t n, double* cost, double* efrac)
+{
+    or_scene sc;
+    hook_scene(&sc, seed);
+    for (int64_t i = 0; i < n; ++i) {
+        stream_t st;
+        st_init(&st, &sc, TAG_DET, (uint64_t)i);
+        real ef, c;
+        kn_sample((real)energy, &st, &ef, &c);
+        cost[i] = (double)c;
+        efrac[i] = (double)ef;
+    }
+}
+
+/* annihilation pairs: angle between the two photons (rad) and their energies */
+void oracle_pair_angles(float sigma, uint64_t seed, int64_t n, double* angle, double* e0, double* e1)
+{
+    or_scene sc;
+    hook_scene(&sc, seed);
+    sc.noncol_sigma = sigma;
+    real pos[3] = {0, 0, 0};
+    for (int64_t i = 0; i < n; ++i) {
+        stream_t st;
+        st_init(&st, &sc, TAG_DECAY, (uint64_t)i);
+        photon_t ph[2];
+        make_pair(&sc, &st, pos, ph, 0.0);
+        double d = (double)ph[0].u[0] * ph[1].u[0] + (double)ph[0].u[1] * ph[1].u[1] + (double)ph[0].u[2] * ph[1].u[2];
+        double n0 = sqrt((double)ph[0].u[0] * ph[0].u[0] + (double)ph[0].u[1] * ph[0].u[1] + (double)ph[0].u[2] * ph[0].u[2]);
+        double n1 = sqrt((double)ph[1].u[0] * ph[1].u[0] + (double)ph[1].u[1] * ph[1].u[1] + (double)ph[1].u[2] * ph[1].u[2]);
+        d /= n0 * n1;
+        if (d > 1) d = 1;
+        if (d < -1) d = -1;
+        angle[i] = acos(d);
+        e0[i] = (double)ph[0].E;
+        e1[i] = (double)ph[1].E;
+    }
+}
+
+/* deterministic math of detmath.h, for accuracy tests:
+ * which 0 logf, 1 expf, 2 sin(2 pi x), 3 cos(2 pi x), 4 cbrtf */
+void oracle_detmath(int which, int64_t n, const float* x, float* y)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        float s, c;
+        switch (which) {
+        case 0: y[i] = dm_logf(x[i]); break;
+        case 1: y[i] = dm_expf(x[i]); break;
+        case 2: dm_sincos_turns(x[i], &s, &c); y[i] = s; break;
+        case 3: dm_sincos_turns(x[i], &s, &c); y[i] = c; break;
+        default: y[i] = dm_cbrtf(x[i]); break;
+        }
+    }
+}
+
+void oracle_detmath_log(int64_t n, const double* x, double* y)
+{
+    for (int64_t i = 0; i < n; ++i) y[i] = dm_log(x[i]);
+}

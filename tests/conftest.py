@@ -1,0 +1,83 @@
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+DATA = os.path.join(ROOT, "data")
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built libgpet.so")
+
+
+def _ensure_surfaces():
+    if not (os.path.exists(os.path.join(DATA, "input4gPET.cmpsf")) and
+            os.path.exists(os.path.join(DATA, "input4gPET.rayff"))):
+        import subprocess
+        subprocess.check_call([sys.executable, os.path.join(DATA, "make_surfaces.py"), DATA])
+
+
+@pytest.fixture(scope="session")
+def data_dir():
+    _ensure_surfaces()
+    return DATA
+
+
+@pytest.fixture(scope="session")
+def oracle_mod(data_dir):
+    import bridge
+    bridge.build()
+    return bridge
+
+
+@pytest.fixture(scope="session")
+def gpet_lib(data_dir):
+    """The native library, built for sm_103a; GPU tests fail loudly without it."""
+    from gpet_gb300 import build as B
+    B.build()
+    from gpet_gb300 import api
+    return api.load_library()
+
+
+@pytest.fixture(scope="session")
+def scene_small(tmp_path_factory, data_dir):
+    from gpet_gb300 import scenes
+    d = tmp_path_factory.mktemp("small")
+    return scenes.small(str(d), n_decays=20000, nvox=40)
+
+
+@pytest.fixture(scope="session")
+def scene_positron(tmp_path_factory, data_dir):
+    from gpet_gb300 import scenes
+    d = tmp_path_factory.mktemp("positron")
+    return scenes.positron(str(d), n_decays=20000, nvox=48)
+
+
+def make_ctx(scene, data_dir, **extra):
+    from gpet_gb300 import api
+    ctx = api.Context(0)
+    opts = dict(scene.options)
+    opts.update(extra)
+    opts["data_dir"] = data_dir
+    opts["base_dir"] = scene.directory
+    ctx.set_options(opts)
+    ctx.load_config(scene.config_path)
+    return ctx
+
+
+def oracle_for(scene, data_dir, panels=None, **extra):
+    import bridge
+    opts = dict(scene.options)
+    opts.update(extra)
+    return bridge.OracleScene(scene.config_path, opts, data_dir, panels=panels, base_dir=scene.directory)
+
+
+def event_key_sort(ev, slot):
+    order = np.lexsort((slot, ev["parn"]))
+    return ev[order], slot[order], order

@@ -1,0 +1,160 @@
+"""Pins of the CPU oracle against known answers: Random123's Philox vectors,
+the reference's own data files (tables at 511 keV, isotope spectra, the
+example detector), and the physics the samplers must reproduce."""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+KAT = json.load(open(os.path.join(GOLDEN, "kat.json")))
+
+
+def test_philox_random123_vectors(oracle_mod):
+    ph = oracle_mod.philox
+    assert ph([0, 0, 0, 0], [0, 0]) == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    assert ph([0xffffffff] * 4, [0xffffffff] * 2) == [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    assert ph([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0]) == \
+        [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+def _dm(oracle_mod, which, x):
+    L = oracle_mod.lib("fp32")
+    L.oracle_detmath.argtypes = [C.c_int, C.c_int64, C.c_void_p, C.c_void_p]
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.zeros_like(x)
+    L.oracle_detmath(which, len(x), x.ctypes.data, y.ctypes.data)
+    return y
+
+
+def test_detmath_accuracy(oracle_mod):
+    u = ((np.arange(1 << 20, dtype=np.float64) * 16 + 0.5) * 2.0 ** -24).astype(np.float32)
+    rel = lambda a, b: np.max(np.abs(a.astype(np.float64) - b) / np.maximum(np.abs(b), 1e-30))
+    assert rel(_dm(oracle_mod, 0, u), np.log(u.astype(np.float64))) < 4e-7
+    xs = np.linspace(-80, 80, 100001).astype(np.float32)
+    assert rel(_dm(oracle_mod, 1, xs), np.exp(xs.astype(np.float64))) < 2e-7
+    tw = 2 * np.pi * u.astype(np.float64)
+    assert np.max(np.abs(_dm(oracle_mod, 2, u) - np.sin(tw))) < 2e-7
+    assert np.max(np.abs(_dm(oracle_mod, 3, u) - np.cos(tw))) < 2e-7
+    assert rel(_dm(oracle_mod, 4, u), np.cbrt(u.astype(np.float64))) < 2e-7
+    L = oracle_mod.lib("fp32")
+    L.oracle_detmath_log.argtypes = [C.c_int64, C.c_void_p, C.c_void_p]
+    xd = np.random.default_rng(0).random(100000) + 1e-300
+    yd = np.zeros_like(xd)
+    L.oracle_detmath_log(len(xd), xd.ctypes.data, yd.ctypes.data)
+    assert np.max(np.abs(yd - np.log(xd)) / np.abs(np.log(xd))) < 1e-15
+
+
+def test_tables_511keV(data_dir):
+    from gpet_gb300 import formats as F
+    T = F.read_tables(data_dir)
+    for m, name in enumerate(T.names):
+        k = KAT["mu_rho_511keV"][name]
+        tot = np.interp(511e3, T.energy, T.lamph[m])
+        assert tot == pytest.approx(k["total"], rel=1e-6)
+        parts = sum(np.interp(511e3, T.energy, t[m]) for t in (T.compt, T.phote, T.rayle))
+        assert parts == pytest.approx(tot, rel=1e-4)
+    # pins quoted for the PET materials (cm^2/g)
+    expect = {"Water": 0.09596, "LYSO": 0.11476, "LSO": 0.11676, "CorticalBone": 0.09047, "DryAir": 0.08630}
+    for n, v in expect.items():
+        assert KAT["mu_rho_511keV"][n]["total"] == pytest.approx(v, abs=6e-6)
+
+
+def test_surfaces_shape_and_monotone(data_dir):
+    from gpet_gb300 import formats as F
+    T = F.read_tables(data_dir)
+    for s in (T.cmpsf, T.rayff):
+        assert s.shape == (10, 301, 151)
+        assert np.all(np.diff(s, axis=1) >= -1e-6)          # cos rises with probability
+        assert np.all(s[:, 0, :] == -1) and np.all(s[:, -1, :] == 1)
+    # Rayleigh at 511 keV is forward peaked; Compton in water has mean cos ~0.3-0.4
+    assert np.mean(T.rayff[1, :, 77]) > 0.9
+    assert 0.25 < np.mean(T.cmpsf[1, :, 77]) < 0.5
+
+
+def test_positron_spectrum_mean(oracle_mod, data_dir):
+    from gpet_gb300 import formats as F
+    iso = F.read_isotopes(os.path.join(data_dir, "isotopes.txt"))
+    L = oracle_mod.lib("fp64")
+    L.oracle_sample_ek.argtypes = [C.c_void_p, C.c_uint64, C.c_int64, C.c_void_p]
+    for row in range(len(iso.halftime)):
+        cf = np.ascontiguousarray(iso.coef[row], np.float32)
+        out = np.zeros(200000)
+        L.oracle_sample_ek(cf.ctypes.data, 7 + row, len(out), out.ctypes.data)
+        mean = out.mean() / 1e6
+        se = out.std() / 1e6 / np.sqrt(len(out))
+        assert abs(mean - KAT["positron_mean_kinetic_MeV"][row]) < 4 * se + 1e-4
+        assert out.min() >= 0 and out.max() <= (cf[0] - 0.511) * 1e6 + 1
+    # F-18: the fitted spectrum's mean kinetic energy (0.276 MeV; the tabulated
+    # F-18 mean is 0.25 MeV, the fit is what the reference samples)
+    assert KAT["positron_mean_kinetic_MeV"][0] == pytest.approx(0.2756, abs=2e-3)
+
+
+@pytest.mark.parametrize("energy", [511e3, 300e3, 100e3])
+def test_klein_nishina_chi2(oracle_mod, energy):
+    from scipy import stats
+    L = oracle_mod.lib("fp64")
+    L.oracle_kn_sample.argtypes = [C.c_double, C.c_uint64, C.c_int64, C.c_void_p, C.c_void_p]
+    n = 400000
+    cost = np.zeros(n)
+    ef = np.zeros(n)
+    L.oracle_kn_sample(energy, 11, n, cost.ctypes.data, ef.ctypes.data)
+    k = energy / 510999.1
+    edges = np.linspace(-1, 1, 41)
+    mu = np.linspace(-1, 1, 200001)
+    r = 1 / (1 + k * (1 - mu))
+    pdf = r * r * (r + 1 / r - (1 - mu * mu))
+    cdf = np.concatenate([[0], np.cumsum((pdf[1:] + pdf[:-1]) / 2 * np.diff(mu))])
+    cdf /= cdf[-1]
+    expct = np.diff(np.interp(edges, mu, cdf)) * n
+    obs, _ = np.histogram(cost, edges)
+    chi2 = np.sum((obs - expct) ** 2 / expct)
+    assert stats.chi2.sf(chi2, len(obs) - 1) > 1e-3
+    # Compton kinematics: efrac = 1/(1 + k(1-cos))
+    assert np.allclose(ef, 1 / (1 + k * (1 - cost)), rtol=1e-9, atol=1e-9)
+
+
+def test_noncollinearity_sigma(oracle_mod):
+    L = oracle_mod.lib("fp64")
+    L.oracle_pair_angles.argtypes = [C.c_float, C.c_uint64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+    n = 200000
+    ang, e0, e1 = np.zeros(n), np.zeros(n), np.zeros(n)
+    sigma = 0.0037056
+    L.oracle_pair_angles(sigma, 5, n, ang.ctypes.data, e0.ctypes.data, e1.ctypes.data)
+    dev = np.pi - ang                       # |theta|, theta ~ N(0, sigma)
+    assert np.sqrt(np.mean(dev ** 2)) == pytest.approx(sigma, rel=0.01)
+    # the reference's energy shift: E = MC2 +- theta*MC2/2 (sum is 2 MC2)
+    assert np.allclose(e0 + e1, 2 * 510999.1, rtol=1e-12)
+    assert np.std(e0) == pytest.approx(sigma * 510999.1 / 2, rel=0.02)
+
+
+def test_geometry_counts_config8():
+    from gpet_gb300 import formats as F
+    g = F.read_geo(os.path.join(GOLDEN, "reference_inputs", "config8.geo"))
+    assert g.counts == (9, 117, 8, 64)
+    assert g.counts == tuple(KAT["config8_counts"][k] for k in ("moduleNy", "moduleN", "crystalNy", "crystalN"))
+    assert np.allclose(g.panels[1], KAT["config8_panel1"], atol=1e-5)
+    # panel 1 is panel 0 turned by 45 degrees about z
+    assert np.allclose(g.panels[1][15:18], [15.909903, -15.909903, 0], atol=1e-4)
+
+
+def test_event_record_layout():
+    from gpet_gb300.formats import EVENT_DTYPE
+    assert EVENT_DTYPE.itemsize == KAT["event_record"]["size"]
+    assert EVENT_DTYPE.fields["t"][1] == KAT["event_record"]["t_offset"]
+    assert EVENT_DTYPE.fields["E"][1] == KAT["event_record"]["E_offset"]
+
+
+def test_example_config_parses():
+    from gpet_gb300 import formats as F
+    c = F.read_config(os.path.join(GOLDEN, "reference_inputs", "input_PET.in"))
+    k = KAT["config"]
+    assert list(c.pdim) == k["pdim"] == [200, 200, 200]
+    assert c.rdepth == 2 and c.rpolicy == 1
+    assert (c.dlevel, c.dtype) == (3, 0) and c.dtime == pytest.approx(2.2)
+    assert (c.ewin_lo, c.ewin_hi) == (30000.0, 700000.0)
+    assert c.surfaces == [[0, 0, 0, 0, 0, 0, 0, 0, 0, 1]]
+    assert c.geofile == "input/config8.geo" and c.sourcefile == "input/pointsource.txt"
