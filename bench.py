@@ -112,6 +112,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def combine_ranks(ms, coincidences, dist=None, device="cpu"):
+    """Whole-job numbers over ranks: the slowest rank's device time and the
+    sum of all ranks' coincidences (each rank simulates its own acquisition
+    with its own Philox key; there is no data exchange)."""
+    if dist is None:
+        return float(ms), float(coincidences)
+    import torch
+    mx = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    sm = torch.tensor([float(coincidences)], dtype=torch.float64, device=device)
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+    return float(mx.item()), float(sm.item())
+
+
 def make_scene(directory, n_decays):
     from gpet_gb300 import scenes
     return scenes.positron(directory, n_decays=n_decays)
@@ -226,14 +240,8 @@ def run_ours(args):
         barrier()
         wall = time.perf_counter() - t_wall0
         clocks = sampler.stop()
-        ms = tot["ms"]
-        if dist:
-            t = torch.tensor([ms, float(tot["coinc"])], dtype=torch.float64, device="cuda:%d" % local)
-            mx = t[:1].clone(); dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-            sm = t[1:].clone(); dist.all_reduce(sm, op=dist.ReduceOp.SUM)
-            ms_max, coinc_all = float(mx.item()), float(sm.item())
-        else:
-            ms_max, coinc_all = ms, float(tot["coinc"])
+        ms_max, coinc_all = combine_ranks(tot["ms"], tot["coinc"], dist,
+                                          "cpu" if args.gloo else "cuda:%d" % local)
         value = coinc_all / (ms_max * 1e-3)
         # e2e through the C ABI with host buffers
         mat, den = F.read_phantom(os.path.join(d, "phantom_mat.dat"), os.path.join(d, "phantom_den.dat"),

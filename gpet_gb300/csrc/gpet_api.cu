@@ -73,6 +73,10 @@ struct gpet_ctx {
     // device work buffers
     DevBuf q_f, q_t, q_i, cnt, qcount;
     int64_t q_cap = 0;
+    DevBuf pb_f, pb_t, pb_n;              // emitted pairs of one sub-chunk
+    int64_t pb_cap = 0;
+    int64_t sub_decays = 1ll << 20;       // pairs buffer stays in L2
+    std::vector<cudaEvent_t> tev;         // per-launch timing events
     DevBuf p_int, p_t, p_f, p_meta;       // pulses: 6 int32, 1 double, 4 float, 1 byte
     int64_t p_cap = 0;
     DevBuf h_id, h_f;
@@ -124,7 +128,7 @@ int gpet_create(int device, gpet_ctx** out)
     if (device < 0 || device >= n) return GPET_ERR_ARG;
     if (cudaSetDevice(device) != cudaSuccess) return GPET_ERR_CUDA;
     cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, k_source_phantom) != cudaSuccess) return GPET_ERR_NOGPU;
+    if (cudaFuncGetAttributes(&fa, k_phantom) != cudaSuccess) return GPET_ERR_NOGPU;
     auto* c = new gpet_ctx();
     c->device = device;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -142,6 +146,7 @@ void gpet_destroy(gpet_ctx* c)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+    for (auto& e : c->tev) cudaEventDestroy(e);
     cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -164,12 +169,14 @@ int gpet_set_option(gpet_ctx* c, const char* key, const char* value)
     else if (k == "record_hits") c->record_hits = (int)std::strtol(value, &end, 10);
     else if (k == "record_exits") c->record_exits = (int)std::strtol(value, &end, 10);
     else if (k == "chunk_decays") c->chunk_decays = std::strtoll(value, &end, 10);
+    else if (k == "sub_decays") c->sub_decays = std::strtoll(value, &end, 10);
     else if (k == "base_dir") { c->base_dir = v; return GPET_OK; }
     else if (k == "data_dir") { c->data_dir = v; return GPET_OK; }
     else return fail(c, GPET_ERR_ARG, "unknown option " + k);
     if (end == value || (end && *end)) return fail(c, GPET_ERR_ARG, "bad value for " + k + ": " + v);
     if (c->coinc_policy < 0 || c->coinc_policy > 1) return fail(c, GPET_ERR_ARG, "coinc_policy must be 0 or 1");
     if (c->chunk_decays < 1024) return fail(c, GPET_ERR_ARG, "chunk_decays must be >= 1024");
+    if (c->sub_decays < 1024) return fail(c, GPET_ERR_ARG, "sub_decays must be >= 1024");
     return GPET_OK;
 }
 
@@ -651,9 +658,28 @@ int gpet_run(gpet_ctx* c, gpet_run_stats* st)
     unsigned long long* qcount = c->cnt.as<unsigned long long>() + 31;
     unsigned long long* pcount = c->cnt.as<unsigned long long>() + 32;
     unsigned long long* hcount = c->cnt.as<unsigned long long>() + 33;
+    unsigned long long* work = c->cnt.as<unsigned long long>() + 40;   // one counter per sub-chunk launch
     int nsm = 0;
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
     const size_t smem = (size_t)c->geo.npanels * kPanelStride * 4;
+    const int64_t sub = std::min<int64_t>(c->sub_decays, chunk);
+    if (sub > c->pb_cap) {
+        CK(c->pb_f.ensure((size_t)sub * 11 * 4));
+        CK(c->pb_t.ensure((size_t)sub * 8));
+        CK(c->pb_n.ensure((size_t)sub));
+        c->pb_cap = sub;
+    }
+    PairBuf pb;
+    pb.f = c->pb_f.as<float>(); pb.t = c->pb_t.as<double>(); pb.nph = c->pb_n.as<uint8_t>(); pb.cap = c->pb_cap;
+    int phantom_blocks = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&phantom_blocks, k_phantom, 256, smem));
+    phantom_blocks = std::max(1, phantom_blocks) * nsm;
+    const int64_t nsub_per_chunk = (chunk + sub - 1) / sub;
+    while ((int64_t)c->tev.size() < 4 * nsub_per_chunk + 4) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        c->tev.push_back(e);
+    }
     float ms_sp = 0, ms_det = 0;
     cudaEventRecord(c->ev[0], c->stream);
     int64_t pulses_used = 0, hits_used = 0;
@@ -663,19 +689,29 @@ int gpet_run(gpet_ctx* c, gpet_run_stats* st)
         QueueDev q;
         q.f = c->q_f.as<float>(); q.t = c->q_t.as<double>(); q.i = c->q_i.as<int32_t>();
         q.count = qcount; q.cap = c->q_cap;
-        int64_t blocks = std::min<int64_t>((d1 - d0 + 255) / 256, (int64_t)nsm * 8);
-        cudaEventRecord(c->ev[1], c->stream);
-        k_source_phantom<<<(unsigned)std::max<int64_t>(blocks, 1), 256, smem, c->stream>>>(
-            c->d_sim.as<SimDesc>(), d0, d1, q, c->record_exits ? c->exits.as<ExitRec>() : nullptr, dcnt);
-        cudaEventRecord(c->ev[2], c->stream);
-        st->kernel_launches++;
+        int ne = 0;
+        for (int64_t s0 = d0; s0 < d1; s0 += sub) {
+            const int64_t n = std::min(d1, s0 + sub) - s0;
+            CK(cudaMemsetAsync(work, 0, 8, c->stream));
+            int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)nsm * 16);
+            cudaEventRecord(c->tev[ne++], c->stream);
+            k_source<<<(unsigned)std::max<int64_t>(blocks, 1), 256, smem, c->stream>>>(c->d_sim.as<SimDesc>(), s0, n,
+                                                                                      pb, dcnt);
+            k_phantom<<<(unsigned)phantom_blocks, 256, smem, c->stream>>>(
+                c->d_sim.as<SimDesc>(), s0, n, pb, work, q,
+                c->record_exits ? c->exits.as<ExitRec>() + 2 * (s0 - d0) : nullptr, dcnt);
+            cudaEventRecord(c->tev[ne++], c->stream);
+            st->kernel_launches += 2;
+        }
         unsigned long long hq = 0;
         CK(cudaMemcpyAsync(&hq, qcount, 8, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         CK(cudaGetLastError());
-        float ms = 0;
-        cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
-        ms_sp += ms;
+        for (int e = 0; e < ne; e += 2) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, c->tev[e], c->tev[e + 1]);
+            ms_sp += ms;
+        }
         if (c->record_exits)
             CK(cudaMemcpy(c->host_exits.data() + 2 * d0, c->exits.p, (size_t)2 * (d1 - d0) * sizeof(ExitRec),
                           cudaMemcpyDeviceToHost));
@@ -698,6 +734,7 @@ int gpet_run(gpet_ctx* c, gpet_run_stats* st)
         CK(cudaMemcpyAsync(hp, pcount, 16, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         CK(cudaGetLastError());
+        float ms = 0;
         cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
         ms_det += ms;
         pulses_used = (int64_t)std::min<unsigned long long>(hp[0], (unsigned long long)c->p_cap);

@@ -57,8 +57,17 @@ struct DigiParams {
     int32_t moduleN, crystalN;
 };
 
-__global__ void k_source_phantom(const SimDesc* __restrict__ gS, int64_t d_begin, int64_t d_end, QueueDev q,
-                                 ExitRec* exits, Counters* cnt);
+// emitted pairs of a sub-chunk of decays, structure of arrays
+struct PairBuf {
+    float* f;                     // [11][cap]: x, y, z, u0 (3), u1 (3), E0, E1
+    double* t;                    // [cap]
+    uint8_t* nph;                 // [cap]: photons emitted (0, 1 or 2)
+    int64_t cap;
+};
+
+__global__ void k_source(const SimDesc* __restrict__ gS, int64_t d0, int64_t n, PairBuf pb, Counters* cnt);
+__global__ void k_phantom(const SimDesc* __restrict__ gS, int64_t d0, int64_t nd, PairBuf pb,
+                          unsigned long long* work, QueueDev q, ExitRec* exits, Counters* cnt);
 __global__ void k_detector(const SimDesc* __restrict__ gS, QueueDev q, PulseDev P, HitDev H, int rec_hits,
                            Counters* cnt);
 

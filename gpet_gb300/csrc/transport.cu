@@ -2,11 +2,13 @@
 // transport kernels (the work of setPosition/setPositionForPhoton, photon and
 // photonde in gPET_kernals.cu:256-1233), for sm_103a.
 //
-// Layout: one thread per decay runs the source stage and both photons through
-// the phantom; photons that reach a panel are compacted (warp ballot, one
-// atomic per warp) into a structure-of-arrays detector queue. A second kernel
-// runs one thread per queued photon through the panel, applies the per-photon
-// adder and readout, and appends pulses and hits (one atomic per warp).
+// Layout: k_source runs one thread per decay and writes the emitted pairs to
+// an L2-resident structure-of-arrays buffer; k_phantom keeps persistent warps
+// whose lanes refill themselves with the next photon as soon as their photon
+// leaves the phantom, and compacts photons that reach a panel (warp ballot,
+// one atomic per warp) into the detector queue; k_detector runs one thread per
+// queued photon through the panel, applies the per-photon adder and readout,
+// and appends pulses and hits (one atomic per warp).
 #include "kernels.h"
 
 namespace gpet {
@@ -76,84 +78,199 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2])
     return 2;
 }
 
-__global__ void __launch_bounds__(256) k_source_phantom(const SimDesc* __restrict__ gS, int64_t d_begin,
-                                                        int64_t d_end, QueueDev q, ExitRec* exits,
-                                                        Counters* cnt)
+// source stage: one thread per decay, the emitted pair (or PSF photon) goes
+// to a structure-of-arrays buffer sized to stay in L2
+__global__ void __launch_bounds__(256) k_source(const SimDesc* __restrict__ gS, int64_t d0, int64_t n, PairBuf pb,
+                                                Counters* cnt)
 {
     __shared__ SimDesc S;
     extern __shared__ float sP[];
     load_sim(gS, S, sP);
+    unsigned long long n_pairs = 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+        Photon ph[2];
+        int nph = sample_decay(S, d0 + j, ph);
+        if (nph == 2) n_pairs++;
+        pb.nph[j] = (uint8_t)nph;
+        if (nph > 0) {
+            pb.f[0 * pb.cap + j] = ph[0].x[0];
+            pb.f[1 * pb.cap + j] = ph[0].x[1];
+            pb.f[2 * pb.cap + j] = ph[0].x[2];
+            pb.f[3 * pb.cap + j] = ph[0].u[0];
+            pb.f[4 * pb.cap + j] = ph[0].u[1];
+            pb.f[5 * pb.cap + j] = ph[0].u[2];
+            pb.f[9 * pb.cap + j] = ph[0].E;
+            pb.t[j] = ph[0].t;
+        }
+        if (nph > 1) {
+            pb.f[6 * pb.cap + j] = ph[1].u[0];
+            pb.f[7 * pb.cap + j] = ph[1].u[1];
+            pb.f[8 * pb.cap + j] = ph[1].u[2];
+            pb.f[10 * pb.cap + j] = ph[1].E;
+        }
+    }
+    n_pairs = warp_sum(n_pairs);
+    if ((threadIdx.x & 31) == 0 && n_pairs) atomicAdd(&cnt->pairs, n_pairs);
+}
+
+// phantom stage: persistent warps; a lane whose photon has left the phantom
+// (or was absorbed) takes the next photon from a shared counter at once, so
+// the lanes of a warp stay busy while histories differ in length. Photon p of
+// the stage is photon (p & 1) of decay d0 + (p >> 1).
+__global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ gS, int64_t d0, int64_t nd,
+                                                    PairBuf pb, unsigned long long* work, QueueDev q,
+                                                    ExitRec* exits, Counters* cnt)
+{
+    __shared__ SimDesc S;
+    extern __shared__ float sP[];
+    load_sim(gS, S, sP);
     const unsigned lt = lanemask_lt();
     const int lane = threadIdx.x & 31;
-    unsigned long long n_pairs = 0, n_entered = 0, n_steps = 0, n_cap = 0, n_drop = 0;
-    for (int64_t base = d_begin + (int64_t)blockIdx.x * blockDim.x; base < d_end; base += stride) {
-        const int64_t d = base + threadIdx.x;
-        const bool valid = d < d_end;
-        Photon ph[2];
-        int nph = 0;
-        if (valid) nph = sample_decay(S, d, ph);
-        if (nph == 2) n_pairs++;
-#pragma unroll 1
-        for (int k = 0; k < 2; ++k) {
-            Local L;
-            bool entered = false;
-            int status = 2;
-            if (valid && k < nph) {
-                Stream st;
-                st_init(st, S.key0, S.key1, kTagPhantom + k, (uint64_t)d);
-                int steps = 0;
-                status = phantom_transport(S, ph[k], st, steps);
-                n_steps += steps;
-                if (status == 3) n_cap++;
-                if (status == 1) entered = enter_panel(sP, S.npanels, ph[k], L);
-            }
-            const unsigned m = __ballot_sync(0xffffffffu, entered);
-            if (m) {
-                unsigned long long b = 0;
-                const int leader = __ffs(m) - 1;
-                if (lane == leader) b = atomicAdd(q.count, (unsigned long long)__popc(m));
-                b = __shfl_sync(0xffffffffu, b, leader);
-                if (entered) {
-                    const unsigned long long j = b + __popc(m & lt);
-                    if (j < (unsigned long long)q.cap) {
-                        q.f[0 * q.cap + j] = L.x[0];
-                        q.f[1 * q.cap + j] = L.x[1];
-                        q.f[2 * q.cap + j] = L.x[2];
-                        q.f[3 * q.cap + j] = L.u[0];
-                        q.f[4 * q.cap + j] = L.u[1];
-                        q.f[5 * q.cap + j] = L.u[2];
-                        q.f[6 * q.cap + j] = L.E;
-                        q.t[j] = L.t;
-                        q.i[0 * q.cap + j] = L.panel;
-                        q.i[1 * q.cap + j] = (int32_t)(2 * d + k);
-                        q.i[2 * q.cap + j] = (int32_t)d;
-                        q.i[3 * q.cap + j] = ph[k].nscat;
-                        n_entered++;
-                    } else {
-                        n_drop++;
+    const int64_t nphot = 2 * nd;
+    unsigned long long n_entered = 0, n_steps = 0, n_cap = 0, n_drop = 0;
+    bool active = false, exhausted = false;
+    int64_t p = 0;
+    int steps = 0;
+    Photon ph;
+    Stream st;
+    for (;;) {
+        // refill idle lanes, one atomic per warp
+        const bool need = !active && !exhausted;
+        const unsigned mneed = __ballot_sync(0xffffffffu, need);
+        if (mneed) {
+            unsigned long long b = 0;
+            const int leader = __ffs(mneed) - 1;
+            if (lane == leader) b = atomicAdd(work, (unsigned long long)__popc(mneed));
+            b = __shfl_sync(0xffffffffu, b, leader);
+            if (need) {
+                p = (int64_t)(b + __popc(mneed & lt));
+                if (p >= nphot) {
+                    exhausted = true;
+                } else {
+                    const int64_t j = p >> 1;
+                    const int k = (int)(p & 1);
+                    const int nph = pb.nph[j];
+                    if (k < nph) {
+                        ph.x[0] = pb.f[0 * pb.cap + j];
+                        ph.x[1] = pb.f[1 * pb.cap + j];
+                        ph.x[2] = pb.f[2 * pb.cap + j];
+                        ph.u[0] = pb.f[(3 + 3 * k) * pb.cap + j];
+                        ph.u[1] = pb.f[(4 + 3 * k) * pb.cap + j];
+                        ph.u[2] = pb.f[(5 + 3 * k) * pb.cap + j];
+                        ph.E = pb.f[(9 + k) * pb.cap + j];
+                        ph.t = pb.t[j];
+                        ph.nscat = 0;
+                        st_init(st, S.key0, S.key1, kTagPhantom + k, (uint64_t)(d0 + j));
+                        steps = 0;
+                        active = true;
+                    } else if (exits) {
+                        ExitRec e;
+                        e.x = e.y = e.z = e.ux = e.uy = e.uz = e.E = 0.0f; e.nscat = 0; e.t = 0.0;
+                        e.status = 2; e.panel = -1;
+                        exits[p] = e;
                     }
                 }
             }
-            if (exits && valid) {
-                ExitRec e;
-                if (k < nph) {
-                    e.x = ph[k].x[0]; e.y = ph[k].x[1]; e.z = ph[k].x[2];
-                    e.ux = ph[k].u[0]; e.uy = ph[k].u[1]; e.uz = ph[k].u[2];
-                    e.E = ph[k].E; e.nscat = ph[k].nscat; e.t = ph[k].t;
+        }
+        if (__all_sync(0xffffffffu, !active && exhausted)) break;
+        // one Woodcock step (photon(), gPET_kernals.cu:274-338)
+        int status = -1;   // -1 continue, 0 absorbed, 1 escaped, 3 step cap
+        if (active) {
+            n_steps++;
+            steps++;
+            float lammin = wck_at(S.wck_ph, S.wck_e0, S.wck_ide, ph.E);
+            float s = -lammin * dm_logf(st_u(st));
+            ph.x[0] += s * ph.u[0];
+            ph.x[1] += s * ph.u[1];
+            ph.x[2] += s * ph.u[2];
+            ph.t += (double)s / kSpe;
+            int ix, iy, iz;
+            if (!abs_vox(S, ph.x[0], ph.x[1], ph.x[2], ix, iy, iz)) {
+                status = 1;
+            } else {
+                uint2 vv = voxel(S, ix, iy, iz);
+                float voxden = __uint_as_float(vv.x);
+                int m = (int)vv.y;
+                float lamden = lammin * voxden;
+                float4 xs = xs_at(S, m, ph.E);
+                float prob = 1.0f - lamden * xs.x;
+                float rn = st_u(st);
+                if (rn < prob) {
                 } else {
-                    e.x = e.y = e.z = e.ux = e.uy = e.uz = e.E = 0.0f; e.nscat = 0; e.t = 0.0;
+                    prob += lamden * xs.y;
+                    if (rn < prob) {
+                        float efrac, cost;
+                        compton_surface(S, ph.E, m, st, efrac, cost);
+                        float phi = st_u(st);
+                        ph.E *= efrac;
+                        ph.nscat++;
+                        if (ph.E < S.eabsph) status = 1;
+                        else rotate(ph.u[0], ph.u[1], ph.u[2], cost, phi);
+                    } else {
+                        prob += lamden * xs.z;
+                        if (rn < prob) {
+                            float cost = rayleigh_surface(S, ph.E, m, st);
+                            float phi = st_u(st);
+                            rotate(ph.u[0], ph.u[1], ph.u[2], cost, phi);
+                            ph.nscat++;
+                        } else {
+                            status = 0;
+                        }
+                    }
                 }
-                e.status = status;
-                e.panel = entered ? L.panel : -1;
-                exits[2 * (d - d_begin) + k] = e;
+            }
+            if (status < 0 && steps >= kMaxSteps) status = 3;
+        }
+        // finished photons: panel entry, compaction into the detector queue
+        Local L;
+        const bool fin = status >= 0;
+        const bool entered = status == 1 && enter_panel(sP, S.npanels, ph, L);
+        const unsigned m = __ballot_sync(0xffffffffu, entered);
+        if (m) {
+            unsigned long long b = 0;
+            const int leader = __ffs(m) - 1;
+            if (lane == leader) b = atomicAdd(q.count, (unsigned long long)__popc(m));
+            b = __shfl_sync(0xffffffffu, b, leader);
+            if (entered) {
+                const unsigned long long jq = b + __popc(m & lt);
+                if (jq < (unsigned long long)q.cap) {
+                    const int64_t d = d0 + (p >> 1);
+                    q.f[0 * q.cap + jq] = L.x[0];
+                    q.f[1 * q.cap + jq] = L.x[1];
+                    q.f[2 * q.cap + jq] = L.x[2];
+                    q.f[3 * q.cap + jq] = L.u[0];
+                    q.f[4 * q.cap + jq] = L.u[1];
+                    q.f[5 * q.cap + jq] = L.u[2];
+                    q.f[6 * q.cap + jq] = L.E;
+                    q.t[jq] = L.t;
+                    q.i[0 * q.cap + jq] = L.panel;
+                    q.i[1 * q.cap + jq] = (int32_t)(2 * d + (p & 1));
+                    q.i[2 * q.cap + jq] = (int32_t)d;
+                    q.i[3 * q.cap + jq] = ph.nscat;
+                    n_entered++;
+                } else {
+                    n_drop++;
+                }
             }
         }
+        if (fin) {
+            if (status == 3) n_cap++;
+            if (exits) {
+                ExitRec e;
+                e.x = ph.x[0]; e.y = ph.x[1]; e.z = ph.x[2];
+                e.ux = ph.u[0]; e.uy = ph.u[1]; e.uz = ph.u[2];
+                e.E = ph.E; e.nscat = ph.nscat; e.t = ph.t;
+                e.status = status;
+                e.panel = entered ? L.panel : -1;
+                exits[p] = e;
+            }
+            active = false;
+        }
     }
-    n_pairs = warp_sum(n_pairs); n_entered = warp_sum(n_entered); n_steps = warp_sum(n_steps);
+    n_entered = warp_sum(n_entered); n_steps = warp_sum(n_steps);
     n_cap = warp_sum(n_cap); n_drop = warp_sum(n_drop);
     if (lane == 0) {
-        if (n_pairs) atomicAdd(&cnt->pairs, n_pairs);
         if (n_entered) atomicAdd(&cnt->entered, n_entered);
         if (n_steps) atomicAdd(&cnt->ph_steps, n_steps);
         if (n_cap) atomicAdd(&cnt->stepcap, n_cap);
