@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
                      "-I" + os.path.join(ROOT, "include")]
-LIB_SOURCES = ["transport.cu", "digitizer.cu", "gpet_api.cu", "loaders.cpp"]
+LIB_SOURCES = ["transport.cu", "digitizer.cu", "gpet_api.cu", "loaders.cpp", "digitize_static.cu"]
 
 
 def nvcc():

@@ -105,6 +105,35 @@ static_assert(sizeof(EventRec) == 48, "Event record is 48 bytes");
 int gather_events(const PulseDev& P, const uint32_t* idx, int64_t n, bool blurred, const DigiScratch& D,
                   EventRec* out, uint8_t* meta, cudaStream_t s);
 
+// digitizer kernels (digitizer.cu), for callers that orchestrate them with
+// their own working memory
+constexpr int kDigiTile = 4096;   // items per block of the radix and scan kernels
+__global__ void k_scan_reduce(const uint32_t* in, int64_t n, uint32_t* aux);
+__global__ void k_scan_aux(uint32_t* aux, int64_t nb, uint32_t* total);
+__global__ void k_scan_down(const uint32_t* in, int64_t n, const uint32_t* aux, uint32_t* out);
+__global__ void k_radix_hist(const uint64_t* keys, int64_t n, int shift, uint32_t* hist, int64_t nblocks);
+__global__ void k_radix_scatter(const uint64_t* kin, const uint32_t* vin, int64_t n, int shift, const uint32_t* off,
+                                int64_t nblocks, uint64_t* kout, uint32_t* vout);
+__global__ void k_blur_threshold(PulseDev P, int64_t n, DigiParams prm, float* Eb, float* xb, float* yb, float* zb,
+                                 int32_t* site, uint32_t* sel, unsigned long long* nsel);
+__global__ void k_time_keys(const uint32_t* sel, int64_t m, const double* t, uint64_t* key, uint32_t* val);
+__global__ void k_tie_fix(const uint64_t* key, uint32_t* idx, int64_t m, const int32_t* parn, const uint8_t* meta);
+__global__ void k_site_keys(const uint32_t* torder, int64_t m, const int32_t* site, uint64_t* key, uint32_t* val);
+__global__ void k_deadtime(const uint32_t* sorder, int64_t m, const int32_t* site, const double* t, double tau,
+                           int dtype, uint32_t* flags, unsigned long long* nalive);
+__global__ void k_window_pred(const uint32_t* torder, int64_t m, const uint32_t* flags, const float* Eb, float lo,
+                              float hi, uint32_t* pred);
+__global__ void k_compact(const uint32_t* torder, const uint32_t* pred, const uint32_t* off, int64_t m,
+                          uint32_t* out);
+__global__ void k_coinc_count(const uint32_t* sidx, int64_t s, const double* t, const int32_t* pann, double W,
+                              int policy, uint32_t* wcount, uint32_t* wend, unsigned long long* nmult);
+__global__ void k_coinc_write(const uint32_t* sidx, int64_t s, const uint32_t* wend, const uint32_t* off,
+                              const int32_t* pann, const int32_t* eid, const uint8_t* meta, int policy,
+                              int64_t* pairs, uint8_t* klass, int64_t cap, unsigned long long* ncls);
+__global__ void k_gather_events(PulseDev P, const uint32_t* idx, int64_t n, int blurred, const float* Eb,
+                                const float* xb, const float* yb, const float* zb, const int32_t* site,
+                                EventRec* out, uint8_t* meta);
+
 // Runs blur .. coincidences on n pulses already in P (device), stream-ordered;
 // returns 0 or a GPET_ERR code. Results land in D.single_idx / D.coinc_*,
 // counts in cnt. `launches` accumulates the kernel launch count.

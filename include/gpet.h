@@ -148,6 +148,57 @@ int gpet_get_majorant(gpet_ctx* ctx, int which, float* tab4096, float* e0, float
 /* tables as parsed: which 0 lamph 1 compt 2 phote 3 rayle 4 cmpsf 5 rayff */
 int gpet_get_table(gpet_ctx* ctx, int which, float* out, int64_t cap, int64_t* n);
 
+/* ------------------------------------------------------------ allocation-free digitizer */
+/* No counterpart in the reference. gpet_digitize_static runs the same
+ * digitizer and coincidence sorter as gpet_digitize, but for callers that
+ * cannot allocate device memory: code running inside another framework's
+ * memory pool or allocator, code whose device allocations are fixed at
+ * start-up (real-time acquisition front ends), or code that must not
+ * synchronise the device the way cudaMalloc/cudaFree do. It allocates
+ * nothing: its working memory is one file-scope device array of
+ * GPET_STATIC_ARENA_BYTES, which every GPU that loads the library holds until
+ * the process exits, and the caller passes inputs and outputs as device
+ * pointers it already owns.
+ *
+ * Limits and behaviour:
+ *  - n <= GPET_STATIC_MAX_PULSES; larger inputs are rejected (GPET_ERR_ARG,
+ *    message in err when err != NULL); more singles or pairs than the caller's
+ *    capacities -> GPET_ERR_CAPACITY, nothing written past them.
+ *  - The first call on a device looks up the array's device address (for the
+ *    current device); make that first call before any stream capture.
+ *  - All calls share the one array, which keeps the last call's contents:
+ *    calls whose work overlaps on the GPU (two host threads, or two streams of
+ *    one device) race and must be serialised by the caller.
+ *  - The call enqueues on `stream` (a cudaStream_t; NULL = legacy default) and
+ *    synchronises it before returning, because the counts size later steps.
+ *  - counts[8] (host) receives: after threshold, after dead time, singles,
+ *    coincidences, true, scatter, random, multiples.
+ * Inputs: d_pulses[n] (48-byte Event records), d_scat[n] (phantom-scatter
+ * flag), d_slot[n] (index within the photon's readout list, < 128).
+ * Outputs: d_singles[singles_cap] in time order, d_single_scat, d_pairs
+ * [pairs_cap][2] (indices into the singles) and d_class[pairs_cap]. */
+#define GPET_STATIC_MAX_PULSES 131072
+#define GPET_STATIC_ARENA_BYTES (16u * 1024u * 1024u)
+
+typedef struct {
+    int32_t blurpolicy;           /* energy blur, main.cu:171 */
+    float Eref, Rref, Eslope, Sblur;
+    float Eth;                    /* threshold before dead time, main.cu:166 */
+    int32_t dlevel, dtype;        /* dead time level and policy, main.cu:176 */
+    float dtime_us;
+    float ewin_lo, ewin_hi;       /* energy window, main.cu:181 */
+    double coinc_window_ns;
+    int32_t coinc_policy;
+    int32_t moduleN, crystalN;    /* site numbering of the detector */
+    uint64_t seed;
+    uint32_t sim_id;
+} gpet_digi_params;
+
+int gpet_digitize_static(const gpet_digi_params* prm, const gpet_event* d_pulses, const uint8_t* d_scat,
+                         const uint8_t* d_slot, int64_t n, gpet_event* d_singles, uint8_t* d_single_scat,
+                         int64_t singles_cap, int64_t* d_pairs, uint8_t* d_class, int64_t pairs_cap,
+                         int64_t counts[8], void* stream, char* err, int32_t err_len);
+
 #ifdef __cplusplus
 }
 #endif
