@@ -31,23 +31,24 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "detected coincidences/s on 1 GB300 (plain MC)"
+SUB_DECAYS = 1 << 20      # decays per k_source/k_phantom launch (library default)
 UNIT = "coincidences/s"
 WORKLOAD = ("positron: F-18 cylinder r=3 cm (positron range on), 128^3 x 0.5 mm water/bone/lung phantom, "
             "1e8 decays per step, 8-panel LYSO ring at 8 cm (8x8 crystals 3x3x20 mm), blur 12%, "
             "paralyzable dead time 0.3 us per block, window 350-650 keV, coincidence window 4 ns")
 
-# Algorithmic bytes of the source+phantom kernel, per decay (the model of the
-# gPET path's data movement: per photon 44 B source state written, 88 B phantom
-# state read+written, 5 B per Woodcock step for the voxel (u8 material + f32
-# density), 44 B per photon handed to the detector).
-def algorithmic_bytes_source_phantom(n_decays, ph_steps, entered):
-    return 2 * n_decays * (44 + 88) + 5 * ph_steps + 44 * entered
+# Algorithmic bytes of the phantom-transport kernel (the dominant one), from
+# the byte model of the gPET path: per photon 88 B of phantom state read and
+# written, 5 B per Woodcock step for the voxel it lands in (u8 material + f32
+# density), 44 B per photon handed to the detector queue.
+def algorithmic_bytes_phantom(n_photons, ph_steps, entered):
+    return 88 * n_photons + 5 * ph_steps + 44 * entered
 
 
-# DRAM bytes per decay of k_source_phantom measured by ncu (dram__bytes_read.sum
-# + dram__bytes_write.sum of one launch on a 2^22-decay case of this workload);
-# None until a capture exists.
-MEASURED_DRAM_BYTES_PER_DECAY = None
+# DRAM bytes per photon of k_phantom measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum of one 2^20-decay launch of this workload, 2,097,152
+# photons: 74.8 MB + 4.7 MB).
+MEASURED_DRAM_BYTES_PER_PHOTON = (74.765824e6 + 4.671744e6) / 2097152
 
 
 def _peaks():
@@ -224,19 +225,22 @@ def run_ours(args):
         barrier()
         sampler.start()
         t_wall0 = time.perf_counter()
-        tot = {"coinc": 0, "ms": 0.0, "ms_sp": 0.0, "ms_det": 0.0, "ms_dig": 0.0, "launches": 0, "ph_steps": 0,
-               "entered": 0, "decays": 0, "singles": 0, "true": 0, "scatter": 0, "random": 0, "chunks": 0}
+        tot = {"coinc": 0, "ms": 0.0, "ms_sp": 0.0, "ms_src": 0.0, "ms_ph": 0.0, "ms_det": 0.0, "ms_dig": 0.0, "launches": 0, "ph_steps": 0,
+               "entered": 0, "decays": 0, "singles": 0, "true": 0, "scatter": 0, "random": 0, "chunks": 0,
+               "pairs": 0}
         for k in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
             ctx.set_option("seed", 20261203 + k)
             st = ctx.run()
             tot["coinc"] += st["n_coinc"]; tot["ms"] += st["ms_total"]; tot["ms_sp"] += st["ms_source_phantom"]
+            tot["ms_src"] += st["ms_source"]; tot["ms_ph"] += st["ms_phantom"]
             tot["ms_det"] += st["ms_detector"]; tot["ms_dig"] += st["ms_digitizer"]
             tot["launches"] += st["kernel_launches"]; tot["ph_steps"] += st["phantom_steps"]
             tot["entered"] += st["n_entered"]; tot["decays"] += st["n_decays"]; tot["singles"] += st["n_singles"]
             tot["true"] += st["n_true"]; tot["scatter"] += st["n_scatter"]; tot["random"] += st["n_random"]
-            tot["chunks"] += -(-st["n_decays"] // (1 << 24))
+            tot["chunks"] += -(-st["n_decays"] // SUB_DECAYS)
+            tot["pairs"] += st["n_pairs"]
         barrier()
         wall = time.perf_counter() - t_wall0
         clocks = sampler.stop()
@@ -268,13 +272,12 @@ def run_ours(args):
             dist.destroy_process_group()
         return
     peak, peak_kind = _peaks()
-    n_launch_sp = max(1, tot["chunks"])
-    bytes_sp = algorithmic_bytes_source_phantom(tot["decays"], tot["ph_steps"], tot["entered"])
-    dur_sp = tot["ms_sp"] * 1e-3 / n_launch_sp
-    achieved = (bytes_sp / n_launch_sp) / dur_sp / 1e9
-    traffic = None
-    if MEASURED_DRAM_BYTES_PER_DECAY is not None:
-        traffic = MEASURED_DRAM_BYTES_PER_DECAY * tot["decays"] / n_launch_sp
+    n_launch = max(1, tot["chunks"])
+    photons = 2 * tot["pairs"]
+    bytes_ph = algorithmic_bytes_phantom(photons, tot["ph_steps"], tot["entered"])
+    dur_ph = tot["ms_ph"] * 1e-3 / n_launch
+    achieved = (bytes_ph / n_launch) / dur_ph / 1e9
+    traffic = MEASURED_DRAM_BYTES_PER_PHOTON * photons / n_launch
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -282,16 +285,19 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "decays_per_step": args.decays, "l2": "flushed between steps (512 MB write)",
                    "per_rank": "independent acquisitions (disjoint Philox keys)"},
         "gpu_launches": tot["launches"],
-        "breakdown_ms_per_step": {"source_phantom": tot["ms_sp"] / args.steps, "detector": tot["ms_det"] / args.steps,
+        "breakdown_ms_per_step": {"source": tot["ms_src"] / args.steps, "phantom": tot["ms_ph"] / args.steps,
+                                  "detector": tot["ms_det"] / args.steps,
                                   "digitizer_and_coincidences": tot["ms_dig"] / args.steps},
         "counts_per_step": {"decays": tot["decays"] / args.steps, "singles": tot["singles"] / args.steps,
                             "coincidences": tot["coinc"] / args.steps, "true": tot["true"] / args.steps,
                             "scatter": tot["scatter"] / args.steps, "random": tot["random"] / args.steps},
         "decays_per_s": tot["decays"] * world / (ms_max * 1e-3),
-        "roofline": {"kernel": "k_source_phantom", "bound": "hbm", "achieved": achieved, "peak": peak,
+        "roofline": {"kernel": "k_phantom", "bound": "hbm", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": bytes_sp / n_launch_sp,
-                     "launch_ms": dur_sp * 1e3},
+                     "algorithmic_bytes_per_launch": bytes_ph / n_launch, "launch_ms": dur_ph * 1e3,
+                     "launches": n_launch,
+                     "note": "issue/latency-bound (RNG, transcendental math, dependent L2 gathers); "
+                             "HBM per the path's byte model"},
         "e2e": {"value": e_coinc / e_wall, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
                 "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps},
         "clocks": clocks,

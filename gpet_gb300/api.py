@@ -34,7 +34,8 @@ class RunStats(C.Structure):
         "n_coinc", "n_true", "n_scatter", "n_random", "n_multiple", "n_overflow", "n_stepcap")] + [
         (n, C.c_double) for n in ("ms_total", "ms_source_phantom", "ms_detector", "ms_digitizer",
                                   "ms_coincidence")] + [
-        ("kernel_launches", C.c_int64), ("phantom_steps", C.c_int64), ("detector_steps", C.c_int64)]
+        ("kernel_launches", C.c_int64), ("phantom_steps", C.c_int64), ("detector_steps", C.c_int64),
+        ("ms_source", C.c_double), ("ms_phantom", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

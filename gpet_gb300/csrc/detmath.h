@@ -200,6 +200,29 @@ DM_FN double dm_log(double x)
     return dm_fmad((double)e, 0.69314718055994531, s * p);
 }
 
+/* log(1 + x) for |x| <= 2^-6 by its Taylor series (terms to x^12), no
+ * division: used for the decay-time sampling of long-lived isotopes */
+DM_FN double dm_log1p_small(double x)
+{
+    double p = -1.0 / 12.0;
+    p = dm_fmad(x, p, 1.0 / 11.0);
+    p = dm_fmad(x, p, -1.0 / 10.0);
+    p = dm_fmad(x, p, 1.0 / 9.0);
+    p = dm_fmad(x, p, -1.0 / 8.0);
+    p = dm_fmad(x, p, 1.0 / 7.0);
+    p = dm_fmad(x, p, -1.0 / 6.0);
+    p = dm_fmad(x, p, 1.0 / 5.0);
+    p = dm_fmad(x, p, -1.0 / 4.0);
+    p = dm_fmad(x, p, 1.0 / 3.0);
+    p = dm_fmad(x, p, -0.5);
+    p = dm_fmad(x, p, 1.0);
+    return x * p;
+}
+
+/* time per unit path, us/cm (1 / 29979.2458), for single-precision flight
+ * times that are added to a double-precision time stamp once */
+#define DM_INV_SPEED 3.3356409519815204e-05f
+
 /* uniform (0,1) float from 24 random bits: (k + 0.5) 2^-24, exact */
 DM_FN float dm_u01(uint32_t x)
 {

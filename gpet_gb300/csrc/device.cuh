@@ -349,9 +349,14 @@ inline __device__ void positron_range(const SimDesc& S, float x[3], float ek, co
 }
 
 // ---------------------------------------------------------------- photons
+// t is the emission time stamp (double, us); tf the flight time since then in
+// single precision, added to t once when the photon leaves the stage (FP64
+// arithmetic on GB300 is ~64x slower than FP32; one double add per photon
+// instead of a double division per step)
 struct Photon {
     float x[3], u[3], E;
     double t;
+    float tf;
     int nscat;
 };
 
@@ -370,7 +375,7 @@ __device__ __forceinline__ void make_pair(const SimDesc& S, Stream& st, const fl
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         ph[k].x[0] = pos[0]; ph[k].x[1] = pos[1]; ph[k].x[2] = pos[2];
-        ph[k].t = t_us; ph[k].nscat = 0;
+        ph[k].t = t_us; ph[k].tf = 0.0f; ph[k].nscat = 0;
     }
     ph[0].u[0] = u0; ph[0].u[1] = u1; ph[0].u[2] = u2;
     ph[0].E = kMC2 + theta * kMC2 / 2.0f;
@@ -436,7 +441,7 @@ __device__ __forceinline__ int phantom_transport(const SimDesc& S, Photon& p, St
         p.x[0] += s * p.u[0];
         p.x[1] += s * p.u[1];
         p.x[2] += s * p.u[2];
-        p.t += (double)s / kSpe;
+        p.tf += s * DM_INV_SPEED;
         int ix, iy, iz;
         if (!abs_vox(S, p.x[0], p.x[1], p.x[2], ix, iy, iz)) return 1;
         uint2 vv = voxel(S, ix, iy, iz);
@@ -471,10 +476,12 @@ __device__ __forceinline__ int phantom_transport(const SimDesc& S, Photon& p, St
     return 3;
 }
 
-// entry state in a panel's local frame
+// entry state in a panel's local frame: t the entry time stamp, tf the
+// flight time inside the panel since then
 struct Local {
     float x[3], u[3], E;
     double t;
+    float tf;
     int panel;
 };
 
@@ -484,21 +491,25 @@ __device__ __forceinline__ bool enter_panel(const float* __restrict__ P0, int np
 {
     for (int i = 0; i < npanels; ++i) {
         const float* P = P0 + i * kPanelStride;
+        // the direction test first: the other projections are only needed
+        // for a panel the photon moves toward (values are unchanged)
+        float tvx = p.u[0] * P[21] + p.u[1] * P[22] + p.u[2] * P[23];
+        if (!(tvx * P[18] >= 0.0f)) continue;
         float px = p.x[0] - P[15], py = p.x[1] - P[16], pz = p.x[2] - P[17];
         float tx = px * P[21] + py * P[22] + pz * P[23];
         float ty = px * P[24] + py * P[25] + pz * P[26];
         float tz = px * P[27] + py * P[28] + pz * P[29];
-        float tvx = p.u[0] * P[21] + p.u[1] * P[22] + p.u[2] * P[23];
         float tvy = p.u[0] * P[24] + p.u[1] * P[25] + p.u[2] * P[26];
         float tvz = p.u[0] * P[27] + p.u[1] * P[28] + p.u[2] * P[29];
-        if (tvx * P[18] >= 0.0f) {
+        {
             float ty2 = ty - tx / tvx * tvy;
             float tz2 = tz - tx / tvx * tvz;
             if (fabsf(ty2) < P[1] / 2.0f && fabsf(tz2) < P[2] / 2.0f) {
                 q.x[0] = 0.0f; q.x[1] = ty2; q.x[2] = tz2;
                 q.u[0] = tvx; q.u[1] = tvy; q.u[2] = tvz;
                 q.E = p.E;
-                q.t = p.t + (double)(-tx) / (kSpe * (double)tvx);
+                q.t = p.t + (double)(p.tf + -tx / tvx * DM_INV_SPEED);
+                q.tf = 0.0f;
                 q.panel = i;
                 return true;
             }

@@ -675,12 +675,12 @@ int gpet_run(gpet_ctx* c, gpet_run_stats* st)
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&phantom_blocks, k_phantom, 256, smem));
     phantom_blocks = std::max(1, phantom_blocks) * nsm;
     const int64_t nsub_per_chunk = (chunk + sub - 1) / sub;
-    while ((int64_t)c->tev.size() < 4 * nsub_per_chunk + 4) {
+    while ((int64_t)c->tev.size() < 3 * nsub_per_chunk + 4) {
         cudaEvent_t e;
         CK(cudaEventCreate(&e));
         c->tev.push_back(e);
     }
-    float ms_sp = 0, ms_det = 0;
+    float ms_sp = 0, ms_det = 0, ms_src = 0, ms_ph = 0;
     cudaEventRecord(c->ev[0], c->stream);
     int64_t pulses_used = 0, hits_used = 0;
     for (int64_t d0 = 0; d0 < nd; d0 += chunk) {
@@ -697,6 +697,7 @@ int gpet_run(gpet_ctx* c, gpet_run_stats* st)
             cudaEventRecord(c->tev[ne++], c->stream);
             k_source<<<(unsigned)std::max<int64_t>(blocks, 1), 256, smem, c->stream>>>(c->d_sim.as<SimDesc>(), s0, n,
                                                                                       pb, dcnt);
+            cudaEventRecord(c->tev[ne++], c->stream);
             k_phantom<<<(unsigned)phantom_blocks, 256, smem, c->stream>>>(
                 c->d_sim.as<SimDesc>(), s0, n, pb, work, q,
                 c->record_exits ? c->exits.as<ExitRec>() + 2 * (s0 - d0) : nullptr, dcnt);
@@ -707,10 +708,13 @@ int gpet_run(gpet_ctx* c, gpet_run_stats* st)
         CK(cudaMemcpyAsync(&hq, qcount, 8, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         CK(cudaGetLastError());
-        for (int e = 0; e < ne; e += 2) {
-            float ms = 0;
-            cudaEventElapsedTime(&ms, c->tev[e], c->tev[e + 1]);
-            ms_sp += ms;
+        for (int e = 0; e < ne; e += 3) {
+            float a = 0, b = 0;
+            cudaEventElapsedTime(&a, c->tev[e], c->tev[e + 1]);
+            cudaEventElapsedTime(&b, c->tev[e + 1], c->tev[e + 2]);
+            ms_src += a;
+            ms_ph += b;
+            ms_sp += a + b;
         }
         if (c->record_exits)
             CK(cudaMemcpy(c->host_exits.data() + 2 * d0, c->exits.p, (size_t)2 * (d1 - d0) * sizeof(ExitRec),
@@ -758,6 +762,8 @@ int gpet_run(gpet_ctx* c, gpet_run_stats* st)
     st->n_decays = nd;
     st->ms_total = ms_tot;
     st->ms_source_phantom = ms_sp;
+    st->ms_source = ms_src;
+    st->ms_phantom = ms_ph;
     st->ms_detector = ms_det;
     st->ms_digitizer = ms_digi;
     st->ms_coincidence = 0;

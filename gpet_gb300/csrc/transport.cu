@@ -52,7 +52,7 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2])
         if (S.psf_ptype == 1) {
             ph[0].x[0] = (float)r[0]; ph[0].x[1] = (float)r[1]; ph[0].x[2] = (float)r[2];
             ph[0].u[0] = (float)r[4]; ph[0].u[1] = (float)r[5]; ph[0].u[2] = (float)r[6];
-            ph[0].E = (float)r[7]; ph[0].t = r[3]; ph[0].nscat = 0;
+            ph[0].E = (float)r[7]; ph[0].t = r[3]; ph[0].tf = 0.0f; ph[0].nscat = 0;
             return (r[3] > 0.0 && ph[0].E >= 0.0f) ? 1 : 0;
         }
         float pos[3] = {(float)r[0], (float)r[1], (float)r[2]};
@@ -64,7 +64,9 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2])
     int si = 0;
     while (si < S.nsrc - 1 && d >= S.src_end[si]) si++;
     double ud = st_ud(st);
-    double tdec = -S.src_tau[si] * dm_log(1.0 - ud * S.src_cfac[si]);
+    const double cf = S.src_cfac[si];
+    const double xl = -ud * cf;
+    double tdec = -S.src_tau[si] * (cf <= 0.015625 ? dm_log1p_small(xl) : dm_log(1.0 + xl));
     double t_us = (S.tstart_s + tdec) * 1e6;
     float br = st_u(st);
     if (!(br < S.iso_ratio[si])) return 0;
@@ -114,21 +116,93 @@ __global__ void __launch_bounds__(256) k_source(const SimDesc* __restrict__ gS, 
     if ((threadIdx.x & 31) == 0 && n_pairs) atomicAdd(&cnt->pairs, n_pairs);
 }
 
+// a photon that has left the phantom (or stopped), waiting for the panel search
+struct FinRec {
+    float x, y, z, ux, uy, uz, E;
+    int32_t nscat;
+    double t;
+    long long p;
+    int32_t status;
+    float tf;
+};
+
+constexpr int kPhWarps = 8;      // warps per k_phantom block (256 threads)
+constexpr int kFinCap = 64;      // finished photons staged per warp
+
 // phantom stage: persistent warps; a lane whose photon has left the phantom
 // (or was absorbed) takes the next photon from a shared counter at once, so
-// the lanes of a warp stay busy while histories differ in length. Photon p of
-// the stage is photon (p & 1) of decay d0 + (p >> 1).
+// the lanes of a warp stay busy while histories differ in length. Finished
+// photons are staged in shared memory and taken through the panel search 32
+// at a time, one per lane. Photon p of the stage is photon (p & 1) of decay
+// d0 + (p >> 1).
 __global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ gS, int64_t d0, int64_t nd,
                                                     PairBuf pb, unsigned long long* work, QueueDev q,
                                                     ExitRec* exits, Counters* cnt)
 {
     __shared__ SimDesc S;
+    __shared__ FinRec fbuf[kPhWarps][kFinCap];
     extern __shared__ float sP[];
     load_sim(gS, S, sP);
     const unsigned lt = lanemask_lt();
     const int lane = threadIdx.x & 31;
+    FinRec* fb = fbuf[threadIdx.x >> 5];
     const int64_t nphot = 2 * nd;
     unsigned long long n_entered = 0, n_steps = 0, n_cap = 0, n_drop = 0;
+    int fcount = 0;   // staged photons of this warp (warp-uniform)
+
+    // panel search + queue append for the staged entries [0, k), one per lane
+    auto drain = [&](int k) {
+        const bool has = lane < k;
+        FinRec r;
+        if (has) r = fb[lane];
+        Photon ph;
+        Local L;
+        bool entered = false;
+        if (has) {
+            ph.x[0] = r.x; ph.x[1] = r.y; ph.x[2] = r.z;
+            ph.u[0] = r.ux; ph.u[1] = r.uy; ph.u[2] = r.uz;
+            ph.E = r.E; ph.t = r.t; ph.tf = r.tf; ph.nscat = r.nscat;
+            entered = r.status == 1 && enter_panel(sP, S.npanels, ph, L);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, entered);
+        if (m) {
+            unsigned long long b = 0;
+            const int leader = __ffs(m) - 1;
+            if (lane == leader) b = atomicAdd(q.count, (unsigned long long)__popc(m));
+            b = __shfl_sync(0xffffffffu, b, leader);
+            if (entered) {
+                const unsigned long long jq = b + __popc(m & lt);
+                if (jq < (unsigned long long)q.cap) {
+                    const int64_t d = d0 + (r.p >> 1);
+                    q.f[0 * q.cap + jq] = L.x[0];
+                    q.f[1 * q.cap + jq] = L.x[1];
+                    q.f[2 * q.cap + jq] = L.x[2];
+                    q.f[3 * q.cap + jq] = L.u[0];
+                    q.f[4 * q.cap + jq] = L.u[1];
+                    q.f[5 * q.cap + jq] = L.u[2];
+                    q.f[6 * q.cap + jq] = L.E;
+                    q.t[jq] = L.t;
+                    q.i[0 * q.cap + jq] = L.panel;
+                    q.i[1 * q.cap + jq] = (int32_t)(2 * d + (r.p & 1));
+                    q.i[2 * q.cap + jq] = (int32_t)d;
+                    q.i[3 * q.cap + jq] = r.nscat;
+                    n_entered++;
+                } else {
+                    n_drop++;
+                }
+            }
+        }
+        if (has && exits) {
+            ExitRec e;
+            e.x = r.x; e.y = r.y; e.z = r.z; e.ux = r.ux; e.uy = r.uy; e.uz = r.uz;
+            e.E = r.E; e.nscat = r.nscat; e.t = r.t + (double)r.tf;
+            e.status = r.status;
+            e.panel = entered ? L.panel : -1;
+            exits[r.p] = e;
+        }
+        __syncwarp();
+    };
+
     bool active = false, exhausted = false;
     int64_t p = 0;
     int steps = 0;
@@ -160,6 +234,7 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ 
                         ph.u[2] = pb.f[(5 + 3 * k) * pb.cap + j];
                         ph.E = pb.f[(9 + k) * pb.cap + j];
                         ph.t = pb.t[j];
+                        ph.tf = 0.0f;
                         ph.nscat = 0;
                         st_init(st, S.key0, S.key1, kTagPhantom + k, (uint64_t)(d0 + j));
                         steps = 0;
@@ -184,7 +259,7 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ 
             ph.x[0] += s * ph.u[0];
             ph.x[1] += s * ph.u[1];
             ph.x[2] += s * ph.u[2];
-            ph.t += (double)s / kSpe;
+            ph.tf += s * DM_INV_SPEED;
             int ix, iy, iz;
             if (!abs_vox(S, ph.x[0], ph.x[1], ph.x[2], ix, iy, iz)) {
                 status = 1;
@@ -222,52 +297,34 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ 
             }
             if (status < 0 && steps >= kMaxSteps) status = 3;
         }
-        // finished photons: panel entry, compaction into the detector queue
-        Local L;
+        // stage finished photons; run the panel search once 32 are waiting
         const bool fin = status >= 0;
-        const bool entered = status == 1 && enter_panel(sP, S.npanels, ph, L);
-        const unsigned m = __ballot_sync(0xffffffffu, entered);
-        if (m) {
-            unsigned long long b = 0;
-            const int leader = __ffs(m) - 1;
-            if (lane == leader) b = atomicAdd(q.count, (unsigned long long)__popc(m));
-            b = __shfl_sync(0xffffffffu, b, leader);
-            if (entered) {
-                const unsigned long long jq = b + __popc(m & lt);
-                if (jq < (unsigned long long)q.cap) {
-                    const int64_t d = d0 + (p >> 1);
-                    q.f[0 * q.cap + jq] = L.x[0];
-                    q.f[1 * q.cap + jq] = L.x[1];
-                    q.f[2 * q.cap + jq] = L.x[2];
-                    q.f[3 * q.cap + jq] = L.u[0];
-                    q.f[4 * q.cap + jq] = L.u[1];
-                    q.f[5 * q.cap + jq] = L.u[2];
-                    q.f[6 * q.cap + jq] = L.E;
-                    q.t[jq] = L.t;
-                    q.i[0 * q.cap + jq] = L.panel;
-                    q.i[1 * q.cap + jq] = (int32_t)(2 * d + (p & 1));
-                    q.i[2 * q.cap + jq] = (int32_t)d;
-                    q.i[3 * q.cap + jq] = ph.nscat;
-                    n_entered++;
-                } else {
-                    n_drop++;
-                }
+        const unsigned mf = __ballot_sync(0xffffffffu, fin);
+        if (mf) {
+            if (fin) {
+                FinRec r;
+                r.x = ph.x[0]; r.y = ph.x[1]; r.z = ph.x[2];
+                r.ux = ph.u[0]; r.uy = ph.u[1]; r.uz = ph.u[2];
+                r.E = ph.E; r.nscat = ph.nscat; r.t = ph.t; r.p = p; r.status = status; r.tf = ph.tf;
+                fb[fcount + __popc(mf & lt)] = r;
+                if (status == 3) n_cap++;
+                active = false;
             }
-        }
-        if (fin) {
-            if (status == 3) n_cap++;
-            if (exits) {
-                ExitRec e;
-                e.x = ph.x[0]; e.y = ph.x[1]; e.z = ph.x[2];
-                e.ux = ph.u[0]; e.uy = ph.u[1]; e.uz = ph.u[2];
-                e.E = ph.E; e.nscat = ph.nscat; e.t = ph.t;
-                e.status = status;
-                e.panel = entered ? L.panel : -1;
-                exits[p] = e;
+            fcount += __popc(mf);
+            __syncwarp();
+            if (fcount >= 32) {
+                drain(32);
+                const int rest = fcount - 32;
+                FinRec r;
+                if (lane < rest) r = fb[32 + lane];
+                __syncwarp();
+                if (lane < rest) fb[lane] = r;
+                __syncwarp();
+                fcount = rest;
             }
-            active = false;
         }
     }
+    if (fcount > 0) drain(fcount);
     n_entered = warp_sum(n_entered); n_steps = warp_sum(n_steps);
     n_cap = warp_sum(n_cap); n_drop = warp_sum(n_drop);
     if (lane == 0) {
@@ -367,6 +424,7 @@ __global__ void __launch_bounds__(256) k_detector(const SimDesc* __restrict__ gS
             L.u[0] = q.f[3 * q.cap + j]; L.u[1] = q.f[4 * q.cap + j]; L.u[2] = q.f[5 * q.cap + j];
             L.E = q.f[6 * q.cap + j];
             L.t = q.t[j];
+            L.tf = 0.0f;
             L.panel = q.i[0 * q.cap + j];
             parn = q.i[1 * q.cap + j];
             eid = q.i[2 * q.cap + j];
@@ -384,7 +442,7 @@ __global__ void __launch_bounds__(256) k_detector(const SimDesc* __restrict__ gS
                 L.x[0] += s * L.u[0];
                 L.x[1] += s * L.u[1];
                 L.x[2] += s * L.u[2];
-                L.t += (double)s / kSpe;
+                L.tf += s * DM_INV_SPEED;
                 if (fabsf(L.x[1]) > Pn[1] * 0.5f || fabsf(L.x[2]) > Pn[2] * 0.5f || L.x[0] * Pn[18] < 0.0f ||
                     L.x[0] * Pn[18] > Pn[0])
                     break;
@@ -410,11 +468,11 @@ __global__ void __launch_bounds__(256) k_detector(const SimDesc* __restrict__ gS
                         PEvent e;
                         e.pann = pann; e.modn = M_id; e.cryn = L_id;
                         e.siten = pann * S.moduleN * S.crystalN + M_id * S.crystalN + L_id;
-                        e.E = de; e.t = L.t; e.x = L.x[0]; e.y = L.x[1]; e.z = L.x[2];
+                        e.E = de; e.t = L.t + (double)L.tf; e.x = L.x[0]; e.y = L.x[1]; e.z = L.x[2];
                         if (rec_hits) {
                             if (nh < kMaxHits) {
                                 hid[nh][0] = pann; hid[nh][1] = M_id; hid[nh][2] = L_id; hid[nh][3] = 1;
-                                hf[nh][0] = de; hf[nh][1] = (float)L.t; hf[nh][2] = L.x[0]; hf[nh][3] = L.x[1];
+                                hf[nh][0] = de; hf[nh][1] = (float)e.t; hf[nh][2] = L.x[0]; hf[nh][3] = L.x[1];
                                 hf[nh][4] = L.x[2];
                                 nh++;
                             } else {
@@ -444,11 +502,11 @@ __global__ void __launch_bounds__(256) k_detector(const SimDesc* __restrict__ gS
                     PEvent e;
                     e.pann = pann; e.modn = M_id; e.cryn = L_id;
                     e.siten = pann * S.moduleN * S.crystalN + M_id * S.crystalN + L_id;
-                    e.E = dep; e.t = L.t; e.x = L.x[0]; e.y = L.x[1]; e.z = L.x[2];
+                    e.E = dep; e.t = L.t + (double)L.tf; e.x = L.x[0]; e.y = L.x[1]; e.z = L.x[2];
                     if (rec_hits) {
                         if (nh < kMaxHits) {
                             hid[nh][0] = pann; hid[nh][1] = M_id; hid[nh][2] = L_id; hid[nh][3] = type;
-                            hf[nh][0] = dep; hf[nh][1] = (float)L.t; hf[nh][2] = L.x[0]; hf[nh][3] = L.x[1];
+                            hf[nh][0] = dep; hf[nh][1] = (float)e.t; hf[nh][2] = L.x[0]; hf[nh][3] = L.x[1];
                             hf[nh][4] = L.x[2];
                             nh++;
                         } else {

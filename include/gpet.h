@@ -64,6 +64,8 @@ typedef struct {
     int64_t kernel_launches;     /* kernels launched by this run */
     int64_t phantom_steps;       /* Woodcock steps in the phantom (all photons) */
     int64_t detector_steps;      /* Woodcock steps in the panels */
+    double ms_source;            /* source stage alone (part of ms_source_phantom) */
+    double ms_phantom;           /* phantom stage alone (part of ms_source_phantom) */
 } gpet_run_stats;
 
 /* ------------------------------------------------------------ lifetime */

@@ -23,7 +23,6 @@ typedef float real;
 #define R_CBRT(x) dm_cbrtf(x)
 #define R_FLOOR(x) floorf(x)
 #define R_FABS(x) fabsf(x)
-#define D_LOG(x) dm_log(x)
 static inline void r_sincos_turns(real u, real* s, real* c) { dm_sincos_turns(u, s, c); }
 #else
 typedef double real;
@@ -33,7 +32,6 @@ typedef double real;
 #define R_CBRT(x) cbrt(x)
 #define R_FLOOR(x) floor(x)
 #define R_FABS(x) fabs(x)
-#define D_LOG(x) log(x)
 static inline void r_sincos_turns(real u, real* s, real* c)
 {
     double a = 6.283185307179586476925 * u;
@@ -45,6 +43,15 @@ static inline void r_sincos_turns(real u, real* s, real* c)
 #define C_MC2 ((real)510999.1)          /* constants.h:37 MC2 (eV) */
 #define C_IMC2 ((real)1.95695060911e-6) /* constants.h:38 */
 #define C_SPE 29979.2458                /* cm/us, gPET_kernals.cu:264 */
+/* Flight times: the FP32 build (like the kernels) accumulates a photon's
+ * flight time in single precision and adds it to its double-precision time
+ * stamp once; the FP64 build accumulates in double at every step, as the
+ * reference does (gPET_kernals.cu:283, 1025). */
+#ifdef ORACLE_FP32
+#define TIME_STEP(p, s) ((p)->tf += (s) * DM_INV_SPEED)
+#else
+#define TIME_STEP(p, s) ((p)->t += (double)(s) / C_SPE)
+#endif
 #define MAX_STEPS 100000
 #define MAX_PULSE 8   /* distinct crystals per photon in the adder list */
 #define MAX_HITS 16   /* deposits recorded per photon */
@@ -376,6 +383,7 @@ static void positron_range(const or_scene* sc, real x[3], real ek, const real* d
 typedef struct {
     real x[3], u[3], E;
     double t;
+    real tf;
     int nscat;
 } photon_t;
 
@@ -414,7 +422,7 @@ static int phantom_transport(const or_scene* sc, const wck_t* wck, photon_t* p, 
         p->x[0] += s * p->u[0];
         p->x[1] += s * p->u[1];
         p->x[2] += s * p->u[2];
-        p->t += (double)s / C_SPE;
+        TIME_STEP(p, s);
         int ix, iy, iz;
         if (!abs_vox(sc, idx, idy, idz, p->x[0], p->x[1], p->x[2], &ix, &iy, &iz)) return 1;
         size_t v = (size_t)ix + (size_t)sc->nx * ((size_t)iy + (size_t)sc->ny * iz);
@@ -452,6 +460,7 @@ static int phantom_transport(const or_scene* sc, const wck_t* wck, photon_t* p, 
 typedef struct {
     real x[3], u[3], E;
     double t;
+    real tf;
     int panel;          /* index into the panel array */
 } local_t;
 
@@ -476,7 +485,12 @@ static int enter_panel(const or_scene* sc, const photon_t* p, local_t* q)
                 q->x[0] = (real)0.0; q->x[1] = ty2; q->x[2] = tz2;
                 q->u[0] = tvx; q->u[1] = tvy; q->u[2] = tvz;
                 q->E = p->E;
+#ifdef ORACLE_FP32
+                q->t = p->t + (double)(p->tf + -tx / tvx * DM_INV_SPEED);
+#else
                 q->t = p->t + (double)(-tx) / (C_SPE * (double)tvx);
+#endif
+                q->tf = (real)0.0;
                 q->panel = i;
                 return 1;
             }
@@ -639,7 +653,7 @@ static void detector_transport(const or_scene* sc, const wck_t* wck, local_t* q,
         q->x[0] += s * q->u[0];
         q->x[1] += s * q->u[1];
         q->x[2] += s * q->u[2];
-        q->t += (double)s / C_SPE;
+        TIME_STEP(q, s);
         if (R_FABS(q->x[1]) > (real)P[1] * (real)0.5 || R_FABS(q->x[2]) > (real)P[2] * (real)0.5 ||
             q->x[0] * (real)P[18] < (real)0.0 || q->x[0] * (real)P[18] > (real)P[0])
             break;
@@ -666,11 +680,11 @@ static void detector_transport(const or_scene* sc, const wck_t* wck, local_t* q,
                 e.parn = parn; e.cryn = L_id; e.modn = M_id; e.pann = pann;
                 e.siten = pann * sc->moduleN * sc->crystalN + M_id * sc->crystalN + L_id;
                 e.eventid = eventid;
-                e.E = (float)de; e.t = q->t;
+                e.E = (float)de; e.t = q->t + (double)q->tf;
                 e.x = (float)q->x[0]; e.y = (float)q->x[1]; e.z = (float)q->x[2];
                 if (rec_hits) {
                     int32_t hid[5] = {parn, pann, M_id, L_id, 1};
-                    float hf[5] = {(float)de, (float)q->t, (float)q->x[0], (float)q->x[1], (float)q->x[2]};
+                    float hf[5] = {(float)de, (float)e.t, (float)q->x[0], (float)q->x[1], (float)q->x[2]};
                     if (nh < MAX_HITS) { tb_push_hit(tb, hid, hf); nh++; } else overflow = 1;
                 }
                 if (!adder(ev, &nev, &e)) overflow = 1;
@@ -698,11 +712,11 @@ static void detector_transport(const or_scene* sc, const wck_t* wck, local_t* q,
                 e.parn = parn; e.cryn = L_id; e.modn = M_id; e.pann = pann;
                 e.siten = pann * sc->moduleN * sc->crystalN + M_id * sc->crystalN + L_id;
                 e.eventid = eventid;
-                e.E = (float)dep; e.t = q->t;
+                e.E = (float)dep; e.t = q->t + (double)q->tf;
                 e.x = (float)q->x[0]; e.y = (float)q->x[1]; e.z = (float)q->x[2];
                 if (rec_hits) {
                     int32_t hid[5] = {parn, pann, M_id, L_id, type};
-                    float hf[5] = {(float)dep, (float)q->t, (float)q->x[0], (float)q->x[1], (float)q->x[2]};
+                    float hf[5] = {(float)dep, (float)e.t, (float)q->x[0], (float)q->x[1], (float)q->x[2]};
                     if (nh < MAX_HITS) { tb_push_hit(tb, hid, hf); nh++; } else overflow = 1;
                 }
                 if (!adder(ev, &nev, &e)) overflow = 1;
@@ -738,7 +752,7 @@ static void make_pair(const or_scene* sc, stream_t* st, const real pos[3], photo
     real theta = st_normal(st) * (real)sc->noncol_sigma;
     for (int k = 0; k < 2; ++k) {
         ph[k].x[0] = pos[0]; ph[k].x[1] = pos[1]; ph[k].x[2] = pos[2];
-        ph[k].t = t_us; ph[k].nscat = 0;
+        ph[k].t = t_us; ph[k].tf = (real)0.0; ph[k].nscat = 0;
     }
     ph[0].u[0] = u0; ph[0].u[1] = u1; ph[0].u[2] = u2;
     ph[0].E = C_MC2 + theta * C_MC2 / (real)2.0;
@@ -754,7 +768,7 @@ static void record_exit(or_exit* ex, const photon_t* p, int status, int panel)
 {
     ex->x = (float)p->x[0]; ex->y = (float)p->x[1]; ex->z = (float)p->x[2];
     ex->ux = (float)p->u[0]; ex->uy = (float)p->u[1]; ex->uz = (float)p->u[2];
-    ex->E = (float)p->E; ex->t = p->t; ex->nscat = p->nscat; ex->status = status; ex->panel = panel;
+    ex->E = (float)p->E; ex->t = p->t + (double)p->tf; ex->nscat = p->nscat; ex->status = status; ex->panel = panel;
 }
 
 static void transport_pair(const or_scene* sc, const prep_t* pp, int64_t d, photon_t ph[2], int have,
@@ -795,7 +809,7 @@ static void simulate_decay(const or_scene* sc, const prep_t* pp, int64_t d, or_e
         if (sc->psf_ptype == 1) {
             ph[0].x[0] = (real)(float)r[0]; ph[0].x[1] = (real)(float)r[1]; ph[0].x[2] = (real)(float)r[2];
             ph[0].u[0] = (real)(float)r[4]; ph[0].u[1] = (real)(float)r[5]; ph[0].u[2] = (real)(float)r[6];
-            ph[0].E = (real)(float)r[7]; ph[0].t = r[3]; ph[0].nscat = 0;
+            ph[0].E = (real)(float)r[7]; ph[0].t = r[3]; ph[0].tf = (real)0.0; ph[0].nscat = 0;
             /* one photon per record: photon slot 1 carries nothing */
             stream_t s0;
             st_init(&s0, sc, TAG_PHANTOM, (uint64_t)d);
@@ -833,7 +847,12 @@ static void simulate_decay(const or_scene* sc, const prep_t* pp, int64_t d, or_e
     /* truncated exponential decay time in [0, dt) (the per-atom test of
      * setPosition, gPET_kernals.cu:519-521, conditioned on decaying) */
     double ud = st_ud(&st);
-    double tdec = -pp->tau[si] * D_LOG(1.0 - ud * pp->cfac[si]);
+    const double xl = -ud * pp->cfac[si];
+#ifdef ORACLE_FP32
+    double tdec = -pp->tau[si] * (pp->cfac[si] <= 0.015625 ? dm_log1p_small(xl) : dm_log(1.0 + xl));
+#else
+    double tdec = -pp->tau[si] * log1p(xl);
+#endif
     double t_us = (sc->tstart_s + tdec) * 1e6;
     real br = st_u(&st);
     if (br < (real)sc->iso_ratio[type]) {
