@@ -67,6 +67,7 @@ def load_library(path=None):
     L.gpet_set_source_file.argtypes = [vp, C.c_char_p, C.c_float, C.c_float]
     L.gpet_set_source_psf.argtypes = [vp, vp, i64, C.c_int]
     L.gpet_run.argtypes = [vp, C.POINTER(RunStats)]
+    L.gpet_run_batched.argtypes = [C.POINTER(vp), i32, C.POINTER(RunStats)]
     L.gpet_digitize.argtypes = [vp, vp, vp, vp, i64, C.POINTER(RunStats)]
     L.gpet_get_singles.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
     L.gpet_get_pulses.argtypes = [vp, vp, vp, vp, i64, C.POINTER(i64)]
@@ -254,3 +255,19 @@ class Context:
         out = np.zeros(n.value, np.float32)
         self._ck(self.L.gpet_get_table(self.h, which, _ptr(out), n.value, C.byref(n)))
         return out
+
+
+def run_batched(contexts):
+    """Run several loaded contexts (one device) as one job (gpet_run_batched);
+    returns each simulation's stats. Each context then reads its own results."""
+    ctxs = list(contexts)
+    if not ctxs:
+        return []
+    L = ctxs[0].L
+    arr = (C.c_void_p * len(ctxs))(*[c.h for c in ctxs])
+    st = (RunStats * len(ctxs))()
+    rc = L.gpet_run_batched(arr, len(ctxs), st)
+    if rc != GPET_OK:
+        msgs = "; ".join(sorted({c.L.gpet_last_error(c.h).decode(errors="replace") for c in ctxs} - {""}))
+        raise GpetError(rc, msgs)
+    return [s.as_dict() for s in st]

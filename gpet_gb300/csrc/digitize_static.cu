@@ -160,9 +160,11 @@ extern "C" int gpet_digitize_static(const gpet_digi_params* prm, const gpet_even
     D.scan_aux = cv.take<uint32_t>((256 * (size_t)nb + kDigiTile - 1) / kDigiTile + (size_t)nb + 16);
     uint8_t* meta_out = cv.take<uint8_t>(N);
     D.dcount = cv.take<unsigned long long>(16);
+    DigiParams* d_prm = cv.take<DigiParams>(1);
+    Counters* d_cnt = cv.take<Counters>(1);
     if (!I || !P.t || !F || !P.meta || !D.idx_a || !D.idx_b || !D.key_a || !D.key_b || !D.torder || !D.flags ||
         !D.site || !D.sel || !B || !D.single_idx || !D.wcount || !D.wend || !D.hist || !D.scan_aux || !meta_out ||
-        !D.dcount)
+        !D.dcount || !d_prm || !d_cnt)
         return set_err(err, err_len, GPET_ERR_CAPACITY, "static arena too small for this input");
     P.parn = I; P.pann = I + N; P.modn = I + 2 * N; P.cryn = I + 3 * N; P.siten = I + 4 * N; P.eventid = I + 5 * N;
     P.E = F; P.x = F + N; P.y = F + 2 * N; P.z = F + 3 * N;
@@ -180,10 +182,12 @@ extern "C" int gpet_digitize_static(const gpet_digi_params* prm, const gpet_even
 
     // the arena keeps the last call's contents: clear the counters
     cudaMemsetAsync(D.dcount, 0, 16 * sizeof(unsigned long long), s);
+    cudaMemsetAsync(d_cnt, 0, sizeof(Counters), s);
+    cudaMemcpyAsync(d_prm, &dp, sizeof(DigiParams), cudaMemcpyHostToDevice, s);
     unsigned long long hc[8] = {0};
     if (n > 0) {
         k_events_to_soa<<<grid256(n), 256, 0, s>>>(reinterpret_cast<const EventRec*>(d_pulses), d_scat, d_slot, n, P);
-        k_blur_threshold<<<grid256(n), 256, 0, s>>>(P, n, dp, D.Eb, D.xb, D.yb, D.zb, D.site, D.sel, D.dcount + 0);
+        k_blur_threshold<<<grid256(n), 256, 0, s>>>(P, n, d_prm, D.Eb, D.xb, D.yb, D.zb, D.site, D.sel, D.dcount + 0);
     }
     cudaMemcpyAsync(hc, D.dcount, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
     if ((ce = cudaStreamSynchronize(s)) != cudaSuccess) return set_err(err, err_len, GPET_ERR_CUDA, cudaGetErrorString(ce));
@@ -199,30 +203,28 @@ extern "C" int gpet_digitize_static(const gpet_digi_params* prm, const gpet_even
         int site_bits = 8;
         const int64_t maxsite = (int64_t)prm->moduleN * prm->crystalN * kMaxPanels;
         while (site_bits < 32 && (1ll << site_bits) <= maxsite) site_bits += 8;
-        k_site_keys<<<grid256(m), 256, 0, s>>>(D.torder, m, D.site, ka, va);
+        k_site_keys<<<grid256(m), 256, 0, s>>>(D.torder, m, D.site, nullptr, ka, va);
         sort(ka, va, kb, vb, m, site_bits, D.hist, D.scan_aux, total, s);
-        k_deadtime<<<grid256(m), 256, 0, s>>>(va, m, D.site, P.t, dp.tau, dp.dtype, D.flags, D.dcount + 1);
-        k_window_pred<<<grid256(m), 256, 0, s>>>(D.torder, m, D.flags, D.Eb, dp.ewin_lo, dp.ewin_hi, D.sel);
+        k_deadtime<<<grid256(m), 256, 0, s>>>(va, m, D.site, nullptr, P.t, d_prm, D.flags, d_cnt);
+        k_window_pred<<<grid256(m), 256, 0, s>>>(D.torder, m, D.flags, D.Eb, nullptr, d_prm, D.sel, d_cnt);
         scan(D.sel, D.wcount, m, D.scan_aux, reinterpret_cast<uint32_t*>(D.dcount + 2), s);
         k_compact<<<grid256(m), 256, 0, s>>>(D.torder, D.sel, D.wcount, m, D.single_idx);
     }
     cudaMemcpyAsync(hc, D.dcount, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
     if ((ce = cudaStreamSynchronize(s)) != cudaSuccess) return set_err(err, err_len, GPET_ERR_CUDA, cudaGetErrorString(ce));
-    const int64_t ndead = m > 0 ? (int64_t)hc[1] : 0;
     const int64_t ns = m > 0 ? (int64_t)(hc[2] & 0xffffffffull) : 0;
-    counts[0] = m; counts[1] = ndead; counts[2] = ns;
+    counts[0] = m; counts[2] = ns;
     if (ns > singles_cap) return set_err(err, err_len, GPET_ERR_CAPACITY, "more singles than singles_cap");
     if (ns > 0 && (!d_singles || !d_single_scat)) return set_err(err, err_len, GPET_ERR_ARG, "null singles buffer");
     int64_t nc = 0;
-    unsigned long long* ncls = D.dcount + 5;
     if (ns > 0) {
         k_gather_events<<<grid256(ns), 256, 0, s>>>(P, D.single_idx, ns, 1, D.Eb, D.xb, D.yb, D.zb, D.site,
                                                     reinterpret_cast<EventRec*>(d_singles), meta_out);
         k_meta_to_scat<<<grid256(ns), 256, 0, s>>>(meta_out, ns, d_single_scat);
         cudaMemsetAsync(D.wcount, 0, sizeof(uint32_t) * ns, s);
         cudaMemsetAsync(D.wend, 0, sizeof(uint32_t) * ns, s);
-        k_coinc_count<<<grid256(ns), 256, 0, s>>>(D.single_idx, ns, P.t, P.pann, dp.window, dp.coinc_policy, D.wcount,
-                                                  D.wend, D.dcount + 3);
+        k_coinc_count<<<grid256(ns), 256, 0, s>>>(D.single_idx, ns, P.t, P.pann, nullptr, d_prm, D.wcount, D.wend,
+                                                  d_cnt);
         scan(D.wcount, D.sel, ns, D.scan_aux, total, s);
         uint32_t hn = 0;
         cudaMemcpyAsync(&hn, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
@@ -234,15 +236,16 @@ extern "C" int gpet_digitize_static(const gpet_digi_params* prm, const gpet_even
         if (nc > 0 && (!d_pairs || !d_class)) return set_err(err, err_len, GPET_ERR_ARG, "null coincidence buffer");
         if (nc > 0)
             k_coinc_write<<<grid256(ns), 256, 0, s>>>(D.single_idx, ns, D.wend, D.sel, P.pann, P.eventid, P.meta,
-                                                      dp.coinc_policy, d_pairs, d_class, pairs_cap, ncls);
+                                                      nullptr, d_prm, d_pairs, d_class, pairs_cap, d_cnt);
     }
-    unsigned long long h8[8] = {0};
-    cudaMemcpyAsync(h8, D.dcount, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    Counters h{};
+    cudaMemcpyAsync(&h, d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s);
     if ((ce = cudaStreamSynchronize(s)) != cudaSuccess) return set_err(err, err_len, GPET_ERR_CUDA, cudaGetErrorString(ce));
     if ((ce = cudaGetLastError()) != cudaSuccess) return set_err(err, err_len, GPET_ERR_CUDA, cudaGetErrorString(ce));
-    counts[4] = ns > 0 ? (int64_t)h8[5] : 0;
-    counts[5] = ns > 0 ? (int64_t)h8[6] : 0;
-    counts[6] = ns > 0 ? (int64_t)h8[7] : 0;
-    counts[7] = ns > 0 ? (int64_t)h8[3] : 0;
+    counts[1] = m > 0 ? (int64_t)h.n_dead : 0;
+    counts[4] = (int64_t)h.n_true;
+    counts[5] = (int64_t)h.n_scat;
+    counts[6] = (int64_t)h.n_rand;
+    counts[7] = (int64_t)h.n_mult;
     return GPET_OK;
 }

@@ -213,10 +213,13 @@ static void radix_sort(uint64_t*& ka, uint32_t*& va, uint64_t*& kb, uint32_t*& v
 }
 
 // ---------------------------------------------------------------- stages
+__device__ __forceinline__ int pulse_sim(const PulseDev& P, int64_t i) { return P.sim ? P.sim[i] : 0; }
+
 // blur (gPET_kernals.cu:814-837) + threshold (energywindow :641-656 with
-// [Eth, 2 MeV]); survivors' pulse indices appended to sel, site stored
-__global__ void k_blur_threshold(PulseDev P, int64_t n, DigiParams prm, float* Eb, float* xb, float* yb, float* zb,
-                                 int32_t* site, uint32_t* sel, unsigned long long* nsel)
+// [Eth, 2 MeV]); survivors' pulse indices appended to sel, site stored.
+// Parameters per simulation: prms[sim].
+__global__ void k_blur_threshold(PulseDev P, int64_t n, const DigiParams* __restrict__ prms, float* Eb, float* xb,
+                                 float* yb, float* zb, int32_t* site, uint32_t* sel, unsigned long long* nsel)
 {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
@@ -226,6 +229,7 @@ __global__ void k_blur_threshold(PulseDev P, int64_t n, DigiParams prm, float* E
         const int64_t i = base + threadIdx.x;
         bool keep = false;
         if (i < n) {
+            const DigiParams& prm = prms[pulse_sim(P, i)];
             const int32_t parn = P.parn[i];
             const uint32_t slot = P.meta[i] & 0x7fu;
             Stream st;
@@ -300,70 +304,111 @@ __global__ void k_tie_fix(const uint64_t* __restrict__ key, uint32_t* idx, int64
     }
 }
 
-__global__ void k_site_keys(const uint32_t* __restrict__ torder, int64_t m, const int32_t* __restrict__ site,
-                            uint64_t* key, uint32_t* val)
+// keys for the stable sort of the time order by simulation
+__global__ void k_sim_keys(const uint32_t* __restrict__ order, int64_t m, const int32_t* __restrict__ psim,
+                           uint64_t* key, uint32_t* val)
 {
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
-        uint32_t p = torder[j];
-        key[j] = (uint64_t)(uint32_t)site[p];
+        uint32_t p = order[j];
+        key[j] = (uint64_t)(uint32_t)psim[p];
         val[j] = p;
     }
 }
 
-// dead time (deadtime, gPET_kernals.cu:657-698, sequential semantics, FP64):
-// sorder is the (site, t, parn, slot) order
-__global__ void k_deadtime(const uint32_t* __restrict__ sorder, int64_t m, const int32_t* __restrict__ site,
-                           const double* __restrict__ t, double tau, int dtype, uint32_t* flags,
-                           unsigned long long* nalive)
+// (simulation, site) keys for the dead-time order
+__global__ void k_site_keys(const uint32_t* __restrict__ torder, int64_t m, const int32_t* __restrict__ site,
+                            const int32_t* __restrict__ psim, uint64_t* key, uint32_t* val)
 {
-    unsigned long long alive = 0;
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t p = sorder[j];
-        if (dtype == 0) {
-            bool keep = true;
-            if (j > 0) {
-                const uint32_t q = sorder[j - 1];
-                keep = !(site[q] == site[p] && t[p] < t[q] + tau);
-            }
-            flags[p] = keep ? 1u : 0u;
-            alive += keep;
-        } else {
-            // anchors: first pulse of a site or >= tau after its predecessor
-            bool anchor = j == 0;
-            if (!anchor) {
-                const uint32_t q = sorder[j - 1];
-                anchor = site[q] != site[p] || !(t[p] < t[q] + tau);
-            }
-            if (!anchor) continue;
-            double tdead = t[p];
-            flags[p] = 1u;
-            alive++;
-            for (int64_t i = j + 1; i < m; ++i) {
-                const uint32_t a = sorder[i], b = sorder[i - 1];
-                if (site[a] != site[b] || !(t[a] < t[b] + tau)) break;   // next anchor
-                if (t[a] < tdead + tau) {
-                    flags[a] = 0u;
-                } else {
-                    flags[a] = 1u;
+        uint32_t p = torder[j];
+        uint64_t sm = psim ? (uint64_t)(uint32_t)psim[p] : 0ull;
+        key[j] = (sm << 32) | (uint64_t)(uint32_t)site[p];
+        val[j] = p;
+    }
+}
+
+// per-simulation count of the elements of an order sorted by simulation
+__global__ void k_count_by_sim(const uint32_t* __restrict__ order, int64_t m, const int32_t* __restrict__ psim,
+                               Counters* cnt, int field)
+{
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = base + threadIdx.x;
+        const int sim = (j < m && psim) ? psim[order[j]] : 0;
+        add_by_sim(cnt, sim, field, j < m ? 1u : 0u);
+    }
+}
+
+// dead time (deadtime, gPET_kernals.cu:657-698, sequential semantics, FP64):
+// sorder is the (simulation, site, t, parn, slot) order
+__global__ void k_deadtime(const uint32_t* __restrict__ sorder, int64_t m, const int32_t* __restrict__ site,
+                           const int32_t* __restrict__ psim, const double* __restrict__ t,
+                           const DigiParams* __restrict__ prms, uint32_t* flags, Counters* cnt)
+{
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = base + threadIdx.x;
+        unsigned alive = 0;
+        int sim = 0;
+        if (j < m) {
+            const uint32_t p = sorder[j];
+            sim = psim ? psim[p] : 0;
+            const double tau = prms[sim].tau;
+            auto same_site = [&](uint32_t a, uint32_t b) {
+                return site[a] == site[b] && (!psim || psim[a] == psim[b]);
+            };
+            if (prms[sim].dtype == 0) {
+                bool keep = true;
+                if (j > 0) {
+                    const uint32_t q = sorder[j - 1];
+                    keep = !(same_site(q, p) && t[p] < t[q] + tau);
+                }
+                flags[p] = keep ? 1u : 0u;
+                alive += keep;
+            } else {
+                // anchors: first pulse of a site or >= tau after its predecessor
+                bool anchor = j == 0;
+                if (!anchor) {
+                    const uint32_t q = sorder[j - 1];
+                    anchor = !same_site(q, p) || !(t[p] < t[q] + tau);
+                }
+                if (anchor) {
+                    double tdead = t[p];
+                    flags[p] = 1u;
                     alive++;
-                    tdead = t[a];
+                    for (int64_t i = j + 1; i < m; ++i) {
+                        const uint32_t a = sorder[i], b = sorder[i - 1];
+                        if (!same_site(b, a) || !(t[a] < t[b] + tau)) break;   // next anchor
+                        if (t[a] < tdead + tau) {
+                            flags[a] = 0u;
+                        } else {
+                            flags[a] = 1u;
+                            alive++;
+                            tdead = t[a];
+                        }
+                    }
                 }
             }
         }
+        add_by_sim(cnt, sim, CF(n_dead), alive);
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) alive += __shfl_xor_sync(0xffffffffu, alive, o);
-    if ((threadIdx.x & 31) == 0 && alive) atomicAdd(nalive, alive);
 }
 
-// energy window (gPET.cu:418) predicate over the time order
+// energy window (gPET.cu:418) predicate over the (simulation, t) order
 __global__ void k_window_pred(const uint32_t* __restrict__ torder, int64_t m, const uint32_t* __restrict__ flags,
-                              const float* __restrict__ Eb, float lo, float hi, uint32_t* pred)
+                              const float* __restrict__ Eb, const int32_t* __restrict__ psim,
+                              const DigiParams* __restrict__ prms, uint32_t* pred, Counters* cnt)
 {
-    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t p = torder[j];
-        const float E = Eb[p];
-        pred[j] = (flags[p] && !(E < lo || E > hi)) ? 1u : 0u;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = base + threadIdx.x;
+        bool ok = false;
+        int sim = 0;
+        if (j < m) {
+            const uint32_t p = torder[j];
+            sim = psim ? psim[p] : 0;
+            const float E = Eb[p];
+            ok = flags[p] && !(E < prms[sim].ewin_lo || E > prms[sim].ewin_hi);
+            pred[j] = ok ? 1u : 0u;
+        }
+        add_by_sim(cnt, sim, CF(n_single), ok ? 1u : 0u);
     }
 }
 
@@ -376,50 +421,55 @@ __global__ void k_compact(const uint32_t* __restrict__ torder, const uint32_t* _
 
 // coincidence windows (no counterpart in the reference): a single not inside
 // an open window opens [t, t+W). One thread walks each cluster of singles
-// (a single >= W after its predecessor cannot be inside an earlier window).
+// (a single >= W after its predecessor, or the first of its simulation,
+// cannot be inside an earlier window).
 __global__ void k_coinc_count(const uint32_t* __restrict__ sidx, int64_t s, const double* __restrict__ t,
-                              const int32_t* __restrict__ pann, double W, int policy, uint32_t* wcount,
-                              uint32_t* wend, unsigned long long* nmult)
+                              const int32_t* __restrict__ pann, const int32_t* __restrict__ psim,
+                              const DigiParams* __restrict__ prms, uint32_t* wcount, uint32_t* wend, Counters* cnt)
 {
-    unsigned long long mult = 0;
+    SimTally mult;
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < s; j += (int64_t)gridDim.x * blockDim.x) {
-        bool anchor = j == 0 || !(t[sidx[j]] < t[sidx[j - 1]] + W);
+        const int sim = psim ? psim[sidx[j]] : 0;
+        const double W = prms[sim].window;
+        const int policy = prms[sim].coinc_policy;
+        auto same_sim = [&](int64_t a, int64_t b) { return !psim || psim[sidx[a]] == psim[sidx[b]]; };
+        bool anchor = j == 0 || !same_sim(j, j - 1) || !(t[sidx[j]] < t[sidx[j - 1]] + W);
         if (!anchor) continue;
         int64_t i = j;
-        while (i < s && (i == j || t[sidx[i]] < t[sidx[i - 1]] + W)) {
+        while (i < s && (i == j || (same_sim(i, i - 1) && t[sidx[i]] < t[sidx[i - 1]] + W))) {
             const double ti = t[sidx[i]];
             int64_t e = i + 1;
-            while (e < s && t[sidx[e]] < ti + W) e++;
-            const int64_t cnt = e - i;
+            while (e < s && same_sim(e, i) && t[sidx[e]] < ti + W) e++;
+            const int64_t cnt_w = e - i;
             uint32_t pairs = 0;
             if (policy == 0) {
-                if (cnt == 2 && pann[sidx[i]] != pann[sidx[i + 1]]) pairs = 1;
+                if (cnt_w == 2 && pann[sidx[i]] != pann[sidx[i + 1]]) pairs = 1;
             } else {
                 for (int64_t a = i; a < e; ++a)
                     for (int64_t b = a + 1; b < e; ++b) pairs += pann[sidx[a]] != pann[sidx[b]];
             }
-            if (cnt > 2) mult++;
+            mult.add(cnt, CF(n_mult), sim, cnt_w > 2 ? 1u : 0u);
             wcount[i] = pairs;
             wend[i] = (uint32_t)e;
             i = e;
         }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mult += __shfl_xor_sync(0xffffffffu, mult, o);
-    if ((threadIdx.x & 31) == 0 && mult) atomicAdd(nmult, mult);
+    mult.flush(cnt, CF(n_mult));
 }
 
 __global__ void k_coinc_write(const uint32_t* __restrict__ sidx, int64_t s, const uint32_t* __restrict__ wend,
                               const uint32_t* __restrict__ off, const int32_t* __restrict__ pann,
-                              const int32_t* __restrict__ eid, const uint8_t* __restrict__ meta, int policy,
-                              int64_t* pairs, uint8_t* klass, int64_t cap, unsigned long long* ncls)
+                              const int32_t* __restrict__ eid, const uint8_t* __restrict__ meta,
+                              const int32_t* __restrict__ psim, const DigiParams* __restrict__ prms,
+                              int64_t* pairs, uint8_t* klass, int64_t cap, Counters* cnt)
 {
-    unsigned long long c0 = 0, c1 = 0, c2 = 0;
+    SimTally c0, c1, c2;
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < s; j += (int64_t)gridDim.x * blockDim.x) {
         const int64_t e = wend[j];
         if (e <= j) continue;
-        const int64_t cnt = e - j;
-        if (policy == 0 && cnt != 2) continue;
+        const int sim = psim ? psim[sidx[j]] : 0;
+        const int64_t cnt_w = e - j;
+        if (prms[sim].coinc_policy == 0 && cnt_w != 2) continue;
         uint32_t o = off[j];
         for (int64_t a = j; a < e; ++a) {
             for (int64_t b = a + 1; b < e; ++b) {
@@ -434,13 +484,15 @@ __global__ void k_coinc_write(const uint32_t* __restrict__ sidx, int64_t s, cons
                     klass[o] = k;
                 }
                 o++;
-                if (k == 0) c0++; else if (k == 1) c1++; else c2++;
+                c0.add(cnt, CF(n_true), sim, k == 0);
+                c1.add(cnt, CF(n_scat), sim, k == 1);
+                c2.add(cnt, CF(n_rand), sim, k == 2);
             }
         }
     }
-    if (c0) atomicAdd(&ncls[0], c0);
-    if (c1) atomicAdd(&ncls[1], c1);
-    if (c2) atomicAdd(&ncls[2], c2);
+    c0.flush(cnt, CF(n_true));
+    c1.flush(cnt, CF(n_scat));
+    c2.flush(cnt, CF(n_rand));
 }
 
 static unsigned grid_for_g(int64_t n)
@@ -497,22 +549,28 @@ static int ensure(void** p, size_t bytes, size_t* have)
     return 0;
 }
 
-int digitize_device(const PulseDev& P, int64_t n, const DigiParams& prm, DigiScratch& D, Counters* cnt,
-                    cudaStream_t s, int64_t* launches, int64_t* n_singles_out, int64_t* n_coinc_out)
+int digitize_device(const PulseDev& P, int64_t n, const DigiParams* d_prms, int nsims, int64_t max_site,
+                    DigiScratch& D, Counters* d_cnt, cudaStream_t s, int64_t* launches, int64_t* n_singles_out,
+                    int64_t* n_coinc_out)
 {
+    // dcount: [0] selected [2] singles (uint32, scan total) [4] scratch scan total
     unsigned long long hc[4] = {0, 0, 0, 0};
     cudaMemsetAsync(D.dcount, 0, 8 * sizeof(unsigned long long), s);
+    const int32_t* psim = nsims > 1 ? P.sim : nullptr;
+    PulseDev Pv = P;
+    Pv.sim = const_cast<int32_t*>(psim);
     if (n > 0) {
-        k_blur_threshold<<<grid_for(n, 256), 256, 0, s>>>(P, n, prm, D.Eb, D.xb, D.yb, D.zb, D.site, D.sel,
+        k_blur_threshold<<<grid_for(n, 256), 256, 0, s>>>(Pv, n, d_prms, D.Eb, D.xb, D.yb, D.zb, D.site, D.sel,
                                                           D.dcount + 0);
         ++*launches;
     }
     cudaMemcpyAsync(hc, D.dcount, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return GPET_ERR_CUDA;
     const int64_t m = (int64_t)hc[0];
-    // dcount: [0] selected [1] alive after dead time [2] singles (uint32, scan
-    // total) [3] multiples [4] scratch scan total [5..7] true/scatter/random
     uint32_t* total = reinterpret_cast<uint32_t*>(D.dcount + 4);
+    int sim_bits = 0;
+    while ((1 << sim_bits) < nsims) sim_bits++;
+    sim_bits = (sim_bits + 7) / 8 * 8;
     // time order
     uint64_t *ka = D.key_a, *kb = D.key_b;
     uint32_t *va = D.idx_a, *vb = D.idx_b;
@@ -522,20 +580,24 @@ int digitize_device(const PulseDev& P, int64_t n, const DigiParams& prm, DigiScr
         radix_sort(ka, va, kb, vb, m, 64, D.hist, D.scan_aux, total, s, launches);
         k_tie_fix<<<grid_for(m, 256), 256, 0, s>>>(ka, va, m, P.parn, P.meta);
         ++*launches;
+        if (psim) {   // (simulation, t, parn, slot)
+            k_sim_keys<<<grid_for(m, 256), 256, 0, s>>>(va, m, psim, ka, va);
+            ++*launches;
+            radix_sort(ka, va, kb, vb, m, sim_bits, D.hist, D.scan_aux, total, s, launches);
+        }
         cudaMemcpyAsync(D.torder, va, sizeof(uint32_t) * m, cudaMemcpyDeviceToDevice, s);
+        k_count_by_sim<<<grid_for(m, 256), 256, 0, s>>>(D.torder, m, psim, d_cnt, CF(n_thr));
         // site order
         int site_bits = 8;
-        {
-            int64_t maxsite = (int64_t)prm.moduleN * prm.crystalN * kMaxPanels;
-            while (site_bits < 32 && (1ll << site_bits) <= maxsite) site_bits += 8;
-        }
-        k_site_keys<<<grid_for(m, 256), 256, 0, s>>>(D.torder, m, D.site, ka, va);
-        ++*launches;
+        while (site_bits < 32 && (1ll << site_bits) <= max_site) site_bits += 8;
+        if (psim) site_bits = 32 + sim_bits;
+        k_site_keys<<<grid_for(m, 256), 256, 0, s>>>(D.torder, m, D.site, psim, ka, va);
+        *launches += 2;
         radix_sort(ka, va, kb, vb, m, site_bits, D.hist, D.scan_aux, total, s, launches);
         // dead time on the site order
-        k_deadtime<<<grid_for(m, 256), 256, 0, s>>>(va, m, D.site, P.t, prm.tau, prm.dtype, D.flags, D.dcount + 1);
+        k_deadtime<<<grid_for(m, 256), 256, 0, s>>>(va, m, D.site, psim, P.t, d_prms, D.flags, d_cnt);
         // energy window over the time order, ordered compaction
-        k_window_pred<<<grid_for(m, 256), 256, 0, s>>>(D.torder, m, D.flags, D.Eb, prm.ewin_lo, prm.ewin_hi, D.sel);
+        k_window_pred<<<grid_for(m, 256), 256, 0, s>>>(D.torder, m, D.flags, D.Eb, psim, d_prms, D.sel, d_cnt);
         *launches += 2;
         scan_exclusive(D.sel, D.wcount, m, D.scan_aux, reinterpret_cast<uint32_t*>(D.dcount + 2), s, launches);
         k_compact<<<grid_for(m, 256), 256, 0, s>>>(D.torder, D.sel, D.wcount, m, D.single_idx);
@@ -543,16 +605,14 @@ int digitize_device(const PulseDev& P, int64_t n, const DigiParams& prm, DigiScr
     }
     cudaMemcpyAsync(hc, D.dcount, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return GPET_ERR_CUDA;
-    const int64_t ndead = m > 0 ? (int64_t)hc[1] : 0;
     const int64_t ns = m > 0 ? (int64_t)(uint32_t)(hc[2] & 0xffffffffull) : 0;
     // coincidences
     int64_t nc = 0;
-    unsigned long long* ncls = D.dcount + 5;
     if (ns > 0) {
         cudaMemsetAsync(D.wcount, 0, sizeof(uint32_t) * ns, s);
         cudaMemsetAsync(D.wend, 0, sizeof(uint32_t) * ns, s);
-        k_coinc_count<<<grid_for(ns, 256), 256, 0, s>>>(D.single_idx, ns, P.t, P.pann, prm.window, prm.coinc_policy,
-                                                        D.wcount, D.wend, D.dcount + 3);
+        k_coinc_count<<<grid_for(ns, 256), 256, 0, s>>>(D.single_idx, ns, P.t, P.pann, psim, d_prms, D.wcount, D.wend,
+                                                        d_cnt);
         ++*launches;
         scan_exclusive(D.wcount, D.sel, ns, D.scan_aux, total, s, launches);
         uint32_t hn = 0;
@@ -571,24 +631,13 @@ int digitize_device(const PulseDev& P, int64_t n, const DigiParams& prm, DigiScr
             }
             D.coinc_cap = cap;
         }
-        cudaMemsetAsync(ncls, 0, 3 * sizeof(unsigned long long), s);
         k_coinc_write<<<grid_for(ns, 256), 256, 0, s>>>(D.single_idx, ns, D.wend, D.sel, P.pann, P.eventid, P.meta,
-                                                        prm.coinc_policy, D.coinc_pairs, D.coinc_class,
-                                                        D.coinc_cap, ncls);
+                                                        psim, d_prms, D.coinc_pairs, D.coinc_class, D.coinc_cap,
+                                                        d_cnt);
         ++*launches;
     }
-    unsigned long long h8[8] = {0};
-    cudaMemcpyAsync(h8, D.dcount, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return GPET_ERR_CUDA;
     if (cudaGetLastError() != cudaSuccess) return GPET_ERR_CUDA;
-    cnt->n_thr = (unsigned long long)m;
-    cnt->n_dead = (unsigned long long)ndead;
-    cnt->n_single = (unsigned long long)ns;
-    cnt->n_coinc = (unsigned long long)nc;
-    cnt->n_mult = ns > 0 ? h8[3] : 0;
-    cnt->n_true = ns > 0 ? h8[5] : 0;
-    cnt->n_scat = ns > 0 ? h8[6] : 0;
-    cnt->n_rand = ns > 0 ? h8[7] : 0;
     *n_singles_out = ns;
     *n_coinc_out = nc;
     return 0;

@@ -36,6 +36,40 @@ struct DevBuf {
 
 }  // namespace
 
+// device work buffers and results of one run; a batch's contexts share the
+// leader's Work and read their own simulation's slice of the results
+struct Work {
+    DevBuf q_f, q_t, q_i;                 // detector queue
+    int64_t q_cap = 0;
+    DevBuf pb_f, pb_t, pb_n;              // emitted pairs of one wave
+    int64_t pb_cap = 0;
+    DevBuf aux;                           // [0] queue count [1] pulses [2] hits [3] wave work counter
+    DevBuf cnt;                           // Counters per simulation
+    DevBuf sims, prms, segs;              // batch descriptors
+    DevBuf p_int, p_t, p_f, p_meta, p_sim;  // pulses: 6 int32, double, 4 float, byte, simulation
+    int64_t p_cap = 0;
+    DevBuf h_id, h_f, h_sim;
+    int64_t h_cap = 0;
+    DevBuf exits;
+    DevBuf g_ev, g_meta;                  // gathered Event records for copy-out
+    DigiScratch dg{};
+    DevBuf dg_idx_a, dg_idx_b, dg_key_a, dg_key_b, dg_torder, dg_flags, dg_site, dg_hist, dg_aux, dg_sel, dg_blur,
+        dg_single, dg_wcount, dg_wend, dg_dcount;
+    std::vector<cudaEvent_t> tev;         // per-launch timing events
+    // results
+    int nsims = 0;
+    int64_t n_pulses = 0, n_hits = 0, n_singles = 0, n_coinc = 0;
+    std::vector<Counters> hcnt;           // per simulation
+    std::vector<uint8_t> sim_hits;        // per simulation: hits recorded
+    std::vector<int64_t> s_off, c_off;    // first single / coincidence of each simulation
+    ~Work()
+    {
+        for (auto& e : tev) cudaEventDestroy(e);
+        if (dg.coinc_pairs) cudaFree(dg.coinc_pairs);
+        if (dg.coinc_class) cudaFree(dg.coinc_class);
+    }
+};
+
 struct gpet_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -49,6 +83,7 @@ struct gpet_ctx {
     int record_hits = 1;
     int record_exits = 0;
     int64_t chunk_decays = 1ll << 24;
+    int64_t sub_decays = 1ll << 20;       // decays per wave: the pair buffer stays in L2
     std::string base_dir = ".";
     std::string data_dir;
     // host scene
@@ -70,24 +105,9 @@ struct gpet_ctx {
     // device scene
     SimDesc sim{};
     DevBuf d_sim, d_xs4, d_cmpsf, d_rayff, d_wck_ph, d_wck_det, d_vox, d_panels, d_psf;
-    // device work buffers
-    DevBuf q_f, q_t, q_i, cnt, qcount;
-    int64_t q_cap = 0;
-    DevBuf pb_f, pb_t, pb_n;              // emitted pairs of one sub-chunk
-    int64_t pb_cap = 0;
-    int64_t sub_decays = 1ll << 20;       // pairs buffer stays in L2
-    std::vector<cudaEvent_t> tev;         // per-launch timing events
-    DevBuf p_int, p_t, p_f, p_meta;       // pulses: 6 int32, 1 double, 4 float, 1 byte
-    int64_t p_cap = 0;
-    DevBuf h_id, h_f;
-    int64_t h_cap = 0;
-    DevBuf exits;
-    DevBuf g_ev, g_meta;                  // gathered Event records for copy-out
-    DigiScratch dg{};
-    DevBuf dg_idx_a, dg_idx_b, dg_key_a, dg_key_b, dg_torder, dg_flags, dg_site, dg_hist, dg_aux, dg_sel, dg_blur,
-        dg_single, dg_wcount, dg_wend, dg_dcount;
-    // results
-    int64_t n_pulses = 0, n_hits = 0, n_singles = 0, n_coinc = 0;
+    // results of the last run this context took part in
+    std::shared_ptr<Work> work;
+    int res_sim = 0;
     std::vector<ExitRec> host_exits;
     gpet_run_stats last{};
     bool have_results = false;
@@ -127,8 +147,7 @@ int gpet_create(int device, gpet_ctx** out)
     if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return GPET_ERR_NOGPU;
     if (device < 0 || device >= n) return GPET_ERR_ARG;
     if (cudaSetDevice(device) != cudaSuccess) return GPET_ERR_CUDA;
-    cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, k_phantom) != cudaSuccess) return GPET_ERR_NOGPU;
+    if (transport_kernels_loadable() != cudaSuccess) return GPET_ERR_NOGPU;
     auto* c = new gpet_ctx();
     c->device = device;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -146,7 +165,7 @@ void gpet_destroy(gpet_ctx* c)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
-    for (auto& e : c->tev) cudaEventDestroy(e);
+    c->work.reset();
     cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -473,94 +492,104 @@ static int64_t total_decays(const gpet_ctx* c)
     return t;
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------- run
 // grow a structure-of-arrays pulse buffer, keeping the first `used` entries
-static int grow_pulses(gpet_ctx* c, int64_t need, int64_t used)
+static int grow_pulses(gpet_ctx* c, Work& W, int64_t need, int64_t used)
 {
-    if (need <= c->p_cap) return GPET_OK;
+    if (need <= W.p_cap) return GPET_OK;
     int64_t cap = std::max<int64_t>(need + need / 2, 1 << 20);
-    DevBuf ni, nt, nf, nm;
+    DevBuf ni, nt, nf, nm, ns;
     CK(ni.ensure((size_t)cap * 6 * 4));
     CK(nt.ensure((size_t)cap * 8));
     CK(nf.ensure((size_t)cap * 4 * 4));
     CK(nm.ensure((size_t)cap));
+    CK(ns.ensure((size_t)cap * 4));
     if (used > 0) {
         for (int a = 0; a < 6; ++a)
-            CK(cudaMemcpyAsync(ni.as<int32_t>() + a * cap, c->p_int.as<int32_t>() + a * c->p_cap, used * 4,
+            CK(cudaMemcpyAsync(ni.as<int32_t>() + a * cap, W.p_int.as<int32_t>() + a * W.p_cap, used * 4,
                                cudaMemcpyDeviceToDevice, c->stream));
-        CK(cudaMemcpyAsync(nt.p, c->p_t.p, used * 8, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(nt.p, W.p_t.p, used * 8, cudaMemcpyDeviceToDevice, c->stream));
         for (int a = 0; a < 4; ++a)
-            CK(cudaMemcpyAsync(nf.as<float>() + a * cap, c->p_f.as<float>() + a * c->p_cap, used * 4,
+            CK(cudaMemcpyAsync(nf.as<float>() + a * cap, W.p_f.as<float>() + a * W.p_cap, used * 4,
                                cudaMemcpyDeviceToDevice, c->stream));
-        CK(cudaMemcpyAsync(nm.p, c->p_meta.p, used, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(nm.p, W.p_meta.p, used, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(ns.p, W.p_sim.p, used * 4, cudaMemcpyDeviceToDevice, c->stream));
         CK(cudaStreamSynchronize(c->stream));
     }
-    std::swap(c->p_int.p, ni.p); std::swap(c->p_int.bytes, ni.bytes);
-    std::swap(c->p_t.p, nt.p); std::swap(c->p_t.bytes, nt.bytes);
-    std::swap(c->p_f.p, nf.p); std::swap(c->p_f.bytes, nf.bytes);
-    std::swap(c->p_meta.p, nm.p); std::swap(c->p_meta.bytes, nm.bytes);
-    c->p_cap = cap;
+    std::swap(W.p_int.p, ni.p); std::swap(W.p_int.bytes, ni.bytes);
+    std::swap(W.p_t.p, nt.p); std::swap(W.p_t.bytes, nt.bytes);
+    std::swap(W.p_f.p, nf.p); std::swap(W.p_f.bytes, nf.bytes);
+    std::swap(W.p_meta.p, nm.p); std::swap(W.p_meta.bytes, nm.bytes);
+    std::swap(W.p_sim.p, ns.p); std::swap(W.p_sim.bytes, ns.bytes);
+    W.p_cap = cap;
     return GPET_OK;
 }
 
-static int grow_hits(gpet_ctx* c, int64_t need, int64_t used)
+static int grow_hits(gpet_ctx* c, Work& W, int64_t need, int64_t used)
 {
-    if (need <= c->h_cap) return GPET_OK;
+    if (need <= W.h_cap) return GPET_OK;
     int64_t cap = std::max<int64_t>(need + need / 2, 1 << 20);
-    DevBuf ni, nf;
+    DevBuf ni, nf, ns;
     CK(ni.ensure((size_t)cap * 20));
     CK(nf.ensure((size_t)cap * 20));
+    CK(ns.ensure((size_t)cap * 4));
     if (used > 0) {
-        CK(cudaMemcpyAsync(ni.p, c->h_id.p, used * 20, cudaMemcpyDeviceToDevice, c->stream));
-        CK(cudaMemcpyAsync(nf.p, c->h_f.p, used * 20, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(ni.p, W.h_id.p, used * 20, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(nf.p, W.h_f.p, used * 20, cudaMemcpyDeviceToDevice, c->stream));
+        CK(cudaMemcpyAsync(ns.p, W.h_sim.p, used * 4, cudaMemcpyDeviceToDevice, c->stream));
         CK(cudaStreamSynchronize(c->stream));
     }
-    std::swap(c->h_id.p, ni.p); std::swap(c->h_id.bytes, ni.bytes);
-    std::swap(c->h_f.p, nf.p); std::swap(c->h_f.bytes, nf.bytes);
-    c->h_cap = cap;
+    std::swap(W.h_id.p, ni.p); std::swap(W.h_id.bytes, ni.bytes);
+    std::swap(W.h_f.p, nf.p); std::swap(W.h_f.bytes, nf.bytes);
+    std::swap(W.h_sim.p, ns.p); std::swap(W.h_sim.bytes, ns.bytes);
+    W.h_cap = cap;
     return GPET_OK;
 }
 
-static PulseDev pulse_view(gpet_ctx* c)
+static PulseDev pulse_view(Work& W)
 {
     PulseDev P;
-    int32_t* I = c->p_int.as<int32_t>();
-    float* F = c->p_f.as<float>();
-    int64_t cap = c->p_cap;
+    int32_t* I = W.p_int.as<int32_t>();
+    float* F = W.p_f.as<float>();
+    int64_t cap = W.p_cap;
     P.parn = I; P.pann = I + cap; P.modn = I + 2 * cap; P.cryn = I + 3 * cap; P.siten = I + 4 * cap;
     P.eventid = I + 5 * cap;
-    P.t = c->p_t.as<double>();
+    P.t = W.p_t.as<double>();
     P.E = F; P.x = F + cap; P.y = F + 2 * cap; P.z = F + 3 * cap;
-    P.meta = c->p_meta.as<uint8_t>();
-    P.count = c->cnt.as<unsigned long long>() + 32;
+    P.meta = W.p_meta.as<uint8_t>();
+    P.sim = W.nsims > 1 ? W.p_sim.as<int32_t>() : nullptr;
+    P.count = W.aux.as<unsigned long long>() + 1;
     P.cap = cap;
     return P;
 }
 
-static int ensure_digi(gpet_ctx* c, int64_t n)
+static int ensure_digi(gpet_ctx* c, Work& W, int64_t n)
 {
     int64_t cap = std::max<int64_t>(n, 1024);
-    if (cap > c->dg.cap) {
+    if (cap > W.dg.cap) {
         cap = cap + cap / 4;
-        CK(c->dg_idx_a.ensure(cap * 4)); CK(c->dg_idx_b.ensure(cap * 4));
-        CK(c->dg_key_a.ensure(cap * 8)); CK(c->dg_key_b.ensure(cap * 8));
-        CK(c->dg_torder.ensure(cap * 4)); CK(c->dg_flags.ensure(cap * 4)); CK(c->dg_site.ensure(cap * 4));
-        CK(c->dg_sel.ensure(cap * 4)); CK(c->dg_blur.ensure(cap * 16)); CK(c->dg_single.ensure(cap * 4));
-        CK(c->dg_wcount.ensure(cap * 4)); CK(c->dg_wend.ensure(cap * 4));
+        CK(W.dg_idx_a.ensure(cap * 4)); CK(W.dg_idx_b.ensure(cap * 4));
+        CK(W.dg_key_a.ensure(cap * 8)); CK(W.dg_key_b.ensure(cap * 8));
+        CK(W.dg_torder.ensure(cap * 4)); CK(W.dg_flags.ensure(cap * 4)); CK(W.dg_site.ensure(cap * 4));
+        CK(W.dg_sel.ensure(cap * 4)); CK(W.dg_blur.ensure(cap * 16)); CK(W.dg_single.ensure(cap * 4));
+        CK(W.dg_wcount.ensure(cap * 4)); CK(W.dg_wend.ensure(cap * 4));
         int64_t nb = (cap + 4095) / 4096;
-        CK(c->dg_hist.ensure((size_t)256 * nb * 4));
+        CK(W.dg_hist.ensure((size_t)256 * nb * 4));
         int64_t na = (256 * nb + 4095) / 4096 + (cap + 4095) / 4096 + 16;
-        CK(c->dg_aux.ensure((size_t)na * 4));
-        CK(c->dg_dcount.ensure(16 * 8));
-        DigiScratch& D = c->dg;
-        D.idx_a = c->dg_idx_a.as<uint32_t>(); D.idx_b = c->dg_idx_b.as<uint32_t>();
-        D.key_a = c->dg_key_a.as<uint64_t>(); D.key_b = c->dg_key_b.as<uint64_t>();
-        D.torder = c->dg_torder.as<uint32_t>(); D.flags = c->dg_flags.as<uint32_t>(); D.site = c->dg_site.as<int32_t>();
-        D.hist = c->dg_hist.as<uint32_t>(); D.scan_aux = c->dg_aux.as<uint32_t>(); D.sel = c->dg_sel.as<uint32_t>();
-        float* B = c->dg_blur.as<float>();
+        CK(W.dg_aux.ensure((size_t)na * 4));
+        CK(W.dg_dcount.ensure(16 * 8));
+        DigiScratch& D = W.dg;
+        D.idx_a = W.dg_idx_a.as<uint32_t>(); D.idx_b = W.dg_idx_b.as<uint32_t>();
+        D.key_a = W.dg_key_a.as<uint64_t>(); D.key_b = W.dg_key_b.as<uint64_t>();
+        D.torder = W.dg_torder.as<uint32_t>(); D.flags = W.dg_flags.as<uint32_t>(); D.site = W.dg_site.as<int32_t>();
+        D.hist = W.dg_hist.as<uint32_t>(); D.scan_aux = W.dg_aux.as<uint32_t>(); D.sel = W.dg_sel.as<uint32_t>();
+        float* B = W.dg_blur.as<float>();
         D.Eb = B; D.xb = B + cap; D.yb = B + 2 * cap; D.zb = B + 3 * cap;
-        D.single_idx = c->dg_single.as<uint32_t>();
-        D.wcount = c->dg_wcount.as<uint32_t>(); D.wend = c->dg_wend.as<uint32_t>();
-        D.dcount = c->dg_dcount.as<unsigned long long>();
+        D.single_idx = W.dg_single.as<uint32_t>();
+        D.wcount = W.dg_wcount.as<uint32_t>(); D.wend = W.dg_wend.as<uint32_t>();
+        D.dcount = W.dg_dcount.as<unsigned long long>();
         D.cap = cap;
         D.hist_cap = 256 * nb;
     }
@@ -582,19 +611,19 @@ static DigiParams digi_params(const gpet_ctx* c)
     return p;
 }
 
-static void fill_stats(gpet_ctx* c, const Counters& h, gpet_run_stats* st)
+static void fill_stats(const Counters& h, gpet_run_stats* st)
 {
     st->n_pairs = (int64_t)h.pairs;
     st->n_entered = (int64_t)h.entered;
-    st->n_pulses = c->n_pulses;
-    st->n_hits = c->n_hits;
+    st->n_pulses = (int64_t)h.n_pulse;
+    st->n_hits = (int64_t)h.n_hit;
     st->n_threshold = (int64_t)h.n_thr;
     st->n_deadtime = (int64_t)h.n_dead;
     st->n_singles = (int64_t)h.n_single;
-    st->n_coinc = (int64_t)h.n_coinc;
     st->n_true = (int64_t)h.n_true;
     st->n_scatter = (int64_t)h.n_scat;
     st->n_random = (int64_t)h.n_rand;
+    st->n_coinc = (int64_t)(h.n_true + h.n_scat + h.n_rand);
     st->n_multiple = (int64_t)h.n_mult;
     st->n_overflow = (int64_t)h.overflow;
     st->n_stepcap = (int64_t)h.stepcap;
@@ -602,107 +631,222 @@ static void fill_stats(gpet_ctx* c, const Counters& h, gpet_run_stats* st)
     st->detector_steps = (int64_t)h.det_steps;
 }
 
-static int digitize_and_finish(gpet_ctx* c, int64_t np, gpet_run_stats* st, Counters& h, float* ms_digi)
+// the leader's Work for a new run: reused unless other contexts still hold
+// results in it
+static Work& fresh_work(gpet_ctx* c)
 {
-    int rc = ensure_digi(c, np);
+    if (!c->work || c->work.use_count() > 1) c->work = std::make_shared<Work>();
+    return *c->work;
+}
+
+// digitize W's pulses for nsims simulations with parameters prms (host),
+// leaving per-simulation counts in W.hcnt and result offsets in W.s_off/c_off
+static int digitize_work(gpet_ctx* c, Work& W, const std::vector<DigiParams>& prms, int64_t max_site,
+                         gpet_run_stats* st, float* ms_digi)
+{
+    const int n = (int)prms.size();
+    int rc = ensure_digi(c, W, W.n_pulses);
     if (rc) return rc;
-    PulseDev P = pulse_view(c);
-    DigiParams prm = digi_params(c);
-    Counters* dcnt = c->cnt.as<Counters>();
+    CK(W.prms.ensure(sizeof(DigiParams) * n));
+    CK(cudaMemcpyAsync(W.prms.p, prms.data(), sizeof(DigiParams) * n, cudaMemcpyHostToDevice, c->stream));
+    PulseDev P = pulse_view(W);
     cudaEventRecord(c->ev[4], c->stream);
     int64_t ns = 0, nc = 0;
-    rc = digitize_device(P, np, prm, c->dg, &h, c->stream, &st->kernel_launches, &ns, &nc);
+    rc = digitize_device(P, W.n_pulses, W.prms.as<DigiParams>(), n, max_site, W.dg, W.cnt.as<Counters>(), c->stream,
+                         &st->kernel_launches, &ns, &nc);
     if (rc) return fail(c, rc, std::string("digitizer failed: ") + cudaGetErrorString(cudaGetLastError()));
     cudaEventRecord(c->ev[5], c->stream);
     CK(cudaEventSynchronize(c->ev[5]));
     cudaEventElapsedTime(ms_digi, c->ev[4], c->ev[5]);
-    (void)dcnt;
-    c->n_singles = ns;
-    c->n_coinc = nc;
-    c->have_results = true;
+    W.hcnt.assign(n, Counters{});
+    CK(cudaMemcpy(W.hcnt.data(), W.cnt.p, sizeof(Counters) * n, cudaMemcpyDeviceToHost));
+    W.n_singles = ns;
+    W.n_coinc = nc;
+    W.s_off.assign(n + 1, 0);
+    W.c_off.assign(n + 1, 0);
+    for (int s = 0; s < n; ++s) {
+        W.s_off[s + 1] = W.s_off[s] + (int64_t)W.hcnt[s].n_single;
+        W.c_off[s + 1] = W.c_off[s] + (int64_t)(W.hcnt[s].n_true + W.hcnt[s].n_scat + W.hcnt[s].n_rand);
+    }
+    if (W.s_off[n] != ns || W.c_off[n] != nc) return fail(c, GPET_ERR_CUDA, "digitizer counts are inconsistent");
     return GPET_OK;
 }
 
-int gpet_run(gpet_ctx* c, gpet_run_stats* st)
+// one wave: decays [g, g + n) of the batch's concatenated decay list
+struct WaveH {
+    int64_t g, n;
+    int first_seg, nseg;
+};
+
+static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats)
 {
-    if (!c) return GPET_ERR_ARG;
-    if (!c->have_tables || !c->have_phantom || !c->have_geo || !c->have_source)
-        return fail(c, GPET_ERR_ARG, "tables, phantom, geometry and source must be set before gpet_run");
+    gpet_ctx* c = cs[0];
+    for (int s = 0; s < nsim; ++s) {
+        gpet_ctx* x = cs[s];
+        if (!x) return fail(c, GPET_ERR_ARG, "null context in the batch");
+        if (!x->have_tables || !x->have_phantom || !x->have_geo || !x->have_source)
+            return fail(x, GPET_ERR_ARG, "tables, phantom, geometry and source must be set before a run");
+        if (x->device != c->device) return fail(c, GPET_ERR_ARG, "a batch must be on one device");
+        for (int r = 0; r < s; ++r)
+            if (cs[r] == x) return fail(c, GPET_ERR_ARG, "a context appears twice in the batch");
+    }
+    if (nsim > 1)
+        for (int s = 0; s < nsim; ++s)
+            if (cs[s]->record_exits) return fail(c, GPET_ERR_ARG, "record_exits is for single runs");
     CK(cudaSetDevice(c->device));
-    gpet_run_stats local{};
-    if (!st) st = &local;
-    std::memset(st, 0, sizeof(*st));
-    int rc = build_sim(c);
-    if (rc) return rc;
-    const int64_t nd = total_decays(c);
-    st->n_decays = nd;
-    const int64_t chunk = std::min<int64_t>(std::max<int64_t>(nd, 1), c->chunk_decays);
-    // queue sized so no photon of a chunk can be dropped
-    if (2 * chunk > c->q_cap) {
-        int64_t cap = 2 * chunk;
-        CK(c->q_f.ensure((size_t)cap * 7 * 4));
-        CK(c->q_t.ensure((size_t)cap * 8));
-        CK(c->q_i.ensure((size_t)cap * 4 * 4));
-        c->q_cap = cap;
+    std::vector<int64_t> nd(nsim);
+    int64_t ND = 0, max_site = 1;
+    bool rec_hits = false;
+    size_t smem = 0;
+    for (int s = 0; s < nsim; ++s) {
+        int rc = build_sim(cs[s]);
+        if (rc) return rc;
+        nd[s] = total_decays(cs[s]);
+        ND += nd[s];
+        rec_hits = rec_hits || cs[s]->record_hits;
+        max_site = std::max<int64_t>(max_site, (int64_t)cs[s]->geo.npanels * cs[s]->geo.moduleN * cs[s]->geo.crystalN);
+        smem = std::max(smem, (size_t)cs[s]->geo.npanels * kPanelStride * 4);
     }
-    CK(c->cnt.ensure(64 * 8));
-    CK(cudaMemsetAsync(c->cnt.p, 0, 64 * 8, c->stream));
-    rc = grow_pulses(c, 1 << 20, 0);
+    Work& W = fresh_work(c);
+    W.nsims = nsim;
+    W.n_pulses = W.n_hits = W.n_singles = W.n_coinc = 0;
+    W.sim_hits.assign(nsim, 0);
+    for (int s = 0; s < nsim; ++s) W.sim_hits[s] = cs[s]->record_hits ? 1 : 0;
+    // descriptors of the batch
+    std::vector<SimDesc> sims(nsim);
+    std::vector<DigiParams> prms(nsim);
+    for (int s = 0; s < nsim; ++s) { sims[s] = cs[s]->sim; prms[s] = digi_params(cs[s]); }
+    CK(W.sims.ensure(sizeof(SimDesc) * nsim));
+    CK(cudaMemcpyAsync(W.sims.p, sims.data(), sizeof(SimDesc) * nsim, cudaMemcpyHostToDevice, c->stream));
+    CK(W.cnt.ensure(sizeof(Counters) * nsim));
+    CK(cudaMemsetAsync(W.cnt.p, 0, sizeof(Counters) * nsim, c->stream));
+    CK(W.aux.ensure(64 * 8));
+    CK(cudaMemsetAsync(W.aux.p, 0, 64 * 8, c->stream));
+    // waves of at most `sub` decays (and kMaxSeg simulations), chunks of at most `chunk` decays
+    const int64_t sub = std::min(c->sub_decays, std::max<int64_t>(ND, 1));
+    const int64_t chunk = std::max(std::min(c->chunk_decays, std::max<int64_t>(ND, 1)), sub);
+    std::vector<int64_t> seg_g0, seg_d0;
+    std::vector<int32_t> seg_sim;
+    std::vector<WaveH> waves;
+    {
+        int s = 0;
+        int64_t ds = 0;   // next decay of simulation s
+        int64_t g = 0;
+        while (s < nsim && ds >= nd[s]) { s++; ds = 0; }
+        while (s < nsim) {
+            WaveH wv{g, 0, (int)seg_sim.size(), 0};
+            while (s < nsim && wv.n < sub && wv.nseg < kMaxSeg) {
+                int64_t take = std::min(nd[s] - ds, sub - wv.n);
+                seg_g0.push_back(wv.n);
+                seg_d0.push_back(ds);
+                seg_sim.push_back(s);
+                wv.nseg++;
+                wv.n += take;
+                ds += take;
+                if (ds >= nd[s]) { s++; ds = 0; while (s < nsim && ds >= nd[s]) s++; }
+            }
+            g += wv.n;
+            waves.push_back(wv);
+        }
+    }
+    // per wave: g0[nseg + 1], d0[nseg], sim[nseg], laid out one wave after another
+    std::vector<int64_t> wg0, wd0;
+    std::vector<int32_t> wsim;
+    std::vector<size_t> woff_g0(waves.size()), woff_d0(waves.size());
+    for (size_t w = 0; w < waves.size(); ++w) {
+        woff_g0[w] = wg0.size();
+        woff_d0[w] = wd0.size();
+        for (int k = 0; k < waves[w].nseg; ++k) {
+            wg0.push_back(seg_g0[waves[w].first_seg + k]);
+            wd0.push_back(seg_d0[waves[w].first_seg + k]);
+            wsim.push_back(seg_sim[waves[w].first_seg + k]);
+        }
+        wg0.push_back(waves[w].n);
+    }
+    const size_t seg_bytes = (wg0.size() + wd0.size()) * 8 + wsim.size() * 4 + 64;
+    CK(W.segs.ensure(seg_bytes));
+    int64_t* d_g0 = W.segs.as<int64_t>();
+    int64_t* d_d0 = d_g0 + wg0.size();
+    int32_t* d_sim = reinterpret_cast<int32_t*>(d_d0 + wd0.size());
+    if (!wg0.empty()) CK(cudaMemcpyAsync(d_g0, wg0.data(), wg0.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    if (!wd0.empty()) CK(cudaMemcpyAsync(d_d0, wd0.data(), wd0.size() * 8, cudaMemcpyHostToDevice, c->stream));
+    if (!wsim.empty()) CK(cudaMemcpyAsync(d_sim, wsim.data(), wsim.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    // buffers
+    if (2 * chunk > W.q_cap) {
+        CK(W.q_f.ensure((size_t)2 * chunk * 7 * 4));
+        CK(W.q_t.ensure((size_t)2 * chunk * 8));
+        CK(W.q_i.ensure((size_t)2 * chunk * 5 * 4));
+        W.q_cap = 2 * chunk;
+    }
+    if (sub > W.pb_cap) {
+        CK(W.pb_f.ensure((size_t)sub * 11 * 4));
+        CK(W.pb_t.ensure((size_t)sub * 8));
+        CK(W.pb_n.ensure((size_t)sub));
+        W.pb_cap = sub;
+    }
+    int rc = grow_pulses(c, W, 1 << 20, 0);
     if (rc) return rc;
-    if (c->record_hits) { rc = grow_hits(c, 1 << 20, 0); if (rc) return rc; }
+    if (rec_hits) { rc = grow_hits(c, W, 1 << 20, 0); if (rc) return rc; }
     if (c->record_exits) {
-        CK(c->exits.ensure((size_t)2 * chunk * sizeof(ExitRec)));
-        c->host_exits.assign((size_t)2 * nd, ExitRec{});
-    }
-    Counters* dcnt = c->cnt.as<Counters>();
-    unsigned long long* qcount = c->cnt.as<unsigned long long>() + 31;
-    unsigned long long* pcount = c->cnt.as<unsigned long long>() + 32;
-    unsigned long long* hcount = c->cnt.as<unsigned long long>() + 33;
-    unsigned long long* work = c->cnt.as<unsigned long long>() + 40;   // one counter per sub-chunk launch
-    int nsm = 0;
-    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
-    const size_t smem = (size_t)c->geo.npanels * kPanelStride * 4;
-    const int64_t sub = std::min<int64_t>(c->sub_decays, chunk);
-    if (sub > c->pb_cap) {
-        CK(c->pb_f.ensure((size_t)sub * 11 * 4));
-        CK(c->pb_t.ensure((size_t)sub * 8));
-        CK(c->pb_n.ensure((size_t)sub));
-        c->pb_cap = sub;
+        CK(W.exits.ensure((size_t)2 * chunk * sizeof(ExitRec)));
+        c->host_exits.assign((size_t)2 * ND, ExitRec{});
+    } else {
+        c->host_exits.clear();
     }
     PairBuf pb;
-    pb.f = c->pb_f.as<float>(); pb.t = c->pb_t.as<double>(); pb.nph = c->pb_n.as<uint8_t>(); pb.cap = c->pb_cap;
+    pb.f = W.pb_f.as<float>(); pb.t = W.pb_t.as<double>(); pb.nph = W.pb_n.as<uint8_t>(); pb.cap = W.pb_cap;
+    Counters* dcnt = W.cnt.as<Counters>();
+    unsigned long long* qcount = W.aux.as<unsigned long long>() + 0;
+    unsigned long long* pcount = W.aux.as<unsigned long long>() + 1;
+    unsigned long long* hcount = W.aux.as<unsigned long long>() + 2;
+    unsigned long long* work = W.aux.as<unsigned long long>() + 3;
+    const bool multi = nsim > 1;
+    // one simulation: its panels are staged in shared memory
+    if (multi) smem = 0;
+    int nsm = 0;
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
     int phantom_blocks = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&phantom_blocks, k_phantom, 256, smem));
+    CK(phantom_blocks_per_sm(multi, smem, &phantom_blocks));
     phantom_blocks = std::max(1, phantom_blocks) * nsm;
-    const int64_t nsub_per_chunk = (chunk + sub - 1) / sub;
-    while ((int64_t)c->tev.size() < 3 * nsub_per_chunk + 4) {
-        cudaEvent_t e;
-        CK(cudaEventCreate(&e));
-        c->tev.push_back(e);
-    }
-    float ms_sp = 0, ms_det = 0, ms_src = 0, ms_ph = 0;
+    const SimDesc* d_sims = W.sims.as<SimDesc>();
+    gpet_run_stats tot{};
+    float ms_det = 0, ms_src = 0, ms_ph = 0;
     cudaEventRecord(c->ev[0], c->stream);
     int64_t pulses_used = 0, hits_used = 0;
-    for (int64_t d0 = 0; d0 < nd; d0 += chunk) {
-        const int64_t d1 = std::min(nd, d0 + chunk);
+    size_t wi = 0;
+    while (wi < waves.size()) {
+        // one chunk: waves until `chunk` decays
+        const int64_t cg0 = waves[wi].g;
+        size_t we = wi;
+        while (we < waves.size() && waves[we].g + waves[we].n - cg0 <= chunk) we++;
+        if (we == wi) we = wi + 1;
         CK(cudaMemsetAsync(qcount, 0, 8, c->stream));
         QueueDev q;
-        q.f = c->q_f.as<float>(); q.t = c->q_t.as<double>(); q.i = c->q_i.as<int32_t>();
-        q.count = qcount; q.cap = c->q_cap;
+        q.f = W.q_f.as<float>(); q.t = W.q_t.as<double>(); q.i = W.q_i.as<int32_t>();
+        q.count = qcount; q.cap = W.q_cap;
         int ne = 0;
-        for (int64_t s0 = d0; s0 < d1; s0 += sub) {
-            const int64_t n = std::min(d1, s0 + sub) - s0;
+        for (size_t w = wi; w < we; ++w) {
+            Wave wave;
+            wave.sims = d_sims;
+            wave.g0 = d_g0 + woff_g0[w];
+            wave.d0 = d_d0 + woff_d0[w];
+            wave.sim = d_sim + woff_d0[w];
+            wave.nseg = waves[w].nseg;
+            wave.n = waves[w].n;
             CK(cudaMemsetAsync(work, 0, 8, c->stream));
-            int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)nsm * 16);
-            cudaEventRecord(c->tev[ne++], c->stream);
-            k_source<<<(unsigned)std::max<int64_t>(blocks, 1), 256, smem, c->stream>>>(c->d_sim.as<SimDesc>(), s0, n,
-                                                                                      pb, dcnt);
-            cudaEventRecord(c->tev[ne++], c->stream);
-            k_phantom<<<(unsigned)phantom_blocks, 256, smem, c->stream>>>(
-                c->d_sim.as<SimDesc>(), s0, n, pb, work, q,
-                c->record_exits ? c->exits.as<ExitRec>() + 2 * (s0 - d0) : nullptr, dcnt);
-            cudaEventRecord(c->tev[ne++], c->stream);
-            st->kernel_launches += 2;
+            int64_t blocks = std::min<int64_t>((wave.n + 255) / 256, (int64_t)nsm * 16);
+            ExitRec* ex = c->record_exits ? W.exits.as<ExitRec>() + 2 * (waves[w].g - cg0) : nullptr;
+            while (W.tev.size() < (size_t)ne + 3) {
+                cudaEvent_t e;
+                CK(cudaEventCreate(&e));
+                W.tev.push_back(e);
+            }
+            cudaEventRecord(W.tev[ne++], c->stream);
+            CK(launch_source(multi, (unsigned)std::max<int64_t>(blocks, 1), smem, c->stream, wave, pb, dcnt));
+            cudaEventRecord(W.tev[ne++], c->stream);
+            CK(launch_phantom(multi, (unsigned)phantom_blocks, smem, c->stream, wave, pb, work, q, ex, dcnt));
+            cudaEventRecord(W.tev[ne++], c->stream);
+            tot.kernel_launches += 2;
         }
         unsigned long long hq = 0;
         CK(cudaMemcpyAsync(&hq, qcount, 8, cudaMemcpyDeviceToHost, c->stream));
@@ -710,28 +854,30 @@ int gpet_run(gpet_ctx* c, gpet_run_stats* st)
         CK(cudaGetLastError());
         for (int e = 0; e < ne; e += 3) {
             float a = 0, b = 0;
-            cudaEventElapsedTime(&a, c->tev[e], c->tev[e + 1]);
-            cudaEventElapsedTime(&b, c->tev[e + 1], c->tev[e + 2]);
+            cudaEventElapsedTime(&a, W.tev[e], W.tev[e + 1]);
+            cudaEventElapsedTime(&b, W.tev[e + 1], W.tev[e + 2]);
             ms_src += a;
             ms_ph += b;
-            ms_sp += a + b;
         }
+        const int64_t cn = waves[we - 1].g + waves[we - 1].n - cg0;
         if (c->record_exits)
-            CK(cudaMemcpy(c->host_exits.data() + 2 * d0, c->exits.p, (size_t)2 * (d1 - d0) * sizeof(ExitRec),
+            CK(cudaMemcpy(c->host_exits.data() + 2 * cg0, W.exits.p, (size_t)2 * cn * sizeof(ExitRec),
                           cudaMemcpyDeviceToHost));
         // room for the worst case of this chunk's queue
-        rc = grow_pulses(c, pulses_used + (int64_t)hq * kMaxPulse, pulses_used);
+        rc = grow_pulses(c, W, pulses_used + (int64_t)hq * kMaxPulse, pulses_used);
         if (rc) return rc;
-        if (c->record_hits) { rc = grow_hits(c, hits_used + (int64_t)hq * kMaxHits, hits_used); if (rc) return rc; }
-        PulseDev P = pulse_view(c);
+        if (rec_hits) { rc = grow_hits(c, W, hits_used + (int64_t)hq * kMaxHits, hits_used); if (rc) return rc; }
+        PulseDev P = pulse_view(W);
+        P.sim = multi ? W.p_sim.as<int32_t>() : nullptr;
         HitDev H;
-        H.id = c->h_id.as<int32_t>(); H.f = c->h_f.as<float>(); H.count = hcount; H.cap = c->h_cap;
+        H.id = W.h_id.as<int32_t>(); H.f = W.h_f.as<float>(); H.count = hcount; H.cap = W.h_cap;
+        H.sim = multi ? W.h_sim.as<int32_t>() : nullptr;
         int64_t dblocks = std::min<int64_t>(((int64_t)hq + 255) / 256, (int64_t)nsm * 8);
         cudaEventRecord(c->ev[1], c->stream);
         if (hq > 0) {
-            k_detector<<<(unsigned)std::max<int64_t>(dblocks, 1), 256, smem, c->stream>>>(c->d_sim.as<SimDesc>(), q, P,
-                                                                                       H, c->record_hits, dcnt);
-            st->kernel_launches++;
+            CK(launch_detector(multi, (unsigned)std::max<int64_t>(dblocks, 1), smem, c->stream, d_sims, q, P, H,
+                               rec_hits ? 1 : 0, dcnt));
+            tot.kernel_launches++;
         }
         cudaEventRecord(c->ev[2], c->stream);
         unsigned long long hp[2] = {0, 0};
@@ -741,34 +887,58 @@ int gpet_run(gpet_ctx* c, gpet_run_stats* st)
         float ms = 0;
         cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
         ms_det += ms;
-        pulses_used = (int64_t)std::min<unsigned long long>(hp[0], (unsigned long long)c->p_cap);
-        hits_used = (int64_t)std::min<unsigned long long>(hp[1], (unsigned long long)c->h_cap);
+        pulses_used = (int64_t)std::min<unsigned long long>(hp[0], (unsigned long long)W.p_cap);
+        hits_used = (int64_t)std::min<unsigned long long>(hp[1], (unsigned long long)W.h_cap);
+        wi = we;
     }
-    Counters h{};
-    CK(cudaMemcpyAsync(&h, dcnt, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    if (h.queue_drop || h.pulse_drop || h.hit_drop)
+    Counters h0{};
+    CK(cudaMemcpy(&h0, dcnt, sizeof(Counters), cudaMemcpyDeviceToHost));
+    if (h0.queue_drop || h0.pulse_drop || h0.hit_drop)
         return fail(c, GPET_ERR_CAPACITY, "a device buffer overflowed (queue/pulse/hit drops)");
-    c->n_pulses = pulses_used;
-    c->n_hits = c->record_hits ? hits_used : 0;
+    W.n_pulses = pulses_used;
+    W.n_hits = rec_hits ? hits_used : 0;
     float ms_digi = 0;
-    rc = digitize_and_finish(c, c->n_pulses, st, h, &ms_digi);
+    rc = digitize_work(c, W, prms, max_site, &tot, &ms_digi);
     if (rc) return rc;
     cudaEventRecord(c->ev[3], c->stream);
     CK(cudaEventSynchronize(c->ev[3]));
     float ms_tot = 0;
     cudaEventElapsedTime(&ms_tot, c->ev[0], c->ev[3]);
-    fill_stats(c, h, st);
-    st->n_decays = nd;
-    st->ms_total = ms_tot;
-    st->ms_source_phantom = ms_sp;
-    st->ms_source = ms_src;
-    st->ms_phantom = ms_ph;
-    st->ms_detector = ms_det;
-    st->ms_digitizer = ms_digi;
-    st->ms_coincidence = 0;
-    c->last = *st;
+    for (int s = 0; s < nsim; ++s) {
+        gpet_run_stats st = tot;
+        fill_stats(W.hcnt[s], &st);
+        if (!W.sim_hits[s]) st.n_hits = 0;
+        st.n_decays = nd[s];
+        st.ms_total = ms_tot;
+        st.ms_source_phantom = ms_src + ms_ph;
+        st.ms_source = ms_src;
+        st.ms_phantom = ms_ph;
+        st.ms_detector = ms_det;
+        st.ms_digitizer = ms_digi;
+        st.ms_coincidence = 0;
+        cs[s]->work = c->work;
+        cs[s]->res_sim = s;
+        cs[s]->have_results = true;
+        cs[s]->last = st;
+        if (s > 0) cs[s]->host_exits.clear();
+        if (stats) stats[s] = st;
+    }
     return GPET_OK;
+}
+
+extern "C" {
+
+int gpet_run(gpet_ctx* c, gpet_run_stats* st)
+{
+    if (!c) return GPET_ERR_ARG;
+    gpet_ctx* one[1] = {c};
+    return run_batch(one, 1, st);
+}
+
+int gpet_run_batched(gpet_ctx* const* ctxs, int32_t n, gpet_run_stats* stats)
+{
+    if (!ctxs || n < 1 || !ctxs[0]) return GPET_ERR_ARG;
+    return run_batch(ctxs, n, stats);
 }
 
 int gpet_digitize(gpet_ctx* c, const gpet_event* ev, const uint8_t* scat, const uint8_t* slot, int64_t n,
@@ -780,10 +950,14 @@ int gpet_digitize(gpet_ctx* c, const gpet_event* ev, const uint8_t* scat, const 
     gpet_run_stats local{};
     if (!st) st = &local;
     std::memset(st, 0, sizeof(*st));
-    int rc = grow_pulses(c, std::max<int64_t>(n, 1), 0);
+    Work& W = fresh_work(c);
+    W.nsims = 1;
+    W.sim_hits.assign(1, 0);
+    int rc = grow_pulses(c, W, std::max<int64_t>(n, 1), 0);
     if (rc) return rc;
-    CK(c->cnt.ensure(64 * 8));
-    CK(cudaMemsetAsync(c->cnt.p, 0, 64 * 8, c->stream));
+    CK(W.cnt.ensure(sizeof(Counters)));
+    CK(cudaMemsetAsync(W.cnt.p, 0, sizeof(Counters), c->stream));
+    CK(W.aux.ensure(64 * 8));
     std::vector<int32_t> I((size_t)n * 6);
     std::vector<double> T((size_t)n);
     std::vector<float> F((size_t)n * 4);
@@ -796,55 +970,69 @@ int gpet_digitize(gpet_ctx* c, const gpet_event* ev, const uint8_t* scat, const 
         if (slot[i] > 0x7f) return fail(c, GPET_ERR_ARG, "slot must be < 128");
         M[i] = (uint8_t)(slot[i] | (scat[i] ? 0x80 : 0));
     }
-    PulseDev P = pulse_view(c);
     for (int a = 0; a < 6; ++a)
-        CK(cudaMemcpyAsync(reinterpret_cast<int32_t*>(c->p_int.p) + a * c->p_cap, I.data() + a * n, n * 4,
-                           cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpyAsync(c->p_t.p, T.data(), n * 8, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(W.p_int.as<int32_t>() + a * W.p_cap, I.data() + a * n, n * 4, cudaMemcpyHostToDevice,
+                           c->stream));
+    CK(cudaMemcpyAsync(W.p_t.p, T.data(), n * 8, cudaMemcpyHostToDevice, c->stream));
     for (int a = 0; a < 4; ++a)
-        CK(cudaMemcpyAsync(reinterpret_cast<float*>(c->p_f.p) + a * c->p_cap, F.data() + a * n, n * 4,
-                           cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpyAsync(c->p_meta.p, M.data(), n, cudaMemcpyHostToDevice, c->stream));
-    (void)P;
-    c->n_pulses = n;
-    c->n_hits = 0;
-    Counters h{};
+        CK(cudaMemcpyAsync(W.p_f.as<float>() + a * W.p_cap, F.data() + a * n, n * 4, cudaMemcpyHostToDevice,
+                           c->stream));
+    CK(cudaMemcpyAsync(W.p_meta.p, M.data(), n, cudaMemcpyHostToDevice, c->stream));
+    W.n_pulses = n;
+    W.n_hits = 0;
+    std::vector<DigiParams> prms(1, digi_params(c));
+    int64_t max_site = std::max<int64_t>(1, (int64_t)c->geo.npanels * c->geo.moduleN * c->geo.crystalN);
     float ms_digi = 0;
-    rc = digitize_and_finish(c, n, st, h, &ms_digi);
+    rc = digitize_work(c, W, prms, max_site, st, &ms_digi);
     if (rc) return rc;
-    fill_stats(c, h, st);
+    fill_stats(W.hcnt[0], st);
+    st->n_pulses = n;
     st->ms_digitizer = ms_digi;
     st->ms_total = ms_digi;
+    c->res_sim = 0;
+    c->have_results = true;
+    c->host_exits.clear();
+    c->last = *st;
     return GPET_OK;
 }
 
+}  // extern "C"
+
 // ---------------------------------------------------------------- outputs
-static int copy_pulse_fields(gpet_ctx* c, const uint32_t* d_idx, int64_t n, bool blurred, std::vector<gpet_event>& out,
-                             std::vector<uint8_t>& meta)
+// Event records of pulses: `idx` lists pulse indices (device) or NULL for all
+static int gather(gpet_ctx* c, Work& W, const uint32_t* d_idx, int64_t n, bool blurred, std::vector<gpet_event>& out,
+                  std::vector<uint8_t>& meta)
 {
     out.resize((size_t)n);
     meta.resize((size_t)n);
     if (n == 0) return GPET_OK;
-    CK(c->g_ev.ensure((size_t)n * sizeof(EventRec)));
-    CK(c->g_meta.ensure((size_t)n));
-    PulseDev P = pulse_view(c);
-    if (gather_events(P, d_idx, n, blurred, c->dg, c->g_ev.as<EventRec>(), c->g_meta.as<uint8_t>(), c->stream))
+    CK(W.g_ev.ensure((size_t)n * sizeof(EventRec)));
+    CK(W.g_meta.ensure((size_t)n));
+    PulseDev P = pulse_view(W);
+    if (gather_events(P, d_idx, n, blurred, W.dg, W.g_ev.as<EventRec>(), W.g_meta.as<uint8_t>(), c->stream))
         return fail(c, GPET_ERR_CUDA, "gather of event records failed");
-    CK(cudaMemcpyAsync(out.data(), c->g_ev.p, (size_t)n * sizeof(EventRec), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(meta.data(), c->g_meta.p, (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(out.data(), W.g_ev.p, (size_t)n * sizeof(EventRec), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(meta.data(), W.g_meta.p, (size_t)n, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return GPET_OK;
 }
 
+static bool results(gpet_ctx* c) { return c->have_results && c->work; }
+
+extern "C" {
+
 int gpet_get_singles(gpet_ctx* c, gpet_event* buf, uint8_t* scat, int64_t cap, int64_t* n)
 {
     if (!c || !n) return GPET_ERR_ARG;
-    *n = c->have_results ? c->n_singles : 0;
+    if (!results(c)) { *n = 0; return GPET_OK; }
+    Work& W = *c->work;
+    const int64_t off = W.s_off[c->res_sim];
+    *n = W.s_off[c->res_sim + 1] - off;
     if (!buf || *n == 0) return GPET_OK;
     if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the singles");
     std::vector<gpet_event> ev;
     std::vector<uint8_t> m;
-    int rc = copy_pulse_fields(c, c->dg.single_idx, *n, true, ev, m);
+    int rc = gather(c, W, W.dg.single_idx + off, *n, true, ev, m);
     if (rc) return rc;
     std::memcpy(buf, ev.data(), sizeof(gpet_event) * (size_t)*n);
     if (scat)
@@ -852,26 +1040,45 @@ int gpet_get_singles(gpet_ctx* c, gpet_event* buf, uint8_t* scat, int64_t cap, i
     return GPET_OK;
 }
 
+// pulses (or hits) of this context's simulation: indices into the batch buffer
+static int own_rows(gpet_ctx* c, Work& W, const DevBuf& simbuf, int64_t total, std::vector<int64_t>& rows)
+{
+    rows.clear();
+    if (W.nsims <= 1) {
+        rows.resize((size_t)total);
+        for (int64_t i = 0; i < total; ++i) rows[i] = i;
+        return GPET_OK;
+    }
+    std::vector<int32_t> sim((size_t)total);
+    if (total) CK(cudaMemcpy(sim.data(), simbuf.p, (size_t)total * 4, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < total; ++i)
+        if (sim[i] == c->res_sim) rows.push_back(i);
+    return GPET_OK;
+}
+
 int gpet_get_pulses(gpet_ctx* c, gpet_event* buf, uint8_t* scat, uint8_t* slot, int64_t cap, int64_t* n)
 {
     if (!c || !n) return GPET_ERR_ARG;
-    *n = c->have_results ? c->n_pulses : 0;
+    if (!results(c)) { *n = 0; return GPET_OK; }
+    Work& W = *c->work;
+    *n = W.nsims <= 1 ? W.n_pulses : (int64_t)W.hcnt[c->res_sim].n_pulse;
     if (!buf || *n == 0) return GPET_OK;
     if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the pulses");
     std::vector<gpet_event> ev;
     std::vector<uint8_t> m;
-    int rc = copy_pulse_fields(c, nullptr, *n, false, ev, m);
+    int rc = gather(c, W, nullptr, W.n_pulses, false, ev, m);
     if (rc) return rc;
-    std::vector<int64_t> order((size_t)*n);
-    for (int64_t i = 0; i < *n; ++i) order[i] = i;
-    std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+    std::vector<int64_t> rows;
+    if ((rc = own_rows(c, W, W.p_sim, W.n_pulses, rows))) return rc;
+    std::sort(rows.begin(), rows.end(), [&](int64_t a, int64_t b) {
         if (ev[a].parn != ev[b].parn) return ev[a].parn < ev[b].parn;
         return (m[a] & 0x7f) < (m[b] & 0x7f);
     });
+    if ((int64_t)rows.size() != *n) return fail(c, GPET_ERR_CUDA, "pulse counts are inconsistent");
     for (int64_t i = 0; i < *n; ++i) {
-        buf[i] = ev[order[i]];
-        if (scat) scat[i] = (m[order[i]] & 0x80) ? 1 : 0;
-        if (slot) slot[i] = m[order[i]] & 0x7f;
+        buf[i] = ev[rows[i]];
+        if (scat) scat[i] = (m[rows[i]] & 0x80) ? 1 : 0;
+        if (slot) slot[i] = m[rows[i]] & 0x7f;
     }
     return GPET_OK;
 }
@@ -879,24 +1086,43 @@ int gpet_get_pulses(gpet_ctx* c, gpet_event* buf, uint8_t* scat, uint8_t* slot, 
 int gpet_get_coincidences(gpet_ctx* c, int64_t* pairs, uint8_t* klass, int64_t cap, int64_t* n)
 {
     if (!c || !n) return GPET_ERR_ARG;
-    *n = c->have_results ? c->n_coinc : 0;
+    if (!results(c)) { *n = 0; return GPET_OK; }
+    Work& W = *c->work;
+    const int64_t off = W.c_off[c->res_sim];
+    *n = W.c_off[c->res_sim + 1] - off;
     if (!pairs || *n == 0) return GPET_OK;
     if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the coincidences");
-    CK(cudaMemcpyAsync(pairs, c->dg.coinc_pairs, sizeof(int64_t) * 2 * (size_t)*n, cudaMemcpyDeviceToHost, c->stream));
-    if (klass) CK(cudaMemcpyAsync(klass, c->dg.coinc_class, (size_t)*n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(pairs, W.dg.coinc_pairs + 2 * off, sizeof(int64_t) * 2 * (size_t)*n, cudaMemcpyDeviceToHost,
+                       c->stream));
+    if (klass) CK(cudaMemcpyAsync(klass, W.dg.coinc_class + off, (size_t)*n, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    const int64_t soff = W.s_off[c->res_sim];
+    for (int64_t i = 0; i < 2 * *n; ++i) pairs[i] -= soff;
     return GPET_OK;
 }
 
 int gpet_get_hits(gpet_ctx* c, int32_t* ids, float* f, int64_t cap, int64_t* n)
 {
     if (!c || !n) return GPET_ERR_ARG;
-    *n = c->have_results ? c->n_hits : 0;
+    if (!results(c)) { *n = 0; return GPET_OK; }
+    Work& W = *c->work;
+    *n = W.nsims <= 1 ? W.n_hits : (int64_t)W.hcnt[c->res_sim].n_hit;
+    if (W.n_hits == 0 || !W.sim_hits[c->res_sim]) *n = 0;
     if ((!ids && !f) || *n == 0) return GPET_OK;
     if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the hits");
-    if (ids) CK(cudaMemcpyAsync(ids, c->h_id.p, (size_t)*n * 20, cudaMemcpyDeviceToHost, c->stream));
-    if (f) CK(cudaMemcpyAsync(f, c->h_f.p, (size_t)*n * 20, cudaMemcpyDeviceToHost, c->stream));
+    std::vector<int32_t> hid((size_t)W.n_hits * 5);
+    std::vector<float> hf((size_t)W.n_hits * 5);
+    CK(cudaMemcpyAsync(hid.data(), W.h_id.p, (size_t)W.n_hits * 20, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hf.data(), W.h_f.p, (size_t)W.n_hits * 20, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    std::vector<int64_t> rows;
+    int rc = own_rows(c, W, W.h_sim, W.n_hits, rows);
+    if (rc) return rc;
+    if ((int64_t)rows.size() != *n) return fail(c, GPET_ERR_CUDA, "hit counts are inconsistent");
+    for (int64_t i = 0; i < *n; ++i) {
+        if (ids) std::memcpy(ids + 5 * i, hid.data() + 5 * rows[i], 20);
+        if (f) std::memcpy(f + 5 * i, hf.data() + 5 * rows[i], 20);
+    }
     return GPET_OK;
 }
 
@@ -922,7 +1148,7 @@ static int append_file(gpet_ctx* c, const std::string& path, const void* p, size
 int gpet_write_outputs(gpet_ctx* c, const char* dir)
 {
     if (!c || !dir) return GPET_ERR_ARG;
-    if (!c->have_results) return fail(c, GPET_ERR_ARG, "no results to write");
+    if (!results(c)) return fail(c, GPET_ERR_ARG, "no results to write");
     std::string d(dir);
     int64_t n = 0;
     int rc;
@@ -955,6 +1181,10 @@ int gpet_write_outputs(gpet_ctx* c, const char* dir)
     if ((rc = append_file(c, d + "/coincidences_class.dat", cl.data(), cl.size()))) return rc;
     return GPET_OK;
 }
+
+}  // extern "C"
+
+extern "C" {
 
 // ---------------------------------------------------------------- introspection
 int gpet_get_panels(gpet_ctx* c, float* out, int32_t cap, int32_t* np)

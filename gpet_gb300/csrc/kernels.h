@@ -1,15 +1,29 @@
 // kernels.h - device buffers and kernel entry points shared by the host
 // runtime (gpet_api.cpp) and the kernel translation units.
 #pragma once
+#include <cstddef>
+
 #include "device.cuh"
 
 namespace gpet {
+
+// A wave of decays: global indices [g0[i], g0[i+1]) are decays d0[i] ..
+// of simulation sim[i] (sims[] in device memory).
+constexpr int kMaxSeg = 128;
+struct Wave {
+    const SimDesc* sims;
+    const int64_t* g0;            // [nseg + 1]
+    const int64_t* d0;            // [nseg]
+    const int32_t* sim;           // [nseg]
+    int32_t nseg;
+    int64_t n;                    // decays in the wave
+};
 
 // detector queue, structure of arrays (cap entries each)
 struct QueueDev {
     float* f;                     // [7][cap]: local x, y, z, ux, uy, uz, E
     double* t;                    // [cap]
-    int32_t* i;                   // [4][cap]: panel index, parn, event id, phantom scatters
+    int32_t* i;                   // [5][cap]: panel index, parn, event id, phantom scatters, simulation
     unsigned long long* count;
     int64_t cap;
 };
@@ -20,6 +34,7 @@ struct PulseDev {
     double* t;
     float *E, *x, *y, *z;
     uint8_t* meta;                // slot | 0x80 if the photon scattered in the phantom
+    int32_t* sim;                 // simulation of each pulse (NULL: all simulation 0)
     unsigned long long* count;
     int64_t cap;
 };
@@ -27,6 +42,7 @@ struct PulseDev {
 struct HitDev {
     int32_t* id;                  // [cap][5]
     float* f;                     // [cap][5]
+    int32_t* sim;                 // [cap] (may be NULL)
     unsigned long long* count;
     int64_t cap;
 };
@@ -34,7 +50,44 @@ struct HitDev {
 struct Counters {
     unsigned long long pairs, entered, stepcap, ph_steps, det_steps, overflow, pulse_drop, hit_drop, queue_drop;
     unsigned long long n_thr, n_dead, n_single, n_coinc, n_true, n_scat, n_rand, n_mult;
+    unsigned long long n_pulse, n_hit;
 };
+
+// cnt[sim].field += v, lanes of a warp grouped by simulation (all lanes of the
+// warp must call it together)
+__device__ __forceinline__ void add_by_sim(Counters* cnt, int sim, int field, unsigned v)
+{
+    const unsigned peers = __match_any_sync(0xffffffffu, sim);
+    const unsigned tot = __reduce_add_sync(peers, v);
+    if (tot && (threadIdx.x & 31) == __ffs(peers) - 1)
+        atomicAdd(reinterpret_cast<unsigned long long*>(cnt + sim) + field, (unsigned long long)tot);
+}
+
+#define CF(name) ((int)(offsetof(Counters, name) / sizeof(unsigned long long)))
+
+// per-thread counter for the simulation the thread is working on; flushed
+// when the simulation changes (rare: waves are contiguous per simulation) and
+// once per warp at the end
+struct SimTally {
+    int sim = -1;
+    unsigned v = 0;
+    __device__ __forceinline__ void add(Counters* cnt, int field, int s, unsigned x)
+    {
+        if (s != sim) {
+            if (v) atomicAdd(reinterpret_cast<unsigned long long*>(cnt + sim) + field, (unsigned long long)v);
+            sim = s;
+            v = 0;
+        }
+        v += x;
+    }
+    __device__ __forceinline__ void flush(Counters* cnt, int field)
+    {
+        add_by_sim(cnt, sim < 0 ? 0 : sim, field, v);
+        v = 0;
+    }
+};
+
+
 
 // phantom exit record (48 bytes), one per photon slot
 struct ExitRec {
@@ -65,11 +118,27 @@ struct PairBuf {
     int64_t cap;
 };
 
-__global__ void k_source(const SimDesc* __restrict__ gS, int64_t d0, int64_t n, PairBuf pb, Counters* cnt);
-__global__ void k_phantom(const SimDesc* __restrict__ gS, int64_t d0, int64_t nd, PairBuf pb,
-                          unsigned long long* work, QueueDev q, ExitRec* exits, Counters* cnt);
-__global__ void k_detector(const SimDesc* __restrict__ gS, QueueDev q, PulseDev P, HitDev H, int rec_hits,
+// Counters is an array indexed by simulation; kMulti selects per-thread
+// simulation descriptors (several simulations in one wave)
+template <bool kMulti> __global__ void k_source(Wave w, PairBuf pb, Counters* cnt);
+template <bool kMulti>
+__global__ void k_phantom(Wave w, PairBuf pb, unsigned long long* work, QueueDev q, ExitRec* exits, Counters* cnt);
+template <bool kMulti>
+__global__ void k_detector(const SimDesc* sims, QueueDev q, PulseDev P, HitDev H, int rec_hits, Counters* cnt);
+
+// host-side launchers (transport.cu): `multi` picks the kMulti instance,
+// smem is the dynamic shared memory (panels of the one simulation, or 0)
+cudaError_t launch_source(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const Wave& w, const PairBuf& pb,
+                          Counters* cnt);
+cudaError_t launch_phantom(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const Wave& w,
+                           const PairBuf& pb, unsigned long long* work, const QueueDev& q, ExitRec* exits,
                            Counters* cnt);
+cudaError_t launch_detector(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const SimDesc* sims,
+                            const QueueDev& q, const PulseDev& P, const HitDev& H, int rec_hits, Counters* cnt);
+// resident k_phantom blocks per SM at 256 threads and `smem` bytes
+cudaError_t phantom_blocks_per_sm(bool multi, size_t smem, int* blocks);
+// cudaSuccess when the transport kernels have an image for the current device
+cudaError_t transport_kernels_loadable();
 
 // ---- digitizer building blocks (digitizer.cu), all stream-ordered
 struct DigiScratch {
@@ -114,30 +183,37 @@ __global__ void k_scan_down(const uint32_t* in, int64_t n, const uint32_t* aux, 
 __global__ void k_radix_hist(const uint64_t* keys, int64_t n, int shift, uint32_t* hist, int64_t nblocks);
 __global__ void k_radix_scatter(const uint64_t* kin, const uint32_t* vin, int64_t n, int shift, const uint32_t* off,
                                 int64_t nblocks, uint64_t* kout, uint32_t* vout);
-__global__ void k_blur_threshold(PulseDev P, int64_t n, DigiParams prm, float* Eb, float* xb, float* yb, float* zb,
-                                 int32_t* site, uint32_t* sel, unsigned long long* nsel);
+__global__ void k_blur_threshold(PulseDev P, int64_t n, const DigiParams* prms, float* Eb, float* xb, float* yb,
+                                 float* zb, int32_t* site, uint32_t* sel, unsigned long long* nsel);
 __global__ void k_time_keys(const uint32_t* sel, int64_t m, const double* t, uint64_t* key, uint32_t* val);
 __global__ void k_tie_fix(const uint64_t* key, uint32_t* idx, int64_t m, const int32_t* parn, const uint8_t* meta);
-__global__ void k_site_keys(const uint32_t* torder, int64_t m, const int32_t* site, uint64_t* key, uint32_t* val);
-__global__ void k_deadtime(const uint32_t* sorder, int64_t m, const int32_t* site, const double* t, double tau,
-                           int dtype, uint32_t* flags, unsigned long long* nalive);
-__global__ void k_window_pred(const uint32_t* torder, int64_t m, const uint32_t* flags, const float* Eb, float lo,
-                              float hi, uint32_t* pred);
+__global__ void k_site_keys(const uint32_t* torder, int64_t m, const int32_t* site, const int32_t* psim,
+                            uint64_t* key, uint32_t* val);
+__global__ void k_deadtime(const uint32_t* sorder, int64_t m, const int32_t* site, const int32_t* psim,
+                           const double* t, const DigiParams* prms, uint32_t* flags, Counters* cnt);
+__global__ void k_window_pred(const uint32_t* torder, int64_t m, const uint32_t* flags, const float* Eb,
+                              const int32_t* psim, const DigiParams* prms, uint32_t* pred, Counters* cnt);
+__global__ void k_count_by_sim(const uint32_t* order, int64_t m, const int32_t* psim, Counters* cnt, int field);
 __global__ void k_compact(const uint32_t* torder, const uint32_t* pred, const uint32_t* off, int64_t m,
                           uint32_t* out);
-__global__ void k_coinc_count(const uint32_t* sidx, int64_t s, const double* t, const int32_t* pann, double W,
-                              int policy, uint32_t* wcount, uint32_t* wend, unsigned long long* nmult);
+__global__ void k_coinc_count(const uint32_t* sidx, int64_t s, const double* t, const int32_t* pann,
+                              const int32_t* psim, const DigiParams* prms, uint32_t* wcount, uint32_t* wend,
+                              Counters* cnt);
 __global__ void k_coinc_write(const uint32_t* sidx, int64_t s, const uint32_t* wend, const uint32_t* off,
-                              const int32_t* pann, const int32_t* eid, const uint8_t* meta, int policy,
-                              int64_t* pairs, uint8_t* klass, int64_t cap, unsigned long long* ncls);
+                              const int32_t* pann, const int32_t* eid, const uint8_t* meta, const int32_t* psim,
+                              const DigiParams* prms, int64_t* pairs, uint8_t* klass, int64_t cap, Counters* cnt);
 __global__ void k_gather_events(PulseDev P, const uint32_t* idx, int64_t n, int blurred, const float* Eb,
                                 const float* xb, const float* yb, const float* zb, const int32_t* site,
                                 EventRec* out, uint8_t* meta);
 
 // Runs blur .. coincidences on n pulses already in P (device), stream-ordered;
-// returns 0 or a GPET_ERR code. Results land in D.single_idx / D.coinc_*,
-// counts in cnt. `launches` accumulates the kernel launch count.
-int digitize_device(const PulseDev& P, int64_t n, const DigiParams& prm, DigiScratch& D, Counters* cnt,
-                    cudaStream_t s, int64_t* launches, int64_t* n_singles_out, int64_t* n_coinc_out);
+// returns 0 or a GPET_ERR code. Pulses of nsims simulations (P.sim) are
+// digitized in one pass with parameters d_prms[sim] (device); singles come out
+// in (simulation, t) order in D.single_idx, coincidences in D.coinc_*,
+// per-simulation counts in d_cnt[sim]. `launches` accumulates kernel launches.
+// max_site bounds every site number (panels x modules x crystals).
+int digitize_device(const PulseDev& P, int64_t n, const DigiParams* d_prms, int nsims, int64_t max_site,
+                    DigiScratch& D, Counters* d_cnt, cudaStream_t s, int64_t* launches, int64_t* n_singles_out,
+                    int64_t* n_coinc_out);
 
 }  // namespace gpet

@@ -9,6 +9,8 @@
 // one atomic per warp) into the detector queue; k_detector runs one thread per
 // queued photon through the panel, applies the per-photon adder and readout,
 // and appends pulses and hits (one atomic per warp).
+#include <cstddef>
+
 #include "kernels.h"
 
 namespace gpet {
@@ -36,6 +38,36 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
+}
+
+// segment table of a wave, staged in shared memory
+struct SegSmem {
+    int64_t g0[kMaxSeg + 1];
+    int64_t d0[kMaxSeg];
+    int32_t sim[kMaxSeg];
+    int32_t nseg;
+};
+
+__device__ __forceinline__ void load_segs(const Wave& w, SegSmem& sg)
+{
+    for (int i = threadIdx.x; i <= w.nseg; i += blockDim.x) sg.g0[i] = w.g0[i];
+    for (int i = threadIdx.x; i < w.nseg; i += blockDim.x) {
+        sg.d0[i] = w.d0[i];
+        sg.sim[i] = w.sim[i];
+    }
+    if (threadIdx.x == 0) sg.nseg = w.nseg;
+}
+
+// segment holding global decay index g (g0 ascending)
+__device__ __forceinline__ int seg_of(const SegSmem& sg, int64_t g)
+{
+    int lo = 0, hi = sg.nseg - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (sg.g0[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
 // source stage of one decay (setPosition gPET_kernals.cu:483-561 for a source
@@ -81,39 +113,53 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2])
 }
 
 // source stage: one thread per decay, the emitted pair (or PSF photon) goes
-// to a structure-of-arrays buffer sized to stay in L2
-__global__ void __launch_bounds__(256) k_source(const SimDesc* __restrict__ gS, int64_t d0, int64_t n, PairBuf pb,
-                                                Counters* cnt)
+// to a structure-of-arrays buffer sized to stay in L2. kMulti: the decays of a
+// wave belong to several simulations and each thread reads its own
+// simulation's descriptor; otherwise the one descriptor is staged in shared
+// memory.
+template <bool kMulti>
+__global__ void __launch_bounds__(256) k_source(Wave w, PairBuf pb, Counters* cnt)
 {
-    __shared__ SimDesc S;
+    __shared__ SimDesc sS;
+    __shared__ SegSmem sg;
     extern __shared__ float sP[];
-    load_sim(gS, S, sP);
-    unsigned long long n_pairs = 0;
+    if (!kMulti) load_sim(w.sims, sS, sP);
+    load_segs(w, sg);
+    __syncthreads();
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
-        Photon ph[2];
-        int nph = sample_decay(S, d0 + j, ph);
-        if (nph == 2) n_pairs++;
-        pb.nph[j] = (uint8_t)nph;
-        if (nph > 0) {
-            pb.f[0 * pb.cap + j] = ph[0].x[0];
-            pb.f[1 * pb.cap + j] = ph[0].x[1];
-            pb.f[2 * pb.cap + j] = ph[0].x[2];
-            pb.f[3 * pb.cap + j] = ph[0].u[0];
-            pb.f[4 * pb.cap + j] = ph[0].u[1];
-            pb.f[5 * pb.cap + j] = ph[0].u[2];
-            pb.f[9 * pb.cap + j] = ph[0].E;
-            pb.t[j] = ph[0].t;
-        }
-        if (nph > 1) {
-            pb.f[6 * pb.cap + j] = ph[1].u[0];
-            pb.f[7 * pb.cap + j] = ph[1].u[1];
-            pb.f[8 * pb.cap + j] = ph[1].u[2];
-            pb.f[10 * pb.cap + j] = ph[1].E;
+    SimTally pairs;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < w.n; base += stride) {
+        const int64_t j = base + threadIdx.x;
+        int nph = 0;
+        int sim = 0;
+        if (j < w.n) {
+            const int sgi = seg_of(sg, j);
+            sim = sg.sim[sgi];
+            const int64_t d = sg.d0[sgi] + (j - sg.g0[sgi]);
+            const SimDesc& S = kMulti ? w.sims[sim] : sS;
+            Photon ph[2];
+            nph = sample_decay(S, d, ph);
+            pb.nph[j] = (uint8_t)nph;
+            if (nph > 0) {
+                pb.f[0 * pb.cap + j] = ph[0].x[0];
+                pb.f[1 * pb.cap + j] = ph[0].x[1];
+                pb.f[2 * pb.cap + j] = ph[0].x[2];
+                pb.f[3 * pb.cap + j] = ph[0].u[0];
+                pb.f[4 * pb.cap + j] = ph[0].u[1];
+                pb.f[5 * pb.cap + j] = ph[0].u[2];
+                pb.f[9 * pb.cap + j] = ph[0].E;
+                pb.t[j] = ph[0].t;
+            }
+            if (nph > 1) {
+                pb.f[6 * pb.cap + j] = ph[1].u[0];
+                pb.f[7 * pb.cap + j] = ph[1].u[1];
+                pb.f[8 * pb.cap + j] = ph[1].u[2];
+                pb.f[10 * pb.cap + j] = ph[1].E;
+            }
+            pairs.add(cnt, CF(pairs), sim, nph == 2 ? 1u : 0u);
         }
     }
-    n_pairs = warp_sum(n_pairs);
-    if ((threadIdx.x & 31) == 0 && n_pairs) atomicAdd(&cnt->pairs, n_pairs);
+    pairs.flush(cnt, CF(pairs));
 }
 
 // a photon that has left the phantom (or stopped), waiting for the panel search
@@ -121,9 +167,12 @@ struct FinRec {
     float x, y, z, ux, uy, uz, E;
     int32_t nscat;
     double t;
-    long long p;
+    long long p;      // photon index within the wave
+    long long d;      // decay index within its simulation
     int32_t status;
     float tf;
+    int32_t sim;
+    int32_t steps;    // Woodcock steps of this photon
 };
 
 constexpr int kPhWarps = 8;      // warps per k_phantom block (256 threads)
@@ -133,27 +182,30 @@ constexpr int kFinCap = 64;      // finished photons staged per warp
 // (or was absorbed) takes the next photon from a shared counter at once, so
 // the lanes of a warp stay busy while histories differ in length. Finished
 // photons are staged in shared memory and taken through the panel search 32
-// at a time, one per lane. Photon p of the stage is photon (p & 1) of decay
-// d0 + (p >> 1).
-__global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ gS, int64_t d0, int64_t nd,
-                                                    PairBuf pb, unsigned long long* work, QueueDev q,
+// at a time, one per lane. Photon p of the wave is photon (p & 1) of the
+// wave's decay p >> 1. kMulti as for k_source.
+template <bool kMulti>
+__global__ void __launch_bounds__(256, 4) k_phantom(Wave w, PairBuf pb, unsigned long long* work, QueueDev q,
                                                     ExitRec* exits, Counters* cnt)
 {
-    __shared__ SimDesc S;
+    __shared__ SimDesc sS;
+    __shared__ SegSmem sg;
     __shared__ FinRec fbuf[kPhWarps][kFinCap];
     extern __shared__ float sP[];
-    load_sim(gS, S, sP);
+    if (!kMulti) load_sim(w.sims, sS, sP);
+    load_segs(w, sg);
+    __syncthreads();
     const unsigned lt = lanemask_lt();
     const int lane = threadIdx.x & 31;
     FinRec* fb = fbuf[threadIdx.x >> 5];
-    const int64_t nphot = 2 * nd;
-    unsigned long long n_entered = 0, n_steps = 0, n_cap = 0, n_drop = 0;
+    const int64_t nphot = 2 * w.n;
     int fcount = 0;   // staged photons of this warp (warp-uniform)
 
     // panel search + queue append for the staged entries [0, k), one per lane
     auto drain = [&](int k) {
         const bool has = lane < k;
         FinRec r;
+        r.sim = 0;
         if (has) r = fb[lane];
         Photon ph;
         Local L;
@@ -162,7 +214,12 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ 
             ph.x[0] = r.x; ph.x[1] = r.y; ph.x[2] = r.z;
             ph.u[0] = r.ux; ph.u[1] = r.uy; ph.u[2] = r.uz;
             ph.E = r.E; ph.t = r.t; ph.tf = r.tf; ph.nscat = r.nscat;
-            entered = r.status == 1 && enter_panel(sP, S.npanels, ph, L);
+            if (kMulti) {
+                const SimDesc& S = w.sims[r.sim];
+                entered = r.status == 1 && enter_panel(S.panels, S.npanels, ph, L);
+            } else {
+                entered = r.status == 1 && enter_panel(sP, sS.npanels, ph, L);
+            }
         }
         const unsigned m = __ballot_sync(0xffffffffu, entered);
         if (m) {
@@ -173,7 +230,7 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ 
             if (entered) {
                 const unsigned long long jq = b + __popc(m & lt);
                 if (jq < (unsigned long long)q.cap) {
-                    const int64_t d = d0 + (r.p >> 1);
+                    const int64_t d = r.d;
                     q.f[0 * q.cap + jq] = L.x[0];
                     q.f[1 * q.cap + jq] = L.x[1];
                     q.f[2 * q.cap + jq] = L.x[2];
@@ -186,12 +243,15 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ 
                     q.i[1 * q.cap + jq] = (int32_t)(2 * d + (r.p & 1));
                     q.i[2 * q.cap + jq] = (int32_t)d;
                     q.i[3 * q.cap + jq] = r.nscat;
-                    n_entered++;
+                    q.i[4 * q.cap + jq] = r.sim;
                 } else {
-                    n_drop++;
+                    entered = false;
+                    atomicAdd(&cnt->queue_drop, 1ull);
                 }
             }
         }
+        add_by_sim(cnt, r.sim, CF(entered), entered ? 1u : 0u);
+        add_by_sim(cnt, r.sim, CF(ph_steps), has ? (unsigned)r.steps : 0u);
         if (has && exits) {
             ExitRec e;
             e.x = r.x; e.y = r.y; e.z = r.z; e.ux = r.ux; e.uy = r.uy; e.uz = r.uz;
@@ -204,7 +264,8 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ 
     };
 
     bool active = false, exhausted = false;
-    int64_t p = 0;
+    int64_t p = 0, d = 0;
+    int sim = 0;
     int steps = 0;
     Photon ph;
     Stream st;
@@ -224,6 +285,9 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ 
                 } else {
                     const int64_t j = p >> 1;
                     const int k = (int)(p & 1);
+                    const int sgi = seg_of(sg, j);
+                    sim = sg.sim[sgi];
+                    d = sg.d0[sgi] + (j - sg.g0[sgi]);
                     const int nph = pb.nph[j];
                     if (k < nph) {
                         ph.x[0] = pb.f[0 * pb.cap + j];
@@ -236,7 +300,8 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ 
                         ph.t = pb.t[j];
                         ph.tf = 0.0f;
                         ph.nscat = 0;
-                        st_init(st, S.key0, S.key1, kTagPhantom + k, (uint64_t)(d0 + j));
+                        const SimDesc& S = kMulti ? w.sims[sim] : sS;
+                        st_init(st, S.key0, S.key1, kTagPhantom + k, (uint64_t)d);
                         steps = 0;
                         active = true;
                     } else if (exits) {
@@ -252,7 +317,7 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ 
         // one Woodcock step (photon(), gPET_kernals.cu:274-338)
         int status = -1;   // -1 continue, 0 absorbed, 1 escaped, 3 step cap
         if (active) {
-            n_steps++;
+            const SimDesc& S = kMulti ? w.sims[sim] : sS;
             steps++;
             float lammin = wck_at(S.wck_ph, S.wck_e0, S.wck_ide, ph.E);
             float s = -lammin * dm_logf(st_u(st));
@@ -305,9 +370,10 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ 
                 FinRec r;
                 r.x = ph.x[0]; r.y = ph.x[1]; r.z = ph.x[2];
                 r.ux = ph.u[0]; r.uy = ph.u[1]; r.uz = ph.u[2];
-                r.E = ph.E; r.nscat = ph.nscat; r.t = ph.t; r.p = p; r.status = status; r.tf = ph.tf;
+                r.E = ph.E; r.nscat = ph.nscat; r.t = ph.t; r.p = p; r.d = d; r.status = status; r.tf = ph.tf;
+                r.sim = sim; r.steps = steps;
                 fb[fcount + __popc(mf & lt)] = r;
-                if (status == 3) n_cap++;
+                if (status == 3) atomicAdd(&cnt[sim].stepcap, 1ull);
                 active = false;
             }
             fcount += __popc(mf);
@@ -325,14 +391,6 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const SimDesc* __restrict__ 
         }
     }
     if (fcount > 0) drain(fcount);
-    n_entered = warp_sum(n_entered); n_steps = warp_sum(n_steps);
-    n_cap = warp_sum(n_cap); n_drop = warp_sum(n_drop);
-    if (lane == 0) {
-        if (n_entered) atomicAdd(&cnt->entered, n_entered);
-        if (n_steps) atomicAdd(&cnt->ph_steps, n_steps);
-        if (n_cap) atomicAdd(&cnt->stepcap, n_cap);
-        if (n_drop) atomicAdd(&cnt->queue_drop, n_drop);
-    }
 }
 
 // ------------------------------------------------------------- detector
@@ -396,18 +454,24 @@ __device__ __forceinline__ int readout(const SimDesc& S, PEvent* ev, int n)
     return k;
 }
 
-__global__ void __launch_bounds__(256) k_detector(const SimDesc* __restrict__ gS, QueueDev q, PulseDev P,
+// kMulti as for k_source: the queue holds photons of several simulations
+template <bool kMulti>
+__global__ void __launch_bounds__(256) k_detector(const SimDesc* sims, QueueDev q, PulseDev P,
                                                   HitDev H, int rec_hits, Counters* cnt)
 {
-    __shared__ SimDesc S;
+    __shared__ SimDesc sS;
     extern __shared__ float sP[];
-    load_sim(gS, S, sP);
+    if (!kMulti) {
+        load_sim(sims, sS, sP);
+        __syncthreads();
+    }
     unsigned long long nq = *q.count;
     if (nq > (unsigned long long)q.cap) nq = (unsigned long long)q.cap;
     const int64_t n = (int64_t)nq;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
-    unsigned long long n_steps = 0, n_over = 0, n_cap = 0, n_pdrop = 0, n_hdrop = 0;
+    unsigned long long n_pdrop = 0, n_hdrop = 0;
+    SimTally t_steps, t_cap, t_over, t_pulse, t_hit;
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
         const int64_t j = base + threadIdx.x;
         const bool valid = j < n;
@@ -416,9 +480,12 @@ __global__ void __launch_bounds__(256) k_detector(const SimDesc* __restrict__ gS
         int nh = 0;
         int32_t hid[kMaxHits][4];
         float hf[kMaxHits][5];
-        int32_t parn = 0, eid = 0, scat = 0;
+        int32_t parn = 0, eid = 0, scat = 0, sim = 0;
         bool overflow = false;
+        unsigned nsteps = 0, capped = 0;
         if (valid) {
+            sim = q.i[4 * q.cap + j];
+            const SimDesc& S = kMulti ? sims[sim] : sS;
             Local L;
             L.x[0] = q.f[0 * q.cap + j]; L.x[1] = q.f[1 * q.cap + j]; L.x[2] = q.f[2 * q.cap + j];
             L.u[0] = q.f[3 * q.cap + j]; L.u[1] = q.f[4 * q.cap + j]; L.u[2] = q.f[5 * q.cap + j];
@@ -429,14 +496,14 @@ __global__ void __launch_bounds__(256) k_detector(const SimDesc* __restrict__ gS
             parn = q.i[1 * q.cap + j];
             eid = q.i[2 * q.cap + j];
             scat = q.i[3 * q.cap + j];
-            const float* Pn = sP + L.panel * kPanelStride;
+            const float* Pn = kMulti ? S.panels + L.panel * kPanelStride : sP + L.panel * kPanelStride;
             const int32_t pann = (int32_t)Pn[30];
             Stream st;
             st_init(st, S.key0, S.key1, kTagDet + (parn & 1), (uint64_t)(uint32_t)eid);
             // photonde transport loop, gPET_kernals.cu:1013-1193
             int step;
             for (step = 0; step < kMaxSteps; ++step) {
-                n_steps++;
+                nsteps++;
                 float lammin = wck_at(S.wck_det, S.wck_e0, S.wck_ide, L.E);
                 float s = -lammin * dm_logf(st_u(st));
                 L.x[0] += s * L.u[0];
@@ -517,9 +584,13 @@ __global__ void __launch_bounds__(256) k_detector(const SimDesc* __restrict__ gS
                 }
                 break;
             }
-            if (step == kMaxSteps) n_cap++;
+            if (step == kMaxSteps) capped = 1;
             if (nev) nev = readout(S, ev, nev);
-            if (overflow) n_over++;
+            t_steps.add(cnt, CF(det_steps), sim, nsteps);
+            t_cap.add(cnt, CF(stepcap), sim, capped);
+            t_over.add(cnt, CF(overflow), sim, overflow ? 1u : 0u);
+            t_pulse.add(cnt, CF(n_pulse), sim, (unsigned)nev);
+            t_hit.add(cnt, CF(n_hit), sim, rec_hits ? (unsigned)nh : 0u);
         }
         // append pulses and hits, one atomic per warp
         int inc = nev;
@@ -540,6 +611,7 @@ __global__ void __launch_bounds__(256) k_detector(const SimDesc* __restrict__ gS
                 P.siten[o] = ev[i].siten; P.eventid[o] = eid; P.t[o] = ev[i].t;
                 P.E[o] = ev[i].E; P.x[o] = ev[i].x; P.y[o] = ev[i].y; P.z[o] = ev[i].z;
                 P.meta[o] = (uint8_t)(i | (scat ? 0x80 : 0));
+                if (P.sim) P.sim[o] = sim;
             }
         }
         if (rec_hits) {
@@ -561,19 +633,65 @@ __global__ void __launch_bounds__(256) k_detector(const SimDesc* __restrict__ gS
                     H.id[5 * o + 1] = hid[i][0]; H.id[5 * o + 2] = hid[i][1]; H.id[5 * o + 3] = hid[i][2];
                     H.id[5 * o + 4] = hid[i][3];
                     for (int c = 0; c < 5; ++c) H.f[5 * o + c] = hf[i][c];
+                    if (H.sim) H.sim[o] = sim;
                 }
             }
         }
     }
-    n_steps = warp_sum(n_steps); n_over = warp_sum(n_over); n_cap = warp_sum(n_cap);
+    t_steps.flush(cnt, CF(det_steps));
+    t_cap.flush(cnt, CF(stepcap));
+    t_over.flush(cnt, CF(overflow));
+    t_pulse.flush(cnt, CF(n_pulse));
+    t_hit.flush(cnt, CF(n_hit));
     n_pdrop = warp_sum(n_pdrop); n_hdrop = warp_sum(n_hdrop);
     if (lane == 0) {
-        if (n_steps) atomicAdd(&cnt->det_steps, n_steps);
-        if (n_over) atomicAdd(&cnt->overflow, n_over);
-        if (n_cap) atomicAdd(&cnt->stepcap, n_cap);
         if (n_pdrop) atomicAdd(&cnt->pulse_drop, n_pdrop);
         if (n_hdrop) atomicAdd(&cnt->hit_drop, n_hdrop);
     }
 }
+
+cudaError_t launch_source(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const Wave& w, const PairBuf& pb,
+                          Counters* cnt)
+{
+    if (multi) k_source<true><<<blocks, 256, smem, s>>>(w, pb, cnt);
+    else k_source<false><<<blocks, 256, smem, s>>>(w, pb, cnt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phantom(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const Wave& w,
+                           const PairBuf& pb, unsigned long long* work, const QueueDev& q, ExitRec* exits,
+                           Counters* cnt)
+{
+    if (multi) k_phantom<true><<<blocks, 256, smem, s>>>(w, pb, work, q, exits, cnt);
+    else k_phantom<false><<<blocks, 256, smem, s>>>(w, pb, work, q, exits, cnt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_detector(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const SimDesc* sims,
+                            const QueueDev& q, const PulseDev& P, const HitDev& H, int rec_hits, Counters* cnt)
+{
+    if (multi) k_detector<true><<<blocks, 256, smem, s>>>(sims, q, P, H, rec_hits, cnt);
+    else k_detector<false><<<blocks, 256, smem, s>>>(sims, q, P, H, rec_hits, cnt);
+    return cudaGetLastError();
+}
+
+cudaError_t phantom_blocks_per_sm(bool multi, size_t smem, int* blocks)
+{
+    return multi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_phantom<true>, 256, smem)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_phantom<false>, 256, smem);
+}
+
+cudaError_t transport_kernels_loadable()
+{
+    cudaFuncAttributes fa;
+    return cudaFuncGetAttributes(&fa, k_phantom<false>);
+}
+
+template __global__ void k_source<false>(Wave, PairBuf, Counters*);
+template __global__ void k_source<true>(Wave, PairBuf, Counters*);
+template __global__ void k_phantom<false>(Wave, PairBuf, unsigned long long*, QueueDev, ExitRec*, Counters*);
+template __global__ void k_phantom<true>(Wave, PairBuf, unsigned long long*, QueueDev, ExitRec*, Counters*);
+template __global__ void k_detector<false>(const SimDesc*, QueueDev, PulseDev, HitDev, int, Counters*);
+template __global__ void k_detector<true>(const SimDesc*, QueueDev, PulseDev, HitDev, int, Counters*);
 
 }  // namespace gpet

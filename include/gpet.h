@@ -112,6 +112,17 @@ int gpet_set_source_psf(gpet_ctx* ctx, const double* rec8, int64_t n, int ptype)
 /* Simulate the configured source and digitize: sampleParticle (gPET.cu:201-437)
  * or simulateParticle (gPET.cu:13-199) followed by the coincidence sorter. */
 int gpet_run(gpet_ctx* ctx, gpet_run_stats* stats);
+/* No counterpart in the reference (one simulation per process there).
+ * Runs n independent simulations (contexts on one device, each fully loaded;
+ * each keeps its own tables, phantom, geometry, source, seed and digitizer
+ * settings) as one job: their decays are concatenated into shared waves so
+ * that many small simulations fill the GPU together, and one digitizer pass
+ * sorts all pulses by (simulation, time). Afterwards each context reads its
+ * own results with the gpet_get_* calls, identical bit for bit to what
+ * gpet_run on that context alone gives. stats[i] (may be NULL) receives each
+ * simulation's counts; the timings are those of the whole job. record_exits
+ * must be 0 when n > 1. */
+int gpet_run_batched(gpet_ctx* const* ctxs, int32_t n, gpet_run_stats* stats);
 /* Digitizer + coincidence sorter alone on a caller pulse list (the digitizer
  * chain of gPET.cu:385-424): scat[i] != 0 marks a photon that scattered in the
  * phantom, slot[i] is the pulse's index within its photon's readout list. */
