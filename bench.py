@@ -247,10 +247,25 @@ def run_ours(args):
         ms_max, coinc_all = combine_ranks(tot["ms"], tot["coinc"], dist,
                                           "cpu" if args.gloo else "cuda:%d" % local)
         value = coinc_all / (ms_max * 1e-3)
-        # e2e through the C ABI with host buffers
-        mat, den = F.read_phantom(os.path.join(d, "phantom_mat.dat"), os.path.join(d, "phantom_den.dat"),
-                                  (128, 128, 128))
+        # e2e through the C ABI with host buffers: the phantom goes up from
+        # pinned host memory, singles and coincidences come back into pinned
+        # host memory, every step
+        mat0, den0 = F.read_phantom(os.path.join(d, "phantom_mat.dat"), os.path.join(d, "phantom_den.dat"),
+                                    (128, 128, 128))
         cfg = F.read_config(sc.config_path)
+
+        def pinned(shape, dtype):
+            nb = int(np.prod(shape)) * np.dtype(dtype).itemsize
+            return torch.empty(nb, dtype=torch.uint8, pin_memory=True).numpy().view(dtype).reshape(shape)
+
+        mat = pinned(mat0.shape, np.int32)
+        den = pinned(den0.shape, np.float32)
+        mat[...] = mat0
+        den[...] = den0
+        cap_s = int(2 * tot["singles"] / max(1, args.steps)) + 1024
+        cap_c = int(2 * tot["coinc"] / max(1, args.steps)) + 1024
+        out_s = (pinned((cap_s,), F.EVENT_DTYPE), pinned((cap_s,), np.uint8))
+        out_c = (pinned((cap_c, 2), np.int64), pinned((cap_c,), np.uint8))
         e2e_steps = max(2, args.steps // 2)
         barrier()
         t0 = time.perf_counter()
@@ -259,8 +274,8 @@ def run_ours(args):
             ctx.set_option("seed", 777 + k)
             ctx.set_phantom(mat, den, cfg.pdim, cfg.poffset, cfg.psize)
             st = ctx.run()
-            singles, scat = ctx.singles()
-            pairs, cls = ctx.coincidences()
+            singles, scat = ctx.singles(out=out_s)
+            pairs, cls = ctx.coincidences(out=out_c)
             e_coinc += len(pairs)
             h2d += mat.nbytes + den.nbytes
             d2h += singles.nbytes + scat.nbytes + pairs.nbytes + cls.nbytes
@@ -311,6 +326,91 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+BATCH_WORKLOAD = ("batched64: 64 simulations of uneven size in one job - phantoms 64^3-256^3 voxels (log-uniform) "
+                  "over a 6.4 cm cube of seeded water/bone/air ellipsoids, 1e5-1e7 F-18 decays each "
+                  "(log-uniform, positron range on), point or cylinder sources, the positron workload's ring "
+                  "and digitizer")
+
+
+def run_batched_workload(args):
+    """The 64-simulation job, once batched (gpet_run_batched) and once as 64
+    separate runs, on the same contexts."""
+    import numpy as np
+    import torch
+    from gpet_gb300 import api, scenes
+    torch.cuda.set_device(0)
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda:0")
+    with tempfile.TemporaryDirectory() as d:
+        sims = scenes.batched(d, n_sims=args.batch_sims)
+        data = os.path.join(ROOT, "data")
+        ctxs = []
+        t0 = time.perf_counter()
+        for bs in sims:
+            ctx = api.Context(0)
+            ctx.set_options(dict(bs.options, data_dir=data, base_dir=d))
+            ctx.load_config(bs.config_path)
+            mat, den = bs.phantom()
+            ctx.set_phantom(mat, den, (bs.nvox,) * 3, (-3.2,) * 3, (6.4,) * 3)
+            ctx.set_source_file(bs.source_path, 0.0, 120.0)
+            ctxs.append(ctx)
+        setup_s = time.perf_counter() - t0
+        seeds = [bs.options["seed"] for bs in sims]
+
+        def reseed(k):
+            for c, sd in zip(ctxs, seeds):
+                c.set_option("seed", sd + 1000003 * k)
+
+        for w in range(args.warmup):
+            reseed(100 + w)
+            api.run_batched(ctxs)
+        sampler = ClockSampler(0)
+        torch.cuda.synchronize()
+        sampler.start()
+        ms_b, coinc_b, decays_b, launches_b, wall_b = 0.0, 0, 0, 0, 0.0
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            reseed(k)
+            t0 = time.perf_counter()
+            st = api.run_batched(ctxs)
+            wall_b += time.perf_counter() - t0
+            ms_b += st[0]["ms_total"]
+            coinc_b += sum(x["n_coinc"] for x in st)
+            decays_b += sum(x["n_decays"] for x in st)
+            launches_b += st[0]["kernel_launches"]
+        clocks = sampler.stop()
+        # the same simulations one after another
+        ms_s, coinc_s, wall_s, launches_s = 0.0, 0, 0.0, 0
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            reseed(k)
+            for c in ctxs:
+                t0 = time.perf_counter()
+                st = c.run()
+                wall_s += time.perf_counter() - t0
+                ms_s += st["ms_total"]
+                coinc_s += st["n_coinc"]
+                launches_s += st["kernel_launches"]
+        for c in ctxs:
+            c.close()
+    line = {"metric": METRIC.replace("(plain MC)", "(plain MC, batched simulations)"),
+            "value": coinc_b / (ms_b * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_b / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": BATCH_WORKLOAD, "simulations": len(sims),
+                       "decays_per_step": decays_b // max(1, args.steps),
+                       "l2": "flushed between steps (512 MB write)"},
+            "gpu_launches": launches_b,
+            "decays_per_s": decays_b / (ms_b * 1e-3),
+            "host_wall_per_step_s": wall_b / args.steps,
+            "separate_runs": {"value": coinc_s / (ms_s * 1e-3), "ms_per_step": ms_s / args.steps,
+                              "host_wall_per_step_s": wall_s / args.steps,
+                              "gpu_launches": launches_s, "same_coincidences": coinc_s == coinc_b},
+            "setup_s": setup_s, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -322,11 +422,16 @@ def main():
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--gloo", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--workload", choices=["positron", "batched64"], default="positron",
+                    help="positron: the headline workload; batched64: 64 uneven simulations in one job")
+    ap.add_argument("--batch-sims", type=int, default=64, help=argparse.SUPPRESS)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched64":
+        run_batched_workload(args)
     else:
         run_ours(args)
 

@@ -173,10 +173,16 @@ class Context:
         self._ck(fn(self.h, *nulls, 0, C.byref(n)))
         return n.value
 
-    def singles(self):
+    def singles(self, out=None):
+        """Singles in time order and their phantom-scatter flags. `out` may
+        give (events, flags) arrays to fill (e.g. views of pinned memory); the
+        returned arrays are then their first n entries."""
         n = self._count(self.L.gpet_get_singles, None, None)
-        ev = np.zeros(n, EVENT_DTYPE)
-        sc = np.zeros(n, np.uint8)
+        if out is not None and len(out[0]) >= n and len(out[1]) >= n:
+            ev, sc = out[0][:n], out[1][:n]
+        else:
+            ev = np.zeros(n, EVENT_DTYPE)
+            sc = np.zeros(n, np.uint8)
         m = C.c_int64()
         if n:
             self._ck(self.L.gpet_get_singles(self.h, _ptr(ev), _ptr(sc), n, C.byref(m)))
@@ -192,10 +198,14 @@ class Context:
             self._ck(self.L.gpet_get_pulses(self.h, _ptr(ev), _ptr(sc), _ptr(sl), n, C.byref(m)))
         return ev, sc, sl
 
-    def coincidences(self):
+    def coincidences(self, out=None):
+        """Index pairs into the singles and class bytes; `out` as for singles()."""
         n = self._count(self.L.gpet_get_coincidences, None, None)
-        pr = np.zeros((n, 2), np.int64)
-        cl = np.zeros(n, np.uint8)
+        if out is not None and len(out[0]) >= n and len(out[1]) >= n:
+            pr, cl = out[0][:n], out[1][:n]
+        else:
+            pr = np.zeros((n, 2), np.int64)
+            cl = np.zeros(n, np.uint8)
         m = C.c_int64()
         if n:
             self._ck(self.L.gpet_get_coincidences(self.h, _ptr(pr), _ptr(cl), n, C.byref(m)))

@@ -105,6 +105,7 @@ struct gpet_ctx {
     // device scene
     SimDesc sim{};
     DevBuf d_sim, d_xs4, d_cmpsf, d_rayff, d_wck_ph, d_wck_det, d_vox, d_panels, d_psf;
+    DevBuf d_mat_stage, d_den_stage, d_maxden;   // phantom upload
     // results of the last run this context took part in
     std::shared_ptr<Work> work;
     int res_sim = 0;
@@ -135,6 +136,39 @@ static std::string resolve(const gpet_ctx* c, const std::string& p)
 {
     if (p.empty() || p[0] == '/') return p;
     return c->base_dir + "/" + p;
+}
+
+// pack (density, material) into the phantom's 8-byte voxels and take each
+// material's largest density for the majorant (initPhantom, initialize.cu:831-884);
+// bad counts voxels whose material index is out of range
+__global__ void k_pack_phantom(const int32_t* __restrict__ mat, const float* __restrict__ den, int64_t n, int nmat,
+                               uint2* __restrict__ vox, unsigned* maxden_bits, unsigned* bad)
+{
+    __shared__ unsigned smax[16];
+    if (threadIdx.x < 16) smax[threadIdx.x] = 0;
+    __syncthreads();
+    unsigned nbad = 0;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int m = mat[v];
+        const float d = den[v];
+        if (m < 0 || m >= nmat) {
+            nbad++;
+            continue;
+        }
+        // positive floats order like their bit patterns
+        if (d > 0.0f) atomicMax(&smax[m], __float_as_uint(d));
+        vox[v] = make_uint2(__float_as_uint(d), (unsigned)m);
+    }
+    if (nbad) atomicAdd(bad, nbad);
+    __syncthreads();
+    if ((int)threadIdx.x < nmat && threadIdx.x < 16 && smax[threadIdx.x]) atomicMax(&maxden_bits[threadIdx.x], smax[threadIdx.x]);
+}
+
+// phantom-scatter flag (0/1) from the pulse meta byte, in place
+__global__ void k_scat_flags(uint8_t* meta, int64_t n)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        meta[i] = (meta[i] & 0x80u) ? 1 : 0;
 }
 
 extern "C" {
@@ -276,21 +310,29 @@ int gpet_set_phantom(gpet_ctx* c, const int32_t* mat, const float* den, const in
     if (!c || !mat || !den || !dims || !offset || !size) return GPET_ERR_ARG;
     if (!c->have_tables) return fail(c, GPET_ERR_ARG, "load the tables before the phantom");
     if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1) return fail(c, GPET_ERR_ARG, "phantom dimensions must be >= 1");
-    cudaSetDevice(c->device);
+    CK(cudaSetDevice(c->device));
     const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
-    float maxden[10] = {0};
-    std::vector<uint2> vox((size_t)n);
-    for (int64_t v = 0; v < n; ++v) {
-        int m = mat[v];
-        if (m < 0 || m >= c->tab.nmat) return fail(c, GPET_ERR_ARG, "phantom material index out of range");
-        if (den[v] > maxden[m]) maxden[m] = den[v];
-        uint32_t bits;
-        std::memcpy(&bits, &den[v], 4);
-        vox[(size_t)v] = make_uint2(bits, (uint32_t)m);
-    }
+    // the caller's arrays go to the device as they are (a DMA when the caller's
+    // memory is pinned) and are packed and checked there
+    c->have_phantom = false;
+    CK(c->d_mat_stage.ensure((size_t)n * 4));
+    CK(c->d_den_stage.ensure((size_t)n * 4));
     CK(c->d_vox.ensure((size_t)n * sizeof(uint2)));
-    CK(cudaMemcpyAsync(c->d_vox.p, vox.data(), (size_t)n * sizeof(uint2), cudaMemcpyHostToDevice, c->stream));
+    CK(c->d_maxden.ensure(32 * 4));
+    CK(cudaMemsetAsync(c->d_maxden.p, 0, 32 * 4, c->stream));
+    CK(cudaMemcpyAsync(c->d_mat_stage.p, mat, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_den_stage.p, den, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+    const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 16);
+    k_pack_phantom<<<(unsigned)blocks, 256, 0, c->stream>>>(c->d_mat_stage.as<int32_t>(), c->d_den_stage.as<float>(),
+                                                             n, c->tab.nmat, c->d_vox.as<uint2>(),
+                                                             c->d_maxden.as<unsigned>(), c->d_maxden.as<unsigned>() + 16);
+    CK(cudaGetLastError());
+    unsigned h[17] = {0};
+    CK(cudaMemcpyAsync(h, c->d_maxden.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    if (h[16]) return fail(c, GPET_ERR_ARG, "phantom material index out of range");
+    float maxden[10] = {0};
+    for (int m = 0; m < 10 && m < c->tab.nmat; ++m) std::memcpy(&maxden[m], &h[m], 4);
     for (int k = 0; k < 3; ++k) { c->pdim[k] = dims[k]; c->poff[k] = offset[k]; c->psz[k] = size[k]; }
     std::memcpy(c->maxden_ph, maxden, sizeof(maxden));
     build_wck(c->tab, table_idle(c->tab), maxden, c->wck_ph, c->wck_e0, c->wck_ide);
@@ -1030,13 +1072,21 @@ int gpet_get_singles(gpet_ctx* c, gpet_event* buf, uint8_t* scat, int64_t cap, i
     *n = W.s_off[c->res_sim + 1] - off;
     if (!buf || *n == 0) return GPET_OK;
     if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the singles");
-    std::vector<gpet_event> ev;
-    std::vector<uint8_t> m;
-    int rc = gather(c, W, W.dg.single_idx + off, *n, true, ev, m);
-    if (rc) return rc;
-    std::memcpy(buf, ev.data(), sizeof(gpet_event) * (size_t)*n);
-    if (scat)
-        for (int64_t i = 0; i < *n; ++i) scat[i] = (m[i] & 0x80) ? 1 : 0;
+    // gathered on the device and copied straight into the caller's buffers
+    CK(W.g_ev.ensure((size_t)*n * sizeof(EventRec)));
+    CK(W.g_meta.ensure((size_t)*n));
+    PulseDev P = pulse_view(W);
+    if (gather_events(P, W.dg.single_idx + off, *n, true, W.dg, W.g_ev.as<EventRec>(), W.g_meta.as<uint8_t>(),
+                      c->stream))
+        return fail(c, GPET_ERR_CUDA, "gather of event records failed");
+    CK(cudaMemcpyAsync(buf, W.g_ev.p, (size_t)*n * sizeof(EventRec), cudaMemcpyDeviceToHost, c->stream));
+    if (scat) {
+        const int64_t blocks = std::min<int64_t>((*n + 255) / 256, 152 * 16);
+        k_scat_flags<<<(unsigned)blocks, 256, 0, c->stream>>>(W.g_meta.as<uint8_t>(), *n);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(scat, W.g_meta.p, (size_t)*n, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
     return GPET_OK;
 }
 

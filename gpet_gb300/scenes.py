@@ -18,6 +18,8 @@ Workloads (materials are row indices of data/input4gPET.matter):
              per block.
   large    : 1e9 F-18 decays in 256x256x512 voxels of 2 mm (30x20 cm body
              ellipse, lungs, spine); 48 panels of 16x16 4x4x20 mm crystals.
+  batched  : 64 simulations of uneven size for one batched job (phantoms
+             64^3-256^3, 1e5-1e7 decays each, point or cylinder sources).
 """
 import os
 from dataclasses import dataclass, field
@@ -168,6 +170,81 @@ def large(directory, n_decays=1_000_000_000, dims=(256, 256, 512), seed=DEFAULT_
     return Scene(directory, os.path.join(directory, "input_PET.in"),
                  {"n_decays": n_decays, "seed": seed, "coinc_window_ns": 4.0},
                  "F-18 body phantom 256x256x512, 48-panel ring")
+
+
+@dataclass
+class BatchSim:
+    """One simulation of a batch: the shared configuration plus its own
+    phantom (made on demand), source file and options."""
+    config_path: str
+    directory: str
+    nvox: int
+    source_path: str
+    options: dict
+    phantom_seed: int
+
+    def phantom(self):
+        return batch_phantom(self.nvox, self.phantom_seed)
+
+
+def batch_phantom(n, seed):
+    """n^3 voxels over a 6.4 cm cube: air, a water body ellipsoid and three to
+    six seeded ellipsoids of water, bone or air inside it."""
+    rng = np.random.default_rng(seed)
+    size = 6.4
+    x = _voxel_centres(n, size, -size / 2).astype(np.float32)
+    X = x[None, None, :]
+    Y = x[None, :, None]
+    Z = x[:, None, None]
+    mat = np.full((n, n, n), MAT_AIR, np.int32)
+    den = np.full((n, n, n), RHO_AIR, np.float32)
+    a = rng.uniform(2.2, 3.1, 3)
+    body = (X / a[0]) ** 2 + (Y / a[1]) ** 2 + (Z / a[2]) ** 2 < 1.0
+    mat[body] = MAT_WATER
+    den[body] = 1.0
+    for _ in range(int(rng.integers(3, 7))):
+        c = rng.uniform(-1.2, 1.2, 3)
+        r = rng.uniform(0.2, 0.9, 3)
+        e = ((X - c[0]) / r[0]) ** 2 + ((Y - c[1]) / r[1]) ** 2 + ((Z - c[2]) / r[2]) ** 2 < 1.0
+        kind = int(rng.integers(0, 3))
+        mat[e], den[e] = ((MAT_WATER, 1.0), (MAT_BONE, 1.85), (MAT_AIR, RHO_AIR))[kind]
+    return mat, den
+
+
+def batched(directory, n_sims=64, seed=DEFAULT_SEED, min_vox=64, max_vox=256, min_decays=100_000,
+            max_decays=10_000_000):
+    """Many uneven simulations for one batched job: phantom sizes log-uniform
+    in [min_vox, max_vox]^3 over the same 6.4 cm cube, decays log-uniform in
+    [min_decays, max_decays], F-18 (positron range on) from a point or a
+    cylinder (r 1-3 cm) with equal odds, each with its own seed; the ring,
+    digitizer and window of the positron workload. Returns the BatchSim list;
+    the seeds it drew are in each entry's options."""
+    os.makedirs(directory, exist_ok=True)
+    rng = np.random.default_rng(seed)
+    c = _base_config(directory, (8, 8, 8), (6.4, 6.4, 6.4), (-3.2, -3.2, -3.2))
+    c.useprange = 1
+    c.dlevel, c.dtype, c.dtime = 2, 0, 0.3
+    mat, den = batch_phantom(8, seed)
+    F.write_phantom(c.matfile, c.denfile, mat, den)
+    F.write_geo(c.geofile, 8, (0, 0, 1), 45.0, (MAT_LYSO, MAT_AIR), (7.1, 0.001025),
+                ring_panel0(8.0, 8, 8, 0.298, 0.002, 2.0))
+    F.write_sources(c.sourcefile, [4_000_000_000], [0], [1], [(0, 0, 0, 3.0, 6.4, 0)])
+    cfg = os.path.join(directory, "input_PET.in")
+    F.write_config(cfg, c)
+    sims = []
+    for i in range(n_sims):
+        nvox = int(round(np.exp(rng.uniform(np.log(min_vox), np.log(max_vox)))))
+        nd = int(round(np.exp(rng.uniform(np.log(min_decays), np.log(max_decays)))))
+        src = os.path.join(directory, "source_%02d.txt" % i)
+        if rng.uniform() < 0.5:
+            F.write_sources(src, [4_000_000_000], [0], [2], [(0, 0, 0, 0.0, 0, 0)])
+        else:
+            F.write_sources(src, [4_000_000_000], [0], [1], [(0, 0, 0, float(rng.uniform(1.0, 3.0)), 6.4, 0)])
+        sims.append(BatchSim(cfg, directory, nvox, src,
+                             {"n_decays": nd, "seed": int(rng.integers(1, 2 ** 62)), "sim_id": i,
+                              "coinc_window_ns": 4.0},
+                             int(rng.integers(1, 2 ** 31))))
+    return sims
 
 
 WORKLOADS = {"small": small, "positron": positron, "large": large}
