@@ -218,6 +218,7 @@ def run_ours(args):
         opts = dict(sc.options, data_dir=data, base_dir=d, sim_id=rank)
         ctx.set_options(opts)
         ctx.load_config(sc.config_path)
+        tuning = ctx.autotune(args.tune_decays) if args.autotune else None
         for w in range(args.warmup):
             ctx.set_option("seed", 1000 + w)
             ctx.run()
@@ -317,6 +318,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps},
         "clocks": clocks,
         "wall_s_timed_region": wall,
+        "launch_shape": tuning if tuning else "library defaults",
     }
     if world == 1 and not args.no_cpu_baseline:
         with tempfile.TemporaryDirectory() as d2:
@@ -363,6 +365,8 @@ def run_batched_workload(args):
         for w in range(args.warmup):
             reseed(100 + w)
             api.run_batched(ctxs)
+        # the same simulations one after another need the tuner no more than
+        # the batch: both use the library defaults
         sampler = ClockSampler(0)
         torch.cuda.synchronize()
         sampler.start()
@@ -421,6 +425,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
+                    help="time launch shapes on a sample before the warm-up (results do not depend on the shape)")
+    ap.add_argument("--tune-decays", type=int, default=1 << 23)
     ap.add_argument("--gloo", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--workload", choices=["positron", "batched64"], default="positron",
                     help="positron: the headline workload; batched64: 64 uneven simulations in one job")

@@ -28,6 +28,16 @@ class GpetError(RuntimeError):
         self.code = code
 
 
+class Tuning(C.Structure):
+    _fields_ = [("sub_decays", C.c_int64), ("chunk_decays", C.c_int64), ("phantom_blocks_per_sm", C.c_int32),
+                ("drain_period", C.c_int32), ("detector_threads", C.c_int32), ("source_threads", C.c_int32),
+                ("candidates", C.c_int32), ("sample_decays", C.c_int64), ("ms_default", C.c_double),
+                ("ms_tuned", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class RunStats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "n_decays", "n_pairs", "n_entered", "n_pulses", "n_hits", "n_threshold", "n_deadtime", "n_singles",
@@ -68,6 +78,7 @@ def load_library(path=None):
     L.gpet_set_source_psf.argtypes = [vp, vp, i64, C.c_int]
     L.gpet_run.argtypes = [vp, C.POINTER(RunStats)]
     L.gpet_run_batched.argtypes = [C.POINTER(vp), i32, C.POINTER(RunStats)]
+    L.gpet_autotune.argtypes = [vp, i64, C.POINTER(Tuning)]
     L.gpet_digitize.argtypes = [vp, vp, vp, vp, i64, C.POINTER(RunStats)]
     L.gpet_get_singles.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
     L.gpet_get_pulses.argtypes = [vp, vp, vp, vp, i64, C.POINTER(i64)]
@@ -158,6 +169,13 @@ class Context:
         st = RunStats()
         self._ck(self.L.gpet_run(self.h, C.byref(st)))
         return st.as_dict()
+
+    def autotune(self, sample_decays=0):
+        """Time launch shapes on a sample of this workload and keep the fastest
+        (gpet_autotune); returns the chosen shape and the sample's times."""
+        t = Tuning()
+        self._ck(self.L.gpet_autotune(self.h, int(sample_decays), C.byref(t)))
+        return t.as_dict()
 
     def digitize(self, pulses, scat, slot):
         pulses = np.ascontiguousarray(pulses, EVENT_DTYPE)

@@ -56,6 +56,11 @@ struct Work {
     DevBuf dg_idx_a, dg_idx_b, dg_key_a, dg_key_b, dg_torder, dg_flags, dg_site, dg_hist, dg_aux, dg_sel, dg_blur,
         dg_single, dg_wcount, dg_wend, dg_dcount;
     std::vector<cudaEvent_t> tev;         // per-launch timing events
+    DevBuf d_waves, d_work;               // wave table and photon counters of one chunk
+    Wave* h_waves = nullptr;              // pinned staging of the wave table
+    size_t h_waves_cap = 0;
+    cudaGraphExec_t gexec = nullptr;      // the chunk's launches, replayed while their arguments stay put
+    std::vector<unsigned char> gkey;
     // results
     int nsims = 0;
     int64_t n_pulses = 0, n_hits = 0, n_singles = 0, n_coinc = 0;
@@ -65,6 +70,8 @@ struct Work {
     ~Work()
     {
         for (auto& e : tev) cudaEventDestroy(e);
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (h_waves) cudaFreeHost(h_waves);
         if (dg.coinc_pairs) cudaFree(dg.coinc_pairs);
         if (dg.coinc_class) cudaFree(dg.coinc_class);
     }
@@ -84,6 +91,12 @@ struct gpet_ctx {
     int record_exits = 0;
     int64_t chunk_decays = 1ll << 24;
     int64_t sub_decays = 1ll << 20;       // decays per wave: the pair buffer stays in L2
+    int phantom_bps = 0;                  // k_phantom blocks per SM (0: as many as fit)
+    int drain_period = 32;                // k_phantom compaction period
+    int det_threads = 256, src_threads = 256;
+    int use_graphs = 1;
+    int autotune = 0;                     // tune the launch shape on the first run
+    bool tuned = false;
     std::string base_dir = ".";
     std::string data_dir;
     // host scene
@@ -223,6 +236,12 @@ int gpet_set_option(gpet_ctx* c, const char* key, const char* value)
     else if (k == "record_exits") c->record_exits = (int)std::strtol(value, &end, 10);
     else if (k == "chunk_decays") c->chunk_decays = std::strtoll(value, &end, 10);
     else if (k == "sub_decays") c->sub_decays = std::strtoll(value, &end, 10);
+    else if (k == "phantom_blocks_per_sm") c->phantom_bps = (int)std::strtol(value, &end, 10);
+    else if (k == "drain_period") c->drain_period = (int)std::strtol(value, &end, 10);
+    else if (k == "detector_threads") c->det_threads = (int)std::strtol(value, &end, 10);
+    else if (k == "source_threads") c->src_threads = (int)std::strtol(value, &end, 10);
+    else if (k == "use_graphs") c->use_graphs = (int)std::strtol(value, &end, 10);
+    else if (k == "autotune") c->autotune = (int)std::strtol(value, &end, 10);
     else if (k == "base_dir") { c->base_dir = v; return GPET_OK; }
     else if (k == "data_dir") { c->data_dir = v; return GPET_OK; }
     else return fail(c, GPET_ERR_ARG, "unknown option " + k);
@@ -230,6 +249,10 @@ int gpet_set_option(gpet_ctx* c, const char* key, const char* value)
     if (c->coinc_policy < 0 || c->coinc_policy > 1) return fail(c, GPET_ERR_ARG, "coinc_policy must be 0 or 1");
     if (c->chunk_decays < 1024) return fail(c, GPET_ERR_ARG, "chunk_decays must be >= 1024");
     if (c->sub_decays < 1024) return fail(c, GPET_ERR_ARG, "sub_decays must be >= 1024");
+    if (c->phantom_bps < 0 || c->phantom_bps > 32) return fail(c, GPET_ERR_ARG, "phantom_blocks_per_sm must be 0..32");
+    if (c->drain_period < 1 || c->drain_period > 32) return fail(c, GPET_ERR_ARG, "drain_period must be 1..32");
+    for (int t : {c->det_threads, c->src_threads})
+        if (t < 32 || t > 256 || t % 32) return fail(c, GPET_ERR_ARG, "threads per block must be 32..256, a multiple of 32");
     return GPET_OK;
 }
 
@@ -714,13 +737,89 @@ static int digitize_work(gpet_ctx* c, Work& W, const std::vector<DigiParams>& pr
     return GPET_OK;
 }
 
+// Everything the launches of one chunk depend on. Two chunks with equal
+// ChunkLaunch values issue identical launches (the waves themselves are read
+// from the device table at run time), so one instantiated CUDA graph serves
+// both; the struct is zero-filled before use so it compares bytewise.
+struct ChunkLaunch {
+    const Wave* d_waves;
+    unsigned long long* d_work;
+    unsigned long long* qcount;
+    PairBuf pb;
+    QueueDev q;
+    Counters* dcnt;
+    const cudaEvent_t* ev;        // 3 per wave
+    size_t smem;
+    int32_t nwaves;
+    int32_t multi;
+    uint32_t src_blocks, src_threads, ph_blocks;
+    int32_t period;
+    int32_t graph;
+};
+
+static cudaError_t enqueue_chunk(const ChunkLaunch& L, cudaStream_t s)
+{
+    const unsigned flag = L.graph ? cudaEventRecordExternal : cudaEventRecordDefault;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(L.qcount, 0, 8, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(L.d_work, 0, 8 * (size_t)L.nwaves, s)) != cudaSuccess) return e;
+    for (int k = 0; k < L.nwaves; ++k) {
+        if ((e = cudaEventRecordWithFlags(L.ev[3 * k], s, flag)) != cudaSuccess) return e;
+        if ((e = launch_source(L.multi != 0, L.src_blocks, L.src_threads, L.smem, s, L.d_waves, k, L.pb, L.dcnt)) !=
+            cudaSuccess)
+            return e;
+        if ((e = cudaEventRecordWithFlags(L.ev[3 * k + 1], s, flag)) != cudaSuccess) return e;
+        if ((e = launch_phantom(L.multi != 0, L.ph_blocks, L.smem, s, L.d_waves, k, L.pb, L.q, L.dcnt, L.period)) !=
+            cudaSuccess)
+            return e;
+        if ((e = cudaEventRecordWithFlags(L.ev[3 * k + 2], s, flag)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// the chunk's launches: replayed from the cached graph when nothing they
+// depend on changed, captured and instantiated again otherwise
+static int launch_chunk(gpet_ctx* c, Work& W, const ChunkLaunch& L)
+{
+    if (!L.graph) {
+        CK(enqueue_chunk(L, c->stream));
+        return GPET_OK;
+    }
+    const unsigned char* key = reinterpret_cast<const unsigned char*>(&L);
+    if (!W.gexec || W.gkey.size() != sizeof(L) || std::memcmp(W.gkey.data(), key, sizeof(L)) != 0) {
+        if (W.gexec) {
+            cudaGraphExecDestroy(W.gexec);
+            W.gexec = nullptr;
+        }
+        W.gkey.clear();
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = enqueue_chunk(L, c->stream);
+        cudaGraph_t g = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&W.gexec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            W.gexec = nullptr;
+            return cuda_fail(c, e, "capture of the chunk's launches");
+        }
+        W.gkey.assign(key, key + sizeof(L));
+    }
+    CK(cudaGraphLaunch(W.gexec, c->stream));
+    return GPET_OK;
+}
+
 // one wave: decays [g, g + n) of the batch's concatenated decay list
 struct WaveH {
     int64_t g, n;
     int first_seg, nseg;
 };
 
-static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats)
+// limit >= 0 runs only the first `limit` decays of each simulation;
+// transport_only stops after the detector stage (no digitizer, no results),
+// stats[0] receiving the stage times: the autotuner's measurement
+static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64_t limit = -1,
+                     bool transport_only = false)
 {
     gpet_ctx* c = cs[0];
     for (int s = 0; s < nsim; ++s) {
@@ -744,6 +843,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats)
         int rc = build_sim(cs[s]);
         if (rc) return rc;
         nd[s] = total_decays(cs[s]);
+        if (limit >= 0) nd[s] = std::min(nd[s], limit);
         ND += nd[s];
         rec_hits = rec_hits || cs[s]->record_hits;
         max_site = std::max<int64_t>(max_site, (int64_t)cs[s]->geo.npanels * cs[s]->geo.moduleN * cs[s]->geo.crystalN);
@@ -829,7 +929,8 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats)
     int rc = grow_pulses(c, W, 1 << 20, 0);
     if (rc) return rc;
     if (rec_hits) { rc = grow_hits(c, W, 1 << 20, 0); if (rc) return rc; }
-    if (c->record_exits) {
+    const bool rec_exits = c->record_exits && !transport_only;
+    if (rec_exits) {
         CK(W.exits.ensure((size_t)2 * chunk * sizeof(ExitRec)));
         c->host_exits.assign((size_t)2 * ND, ExitRec{});
     } else {
@@ -841,16 +942,39 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats)
     unsigned long long* qcount = W.aux.as<unsigned long long>() + 0;
     unsigned long long* pcount = W.aux.as<unsigned long long>() + 1;
     unsigned long long* hcount = W.aux.as<unsigned long long>() + 2;
-    unsigned long long* work = W.aux.as<unsigned long long>() + 3;
     const bool multi = nsim > 1;
     // one simulation: its panels are staged in shared memory
     if (multi) smem = 0;
     int nsm = 0;
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
-    int phantom_blocks = 0;
-    CK(phantom_blocks_per_sm(multi, smem, &phantom_blocks));
-    phantom_blocks = std::max(1, phantom_blocks) * nsm;
+    int bps = 0;
+    CK(phantom_blocks_per_sm(multi, smem, &bps));
+    bps = std::max(1, bps);
+    if (c->phantom_bps > 0) bps = std::min(bps, c->phantom_bps);
     const SimDesc* d_sims = W.sims.as<SimDesc>();
+    // wave table and counters for the largest chunk
+    size_t max_k = 1;
+    for (size_t w0 = 0; w0 < waves.size();) {
+        size_t w1 = w0;
+        while (w1 < waves.size() && waves[w1].g + waves[w1].n - waves[w0].g <= chunk) w1++;
+        if (w1 == w0) w1 = w0 + 1;
+        max_k = std::max(max_k, w1 - w0);
+        w0 = w1;
+    }
+    CK(W.d_waves.ensure(max_k * sizeof(Wave)));
+    CK(W.d_work.ensure(max_k * 8));
+    if (W.h_waves_cap < max_k) {
+        if (W.h_waves) cudaFreeHost(W.h_waves);
+        W.h_waves = nullptr;
+        W.h_waves_cap = 0;
+        CK(cudaMallocHost(reinterpret_cast<void**>(&W.h_waves), max_k * sizeof(Wave)));
+        W.h_waves_cap = max_k;
+    }
+    while (W.tev.size() < 3 * max_k) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        W.tev.push_back(e);
+    }
     gpet_run_stats tot{};
     float ms_det = 0, ms_src = 0, ms_ph = 0;
     cudaEventRecord(c->ev[0], c->stream);
@@ -862,39 +986,49 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats)
         size_t we = wi;
         while (we < waves.size() && waves[we].g + waves[we].n - cg0 <= chunk) we++;
         if (we == wi) we = wi + 1;
-        CK(cudaMemsetAsync(qcount, 0, 8, c->stream));
-        QueueDev q;
-        q.f = W.q_f.as<float>(); q.t = W.q_t.as<double>(); q.i = W.q_i.as<int32_t>();
-        q.count = qcount; q.cap = W.q_cap;
-        int ne = 0;
-        for (size_t w = wi; w < we; ++w) {
-            Wave wave;
+        const int K = (int)(we - wi);
+        for (int k = 0; k < K; ++k) {
+            const size_t w = wi + k;
+            Wave& wave = W.h_waves[k];
             wave.sims = d_sims;
             wave.g0 = d_g0 + woff_g0[w];
             wave.d0 = d_d0 + woff_d0[w];
             wave.sim = d_sim + woff_d0[w];
             wave.nseg = waves[w].nseg;
             wave.n = waves[w].n;
-            CK(cudaMemsetAsync(work, 0, 8, c->stream));
-            int64_t blocks = std::min<int64_t>((wave.n + 255) / 256, (int64_t)nsm * 16);
-            ExitRec* ex = c->record_exits ? W.exits.as<ExitRec>() + 2 * (waves[w].g - cg0) : nullptr;
-            while (W.tev.size() < (size_t)ne + 3) {
-                cudaEvent_t e;
-                CK(cudaEventCreate(&e));
-                W.tev.push_back(e);
-            }
-            cudaEventRecord(W.tev[ne++], c->stream);
-            CK(launch_source(multi, (unsigned)std::max<int64_t>(blocks, 1), smem, c->stream, wave, pb, dcnt));
-            cudaEventRecord(W.tev[ne++], c->stream);
-            CK(launch_phantom(multi, (unsigned)phantom_blocks, smem, c->stream, wave, pb, work, q, ex, dcnt));
-            cudaEventRecord(W.tev[ne++], c->stream);
-            tot.kernel_launches += 2;
+            wave.work = W.d_work.as<unsigned long long>() + k;
+            wave.exits = rec_exits ? W.exits.as<ExitRec>() + 2 * (waves[w].g - cg0) : nullptr;
         }
+        CK(cudaMemcpyAsync(W.d_waves.p, W.h_waves, K * sizeof(Wave), cudaMemcpyHostToDevice, c->stream));
+        QueueDev q;
+        q.f = W.q_f.as<float>(); q.t = W.q_t.as<double>(); q.i = W.q_i.as<int32_t>();
+        q.count = qcount; q.cap = W.q_cap;
+        ChunkLaunch L;
+        std::memset(&L, 0, sizeof(L));
+        L.d_waves = W.d_waves.as<Wave>();
+        L.d_work = W.d_work.as<unsigned long long>();
+        L.qcount = qcount;
+        L.pb = pb;
+        L.q = q;
+        L.dcnt = dcnt;
+        L.ev = W.tev.data();
+        L.smem = smem;
+        L.nwaves = K;
+        L.multi = multi ? 1 : 0;
+        L.src_threads = (uint32_t)c->src_threads;
+        L.src_blocks = (uint32_t)std::max<int64_t>(1, std::min<int64_t>((sub + c->src_threads - 1) / c->src_threads,
+                                                                      (int64_t)nsm * 32));
+        L.ph_blocks = (uint32_t)(bps * nsm);
+        L.period = c->drain_period;
+        L.graph = c->use_graphs ? 1 : 0;
+        rc = launch_chunk(c, W, L);
+        if (rc) return rc;
+        tot.kernel_launches += 2 * K;
         unsigned long long hq = 0;
         CK(cudaMemcpyAsync(&hq, qcount, 8, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         CK(cudaGetLastError());
-        for (int e = 0; e < ne; e += 3) {
+        for (int e = 0; e < 3 * K; e += 3) {
             float a = 0, b = 0;
             cudaEventElapsedTime(&a, W.tev[e], W.tev[e + 1]);
             cudaEventElapsedTime(&b, W.tev[e + 1], W.tev[e + 2]);
@@ -902,7 +1036,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats)
             ms_ph += b;
         }
         const int64_t cn = waves[we - 1].g + waves[we - 1].n - cg0;
-        if (c->record_exits)
+        if (rec_exits)
             CK(cudaMemcpy(c->host_exits.data() + 2 * cg0, W.exits.p, (size_t)2 * cn * sizeof(ExitRec),
                           cudaMemcpyDeviceToHost));
         // room for the worst case of this chunk's queue
@@ -914,11 +1048,12 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats)
         HitDev H;
         H.id = W.h_id.as<int32_t>(); H.f = W.h_f.as<float>(); H.count = hcount; H.cap = W.h_cap;
         H.sim = multi ? W.h_sim.as<int32_t>() : nullptr;
-        int64_t dblocks = std::min<int64_t>(((int64_t)hq + 255) / 256, (int64_t)nsm * 8);
+        const int dt = c->det_threads;
+        int64_t dblocks = std::min<int64_t>(((int64_t)hq + dt - 1) / dt, (int64_t)nsm * 8 * (256 / dt));
         cudaEventRecord(c->ev[1], c->stream);
         if (hq > 0) {
-            CK(launch_detector(multi, (unsigned)std::max<int64_t>(dblocks, 1), smem, c->stream, d_sims, q, P, H,
-                               rec_hits ? 1 : 0, dcnt));
+            CK(launch_detector(multi, (unsigned)std::max<int64_t>(dblocks, 1), (unsigned)dt, smem, c->stream, d_sims,
+                               q, P, H, rec_hits ? 1 : 0, dcnt));
             tot.kernel_launches++;
         }
         cudaEventRecord(c->ev[2], c->stream);
@@ -939,6 +1074,19 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats)
         return fail(c, GPET_ERR_CAPACITY, "a device buffer overflowed (queue/pulse/hit drops)");
     W.n_pulses = pulses_used;
     W.n_hits = rec_hits ? hits_used : 0;
+    if (transport_only) {
+        // results of this partial run are not kept
+        for (int s = 0; s < nsim; ++s) cs[s]->have_results = false;
+        if (stats) {
+            stats[0] = tot;
+            stats[0].ms_source = ms_src;
+            stats[0].ms_phantom = ms_ph;
+            stats[0].ms_source_phantom = ms_src + ms_ph;
+            stats[0].ms_detector = ms_det;
+            stats[0].n_pulses = pulses_used;
+        }
+        return GPET_OK;
+    }
     float ms_digi = 0;
     rc = digitize_work(c, W, prms, max_site, &tot, &ms_digi);
     if (rc) return rc;
@@ -968,13 +1116,150 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats)
     return GPET_OK;
 }
 
+// ---------------------------------------------------------------- autotuner
+// Launch-shape parameters of the transport: none of them changes a result
+// (every random stream is keyed by decay, photon and pulse, and every output
+// is put in a total order), only the time.
+struct Shape {
+    int64_t sub, chunk;
+    int bps, period, det_threads, src_threads;
+};
+
+static Shape get_shape(const gpet_ctx* c)
+{
+    return {c->sub_decays, c->chunk_decays, c->phantom_bps, c->drain_period, c->det_threads, c->src_threads};
+}
+
+static void set_shape(gpet_ctx* c, const Shape& s)
+{
+    c->sub_decays = s.sub; c->chunk_decays = s.chunk; c->phantom_bps = s.bps; c->drain_period = s.period;
+    c->det_threads = s.det_threads; c->src_threads = s.src_threads;
+}
+
+// transport time (source + phantom + detector, device) of the first `sample`
+// decays with the context's current shape: the best of `reps` runs
+static int time_transport(gpet_ctx* c, int64_t sample, int reps, double* ms)
+{
+    gpet_ctx* one[1] = {c};
+    double best = 1e30;
+    for (int r = 0; r < reps; ++r) {
+        gpet_run_stats st{};
+        int rc = run_batch(one, 1, &st, sample, true);
+        if (rc) return rc;
+        best = std::min(best, st.ms_source + st.ms_phantom + st.ms_detector);
+    }
+    *ms = best;
+    return GPET_OK;
+}
+
+// Coordinate descent over the shape, one parameter at a time, each candidate
+// timed on the same sample of the context's own workload.
+static int autotune(gpet_ctx* c, int64_t sample, gpet_tuning* out)
+{
+    if (!c->have_tables || !c->have_phantom || !c->have_geo || !c->have_source)
+        return fail(c, GPET_ERR_ARG, "tables, phantom, geometry and source must be set before tuning");
+    gpet_ctx* one[1] = {c};
+    (void)one;
+    int rc = build_sim(c);
+    if (rc) return rc;
+    const int64_t total = total_decays(c);
+    if (sample <= 0) sample = std::min<int64_t>(total, 1ll << 23);
+    sample = std::min(sample, total);
+    const Shape start = get_shape(c);
+    if (sample < 4096) {
+        if (out) std::memset(out, 0, sizeof(*out));
+        c->tuned = true;
+        return GPET_OK;
+    }
+    int cands = 0;
+    double best_ms = 0;
+    rc = time_transport(c, sample, 1, &best_ms);   // warm-up: buffers, graph, caches
+    if (rc) { set_shape(c, start); return rc; }
+    rc = time_transport(c, sample, 2, &best_ms);
+    if (rc) { set_shape(c, start); return rc; }
+    const double ms_default = best_ms;
+    Shape best = start;
+    cands++;
+    auto consider = [&](Shape cand) -> int {
+        set_shape(c, cand);
+        double ms = 0;
+        int r = time_transport(c, sample, 2, &ms);
+        cands++;
+        if (r) return r;
+        if (ms < best_ms * 0.995) {
+            best_ms = ms;
+            best = cand;
+        }
+        set_shape(c, best);
+        return GPET_OK;
+    };
+    for (int64_t sub : {1ll << 18, 1ll << 19, 1ll << 20, 1ll << 21}) {
+        if (sub == best.sub || sub > sample) continue;
+        Shape t = best; t.sub = sub; t.chunk = std::max(t.chunk, sub);
+        if ((rc = consider(t))) break;
+    }
+    int maxb = 0;
+    if (!rc && phantom_blocks_per_sm(false, (size_t)c->geo.npanels * kPanelStride * 4, &maxb) == cudaSuccess)
+        for (int b = maxb - 1; b >= std::max(1, maxb - 2) && !rc; --b) {
+            Shape t = best; t.bps = b;
+            rc = consider(t);
+        }
+    for (int p : {24, 16, 8}) {
+        if (rc || p == best.period) continue;
+        Shape t = best; t.period = p;
+        rc = consider(t);
+    }
+    for (int th : {128, 64}) {
+        if (rc || th == best.det_threads) continue;
+        Shape t = best; t.det_threads = th;
+        rc = consider(t);
+    }
+    for (int th : {128}) {
+        if (rc || th == best.src_threads) continue;
+        Shape t = best; t.src_threads = th;
+        rc = consider(t);
+    }
+    for (int64_t ch : {sample / 4, sample / 2}) {
+        if (rc || ch < best.sub || ch < 1024 || ch == best.chunk) continue;
+        Shape t = best; t.chunk = ch;
+        rc = consider(t);
+    }
+    if (rc) { set_shape(c, start); return rc; }
+    set_shape(c, best);
+    c->tuned = true;
+    if (out) {
+        out->sub_decays = best.sub;
+        out->chunk_decays = best.chunk;
+        out->phantom_blocks_per_sm = best.bps;
+        out->drain_period = best.period;
+        out->detector_threads = best.det_threads;
+        out->source_threads = best.src_threads;
+        out->candidates = cands;
+        out->sample_decays = sample;
+        out->ms_default = ms_default;
+        out->ms_tuned = best_ms;
+    }
+    return GPET_OK;
+}
+
 extern "C" {
 
 int gpet_run(gpet_ctx* c, gpet_run_stats* st)
 {
     if (!c) return GPET_ERR_ARG;
+    if (c->autotune && !c->tuned) {
+        int rc = autotune(c, 0, nullptr);
+        if (rc) return rc;
+    }
     gpet_ctx* one[1] = {c};
     return run_batch(one, 1, st);
+}
+
+int gpet_autotune(gpet_ctx* c, int64_t sample_decays, gpet_tuning* out)
+{
+    if (!c) return GPET_ERR_ARG;
+    CK(cudaSetDevice(c->device));
+    return autotune(c, sample_decays, out);
 }
 
 int gpet_run_batched(gpet_ctx* const* ctxs, int32_t n, gpet_run_stats* stats)

@@ -7,8 +7,18 @@
 
 namespace gpet {
 
+// phantom exit record (48 bytes), one per photon slot
+struct ExitRec {
+    float x, y, z, ux, uy, uz, E;
+    int32_t nscat;
+    double t;
+    int32_t status, panel;
+};
+
 // A wave of decays: global indices [g0[i], g0[i+1]) are decays d0[i] ..
-// of simulation sim[i] (sims[] in device memory).
+// of simulation sim[i] (sims[] in device memory). Waves live in a device
+// table that the kernels index, so that the launches of a chunk of waves do
+// not change from chunk to chunk (one CUDA graph serves them all).
 constexpr int kMaxSeg = 128;
 struct Wave {
     const SimDesc* sims;
@@ -17,6 +27,8 @@ struct Wave {
     const int32_t* sim;           // [nseg]
     int32_t nseg;
     int64_t n;                    // decays in the wave
+    unsigned long long* work;     // photon counter of k_phantom, zero at launch
+    ExitRec* exits;               // per photon of the wave, or NULL
 };
 
 // detector queue, structure of arrays (cap entries each)
@@ -87,16 +99,6 @@ struct SimTally {
     }
 };
 
-
-
-// phantom exit record (48 bytes), one per photon slot
-struct ExitRec {
-    float x, y, z, ux, uy, uz, E;
-    int32_t nscat;
-    double t;
-    int32_t status, panel;
-};
-
 // digitizer parameters (main.cu:158-182 plus the coincidence sorter)
 struct DigiParams {
     uint32_t key0, key1;
@@ -120,21 +122,25 @@ struct PairBuf {
 
 // Counters is an array indexed by simulation; kMulti selects per-thread
 // simulation descriptors (several simulations in one wave)
-template <bool kMulti> __global__ void k_source(Wave w, PairBuf pb, Counters* cnt);
+// waves[wi] is the wave to process. period: k_phantom takes its staged
+// finished photons through the panel search once at least `period` (1..32)
+// are waiting
+template <bool kMulti> __global__ void k_source(const Wave* waves, int wi, PairBuf pb, Counters* cnt);
 template <bool kMulti>
-__global__ void k_phantom(Wave w, PairBuf pb, unsigned long long* work, QueueDev q, ExitRec* exits, Counters* cnt);
+__global__ void k_phantom(const Wave* waves, int wi, PairBuf pb, QueueDev q, Counters* cnt, int period);
 template <bool kMulti>
 __global__ void k_detector(const SimDesc* sims, QueueDev q, PulseDev P, HitDev H, int rec_hits, Counters* cnt);
 
 // host-side launchers (transport.cu): `multi` picks the kMulti instance,
-// smem is the dynamic shared memory (panels of the one simulation, or 0)
-cudaError_t launch_source(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const Wave& w, const PairBuf& pb,
-                          Counters* cnt);
-cudaError_t launch_phantom(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const Wave& w,
-                           const PairBuf& pb, unsigned long long* work, const QueueDev& q, ExitRec* exits,
-                           Counters* cnt);
-cudaError_t launch_detector(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const SimDesc* sims,
-                            const QueueDev& q, const PulseDev& P, const HitDev& H, int rec_hits, Counters* cnt);
+// smem is the dynamic shared memory (panels of the one simulation, or 0);
+// threads per block: a multiple of 32 up to 256 (k_phantom: 256)
+cudaError_t launch_source(bool multi, unsigned blocks, unsigned threads, size_t smem, cudaStream_t s,
+                          const Wave* waves, int wi, const PairBuf& pb, Counters* cnt);
+cudaError_t launch_phantom(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const Wave* waves, int wi,
+                           const PairBuf& pb, const QueueDev& q, Counters* cnt, int period);
+cudaError_t launch_detector(bool multi, unsigned blocks, unsigned threads, size_t smem, cudaStream_t s,
+                            const SimDesc* sims, const QueueDev& q, const PulseDev& P, const HitDev& H, int rec_hits,
+                            Counters* cnt);
 // resident k_phantom blocks per SM at 256 threads and `smem` bytes
 cudaError_t phantom_blocks_per_sm(bool multi, size_t smem, int* blocks);
 // cudaSuccess when the transport kernels have an image for the current device

@@ -118,8 +118,9 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2])
 // simulation's descriptor; otherwise the one descriptor is staged in shared
 // memory.
 template <bool kMulti>
-__global__ void __launch_bounds__(256) k_source(Wave w, PairBuf pb, Counters* cnt)
+__global__ void __launch_bounds__(256) k_source(const Wave* waves, int wi, PairBuf pb, Counters* cnt)
 {
+    const Wave w = waves[wi];
     __shared__ SimDesc sS;
     __shared__ SegSmem sg;
     extern __shared__ float sP[];
@@ -185,9 +186,12 @@ constexpr int kFinCap = 64;      // finished photons staged per warp
 // at a time, one per lane. Photon p of the wave is photon (p & 1) of the
 // wave's decay p >> 1. kMulti as for k_source.
 template <bool kMulti>
-__global__ void __launch_bounds__(256, 4) k_phantom(Wave w, PairBuf pb, unsigned long long* work, QueueDev q,
-                                                    ExitRec* exits, Counters* cnt)
+__global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, PairBuf pb, QueueDev q, Counters* cnt,
+                                                    int period)
 {
+    const Wave w = waves[wi];
+    unsigned long long* const work = w.work;
+    ExitRec* const exits = w.exits;
     __shared__ SimDesc sS;
     __shared__ SegSmem sg;
     __shared__ FinRec fbuf[kPhWarps][kFinCap];
@@ -378,11 +382,14 @@ __global__ void __launch_bounds__(256, 4) k_phantom(Wave w, PairBuf pb, unsigned
             }
             fcount += __popc(mf);
             __syncwarp();
-            if (fcount >= 32) {
-                drain(32);
-                const int rest = fcount - 32;
+            // fcount <= 31 before staging, so <= 63 < kFinCap here, and the
+            // rest after a drain of min(fcount, 32) is <= 31 again
+            if (fcount >= period) {
+                const int k = fcount < 32 ? fcount : 32;
+                drain(k);
+                const int rest = fcount - k;
                 FinRec r;
-                if (lane < rest) r = fb[32 + lane];
+                if (lane < rest) r = fb[k + lane];
                 __syncwarp();
                 if (lane < rest) fb[lane] = r;
                 __syncwarp();
@@ -650,28 +657,33 @@ __global__ void __launch_bounds__(256) k_detector(const SimDesc* sims, QueueDev 
     }
 }
 
-cudaError_t launch_source(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const Wave& w, const PairBuf& pb,
-                          Counters* cnt)
+static bool valid_threads(unsigned t) { return t >= 32 && t <= 256 && t % 32 == 0; }
+
+cudaError_t launch_source(bool multi, unsigned blocks, unsigned threads, size_t smem, cudaStream_t s,
+                          const Wave* waves, int wi, const PairBuf& pb, Counters* cnt)
 {
-    if (multi) k_source<true><<<blocks, 256, smem, s>>>(w, pb, cnt);
-    else k_source<false><<<blocks, 256, smem, s>>>(w, pb, cnt);
+    if (!valid_threads(threads)) return cudaErrorInvalidValue;
+    if (multi) k_source<true><<<blocks, threads, smem, s>>>(waves, wi, pb, cnt);
+    else k_source<false><<<blocks, threads, smem, s>>>(waves, wi, pb, cnt);
     return cudaGetLastError();
 }
 
-cudaError_t launch_phantom(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const Wave& w,
-                           const PairBuf& pb, unsigned long long* work, const QueueDev& q, ExitRec* exits,
-                           Counters* cnt)
+cudaError_t launch_phantom(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const Wave* waves, int wi,
+                           const PairBuf& pb, const QueueDev& q, Counters* cnt, int period)
 {
-    if (multi) k_phantom<true><<<blocks, 256, smem, s>>>(w, pb, work, q, exits, cnt);
-    else k_phantom<false><<<blocks, 256, smem, s>>>(w, pb, work, q, exits, cnt);
+    if (period < 1 || period > 32) return cudaErrorInvalidValue;
+    if (multi) k_phantom<true><<<blocks, 256, smem, s>>>(waves, wi, pb, q, cnt, period);
+    else k_phantom<false><<<blocks, 256, smem, s>>>(waves, wi, pb, q, cnt, period);
     return cudaGetLastError();
 }
 
-cudaError_t launch_detector(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const SimDesc* sims,
-                            const QueueDev& q, const PulseDev& P, const HitDev& H, int rec_hits, Counters* cnt)
+cudaError_t launch_detector(bool multi, unsigned blocks, unsigned threads, size_t smem, cudaStream_t s,
+                            const SimDesc* sims, const QueueDev& q, const PulseDev& P, const HitDev& H, int rec_hits,
+                            Counters* cnt)
 {
-    if (multi) k_detector<true><<<blocks, 256, smem, s>>>(sims, q, P, H, rec_hits, cnt);
-    else k_detector<false><<<blocks, 256, smem, s>>>(sims, q, P, H, rec_hits, cnt);
+    if (!valid_threads(threads)) return cudaErrorInvalidValue;
+    if (multi) k_detector<true><<<blocks, threads, smem, s>>>(sims, q, P, H, rec_hits, cnt);
+    else k_detector<false><<<blocks, threads, smem, s>>>(sims, q, P, H, rec_hits, cnt);
     return cudaGetLastError();
 }
 
@@ -687,10 +699,10 @@ cudaError_t transport_kernels_loadable()
     return cudaFuncGetAttributes(&fa, k_phantom<false>);
 }
 
-template __global__ void k_source<false>(Wave, PairBuf, Counters*);
-template __global__ void k_source<true>(Wave, PairBuf, Counters*);
-template __global__ void k_phantom<false>(Wave, PairBuf, unsigned long long*, QueueDev, ExitRec*, Counters*);
-template __global__ void k_phantom<true>(Wave, PairBuf, unsigned long long*, QueueDev, ExitRec*, Counters*);
+template __global__ void k_source<false>(const Wave*, int, PairBuf, Counters*);
+template __global__ void k_source<true>(const Wave*, int, PairBuf, Counters*);
+template __global__ void k_phantom<false>(const Wave*, int, PairBuf, QueueDev, Counters*, int);
+template __global__ void k_phantom<true>(const Wave*, int, PairBuf, QueueDev, Counters*, int);
 template __global__ void k_detector<false>(const SimDesc*, QueueDev, PulseDev, HitDev, int, Counters*);
 template __global__ void k_detector<true>(const SimDesc*, QueueDev, PulseDev, HitDev, int, Counters*);
 

@@ -81,7 +81,11 @@ const char* gpet_last_error(gpet_ctx* ctx);
  *   coinc_window_ns (4), coinc_policy (0 single window with exactly two
  *   singles, 1 all pairs), record_hits (1), record_exits (0),
  *   base_dir (directory relative paths in input_PET.in resolve against),
- *   data_dir (table directory, default <base_dir>/data), chunk_decays. */
+ *   data_dir (table directory, default <base_dir>/data); launch shape
+ *   (results do not depend on it): sub_decays, chunk_decays,
+ *   phantom_blocks_per_sm, drain_period, detector_threads, source_threads,
+ *   use_graphs (1: each chunk's wave launches replay as one CUDA graph),
+ *   autotune (1: gpet_autotune on the first gpet_run). */
 int gpet_set_option(gpet_ctx* ctx, const char* key, const char* value);
 
 /* ------------------------------------------------------------ inputs */
@@ -123,6 +127,25 @@ int gpet_run(gpet_ctx* ctx, gpet_run_stats* stats);
  * simulation's counts; the timings are those of the whole job. record_exits
  * must be 0 when n > 1. */
 int gpet_run_batched(gpet_ctx* const* ctxs, int32_t n, gpet_run_stats* stats);
+/* No counterpart in the reference. Launch-shape parameters of the transport
+ * (also settable as options): none changes a result, only the time. */
+typedef struct {
+    int64_t sub_decays;            /* decays per wave (source -> phantom through L2), option sub_decays */
+    int64_t chunk_decays;          /* decays per detector pass (queue capacity), option chunk_decays */
+    int32_t phantom_blocks_per_sm; /* k_phantom occupancy, option phantom_blocks_per_sm (0 = as many as fit) */
+    int32_t drain_period;          /* k_phantom compaction period: staged photons taken through the panel
+                                      search once this many (1..32) wait, option drain_period */
+    int32_t detector_threads;      /* threads per k_detector block, option detector_threads */
+    int32_t source_threads;        /* threads per k_source block, option source_threads */
+    int32_t candidates;            /* shapes timed */
+    int64_t sample_decays;         /* decays each candidate ran */
+    double ms_default, ms_tuned;   /* transport device time of the sample, before and after */
+} gpet_tuning;
+/* Time candidate shapes on the first sample_decays (<= 0: min(total, 2^23))
+ * decays of this context's own workload, coordinate descent over the fields
+ * of gpet_tuning, and keep the fastest in the context. Discards the context's
+ * previous results. Option autotune=1 runs it on the first gpet_run. */
+int gpet_autotune(gpet_ctx* ctx, int64_t sample_decays, gpet_tuning* out);
 /* Digitizer + coincidence sorter alone on a caller pulse list (the digitizer
  * chain of gPET.cu:385-424): scat[i] != 0 marks a photon that scattered in the
  * phantom, slot[i] is the pulse's index within its photon's readout list. */
