@@ -18,6 +18,9 @@ GPET_OK = 0
 ERRORS = {-1: "bad argument or state", -2: "missing or malformed input file", -3: "CUDA runtime error",
           -4: "a bounded buffer overflowed", -5: "no CUDA device or kernels not built for it"}
 
+ENTRY_DTYPE = np.dtype([("panel", "<i4"), ("y", "<f4"), ("z", "<f4"), ("ux", "<f4"), ("uy", "<f4"), ("uz", "<f4"),
+                        ("E", "<f4"), ("crystal", "<i4"), ("depth", "<f4"), ("Edep", "<f4")])
+
 EXIT_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("ux", "<f4"), ("uy", "<f4"), ("uz", "<f4"),
                        ("E", "<f4"), ("nscat", "<i4"), ("t", "<f8"), ("status", "<i4"), ("panel", "<i4")])
 
@@ -45,7 +48,8 @@ class RunStats(C.Structure):
         (n, C.c_double) for n in ("ms_total", "ms_source_phantom", "ms_detector", "ms_digitizer",
                                   "ms_coincidence")] + [
         ("kernel_launches", C.c_int64), ("phantom_steps", C.c_int64), ("detector_steps", C.c_int64),
-        ("ms_source", C.c_double), ("ms_phantom", C.c_double)]
+        ("ms_source", C.c_double), ("ms_phantom", C.c_double), ("n_surrogate", C.c_int64),
+        ("ms_surrogate", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -79,6 +83,23 @@ def load_library(path=None):
     L.gpet_run.argtypes = [vp, C.POINTER(RunStats)]
     L.gpet_run_batched.argtypes = [C.POINTER(vp), i32, C.POINTER(RunStats)]
     L.gpet_autotune.argtypes = [vp, i64, C.POINTER(Tuning)]
+    f32p = C.POINTER(C.c_float)
+    L.gpet_get_entries.argtypes = [vp, vp, i64, C.POINTER(i64)]
+    L.gpet_surrogate_create.argtypes = [vp, C.c_uint64, C.POINTER(vp)]
+    L.gpet_surrogate_destroy.argtypes = [vp]
+    L.gpet_surrogate_destroy.restype = None
+    L.gpet_surrogate_last_error.argtypes = [vp]
+    L.gpet_surrogate_last_error.restype = C.c_char_p
+    L.gpet_surrogate_param_count.argtypes = [vp]
+    L.gpet_surrogate_param_count.restype = i64
+    L.gpet_surrogate_get_params.argtypes = [vp, vp, i64]
+    L.gpet_surrogate_set_params.argtypes = [vp, vp, i64]
+    L.gpet_surrogate_set_domain.argtypes = [vp, C.c_float, C.c_float, C.c_float, vp, i32]
+    L.gpet_surrogate_grad.argtypes = [vp, vp, i64, f32p, vp]
+    L.gpet_surrogate_forward.argtypes = [vp, vp, i64, vp]
+    L.gpet_surrogate_train.argtypes = [vp, vp, i64, i32, i32, C.c_float, C.c_uint64, vp]
+    L.gpet_set_surrogate.argtypes = [vp, vp]
+    L.gpet_umma_selftest.argtypes = [C.c_int, vp, vp, i32, i32, vp]
     L.gpet_digitize.argtypes = [vp, vp, vp, vp, i64, C.POINTER(RunStats)]
     L.gpet_get_singles.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
     L.gpet_get_pulses.argtypes = [vp, vp, vp, vp, i64, C.POINTER(i64)]
@@ -246,6 +267,19 @@ class Context:
             self._ck(self.L.gpet_get_exits(self.h, _ptr(out), n, C.byref(m)))
         return out
 
+    def entries(self):
+        """Entry records of the last run (option record_entries=1)."""
+        n = self._count(self.L.gpet_get_entries, None)
+        out = np.zeros(n, ENTRY_DTYPE)
+        m = C.c_int64()
+        if n:
+            self._ck(self.L.gpet_get_entries(self.h, _ptr(out), n, C.byref(m)))
+        return out
+
+    def set_surrogate(self, sur):
+        self._ck(self.L.gpet_set_surrogate(self.h, sur.h if sur is not None else None))
+        self._sur = sur      # keeps it alive while attached
+
     def write_outputs(self, out_dir):
         self._ck(self.L.gpet_write_outputs(self.h, os.fspath(out_dir).encode()))
 
@@ -299,3 +333,67 @@ def run_batched(contexts):
         msgs = "; ".join(sorted({c.L.gpet_last_error(c.h).decode(errors="replace") for c in ctxs} - {""}))
         raise GpetError(rc, msgs)
     return [s.as_dict() for s in st]
+
+
+class Surrogate:
+    """Learned detector response for a context's detector (gpet_surrogate_*)."""
+
+    def __init__(self, ctx, seed=1):
+        self.L = ctx.L
+        h = C.c_void_p()
+        rc = self.L.gpet_surrogate_create(ctx.h, seed, C.byref(h))
+        if rc != GPET_OK:
+            raise GpetError(rc, "gpet_surrogate_create failed (detector not supported or no GPU)")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gpet_surrogate_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        if rc != GPET_OK:
+            raise GpetError(rc, self.L.gpet_surrogate_last_error(self.h).decode(errors="replace"))
+
+    @property
+    def param_count(self):
+        return int(self.L.gpet_surrogate_param_count(self.h))
+
+    def params(self):
+        out = np.zeros(self.param_count, np.float32)
+        self._ck(self.L.gpet_surrogate_get_params(self.h, _ptr(out), len(out)))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        self._ck(self.L.gpet_surrogate_set_params(self.h, _ptr(p), len(p)))
+
+    def set_domain(self, e_lo, e_hi, margin, panel_ok=None):
+        po = None if panel_ok is None else np.ascontiguousarray(panel_ok, np.uint8)
+        self._ck(self.L.gpet_surrogate_set_domain(self.h, e_lo, e_hi, margin, _ptr(po),
+                                                  0 if po is None else len(po)))
+
+    def grad(self, rec):
+        rec = np.ascontiguousarray(rec, ENTRY_DTYPE)
+        g = np.zeros(self.param_count, np.float32)
+        loss = C.c_float()
+        self._ck(self.L.gpet_surrogate_grad(self.h, _ptr(rec), len(rec), C.byref(loss), _ptr(g)))
+        return loss.value, g
+
+    def forward(self, rec):
+        rec = np.ascontiguousarray(rec, ENTRY_DTYPE)
+        out = np.zeros((len(rec), 144), np.float32)
+        self._ck(self.L.gpet_surrogate_forward(self.h, _ptr(rec), len(rec), _ptr(out)))
+        return out
+
+    def train(self, rec, epochs=1, batch=8192, lr=1e-3, seed=7):
+        rec = np.ascontiguousarray(rec, ENTRY_DTYPE)
+        losses = np.zeros(epochs, np.float32)
+        self._ck(self.L.gpet_surrogate_train(self.h, _ptr(rec), len(rec), epochs, batch, lr, seed, _ptr(losses)))
+        return losses

@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
                      "-I" + os.path.join(ROOT, "include")]
-LIB_SOURCES = ["transport.cu", "digitizer.cu", "gpet_api.cu", "loaders.cpp", "digitize_static.cu"]
+LIB_SOURCES = ["transport.cu", "digitizer.cu", "gpet_api.cu", "loaders.cpp", "digitize_static.cu", "surrogate.cu"]
 
 
 def nvcc():
@@ -49,7 +49,7 @@ def build(verbose=False, extra_flags=()):
     os.makedirs(OUT, exist_ok=True)
     cc = nvcc()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh", ".hpp"))]
-    headers.append(os.path.join(ROOT, "include", "gpet.h"))
+    headers += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
     objs = []
     jobs = []
     for src in LIB_SOURCES:
@@ -77,7 +77,7 @@ def ptxas_report():
     """Registers / spills / shared memory per kernel (-Xptxas -v)."""
     cc = nvcc()
     out = []
-    for src in ("transport.cu", "digitizer.cu"):
+    for src in ("transport.cu", "digitizer.cu", "surrogate.cu"):
         r = subprocess.run([cc] + NVCC_FLAGS + ["-Xptxas", "-v", "-c", os.path.join(CSRC, src), "-o", os.devnull],
                            capture_output=True, text=True)
         out.append(r.stderr)

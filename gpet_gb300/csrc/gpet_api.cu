@@ -11,7 +11,9 @@
 
 #include "kernels.h"
 #include "loaders.hpp"
+#include "surrogate.h"
 #include "../../include/gpet.h"
+#include "../../include/gpet_surrogate.h"
 
 using namespace gpet;
 
@@ -41,9 +43,12 @@ struct DevBuf {
 struct Work {
     DevBuf q_f, q_t, q_i;                 // detector queue
     int64_t q_cap = 0;
+    DevBuf q2_f, q2_t, q2_i, sidx;        // with a surrogate: the Monte Carlo part of the queue, the surrogate's list
+    DevBuf ent;                           // entry records of one chunk
+    DevBuf serr;                          // surrogate kernel error flag
     DevBuf pb_f, pb_t, pb_n;              // emitted pairs of one wave
     int64_t pb_cap = 0;
-    DevBuf aux;                           // [0] queue count [1] pulses [2] hits [3] wave work counter
+    DevBuf aux;                           // [0] queue count [1] pulses [2] hits [4] Monte Carlo queue [5] surrogate list
     DevBuf cnt;                           // Counters per simulation
     DevBuf sims, prms, segs;              // batch descriptors
     DevBuf p_int, p_t, p_f, p_meta, p_sim;  // pulses: 6 int32, double, 4 float, byte, simulation
@@ -97,6 +102,8 @@ struct gpet_ctx {
     int use_graphs = 1;
     int autotune = 0;                     // tune the launch shape on the first run
     bool tuned = false;
+    int record_entries = 0;               // keep the entry records of the detector stage
+    gpet_surrogate* sur = nullptr;        // learned detector response (not owned)
     std::string base_dir = ".";
     std::string data_dir;
     // host scene
@@ -123,6 +130,7 @@ struct gpet_ctx {
     std::shared_ptr<Work> work;
     int res_sim = 0;
     std::vector<ExitRec> host_exits;
+    std::vector<EntryRec> host_entries;
     gpet_run_stats last{};
     bool have_results = false;
     cudaEvent_t ev[8] = {};
@@ -242,6 +250,7 @@ int gpet_set_option(gpet_ctx* c, const char* key, const char* value)
     else if (k == "source_threads") c->src_threads = (int)std::strtol(value, &end, 10);
     else if (k == "use_graphs") c->use_graphs = (int)std::strtol(value, &end, 10);
     else if (k == "autotune") c->autotune = (int)std::strtol(value, &end, 10);
+    else if (k == "record_entries") c->record_entries = (int)std::strtol(value, &end, 10);
     else if (k == "base_dir") { c->base_dir = v; return GPET_OK; }
     else if (k == "data_dir") { c->data_dir = v; return GPET_OK; }
     else return fail(c, GPET_ERR_ARG, "unknown option " + k);
@@ -694,6 +703,7 @@ static void fill_stats(const Counters& h, gpet_run_stats* st)
     st->n_stepcap = (int64_t)h.stepcap;
     st->phantom_steps = (int64_t)h.ph_steps;
     st->detector_steps = (int64_t)h.det_steps;
+    st->n_surrogate = (int64_t)h.n_surrogate;
 }
 
 // the leader's Work for a new run: reused unless other contexts still hold
@@ -832,8 +842,11 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
             if (cs[r] == x) return fail(c, GPET_ERR_ARG, "a context appears twice in the batch");
     }
     if (nsim > 1)
-        for (int s = 0; s < nsim; ++s)
+        for (int s = 0; s < nsim; ++s) {
             if (cs[s]->record_exits) return fail(c, GPET_ERR_ARG, "record_exits is for single runs");
+            if (cs[s]->record_entries) return fail(c, GPET_ERR_ARG, "record_entries is for single runs");
+            if (cs[s]->sur != c->sur) return fail(c, GPET_ERR_ARG, "the simulations of a batch share one surrogate or none");
+        }
     CK(cudaSetDevice(c->device));
     std::vector<int64_t> nd(nsim);
     int64_t ND = 0, max_site = 1;
@@ -920,6 +933,13 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         CK(W.q_i.ensure((size_t)2 * chunk * 5 * 4));
         W.q_cap = 2 * chunk;
     }
+    if (c->sur) {
+        CK(W.q2_f.ensure((size_t)W.q_cap * 7 * 4));
+        CK(W.q2_t.ensure((size_t)W.q_cap * 8));
+        CK(W.q2_i.ensure((size_t)W.q_cap * 5 * 4));
+        CK(W.sidx.ensure((size_t)W.q_cap * 4));
+    }
+    if (c->record_entries && !transport_only) CK(W.ent.ensure((size_t)W.q_cap * sizeof(EntryRec)));
     if (sub > W.pb_cap) {
         CK(W.pb_f.ensure((size_t)sub * 11 * 4));
         CK(W.pb_t.ensure((size_t)sub * 8));
@@ -930,6 +950,22 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     if (rc) return rc;
     if (rec_hits) { rc = grow_hits(c, W, 1 << 20, 0); if (rc) return rc; }
     const bool rec_exits = c->record_exits && !transport_only;
+    const bool rec_entries = c->record_entries && !transport_only;
+    c->host_entries.clear();
+    // the learned detector response, checked against every simulation's detector
+    SurrogateDev sdev{};
+    const bool use_sur = c->sur != nullptr;
+    if (use_sur) {
+        for (int s = 0; s < nsim; ++s) {
+            SurGeom g{};
+            int r2 = ctx_geometry(cs[s], &g);
+            if (r2) return fail(c, r2, "no detector geometry");
+            const char* why = "";
+            if (surrogate_view(c->sur, g, &sdev, &why)) return fail(cs[s], GPET_ERR_ARG, why);
+        }
+        CK(W.serr.ensure(4));
+        CK(cudaMemsetAsync(W.serr.p, 0, 4, c->stream));
+    }
     if (rec_exits) {
         CK(W.exits.ensure((size_t)2 * chunk * sizeof(ExitRec)));
         c->host_exits.assign((size_t)2 * ND, ExitRec{});
@@ -976,7 +1012,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         W.tev.push_back(e);
     }
     gpet_run_stats tot{};
-    float ms_det = 0, ms_src = 0, ms_ph = 0;
+    float ms_det = 0, ms_src = 0, ms_ph = 0, ms_sur = 0;
     cudaEventRecord(c->ev[0], c->stream);
     int64_t pulses_used = 0, hits_used = 0;
     size_t wi = 0;
@@ -1050,10 +1086,27 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         H.sim = multi ? W.h_sim.as<int32_t>() : nullptr;
         const int dt = c->det_threads;
         int64_t dblocks = std::min<int64_t>(((int64_t)hq + dt - 1) / dt, (int64_t)nsm * 8 * (256 / dt));
+        EntryRec* ent = rec_entries ? W.ent.as<EntryRec>() : nullptr;
         cudaEventRecord(c->ev[1], c->stream);
-        if (hq > 0) {
+        if (hq > 0 && use_sur) {
+            // photons in the surrogate's domain take the learned response, the
+            // others the Monte Carlo; the kernels read their counts on the device
+            QueueDev q2;
+            q2.f = W.q2_f.as<float>(); q2.t = W.q2_t.as<double>(); q2.i = W.q2_i.as<int32_t>();
+            q2.count = W.aux.as<unsigned long long>() + 4; q2.cap = W.q_cap;
+            unsigned long long* scount = W.aux.as<unsigned long long>() + 5;
+            CK(cudaMemsetAsync(q2.count, 0, 16, c->stream));
+            CK(launch_route(sdev, q, (int64_t)hq, q2, W.sidx.as<uint32_t>(), scount, c->stream));
             CK(launch_detector(multi, (unsigned)std::max<int64_t>(dblocks, 1), (unsigned)dt, smem, c->stream, d_sims,
-                               q, P, H, rec_hits ? 1 : 0, dcnt));
+                               q2, P, H, rec_hits ? 1 : 0, dcnt, ent));
+            cudaEventRecord(c->ev[6], c->stream);
+            CK(launch_surrogate(sdev, d_sims, q, W.sidx.as<uint32_t>(), scount, (int64_t)hq, P, dcnt,
+                                W.serr.as<int>(), c->stream));
+            cudaEventRecord(c->ev[7], c->stream);
+            tot.kernel_launches += 3;
+        } else if (hq > 0) {
+            CK(launch_detector(multi, (unsigned)std::max<int64_t>(dblocks, 1), (unsigned)dt, smem, c->stream, d_sims,
+                               q, P, H, rec_hits ? 1 : 0, dcnt, ent));
             tot.kernel_launches++;
         }
         cudaEventRecord(c->ev[2], c->stream);
@@ -1064,6 +1117,18 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         float ms = 0;
         cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
         ms_det += ms;
+        if (hq > 0 && use_sur) {
+            cudaEventElapsedTime(&ms, c->ev[6], c->ev[7]);
+            ms_sur += ms;
+        }
+        if (rec_entries && hq > 0) {
+            unsigned long long ne = hq;
+            if (use_sur) CK(cudaMemcpy(&ne, W.aux.as<unsigned long long>() + 4, 8, cudaMemcpyDeviceToHost));
+            const size_t old = c->host_entries.size();
+            c->host_entries.resize(old + (size_t)ne);
+            CK(cudaMemcpy(c->host_entries.data() + old, W.ent.p, (size_t)ne * sizeof(EntryRec),
+                          cudaMemcpyDeviceToHost));
+        }
         pulses_used = (int64_t)std::min<unsigned long long>(hp[0], (unsigned long long)W.p_cap);
         hits_used = (int64_t)std::min<unsigned long long>(hp[1], (unsigned long long)W.h_cap);
         wi = we;
@@ -1072,6 +1137,11 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     CK(cudaMemcpy(&h0, dcnt, sizeof(Counters), cudaMemcpyDeviceToHost));
     if (h0.queue_drop || h0.pulse_drop || h0.hit_drop)
         return fail(c, GPET_ERR_CAPACITY, "a device buffer overflowed (queue/pulse/hit drops)");
+    if (use_sur) {
+        int herr = 0;
+        CK(cudaMemcpy(&herr, W.serr.p, 4, cudaMemcpyDeviceToHost));
+        if (herr) return fail(c, GPET_ERR_CUDA, "a tensor-core wait of the surrogate gave up");
+    }
     W.n_pulses = pulses_used;
     W.n_hits = rec_hits ? hits_used : 0;
     if (transport_only) {
@@ -1104,6 +1174,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         st.ms_source = ms_src;
         st.ms_phantom = ms_ph;
         st.ms_detector = ms_det;
+        st.ms_surrogate = ms_sur;
         st.ms_digitizer = ms_digi;
         st.ms_coincidence = 0;
         cs[s]->work = c->work;
@@ -1514,6 +1585,56 @@ int gpet_write_outputs(gpet_ctx* c, const char* dir)
     for (int64_t i = 0; i < nc; ++i) { ce[2 * i] = sg[pr[2 * i]]; ce[2 * i + 1] = sg[pr[2 * i + 1]]; }
     if ((rc = append_file(c, d + "/coincidences.dat", ce.data(), sizeof(gpet_event) * ce.size()))) return rc;
     if ((rc = append_file(c, d + "/coincidences_class.dat", cl.data(), cl.size()))) return rc;
+    return GPET_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- surrogate glue
+namespace gpet {
+
+int ctx_geometry(const gpet_ctx* c, SurGeom* g)
+{
+    if (!c || !c->have_geo || c->geo.panels.empty()) return GPET_ERR_ARG;
+    std::memset(g, 0, sizeof(*g));
+    g->device = c->device;
+    g->npanels = c->geo.npanels;
+    for (int k = 0; k < 15; ++k) g->panel0[k] = c->geo.panels[k];
+    g->dirsign = c->geo.panels[18] < 0.0f ? -1.0f : 1.0f;
+    g->moduleN = c->geo.moduleN;
+    g->crystalN = c->geo.crystalN;
+    g->crystalNy = c->geo.crystalNy;
+    g->rdepth = c->have_cfg ? c->cfg.rdepth : 2;
+    g->rpolicy = c->have_cfg ? c->cfg.rpolicy : 1;
+    for (int k = 0; k < 2; ++k) { g->det_mat[k] = c->geo.det_mat[k]; g->det_den[k] = c->geo.det_den[k]; }
+    return GPET_OK;
+}
+
+}  // namespace gpet
+
+extern "C" {
+
+int gpet_set_surrogate(gpet_ctx* c, gpet_surrogate* s)
+{
+    if (!c) return GPET_ERR_ARG;
+    if (s) {
+        SurGeom g{};
+        if (ctx_geometry(c, &g)) return fail(c, GPET_ERR_ARG, "load the geometry before attaching a surrogate");
+        SurrogateDev d{};
+        const char* why = "";
+        if (surrogate_view(s, g, &d, &why)) return fail(c, GPET_ERR_ARG, why);
+    }
+    c->sur = s;
+    return GPET_OK;
+}
+
+int gpet_get_entries(gpet_ctx* c, gpet_entry* buf, int64_t cap, int64_t* n)
+{
+    if (!c || !n) return GPET_ERR_ARG;
+    *n = (int64_t)c->host_entries.size();
+    if (!buf || *n == 0) return GPET_OK;
+    if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the entry records");
+    std::memcpy(buf, c->host_entries.data(), sizeof(EntryRec) * (size_t)*n);
     return GPET_OK;
 }
 

@@ -63,7 +63,19 @@ struct Counters {
     unsigned long long pairs, entered, stepcap, ph_steps, det_steps, overflow, pulse_drop, hit_drop, queue_drop;
     unsigned long long n_thr, n_dead, n_single, n_coinc, n_true, n_scat, n_rand, n_mult;
     unsigned long long n_pulse, n_hit;
+    unsigned long long n_surrogate;   // photons whose response came from the surrogate
 };
+
+// a photon entering a panel and its detector response after adder and
+// readout (training data of the surrogate), 40 bytes
+struct EntryRec {
+    int32_t panel;
+    float y, z, ux, uy, uz, E;    // entry point and direction (panel-local), energy (eV)
+    int32_t crystal;              // crystal of its first pulse, -1: no pulse
+    float depth;                  // depth of that pulse below the entry face (cm)
+    float Edep;                   // its energy (eV)
+};
+static_assert(sizeof(EntryRec) == 40, "entry record is 40 bytes");
 
 // cnt[sim].field += v, lanes of a warp grouped by simulation (all lanes of the
 // warp must call it together)
@@ -129,7 +141,8 @@ template <bool kMulti> __global__ void k_source(const Wave* waves, int wi, PairB
 template <bool kMulti>
 __global__ void k_phantom(const Wave* waves, int wi, PairBuf pb, QueueDev q, Counters* cnt, int period);
 template <bool kMulti>
-__global__ void k_detector(const SimDesc* sims, QueueDev q, PulseDev P, HitDev H, int rec_hits, Counters* cnt);
+__global__ void k_detector(const SimDesc* sims, QueueDev q, PulseDev P, HitDev H, int rec_hits, Counters* cnt,
+                           EntryRec* entries);
 
 // host-side launchers (transport.cu): `multi` picks the kMulti instance,
 // smem is the dynamic shared memory (panels of the one simulation, or 0);
@@ -138,9 +151,10 @@ cudaError_t launch_source(bool multi, unsigned blocks, unsigned threads, size_t 
                           const Wave* waves, int wi, const PairBuf& pb, Counters* cnt);
 cudaError_t launch_phantom(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const Wave* waves, int wi,
                            const PairBuf& pb, const QueueDev& q, Counters* cnt, int period);
+// entries: one record per queue entry (or NULL)
 cudaError_t launch_detector(bool multi, unsigned blocks, unsigned threads, size_t smem, cudaStream_t s,
                             const SimDesc* sims, const QueueDev& q, const PulseDev& P, const HitDev& H, int rec_hits,
-                            Counters* cnt);
+                            Counters* cnt, EntryRec* entries);
 // resident k_phantom blocks per SM at 256 threads and `smem` bytes
 cudaError_t phantom_blocks_per_sm(bool multi, size_t smem, int* blocks);
 // cudaSuccess when the transport kernels have an image for the current device

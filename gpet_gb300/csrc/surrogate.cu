@@ -1,0 +1,1276 @@
+// surrogate.cu - the learned detector response (a new stage; the reference
+// always transports photons through the panels, gPET_kernals.cu:839-1233).
+//
+// Model: 14 inputs (entry point y, z in the panel, direction, energy, an
+// 8-wide learned panel embedding; padded to 16) -> 4 x 256 SiLU -> 140
+// outputs (64 crystal logits, a 4-component Gaussian mixture over the depth of
+// the pulse, 64 logits of the deposited-energy fraction; padded to 144).
+// BF16 weights and activations, FP32 accumulation in tensor memory.
+//
+//   k_mlp_fwd<train>  fused forward: one CTA of 128 threads per 128 samples;
+//                     activations stay in shared memory, each layer's weight
+//                     image arrives by bulk copy (the next one while the
+//                     current layer's epilogue runs), tcgen05.mma into TMEM,
+//                     epilogue (bias, SiLU, bf16) back into shared memory.
+//                     train: saves pre-activations and activations; else:
+//                     samples the response and appends pulses.
+//   k_umma_gemm       D (+)= A * B^T from strided global operands, split over
+//                     K: the backward products dH = dZ W and dW = dZ^T H.
+//   elementwise       features, loss and output gradient, SiLU backward,
+//                     bias and embedding gradients, Adam, weight images.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "surrogate.h"
+#include "umma.cuh"
+#include "../../include/gpet.h"
+#include "../../include/gpet_surrogate.h"
+
+namespace gpet {
+
+constexpr uint32_t kWaitLimit = 1u << 24;   // mbarrier polls before a wait gives up
+constexpr uint32_t kTagSurrogate = 6;       // Philox stream tag of the surrogate's draws
+
+namespace sg {
+constexpr int kIn = 16, kFeat = 14, kHid = 256, kOut = 144, kOutUsed = 140, kEmb = 8;
+constexpr int kCry = 64, kMix = 4, kBins = 64;
+constexpr int kColW = 64, kColMu = 68, kColLs = 72, kColE = 76;
+constexpr int kLayers = 5;
+constexpr float kLsMin = -7.0f, kLsMax = 3.0f;   // log sigma of a mixture component, clamped
+__host__ __device__ constexpr int fan_in(int l) { return l == 0 ? kIn : kHid; }
+__host__ __device__ constexpr int fan_out(int l) { return l == kLayers - 1 ? kOut : kHid; }
+__host__ __device__ constexpr int64_t w_off(int l)
+{
+    int64_t o = 0;
+    for (int i = 0; i < l; ++i) o += (int64_t)fan_out(i) * fan_in(i) + fan_out(i);
+    return o;
+}
+__host__ __device__ constexpr int64_t b_off(int l) { return w_off(l) + (int64_t)fan_out(l) * fan_in(l); }
+constexpr int64_t kEmbOff = w_off(kLayers);
+__host__ __device__ constexpr uint32_t img_off(int l)
+{
+    uint32_t o = 0;
+    for (int i = 0; i < l; ++i) o += (uint32_t)(fan_out(i) * fan_in(i) * 2);
+    return o;
+}
+constexpr uint32_t kImgBytes = img_off(kLayers);
+constexpr uint32_t kSmemA = 128 * kHid * 2;   // activations of 128 samples
+constexpr uint32_t kSmemB = kHid * kHid * 2;  // one weight image
+static_assert(kSmemB >= (uint32_t)kOut * kHid * 2, "head image fits");
+}  // namespace sg
+
+__device__ __forceinline__ float silu(float z) { return z / (1.0f + expf(-z)); }
+__device__ __forceinline__ float silu_grad(float z)
+{
+    const float s = 1.0f / (1.0f + expf(-z));
+    return s * (1.0f + z * (1.0f - s));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b)
+{
+    const __nv_bfloat16 x = __float2bfloat16_rn(a), y = __float2bfloat16_rn(b);
+    return (uint32_t)__bfloat16_as_ushort(x) | ((uint32_t)__bfloat16_as_ushort(y) << 16);
+}
+
+// 16 features of a photon entering a panel (the last two are zero)
+__device__ __forceinline__ void features(const SurrogateDev& sd, const float* __restrict__ emb, int panel, float y,
+                                         float z, float ux, float uy, float uz, float E, float f[16])
+{
+    f[0] = y / sd.half_y;
+    f[1] = z / sd.half_z;
+    f[2] = ux;
+    f[3] = uy;
+    f[4] = uz;
+    f[5] = E * (1.0f / 511000.0f);
+    for (int k = 0; k < sg::kEmb; ++k) f[6 + k] = emb[panel * sg::kEmb + k];
+    f[14] = 0.0f;
+    f[15] = 0.0f;
+}
+
+// ---------------------------------------------------------------- self-test
+// D[128 x N] = A[128 x K] * B[N x K]^T for one CTA of 128 threads: A and B
+// row-major bf16 in global memory, D row-major f32. K a multiple of 16 up to
+// 256, N a multiple of 16 up to 256.
+__global__ void __launch_bounds__(128) k_umma_selftest(const __nv_bfloat16* __restrict__ A,
+                                                       const __nv_bfloat16* __restrict__ B, int K, int N, float* D,
+                                                       int* err)
+{
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tbase;
+    unsigned char* sA = sm;
+    unsigned char* sB = sm + 128 * K * 2;
+    for (int i = threadIdx.x; i < 128 * K; i += 128)
+        *reinterpret_cast<__nv_bfloat16*>(sA + umma::img_offset(i / K, i % K, 128)) = A[i];
+    for (int i = threadIdx.x; i < N * K; i += 128)
+        *reinterpret_cast<__nv_bfloat16*>(sB + umma::img_offset(i / K, i % K, N)) = B[i];
+    const int warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        umma::mbar_init(&bar, 1);
+        umma::fence_mbar_init();
+    }
+    if (warp == 0) {
+        umma::tmem_alloc(&tbase, 256);
+        umma::tmem_relinquish();
+    }
+    umma::fence_proxy_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tbase;
+    if (threadIdx.x == 0) {
+        const uint32_t idesc = umma::idesc_bf16_f32(128, (uint32_t)N);
+        for (int ks = 0; ks < K / 16; ++ks) {
+            const uint64_t ad = umma::smem_desc(umma::smem_u32(sA) + ks * 2 * 128 * 16, 128 * 16, 128);
+            const uint64_t bd = umma::smem_desc(umma::smem_u32(sB) + ks * 2 * N * 16, (uint32_t)N * 16, 128);
+            umma::mma_bf16(tmem, ad, bd, idesc, ks > 0);
+        }
+        umma::mma_commit(&bar);
+    }
+    const bool ok = __syncthreads_and(umma::mbar_wait(&bar, 0, kWaitLimit));
+    umma::fence_after_sync();
+    if (!ok) {
+        if (threadIdx.x == 0) atomicOr(err, 1);
+    } else {
+        const uint32_t row = 32 * warp + (threadIdx.x & 31);
+        const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
+        for (int c = 0; c < N; c += 32) {
+            float v[32];
+            umma::tmem_ld32(taddr + c, v);
+            for (int j = 0; j < 32 && c + j < N; ++j) D[row * N + c + j] = v[j];
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, 256);
+}
+
+// ---------------------------------------------------------------- forward
+struct FwdTrain {
+    const __nv_bfloat16* X;       // [n][16]
+    int64_t n;
+    float* Z;                     // [4][n][256] pre-activations of the hidden layers
+    __nv_bfloat16* H;             // [4][n][256] their bf16 activations
+    float* out;                   // [n][144]
+};
+
+struct FwdInfer {
+    QueueDev q;
+    const uint32_t* sidx;
+    const unsigned long long* scount;
+    const SimDesc* sims;
+    PulseDev P;
+    Counters* cnt;
+};
+
+// a warp's 32 TMEM lanes, columns [c0, c0 + 32): all lanes must call it
+__device__ __forceinline__ void ld_cols(uint32_t taddr, int c0, float (&v)[32]) { umma::tmem_ld32(taddr + c0, v); }
+
+// sample a photon's response from the head's outputs (in TMEM) and append
+// its pulse; all 128 threads call it (the TMEM loads are warp-collective)
+__device__ __noinline__ void sample_and_append(const SurrogateDev& sd, const FwdInfer& in, uint32_t taddr, bool valid,
+                                               int sim, int panel, int parn, int eid, int scat, float E, float ux,
+                                               double t0, int lane)
+{
+    using namespace sg;
+    const float* bias = sd.params + b_off(kLayers - 1);
+    const SimDesc& S = in.sims[valid ? sim : 0];
+    Stream st;
+    st_init(st, S.key0, S.key1, kTagSurrogate, (uint64_t)(uint32_t)parn);
+    const float ue = st_u(st), uw = st_u(st), uc = st_u(st), um = st_u(st);
+    const float zn = st_normal(st);
+    // deposited-energy fraction: columns [76, 140)
+    float mx = -1e30f;
+    for (int c = 64; c < 160; c += 32) {
+        float v[32];
+        ld_cols(taddr, c, v);
+        for (int j = 0; j < 32; ++j) {
+            const int col = c + j;
+            if (col >= kColE && col < kColE + kBins) mx = fmaxf(mx, v[j] + bias[col]);
+        }
+    }
+    float sum = 0.0f;
+    for (int c = 64; c < 160; c += 32) {
+        float v[32];
+        ld_cols(taddr, c, v);
+        for (int j = 0; j < 32; ++j) {
+            const int col = c + j;
+            if (col >= kColE && col < kColE + kBins) sum += expf(v[j] + bias[col] - mx);
+        }
+    }
+    int bin = kBins - 1;
+    {
+        const float target = ue * sum;
+        float acc = 0.0f;
+        bool found = false;
+        for (int c = 64; c < 160; c += 32) {
+            float v[32];
+            ld_cols(taddr, c, v);
+            for (int j = 0; j < 32; ++j) {
+                const int col = c + j;
+                if (col >= kColE && col < kColE + kBins && !found) {
+                    acc += expf(v[j] + bias[col] - mx);
+                    if (acc >= target) { bin = col - kColE; found = true; }
+                }
+            }
+        }
+    }
+    // crystal: columns [0, crystalN)
+    float cm = -1e30f;
+    for (int c = 0; c < 64; c += 32) {
+        float v[32];
+        ld_cols(taddr, c, v);
+        for (int j = 0; j < 32; ++j)
+            if (c + j < sd.crystalN) cm = fmaxf(cm, v[j] + bias[c + j]);
+    }
+    float cs = 0.0f;
+    for (int c = 0; c < 64; c += 32) {
+        float v[32];
+        ld_cols(taddr, c, v);
+        for (int j = 0; j < 32; ++j)
+            if (c + j < sd.crystalN) cs += expf(v[j] + bias[c + j] - cm);
+    }
+    int cry = sd.crystalN - 1;
+    {
+        const float target = uc * cs;
+        float acc = 0.0f;
+        bool found = false;
+        for (int c = 0; c < 64; c += 32) {
+            float v[32];
+            ld_cols(taddr, c, v);
+            for (int j = 0; j < 32; ++j)
+                if (c + j < sd.crystalN && !found) {
+                    acc += expf(v[j] + bias[c + j] - cm);
+                    if (acc >= target) { cry = c + j; found = true; }
+                }
+        }
+    }
+    // depth: mixture columns [64, 76)
+    float depth_n;
+    {
+        float v[32];
+        ld_cols(taddr, 64, v);
+        float wm = -1e30f;
+        for (int k = 0; k < kMix; ++k) wm = fmaxf(wm, v[k] + bias[kColW + k]);
+        float ws = 0.0f;
+        for (int k = 0; k < kMix; ++k) ws += expf(v[k] + bias[kColW + k] - wm);
+        int comp = kMix - 1;
+        float acc = 0.0f;
+        for (int k = 0; k < kMix; ++k) {
+            acc += expf(v[k] + bias[kColW + k] - wm);
+            if (acc >= um * ws) { comp = k; break; }
+        }
+        const float mu = v[kColMu - 64 + comp] + bias[kColMu + comp];
+        const float ls = fminf(fmaxf(v[kColLs - 64 + comp] + bias[kColLs + comp], kLsMin), kLsMax);
+        depth_n = fminf(fmaxf(mu + expf(ls) * zn, 0.0f), 1.0f);
+    }
+    const bool pulse = valid && bin > 0;
+    const float Edep = bin == kBins - 1 ? E : ((float)bin + uw) * (1.0f / kBins) * E;
+    // append, one atomic per warp
+    const unsigned m = __ballot_sync(0xffffffffu, pulse);
+    unsigned long long base = 0;
+    if (m) {
+        const int leader = __ffs(m) - 1;
+        if (lane == leader) base = atomicAdd(in.P.count, (unsigned long long)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+    }
+    if (pulse) {
+        unsigned lt;
+        asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+        const unsigned long long o = base + __popc(m & lt);
+        if (o < (unsigned long long)in.P.cap) {
+            const float* Pn = S.panels + panel * kPanelStride;
+            const int32_t pann = (int32_t)Pn[30];
+            const int depth = S.rpolicy == 1 ? 2 : S.rdepth;
+            const int ly = cry % sd.crystalNy, lz = cry / sd.crystalNy;
+            const float dcm = depth_n * sd.depth;
+            in.P.parn[o] = parn;
+            in.P.pann[o] = pann;
+            in.P.modn[o] = 0;
+            in.P.cryn[o] = cry;
+            in.P.siten[o] = depth == 0 ? 0 : (depth == 1 ? pann : pann * S.moduleN);
+            in.P.eventid[o] = eid;
+            in.P.t[o] = t0 + (double)(dcm / fmaxf(fabsf(ux), 1e-6f) * DM_INV_SPEED);
+            in.P.E[o] = Edep;
+            in.P.x[o] = dcm * sd.dirsign;
+            in.P.y[o] = -sd.half_y + (float)ly * sd.cry_pitch_y + 0.5f * sd.cry_y;
+            in.P.z[o] = -sd.half_z + (float)lz * sd.cry_pitch_z + 0.5f * sd.cry_z;
+            in.P.meta[o] = (uint8_t)(scat ? 0x80 : 0);
+            if (in.P.sim) in.P.sim[o] = sim;
+        } else {
+            atomicAdd(&in.cnt->pulse_drop, 1ull);
+        }
+    }
+    add_by_sim(in.cnt, valid ? sim : 0, CF(n_pulse), pulse ? 1u : 0u);
+    add_by_sim(in.cnt, valid ? sim : 0, CF(n_surrogate), valid ? 1u : 0u);
+}
+
+template <bool kTrain>
+__global__ void __launch_bounds__(128, 1) k_mlp_fwd(SurrogateDev sd, FwdTrain tr, FwdInfer in, int* err)
+{
+    using namespace sg;
+    extern __shared__ __align__(128) unsigned char sm[];
+    unsigned char* sA = sm;
+    unsigned char* sB = sm + kSmemA;
+    __shared__ __align__(8) uint64_t bar_ld, bar_mma;
+    __shared__ uint32_t tbase;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int64_t n;
+    if (kTrain) {
+        n = tr.n;
+    } else {
+        unsigned long long c = *in.scount;
+        n = (int64_t)(c < (unsigned long long)in.q.cap ? c : (unsigned long long)in.q.cap);
+    }
+    if ((int64_t)blockIdx.x * 128 >= n) return;   // the whole CTA, before any barrier or allocation
+    if (threadIdx.x == 0) {
+        umma::mbar_init(&bar_ld, 1);
+        umma::mbar_init(&bar_mma, 1);
+        umma::fence_mbar_init();
+    }
+    if (warp == 0) {
+        umma::tmem_alloc(&tbase, 256);
+        umma::tmem_relinquish();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tbase;
+    const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
+    uint32_t n_ld = 0, n_mma = 0;   // completed phases of the two barriers
+    bool ok = true;
+    // persistent over tiles of 128 samples
+    for (int64_t row0 = (int64_t)blockIdx.x * 128; row0 < n && ok; row0 += (int64_t)gridDim.x * 128) {
+        const int64_t row = row0 + threadIdx.x;
+        const bool valid = row < n;
+        if (threadIdx.x == 0) {
+            umma::mbar_expect_tx(&bar_ld, (uint32_t)(fan_out(0) * fan_in(0) * 2));
+            umma::bulk_g2s(sB, sd.img + img_off(0), (uint32_t)(fan_out(0) * fan_in(0) * 2), &bar_ld);
+        }
+        // the photon (inference) and its features
+        float f[16];
+        int sim = 0, panel = 0, parn = 0, eid = 0, scat = 0;
+        float E = 0.0f, ux = 0.0f;
+        double t0 = 0.0;
+        for (int k = 0; k < 16; ++k) f[k] = 0.0f;
+        if (kTrain) {
+            if (valid) {
+                const uint4* x = reinterpret_cast<const uint4*>(tr.X + row * kIn);
+                const uint4 a = x[0], b = x[1];
+                const uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+                for (int k = 0; k < 8; ++k) {
+                    f[2 * k] = __uint_as_float(w[k] << 16);
+                    f[2 * k + 1] = __uint_as_float(w[k] & 0xffff0000u);
+                }
+            }
+        } else if (valid) {
+            const int64_t j = in.sidx[row];
+            const int64_t cap = in.q.cap;
+            const float y = in.q.f[1 * cap + j], z = in.q.f[2 * cap + j];
+            ux = in.q.f[3 * cap + j];
+            const float uy = in.q.f[4 * cap + j], uz = in.q.f[5 * cap + j];
+            E = in.q.f[6 * cap + j];
+            t0 = in.q.t[j];
+            panel = in.q.i[0 * cap + j];
+            parn = in.q.i[1 * cap + j];
+            eid = in.q.i[2 * cap + j];
+            scat = in.q.i[3 * cap + j];
+            sim = in.q.i[4 * cap + j];
+            features(sd, sd.params + kEmbOff, panel, y, z, ux, uy, uz, E, f);
+        }
+        {
+            uint4 a, b;
+            a.x = pack_bf16(f[0], f[1]); a.y = pack_bf16(f[2], f[3]); a.z = pack_bf16(f[4], f[5]);
+            a.w = pack_bf16(f[6], f[7]);
+            b.x = pack_bf16(f[8], f[9]); b.y = pack_bf16(f[10], f[11]); b.z = pack_bf16(f[12], f[13]);
+            b.w = pack_bf16(f[14], f[15]);
+            *reinterpret_cast<uint4*>(sA + umma::img_offset(threadIdx.x, 0, 128)) = a;
+            *reinterpret_cast<uint4*>(sA + umma::img_offset(threadIdx.x, 8, 128)) = b;
+        }
+        umma::fence_proxy_async();
+        umma::fence_before_sync();
+        __syncthreads();
+        umma::fence_after_sync();
+        for (int l = 0; l < kLayers; ++l) {
+            const int K = fan_in(l), N = fan_out(l);
+            ok = __syncthreads_and(umma::mbar_wait(&bar_ld, n_ld & 1u, kWaitLimit));
+            n_ld++;
+            if (!ok) break;
+            if (threadIdx.x == 0) {
+                umma::fence_after_sync();
+                const uint32_t idesc = umma::idesc_bf16_f32(128, (uint32_t)N);
+                for (int ks = 0; ks < K / 16; ++ks) {
+                    const uint64_t ad = umma::smem_desc(umma::smem_u32(sA) + ks * 2 * 128 * 16, 128 * 16, 128);
+                    const uint64_t bd =
+                        umma::smem_desc(umma::smem_u32(sB) + ks * 2 * N * 16, (uint32_t)N * 16, 128);
+                    umma::mma_bf16(tmem, ad, bd, idesc, ks > 0);
+                }
+                umma::mma_commit(&bar_mma);
+            }
+            ok = __syncthreads_and(umma::mbar_wait(&bar_mma, n_mma & 1u, kWaitLimit));
+            n_mma++;
+            umma::fence_after_sync();
+            if (!ok) break;
+            // the weight buffer is free: the next layer's image arrives during the epilogue
+            if (threadIdx.x == 0 && l + 1 < kLayers) {
+                const uint32_t bytes = (uint32_t)(fan_out(l + 1) * fan_in(l + 1) * 2);
+                umma::mbar_expect_tx(&bar_ld, bytes);
+                for (uint32_t o = 0; o < bytes; o += 32768u)
+                    umma::bulk_g2s(sB + o, sd.img + img_off(l + 1) + o, bytes - o < 32768u ? bytes - o : 32768u,
+                                   &bar_ld);
+            }
+            const float* bias = sd.params + b_off(l);
+            if (l + 1 < kLayers) {
+                for (int c = 0; c < kHid; c += 32) {
+                    float v[32];
+                    ld_cols(taddr, c, v);
+                    uint32_t hp[16];
+#pragma unroll
+                    for (int j = 0; j < 32; j += 2) {
+                        const float z0 = v[j] + bias[c + j], z1 = v[j + 1] + bias[c + j + 1];
+                        if (kTrain && valid) {
+                            float* zr = tr.Z + ((int64_t)l * tr.n + row) * kHid + c + j;
+                            zr[0] = z0;
+                            zr[1] = z1;
+                        }
+                        hp[j / 2] = pack_bf16(silu(z0), silu(z1));
+                    }
+                    if (kTrain && valid) {
+                        uint4* dst = reinterpret_cast<uint4*>(tr.H + ((int64_t)l * tr.n + row) * kHid + c);
+                        for (int q = 0; q < 4; ++q)
+                            dst[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
+                    }
+                    for (int q = 0; q < 4; ++q)
+                        *reinterpret_cast<uint4*>(sA + umma::img_offset(threadIdx.x, c + 8 * q, 128)) =
+                            make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
+                }
+            } else if (kTrain) {
+                for (int c = 0; c < kOut; c += 32) {
+                    float v[32];
+                    ld_cols(taddr, c, v);
+                    if (valid)
+                        for (int j = 0; j < 32 && c + j < kOut; ++j) tr.out[row * kOut + c + j] = v[j] + bias[c + j];
+                }
+            }
+            umma::fence_proxy_async();
+            umma::fence_before_sync();
+            __syncthreads();
+            umma::fence_after_sync();
+        }
+        if (!kTrain && ok) sample_and_append(sd, in, taddr, valid, sim, panel, parn, eid, scat, E, ux, t0, lane);
+        umma::fence_before_sync();
+        __syncthreads();
+        umma::fence_after_sync();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, 256);
+    if (!ok && threadIdx.x == 0) atomicOr(err, 1);
+}
+
+// ---------------------------------------------------------------- generic GEMM
+// element (r, k) of an operand: p[r * rs + k * ks], zero outside rows x K
+struct Opnd {
+    const void* p;
+    int32_t f32;                  // 1: float source (rounded to bf16), 0: bf16
+    int64_t rs, ks, rows;
+};
+
+__device__ __forceinline__ __nv_bfloat16 opnd_at(const Opnd& o, int64_t r, int64_t k)
+{
+    const int64_t i = r * o.rs + k * o.ks;
+    return o.f32 ? __float2bfloat16_rn(static_cast<const float*>(o.p)[i])
+                 : static_cast<const __nv_bfloat16*>(o.p)[i];
+}
+
+// fill an R x 64 operand image from rows [r0, r0 + R), columns [k0, k0 + 64)
+__device__ __forceinline__ void fill_image(unsigned char* img, const Opnd& o, int R, int64_t r0, int64_t k0, int64_t K)
+{
+    const bool kfast = o.ks == 1;
+    for (int i = threadIdx.x; i < R * 64; i += blockDim.x) {
+        const int r = kfast ? i / 64 : i % R;
+        const int k = kfast ? i % 64 : i / R;
+        const int64_t gr = r0 + r, gk = k0 + k;
+        const __nv_bfloat16 v = (gr < o.rows && gk < K) ? opnd_at(o, gr, gk) : __float2bfloat16_rn(0.0f);
+        *reinterpret_cast<__nv_bfloat16*>(img + umma::img_offset(r, k, R)) = v;
+    }
+}
+
+// D[r][n] (+)= sum_k A(r, k) B(n, k) for rows r in [128 blockIdx.x, +128),
+// n < N (a multiple of 16, <= 256), k in this CTA's split of [0, K)
+__global__ void __launch_bounds__(128) k_umma_gemm(Opnd A, Opnd B, int N, int64_t K, int64_t k_per_cta, float* D,
+                                                   int64_t ldd, int64_t d_rows, int atomic, int* err)
+{
+    extern __shared__ __align__(128) unsigned char sm[];
+    unsigned char* sA = sm;
+    unsigned char* sB = sm + 128 * 64 * 2;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tbase;
+    const int warp = threadIdx.x >> 5;
+    const int64_t m0 = (int64_t)blockIdx.x * 128;
+    const int64_t kb = (int64_t)blockIdx.y * k_per_cta;
+    const int64_t ke = kb + k_per_cta < K ? kb + k_per_cta : K;
+    if (kb >= ke) return;
+    if (threadIdx.x == 0) {
+        umma::mbar_init(&bar, 1);
+        umma::fence_mbar_init();
+    }
+    if (warp == 0) {
+        umma::tmem_alloc(&tbase, 256);
+        umma::tmem_relinquish();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tbase;
+    bool ok = true;
+    uint32_t phase = 0;
+    for (int64_t kc = kb; kc < ke && ok; kc += 64, phase ^= 1u) {
+        fill_image(sA, A, 128, m0, kc, ke);
+        fill_image(sB, B, N, 0, kc, ke);
+        umma::fence_proxy_async();
+        umma::fence_before_sync();
+        __syncthreads();
+        umma::fence_after_sync();
+        if (threadIdx.x == 0) {
+            const uint32_t idesc = umma::idesc_bf16_f32(128, (uint32_t)N);
+            for (int ks = 0; ks < 4; ++ks) {
+                const uint64_t ad = umma::smem_desc(umma::smem_u32(sA) + ks * 2 * 128 * 16, 128 * 16, 128);
+                const uint64_t bd = umma::smem_desc(umma::smem_u32(sB) + ks * 2 * N * 16, (uint32_t)N * 16, 128);
+                umma::mma_bf16(tmem, ad, bd, idesc, kc > kb || ks > 0);
+            }
+            umma::mma_commit(&bar);
+        }
+        ok = __syncthreads_and(umma::mbar_wait(&bar, phase, kWaitLimit));
+        umma::fence_after_sync();
+    }
+    if (ok) {
+        const int64_t r = m0 + 32 * warp + (threadIdx.x & 31);
+        const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
+        for (int c = 0; c < N; c += 32) {
+            float v[32];
+            umma::tmem_ld32(taddr + c, v);
+            if (r < d_rows)
+                for (int j = 0; j < 32 && c + j < N; ++j) {
+                    if (atomic) atomicAdd(&D[r * ldd + c + j], v[j]);
+                    else D[r * ldd + c + j] = v[j];
+                }
+        }
+    } else if (threadIdx.x == 0) {
+        atomicOr(err, 1);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, 256);
+}
+
+// ---------------------------------------------------------------- training kernels
+// features and targets of entry records; the embedding comes from params
+__global__ void k_entry_features(const EntryRec* __restrict__ rec, int64_t n, SurrogateDev sd,
+                                 const float* __restrict__ params, __nv_bfloat16* X, int32_t* cry, float* dep,
+                                 int32_t* bin, int32_t* panel)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const EntryRec e = rec[i];
+        float f[16];
+        features(sd, params + sg::kEmbOff, e.panel, e.y, e.z, e.ux, e.uy, e.uz, e.E, f);
+        uint4 a, b;
+        a.x = pack_bf16(f[0], f[1]); a.y = pack_bf16(f[2], f[3]); a.z = pack_bf16(f[4], f[5]); a.w = pack_bf16(f[6], f[7]);
+        b.x = pack_bf16(f[8], f[9]); b.y = pack_bf16(f[10], f[11]); b.z = pack_bf16(f[12], f[13]);
+        b.w = pack_bf16(f[14], f[15]);
+        reinterpret_cast<uint4*>(X + i * sg::kIn)[0] = a;
+        reinterpret_cast<uint4*>(X + i * sg::kIn)[1] = b;
+        const bool has = e.crystal >= 0 && e.Edep > 0.0f;
+        cry[i] = has ? e.crystal : -1;
+        dep[i] = has ? e.depth / sd.depth : 0.0f;
+        int b2 = 0;
+        if (has) {
+            b2 = (int)(e.Edep / e.E * (float)sg::kBins);
+            b2 = b2 < 1 ? 1 : (b2 > sg::kBins - 1 ? sg::kBins - 1 : b2);
+        }
+        bin[i] = b2;
+        panel[i] = e.panel;
+    }
+}
+
+// loss of each sample and d loss / d output (mean over the n samples)
+__global__ void k_loss(const float* __restrict__ out, int64_t n, const int32_t* __restrict__ cry,
+                       const float* __restrict__ dep, const int32_t* __restrict__ bin, int crystalN, float* dout,
+                       float* loss_sum)
+{
+    using namespace sg;
+    __shared__ float red[8];
+    const float scale = 1.0f / (float)n;
+    float lsum = 0.0f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float* o = out + i * kOut;
+        float* d = dout + i * kOut;
+        for (int c = 0; c < kOut; ++c) d[c] = 0.0f;
+        // energy fraction: cross entropy over 64 bins
+        {
+            float mx = -1e30f;
+            for (int k = 0; k < kBins; ++k) mx = fmaxf(mx, o[kColE + k]);
+            float s = 0.0f;
+            for (int k = 0; k < kBins; ++k) s += expf(o[kColE + k] - mx);
+            const float lse = mx + logf(s);
+            lsum += lse - o[kColE + bin[i]];
+            for (int k = 0; k < kBins; ++k)
+                d[kColE + k] = (expf(o[kColE + k] - lse) - (k == bin[i] ? 1.0f : 0.0f)) * scale;
+        }
+        if (cry[i] >= 0) {
+            float mx = -1e30f;
+            for (int k = 0; k < crystalN; ++k) mx = fmaxf(mx, o[k]);
+            float s = 0.0f;
+            for (int k = 0; k < crystalN; ++k) s += expf(o[k] - mx);
+            const float lse = mx + logf(s);
+            lsum += lse - o[cry[i]];
+            for (int k = 0; k < crystalN; ++k) d[k] = (expf(o[k] - lse) - (k == cry[i] ? 1.0f : 0.0f)) * scale;
+            // depth: Gaussian mixture negative log likelihood
+            const float x = dep[i];
+            float lw[kMix], lp[kMix], ls[kMix], mu[kMix];
+            float wm = -1e30f;
+            for (int k = 0; k < kMix; ++k) wm = fmaxf(wm, o[kColW + k]);
+            float ws = 0.0f;
+            for (int k = 0; k < kMix; ++k) ws += expf(o[kColW + k] - wm);
+            const float wlse = wm + logf(ws);
+            float pm = -1e30f;
+            for (int k = 0; k < kMix; ++k) {
+                lw[k] = o[kColW + k] - wlse;
+                mu[k] = o[kColMu + k];
+                ls[k] = fminf(fmaxf(o[kColLs + k], kLsMin), kLsMax);
+                const float zz = (x - mu[k]) * expf(-ls[k]);
+                lp[k] = lw[k] - 0.5f * zz * zz - ls[k] - 0.91893853320467274f;
+                pm = fmaxf(pm, lp[k]);
+            }
+            float ps = 0.0f;
+            for (int k = 0; k < kMix; ++k) ps += expf(lp[k] - pm);
+            const float plse = pm + logf(ps);
+            lsum += -plse;
+            for (int k = 0; k < kMix; ++k) {
+                const float g = expf(lp[k] - plse);     // responsibility
+                const float pw = expf(lw[k]);
+                const float iv = expf(-2.0f * ls[k]);
+                const float dx = x - mu[k];
+                d[kColW + k] = (pw - g) * scale;
+                d[kColMu + k] = -g * dx * iv * scale;
+                const float raw = o[kColLs + k];
+                d[kColLs + k] = (raw > kLsMin && raw < kLsMax) ? -g * (dx * dx * iv - 1.0f) * scale : 0.0f;
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lsum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float s = 0.0f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+        atomicAdd(loss_sum, s * scale);
+    }
+}
+
+// dZ = dH * SiLU'(Z), in place on dH
+__global__ void k_silu_back(float* dH, const float* __restrict__ Z, int64_t count)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+        dH[i] *= silu_grad(Z[i]);
+}
+
+// column sums of a [n][cols] matrix into g (+=)
+__global__ void k_colsum(const float* __restrict__ M, int64_t n, int cols, float* g)
+{
+    const int c = blockIdx.x;
+    float s = 0.0f;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += M[i * cols + c];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ float red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.0f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        g[c] += t;
+    }
+}
+
+// embedding gradient: the input gradient's columns 6..13, by panel
+__global__ void k_emb_grad(const float* __restrict__ dX, const int32_t* __restrict__ panel, int64_t n, float* gemb)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * sg::kEmb;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = i / sg::kEmb;
+        const int k = (int)(i % sg::kEmb);
+        atomicAdd(&gemb[panel[s] * sg::kEmb + k], dX[s * sg::kIn + 6 + k]);
+    }
+}
+
+// padding entries of the parameter vector (inputs 14, 15 of the first layer,
+// outputs 140..143 of the head) stay zero
+__device__ __forceinline__ bool is_pad(int64_t i)
+{
+    using namespace sg;
+    if (i < b_off(0)) return ((i - w_off(0)) % fan_in(0)) >= kFeat;
+    if (i >= w_off(kLayers - 1) && i < b_off(kLayers - 1)) return (i - w_off(kLayers - 1)) / kHid >= kOutUsed;
+    if (i >= b_off(kLayers - 1) && i < kEmbOff) return (i - b_off(kLayers - 1)) >= kOutUsed;
+    return false;
+}
+
+__global__ void k_adam(float* p, const float* __restrict__ g, float* m, float* v, int64_t n, float lr, float b1,
+                       float b2, float eps, float c1, float c2)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (is_pad(i)) {
+            p[i] = 0.0f;
+            continue;
+        }
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.0f - b1) * gi;
+        const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+    }
+}
+
+// bf16 copies of the weights: row-major (backward operands) and operand
+// images (forward)
+__global__ void k_weights(const float* __restrict__ p, __nv_bfloat16* wrow, unsigned char* img)
+{
+    using namespace sg;
+    int64_t total = 0;
+    for (int l = 0; l < kLayers; ++l) total += (int64_t)fan_out(l) * fan_in(l);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        int l = 0;
+        int64_t j = i;
+        while (j >= (int64_t)fan_out(l) * fan_in(l)) {
+            j -= (int64_t)fan_out(l) * fan_in(l);
+            ++l;
+        }
+        const int K = fan_in(l), N = fan_out(l);
+        const int o = (int)(j / K), k = (int)(j % K);
+        const __nv_bfloat16 v = __float2bfloat16_rn(p[w_off(l) + j]);
+        wrow[w_off(l) + j] = v;
+        *reinterpret_cast<__nv_bfloat16*>(img + img_off(l) + umma::img_offset(o, k, N)) = v;
+    }
+}
+
+// split the queue: photons in the validated domain -> sidx, the rest -> q2
+__global__ void k_route(SurrogateDev sd, QueueDev q, QueueDev q2, uint32_t* sidx, unsigned long long* scount)
+{
+    unsigned long long c = *q.count;
+    const int64_t n = (int64_t)(c < (unsigned long long)q.cap ? c : (unsigned long long)q.cap);
+    const int lane = threadIdx.x & 31;
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = base + threadIdx.x;
+        const bool valid = j < n;
+        bool elig = false;
+        if (valid) {
+            const float y = q.f[1 * q.cap + j], z = q.f[2 * q.cap + j], E = q.f[6 * q.cap + j];
+            const int panel = q.i[0 * q.cap + j];
+            elig = E >= sd.e_lo && E <= sd.e_hi && fabsf(y) <= sd.half_y - sd.margin &&
+                   fabsf(z) <= sd.half_z - sd.margin && panel >= 0 && panel < sd.npanels && sd.panel_ok[panel];
+        }
+        const unsigned ms = __ballot_sync(0xffffffffu, elig);
+        if (ms) {
+            unsigned long long b = 0;
+            const int leader = __ffs(ms) - 1;
+            if (lane == leader) b = atomicAdd(scount, (unsigned long long)__popc(ms));
+            b = __shfl_sync(0xffffffffu, b, leader);
+            if (elig) sidx[b + __popc(ms & lt)] = (uint32_t)j;
+        }
+        const bool mc = valid && !elig;
+        const unsigned mm = __ballot_sync(0xffffffffu, mc);
+        if (mm) {
+            unsigned long long b = 0;
+            const int leader = __ffs(mm) - 1;
+            if (lane == leader) b = atomicAdd(q2.count, (unsigned long long)__popc(mm));
+            b = __shfl_sync(0xffffffffu, b, leader);
+            const unsigned long long o = b + __popc(mm & lt);
+            if (mc && o < (unsigned long long)q2.cap) {
+                for (int a = 0; a < 7; ++a) q2.f[a * q2.cap + o] = q.f[a * q.cap + j];
+                q2.t[o] = q.t[j];
+                for (int a = 0; a < 5; ++a) q2.i[a * q2.cap + o] = q.i[a * q.cap + j];
+            }
+        }
+    }
+}
+
+static unsigned grid_cap(int64_t n, int threads, int64_t cap)
+{
+    int64_t b = (n + threads - 1) / threads;
+    return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+static int sm_count()
+{
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+cudaError_t launch_route(const SurrogateDev& sd, const QueueDev& q, int64_t max_n, const QueueDev& q2,
+                         uint32_t* sidx, unsigned long long* scount, cudaStream_t s)
+{
+    k_route<<<grid_cap(max_n, 256, (int64_t)sm_count() * 8), 256, 0, s>>>(sd, q, q2, sidx, scount);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_surrogate(const SurrogateDev& sd, const SimDesc* sims, const QueueDev& q, const uint32_t* sidx,
+                             const unsigned long long* scount, int64_t max_n, const PulseDev& P, Counters* cnt,
+                             int* err, cudaStream_t s)
+{
+    const int smem = (int)(sg::kSmemA + sg::kSmemB);
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_fwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    FwdInfer in{q, sidx, scount, sims, P, cnt};
+    FwdTrain tr{};
+    k_mlp_fwd<false><<<grid_cap(max_n, 128, sm_count()), 128, smem, s>>>(sd, tr, in, err);
+    return cudaGetLastError();
+}
+
+}  // namespace gpet
+
+// ---------------------------------------------------------------- host object
+using namespace gpet;
+
+namespace {
+
+struct Buf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~Buf() { if (p) cudaFree(p); }
+    cudaError_t ensure(size_t n)
+    {
+        if (n <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, n ? n : 16);
+        if (e == cudaSuccess) bytes = n;
+        return e;
+    }
+    template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+uint64_t splitmix(uint64_t& x)
+{
+    uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+}  // namespace
+
+static_assert(sizeof(gpet_entry) == sizeof(EntryRec), "entry record layouts agree");
+
+struct gpet_surrogate {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    SurGeom geom{};
+    float e_lo = 100000.0f, e_hi = 520000.0f, margin = 0.3f;
+    std::vector<uint8_t> panel_ok;
+    int64_t nparam = 0;
+    int64_t adam_t = 0;
+    Buf params, grads, adam_m, adam_v, wrow, img, panel_ok_d, errflag, loss;
+    // training batch scratch
+    int64_t cap = 0;
+    Buf X, Z, H, out, dout, dA, dB, cry, dep, bin, pan, rec;
+};
+
+namespace {
+
+int sfail(gpet_surrogate* s, int code, const std::string& m)
+{
+    if (s) s->err = m;
+    return code;
+}
+
+#define SCK(call)                                                                              \
+    do {                                                                                       \
+        cudaError_t e__ = (call);                                                              \
+        if (e__ != cudaSuccess) return sfail(s, GPET_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e__)); \
+    } while (0)
+
+SurrogateDev make_view(const gpet_surrogate* s)
+{
+    SurrogateDev d{};
+    const SurGeom& g = s->geom;
+    d.params = s->params.as<float>();
+    d.img = s->img.as<unsigned char>();
+    d.panel_ok = s->panel_ok_d.as<uint8_t>();
+    d.npanels = g.npanels;
+    d.half_y = 0.5f * g.panel0[1];
+    d.half_z = 0.5f * g.panel0[2];
+    d.depth = g.panel0[0];
+    d.dirsign = g.dirsign;
+    d.e_lo = s->e_lo;
+    d.e_hi = s->e_hi;
+    d.margin = s->margin;
+    d.crystalN = g.crystalN;
+    d.crystalNy = g.crystalNy;
+    d.rdepth = g.rdepth;
+    d.rpolicy = g.rpolicy;
+    d.moduleN = g.moduleN;
+    d.cry_y = g.panel0[10];
+    d.cry_z = g.panel0[11];
+    d.cry_pitch_y = g.panel0[10] + g.panel0[13];
+    d.cry_pitch_z = g.panel0[11] + g.panel0[14];
+    return d;
+}
+
+int refresh_weights(gpet_surrogate* s)
+{
+    k_weights<<<152 * 4, 256, 0, s->stream>>>(s->params.as<float>(), s->wrow.as<__nv_bfloat16>(),
+                                             s->img.as<unsigned char>());
+    SCK(cudaGetLastError());
+    return GPET_OK;
+}
+
+int ensure_batch(gpet_surrogate* s, int64_t n)
+{
+    using namespace sg;
+    if (n <= s->cap) return GPET_OK;
+    const int64_t c = std::max<int64_t>(n, 1024);
+    SCK(s->X.ensure((size_t)c * kIn * 2));
+    SCK(s->Z.ensure((size_t)4 * c * kHid * 4));
+    SCK(s->H.ensure((size_t)4 * c * kHid * 2));
+    SCK(s->out.ensure((size_t)c * kOut * 4));
+    SCK(s->dout.ensure((size_t)c * kOut * 4));
+    SCK(s->dA.ensure((size_t)c * kHid * 4));
+    SCK(s->dB.ensure((size_t)c * kHid * 4));
+    SCK(s->cry.ensure((size_t)c * 4));
+    SCK(s->dep.ensure((size_t)c * 4));
+    SCK(s->bin.ensure((size_t)c * 4));
+    SCK(s->pan.ensure((size_t)c * 4));
+    SCK(s->rec.ensure((size_t)c * sizeof(EntryRec)));
+    s->cap = c;
+    return GPET_OK;
+}
+
+// D = A * B^T over K, strided operands; d_rows rows of D are written
+// k_umma_gemm uses 48 KB of shared memory but asks for 96 KB, so that at most
+// two CTAs share an SM and their TMEM (2 x 256 of 512 columns) always fits
+constexpr int kGemmSmem = 96 * 1024;
+
+int gemm(gpet_surrogate* s, const Opnd& A, int64_t m_rows, const Opnd& B, int N, int64_t K, float* D, int64_t ldd,
+         bool atomic)
+{
+    const int smem = kGemmSmem;
+    const int64_t mt = (m_rows + 127) / 128;
+    int64_t splits = 1, kper = K;
+    if (atomic) {
+        splits = std::max<int64_t>(1, std::min<int64_t>((K + 63) / 64, std::max<int64_t>(1, 152 / mt)));
+        kper = ((K + splits - 1) / splits + 63) / 64 * 64;
+        splits = (K + kper - 1) / kper;
+    }
+    dim3 grid((unsigned)mt, (unsigned)splits);
+    k_umma_gemm<<<grid, 128, smem, s->stream>>>(A, B, N, K, kper, D, ldd, m_rows, atomic ? 1 : 0,
+                                                 s->errflag.as<int>());
+    SCK(cudaGetLastError());
+    return GPET_OK;
+}
+
+// forward + loss + backward of n samples already in s->rec; gradients into
+// s->grads (zeroed here), mean loss into *loss
+int loss_and_grad(gpet_surrogate* s, int64_t n, float* loss)
+{
+    using namespace sg;
+    int rc = ensure_batch(s, n);
+    if (rc) return rc;
+    SurrogateDev sd = make_view(s);
+    cudaStream_t st = s->stream;
+    const unsigned g1 = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    k_entry_features<<<g1, 256, 0, st>>>(s->rec.as<EntryRec>(), n, sd, s->params.as<float>(), s->X.as<__nv_bfloat16>(),
+                                         s->cry.as<int32_t>(), s->dep.as<float>(), s->bin.as<int32_t>(),
+                                         s->pan.as<int32_t>());
+    FwdTrain tr{s->X.as<__nv_bfloat16>(), n, s->Z.as<float>(), s->H.as<__nv_bfloat16>(), s->out.as<float>()};
+    FwdInfer in{};
+    const int smem = (int)(kSmemA + kSmemB);
+    SCK(cudaFuncSetAttribute(k_mlp_fwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    SCK(cudaFuncSetAttribute(k_umma_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem));
+    k_mlp_fwd<true><<<grid_cap(n, 128, 152), 128, smem, st>>>(sd, tr, in, s->errflag.as<int>());
+    SCK(cudaGetLastError());
+    SCK(cudaMemsetAsync(s->loss.p, 0, 4, st));
+    SCK(cudaMemsetAsync(s->grads.p, 0, (size_t)s->nparam * 4, st));
+    k_loss<<<g1, 256, 0, st>>>(s->out.as<float>(), n, s->cry.as<int32_t>(), s->dep.as<float>(), s->bin.as<int32_t>(),
+                               s->geom.crystalN, s->dout.as<float>(), s->loss.as<float>());
+    SCK(cudaGetLastError());
+    float* G = s->grads.as<float>();
+    const __nv_bfloat16* Wb = s->wrow.as<__nv_bfloat16>();
+    // layer by layer from the head down; dZ of layer l lives in `dz`
+    float* dz = s->dout.as<float>();
+    float* dh_next = s->dA.as<float>();
+    float* dh_other = s->dB.as<float>();
+    for (int l = kLayers - 1; l >= 0; --l) {
+        const int K = fan_in(l), N = fan_out(l);
+        // dW = dZ^T * input: rows N (outputs), K columns (inputs), sum over samples
+        Opnd A{dz, 1, 1, N, N};
+        Opnd B = l == 0 ? Opnd{s->X.as<__nv_bfloat16>(), 0, 1, kIn, K}
+                        : Opnd{s->H.as<__nv_bfloat16>() + (int64_t)(l - 1) * n * kHid, 0, 1, kHid, K};
+        rc = gemm(s, A, N, B, K, n, G + w_off(l), K, true);
+        if (rc) return rc;
+        k_colsum<<<N, 256, 0, st>>>(dz, n, N, G + b_off(l));
+        SCK(cudaGetLastError());
+        // dInput = dZ * W: n rows, K columns, sum over the N outputs
+        Opnd Ad{dz, 1, N, 1, n};
+        Opnd Bw{Wb + w_off(l), 0, 1, K, K};   // B(r = input k, c = output o) = W[o][k]
+        rc = gemm(s, Ad, n, Bw, K, N, dh_next, K, false);
+        if (rc) return rc;
+        if (l > 0) {
+            k_silu_back<<<152 * 8, 256, 0, st>>>(dh_next, s->Z.as<float>() + (int64_t)(l - 1) * n * kHid,
+                                                 n * (int64_t)kHid);
+            SCK(cudaGetLastError());
+            dz = dh_next;
+            std::swap(dh_next, dh_other);
+        } else {
+            k_emb_grad<<<g1, 256, 0, st>>>(dh_next, s->pan.as<int32_t>(), n, G + kEmbOff);
+            SCK(cudaGetLastError());
+        }
+    }
+    int herr = 0;
+    SCK(cudaMemcpyAsync(&herr, s->errflag.p, 4, cudaMemcpyDeviceToHost, st));
+    if (loss) SCK(cudaMemcpyAsync(loss, s->loss.p, 4, cudaMemcpyDeviceToHost, st));
+    SCK(cudaStreamSynchronize(st));
+    if (herr) return sfail(s, GPET_ERR_CUDA, "a tensor-core wait gave up");
+    return GPET_OK;
+}
+
+}  // namespace
+
+namespace gpet {
+
+int surrogate_view(const gpet_surrogate* s, const SurGeom& g, SurrogateDev* out, const char** why)
+{
+    const SurGeom& h = s->geom;
+    bool same = h.device == g.device && h.npanels == g.npanels && h.moduleN == g.moduleN && h.crystalN == g.crystalN &&
+                h.crystalNy == g.crystalNy && h.rdepth == g.rdepth && h.rpolicy == g.rpolicy &&
+                h.dirsign == g.dirsign;
+    for (int k = 0; k < 15 && same; ++k) same = h.panel0[k] == g.panel0[k];
+    for (int k = 0; k < 2 && same; ++k) same = h.det_mat[k] == g.det_mat[k] && h.det_den[k] == g.det_den[k];
+    if (!same) {
+        *why = "the surrogate was made for another detector (geometry, materials or readout)";
+        return GPET_ERR_ARG;
+    }
+    *out = make_view(s);
+    return GPET_OK;
+}
+
+}  // namespace gpet
+
+extern "C" {
+
+int gpet_umma_selftest(int device, const uint16_t* a_bf16, const uint16_t* b_bf16, int32_t K, int32_t N,
+                       float* d_out)
+{
+    if (!a_bf16 || !b_bf16 || !d_out || K < 16 || K > 256 || K % 16 || N < 16 || N > 256 || N % 16)
+        return GPET_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return GPET_ERR_NOGPU;
+    __nv_bfloat16 *dA = nullptr, *dB = nullptr;
+    float* dD = nullptr;
+    int* dErr = nullptr;
+    int rc = GPET_OK;
+    const size_t smem = (size_t)(128 + N) * K * 2;
+    if (cudaMalloc(&dA, 128 * K * 2) != cudaSuccess || cudaMalloc(&dB, (size_t)N * K * 2) != cudaSuccess ||
+        cudaMalloc(&dD, (size_t)128 * N * 4) != cudaSuccess || cudaMalloc(&dErr, 4) != cudaSuccess) {
+        rc = GPET_ERR_CUDA;
+    } else {
+        cudaMemcpy(dA, a_bf16, 128 * K * 2, cudaMemcpyHostToDevice);
+        cudaMemcpy(dB, b_bf16, (size_t)N * K * 2, cudaMemcpyHostToDevice);
+        cudaMemset(dD, 0, (size_t)128 * N * 4);
+        cudaMemset(dErr, 0, 4);
+        cudaFuncSetAttribute(k_umma_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_umma_selftest<<<1, 128, smem>>>(dA, dB, K, N, dD, dErr);
+        int herr = 0;
+        if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = GPET_ERR_CUDA;
+        else if (cudaMemcpy(&herr, dErr, 4, cudaMemcpyDeviceToHost) != cudaSuccess || herr) rc = GPET_ERR_CUDA;
+        else if (cudaMemcpy(d_out, dD, (size_t)128 * N * 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = GPET_ERR_CUDA;
+    }
+    cudaFree(dA);
+    cudaFree(dB);
+    cudaFree(dD);
+    cudaFree(dErr);
+    return rc;
+}
+
+int gpet_surrogate_create(gpet_ctx* ctx, uint64_t seed, gpet_surrogate** out)
+{
+    if (!ctx || !out) return GPET_ERR_ARG;
+    *out = nullptr;
+    SurGeom g{};
+    int rc = ctx_geometry(ctx, &g);
+    if (rc) return rc;
+    if (g.moduleN != 1 || g.crystalN > sg::kCry || g.crystalN < 1 || g.rdepth > 2 || g.npanels < 1)
+        return GPET_ERR_ARG;   // more than one pulse per photon possible, or too many crystals
+    if (cudaSetDevice(g.device) != cudaSuccess) return GPET_ERR_NOGPU;
+    auto* s = new gpet_surrogate();
+    s->device = g.device;
+    s->geom = g;
+    s->panel_ok.assign(g.npanels, 1);
+    s->nparam = sg::kEmbOff + (int64_t)g.npanels * sg::kEmb;
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete s;
+        return GPET_ERR_CUDA;
+    }
+    // initial parameters: uniform(-1/sqrt(fan in), +) weights (head x 0.1),
+    // zero biases, embedding uniform(-0.1, 0.1)
+    std::vector<float> p((size_t)s->nparam, 0.0f);
+    uint64_t st = seed ^ 0x5851F42D4C957F2Dull;
+    auto uni = [&]() { return (float)((splitmix(st) >> 11) * (1.0 / 9007199254740992.0)) * 2.0f - 1.0f; };
+    for (int l = 0; l < sg::kLayers; ++l) {
+        const int K = sg::fan_in(l), N = sg::fan_out(l);
+        const float a = (l == sg::kLayers - 1 ? 0.1f : 1.0f) / std::sqrt((float)(l == 0 ? sg::kFeat : K));
+        for (int o = 0; o < N; ++o)
+            for (int k = 0; k < K; ++k) {
+                const bool pad = (l == 0 && k >= sg::kFeat) || (l == sg::kLayers - 1 && o >= sg::kOutUsed);
+                p[(size_t)(sg::w_off(l) + (int64_t)o * K + k)] = pad ? 0.0f : a * uni();
+            }
+    }
+    for (int64_t i = sg::kEmbOff; i < s->nparam; ++i) p[(size_t)i] = 0.1f * uni();
+    rc = GPET_OK;
+    if (s->params.ensure((size_t)s->nparam * 4) || s->grads.ensure((size_t)s->nparam * 4) ||
+        s->adam_m.ensure((size_t)s->nparam * 4) || s->adam_v.ensure((size_t)s->nparam * 4) ||
+        s->wrow.ensure((size_t)s->nparam * 2) || s->img.ensure(sg::kImgBytes) ||
+        s->panel_ok_d.ensure((size_t)g.npanels) || s->errflag.ensure(4) || s->loss.ensure(4))
+        rc = GPET_ERR_CUDA;
+    if (!rc) {
+        cudaMemcpy(s->params.p, p.data(), p.size() * 4, cudaMemcpyHostToDevice);
+        cudaMemset(s->adam_m.p, 0, (size_t)s->nparam * 4);
+        cudaMemset(s->adam_v.p, 0, (size_t)s->nparam * 4);
+        cudaMemset(s->errflag.p, 0, 4);
+        cudaMemcpy(s->panel_ok_d.p, s->panel_ok.data(), s->panel_ok.size(), cudaMemcpyHostToDevice);
+        rc = refresh_weights(s);
+        if (!rc && cudaStreamSynchronize(s->stream) != cudaSuccess) rc = GPET_ERR_CUDA;
+    }
+    if (rc) {
+        cudaStreamDestroy(s->stream);
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return GPET_OK;
+}
+
+void gpet_surrogate_destroy(gpet_surrogate* s)
+{
+    if (!s) return;
+    cudaSetDevice(s->device);
+    cudaStreamSynchronize(s->stream);
+    cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+const char* gpet_surrogate_last_error(gpet_surrogate* s) { return s ? s->err.c_str() : "null surrogate"; }
+
+int64_t gpet_surrogate_param_count(gpet_surrogate* s) { return s ? s->nparam : -1; }
+
+int gpet_surrogate_get_params(gpet_surrogate* s, float* out, int64_t n)
+{
+    if (!s || !out || n != s->nparam) return GPET_ERR_ARG;
+    SCK(cudaSetDevice(s->device));
+    SCK(cudaMemcpy(out, s->params.p, (size_t)n * 4, cudaMemcpyDeviceToHost));
+    return GPET_OK;
+}
+
+int gpet_surrogate_set_params(gpet_surrogate* s, const float* in, int64_t n)
+{
+    if (!s || !in || n != s->nparam) return GPET_ERR_ARG;
+    SCK(cudaSetDevice(s->device));
+    SCK(cudaMemcpy(s->params.p, in, (size_t)n * 4, cudaMemcpyHostToDevice));
+    int rc = refresh_weights(s);
+    if (rc) return rc;
+    SCK(cudaStreamSynchronize(s->stream));
+    return GPET_OK;
+}
+
+int gpet_surrogate_set_domain(gpet_surrogate* s, float e_lo, float e_hi, float margin, const uint8_t* panel_ok,
+                              int32_t npanels)
+{
+    if (!s || !(e_lo >= 0.0f) || !(e_hi >= e_lo) || !(margin >= 0.0f)) return GPET_ERR_ARG;
+    if (panel_ok && npanels != s->geom.npanels) return sfail(s, GPET_ERR_ARG, "one flag per panel");
+    SCK(cudaSetDevice(s->device));
+    s->e_lo = e_lo;
+    s->e_hi = e_hi;
+    s->margin = margin;
+    if (panel_ok) {
+        s->panel_ok.assign(panel_ok, panel_ok + npanels);
+        SCK(cudaMemcpy(s->panel_ok_d.p, s->panel_ok.data(), s->panel_ok.size(), cudaMemcpyHostToDevice));
+    }
+    return GPET_OK;
+}
+
+int gpet_surrogate_grad(gpet_surrogate* s, const gpet_entry* rec, int64_t n, float* loss, float* grad)
+{
+    if (!s || !rec || n < 1 || !loss) return GPET_ERR_ARG;
+    SCK(cudaSetDevice(s->device));
+    int rc = ensure_batch(s, n);
+    if (rc) return rc;
+    SCK(cudaMemcpyAsync(s->rec.p, rec, (size_t)n * sizeof(EntryRec), cudaMemcpyHostToDevice, s->stream));
+    rc = loss_and_grad(s, n, loss);
+    if (rc) return rc;
+    if (grad) SCK(cudaMemcpy(grad, s->grads.p, (size_t)s->nparam * 4, cudaMemcpyDeviceToHost));
+    return GPET_OK;
+}
+
+int gpet_surrogate_forward(gpet_surrogate* s, const gpet_entry* rec, int64_t n, float* out144)
+{
+    if (!s || !rec || n < 1 || !out144) return GPET_ERR_ARG;
+    SCK(cudaSetDevice(s->device));
+    float loss = 0.0f;
+    int rc = gpet_surrogate_grad(s, rec, n, &loss, nullptr);
+    if (rc) return rc;
+    SCK(cudaMemcpy(out144, s->out.p, (size_t)n * sg::kOut * 4, cudaMemcpyDeviceToHost));
+    return GPET_OK;
+}
+
+int gpet_surrogate_train(gpet_surrogate* s, const gpet_entry* rec, int64_t n, int32_t epochs, int32_t batch,
+                         float lr, uint64_t seed, float* epoch_loss)
+{
+    if (!s || !rec || n < 1 || epochs < 1 || batch < 128 || !(lr > 0.0f)) return GPET_ERR_ARG;
+    SCK(cudaSetDevice(s->device));
+    const int64_t B = std::min<int64_t>(batch, n);
+    int rc = ensure_batch(s, B);
+    if (rc) return rc;
+    // each epoch visits the records in a new shuffled order, in batches of B
+    std::vector<int64_t> order((size_t)n);
+    for (int64_t i = 0; i < n; ++i) order[(size_t)i] = i;
+    uint64_t st = seed;
+    std::vector<EntryRec> hb((size_t)B);
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    for (int ep = 0; ep < epochs; ++ep) {
+        for (int64_t i = n - 1; i > 0; --i) std::swap(order[(size_t)i], order[(size_t)(splitmix(st) % (uint64_t)(i + 1))]);
+        double lsum = 0.0;
+        int64_t nb = 0;
+        for (int64_t b0 = 0; b0 + B <= n; b0 += B) {
+            for (int64_t k = 0; k < B; ++k) hb[(size_t)k] = reinterpret_cast<const EntryRec*>(rec)[order[(size_t)(b0 + k)]];
+            SCK(cudaMemcpyAsync(s->rec.p, hb.data(), (size_t)B * sizeof(EntryRec), cudaMemcpyHostToDevice, s->stream));
+            float l = 0.0f;
+            rc = loss_and_grad(s, B, &l);
+            if (rc) return rc;
+            s->adam_t++;
+            const float c1 = 1.0f / (1.0f - std::pow(b1, (float)s->adam_t));
+            const float c2 = 1.0f / (1.0f - std::pow(b2, (float)s->adam_t));
+            k_adam<<<152 * 4, 256, 0, s->stream>>>(s->params.as<float>(), s->grads.as<float>(), s->adam_m.as<float>(),
+                                                   s->adam_v.as<float>(), s->nparam, lr, b1, b2, eps, c1, c2);
+            SCK(cudaGetLastError());
+            rc = refresh_weights(s);
+            if (rc) return rc;
+            lsum += l;
+            nb++;
+        }
+        if (epoch_loss) epoch_loss[ep] = nb ? (float)(lsum / nb) : 0.0f;
+    }
+    SCK(cudaStreamSynchronize(s->stream));
+    return GPET_OK;
+}
+
+}  // extern "C"

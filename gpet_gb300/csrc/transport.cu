@@ -464,7 +464,7 @@ __device__ __forceinline__ int readout(const SimDesc& S, PEvent* ev, int n)
 // kMulti as for k_source: the queue holds photons of several simulations
 template <bool kMulti>
 __global__ void __launch_bounds__(256) k_detector(const SimDesc* sims, QueueDev q, PulseDev P,
-                                                  HitDev H, int rec_hits, Counters* cnt)
+                                                  HitDev H, int rec_hits, Counters* cnt, EntryRec* entries)
 {
     __shared__ SimDesc sS;
     extern __shared__ float sP[];
@@ -505,6 +505,13 @@ __global__ void __launch_bounds__(256) k_detector(const SimDesc* sims, QueueDev 
             scat = q.i[3 * q.cap + j];
             const float* Pn = kMulti ? S.panels + L.panel * kPanelStride : sP + L.panel * kPanelStride;
             const int32_t pann = (int32_t)Pn[30];
+            EntryRec er;
+            if (entries) {
+                er.panel = L.panel;
+                er.y = L.x[1]; er.z = L.x[2];
+                er.ux = L.u[0]; er.uy = L.u[1]; er.uz = L.u[2];
+                er.E = L.E;
+            }
             Stream st;
             st_init(st, S.key0, S.key1, kTagDet + (parn & 1), (uint64_t)(uint32_t)eid);
             // photonde transport loop, gPET_kernals.cu:1013-1193
@@ -593,6 +600,12 @@ __global__ void __launch_bounds__(256) k_detector(const SimDesc* sims, QueueDev 
             }
             if (step == kMaxSteps) capped = 1;
             if (nev) nev = readout(S, ev, nev);
+            if (entries) {
+                er.crystal = nev ? ev[0].cryn : -1;
+                er.depth = nev ? ev[0].x * Pn[18] : 0.0f;
+                er.Edep = nev ? ev[0].E : 0.0f;
+                entries[j] = er;
+            }
             t_steps.add(cnt, CF(det_steps), sim, nsteps);
             t_cap.add(cnt, CF(stepcap), sim, capped);
             t_over.add(cnt, CF(overflow), sim, overflow ? 1u : 0u);
@@ -679,11 +692,11 @@ cudaError_t launch_phantom(bool multi, unsigned blocks, size_t smem, cudaStream_
 
 cudaError_t launch_detector(bool multi, unsigned blocks, unsigned threads, size_t smem, cudaStream_t s,
                             const SimDesc* sims, const QueueDev& q, const PulseDev& P, const HitDev& H, int rec_hits,
-                            Counters* cnt)
+                            Counters* cnt, EntryRec* entries)
 {
     if (!valid_threads(threads)) return cudaErrorInvalidValue;
-    if (multi) k_detector<true><<<blocks, threads, smem, s>>>(sims, q, P, H, rec_hits, cnt);
-    else k_detector<false><<<blocks, threads, smem, s>>>(sims, q, P, H, rec_hits, cnt);
+    if (multi) k_detector<true><<<blocks, threads, smem, s>>>(sims, q, P, H, rec_hits, cnt, entries);
+    else k_detector<false><<<blocks, threads, smem, s>>>(sims, q, P, H, rec_hits, cnt, entries);
     return cudaGetLastError();
 }
 
@@ -703,7 +716,7 @@ template __global__ void k_source<false>(const Wave*, int, PairBuf, Counters*);
 template __global__ void k_source<true>(const Wave*, int, PairBuf, Counters*);
 template __global__ void k_phantom<false>(const Wave*, int, PairBuf, QueueDev, Counters*, int);
 template __global__ void k_phantom<true>(const Wave*, int, PairBuf, QueueDev, Counters*, int);
-template __global__ void k_detector<false>(const SimDesc*, QueueDev, PulseDev, HitDev, int, Counters*);
-template __global__ void k_detector<true>(const SimDesc*, QueueDev, PulseDev, HitDev, int, Counters*);
+template __global__ void k_detector<false>(const SimDesc*, QueueDev, PulseDev, HitDev, int, Counters*, EntryRec*);
+template __global__ void k_detector<true>(const SimDesc*, QueueDev, PulseDev, HitDev, int, Counters*, EntryRec*);
 
 }  // namespace gpet

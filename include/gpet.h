@@ -66,6 +66,8 @@ typedef struct {
     int64_t detector_steps;      /* Woodcock steps in the panels */
     double ms_source;            /* source stage alone (part of ms_source_phantom) */
     double ms_phantom;           /* phantom stage alone (part of ms_source_phantom) */
+    int64_t n_surrogate;         /* photons whose detector response came from the surrogate */
+    double ms_surrogate;         /* surrogate stage (part of ms_detector) */
 } gpet_run_stats;
 
 /* ------------------------------------------------------------ lifetime */

@@ -1,0 +1,78 @@
+/* gpet_surrogate.h - learned detector response: C ABI.
+ *
+ * No counterpart in the reference, which always transports each photon
+ * through the panel crystals (photonde, gPET_kernals.cu:839-1233). An MLP
+ * (14 inputs -> 4 x 256 SiLU -> 140 outputs, BF16 weights, FP32
+ * accumulation on the tcgen05 tensor cores) maps a photon entering a panel to
+ * its detector response; photons outside the domain it was validated on are
+ * transported by the plain Monte Carlo. */
+#ifndef GPET_SURROGATE_H
+#define GPET_SURROGATE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gpet_ctx gpet_ctx;
+typedef struct gpet_surrogate gpet_surrogate;
+
+/* A photon entering a panel and its detector response after the adder and
+ * readout: the surrogate's training record (40 bytes). Option
+ * record_entries=1 on a context keeps one per photon that reaches a panel
+ * (photons the surrogate handled are not recorded). */
+typedef struct {
+    int32_t panel;        /* panel index */
+    float y, z;           /* entry point in the panel's local frame (cm) */
+    float ux, uy, uz;     /* direction in the panel's local frame */
+    float E;              /* energy at entry (eV) */
+    int32_t crystal;      /* crystal of the photon's first pulse, -1: no pulse */
+    float depth;          /* depth of that pulse below the entry face (cm) */
+    float Edep;           /* its energy (eV) */
+} gpet_entry;
+
+int gpet_get_entries(gpet_ctx* ctx, gpet_entry* buf, int64_t cap, int64_t* n);
+
+/* A surrogate for the detector of `ctx` (its panel geometry, materials and
+ * readout, which must give at most one pulse per photon: one module per
+ * panel, readout depth <= 2, at most 64 crystals), with seeded random
+ * initial weights, on ctx's device. */
+int gpet_surrogate_create(gpet_ctx* ctx, uint64_t seed, gpet_surrogate** out);
+void gpet_surrogate_destroy(gpet_surrogate* s);
+const char* gpet_surrogate_last_error(gpet_surrogate* s);
+/* Parameters, fp32, in this order: for each layer l = 0..4 its weights
+ * [out][in] then biases [out] (in: 16, 256, 256, 256, 256; out: 256, 256,
+ * 256, 256, 144; input columns 14-15 and output rows 140-143 are padding
+ * and stay zero), then the panel embedding [npanels][8]. */
+int64_t gpet_surrogate_param_count(gpet_surrogate* s);
+int gpet_surrogate_get_params(gpet_surrogate* s, float* out, int64_t n);
+int gpet_surrogate_set_params(gpet_surrogate* s, const float* in, int64_t n);
+/* Validated domain: photons entering with energy in [e_lo, e_hi] eV, at
+ * least `margin` cm inside the panel's y and z edges, on a panel flagged in
+ * panel_ok (NULL: all) take the surrogate; the others the Monte Carlo. */
+int gpet_surrogate_set_domain(gpet_surrogate* s, float e_lo, float e_hi, float margin, const uint8_t* panel_ok,
+                              int32_t npanels);
+/* Mean loss of n records and its gradient (param_count floats, NULL: none)
+ * at the current parameters; no update. */
+int gpet_surrogate_grad(gpet_surrogate* s, const gpet_entry* rec, int64_t n, float* loss, float* grad);
+/* Raw head outputs [n][144] of n records (for checks). */
+int gpet_surrogate_forward(gpet_surrogate* s, const gpet_entry* rec, int64_t n, float* out144);
+/* Adam (beta 0.9, 0.999) over `epochs` shuffled passes in batches of
+ * `batch`; epoch_loss[epochs] (may be NULL) receives each pass's mean loss. */
+int gpet_surrogate_train(gpet_surrogate* s, const gpet_entry* rec, int64_t n, int32_t epochs, int32_t batch,
+                         float lr, uint64_t seed, float* epoch_loss);
+/* Use (s) or stop using (NULL) the surrogate in this context's runs; s must
+ * outlive its use. Its photons produce pulses but no hits. */
+int gpet_set_surrogate(gpet_ctx* ctx, gpet_surrogate* s);
+
+/* Tensor-core self-test: D[128 x N] = A[128 x K] * B[N x K]^T with A, B
+ * row-major bf16 (raw 16-bit patterns) and D row-major f32, one tile on
+ * `device`. K, N multiples of 16 in [16, 256]. */
+int gpet_umma_selftest(int device, const uint16_t* a_bf16, const uint16_t* b_bf16, int32_t K, int32_t N,
+                       float* d_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -75,8 +75,12 @@ def test_psf_and_event_readers(tmp_path):
 
 
 def _declared_symbols():
-    txt = open(os.path.join(ROOT, "include", "gpet.h")).read()
-    return sorted(set(re.findall(r"\b(gpet_[a-z_]+)\s*\(", txt)))
+    syms = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", h)).read()
+            syms |= set(re.findall(r"\b(gpet_[a-z0-9_]+)\s*\(", txt))
+    return sorted(syms)
 
 
 def test_library_exports_every_declared_symbol(gpet_lib):
