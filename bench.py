@@ -415,6 +415,110 @@ def run_batched_workload(args):
     print(json.dumps(line), flush=True)
 
 
+def _chi2(a, b):
+    """Two-sample chi-square of histograms with counts a and b (same bins)."""
+    import numpy as np
+    from scipy import stats
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    keep = (a + b) > 0
+    a, b = a[keep], b[keep]
+    ka = np.sqrt(b.sum() / a.sum())
+    kb = 1.0 / ka
+    chi2 = float((((ka * a - kb * b) ** 2) / (a + b)).sum())
+    ndf = int(keep.sum()) - 1
+    rel = np.abs(b / b.sum() - a / a.sum()) / np.maximum(a / a.sum(), 1e-12)
+    return {"chi2": chi2, "ndf": ndf, "p": float(stats.chi2.sf(chi2, ndf)), "max_rel_dev": float(rel.max()),
+            "mean_rel_dev": float(rel.mean())}
+
+
+def run_surrogate_workload(args):
+    """The headline workload with the learned detector response: training on
+    entry records of independent Monte Carlo runs (untimed), then the same
+    acquisitions with and without the surrogate, timed like the headline,
+    and the two-sample chi-square of their singles spectra and crystal maps."""
+    import numpy as np
+    import torch
+    from gpet_gb300 import api
+    torch.cuda.set_device(0)
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda:0")
+    peak_t = 1917.6
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak_t = float(json.load(f)["bf16_tflops"])
+    except Exception:
+        pass
+    with tempfile.TemporaryDirectory() as d:
+        sc = make_scene(d, args.decays)
+        data = os.path.join(ROOT, "data")
+
+        def ctx_for(**extra):
+            c = api.Context(0)
+            c.set_options(dict(sc.options, data_dir=data, base_dir=d, **extra))
+            c.load_config(sc.config_path)
+            return c
+
+        t0 = time.perf_counter()
+        gen = ctx_for(record_entries=1, n_decays=args.train_decays, seed=555)
+        gen.run()
+        rec = gen.entries()
+        sur = api.Surrogate(gen, seed=9)
+        losses = sur.train(rec, epochs=args.train_epochs, batch=8192, lr=2e-3)
+        sur.set_domain(1.0e5, 5.2e5, 0.3)
+        train_s = time.perf_counter() - t0
+        gen.close()
+        res = {}
+        for mode in ("mc", "surrogate"):
+            ctx = ctx_for()
+            ctx.autotune(1 << 23)
+            if mode == "surrogate":
+                ctx.set_surrogate(sur)
+            for w in range(args.warmup):
+                ctx.set_option("seed", 1000 + w)
+                ctx.run()
+            tot = {"ms": 0.0, "det": 0.0, "sur": 0.0, "coinc": 0, "nsur": 0, "entered": 0}
+            hist_e = np.zeros(60)
+            hist_c = np.zeros(64)
+            for k in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                ctx.set_option("seed", 20261203 + k)
+                st = ctx.run()
+                tot["ms"] += st["ms_total"]; tot["det"] += st["ms_detector"]; tot["sur"] += st["ms_surrogate"]
+                tot["coinc"] += st["n_coinc"]; tot["nsur"] += st["n_surrogate"]; tot["entered"] += st["n_entered"]
+                s_ev, _ = ctx.singles()
+                hist_e += np.histogram(s_ev["E"], bins=60, range=(3.5e5, 6.5e5))[0]
+                hist_c += np.bincount(s_ev["cryn"], minlength=64)[:64]
+            res[mode] = (tot, hist_e, hist_c)
+            ctx.close()
+    mc, su = res["mc"][0], res["surrogate"][0]
+    flops = 2 * 236032 * su["nsur"]
+    ach = flops / max(su["sur"] * 1e-3, 1e-12) / 1e12
+    line = {"metric": METRIC.replace("(plain MC)", "(surrogate detector response)"),
+            "value": su["coinc"] / (su["ms"] * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": su["ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (MLP), f32 (transport)", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "decays_per_step": args.decays,
+                       "training": {"decays": args.train_decays, "records": int(len(rec)),
+                                    "epochs": args.train_epochs, "loss_per_epoch": [float(x) for x in losses],
+                                    "seconds": train_s},
+                       "domain": "entry energy 100-520 keV, >= 3 mm inside the panel edges, all panels"},
+            "plain_mc": {"value": mc["coinc"] / (mc["ms"] * 1e-3), "ms_per_step": mc["ms"] / args.steps,
+                         "detector_ms_per_step": mc["det"] / args.steps},
+            "surrogate": {"detector_ms_per_step": su["det"] / args.steps,
+                          "mlp_ms_per_step": su["sur"] / args.steps,
+                          "photons_per_step": su["nsur"] / args.steps,
+                          "fraction_of_entered": su["nsur"] / max(1, su["entered"])},
+            "roofline_mlp": {"kernel": "k_mlp_fwd<false>", "bound": "tensor", "achieved": ach, "peak": peak_t,
+                             "unit": "TFLOP/s", "frac": ach / peak_t,
+                             "flops_per_photon": 2 * 236032},
+            "parity": {"singles_energy_350_650keV": _chi2(res["mc"][1], res["surrogate"][1]),
+                       "singles_per_crystal": _chi2(res["mc"][2], res["surrogate"][2]),
+                       "singles_mc": float(res["mc"][1].sum()), "singles_surrogate": float(res["surrogate"][1].sum()),
+                       "coincidences_mc": mc["coinc"], "coincidences_surrogate": su["coinc"]}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -429,8 +533,11 @@ def main():
                     help="time launch shapes on a sample before the warm-up (results do not depend on the shape)")
     ap.add_argument("--tune-decays", type=int, default=1 << 23)
     ap.add_argument("--gloo", action="store_true", help=argparse.SUPPRESS)
-    ap.add_argument("--workload", choices=["positron", "batched64"], default="positron",
-                    help="positron: the headline workload; batched64: 64 uneven simulations in one job")
+    ap.add_argument("--workload", choices=["positron", "batched64", "surrogate"], default="positron",
+                    help="positron: the headline workload; batched64: 64 uneven simulations in one job; "
+                         "surrogate: the headline workload with the learned detector response")
+    ap.add_argument("--train-decays", type=int, default=20_000_000, help=argparse.SUPPRESS)
+    ap.add_argument("--train-epochs", type=int, default=3, help=argparse.SUPPRESS)
     ap.add_argument("--batch-sims", type=int, default=64, help=argparse.SUPPRESS)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
@@ -439,6 +546,8 @@ def main():
         run_reference(args)
     elif args.workload == "batched64":
         run_batched_workload(args)
+    elif args.workload == "surrogate":
+        run_surrogate_workload(args)
     else:
         run_ours(args)
 

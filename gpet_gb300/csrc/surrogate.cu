@@ -7,7 +7,8 @@
 // the pulse, 64 logits of the deposited-energy fraction; padded to 144).
 // BF16 weights and activations, FP32 accumulation in tensor memory.
 //
-//   k_mlp_fwd<train>  fused forward: one CTA of 128 threads per 128 samples;
+//   k_mlp_fwd<train>  fused forward: one CTA of 512 threads per 128 samples
+//                     (a tile; CTAs are persistent over tiles);
 //                     activations stay in shared memory, each layer's weight
 //                     image arrives by bulk copy (the next one while the
 //                     current layer's epilogue runs), tcgen05.mma into TMEM,
@@ -65,7 +66,9 @@ constexpr uint32_t kSmemB = kHid * kHid * 2;  // one weight image
 static_assert(kSmemB >= (uint32_t)kOut * kHid * 2, "head image fits");
 }  // namespace sg
 
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + expf(-z)); }
+// forward SiLU with the fast exponential and reciprocal: its result is
+// rounded to bf16 next
+__device__ __forceinline__ float silu(float z) { return z * __frcp_rn(1.0f + __expf(-z)); }
 __device__ __forceinline__ float silu_grad(float z)
 {
     const float s = 1.0f / (1.0f + expf(-z));
@@ -201,7 +204,7 @@ __device__ __noinline__ void sample_and_append(const SurrogateDev& sd, const Fwd
         ld_cols(taddr, c, v);
         for (int j = 0; j < 32; ++j) {
             const int col = c + j;
-            if (col >= kColE && col < kColE + kBins) sum += expf(v[j] + bias[col] - mx);
+            if (col >= kColE && col < kColE + kBins) sum += __expf(v[j] + bias[col] - mx);
         }
     }
     int bin = kBins - 1;
@@ -215,7 +218,7 @@ __device__ __noinline__ void sample_and_append(const SurrogateDev& sd, const Fwd
             for (int j = 0; j < 32; ++j) {
                 const int col = c + j;
                 if (col >= kColE && col < kColE + kBins && !found) {
-                    acc += expf(v[j] + bias[col] - mx);
+                    acc += __expf(v[j] + bias[col] - mx);
                     if (acc >= target) { bin = col - kColE; found = true; }
                 }
             }
@@ -234,7 +237,7 @@ __device__ __noinline__ void sample_and_append(const SurrogateDev& sd, const Fwd
         float v[32];
         ld_cols(taddr, c, v);
         for (int j = 0; j < 32; ++j)
-            if (c + j < sd.crystalN) cs += expf(v[j] + bias[c + j] - cm);
+            if (c + j < sd.crystalN) cs += __expf(v[j] + bias[c + j] - cm);
     }
     int cry = sd.crystalN - 1;
     {
@@ -246,7 +249,7 @@ __device__ __noinline__ void sample_and_append(const SurrogateDev& sd, const Fwd
             ld_cols(taddr, c, v);
             for (int j = 0; j < 32; ++j)
                 if (c + j < sd.crystalN && !found) {
-                    acc += expf(v[j] + bias[c + j] - cm);
+                    acc += __expf(v[j] + bias[c + j] - cm);
                     if (acc >= target) { cry = c + j; found = true; }
                 }
         }
@@ -259,16 +262,16 @@ __device__ __noinline__ void sample_and_append(const SurrogateDev& sd, const Fwd
         float wm = -1e30f;
         for (int k = 0; k < kMix; ++k) wm = fmaxf(wm, v[k] + bias[kColW + k]);
         float ws = 0.0f;
-        for (int k = 0; k < kMix; ++k) ws += expf(v[k] + bias[kColW + k] - wm);
+        for (int k = 0; k < kMix; ++k) ws += __expf(v[k] + bias[kColW + k] - wm);
         int comp = kMix - 1;
         float acc = 0.0f;
         for (int k = 0; k < kMix; ++k) {
-            acc += expf(v[k] + bias[kColW + k] - wm);
+            acc += __expf(v[k] + bias[kColW + k] - wm);
             if (acc >= um * ws) { comp = k; break; }
         }
         const float mu = v[kColMu - 64 + comp] + bias[kColMu + comp];
         const float ls = fminf(fmaxf(v[kColLs - 64 + comp] + bias[kColLs + comp], kLsMin), kLsMax);
-        depth_n = fminf(fmaxf(mu + expf(ls) * zn, 0.0f), 1.0f);
+        depth_n = fminf(fmaxf(mu + __expf(ls) * zn, 0.0f), 1.0f);
     }
     const bool pulse = valid && bin > 0;
     const float Edep = bin == kBins - 1 ? E : ((float)bin + uw) * (1.0f / kBins) * E;
@@ -311,8 +314,13 @@ __device__ __noinline__ void sample_and_append(const SurrogateDev& sd, const Fwd
     add_by_sim(in.cnt, valid ? sim : 0, CF(n_surrogate), valid ? 1u : 0u);
 }
 
+// threads: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows of the tile)
+// and handles column quarter w / 4 of each layer's epilogue; warps 0-3 (one
+// thread per row) build the inputs and sample the outputs
+constexpr int kFwdThreads = 512;
+
 template <bool kTrain>
-__global__ void __launch_bounds__(128, 1) k_mlp_fwd(SurrogateDev sd, FwdTrain tr, FwdInfer in, int* err)
+__global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd(SurrogateDev sd, FwdTrain tr, FwdInfer in, int* err)
 {
     using namespace sg;
     extern __shared__ __align__(128) unsigned char sm[];
@@ -342,12 +350,14 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fwd(SurrogateDev sd, FwdTrain tr
     __syncthreads();
     umma::fence_after_sync();
     const uint32_t tmem = tbase;
-    const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
+    const int quarter = warp & 3, cq = warp >> 2;
+    const int rloc = 32 * quarter + lane;          // row of the tile this thread reads from TMEM
+    const uint32_t taddr = tmem + ((uint32_t)(32 * quarter) << 16);
     uint32_t n_ld = 0, n_mma = 0;   // completed phases of the two barriers
     bool ok = true;
     // persistent over tiles of 128 samples
     for (int64_t row0 = (int64_t)blockIdx.x * 128; row0 < n && ok; row0 += (int64_t)gridDim.x * 128) {
-        const int64_t row = row0 + threadIdx.x;
+        const int64_t row = row0 + rloc;
         const bool valid = row < n;
         if (threadIdx.x == 0) {
             umma::mbar_expect_tx(&bar_ld, (uint32_t)(fan_out(0) * fan_in(0) * 2));
@@ -359,7 +369,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fwd(SurrogateDev sd, FwdTrain tr
         float E = 0.0f, ux = 0.0f;
         double t0 = 0.0;
         for (int k = 0; k < 16; ++k) f[k] = 0.0f;
-        if (kTrain) {
+        if (cq != 0) {
+            // warps 4-15 only run the epilogues
+        } else if (kTrain) {
             if (valid) {
                 const uint4* x = reinterpret_cast<const uint4*>(tr.X + row * kIn);
                 const uint4 a = x[0], b = x[1];
@@ -384,14 +396,14 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fwd(SurrogateDev sd, FwdTrain tr
             sim = in.q.i[4 * cap + j];
             features(sd, sd.params + kEmbOff, panel, y, z, ux, uy, uz, E, f);
         }
-        {
+        if (cq == 0) {
             uint4 a, b;
             a.x = pack_bf16(f[0], f[1]); a.y = pack_bf16(f[2], f[3]); a.z = pack_bf16(f[4], f[5]);
             a.w = pack_bf16(f[6], f[7]);
             b.x = pack_bf16(f[8], f[9]); b.y = pack_bf16(f[10], f[11]); b.z = pack_bf16(f[12], f[13]);
             b.w = pack_bf16(f[14], f[15]);
-            *reinterpret_cast<uint4*>(sA + umma::img_offset(threadIdx.x, 0, 128)) = a;
-            *reinterpret_cast<uint4*>(sA + umma::img_offset(threadIdx.x, 8, 128)) = b;
+            *reinterpret_cast<uint4*>(sA + umma::img_offset(rloc, 0, 128)) = a;
+            *reinterpret_cast<uint4*>(sA + umma::img_offset(rloc, 8, 128)) = b;
         }
         umma::fence_proxy_async();
         umma::fence_before_sync();
@@ -427,7 +439,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fwd(SurrogateDev sd, FwdTrain tr
             }
             const float* bias = sd.params + b_off(l);
             if (l + 1 < kLayers) {
-                for (int c = 0; c < kHid; c += 32) {
+                for (int c = 64 * cq; c < 64 * cq + 64; c += 32) {
                     float v[32];
                     ld_cols(taddr, c, v);
                     uint32_t hp[16];
@@ -447,11 +459,12 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fwd(SurrogateDev sd, FwdTrain tr
                             dst[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
                     }
                     for (int q = 0; q < 4; ++q)
-                        *reinterpret_cast<uint4*>(sA + umma::img_offset(threadIdx.x, c + 8 * q, 128)) =
+                        *reinterpret_cast<uint4*>(sA + umma::img_offset(rloc, c + 8 * q, 128)) =
                             make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
                 }
             } else if (kTrain) {
-                for (int c = 0; c < kOut; c += 32) {
+                // chunks of 32 columns: quarter cq takes chunk cq, quarter 0 also chunk 4
+                for (int c = 32 * cq; c < kOut; c += 128) {
                     float v[32];
                     ld_cols(taddr, c, v);
                     if (valid)
@@ -463,7 +476,8 @@ __global__ void __launch_bounds__(128, 1) k_mlp_fwd(SurrogateDev sd, FwdTrain tr
             __syncthreads();
             umma::fence_after_sync();
         }
-        if (!kTrain && ok) sample_and_append(sd, in, taddr, valid, sim, panel, parn, eid, scat, E, ux, t0, lane);
+        if (!kTrain && ok && cq == 0)
+            sample_and_append(sd, in, taddr, valid, sim, panel, parn, eid, scat, E, ux, t0, lane);
         umma::fence_before_sync();
         __syncthreads();
         umma::fence_after_sync();
@@ -832,7 +846,7 @@ cudaError_t launch_surrogate(const SurrogateDev& sd, const SimDesc* sims, const 
     if (e != cudaSuccess) return e;
     FwdInfer in{q, sidx, scount, sims, P, cnt};
     FwdTrain tr{};
-    k_mlp_fwd<false><<<grid_cap(max_n, 128, sm_count()), 128, smem, s>>>(sd, tr, in, err);
+    k_mlp_fwd<false><<<grid_cap(max_n, 128, sm_count()), kFwdThreads, smem, s>>>(sd, tr, in, err);
     return cudaGetLastError();
 }
 
@@ -998,7 +1012,7 @@ int loss_and_grad(gpet_surrogate* s, int64_t n, float* loss)
     const int smem = (int)(kSmemA + kSmemB);
     SCK(cudaFuncSetAttribute(k_mlp_fwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     SCK(cudaFuncSetAttribute(k_umma_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem));
-    k_mlp_fwd<true><<<grid_cap(n, 128, 152), 128, smem, st>>>(sd, tr, in, s->errflag.as<int>());
+    k_mlp_fwd<true><<<grid_cap(n, 128, 152), kFwdThreads, smem, st>>>(sd, tr, in, s->errflag.as<int>());
     SCK(cudaGetLastError());
     SCK(cudaMemsetAsync(s->loss.p, 0, 4, st));
     SCK(cudaMemsetAsync(s->grads.p, 0, (size_t)s->nparam * 4, st));
