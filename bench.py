@@ -45,10 +45,10 @@ def algorithmic_bytes_phantom(n_photons, ph_steps, entered):
     return 88 * n_photons + 5 * ph_steps + 44 * entered
 
 
-# DRAM bytes per photon of k_phantom measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum of one 2^20-decay launch of this workload, 2,097,152
-# photons: 74.8 MB + 4.7 MB).
-MEASURED_DRAM_BYTES_PER_PHOTON = (74.765824e6 + 4.671744e6) / 2097152
+# DRAM bytes per photon slot of k_phantom measured by ncu (dram__bytes_read.sum
+# + dram__bytes_write.sum of one 2^21-decay launch of this workload, 4,194,304
+# photon slots: 146.4 MB + 14.8 MB; the tuned launch shape of the headline run)
+MEASURED_DRAM_BYTES_PER_PHOTON = (146.420224e6 + 14.797312e6) / 4194304
 
 
 def _peaks():
@@ -216,6 +216,7 @@ def run_ours(args):
         data = os.path.join(ROOT, "data")
         ctx = api.Context(local)
         opts = dict(sc.options, data_dir=data, base_dir=d, sim_id=rank)
+        opts.update(args.set)
         ctx.set_options(opts)
         ctx.load_config(sc.config_path)
         tuning = ctx.autotune(args.tune_decays) if args.autotune else None
@@ -267,7 +268,7 @@ def run_ours(args):
         cap_c = int(2 * tot["coinc"] / max(1, args.steps)) + 1024
         out_s = (pinned((cap_s,), F.EVENT_DTYPE), pinned((cap_s,), np.uint8))
         out_c = (pinned((cap_c, 2), np.int64), pinned((cap_c,), np.uint8))
-        e2e_steps = max(2, args.steps // 2)
+        e2e_steps = max(2, args.steps // 2) if args.e2e_steps < 0 else args.e2e_steps
         barrier()
         t0 = time.perf_counter()
         e_coinc, h2d, d2h = 0, 0, 0
@@ -315,7 +316,7 @@ def run_ours(args):
                      "note": "issue/latency-bound (RNG, transcendental math, dependent L2 gathers); "
                              "HBM per the path's byte model"},
         "e2e": {"value": e_coinc / e_wall, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
-                "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps},
+                "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps} if e2e_steps > 0 else None,
         "clocks": clocks,
         "wall_s_timed_region": wall,
         "launch_shape": tuning if tuning else "library defaults",
@@ -532,6 +533,10 @@ def main():
     ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
                     help="time launch shapes on a sample before the warm-up (results do not depend on the shape)")
     ap.add_argument("--tune-decays", type=int, default=1 << 23)
+    ap.add_argument("--set", action="append", default=[], metavar="KEY=VALUE",
+                    help="context option for the headline workload (e.g. a fixed launch shape for profiling)")
+    ap.add_argument("--e2e-steps", type=int, default=-1,
+                    help="steps of the end-to-end leg (default max(2, steps/2); 0 skips it: profiling only)")
     ap.add_argument("--gloo", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--workload", choices=["positron", "batched64", "surrogate"], default="positron",
                     help="positron: the headline workload; batched64: 64 uneven simulations in one job; "
@@ -540,6 +545,7 @@ def main():
     ap.add_argument("--train-epochs", type=int, default=3, help=argparse.SUPPRESS)
     ap.add_argument("--batch-sims", type=int, default=64, help=argparse.SUPPRESS)
     args = ap.parse_args()
+    args.set = dict(kv.split("=", 1) for kv in args.set)
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
