@@ -220,6 +220,8 @@ def run_ours(args):
         ctx.set_options(opts)
         ctx.load_config(sc.config_path)
         tuning = ctx.autotune(args.tune_decays) if args.autotune else None
+        # decays per k_source / k_phantom launch of this run
+        sub_decays = int(tuning["sub_decays"]) if tuning else int(args.set.get("sub_decays", SUB_DECAYS))
         for w in range(args.warmup):
             ctx.set_option("seed", 1000 + w)
             ctx.run()
@@ -241,7 +243,7 @@ def run_ours(args):
             tot["launches"] += st["kernel_launches"]; tot["ph_steps"] += st["phantom_steps"]
             tot["entered"] += st["n_entered"]; tot["decays"] += st["n_decays"]; tot["singles"] += st["n_singles"]
             tot["true"] += st["n_true"]; tot["scatter"] += st["n_scatter"]; tot["random"] += st["n_random"]
-            tot["chunks"] += -(-st["n_decays"] // SUB_DECAYS)
+            tot["chunks"] += -(-st["n_decays"] // sub_decays)
             tot["pairs"] += st["n_pairs"]
         barrier()
         wall = time.perf_counter() - t_wall0
