@@ -21,6 +21,9 @@ ERRORS = {-1: "bad argument or state", -2: "missing or malformed input file", -3
 ENTRY_DTYPE = np.dtype([("panel", "<i4"), ("y", "<f4"), ("z", "<f4"), ("ux", "<f4"), ("uy", "<f4"), ("uz", "<f4"),
                         ("E", "<f4"), ("crystal", "<i4"), ("depth", "<f4"), ("Edep", "<f4")])
 
+PSF_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("ux", "<f4"), ("uy", "<f4"), ("uz", "<f4"),
+                      ("E", "<f4"), ("eventid", "<i4"), ("t", "<f8")])
+
 EXIT_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("ux", "<f4"), ("uy", "<f4"), ("uz", "<f4"),
                        ("E", "<f4"), ("nscat", "<i4"), ("t", "<f8"), ("status", "<i4"), ("panel", "<i4")])
 
@@ -85,6 +88,8 @@ def load_library(path=None):
     L.gpet_autotune.argtypes = [vp, i64, C.POINTER(Tuning)]
     f32p = C.POINTER(C.c_float)
     L.gpet_get_entries.argtypes = [vp, vp, i64, C.POINTER(i64)]
+    L.gpet_get_source_records.argtypes = [vp, vp, i64, C.POINTER(i64)]
+    L.gpet_get_phantom_records.argtypes = [vp, vp, i64, C.POINTER(i64)]
     L.gpet_surrogate_create.argtypes = [vp, C.c_uint64, C.POINTER(vp)]
     L.gpet_surrogate_destroy.argtypes = [vp]
     L.gpet_surrogate_destroy.restype = None
@@ -274,6 +279,24 @@ class Context:
         m = C.c_int64()
         if n:
             self._ck(self.L.gpet_get_entries(self.h, _ptr(out), n, C.byref(m)))
+        return out
+
+    def source_records(self):
+        """Emitted photons of the last run (option record_source=1)."""
+        n = self._count(self.L.gpet_get_source_records, None)
+        out = np.zeros(n, PSF_DTYPE)
+        m = C.c_int64()
+        if n:
+            self._ck(self.L.gpet_get_source_records(self.h, _ptr(out), n, C.byref(m)))
+        return out
+
+    def phantom_records(self):
+        """Photons leaving the phantom in the last run (option record_exits=1)."""
+        n = self._count(self.L.gpet_get_phantom_records, None)
+        out = np.zeros(n, PSF_DTYPE)
+        m = C.c_int64()
+        if n:
+            self._ck(self.L.gpet_get_phantom_records(self.h, _ptr(out), n, C.byref(m)))
         return out
 
     def set_surrogate(self, sur):

@@ -55,7 +55,7 @@ struct Work {
     int64_t p_cap = 0;
     DevBuf h_id, h_f, h_sim;
     int64_t h_cap = 0;
-    DevBuf exits;
+    DevBuf exits, source;                 // per photon slot of a chunk
     DevBuf g_ev, g_meta;                  // gathered Event records for copy-out
     DigiScratch dg{};
     DevBuf dg_idx_a, dg_idx_b, dg_key_a, dg_key_b, dg_torder, dg_flags, dg_site, dg_hist, dg_aux, dg_sel, dg_blur,
@@ -103,6 +103,8 @@ struct gpet_ctx {
     int autotune = 0;                     // tune the launch shape on the first run
     bool tuned = false;
     int record_entries = 0;               // keep the entry records of the detector stage
+    int record_source = 0;                // keep the emitted photons (source phase space)
+    int psf_sphere = 0;                   // phantom phase space projected onto the record sphere
     gpet_surrogate* sur = nullptr;        // learned detector response (not owned)
     std::string base_dir = ".";
     std::string data_dir;
@@ -131,6 +133,7 @@ struct gpet_ctx {
     int res_sim = 0;
     std::vector<ExitRec> host_exits;
     std::vector<EntryRec> host_entries;
+    std::vector<SrcRec> host_source;
     gpet_run_stats last{};
     bool have_results = false;
     cudaEvent_t ev[8] = {};
@@ -251,6 +254,8 @@ int gpet_set_option(gpet_ctx* c, const char* key, const char* value)
     else if (k == "use_graphs") c->use_graphs = (int)std::strtol(value, &end, 10);
     else if (k == "autotune") c->autotune = (int)std::strtol(value, &end, 10);
     else if (k == "record_entries") c->record_entries = (int)std::strtol(value, &end, 10);
+    else if (k == "record_source") c->record_source = (int)std::strtol(value, &end, 10);
+    else if (k == "psf_sphere") c->psf_sphere = (int)std::strtol(value, &end, 10);
     else if (k == "base_dir") { c->base_dir = v; return GPET_OK; }
     else if (k == "data_dir") { c->data_dir = v; return GPET_OK; }
     else return fail(c, GPET_ERR_ARG, "unknown option " + k);
@@ -845,6 +850,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         for (int s = 0; s < nsim; ++s) {
             if (cs[s]->record_exits) return fail(c, GPET_ERR_ARG, "record_exits is for single runs");
             if (cs[s]->record_entries) return fail(c, GPET_ERR_ARG, "record_entries is for single runs");
+            if (cs[s]->record_source) return fail(c, GPET_ERR_ARG, "record_source is for single runs");
             if (cs[s]->sur != c->sur) return fail(c, GPET_ERR_ARG, "the simulations of a batch share one surrogate or none");
         }
     CK(cudaSetDevice(c->device));
@@ -952,6 +958,13 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     const bool rec_exits = c->record_exits && !transport_only;
     const bool rec_entries = c->record_entries && !transport_only;
     c->host_entries.clear();
+    const bool rec_source = c->record_source && !transport_only;
+    if (rec_source) {
+        CK(W.source.ensure((size_t)2 * chunk * sizeof(SrcRec)));
+        c->host_source.assign((size_t)2 * ND, SrcRec{});
+    } else {
+        c->host_source.clear();
+    }
     // the learned detector response, checked against every simulation's detector
     SurrogateDev sdev{};
     const bool use_sur = c->sur != nullptr;
@@ -1034,6 +1047,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
             wave.n = waves[w].n;
             wave.work = W.d_work.as<unsigned long long>() + k;
             wave.exits = rec_exits ? W.exits.as<ExitRec>() + 2 * (waves[w].g - cg0) : nullptr;
+            wave.source = rec_source ? W.source.as<SrcRec>() + 2 * (waves[w].g - cg0) : nullptr;
         }
         CK(cudaMemcpyAsync(W.d_waves.p, W.h_waves, K * sizeof(Wave), cudaMemcpyHostToDevice, c->stream));
         QueueDev q;
@@ -1074,6 +1088,9 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         const int64_t cn = waves[we - 1].g + waves[we - 1].n - cg0;
         if (rec_exits)
             CK(cudaMemcpy(c->host_exits.data() + 2 * cg0, W.exits.p, (size_t)2 * cn * sizeof(ExitRec),
+                          cudaMemcpyDeviceToHost));
+        if (rec_source)
+            CK(cudaMemcpy(c->host_source.data() + 2 * cg0, W.source.p, (size_t)2 * cn * sizeof(SrcRec),
                           cudaMemcpyDeviceToHost));
         // room for the worst case of this chunk's queue
         rc = grow_pulses(c, W, pulses_used + (int64_t)hq * kMaxPulse, pulses_used);
@@ -1542,6 +1559,53 @@ int gpet_get_exits(gpet_ctx* c, void* buf, int64_t cap, int64_t* n)
     return GPET_OK;
 }
 
+static_assert(sizeof(gpet_psf_record) == sizeof(SrcRec), "phase-space record layouts agree");
+
+// getDistance, gPET_kernals.cu:148-171: distance along u from x to the
+// record sphere (centre c, radius r); the root choice is the reference's
+static float sphere_distance(const float x[3], const float u[3], const float sph[4])
+{
+    const float cx = x[0] - sph[0], cy = x[1] - sph[1], cz = x[2] - sph[2];
+    const float a = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    const float b = 2.0f * (u[0] * cx + u[1] * cy + u[2] * cz);
+    const float cc = (cx * cx + cy * cy + cz * cz) - sph[3] * sph[3];
+    const float disc = b * b - 4.0f * a * cc;
+    if (disc < 0.0f) return 0.0f;
+    if (cc < 0.0f) return (-b + std::sqrt(disc)) / (2.0f * a);
+    if (b < 0.0f) return (-b - std::sqrt(disc)) / (2.0f * a);
+    return (-b + std::sqrt(disc)) / (2.0f * a);
+}
+
+// phantom phase space (gPET.cu:91-114, 328-352): photons that left the
+// phantom (time > 0), optionally moved onto the record sphere
+static void phantom_records(const gpet_ctx* c, std::vector<SrcRec>& out)
+{
+    out.clear();
+    const float* sph = c->cfg.recordsphere;
+    for (size_t i = 0; i < c->host_exits.size(); ++i) {
+        const ExitRec& e = c->host_exits[i];
+        if (e.status != 1 || !(e.t > 0.0)) continue;
+        SrcRec r;
+        r.x = e.x; r.y = e.y; r.z = e.z; r.ux = e.ux; r.uy = e.uy; r.uz = e.uz; r.E = e.E;
+        r.eventid = (int32_t)(i / 2);
+        r.t = e.t;
+        if (c->psf_sphere) {
+            const float x[3] = {e.x, e.y, e.z}, u[3] = {e.ux, e.uy, e.uz};
+            const float d = sphere_distance(x, u, sph);
+            r.x = e.x + d * e.ux; r.y = e.y + d * e.uy; r.z = e.z + d * e.uz;
+            r.t = e.t + (double)d / kSpe;
+        }
+        out.push_back(r);
+    }
+}
+
+static void source_records(const gpet_ctx* c, std::vector<SrcRec>& out)
+{
+    out.clear();
+    for (const SrcRec& r : c->host_source)
+        if (r.t > 0.0) out.push_back(r);
+}
+
 static int append_file(gpet_ctx* c, const std::string& path, const void* p, size_t bytes)
 {
     FILE* f = std::fopen(path.c_str(), "ab");
@@ -1585,6 +1649,57 @@ int gpet_write_outputs(gpet_ctx* c, const char* dir)
     for (int64_t i = 0; i < nc; ++i) { ce[2 * i] = sg[pr[2 * i]]; ce[2 * i + 1] = sg[pr[2 * i + 1]]; }
     if ((rc = append_file(c, d + "/coincidences.dat", ce.data(), sizeof(gpet_event) * ce.size()))) return rc;
     if ((rc = append_file(c, d + "/coincidences_class.dat", cl.data(), cl.size()))) return rc;
+    // phase-space records: 28-byte state (float3 position, float4 direction +
+    // energy), int32 event id, double time in three files each
+    auto write_psf = [&](const std::vector<SrcRec>& v, const std::string& stem) -> int {
+        std::vector<float> st(v.size() * 7);
+        std::vector<int32_t> id(v.size());
+        std::vector<double> tt(v.size());
+        for (size_t i = 0; i < v.size(); ++i) {
+            const SrcRec& r = v[i];
+            const float f[7] = {r.x, r.y, r.z, r.ux, r.uy, r.uz, r.E};
+            std::memcpy(&st[7 * i], f, sizeof(f));
+            id[i] = r.eventid;
+            tt[i] = r.t;
+        }
+        int r2;
+        if ((r2 = append_file(c, d + "/out" + stem + ".dat", st.data(), st.size() * 4))) return r2;
+        if ((r2 = append_file(c, d + "/id" + stem + ".dat", id.data(), id.size() * 4))) return r2;
+        return append_file(c, d + "/time" + stem + ".dat", tt.data(), tt.size() * 8);
+    };
+    std::vector<SrcRec> v;
+    if (!c->host_source.empty()) {
+        source_records(c, v);
+        if ((rc = write_psf(v, "source"))) return rc;
+    }
+    if (!c->host_exits.empty()) {
+        phantom_records(c, v);
+        if ((rc = write_psf(v, "phantom"))) return rc;
+    }
+    return GPET_OK;
+}
+
+int gpet_get_source_records(gpet_ctx* c, gpet_psf_record* buf, int64_t cap, int64_t* n)
+{
+    if (!c || !n) return GPET_ERR_ARG;
+    std::vector<SrcRec> v;
+    source_records(c, v);
+    *n = (int64_t)v.size();
+    if (!buf || *n == 0) return GPET_OK;
+    if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the source records");
+    std::memcpy(buf, v.data(), sizeof(SrcRec) * v.size());
+    return GPET_OK;
+}
+
+int gpet_get_phantom_records(gpet_ctx* c, gpet_psf_record* buf, int64_t cap, int64_t* n)
+{
+    if (!c || !n) return GPET_ERR_ARG;
+    std::vector<SrcRec> v;
+    phantom_records(c, v);
+    *n = (int64_t)v.size();
+    if (!buf || *n == 0) return GPET_OK;
+    if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the phantom records");
+    std::memcpy(buf, v.data(), sizeof(SrcRec) * v.size());
     return GPET_OK;
 }
 

@@ -15,6 +15,15 @@ struct ExitRec {
     int32_t status, panel;
 };
 
+// an emitted photon (source phase space, gPET.cu:63-87), 40 bytes; t = 0
+// when the photon slot carries nothing
+struct SrcRec {
+    float x, y, z, ux, uy, uz, E;
+    int32_t eventid;
+    double t;
+};
+static_assert(sizeof(SrcRec) == 40, "source record is 40 bytes");
+
 // A wave of decays: global indices [g0[i], g0[i+1]) are decays d0[i] ..
 // of simulation sim[i] (sims[] in device memory). Waves live in a device
 // table that the kernels index, so that the launches of a chunk of waves do
@@ -29,6 +38,7 @@ struct Wave {
     int64_t n;                    // decays in the wave
     unsigned long long* work;     // photon counter of k_phantom, zero at launch
     ExitRec* exits;               // per photon of the wave, or NULL
+    SrcRec* source;               // per photon of the wave, or NULL
 };
 
 // detector queue, structure of arrays (cap entries each)

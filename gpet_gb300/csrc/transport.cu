@@ -308,11 +308,25 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
                         st_init(st, S.key0, S.key1, kTagPhantom + k, (uint64_t)d);
                         steps = 0;
                         active = true;
-                    } else if (exits) {
-                        ExitRec e;
-                        e.x = e.y = e.z = e.ux = e.uy = e.uz = e.E = 0.0f; e.nscat = 0; e.t = 0.0;
-                        e.status = 2; e.panel = -1;
-                        exits[p] = e;
+                        if (w.source) {
+                            SrcRec r;
+                            r.x = ph.x[0]; r.y = ph.x[1]; r.z = ph.x[2];
+                            r.ux = ph.u[0]; r.uy = ph.u[1]; r.uz = ph.u[2];
+                            r.E = ph.E; r.eventid = (int32_t)d; r.t = ph.t;
+                            w.source[p] = r;
+                        }
+                    } else {
+                        if (exits) {
+                            ExitRec e;
+                            e.x = e.y = e.z = e.ux = e.uy = e.uz = e.E = 0.0f; e.nscat = 0; e.t = 0.0;
+                            e.status = 2; e.panel = -1;
+                            exits[p] = e;
+                        }
+                        if (w.source) {
+                            SrcRec r;
+                            r.x = r.y = r.z = r.ux = r.uy = r.uz = r.E = 0.0f; r.eventid = 0; r.t = 0.0;
+                            w.source[p] = r;
+                        }
                     }
                 }
             }

@@ -448,3 +448,25 @@ def read_coincidences(path):
     cls_path = path.replace(".dat", "_class.dat")
     cls = np.fromfile(cls_path, dtype=np.uint8) if os.path.exists(cls_path) else None
     return ev, cls
+
+
+# ---------------------------------------------------------------- phase space
+PSF_STATE_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("ux", "<f4"), ("uy", "<f4"), ("uz", "<f4"),
+                            ("E", "<f4")])
+
+
+def read_phase_space(directory, stem):
+    """out<stem>.dat (float3 position + float4 direction/energy per photon),
+    id<stem>.dat (int32 event id) and time<stem>.dat (double, us) as written
+    by gPET with OUTPUTPSF (gPET.cu:63-114); stem is "source" or "phantom"."""
+    st = np.fromfile(os.path.join(directory, "out%s.dat" % stem), PSF_STATE_DTYPE)
+    ids = np.fromfile(os.path.join(directory, "id%s.dat" % stem), "<i4")
+    t = np.fromfile(os.path.join(directory, "time%s.dat" % stem), "<f8")
+    if not (len(st) == len(ids) == len(t)):
+        raise ValueError("phase-space files of %s disagree in length" % stem)
+    out = np.zeros(len(st), [(n, st.dtype[n]) for n in st.dtype.names] + [("eventid", "<i4"), ("t", "<f8")])
+    for n in st.dtype.names:
+        out[n] = st[n]
+    out["eventid"] = ids
+    out["t"] = t
+    return out

@@ -170,9 +170,26 @@ int gpet_get_hits(gpet_ctx* ctx, int32_t* ids, float* f, int64_t cap, int64_t* n
  * words: x,y,z,ux,uy,uz,E (float), nscat (int32), t (double), status (int32:
  * 0 absorbed, 1 escaped, 2 not emitted, 3 step cap), panel (int32, -1 none). */
 int gpet_get_exits(gpet_ctx* ctx, void* buf, int64_t cap, int64_t* n);
+/* Phase-space records (OUTPUTPSF 1/2, gPET.cu:63-114, 296-352), 40 bytes:
+ * position, direction, energy (float), event id (int32), time (double, us). */
+typedef struct {
+    float x, y, z, ux, uy, uz, E;
+    int32_t eventid;
+    double t;
+} gpet_psf_record;
+/* Emitted photons (option record_source=1): the annihilation photons (or
+ * the PSF's photons) as they leave the source stage, time > 0 only. */
+int gpet_get_source_records(gpet_ctx* ctx, gpet_psf_record* buf, int64_t cap, int64_t* n);
+/* Photons leaving the phantom (option record_exits=1), time > 0 only; with
+ * option psf_sphere=1 moved along their direction onto the record sphere of
+ * input_PET.in (getDistance, gPET_kernals.cu:148-171; RECORDPSF -1). */
+int gpet_get_phantom_records(gpet_ctx* ctx, gpet_psf_record* buf, int64_t cap, int64_t* n);
 /* Append the run's records to out_dir: singles.dat, adder.dat, HitsID.dat,
  * Hits.dat (outevents/outputData, detector.cu:287-307, 387-408) and
- * coincidences.dat (+ coincidences_class.dat). */
+ * coincidences.dat (+ coincidences_class.dat); with record_source=1
+ * outsource.dat / idsource.dat / timesource.dat, with record_exits=1
+ * outphantom.dat / idphantom.dat / timephantom.dat (28-byte state, int32 id,
+ * double time per photon, the reference's layouts). */
 int gpet_write_outputs(gpet_ctx* ctx, const char* out_dir);
 
 /* ------------------------------------------------------------ introspection */

@@ -42,6 +42,9 @@ class _Exit(C.Structure):
 EXIT_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("ux", "<f4"), ("uy", "<f4"), ("uz", "<f4"),
                        ("E", "<f4"), ("nscat", "<i4"), ("t", "<f8"), ("status", "<i4"), ("panel", "<i4")])
 assert EXIT_DTYPE.itemsize == C.sizeof(_Exit)
+# emitted-photon / phantom-exit phase-space record (40 bytes)
+PSF_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("ux", "<f4"), ("uy", "<f4"), ("uz", "<f4"),
+                      ("E", "<f4"), ("eventid", "<i4"), ("t", "<f8")])
 
 _FP = C.POINTER(C.c_float)
 _IP = C.POINTER(C.c_int32)
@@ -81,7 +84,7 @@ class _Result(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "n_decays", "n_pairs", "n_entered", "n_pulses", "n_hits", "n_threshold", "n_deadtime", "n_singles",
         "n_coinc", "n_true", "n_scatter", "n_random", "n_multiple", "n_overflow", "n_stepcap")] + [
-        ("exits", C.POINTER(_Exit)), ("pulses", C.POINTER(_Event)),
+        ("exits", C.POINTER(_Exit)), ("source", C.c_void_p), ("pulses", C.POINTER(_Event)),
         ("pulse_scat", C.POINTER(C.c_uint8)), ("pulse_slot", C.POINTER(C.c_uint8)),
         ("hit_id", _IP), ("hit_f", _FP),
         ("singles", C.POINTER(_Event)), ("single_scat", C.POINTER(C.c_uint8)), ("single_slot", C.POINTER(C.c_uint8)),
@@ -227,16 +230,19 @@ class OracleScene:
         s.seed = int(options.get("seed", 20261203)); s.sim_id = int(options.get("sim_id", 0))
         self.s = s
 
-    def run(self, d_begin=0, d_end=None, precision="fp64", threads=0, exits=False, hits=False):
+    def run(self, d_begin=0, d_end=None, precision="fp64", threads=0, exits=False, hits=False, source=False):
         d_end = self.n_decays if d_end is None else d_end
         r = _Result()
         L = lib(precision)
-        rc = L.oracle_run(C.byref(self.s), d_begin, d_end, threads, (1 if exits else 0) | (2 if hits else 0),
-                          C.byref(r))
+        rc = L.oracle_run(C.byref(self.s), d_begin, d_end, threads,
+                          (1 if exits else 0) | (2 if hits else 0) | (4 if source else 0), C.byref(r))
         if rc != 0:
             raise RuntimeError("oracle_run failed: %d" % rc)
         try:
-            return _collect(r, exits)
+            out = _collect(r, exits)
+            if source:
+                out["source"] = _arr(r.source, 2 * r.n_decays, PSF_DTYPE)
+            return out
         finally:
             L.oracle_free_result(C.byref(r))
 

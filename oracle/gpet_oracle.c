@@ -771,10 +771,21 @@ static void record_exit(or_exit* ex, const photon_t* p, int status, int panel)
     ex->E = (float)p->E; ex->t = p->t + (double)p->tf; ex->nscat = p->nscat; ex->status = status; ex->panel = panel;
 }
 
+static void record_src(or_src* s, const photon_t* p, int64_t d)
+{
+    s->x = (float)p->x[0]; s->y = (float)p->x[1]; s->z = (float)p->x[2];
+    s->ux = (float)p->u[0]; s->uy = (float)p->u[1]; s->uz = (float)p->u[2];
+    s->E = (float)p->E; s->eventid = (int32_t)d; s->t = p->t;
+}
+
 static void transport_pair(const or_scene* sc, const prep_t* pp, int64_t d, photon_t ph[2], int have,
-                           or_exit* exits, tbuf_t* tb, int flags)
+                           or_exit* exits, or_src* src, tbuf_t* tb, int flags)
 {
     for (int k = 0; k < 2; ++k) {
+        if (src) {
+            if (have) record_src(&src[k], &ph[k], d);
+            else memset(&src[k], 0, sizeof(or_src));
+        }
         if (!have) {
             if (exits) { photon_t z; memset(&z, 0, sizeof(z)); record_exit(&exits[k], &z, 2, -1); }
             continue;
@@ -797,7 +808,8 @@ static void transport_pair(const or_scene* sc, const prep_t* pp, int64_t d, phot
     }
 }
 
-static void simulate_decay(const or_scene* sc, const prep_t* pp, int64_t d, or_exit* exits, tbuf_t* tb, int flags)
+static void simulate_decay(const or_scene* sc, const prep_t* pp, int64_t d, or_exit* exits, or_src* src, tbuf_t* tb,
+                           int flags)
 {
     stream_t st;
     st_init(&st, sc, TAG_DECAY, (uint64_t)d);
@@ -811,6 +823,11 @@ static void simulate_decay(const or_scene* sc, const prep_t* pp, int64_t d, or_e
             ph[0].u[0] = (real)(float)r[4]; ph[0].u[1] = (real)(float)r[5]; ph[0].u[2] = (real)(float)r[6];
             ph[0].E = (real)(float)r[7]; ph[0].t = r[3]; ph[0].tf = (real)0.0; ph[0].nscat = 0;
             /* one photon per record: photon slot 1 carries nothing */
+            if (src) {
+                if (r[3] > 0.0 && ph[0].E >= (real)0.0) record_src(&src[0], &ph[0], d);
+                else memset(&src[0], 0, sizeof(or_src));
+                memset(&src[1], 0, sizeof(or_src));
+            }
             stream_t s0;
             st_init(&s0, sc, TAG_PHANTOM, (uint64_t)d);
             int status = r[3] > 0.0 && ph[0].E >= (real)0.0 ? phantom_transport(sc, &pp->wph, &ph[0], &s0) : 2;
@@ -837,7 +854,7 @@ static void simulate_decay(const or_scene* sc, const prep_t* pp, int64_t d, or_e
         make_pair(sc, &st, pos, ph, r[3]);
         have = 1;
         tb->n_pairs++;
-        transport_pair(sc, pp, d, ph, have, exits, tb, flags);
+        transport_pair(sc, pp, d, ph, have, exits, src, tb, flags);
         return;
     }
     /* source mode: decay d belongs to the source whose index range holds it */
@@ -866,7 +883,7 @@ static void simulate_decay(const or_scene* sc, const prep_t* pp, int64_t d, or_e
         have = 1;
         tb->n_pairs++;
     }
-    transport_pair(sc, pp, d, ph, have, exits, tb, flags);
+    transport_pair(sc, pp, d, ph, have, exits, src, tb, flags);
 }
 
 /* ------------------------------------------------------------- digitizer */
@@ -1067,6 +1084,7 @@ int oracle_run(const or_scene* sc, int64_t d_begin, int64_t d_end, int nthreads,
     if (nd < 0) { free(pp); return -4; }
     out->n_decays = nd;
     if (flags & 1) out->exits = (or_exit*)calloc((size_t)(2 * nd + 1), sizeof(or_exit));
+    if (flags & 4) out->source = (or_src*)calloc((size_t)(2 * nd + 1), sizeof(or_src));
 #ifdef _OPENMP
     if (nthreads < 1) nthreads = omp_get_max_threads();
 #else
@@ -1086,7 +1104,8 @@ int oracle_run(const or_scene* sc, int64_t d_begin, int64_t d_end, int nthreads,
 #pragma omp for schedule(dynamic, 256)
 #endif
         for (int64_t d = d_begin; d < d_end; ++d)
-            simulate_decay(sc, pp, d, out->exits ? out->exits + 2 * (d - d_begin) : NULL, &tb[tid], flags);
+            simulate_decay(sc, pp, d, out->exits ? out->exits + 2 * (d - d_begin) : NULL,
+                           out->source ? out->source + 2 * (d - d_begin) : NULL, &tb[tid], flags);
     }
     int64_t np = 0, nh = 0;
     for (int t = 0; t < nthreads; ++t) {
@@ -1141,7 +1160,7 @@ int oracle_digitize(const or_scene* sc, const or_event* pulses, const uint8_t* s
 
 void oracle_free_result(or_result* r)
 {
-    free(r->exits); free(r->pulses); free(r->pulse_scat); free(r->pulse_slot);
+    free(r->exits); free(r->source); free(r->pulses); free(r->pulse_scat); free(r->pulse_slot);
     free(r->hit_id); free(r->hit_f); free(r->singles); free(r->single_scat); free(r->single_slot);
     free(r->coinc); free(r->coinc_class);
     memset(r, 0, sizeof(*r));

@@ -92,6 +92,14 @@ typedef struct {
     int32_t panel;                 /* entered panel index, -1 none */
 } or_exit;
 
+/* an emitted photon (the source phase space, gPET.cu:63-87): t = 0 when the
+ * photon slot carries nothing */
+typedef struct {
+    float x, y, z, ux, uy, uz, E;
+    int32_t eventid;
+    double t;
+} or_src;
+
 typedef struct {
     int64_t n_decays, n_pairs, n_entered;
     int64_t n_pulses, n_hits;
@@ -100,6 +108,7 @@ typedef struct {
     int64_t n_overflow, n_stepcap;
     /* arrays owned by the oracle, free with oracle_free_result */
     or_exit* exits;               /* [2*n_decays] when requested */
+    or_src* source;               /* [2*n_decays] when requested */
     or_event* pulses;             /* after adder + readout, sorted by (parn, slot) */
     uint8_t* pulse_scat;
     uint8_t* pulse_slot;
@@ -113,7 +122,8 @@ typedef struct {
 } or_result;
 
 /* Simulate decays [d_begin, d_end) (or PSF records) and digitize.
- * flags bit0: record exits; bit1: record hits. Returns 0 on success. */
+ * flags bit0: record exits; bit1: record hits; bit2: record the emitted
+ * photons. Returns 0 on success. */
 int oracle_run(const or_scene* sc, int64_t d_begin, int64_t d_end, int nthreads, int flags, or_result* out);
 /* Digitizer + coincidence sorter alone on a given pulse list (same semantics). */
 int oracle_digitize(const or_scene* sc, const or_event* pulses, const uint8_t* scat, const uint8_t* slot,

@@ -106,3 +106,19 @@ def test_null_context_is_an_error(gpet_lib):
     assert gpet_lib.gpet_run(None, None) == -1
     assert gpet_lib.gpet_set_option(None, b"seed", b"1") == -1
     assert gpet_lib.gpet_last_error(None) == b"null context"
+
+
+def test_phase_space_reader(tmp_path):
+    from gpet_gb300 import formats as F
+    rng = np.random.default_rng(2)
+    st = rng.standard_normal((5, 7)).astype("<f4")
+    ids = np.arange(5, dtype="<i4") * 3
+    t = rng.uniform(1, 2, 5)
+    st.tofile(str(tmp_path / "outphantom.dat"))
+    ids.tofile(str(tmp_path / "idphantom.dat"))
+    t.tofile(str(tmp_path / "timephantom.dat"))
+    r = F.read_phase_space(str(tmp_path), "phantom")
+    assert np.array_equal(r["uy"], st[:, 4]) and np.array_equal(r["eventid"], ids) and np.array_equal(r["t"], t)
+    (tmp_path / "timephantom.dat").write_bytes(b"\0" * 8)
+    with pytest.raises(ValueError):
+        F.read_phase_space(str(tmp_path), "phantom")

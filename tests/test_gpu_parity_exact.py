@@ -74,3 +74,76 @@ def test_singles_and_coincidences_bit_exact(which, scene_small, scene_positron, 
     assert (st["n_true"], st["n_scatter"], st["n_random"], st["n_multiple"]) == (
         r["n_true"], r["n_scatter"], r["n_random"], r["n_multiple"])
     assert st["n_coinc"] > 0
+
+
+def _sphere_distance(x, u, sph):
+    """getDistance (gPET_kernals.cu:148-171) in float32, the reference's root choice."""
+    f = np.float32
+    cx, cy, cz = f(x[0] - sph[0]), f(x[1] - sph[1]), f(x[2] - sph[2])
+    a = f(f(u[0] * u[0]) + f(u[1] * u[1])) + f(u[2] * u[2])
+    b = f(2.0) * (f(f(u[0] * cx) + f(u[1] * cy)) + f(u[2] * cz))
+    c = (f(f(cx * cx) + f(cy * cy)) + f(cz * cz)) - f(sph[3]) * f(sph[3])
+    disc = f(b * b) - f(f(4.0) * a) * c
+    if disc < 0:
+        return f(0.0)
+    r = np.sqrt(disc, dtype=np.float32)
+    if c < 0:
+        return f((-b + r) / (f(2.0) * a))
+    if b < 0:
+        return f((-b - r) / (f(2.0) * a))
+    return f((-b + r) / (f(2.0) * a))
+
+
+@pytest.mark.parametrize("which", ["small", "positron"])
+def test_phase_space_records_bit_exact(which, scene_small, scene_positron, data_dir, gpet_lib, oracle_mod, tmp_path):
+    """Source and phantom phase space (OUTPUTPSF 1/2) against the FP32 oracle."""
+    from gpet_gb300 import formats as F
+    scene = scene_small if which == "small" else scene_positron
+    ctx = make_ctx(scene, data_dir, record_exits=1, record_source=1)
+    st = ctx.run()
+    o = oracle_for(scene, data_dir, panels=ctx.panels())
+    r = o.run(precision="fp32", exits=True, source=True)
+    src = ctx.source_records()
+    osrc = r["source"][r["source"]["t"] > 0]
+    assert len(src) == len(osrc) > 0
+    assert np.array_equal(src.view(np.uint8), osrc.view(np.uint8))
+    assert len(src) == 2 * st["n_pairs"] or which == "small"
+    ph = ctx.phantom_records()
+    ex = r["exits"]
+    keep = (ex["status"] == 1) & (ex["t"] > 0)
+    assert len(ph) == keep.sum()
+    for k in ("x", "y", "z", "ux", "uy", "uz", "E", "t"):
+        assert np.array_equal(ph[k], ex[k][keep]), k
+    assert np.array_equal(ph["eventid"], np.nonzero(keep)[0] // 2)
+    # the files, in the reference's layouts
+    ctx.write_outputs(str(tmp_path))
+    back = F.read_phase_space(str(tmp_path), "source")
+    assert len(back) == len(src) and np.array_equal(back["E"], src["E"]) and np.array_equal(back["t"], src["t"])
+    assert (tmp_path / "outphantom.dat").stat().st_size == 28 * len(ph)
+    assert (tmp_path / "idphantom.dat").stat().st_size == 4 * len(ph)
+    assert (tmp_path / "timephantom.dat").stat().st_size == 8 * len(ph)
+
+
+def test_phantom_records_on_record_sphere(scene_small, data_dir, gpet_lib):
+    """psf_sphere=1: exit photons moved along their direction onto the record
+    sphere of input_PET.in (getDistance)."""
+    from gpet_gb300 import formats as F
+    ctx = make_ctx(scene_small, data_dir, record_exits=1)
+    ctx.run()
+    plain = ctx.phantom_records()
+    ctx.set_option("psf_sphere", 1)
+    proj = ctx.phantom_records()
+    sph = np.array(F.read_config(scene_small.config_path).recordsphere, np.float32)
+    assert len(proj) == len(plain) > 100
+    on = 0
+    for a, b in zip(plain[:500], proj[:500]):
+        x = np.array([a["x"], a["y"], a["z"]], np.float32)
+        u = np.array([a["ux"], a["uy"], a["uz"]], np.float32)
+        d = _sphere_distance(x, u, sph)
+        want = x + d * u
+        assert np.allclose([b["x"], b["y"], b["z"]], want, rtol=1e-6, atol=1e-6)
+        assert abs(b["t"] - (a["t"] + float(d) / 29979.2458)) < 1e-9
+        if d > 0:
+            on += 1
+            assert abs(np.linalg.norm(want - sph[:3]) - sph[3]) < 1e-4
+    assert on > 100
