@@ -52,7 +52,7 @@ class RunStats(C.Structure):
                                   "ms_coincidence")] + [
         ("kernel_launches", C.c_int64), ("phantom_steps", C.c_int64), ("detector_steps", C.c_int64),
         ("ms_source", C.c_double), ("ms_phantom", C.c_double), ("n_surrogate", C.c_int64),
-        ("ms_surrogate", C.c_double)]
+        ("ms_surrogate", C.c_double), ("n_noise", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

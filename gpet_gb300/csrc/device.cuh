@@ -25,7 +25,7 @@ constexpr float kMC2 = 510999.1f;              // constants.h:37
 constexpr float kIMC2 = 1.95695060911e-6f;     // constants.h:38
 constexpr double kSpe = 29979.2458;            // cm/us, gPET_kernals.cu:264
 
-enum : uint32_t { kTagDecay = 1, kTagPhantom = 2, kTagDet = 4, kTagBlur = 8 };
+enum : uint32_t { kTagDecay = 1, kTagPhantom = 2, kTagDet = 4, kTagBlur = 8, kTagNoise = 9 };
 
 // Everything one simulation needs on the device. Lives in device memory; the
 // kernels copy it into shared memory once per block.

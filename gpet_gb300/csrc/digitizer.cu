@@ -232,19 +232,21 @@ __global__ void k_blur_threshold(PulseDev P, int64_t n, const DigiParams* __rest
             const DigiParams& prm = prms[pulse_sim(P, i)];
             const int32_t parn = P.parn[i];
             const uint32_t slot = P.meta[i] & 0x7fu;
-            Stream st;
-            st_init(st, prm.key0, prm.key1, kTagBlur, ((uint64_t)(uint32_t)parn << 4) | slot);
             float E = P.E[i], x = P.x[i], y = P.y[i], z = P.z[i];
-            float R = 0.0f;
-            if (prm.blurpolicy == 0) R = dm_sqrt(prm.Eref / E) * prm.Rref;
-            if (prm.blurpolicy == 1) R = prm.Rref + prm.Eslope * (E - prm.Eref) / 1.0e6f;
-            if (R < 0.0f) R = 0.0f;
-            float zn = st_normal(st);
-            E += zn * R * E / 2.35482f;
-            if (prm.Sblur > 0.0f) {
-                x += prm.Sblur * st_normal(st);
-                y += prm.Sblur * st_normal(st);
-                z += prm.Sblur * st_normal(st);
+            if (parn >= 0) {   // background singles (parn -1) carry their own energy spread
+                Stream st;
+                st_init(st, prm.key0, prm.key1, kTagBlur, ((uint64_t)(uint32_t)parn << 4) | slot);
+                float R = 0.0f;
+                if (prm.blurpolicy == 0) R = dm_sqrt(prm.Eref / E) * prm.Rref;
+                if (prm.blurpolicy == 1) R = prm.Rref + prm.Eslope * (E - prm.Eref) / 1.0e6f;
+                if (R < 0.0f) R = 0.0f;
+                float zn = st_normal(st);
+                E += zn * R * E / 2.35482f;
+                if (prm.Sblur > 0.0f) {
+                    x += prm.Sblur * st_normal(st);
+                    y += prm.Sblur * st_normal(st);
+                    z += prm.Sblur * st_normal(st);
+                }
             }
             Eb[i] = E; xb[i] = x; yb[i] = y; zb[i] = z;
             keep = !(E < prm.Eth || E > 2000000.0f);
@@ -476,7 +478,7 @@ __global__ void k_coinc_write(const uint32_t* __restrict__ sidx, int64_t s, cons
                 const uint32_t pa = sidx[a], pb = sidx[b];
                 if (pann[pa] == pann[pb]) continue;
                 uint8_t k;
-                if (eid[pa] == eid[pb]) k = ((meta[pa] | meta[pb]) & 0x80u) ? 1 : 0;
+                if (eid[pa] == eid[pb] && eid[pa] >= 0) k = ((meta[pa] | meta[pb]) & 0x80u) ? 1 : 0;
                 else k = 2;
                 if (o < cap) {
                     pairs[2 * (int64_t)o] = a;
@@ -493,6 +495,66 @@ __global__ void k_coinc_write(const uint32_t* __restrict__ sidx, int64_t s, cons
     c0.flush(cnt, CF(n_true));
     c1.flush(cnt, CF(n_scat));
     c2.flush(cnt, CF(n_rand));
+}
+
+// ---------------------------------------------------------------- background singles
+// events of interval i; with P, written from index o on
+__device__ int noise_interval(const NoiseParams& np, int64_t i, const PulseDev* P, int64_t o)
+{
+    Stream st;
+    st_init(st, np.key0, np.key1, kTagNoise, (uint64_t)i);
+    double t = np.t0_us + (double)i * np.interval_us;
+    double te = np.t0_us + (double)(i + 1) * np.interval_us;
+    if (te > np.t1_us) te = np.t1_us;
+    int k = 0;
+    for (; k < kMaxNoisePerInterval; ++k) {
+        const float u = st_u(st);
+        t += (double)(-np.lambda_us * dm_logf(u));
+        if (!(t < te)) break;
+        if (!P) {   // count only: skip the event's eight draws
+            for (int d = 0; d < 8; ++d) (void)st_next(st);
+            continue;
+        }
+        const float E = np.emean + np.sigma * st_normal(st);
+        const float x = st_u(st);
+        const float y = st_u(st);
+        const float z = st_u(st);
+        int pann = (int)((float)np.npanels * st_u(st));
+        int modn = (int)((float)np.moduleN * st_u(st));
+        int cryn = (int)((float)np.crystalN * st_u(st));
+        pann = pann > np.npanels - 1 ? np.npanels - 1 : pann;
+        modn = modn > np.moduleN - 1 ? np.moduleN - 1 : modn;
+        cryn = cryn > np.crystalN - 1 ? np.crystalN - 1 : cryn;
+        const int64_t j = o + k;
+        P->parn[j] = -1;
+        P->pann[j] = pann;
+        P->modn[j] = modn;
+        P->cryn[j] = cryn;
+        P->siten[j] = pann * np.moduleN * np.crystalN + modn * np.crystalN + cryn;
+        P->eventid[j] = -1;
+        P->t[j] = t;
+        P->E[j] = E;
+        P->x[j] = x;
+        P->y[j] = y;
+        P->z[j] = z;
+        P->meta[j] = 0;
+        if (P->sim) P->sim[j] = np.sim;
+    }
+    return k;
+}
+
+__global__ void k_noise_count(NoiseParams np, uint32_t* cnt)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np.nint; i += (int64_t)gridDim.x * blockDim.x)
+        cnt[i] = (uint32_t)noise_interval(np, i, nullptr, 0);
+}
+
+__global__ void k_noise_write(NoiseParams np, const uint32_t* __restrict__ off, PulseDev P, int64_t base, Counters* cnt)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np.nint; i += (int64_t)gridDim.x * blockDim.x) {
+        const int k = noise_interval(np, i, &P, base + off[i]);
+        if (k) atomicAdd(&cnt[np.sim].n_noise, (unsigned long long)k);
+    }
 }
 
 static unsigned grid_for_g(int64_t n)
@@ -547,6 +609,31 @@ static int ensure(void** p, size_t bytes, size_t* have)
     if (cudaMalloc(p, bytes ? bytes : 16) != cudaSuccess) return GPET_ERR_CUDA;
     *have = bytes;
     return 0;
+}
+
+int noise_count(const NoiseParams& np, DigiScratch& D, cudaStream_t s, int64_t* launches, int64_t* total_out)
+{
+    *total_out = 0;
+    if (np.nint <= 0) return 0;
+    if (np.nint > D.cap) return GPET_ERR_CAPACITY;
+    k_noise_count<<<grid_for(np.nint, 256), 256, 0, s>>>(np, D.sel);
+    ++*launches;
+    uint32_t* total = reinterpret_cast<uint32_t*>(D.dcount + 6);
+    scan_exclusive(D.sel, D.wcount, np.nint, D.scan_aux, total, s, launches);
+    uint32_t h = 0;
+    cudaMemcpyAsync(&h, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) return GPET_ERR_CUDA;
+    *total_out = h;
+    return 0;
+}
+
+int noise_write(const NoiseParams& np, const DigiScratch& D, const PulseDev& P, int64_t base, Counters* cnt,
+                cudaStream_t s, int64_t* launches)
+{
+    if (np.nint <= 0) return 0;
+    k_noise_write<<<grid_for(np.nint, 256), 256, 0, s>>>(np, D.wcount, P, base, cnt);
+    ++*launches;
+    return cudaGetLastError() == cudaSuccess ? 0 : GPET_ERR_CUDA;
 }
 
 int digitize_device(const PulseDev& P, int64_t n, const DigiParams* d_prms, int nsims, int64_t max_site,

@@ -69,6 +69,7 @@ struct Work {
     // results
     int nsims = 0;
     int64_t n_pulses = 0, n_hits = 0, n_singles = 0, n_coinc = 0;
+    int64_t n_digi = 0;                   // pulses digitized: n_pulses plus background singles
     std::vector<Counters> hcnt;           // per simulation
     std::vector<uint8_t> sim_hits;        // per simulation: hits recorded
     std::vector<int64_t> s_off, c_off;    // first single / coincidence of each simulation
@@ -104,6 +105,9 @@ struct gpet_ctx {
     bool tuned = false;
     int record_entries = 0;               // keep the entry records of the detector stage
     int record_source = 0;                // keep the emitted photons (source phase space)
+    float noise_lambda_us = 0.0f;         // background singles: mean gap (us), 0 = none
+    float noise_emean = 511000.0f, noise_sigma = 0.0f;
+    double noise_interval_us = 1000.0;
     int psf_sphere = 0;                   // phantom phase space projected onto the record sphere
     gpet_surrogate* sur = nullptr;        // learned detector response (not owned)
     std::string base_dir = ".";
@@ -256,6 +260,10 @@ int gpet_set_option(gpet_ctx* c, const char* key, const char* value)
     else if (k == "record_entries") c->record_entries = (int)std::strtol(value, &end, 10);
     else if (k == "record_source") c->record_source = (int)std::strtol(value, &end, 10);
     else if (k == "psf_sphere") c->psf_sphere = (int)std::strtol(value, &end, 10);
+    else if (k == "noise_lambda_us") c->noise_lambda_us = std::strtof(value, &end);
+    else if (k == "noise_emean_ev") c->noise_emean = std::strtof(value, &end);
+    else if (k == "noise_sigma_ev") c->noise_sigma = std::strtof(value, &end);
+    else if (k == "noise_interval_us") c->noise_interval_us = std::strtod(value, &end);
     else if (k == "base_dir") { c->base_dir = v; return GPET_OK; }
     else if (k == "data_dir") { c->data_dir = v; return GPET_OK; }
     else return fail(c, GPET_ERR_ARG, "unknown option " + k);
@@ -264,6 +272,10 @@ int gpet_set_option(gpet_ctx* c, const char* key, const char* value)
     if (c->chunk_decays < 1024) return fail(c, GPET_ERR_ARG, "chunk_decays must be >= 1024");
     if (c->sub_decays < 1024) return fail(c, GPET_ERR_ARG, "sub_decays must be >= 1024");
     if (c->phantom_bps < 0 || c->phantom_bps > 32) return fail(c, GPET_ERR_ARG, "phantom_blocks_per_sm must be 0..32");
+    if (!(c->noise_lambda_us >= 0.0f) || !(c->noise_interval_us > 0.0) || !(c->noise_sigma >= 0.0f))
+        return fail(c, GPET_ERR_ARG, "noise_lambda_us >= 0, noise_interval_us > 0, noise_sigma_ev >= 0");
+    if (c->noise_lambda_us > 0.0f && c->noise_interval_us > 1024.0 * c->noise_lambda_us)
+        return fail(c, GPET_ERR_ARG, "noise_interval_us may hold at most 1024 mean gaps");
     if (c->drain_period < 1 || c->drain_period > 32) return fail(c, GPET_ERR_ARG, "drain_period must be 1..32");
     for (int t : {c->det_threads, c->src_threads})
         if (t < 32 || t > 256 || t % 32) return fail(c, GPET_ERR_ARG, "threads per block must be 32..256, a multiple of 32");
@@ -709,6 +721,7 @@ static void fill_stats(const Counters& h, gpet_run_stats* st)
     st->phantom_steps = (int64_t)h.ph_steps;
     st->detector_steps = (int64_t)h.det_steps;
     st->n_surrogate = (int64_t)h.n_surrogate;
+    st->n_noise = (int64_t)h.n_noise;
 }
 
 // the leader's Work for a new run: reused unless other contexts still hold
@@ -719,20 +732,58 @@ static Work& fresh_work(gpet_ctx* c)
     return *c->work;
 }
 
+// background singles of every simulation whose context asks for them,
+// appended after W's first W.n_pulses pulses; sets W.n_digi
+static int add_noise(gpet_ctx* c, Work& W, gpet_ctx* const* cs, int nsim, int64_t* launches)
+{
+    int64_t nd = W.n_pulses;
+    for (int s = 0; s < nsim; ++s) {
+        const gpet_ctx* x = cs[s];
+        if (!(x->noise_lambda_us > 0.0f)) continue;
+        NoiseParams np{};
+        np.key0 = (uint32_t)x->seed;
+        np.key1 = (uint32_t)(x->seed >> 32) + x->sim_id;
+        np.lambda_us = x->noise_lambda_us;
+        np.emean = x->noise_emean;
+        np.sigma = x->noise_sigma;
+        np.t0_us = (double)x->tstart * 1e6;
+        np.t1_us = (double)x->tend * 1e6;
+        np.interval_us = x->noise_interval_us;
+        np.nint = np.t1_us > np.t0_us ? (int64_t)std::ceil((np.t1_us - np.t0_us) / np.interval_us) : 0;
+        np.npanels = x->geo.npanels;
+        np.moduleN = x->geo.moduleN;
+        np.crystalN = x->geo.crystalN;
+        np.sim = s;
+        if (np.nint <= 0) continue;
+        int rc = ensure_digi(c, W, std::max<int64_t>(np.nint, nd));
+        if (rc) return rc;
+        int64_t tot = 0;
+        if (noise_count(np, W.dg, c->stream, launches, &tot)) return fail(c, GPET_ERR_CUDA, "background singles (count)");
+        rc = grow_pulses(c, W, nd + tot, nd);
+        if (rc) return rc;
+        PulseDev P = pulse_view(W);
+        if (noise_write(np, W.dg, P, nd, W.cnt.as<Counters>(), c->stream, launches))
+            return fail(c, GPET_ERR_CUDA, "background singles (write)");
+        nd += tot;
+    }
+    W.n_digi = nd;
+    return GPET_OK;
+}
+
 // digitize W's pulses for nsims simulations with parameters prms (host),
 // leaving per-simulation counts in W.hcnt and result offsets in W.s_off/c_off
 static int digitize_work(gpet_ctx* c, Work& W, const std::vector<DigiParams>& prms, int64_t max_site,
                          gpet_run_stats* st, float* ms_digi)
 {
     const int n = (int)prms.size();
-    int rc = ensure_digi(c, W, W.n_pulses);
+    int rc = ensure_digi(c, W, W.n_digi);
     if (rc) return rc;
     CK(W.prms.ensure(sizeof(DigiParams) * n));
     CK(cudaMemcpyAsync(W.prms.p, prms.data(), sizeof(DigiParams) * n, cudaMemcpyHostToDevice, c->stream));
     PulseDev P = pulse_view(W);
     cudaEventRecord(c->ev[4], c->stream);
     int64_t ns = 0, nc = 0;
-    rc = digitize_device(P, W.n_pulses, W.prms.as<DigiParams>(), n, max_site, W.dg, W.cnt.as<Counters>(), c->stream,
+    rc = digitize_device(P, W.n_digi, W.prms.as<DigiParams>(), n, max_site, W.dg, W.cnt.as<Counters>(), c->stream,
                          &st->kernel_launches, &ns, &nc);
     if (rc) return fail(c, rc, std::string("digitizer failed: ") + cudaGetErrorString(cudaGetLastError()));
     cudaEventRecord(c->ev[5], c->stream);
@@ -1174,6 +1225,8 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         }
         return GPET_OK;
     }
+    rc = add_noise(c, W, cs, nsim, &tot.kernel_launches);
+    if (rc) return rc;
     float ms_digi = 0;
     rc = digitize_work(c, W, prms, max_site, &tot, &ms_digi);
     if (rc) return rc;
@@ -1395,6 +1448,9 @@ int gpet_digitize(gpet_ctx* c, const gpet_event* ev, const uint8_t* scat, const 
     CK(cudaMemcpyAsync(W.p_meta.p, M.data(), n, cudaMemcpyHostToDevice, c->stream));
     W.n_pulses = n;
     W.n_hits = 0;
+    gpet_ctx* one[1] = {c};
+    rc = add_noise(c, W, one, 1, &st->kernel_launches);
+    if (rc) return rc;
     std::vector<DigiParams> prms(1, digi_params(c));
     int64_t max_site = std::max<int64_t>(1, (int64_t)c->geo.npanels * c->geo.moduleN * c->geo.crystalN);
     float ms_digi = 0;

@@ -74,6 +74,7 @@ struct Counters {
     unsigned long long n_thr, n_dead, n_single, n_coinc, n_true, n_scat, n_rand, n_mult;
     unsigned long long n_pulse, n_hit;
     unsigned long long n_surrogate;   // photons whose response came from the surrogate
+    unsigned long long n_noise;       // background singles added before the digitizer
 };
 
 // a photon entering a panel and its detector response after adder and
@@ -235,6 +236,27 @@ __global__ void k_coinc_write(const uint32_t* sidx, int64_t s, const uint32_t* w
 __global__ void k_gather_events(PulseDev P, const uint32_t* idx, int64_t n, int blurred, const float* Eb,
                                 const float* xb, const float* yb, const float* zb, const int32_t* site,
                                 EventRec* out, uint8_t* meta);
+
+// Background singles (addnoise, gPET_kernals.cu:699-735; never launched by
+// the reference): a Poisson process over [t0, t1) us cut into intervals of
+// interval_us, each drawn from its own stream (tag 9, id = interval):
+// exponential gaps of mean lambda_us, energy N(emean, sigma), uniform panel,
+// module and crystal, x/y/z uniform in (0, 1) as in the reference, parn and
+// eventid -1. They skip the blur and are never "the same decay".
+struct NoiseParams {
+    uint32_t key0, key1;
+    float lambda_us, emean, sigma;
+    double t0_us, t1_us, interval_us;
+    int64_t nint;
+    int32_t npanels, moduleN, crystalN, sim;
+};
+constexpr int kMaxNoisePerInterval = 4096;
+// events per interval into D.sel, their exclusive prefix into D.wcount, the
+// total into *total_out (synchronises the stream); D.cap >= nint
+int noise_count(const NoiseParams& np, DigiScratch& D, cudaStream_t s, int64_t* launches, int64_t* total_out);
+// write them into P from index `base` on (after noise_count)
+int noise_write(const NoiseParams& np, const DigiScratch& D, const PulseDev& P, int64_t base, Counters* cnt,
+                cudaStream_t s, int64_t* launches);
 
 // Runs blur .. coincidences on n pulses already in P (device), stream-ordered;
 // returns 0 or a GPET_ERR code. Pulses of nsims simulations (P.sim) are

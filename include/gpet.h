@@ -68,6 +68,7 @@ typedef struct {
     double ms_phantom;           /* phantom stage alone (part of ms_source_phantom) */
     int64_t n_surrogate;         /* photons whose detector response came from the surrogate */
     double ms_surrogate;         /* surrogate stage (part of ms_detector) */
+    int64_t n_noise;             /* background singles added before the digitizer */
 } gpet_run_stats;
 
 /* ------------------------------------------------------------ lifetime */
@@ -87,7 +88,10 @@ const char* gpet_last_error(gpet_ctx* ctx);
  *   (results do not depend on it): sub_decays, chunk_decays,
  *   phantom_blocks_per_sm, drain_period, detector_threads, source_threads,
  *   use_graphs (1: each chunk's wave launches replay as one CUDA graph),
- *   autotune (1: gpet_autotune on the first gpet_run). */
+ *   autotune (1: gpet_autotune on the first gpet_run); background singles
+ *   (addnoise, gPET_kernals.cu:699-735): noise_lambda_us (mean gap, 0 = off),
+ *   noise_emean_ev, noise_sigma_ev, noise_interval_us (1000; each interval
+ *   has its own random stream). */
 int gpet_set_option(gpet_ctx* ctx, const char* key, const char* value);
 
 /* ------------------------------------------------------------ inputs */

@@ -77,13 +77,15 @@ class _Scene(C.Structure):
         ("dtime_us", C.c_float), ("ewin_lo", C.c_float), ("ewin_hi", C.c_float),
         ("coinc_window_us", C.c_double), ("coinc_policy", C.c_int32),
         ("seed", C.c_uint64), ("sim_id", C.c_uint32),
+        ("noise_lambda_us", C.c_float), ("noise_emean", C.c_float), ("noise_sigma", C.c_float),
+        ("noise_interval_us", C.c_double), ("noise_t0_us", C.c_double), ("noise_t1_us", C.c_double),
     ]
 
 
 class _Result(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "n_decays", "n_pairs", "n_entered", "n_pulses", "n_hits", "n_threshold", "n_deadtime", "n_singles",
-        "n_coinc", "n_true", "n_scatter", "n_random", "n_multiple", "n_overflow", "n_stepcap")] + [
+        "n_coinc", "n_true", "n_scatter", "n_random", "n_multiple", "n_overflow", "n_stepcap", "n_noise")] + [
         ("exits", C.POINTER(_Exit)), ("source", C.c_void_p), ("pulses", C.POINTER(_Event)),
         ("pulse_scat", C.POINTER(C.c_uint8)), ("pulse_slot", C.POINTER(C.c_uint8)),
         ("hit_id", _IP), ("hit_f", _FP),
@@ -228,6 +230,12 @@ class OracleScene:
         s.coinc_window_us = float(options.get("coinc_window_ns", 4.0)) * 1e-3
         s.coinc_policy = int(options.get("coinc_policy", 0))
         s.seed = int(options.get("seed", 20261203)); s.sim_id = int(options.get("sim_id", 0))
+        s.noise_lambda_us = float(options.get("noise_lambda_us", 0.0))
+        s.noise_emean = float(options.get("noise_emean_ev", 511000.0))
+        s.noise_sigma = float(options.get("noise_sigma_ev", 0.0))
+        s.noise_interval_us = float(options.get("noise_interval_us", 1000.0))
+        s.noise_t0_us = float(np.float32(cfg.tstart)) * 1e6
+        s.noise_t1_us = float(np.float32(cfg.tend)) * 1e6
         self.s = s
 
     def run(self, d_begin=0, d_end=None, precision="fp64", threads=0, exits=False, hits=False, source=False):
@@ -270,7 +278,7 @@ def _arr(ptr, n, dtype, shape=None):
 
 
 def _collect(r, exits):
-    out = {k: int(getattr(r, k)) for k, _ in _Result._fields_[:15]}
+    out = {k: int(getattr(r, k)) for k, _ in _Result._fields_[:16]}
     if exits:
         out["exits"] = _arr(r.exits, 2 * r.n_decays, EXIT_DTYPE)
     out["pulses"] = _arr(r.pulses, r.n_pulses, F.EVENT_DTYPE)

@@ -56,7 +56,7 @@ static inline void r_sincos_turns(real u, real* s, real* c)
 #define MAX_PULSE 8   /* distinct crystals per photon in the adder list */
 #define MAX_HITS 16   /* deposits recorded per photon */
 
-enum { TAG_DECAY = 1, TAG_PHANTOM = 2, TAG_DET = 4, TAG_BLUR = 8 };
+enum { TAG_DECAY = 1, TAG_PHANTOM = 2, TAG_DET = 4, TAG_BLUR = 8, TAG_NOISE = 9 };
 
 /* ------------------------------------------------------------------ RNG */
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), restated from the paper. */
@@ -113,6 +113,9 @@ static inline real st_normal(stream_t* s)
     r_sincos_turns(u2, &sn, &cs);
     return R_SQRT((real)-2.0 * R_LOG(u1)) * cs;
 }
+
+/* uniform in float in both builds (digitizer stages) */
+static inline float st_uf(stream_t* s) { return dm_u01(st_next(s)); }
 
 /* the digitizer always computes in the Event record's float */
 static inline float st_normal_f(stream_t* s)
@@ -923,6 +926,7 @@ static int cmp_parn_slot(const void* a, const void* b)
  * on the order pulses are processed in */
 static void blur_pulse(const or_scene* sc, dpulse_t* p)
 {
+    if (p->e.parn < 0) return;   /* background singles carry their own energy spread */
     stream_t st;
     st_init(&st, sc, TAG_BLUR, ((uint64_t)(uint32_t)p->e.parn << 4) | p->slot);
     float R = 0.0f;
@@ -948,6 +952,62 @@ static int32_t dead_site(const or_scene* sc, const or_event* e)
     case 2: return e->pann * sc->moduleN + e->modn;
     default: return e->siten;
     }
+}
+
+/* background singles (addnoise, gPET_kernals.cu:699-735, never launched by
+ * the reference): a Poisson process over [t0, t1) cut into intervals, each
+ * drawn from its own stream; exponential gaps of mean lambda, energy
+ * N(emean, sigma), a uniform panel, module and crystal, x/y/z uniform in
+ * (0, 1) as the reference leaves them, parn = eventid = -1. Time in double
+ * (the reference kernel accumulates it in float). */
+#define MAX_NOISE_PER_INTERVAL 4096
+static int64_t noise_interval(const or_scene* sc, int64_t i, dpulse_t* out)
+{
+    stream_t st;
+    st_init(&st, sc, TAG_NOISE, (uint64_t)i);
+    double t = sc->noise_t0_us + (double)i * sc->noise_interval_us;
+    double te = sc->noise_t0_us + (double)(i + 1) * sc->noise_interval_us;
+    if (te > sc->noise_t1_us) te = sc->noise_t1_us;
+    int64_t k = 0;
+    for (; k < MAX_NOISE_PER_INTERVAL; ++k) {
+        float u = st_uf(&st);
+        t += (double)(-sc->noise_lambda_us * dm_logf(u));
+        if (!(t < te)) break;
+        if (!out) {   /* count only: skip the event's draws */
+            for (int d = 0; d < 8; ++d) (void)st_uf(&st);
+            continue;
+        }
+        dpulse_t* p = &out[k];
+        memset(p, 0, sizeof(*p));
+        p->e.E = sc->noise_emean + sc->noise_sigma * st_normal_f(&st);
+        p->e.x = st_uf(&st); p->e.y = st_uf(&st); p->e.z = st_uf(&st);
+        int pann = (int)((float)sc->npanels * st_uf(&st));
+        int modn = (int)((float)sc->moduleN * st_uf(&st));
+        int cryn = (int)((float)sc->crystalN * st_uf(&st));
+        if (pann > sc->npanels - 1) pann = sc->npanels - 1;
+        if (modn > sc->moduleN - 1) modn = sc->moduleN - 1;
+        if (cryn > sc->crystalN - 1) cryn = sc->crystalN - 1;
+        p->e.pann = pann; p->e.modn = modn; p->e.cryn = cryn;
+        p->e.siten = pann * sc->moduleN * sc->crystalN + modn * sc->crystalN + cryn;
+        p->e.parn = -1; p->e.eventid = -1; p->e.t = t;
+    }
+    return k;
+}
+
+static dpulse_t* add_noise(const or_scene* sc, dpulse_t* p, int64_t* n, int64_t* nnoise)
+{
+    *nnoise = 0;
+    if (!(sc->noise_lambda_us > 0.0f) || !(sc->noise_interval_us > 0.0) || !(sc->noise_t1_us > sc->noise_t0_us))
+        return p;
+    const int64_t nint = (int64_t)ceil((sc->noise_t1_us - sc->noise_t0_us) / sc->noise_interval_us);
+    int64_t tot = 0;
+    for (int64_t i = 0; i < nint; ++i) tot += noise_interval(sc, i, NULL);
+    p = (dpulse_t*)realloc(p, sizeof(dpulse_t) * (size_t)(*n + tot + 1));
+    int64_t o = *n;
+    for (int64_t i = 0; i < nint; ++i) o += noise_interval(sc, i, p + o);
+    *nnoise = tot;
+    *n += tot;
+    return p;
 }
 
 static void digitize(const or_scene* sc, dpulse_t* p, int64_t n, or_result* out)
@@ -1029,7 +1089,7 @@ static void digitize(const or_scene* sc, dpulse_t* p, int64_t n, or_result* out)
                 }
                 cc[2 * nc] = a; cc[2 * nc + 1] = b;
                 uint8_t klass;
-                if (out->singles[a].eventid == out->singles[b].eventid)
+                if (out->singles[a].eventid == out->singles[b].eventid && out->singles[a].eventid >= 0)
                     klass = (out->single_scat[a] || out->single_scat[b]) ? 1 : 0;
                 else
                     klass = 2;
@@ -1138,6 +1198,7 @@ int oracle_run(const or_scene* sc, int64_t d_begin, int64_t d_end, int nthreads,
     for (int64_t i = 0; i < np; ++i) {
         out->pulses[i] = p[i].e; out->pulse_scat[i] = p[i].scat; out->pulse_slot[i] = p[i].slot;
     }
+    p = add_noise(sc, p, &np, &out->n_noise);
     digitize(sc, p, np, out);
     free(p);
     free(pp);
@@ -1153,6 +1214,7 @@ int oracle_digitize(const or_scene* sc, const or_event* pulses, const uint8_t* s
         p[i].e = pulses[i]; p[i].scat = scat[i]; p[i].slot = slot[i]; p[i].site = 0;
     }
     out->n_pulses = n;
+    p = add_noise(sc, p, &n, &out->n_noise);
     digitize(sc, p, n, out);
     free(p);
     return 0;

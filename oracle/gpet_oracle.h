@@ -82,6 +82,11 @@ typedef struct {
     int32_t coinc_policy;         /* 0: single window, exactly two; 1: all pairs */
     uint64_t seed;
     uint32_t sim_id;
+    /* background singles (addnoise, gPET_kernals.cu:699-735): mean time
+     * between them (us, 0 = off), energy mean and spread (eV), the length of
+     * the intervals each drawn from its own stream, and the window (us) */
+    float noise_lambda_us, noise_emean, noise_sigma;
+    double noise_interval_us, noise_t0_us, noise_t1_us;
 } or_scene;
 
 typedef struct {
@@ -105,7 +110,7 @@ typedef struct {
     int64_t n_pulses, n_hits;
     int64_t n_threshold, n_deadtime, n_singles;
     int64_t n_coinc, n_true, n_scatter, n_random, n_multiple;
-    int64_t n_overflow, n_stepcap;
+    int64_t n_overflow, n_stepcap, n_noise;
     /* arrays owned by the oracle, free with oracle_free_result */
     or_exit* exits;               /* [2*n_decays] when requested */
     or_src* source;               /* [2*n_decays] when requested */

@@ -80,3 +80,34 @@ def test_digitizer_twice_same_context(scene_small, data_dir, gpet_lib, oracle_mo
     for seed in (1, 2):
         ev, scat, slot = synthetic_pulses(5000, seed)
         _check(ctx, o, ev, scat, slot)
+
+
+@pytest.mark.parametrize("n", [0, 5000])
+def test_digitizer_with_background_singles(scene_positron, data_dir, gpet_lib, oracle_mod, tmp_path, n):
+    """addnoise (gPET_kernals.cu:699-735): a Poisson stream of background
+    singles joins the pulses before the digitizer; bit-exact against the
+    oracle, never classed as the same decay."""
+    from gpet_gb300 import formats as F
+    cfg = F.read_config(scene_positron.config_path)
+    cfg.tstart, cfg.tend = 0.0, 0.5
+    path = tmp_path / "input_PET.in"
+    F.write_config(str(path), cfg)
+    import copy
+    sc = copy.copy(scene_positron)
+    sc.config_path = str(path)
+    opts = dict(noise_lambda_us=20.0, noise_emean_ev=450000.0, noise_sigma_ev=60000.0, noise_interval_us=500.0,
+                coinc_policy=1)
+    ctx = make_ctx(sc, data_dir, **opts)
+    o = oracle_for(sc, data_dir, **opts)
+    ev, scat, slot = synthetic_pulses(n, seed=11, t_span=5e5)
+    st = _check(ctx, o, ev, scat, slot)
+    r = o.digitize(ev, scat, slot, precision="fp32")
+    assert st["n_noise"] == r["n_noise"]
+    mean = 5e5 / 20.0
+    assert abs(st["n_noise"] - mean) < 5 * np.sqrt(mean)
+    gs, _ = ctx.singles()
+    noise = gs["parn"] == -1
+    assert noise.sum() > 0 and (gs["eventid"][noise] == -1).all()
+    pr, cl = ctx.coincidences()
+    with_noise = noise[pr[:, 0]] | noise[pr[:, 1]]
+    assert with_noise.any() and (cl[with_noise] == 2).all()

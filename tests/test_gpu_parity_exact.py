@@ -147,3 +147,43 @@ def test_phantom_records_on_record_sphere(scene_small, data_dir, gpet_lib):
             on += 1
             assert abs(np.linalg.norm(want - sph[:3]) - sph[3]) < 1e-4
     assert on > 100
+
+
+def test_quadric_exclusion_bit_exact(scene_small, data_dir, gpet_lib, oracle_mod, tmp_path):
+    """crystalSearch's quadratic surfaces (gPET_kernals.cu:1241-1249): a
+    cylinder of radius 0.35 cm around each panel's local x axis counts as gap
+    material; histories, pulses and singles must still match the oracle."""
+    from gpet_gb300 import formats as F
+    from gpet_gb300.scenes import Scene
+    cfg = F.read_config(scene_small.config_path)
+    cfg.surfaces = [[0, 1, 1, 0, 0, 0, 0, 0, 0, -0.35 ** 2]]
+    path = str(tmp_path / "input_PET.in")
+    F.write_config(path, cfg)
+    scene = Scene(scene_small.directory, path, dict(scene_small.options), "quadric")
+    ctx, st, r = _run_both(scene, data_dir)
+    gx, ox = ctx.exits(), r["exits"]
+    assert _first_diff(gx, ox, ["status", "panel", "nscat", "E", "x", "y", "z", "t"]) is None
+    gp, gsc, gsl = ctx.pulses()
+    assert np.array_equal(gp.view(np.uint8), r["pulses"].view(np.uint8))
+    gs, _ = ctx.singles()
+    assert np.array_equal(gs.view(np.uint8), r["singles"].view(np.uint8))
+    # the excluded cylinder holds no deposit
+    gid, gf = ctx.hits()
+    assert len(gid) > 0
+    assert (gf[:, 3] ** 2 + gf[:, 4] ** 2 >= 0.35 ** 2 - 1e-6).all()
+    # and it changed something against the unexcluded detector
+    ref = make_ctx(scene_small, data_dir)
+    assert ref.run()["n_hits"] != st["n_hits"]
+
+
+def test_run_with_background_singles_bit_exact(scene_small, data_dir, gpet_lib, oracle_mod):
+    opts = dict(noise_lambda_us=2000.0, noise_emean_ev=480000.0, noise_sigma_ev=40000.0, noise_interval_us=1000.0)
+    ctx, st, r = _run_both(scene_small, data_dir, **opts)
+    assert st["n_noise"] == r["n_noise"] > 0
+    gs, gsc = ctx.singles()
+    assert np.array_equal(gs.view(np.uint8), r["singles"].view(np.uint8))
+    pr, cl = ctx.coincidences()
+    assert np.array_equal(pr, r["coinc"]) and np.array_equal(cl, r["coinc_class"])
+    # adder.dat content: the transport's pulses only
+    gp, _, _ = ctx.pulses()
+    assert (gp["parn"] >= 0).all() and len(gp) == r["n_pulses"]

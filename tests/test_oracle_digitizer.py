@@ -114,3 +114,28 @@ def test_fp32_and_fp64_oracles_agree_statistically(scene_positron, data_dir, ora
     for k in ("n_pairs", "n_entered", "n_pulses", "n_singles", "n_coinc"):
         sa, sb = a[k], b[k]
         assert abs(sa - sb) <= 4 * np.sqrt(max(sa, 1)) + 2, (k, sa, sb)
+
+
+def test_background_singles_statistics(oracle_mod, scene_small, data_dir):
+    """The oracle's background stream: Poisson count, Gaussian energy, uniform
+    crystals, times inside the window."""
+    from conftest import oracle_for
+    from gpet_gb300.formats import EVENT_DTYPE
+    o = oracle_for(scene_small, data_dir, noise_lambda_us=50.0, noise_emean_ev=400000.0, noise_sigma_ev=50000.0,
+                   noise_interval_us=800.0, coinc_policy=1)
+    o.s.ewin_lo, o.s.ewin_hi, o.s.Eth, o.s.dtime_us = 0.0, 2.0e6, 0.0, 0.0
+    o.s.noise_t1_us = 2.0e6
+    r = o.digitize(np.zeros(0, EVENT_DTYPE), np.zeros(0, np.uint8), np.zeros(0, np.uint8), precision="fp64")
+    mean = 2.0e6 / 50.0
+    assert abs(r["n_noise"] - mean) < 5 * np.sqrt(mean)
+    s = r["singles"]
+    assert len(s) == r["n_noise"]
+    assert abs(s["E"].mean() - 400000.0) < 5 * 50000.0 / np.sqrt(len(s))
+    assert abs(s["E"].std() - 50000.0) < 0.05 * 50000.0
+    assert (s["t"] >= 0).all() and (s["t"] < 2.0e6).all() and (np.diff(s["t"]) >= 0).all()
+    counts = np.bincount(s["cryn"], minlength=64)
+    exp = len(s) / 64.0
+    chi2 = ((counts - exp) ** 2 / exp).sum()
+    assert chi2 < 63 + 5 * np.sqrt(2 * 63)
+    assert (s["parn"] == -1).all() and (s["eventid"] == -1).all()
+    assert (r["coinc_class"] == 2).all()
