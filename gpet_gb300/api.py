@@ -44,6 +44,11 @@ class Tuning(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class SinoParams(C.Structure):
+    _fields_ = [("n_s", C.c_int32), ("n_phi", C.c_int32), ("n_z", C.c_int32), ("s_max", C.c_float),
+                ("z_max", C.c_float), ("class_mask", C.c_int32)]
+
+
 class RunStats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "n_decays", "n_pairs", "n_entered", "n_pulses", "n_hits", "n_threshold", "n_deadtime", "n_singles",
@@ -89,6 +94,7 @@ def load_library(path=None):
     f32p = C.POINTER(C.c_float)
     L.gpet_get_entries.argtypes = [vp, vp, i64, C.POINTER(i64)]
     L.gpet_get_source_records.argtypes = [vp, vp, i64, C.POINTER(i64)]
+    L.gpet_sinogram.argtypes = [vp, C.POINTER(SinoParams), vp]
     L.gpet_get_phantom_records.argtypes = [vp, vp, i64, C.POINTER(i64)]
     L.gpet_surrogate_create.argtypes = [vp, C.c_uint64, C.POINTER(vp)]
     L.gpet_surrogate_destroy.argtypes = [vp]
@@ -279,6 +285,14 @@ class Context:
         m = C.c_int64()
         if n:
             self._ck(self.L.gpet_get_entries(self.h, _ptr(out), n, C.byref(m)))
+        return out
+
+    def sinogram(self, n_s, n_phi, n_z, s_max, z_max, classes=(0, 1, 2)):
+        """The last run's coincidences as a [n_z][n_phi][n_s] sinogram
+        (gpet_sinogram); classes: 0 true, 1 scatter, 2 random."""
+        p = SinoParams(n_s, n_phi, n_z, s_max, z_max, sum(1 << k for k in classes))
+        out = np.zeros((n_z, n_phi, n_s), np.uint32)
+        self._ck(self.L.gpet_sinogram(self.h, C.byref(p), _ptr(out)))
         return out
 
     def source_records(self):

@@ -636,6 +636,62 @@ int noise_write(const NoiseParams& np, const DigiScratch& D, const PulseDev& P, 
     return cudaGetLastError() == cudaSuccess ? 0 : GPET_ERR_CUDA;
 }
 
+// ---------------------------------------------------------------- sinogram
+__device__ __forceinline__ void global_pos(const float* Pn, float x, float y, float z, double g[3])
+{
+    for (int k = 0; k < 3; ++k)
+        g[k] = (double)Pn[15 + k] + (double)x * (double)Pn[21 + k] + (double)y * (double)Pn[24 + k] +
+               (double)z * (double)Pn[27 + k];
+}
+
+__global__ void k_sinogram(const int64_t* __restrict__ pairs, const uint8_t* __restrict__ klass, int64_t c0,
+                           int64_t nc, const uint32_t* __restrict__ single_idx, const float* __restrict__ xb,
+                           const float* __restrict__ yb, const float* __restrict__ zb, const int32_t* __restrict__ pann,
+                           const float* __restrict__ panels, const int32_t* __restrict__ id2panel, int32_t nid,
+                           SinoParams sp, uint32_t* hist)
+{
+    const double kPi = 3.14159265358979323846;
+    for (int64_t c = c0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < c0 + nc;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        if (!((sp.class_mask >> klass[c]) & 1)) continue;
+        double g[2][3];
+        bool ok = true;
+        for (int e = 0; e < 2; ++e) {
+            const uint32_t p = single_idx[pairs[2 * c + e]];
+            const int id = pann[p];
+            const int pi = (id >= 0 && id < nid) ? id2panel[id] : -1;
+            if (pi < 0) { ok = false; break; }
+            global_pos(panels + pi * kPanelStride, xb[p], yb[p], zb[p], g[e]);
+        }
+        if (!ok) continue;
+        const double dx = g[1][0] - g[0][0], dy = g[1][1] - g[0][1];
+        const double len = sqrt(dx * dx + dy * dy);
+        if (!(len > 0.0)) continue;
+        double phi = atan2(dy, dx);
+        double sd = (g[0][0] * -dy + g[0][1] * dx) / len;
+        if (phi < 0.0) { phi += kPi; sd = -sd; }
+        if (phi >= kPi) { phi -= kPi; sd = -sd; }
+        const double z = 0.5 * (g[0][2] + g[1][2]);
+        const double fs = (sd + sp.s_max) / (2.0 * sp.s_max) * sp.n_s;
+        const double fp = phi / kPi * sp.n_phi;
+        const double fz = (z + sp.z_max) / (2.0 * sp.z_max) * sp.n_z;
+        if (!(fs >= 0.0 && fs < sp.n_s && fz >= 0.0 && fz < sp.n_z)) continue;
+        int is = (int)fs, ip = (int)fp, iz = (int)fz;
+        if (ip >= sp.n_phi) ip = sp.n_phi - 1;
+        atomicAdd(&hist[((int64_t)iz * sp.n_phi + ip) * sp.n_s + is], 1u);
+    }
+}
+
+int sinogram_device(const int64_t* pairs, const uint8_t* klass, int64_t c0, int64_t nc, const uint32_t* single_idx,
+                    const DigiScratch& D, const int32_t* pann, const float* panels, const int32_t* id2panel,
+                    int32_t nid, SinoParams sp, uint32_t* hist, cudaStream_t s)
+{
+    if (nc <= 0) return 0;
+    k_sinogram<<<grid_for(nc, 256), 256, 0, s>>>(pairs, klass, c0, nc, single_idx, D.xb, D.yb, D.zb, pann, panels,
+                                                 id2panel, nid, sp, hist);
+    return cudaGetLastError() == cudaSuccess ? 0 : GPET_ERR_CUDA;
+}
+
 int digitize_device(const PulseDev& P, int64_t n, const DigiParams* d_prms, int nsims, int64_t max_site,
                     DigiScratch& D, Counters* d_cnt, cudaStream_t s, int64_t* launches, int64_t* n_singles_out,
                     int64_t* n_coinc_out)

@@ -1735,6 +1735,40 @@ int gpet_write_outputs(gpet_ctx* c, const char* dir)
     return GPET_OK;
 }
 
+int gpet_sinogram(gpet_ctx* c, const gpet_sino_params* sp, uint32_t* out)
+{
+    if (!c || !sp || !out) return GPET_ERR_ARG;
+    if (sp->n_s < 1 || sp->n_phi < 1 || sp->n_z < 1 || !(sp->s_max > 0.0f) || !(sp->z_max > 0.0f) ||
+        (int64_t)sp->n_s * sp->n_phi * sp->n_z > (1ll << 31))
+        return fail(c, GPET_ERR_ARG, "bad sinogram size");
+    const size_t nbins = (size_t)sp->n_s * sp->n_phi * sp->n_z;
+    std::memset(out, 0, nbins * 4);
+    if (!results(c)) return GPET_OK;
+    CK(cudaSetDevice(c->device));
+    Work& W = *c->work;
+    const int64_t c0 = W.c_off[c->res_sim], nc = W.c_off[c->res_sim + 1] - c0;
+    if (nc == 0) return GPET_OK;
+    // panel id -> panel record
+    std::vector<int32_t> id2p(kMaxPanels, -1);
+    for (int i = 0; i < c->geo.npanels; ++i) {
+        const int id = (int)c->geo.panels[(size_t)i * kPanelStride + 30];
+        if (id >= 0 && id < kMaxPanels) id2p[id] = i;
+    }
+    DevBuf hist, map;
+    CK(hist.ensure(nbins * 4));
+    CK(map.ensure(id2p.size() * 4));
+    CK(cudaMemsetAsync(hist.p, 0, nbins * 4, c->stream));
+    CK(cudaMemcpyAsync(map.p, id2p.data(), id2p.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    SinoParams p{sp->n_s, sp->n_phi, sp->n_z, sp->s_max, sp->z_max, sp->class_mask};
+    PulseDev P = pulse_view(W);
+    if (sinogram_device(W.dg.coinc_pairs, W.dg.coinc_class, c0, nc, W.dg.single_idx, W.dg, P.pann,
+                        c->d_panels.as<float>(), map.as<int32_t>(), kMaxPanels, p, hist.as<uint32_t>(), c->stream))
+        return fail(c, GPET_ERR_CUDA, "sinogram kernel failed");
+    CK(cudaMemcpyAsync(out, hist.p, nbins * 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return GPET_OK;
+}
+
 int gpet_get_source_records(gpet_ctx* c, gpet_psf_record* buf, int64_t cap, int64_t* n)
 {
     if (!c || !n) return GPET_ERR_ARG;

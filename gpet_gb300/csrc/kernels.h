@@ -258,6 +258,20 @@ int noise_count(const NoiseParams& np, DigiScratch& D, cudaStream_t s, int64_t* 
 int noise_write(const NoiseParams& np, const DigiScratch& D, const PulseDev& P, int64_t base, Counters* cnt,
                 cudaStream_t s, int64_t* launches);
 
+// List-mode coincidences -> sinogram (single-slice rebinning): each pair's
+// line between the two singles' global positions (blurred, panel-local ->
+// global with the panel axes) gives angle phi in [0, pi), signed distance s
+// from the axis and mean z; hist[(iz * n_phi + iphi) * n_s + is] counts the
+// pairs whose class bit is set in class_mask (1 true, 2 scatter, 4 random).
+struct SinoParams {
+    int32_t n_s, n_phi, n_z;
+    float s_max, z_max;
+    int32_t class_mask;
+};
+int sinogram_device(const int64_t* pairs, const uint8_t* klass, int64_t c0, int64_t nc, const uint32_t* single_idx,
+                    const DigiScratch& D, const int32_t* pann, const float* panels, const int32_t* id2panel,
+                    int32_t nid, SinoParams sp, uint32_t* hist, cudaStream_t s);
+
 // Runs blur .. coincidences on n pulses already in P (device), stream-ordered;
 // returns 0 or a GPET_ERR code. Pulses of nsims simulations (P.sim) are
 // digitized in one pass with parameters d_prms[sim] (device); singles come out

@@ -188,6 +188,21 @@ int gpet_get_source_records(gpet_ctx* ctx, gpet_psf_record* buf, int64_t cap, in
  * option psf_sphere=1 moved along their direction onto the record sphere of
  * input_PET.in (getDistance, gPET_kernals.cu:148-171; RECORDPSF -1). */
 int gpet_get_phantom_records(gpet_ctx* ctx, gpet_psf_record* buf, int64_t cap, int64_t* n);
+/* No counterpart in the reference (its list-mode output stops at the
+ * singles; readOutput.m reads the records). The last run's coincidences
+ * binned into a sinogram by single-slice rebinning: for each pair, the line
+ * between the two singles' global positions (their blurred panel-local
+ * positions mapped through the panel axes) gives the angle phi in [0, pi),
+ * the signed distance s of the line from the z axis and the mean z;
+ * out[(iz * n_phi + iphi) * n_s + is] (n_s * n_phi * n_z counts) counts the
+ * pairs with s in [-s_max, s_max), z in [-z_max, z_max) whose class bit is in
+ * class_mask (1 true, 2 scatter, 4 random). */
+typedef struct {
+    int32_t n_s, n_phi, n_z;
+    float s_max, z_max;           /* cm */
+    int32_t class_mask;
+} gpet_sino_params;
+int gpet_sinogram(gpet_ctx* ctx, const gpet_sino_params* params, uint32_t* out);
 /* Append the run's records to out_dir: singles.dat, adder.dat, HitsID.dat,
  * Hits.dat (outevents/outputData, detector.cu:287-307, 387-408) and
  * coincidences.dat (+ coincidences_class.dat); with record_source=1
