@@ -51,8 +51,9 @@ struct SimDesc {
     // detector
     int32_t npanels;
     const float* panels;          // [npanels][32]
-    int32_t det_mat[2];
-    float det_den[2];
+    int32_t ndetmat;              // 0 crystal, 1 gap, 2.. crystal regions of surfaces 0..
+    int32_t det_mat[8];
+    float det_den[8];
     int32_t moduleN, crystalN, moduleNy, crystalNy;
     int32_t nsurface;
     float surface[10 * kMaxSurf];
@@ -518,16 +519,24 @@ __device__ __forceinline__ bool enter_panel(const float* __restrict__ P0, int np
     return false;
 }
 
-// crystalSearch, gPET_kernals.cu:1236-1279 (m_id 0 crystal, 1 gap)
+// crystalSearch, gPET_kernals.cu:1236-1279 (m_id 0 crystal, 1 gap). A point
+// inside quadratic surface k is gap (the reference), or, when the detector
+// lists a material 2 + k, crystal of that material (still gap between
+// crystals)
 __device__ __forceinline__ void crystal_search(const SimDesc& S, const float* P, const float x[3], int& m_id,
                                                int& M_id, int& L_id)
 {
     float xx = x[0], y = x[1], z = x[2];
+    int region = 0;
     for (int k = 0; k < S.nsurface; ++k) {
         const float* a = S.surface + 10 * k;
         float v = a[0] * xx * xx + a[1] * y * y + a[2] * z * z + a[3] * xx * y + a[4] * xx * z + a[5] * y * z +
                   a[6] * xx + a[7] * y + a[8] * z + a[9];
-        if (v < 0.0f) { m_id = 1; return; }
+        if (v < 0.0f) {
+            if (2 + k < S.ndetmat) { region = 2 + k; break; }
+            m_id = 1;
+            return;
+        }
     }
     y = P[1] / 2.0f + x[1];
     z = P[2] / 2.0f + x[2];
@@ -545,7 +554,7 @@ __device__ __forceinline__ void crystal_search(const SimDesc& S, const float* P,
     y = y - (float)ly * pcy;
     z = z - (float)lz * pcz;
     if (y > P[10] || z > P[11]) { m_id = 1; return; }
-    m_id = 0;
+    m_id = region;
 }
 
 }  // namespace gpet

@@ -401,9 +401,13 @@ int gpet_load_geometry(gpet_ctx* c, const char* path)
     if (!e.empty()) return fail(c, GPET_ERR_IO, e);
     for (int k = 0; k < 2; ++k)
         if (g.det_mat[k] < 0 || g.det_mat[k] >= c->tab.nmat) return fail(c, GPET_ERR_ARG, "detector material out of range");
+    for (int k = 2; k < g.ndetmat; ++k)
+        if (g.det_mat[k] < 0 || g.det_mat[k] >= c->tab.nmat) return fail(c, GPET_ERR_ARG, "detector material out of range");
     c->geo = std::move(g);
     float dmax[10] = {0};
     for (int k = 0; k < 2; ++k)
+        if (c->geo.det_den[k] > dmax[c->geo.det_mat[k]]) dmax[c->geo.det_mat[k]] = c->geo.det_den[k];
+    for (int k = 2; k < c->geo.ndetmat; ++k)
         if (c->geo.det_den[k] > dmax[c->geo.det_mat[k]]) dmax[c->geo.det_mat[k]] = c->geo.det_den[k];
     float e0, ide;
     build_wck(c->tab, table_idle(c->tab), dmax, c->wck_det, e0, ide);
@@ -533,7 +537,8 @@ static int build_sim(gpet_ctx* c)
     S.vox = c->d_vox.as<uint2>();
     S.npanels = c->geo.npanels;
     S.panels = c->d_panels.as<float>();
-    for (int k = 0; k < 2; ++k) { S.det_mat[k] = c->geo.det_mat[k]; S.det_den[k] = c->geo.det_den[k]; }
+    S.ndetmat = c->geo.ndetmat;
+    for (int k = 0; k < c->geo.ndetmat; ++k) { S.det_mat[k] = c->geo.det_mat[k]; S.det_den[k] = c->geo.det_den[k]; }
     S.moduleN = c->geo.moduleN; S.crystalN = c->geo.crystalN; S.moduleNy = c->geo.moduleNy; S.crystalNy = c->geo.crystalNy;
     const Config& cf = c->cfg;
     S.nsurface = c->have_cfg ? (int)cf.surfaces.size() / 10 : 0;
@@ -1811,7 +1816,8 @@ int ctx_geometry(const gpet_ctx* c, SurGeom* g)
     g->crystalNy = c->geo.crystalNy;
     g->rdepth = c->have_cfg ? c->cfg.rdepth : 2;
     g->rpolicy = c->have_cfg ? c->cfg.rpolicy : 1;
-    for (int k = 0; k < 2; ++k) { g->det_mat[k] = c->geo.det_mat[k]; g->det_den[k] = c->geo.det_den[k]; }
+    g->ndetmat = c->geo.ndetmat;
+    for (int k = 0; k < c->geo.ndetmat; ++k) { g->det_mat[k] = c->geo.det_mat[k]; g->det_den[k] = c->geo.det_den[k]; }
     return GPET_OK;
 }
 

@@ -259,10 +259,22 @@ std::string read_geometry(const std::string& path, Geometry& g)
     if (g.npanels < 1 || g.npanels > kMaxPanelsHost) return path + ": 1..256 panels supported";
     r.header(); v = r.values(3); for (int k = 0; k < 3; ++k) g.axis[k] = f32(v[k]);
     r.header(); v = r.values(1); g.angle = f32(v[0]);
-    r.header(); v = r.values(4);
-    if (!r.err.empty()) return path + ": " + r.err;
-    g.det_mat[0] = i32(v[0]); g.det_den[0] = f32(v[1]);
-    g.det_mat[1] = i32(v[2]); g.det_den[1] = f32(v[3]);
+    // (material, density) pairs up to the separator line: two in the
+    // reference's files, more for crystal regions marked by the surfaces
+    r.header();
+    v.clear();
+    while (r.i < r.lines.size()) {
+        auto t = tokens(r.lines[r.i]);
+        if (t.empty()) { ++r.i; continue; }
+        char* end = nullptr;
+        std::strtod(t[0].c_str(), &end);
+        if (end == t[0].c_str() || *end) break;   // not a number: the separator
+        v.insert(v.end(), t.begin(), t.end());
+        ++r.i;
+    }
+    if (v.size() < 4 || v.size() % 2 || v.size() / 2 > 8) return path + ": 2 to 8 (material, density) pairs expected";
+    g.ndetmat = (int)(v.size() / 2);
+    for (int k = 0; k < g.ndetmat; ++k) { g.det_mat[k] = i32(v[2 * k]); g.det_den[k] = f32(v[2 * k + 1]); }
     r.header();                                  // separator line
     float P[32] = {0};
     r.header(); v = r.values(1); P[30] = (float)i32(v[0]);

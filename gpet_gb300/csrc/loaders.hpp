@@ -54,8 +54,12 @@ struct Geometry {                    // detector.cu:64-285
     int npanels = 0;
     float axis[3] = {0, 0, 1};
     float angle = 0;
-    int det_mat[2] = {0, 0};
-    float det_den[2] = {0, 0};
+    // detector materials: 0 crystal, 1 gap (the reference's two,
+    // detector.cu:110-118), 2.. crystal materials of the regions that the
+    // quadratic surfaces 0.. mark (more (material, density) pairs in the file)
+    int ndetmat = 2;
+    int det_mat[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    float det_den[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     std::vector<float> panels;       // [npanels][32]
     int moduleNy = 0, moduleN = 0, crystalNy = 0, crystalN = 0;
 };

@@ -1070,7 +1070,8 @@ int surrogate_view(const gpet_surrogate* s, const SurGeom& g, SurrogateDev* out,
                 h.crystalNy == g.crystalNy && h.rdepth == g.rdepth && h.rpolicy == g.rpolicy &&
                 h.dirsign == g.dirsign;
     for (int k = 0; k < 15 && same; ++k) same = h.panel0[k] == g.panel0[k];
-    for (int k = 0; k < 2 && same; ++k) same = h.det_mat[k] == g.det_mat[k] && h.det_den[k] == g.det_den[k];
+    same = same && h.ndetmat == g.ndetmat;
+    for (int k = 0; k < h.ndetmat && same; ++k) same = h.det_mat[k] == g.det_mat[k] && h.det_den[k] == g.det_den[k];
     if (!same) {
         *why = "the surrogate was made for another detector (geometry, materials or readout)";
         return GPET_ERR_ARG;

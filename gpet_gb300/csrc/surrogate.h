@@ -17,8 +17,9 @@ struct SurGeom {
     float dirsign;                // local x of a panel grows outward (-1) or inward (+1)
     int32_t moduleN, crystalN, crystalNy;
     int32_t rdepth, rpolicy;
-    int32_t det_mat[2];
-    float det_den[2];
+    int32_t ndetmat;
+    int32_t det_mat[8];
+    float det_den[8];
 };
 
 // device view of a surrogate for the routing and inference kernels

@@ -559,7 +559,7 @@ __global__ void __launch_bounds__(256) k_detector(const SimDesc* sims, QueueDev 
                     kn_sample(L.E, st, efrac, cost);
                     float de = L.E * (1.0f - efrac);
                     float phi = st_u(st);
-                    if (m_id == 0) {
+                    if (m_id != 1) {   // a crystal (not the gap)
                         PEvent e;
                         e.pann = pann; e.modn = M_id; e.cryn = L_id;
                         e.siten = pann * S.moduleN * S.crystalN + M_id * S.crystalN + L_id;
@@ -593,7 +593,7 @@ __global__ void __launch_bounds__(256) k_detector(const SimDesc* sims, QueueDev 
                     }
                     type = 4; dep = L.E;
                 }
-                if (m_id == 0) {
+                if (m_id != 1) {   // a crystal (not the gap)
                     PEvent e;
                     e.pann = pann; e.modn = M_id; e.cryn = L_id;
                     e.siten = pann * S.moduleN * S.crystalN + M_id * S.crystalN + L_id;

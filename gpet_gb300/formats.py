@@ -213,9 +213,24 @@ def read_geo(path):
     r.header(); axis = tuple(f32(v) for v in r.values(3))
     r.header(); ang = f32(r.values(1)[0])
     r.header()
-    v = r.values(4)
-    det_mat = (int(v[0]), int(v[2]))
-    det_den = (f32(v[1]), f32(v[3]))
+    # (material, density) pairs up to the separator: the reference's two,
+    # more for crystal regions marked by the quadratic surfaces
+    v = []
+    while r.i < len(r.lines):
+        t = r.lines[r.i].split()
+        if not t:
+            r.i += 1
+            continue
+        try:
+            float(t[0])
+        except ValueError:
+            break
+        v += t
+        r.i += 1
+    if len(v) < 4 or len(v) % 2 or len(v) // 2 > 8:
+        raise ValueError("%s: 2 to 8 (material, density) pairs expected" % path)
+    det_mat = tuple(int(v[2 * k]) for k in range(len(v) // 2))
+    det_den = tuple(f32(v[2 * k + 1]) for k in range(len(v) // 2))
     r.header()                      # separator line
     r.header(); pane = int(r.values(1)[0])
     vals = {}
@@ -253,7 +268,7 @@ def write_geo(path, npanels, axis, angle_deg, det_mat, det_den, panel0):
         "panel rotational axis in the global coordinate", v3(axis),
         "panel rotational angle (in degree, plus: counterclockwise, minus: clockwise)", repr(float(angle_deg)),
         "material density (in the order of crystal material, air)",
-        "%d %s" % (det_mat[0], repr(float(det_den[0]))), "%d %s" % (det_mat[1], repr(float(det_den[1]))),
+    ] + ["%d %s" % (m, repr(float(d))) for m, d in zip(det_mat, det_den)] + [
         "%" * 49,
         "starting panel index", str(panel0.get("start", 0)),
         "dimension(cm)", v3(panel0["len"]),

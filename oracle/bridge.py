@@ -79,6 +79,7 @@ class _Scene(C.Structure):
         ("seed", C.c_uint64), ("sim_id", C.c_uint32),
         ("noise_lambda_us", C.c_float), ("noise_emean", C.c_float), ("noise_sigma", C.c_float),
         ("noise_interval_us", C.c_double), ("noise_t0_us", C.c_double), ("noise_t1_us", C.c_double),
+        ("nxdet", C.c_int32), ("xdet_mat", C.c_int32 * 6), ("xdet_den", C.c_float * 6),
     ]
 
 
@@ -189,8 +190,12 @@ class OracleScene:
         s.offx, s.offy, s.offz = cfg.poffset
         s.mat = self.mat.ctypes.data_as(_IP); s.den = self.den.ctypes.data_as(_FP)
         s.npanels = geo.npanels; s.panels = self.panels.ctypes.data_as(_FP)
-        s.det_mat[0], s.det_mat[1] = geo.det_mat
-        s.det_den[0], s.det_den[1] = geo.det_den
+        s.det_mat[0], s.det_mat[1] = geo.det_mat[:2]
+        s.det_den[0], s.det_den[1] = geo.det_den[:2]
+        s.nxdet = len(geo.det_mat) - 2
+        for k in range(s.nxdet):
+            s.xdet_mat[k] = geo.det_mat[2 + k]
+            s.xdet_den[k] = geo.det_den[2 + k]
         mny, mn, cny, cn = F.panel_counts(self.panels[0])
         s.moduleN, s.crystalN, s.moduleNy, s.crystalNy = mn, cn, mny, cny
         s.nsurface = len(cfg.surfaces)

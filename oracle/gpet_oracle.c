@@ -502,16 +502,23 @@ static int enter_panel(const or_scene* sc, const photon_t* p, local_t* q)
     return 0;
 }
 
-/* crystalSearch, gPET_kernals.cu:1236-1279: m_id 0 crystal, 1 gap */
+/* crystalSearch, gPET_kernals.cu:1236-1279: m_id 0 crystal, 1 gap; inside
+ * quadratic surface k: gap (the reference), or crystal of the extra material
+ * 2 + k when the detector lists one */
 static void crystal_search(const or_scene* sc, const float* P, const real x[3], int* m_id, int* M_id, int* L_id)
 {
     real xx = x[0], y = x[1], z = x[2];
+    int region = 0;
     for (int k = 0; k < sc->nsurface; ++k) {
         const float* a = sc->surface + 10 * k;
         real v = (real)a[0] * xx * xx + (real)a[1] * y * y + (real)a[2] * z * z + (real)a[3] * xx * y +
                  (real)a[4] * xx * z + (real)a[5] * y * z + (real)a[6] * xx + (real)a[7] * y + (real)a[8] * z +
                  (real)a[9];
-        if (v < (real)0.0) { *m_id = 1; return; }
+        if (v < (real)0.0) {
+            if (k < sc->nxdet) { region = 2 + k; break; }
+            *m_id = 1;
+            return;
+        }
     }
     y = (real)P[1] / (real)2.0 + x[1];
     z = (real)P[2] / (real)2.0 + x[2];
@@ -529,7 +536,7 @@ static void crystal_search(const or_scene* sc, const float* P, const real x[3], 
     y = y - (real)ly * pcy;
     z = z - (real)lz * pcz;
     if (y > (real)P[10] || z > (real)P[11]) { *m_id = 1; return; }
-    *m_id = 0;
+    *m_id = region;
 }
 
 /* comsam (free electron Klein-Nishina), gPET_kernals.cu:90-126 */
@@ -662,8 +669,8 @@ static void detector_transport(const or_scene* sc, const wck_t* wck, local_t* q,
             break;
         int m_id = -1, M_id = -1, L_id = -1;
         crystal_search(sc, P, q->x, &m_id, &M_id, &L_id);
-        real den = (real)sc->det_den[m_id];
-        int mat = sc->det_mat[m_id];
+        real den = (real)(m_id < 2 ? sc->det_den[m_id] : sc->xdet_den[m_id - 2]);
+        int mat = m_id < 2 ? sc->det_mat[m_id] : sc->xdet_mat[m_id - 2];
         real lamden = lammin * den;
         real prob = (real)1.0 - lamden * xs_at(sc, sc->lamph, mat, q->E);
         if (prob < (real)0.0) prob = (real)0.0;
@@ -678,7 +685,7 @@ static void detector_transport(const or_scene* sc, const wck_t* wck, local_t* q,
             kn_sample(q->E, st, &efrac, &cost);
             real de = q->E * ((real)1.0 - efrac);
             real phi = st_u(st);
-            if (m_id == 0) {
+            if (m_id != 1) {   /* a crystal (not the gap) */
                 or_event e;
                 e.parn = parn; e.cryn = L_id; e.modn = M_id; e.pann = pann;
                 e.siten = pann * sc->moduleN * sc->crystalN + M_id * sc->crystalN + L_id;
@@ -710,7 +717,7 @@ static void detector_transport(const or_scene* sc, const wck_t* wck, local_t* q,
             type = 4; dep = q->E; stop = 1;
         }
         if (stop) {
-            if (m_id == 0) {
+            if (m_id != 1) {   /* a crystal (not the gap) */
                 or_event e;
                 e.parn = parn; e.cryn = L_id; e.modn = M_id; e.pann = pann;
                 e.siten = pann * sc->moduleN * sc->crystalN + M_id * sc->crystalN + L_id;
@@ -1123,6 +1130,8 @@ static int prepare(const or_scene* sc, prep_t* pp)
     float dmax[10] = {0};
     for (int i = 0; i < 2; ++i)
         if (sc->det_den[i] > dmax[sc->det_mat[i]]) dmax[sc->det_mat[i]] = sc->det_den[i];
+    for (int i = 0; i < sc->nxdet; ++i)
+        if (sc->xdet_den[i] > dmax[sc->xdet_mat[i]]) dmax[sc->xdet_mat[i]] = sc->xdet_den[i];
     build_wck(sc, dmax, &pp->wdet);
     if (sc->nsrc > 64) return -3;
     for (int i = 0; i < sc->nsrc; ++i) {

@@ -87,6 +87,11 @@ typedef struct {
      * the intervals each drawn from its own stream, and the window (us) */
     float noise_lambda_us, noise_emean, noise_sigma;
     double noise_interval_us, noise_t0_us, noise_t1_us;
+    /* detector materials beyond the reference's two: crystal regions marked
+     * by quadratic surface k are material xdet_mat[k] at xdet_den[k] */
+    int32_t nxdet;
+    int32_t xdet_mat[6];
+    float xdet_den[6];
 } or_scene;
 
 typedef struct {

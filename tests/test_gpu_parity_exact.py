@@ -187,3 +187,43 @@ def test_run_with_background_singles_bit_exact(scene_small, data_dir, gpet_lib, 
     # adder.dat content: the transport's pulses only
     gp, _, _ = ctx.pulses()
     assert (gp["parn"] >= 0).all() and len(gp) == r["n_pulses"]
+
+
+def test_multi_material_detector_bit_exact(scene_small, data_dir, gpet_lib, oracle_mod, tmp_path):
+    """A third detector material: the back half of every crystal (depth
+    beyond 0.5 cm, marked by the plane x + 0.5 < 0 in panel coordinates) is
+    LSO (material 9, 7.4 g/cm3) instead of LYSO; both materials collect
+    deposits. Histories, hits, pulses and singles bit for bit against the
+    oracle."""
+    from gpet_gb300 import formats as F
+    from gpet_gb300.scenes import Scene, ring_panel0, MAT_LYSO, MAT_AIR
+    geo = str(tmp_path / "ring3.geo")
+    F.write_geo(geo, 8, (0, 0, 1), 45.0, (MAT_LYSO, MAT_AIR, 9), (7.1, 0.001025, 7.4),
+                ring_panel0(4.0, 8, 8, 0.15, 0.001, 1.0))
+    g = F.read_geo(geo)
+    assert g.det_mat == (MAT_LYSO, MAT_AIR, 9)
+    cfg = F.read_config(scene_small.config_path)
+    cfg.geofile = geo
+    cfg.surfaces = [[0, 0, 0, 0, 0, 0, 1, 0, 0, 0.5]]
+    path = str(tmp_path / "input_PET.in")
+    F.write_config(path, cfg)
+    scene = Scene(scene_small.directory, path, dict(scene_small.options), "three materials")
+    ctx, st, r = _run_both(scene, data_dir)
+    gx, ox = ctx.exits(), r["exits"]
+    assert _first_diff(gx, ox, ["status", "panel", "nscat", "E", "x", "y", "z", "t"]) is None
+    gp, _, _ = ctx.pulses()
+    assert np.array_equal(gp.view(np.uint8), r["pulses"].view(np.uint8))
+    gs, _ = ctx.singles()
+    assert np.array_equal(gs.view(np.uint8), r["singles"].view(np.uint8))
+    gid, gf = ctx.hits()
+    back = gf[:, 2] < -0.5
+    assert back.any() and (~back).any()        # deposits in both materials
+    # the same surface without a third material is an exclusion zone instead
+    cfg2 = F.read_config(scene_small.config_path)
+    cfg2.surfaces = cfg.surfaces
+    p2 = str(tmp_path / "input2.in")
+    F.write_config(p2, cfg2)
+    ctx2 = make_ctx(Scene(scene_small.directory, p2, dict(scene_small.options), "excluded"), data_dir)
+    ctx2.run()
+    _, gf2 = ctx2.hits()
+    assert (gf2[:, 2] >= -0.5 - 1e-6).all()
