@@ -200,23 +200,24 @@ DM_FN double dm_log(double x)
     return dm_fmad((double)e, 0.69314718055994531, s * p);
 }
 
-/* log(1 + x) for |x| <= 2^-6 by its Taylor series (terms to x^12), no
- * division: used for the decay-time sampling of long-lived isotopes */
+/* log(1 + x) for |x| <= 2^-6 by its Taylor series x (1 - x/2 + ... - x^9/10)
+ * (truncation below 2^-57 relative), no division: used for the decay-time
+ * sampling of long-lived isotopes. Estrin's scheme: dependency depth 6
+ * instead of 10 (FP64 latency is long on this GPU) */
 DM_FN double dm_log1p_small(double x)
 {
-    double p = -1.0 / 12.0;
-    p = dm_fmad(x, p, 1.0 / 11.0);
-    p = dm_fmad(x, p, -1.0 / 10.0);
-    p = dm_fmad(x, p, 1.0 / 9.0);
-    p = dm_fmad(x, p, -1.0 / 8.0);
-    p = dm_fmad(x, p, 1.0 / 7.0);
-    p = dm_fmad(x, p, -1.0 / 6.0);
-    p = dm_fmad(x, p, 1.0 / 5.0);
-    p = dm_fmad(x, p, -1.0 / 4.0);
-    p = dm_fmad(x, p, 1.0 / 3.0);
-    p = dm_fmad(x, p, -0.5);
-    p = dm_fmad(x, p, 1.0);
-    return x * p;
+    const double x2 = x * x;
+    const double x4 = x2 * x2;
+    const double x8 = x4 * x4;
+    const double p01 = dm_fmad(x, -0.5, 1.0);
+    const double p23 = dm_fmad(x, -1.0 / 4.0, 1.0 / 3.0);
+    const double p45 = dm_fmad(x, -1.0 / 6.0, 1.0 / 5.0);
+    const double p67 = dm_fmad(x, -1.0 / 8.0, 1.0 / 7.0);
+    const double p89 = dm_fmad(x, -1.0 / 10.0, 1.0 / 9.0);
+    const double p03 = dm_fmad(x2, p23, p01);
+    const double p47 = dm_fmad(x2, p67, p45);
+    const double p07 = dm_fmad(x4, p47, p03);
+    return x * dm_fmad(x8, p89, p07);
 }
 
 /* time per unit path, us/cm (1 / 29979.2458), for single-precision flight
@@ -229,11 +230,23 @@ DM_FN float dm_u01(uint32_t x)
     return ((float)(x >> 8) + 0.5f) * 5.9604644775390625e-08f;
 }
 
-/* uniform (0,1) double from 53 random bits */
+/* uniform (0,1) double from 52 random bits: (k + 1/2) 2^-52, made as
+ * (1 + k 2^-52) - (1 - 2^-53), one exact subtraction */
 DM_FN double dm_u01d(uint32_t hi, uint32_t lo)
 {
-    uint64_t k = ((uint64_t)(hi >> 5) << 26) | (uint64_t)(lo >> 6);
-    return ((double)k + 0.5) * 1.1102230246251565e-16;
+    const uint64_t k = ((uint64_t)(hi & 0xFFFFFu) << 32) | (uint64_t)lo;
+    return dm_u2d(0x3FF0000000000000ull | k) - dm_u2d(0x3FEFFFFFFFFFFFFFull);
+}
+
+/* two independent standard normals from two uniforms (Box-Muller, both
+ * branches) */
+DM_FN void dm_normal2(float u1, float u2, float* n1, float* n2)
+{
+    float s, c;
+    dm_sincos_turns(u2, &s, &c);
+    const float R = dm_sqrt(-2.0f * dm_logf(u1));
+    *n1 = R * c;
+    *n2 = R * s;
 }
 
 /* standard normal from two uniforms (Box-Muller, cosine branch) */

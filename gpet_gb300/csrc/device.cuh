@@ -62,10 +62,10 @@ struct SimDesc {
     int64_t src_end[kMaxSrc];     // exclusive end of each source's decay range
     int32_t src_type[kMaxSrc], src_shape[kMaxSrc];
     float src_coef[kMaxSrc][6];
-    double src_tau[kMaxSrc], src_cfac[kMaxSrc];
+    double src_ntau_us[kMaxSrc], src_cfac[kMaxSrc];   // -lifetime (us), 1 - exp(-window / lifetime)
     float iso_ratio[kMaxSrc];     // indexed by source (ratio of its isotope)
     float iso_coef[kMaxSrc][8];   // indexed by source
-    double tstart_s;
+    double tstart_us;
     int32_t useprange;
     float noncol_sigma, eabsph;
     int64_t npsf;
@@ -136,6 +136,13 @@ __device__ __forceinline__ float st_normal(Stream& s)
     float u1 = st_u(s);
     float u2 = st_u(s);
     return dm_normal(u1, u2);
+}
+
+__device__ __forceinline__ void st_normal2(Stream& s, float& n1, float& n2)
+{
+    float u1 = st_u(s);
+    float u2 = st_u(s);
+    dm_normal2(u1, u2, &n1, &n2);
 }
 
 // ---------------------------------------------------------------- lookups
@@ -304,14 +311,22 @@ inline __device__ void positron_range(const SimDesc& S, float x[3], float ek, co
     float rex = 0.1f * b1 * ekin * ekin / (b2 + ekin);
     float sigma = rex / 2.0f;
     float d[3];
-    d[0] = sigma * st_normal(st);
-    d[1] = sigma * st_normal(st);
-    d[2] = sigma * st_normal(st);
+    {
+        float n1, n2;
+        st_normal2(st, n1, n2);
+        d[0] = sigma * n1;
+        d[1] = sigma * n2;
+        d[2] = sigma * st_normal(st);
+    }
     float r = dm_sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     if (dir) {
         float tmp = dm_sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
         d[0] = r * dir[0] / tmp; d[1] = r * dir[1] / tmp; d[2] = r * dir[2] / tmp;
     }
+    // reciprocals once: the voxel walk multiplies instead of dividing
+    const float id0 = 1.0f / d[0], id1 = 1.0f / d[1], id2 = 1.0f / d[2];
+    const float ir = 1.0f / r;
+    const float dn0 = d[0] * ir, dn1 = d[1] * ir, dn2 = d[2] * ir;
     int vx = 0, vy = 0, vz = 0;
     bool inside = abs_vox(S, x[0], x[1], x[2], vx, vy, vz);
     if (!inside) { vx = vy = vz = 0; }
@@ -323,11 +338,11 @@ inline __device__ void positron_range(const SimDesc& S, float x[3], float ek, co
         step = 1000.0f;
         if (inside) {
             int ax = 0;
-            float bb = (S.offx + (float)(vx + (d[0] > 0.0f)) * S.dx - x[0]) / d[0];
+            float bb = (S.offx + (float)(vx + (d[0] > 0.0f)) * S.dx - x[0]) * id0;
             if (step > bb) { step = bb; ax = 1; }
-            bb = (S.offy + (float)(vy + (d[1] > 0.0f)) * S.dy - x[1]) / d[1];
+            bb = (S.offy + (float)(vy + (d[1] > 0.0f)) * S.dy - x[1]) * id1;
             if (step > bb) { step = bb; ax = 2; }
-            bb = (S.offz + (float)(vz + (d[2] > 0.0f)) * S.dz - x[2]) / d[2];
+            bb = (S.offz + (float)(vz + (d[2] > 0.0f)) * S.dz - x[2]) * id2;
             if (step > bb) { step = bb; ax = 3; }
             if (ax == 1) vx += d[0] > 0.0f ? 1 : -1;
             else if (ax == 2) vy += d[1] > 0.0f ? 1 : -1;
@@ -340,9 +355,9 @@ inline __device__ void positron_range(const SimDesc& S, float x[3], float ek, co
             step = (r - s) / 0.0012905f;
             s = r + 100.0f;
         }
-        x[0] += step * d[0] / r;
-        x[1] += step * d[1] / r;
-        x[2] += step * d[2] / r;
+        x[0] += step * dn0;
+        x[1] += step * dn1;
+        x[2] += step * dn2;
         if (x[0] < S.offx || x[0] > xmax) inside = false;
         if (x[1] < S.offy || x[1] > ymax) inside = false;
         if (x[2] < S.offz || x[2] > zmax) inside = false;

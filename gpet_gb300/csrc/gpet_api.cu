@@ -568,12 +568,12 @@ static int build_sim(gpet_ctx* c)
             for (int k = 0; k < 6; ++k) S.src_coef[i][k] = c->src.coef[6 * i + k];
             double th = (double)c->tab.iso_halftime[ty];
             double tau = th / 0.69314718055994530942;
-            S.src_tau[i] = tau;
+            S.src_ntau_us[i] = -tau * 1e6;
             S.src_cfac[i] = -std::expm1(-dt / tau);
             S.iso_ratio[i] = c->tab.iso_ratio[ty];
             for (int k = 0; k < 8; ++k) S.iso_coef[i][k] = c->tab.iso_coef[8 * ty + k];
         }
-        S.tstart_s = (double)c->tstart;
+        S.tstart_us = (double)c->tstart * 1e6;
     }
     if (cudaSuccess != c->d_sim.ensure(sizeof(SimDesc))) return fail(c, GPET_ERR_CUDA, "sim upload");
     cudaMemcpyAsync(c->d_sim.p, &S, sizeof(SimDesc), cudaMemcpyHostToDevice, c->stream);

@@ -98,8 +98,9 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2])
     double ud = st_ud(st);
     const double cf = S.src_cfac[si];
     const double xl = -ud * cf;
-    double tdec = -S.src_tau[si] * (cf <= 0.015625 ? dm_log1p_small(xl) : dm_log(1.0 + xl));
-    double t_us = (S.tstart_s + tdec) * 1e6;
+    // t = tstart - lifetime log(1 - u (1 - exp(-window / lifetime))), in us
+    const double L = cf <= 0.015625 ? dm_log1p_small(xl) : dm_log(1.0 + xl);
+    double t_us = dm_fmad(S.src_ntau_us[si], L, S.tstart_us);
     float br = st_u(st);
     if (!(br < S.iso_ratio[si])) return 0;
     float pos[3];

@@ -106,6 +106,20 @@ static inline double st_ud(stream_t* s)
 }
 
 /* normal deviate: Box-Muller, two uniforms (replaces curand_normal) */
+static inline void st_normal2(stream_t* s, real* n1, real* n2)
+{
+    real u1 = st_u(s), u2 = st_u(s);
+#ifdef ORACLE_FP32
+    dm_normal2(u1, u2, n1, n2);
+#else
+    real sn, cs;
+    r_sincos_turns(u2, &sn, &cs);
+    real R = R_SQRT((real)-2.0 * R_LOG(u1));
+    *n1 = R * cs;
+    *n2 = R * sn;
+#endif
+}
+
 static inline real st_normal(stream_t* s)
 {
     real u1 = st_u(s), u2 = st_u(s);
@@ -330,14 +344,22 @@ static void positron_range(const or_scene* sc, real x[3], real ek, const real* d
     real rex = (real)0.1 * b1 * ekin * ekin / (b2 + ekin);
     real sigma = rex / (real)2.0;
     real d[3];
-    d[0] = sigma * st_normal(st);
-    d[1] = sigma * st_normal(st);
-    d[2] = sigma * st_normal(st);
+    {
+        real n1, n2;
+        st_normal2(st, &n1, &n2);
+        d[0] = sigma * n1;
+        d[1] = sigma * n2;
+        d[2] = sigma * st_normal(st);
+    }
     real r = R_SQRT(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     if (dir) {
         real tmp = R_SQRT(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
         d[0] = r * dir[0] / tmp; d[1] = r * dir[1] / tmp; d[2] = r * dir[2] / tmp;
     }
+    /* the walk multiplies by reciprocals computed once */
+    const real id0 = (real)1.0 / d[0], id1 = (real)1.0 / d[1], id2 = (real)1.0 / d[2];
+    const real ir = (real)1.0 / r;
+    const real dn0 = d[0] * ir, dn1 = d[1] * ir, dn2 = d[2] * ir;
     real idx = (real)1.0 / (real)sc->dx, idy = (real)1.0 / (real)sc->dy, idz = (real)1.0 / (real)sc->dz;
     int vx = 0, vy = 0, vz = 0;
     int inside = abs_vox(sc, (real)(1.0f / sc->dx), (real)(1.0f / sc->dy), (real)(1.0f / sc->dz),
@@ -356,11 +378,11 @@ static void positron_range(const or_scene* sc, real x[3], real ek, const real* d
         step = (real)1000.0;
         if (inside) {
             int ax = 0;
-            real bb = ((real)sc->offx + (real)(vx + (d[0] > (real)0.0)) * (real)sc->dx - x[0]) / d[0];
+            real bb = ((real)sc->offx + (real)(vx + (d[0] > (real)0.0)) * (real)sc->dx - x[0]) * id0;
             if (step > bb) { step = bb; ax = 1; }
-            bb = ((real)sc->offy + (real)(vy + (d[1] > (real)0.0)) * (real)sc->dy - x[1]) / d[1];
+            bb = ((real)sc->offy + (real)(vy + (d[1] > (real)0.0)) * (real)sc->dy - x[1]) * id1;
             if (step > bb) { step = bb; ax = 2; }
-            bb = ((real)sc->offz + (real)(vz + (d[2] > (real)0.0)) * (real)sc->dz - x[2]) / d[2];
+            bb = ((real)sc->offz + (real)(vz + (d[2] > (real)0.0)) * (real)sc->dz - x[2]) * id2;
             if (step > bb) { step = bb; ax = 3; }
             if (ax == 1) vx += d[0] > (real)0.0 ? 1 : -1;
             else if (ax == 2) vy += d[1] > (real)0.0 ? 1 : -1;
@@ -373,9 +395,9 @@ static void positron_range(const or_scene* sc, real x[3], real ek, const real* d
             step = (r - s) / (real)0.0012905;
             s = r + (real)100.0;
         }
-        x[0] += step * d[0] / r;
-        x[1] += step * d[1] / r;
-        x[2] += step * d[2] / r;
+        x[0] += step * dn0;
+        x[1] += step * dn1;
+        x[2] += step * dn2;
         if (x[0] < (real)sc->offx || x[0] > xmax) inside = 0;
         if (x[1] < (real)sc->offy || x[1] > ymax) inside = 0;
         if (x[2] < (real)sc->offz || x[2] > zmax) inside = 0;
@@ -746,7 +768,7 @@ static void detector_transport(const or_scene* sc, const wck_t* wck, local_t* q,
 /* --------------------------------------------------------- one decay */
 typedef struct {
     wck_t wph, wdet;
-    double tau[64], cfac[64];       /* per source: 1/lambda (s), 1 - exp(-dt/tau) */
+    double ntau_us[64], cfac[64];   /* per source: -lifetime (us), 1 - exp(-dt/lifetime) */
 } prep_t;
 
 static void make_pair(const or_scene* sc, stream_t* st, const real pos[3], photon_t ph[2], double t_us)
@@ -875,12 +897,13 @@ static void simulate_decay(const or_scene* sc, const prep_t* pp, int64_t d, or_e
      * setPosition, gPET_kernals.cu:519-521, conditioned on decaying) */
     double ud = st_ud(&st);
     const double xl = -ud * pp->cfac[si];
+    /* t = tstart - lifetime log(1 - u (1 - exp(-window / lifetime))), in us */
 #ifdef ORACLE_FP32
-    double tdec = -pp->tau[si] * (pp->cfac[si] <= 0.015625 ? dm_log1p_small(xl) : dm_log(1.0 + xl));
+    const double L = pp->cfac[si] <= 0.015625 ? dm_log1p_small(xl) : dm_log(1.0 + xl);
 #else
-    double tdec = -pp->tau[si] * log1p(xl);
+    const double L = log1p(xl);
 #endif
-    double t_us = (sc->tstart_s + tdec) * 1e6;
+    double t_us = dm_fmad(pp->ntau_us[si], L, sc->tstart_s * 1e6);
     real br = st_u(&st);
     if (br < (real)sc->iso_ratio[type]) {
         real pos[3];
@@ -1137,7 +1160,7 @@ static int prepare(const or_scene* sc, prep_t* pp)
     for (int i = 0; i < sc->nsrc; ++i) {
         double th = (double)sc->iso_halftime[sc->src_type[i]];
         double tau = th / 0.69314718055994530942;
-        pp->tau[i] = tau;
+        pp->ntau_us[i] = -tau * 1e6;
         pp->cfac[i] = -expm1(-sc->dt_s / tau);
     }
     return 0;
@@ -1316,4 +1339,17 @@ void oracle_detmath(int which, int64_t n, const float* x, float* y)
 void oracle_detmath_log(int64_t n, const double* x, double* y)
 {
     for (int64_t i = 0; i < n; ++i) y[i] = dm_log(x[i]);
+}
+
+/* which 0: dm_log1p_small, 1: dm_u01d of (hi, lo) given as x = hi * 2^32 + lo */
+void oracle_detmath_d(int which, int64_t n, const double* x, double* y)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        if (which == 0) {
+            y[i] = dm_log1p_small(x[i]);
+        } else {
+            const uint64_t v = (uint64_t)x[i];
+            y[i] = dm_u01d((uint32_t)(v >> 32), (uint32_t)v);
+        }
+    }
 }

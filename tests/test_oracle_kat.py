@@ -158,3 +158,20 @@ def test_example_config_parses():
     assert (c.ewin_lo, c.ewin_hi) == (30000.0, 700000.0)
     assert c.surfaces == [[0, 0, 0, 0, 0, 0, 0, 0, 0, 1]]
     assert c.geofile == "input/config8.geo" and c.sourcefile == "input/pointsource.txt"
+
+
+def test_detmath_double_helpers(oracle_mod):
+    """The decay-time series and the 52-bit uniform of detmath.h."""
+    L = oracle_mod.lib("fp32")
+    L.oracle_detmath_d.argtypes = [C.c_int, C.c_int64, C.c_void_p, C.c_void_p]
+    x = -np.linspace(1e-12, 2.0 ** -6, 200001)
+    y = np.zeros_like(x)
+    L.oracle_detmath_d(0, len(x), x.ctypes.data, y.ctypes.data)
+    assert np.max(np.abs(y - np.log1p(x)) / np.abs(np.log1p(x))) < 8 * 2.0 ** -53
+    # (hi, lo) as hi * 2^32 + lo; the top 12 bits of hi are not used
+    hl = np.array([0, 1, 0xFFFFF00000000, 0xFFFFFFFFFFFFF, 0x123456789ABCD, 0x7FF0000000000000], np.float64)
+    u = np.zeros_like(hl)
+    L.oracle_detmath_d(1, len(hl), hl.ctypes.data, u.ctypes.data)
+    k = np.array([0, 1, 0xFFFFF00000000, 0xFFFFFFFFFFFFF, 0x123456789ABCD, 0], np.float64)
+    assert np.array_equal(u, (k + 0.5) * 2.0 ** -52)
+    assert u.min() > 0 and u.max() < 1
