@@ -534,7 +534,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
                     help="time launch shapes on a sample before the warm-up (results do not depend on the shape)")
-    ap.add_argument("--tune-decays", type=int, default=1 << 23)
+    ap.add_argument("--tune-decays", type=int, default=1 << 24)
     ap.add_argument("--set", action="append", default=[], metavar="KEY=VALUE",
                     help="context option for the headline workload (e.g. a fixed launch shape for profiling)")
     ap.add_argument("--e2e-steps", type=int, default=-1,

@@ -72,6 +72,11 @@ struct SimDesc {
     const double* psf;            // [npsf][8]
     int32_t psf_ptype;
     int32_t rdepth, rpolicy;
+    // bound of the panel entry faces for a quick rejection (see
+    // may_reach_panels): faces parallel to the z axis, none closer to it than
+    // sqrt(ring_rin2), all within [ring_zmin, ring_zmax] (padded)
+    int32_t ring_test;
+    float ring_zmin, ring_zmax, ring_rin2;
     int32_t pad_;
 };
 
@@ -503,6 +508,23 @@ struct Local {
 
 // panel search of photonde, gPET_kernals.cu:963-1009 (panels staged in
 // shared memory)
+// False only when the photon's line cannot meet any panel entry face: while
+// it is inside the faces' z range it stays closer to the z axis than every
+// face (its squared distance to the axis is convex along the line, so the
+// two ends of that range bound it). enter_panel would then find nothing; the
+// bounds are padded, so this never changes a result.
+__device__ __forceinline__ bool may_reach_panels(const SimDesc& S, const Photon& p)
+{
+    if (!S.ring_test) return true;
+    const float uz = p.u[2];
+    if (uz == 0.0f) return p.x[2] >= S.ring_zmin && p.x[2] <= S.ring_zmax;
+    const float iu = 1.0f / uz;
+    const float t1 = (S.ring_zmin - p.x[2]) * iu, t2 = (S.ring_zmax - p.x[2]) * iu;
+    const float x1 = p.x[0] + t1 * p.u[0], y1 = p.x[1] + t1 * p.u[1];
+    const float x2 = p.x[0] + t2 * p.u[0], y2 = p.x[1] + t2 * p.u[1];
+    return fmaxf(x1 * x1 + y1 * y1, x2 * x2 + y2 * y2) >= S.ring_rin2;
+}
+
 __device__ __forceinline__ bool enter_panel(const float* __restrict__ P0, int npanels, const Photon& p, Local& q)
 {
     for (int i = 0; i < npanels; ++i) {

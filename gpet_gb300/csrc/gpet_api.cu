@@ -515,6 +515,36 @@ static std::string source_layout(gpet_ctx* c)
     return "";
 }
 
+// the bound of the panel entry faces used by may_reach_panels: every face
+// must be parallel to the z axis; its plane's distance to the axis bounds the
+// face from below, its corners bound its z range; both padded
+static void ring_bound(const Geometry& g, SimDesc& S)
+{
+    S.ring_test = 0;
+    double zmin = 1e30, zmax = -1e30, rin = 1e30;
+    for (int i = 0; i < g.npanels; ++i) {
+        const float* P = &g.panels[(size_t)i * kPanelStride];
+        const double nx = P[21], ny = P[22], nz = P[23];
+        const double nxy = std::sqrt(nx * nx + ny * ny);
+        if (std::fabs(nz) > 1e-6 || !(nxy > 0.5)) return;
+        const double d = std::fabs(nx * P[15] + ny * P[16]) / nxy;
+        rin = std::min(rin, d);
+        for (int sy = -1; sy <= 1; sy += 2)
+            for (int sz = -1; sz <= 1; sz += 2) {
+                const double z = (double)P[17] + sy * 0.5 * P[1] * P[26] + sz * 0.5 * P[2] * P[29];
+                zmin = std::min(zmin, z);
+                zmax = std::max(zmax, z);
+            }
+    }
+    const double pad = 1e-3;
+    const double r = rin * (1.0 - 1e-4) - pad;
+    if (!(r > 0.0) || !(zmax >= zmin)) return;
+    S.ring_zmin = (float)(zmin - pad - 1e-4 * std::fabs(zmin));
+    S.ring_zmax = (float)(zmax + pad + 1e-4 * std::fabs(zmax));
+    S.ring_rin2 = (float)(r * r);
+    S.ring_test = 1;
+}
+
 static int build_sim(gpet_ctx* c)
 {
     SimDesc& S = c->sim;
@@ -547,6 +577,7 @@ static int build_sim(gpet_ctx* c)
     S.eabsph = c->have_cfg ? cf.eabsph : 1000.0f;
     S.useprange = c->have_cfg ? cf.useprange : 0;
     S.rdepth = c->have_cfg ? cf.rdepth : 2;
+    ring_bound(c->geo, S);
     S.rpolicy = c->have_cfg ? cf.rpolicy : 1;
     if (c->use_psf) {
         S.npsf = (int64_t)c->psf.size() / 8;
@@ -1309,7 +1340,7 @@ static int autotune(gpet_ctx* c, int64_t sample, gpet_tuning* out)
     int rc = build_sim(c);
     if (rc) return rc;
     const int64_t total = total_decays(c);
-    if (sample <= 0) sample = std::min<int64_t>(total, 1ll << 23);
+    if (sample <= 0) sample = std::min<int64_t>(total, 1ll << 24);
     sample = std::min(sample, total);
     const Shape start = get_shape(c);
     if (sample < 4096) {
@@ -1339,7 +1370,7 @@ static int autotune(gpet_ctx* c, int64_t sample, gpet_tuning* out)
         set_shape(c, best);
         return GPET_OK;
     };
-    for (int64_t sub : {1ll << 18, 1ll << 19, 1ll << 20, 1ll << 21}) {
+    for (int64_t sub : {1ll << 19, 1ll << 20, 1ll << 21, 1ll << 22, 1ll << 23, 1ll << 24}) {
         if (sub == best.sub || sub > sample) continue;
         Shape t = best; t.sub = sub; t.chunk = std::max(t.chunk, sub);
         if ((rc = consider(t))) break;

@@ -207,6 +207,7 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
     int fcount = 0;   // staged photons of this warp (warp-uniform)
 
     // panel search + queue append for the staged entries [0, k), one per lane
+    // (escaped photons that may reach a panel)
     auto drain = [&](int k) {
         const bool has = lane < k;
         FinRec r;
@@ -221,9 +222,9 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
             ph.E = r.E; ph.t = r.t; ph.tf = r.tf; ph.nscat = r.nscat;
             if (kMulti) {
                 const SimDesc& S = w.sims[r.sim];
-                entered = r.status == 1 && enter_panel(S.panels, S.npanels, ph, L);
+                entered = enter_panel(S.panels, S.npanels, ph, L);
             } else {
-                entered = r.status == 1 && enter_panel(sP, sS.npanels, ph, L);
+                entered = enter_panel(sP, sS.npanels, ph, L);
             }
         }
         const unsigned m = __ballot_sync(0xffffffffu, entered);
@@ -256,7 +257,6 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
             }
         }
         add_by_sim(cnt, r.sim, CF(entered), entered ? 1u : 0u);
-        add_by_sim(cnt, r.sim, CF(ph_steps), has ? (unsigned)r.steps : 0u);
         if (has && exits) {
             ExitRec e;
             e.x = r.x; e.y = r.y; e.z = r.z; e.ux = r.ux; e.uy = r.uy; e.uz = r.uz;
@@ -272,6 +272,7 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
     int64_t p = 0, d = 0;
     int sim = 0;
     int steps = 0;
+    SimTally t_steps;
     Photon ph;
     Stream st;
     for (;;) {
@@ -381,18 +382,38 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
             }
             if (status < 0 && steps >= kMaxSteps) status = 3;
         }
-        // stage finished photons; run the panel search once 32 are waiting
+        // a finished photon that may reach a panel is staged for the panel
+        // search, which runs once 32 are waiting (full warps); the others
+        // (absorbed, step cap, or no panel within reach) are settled here
         const bool fin = status >= 0;
-        const unsigned mf = __ballot_sync(0xffffffffu, fin);
+        bool search = false;
+        if (fin) {
+            const SimDesc& S = kMulti ? w.sims[sim] : sS;
+            search = status == 1 && may_reach_panels(S, ph);
+            t_steps.add(cnt, CF(ph_steps), sim, (unsigned)steps);
+            if (status == 3) atomicAdd(&cnt[sim].stepcap, 1ull);
+            if (!search) {
+                if (exits) {
+                    ExitRec e;
+                    e.x = ph.x[0]; e.y = ph.x[1]; e.z = ph.x[2];
+                    e.ux = ph.u[0]; e.uy = ph.u[1]; e.uz = ph.u[2];
+                    e.E = ph.E; e.nscat = ph.nscat; e.t = ph.t + (double)ph.tf;
+                    e.status = status;
+                    e.panel = -1;
+                    exits[p] = e;
+                }
+                active = false;
+            }
+        }
+        const unsigned mf = __ballot_sync(0xffffffffu, search);
         if (mf) {
-            if (fin) {
+            if (search) {
                 FinRec r;
                 r.x = ph.x[0]; r.y = ph.x[1]; r.z = ph.x[2];
                 r.ux = ph.u[0]; r.uy = ph.u[1]; r.uz = ph.u[2];
                 r.E = ph.E; r.nscat = ph.nscat; r.t = ph.t; r.p = p; r.d = d; r.status = status; r.tf = ph.tf;
                 r.sim = sim; r.steps = steps;
                 fb[fcount + __popc(mf & lt)] = r;
-                if (status == 3) atomicAdd(&cnt[sim].stepcap, 1ull);
                 active = false;
             }
             fcount += __popc(mf);
@@ -413,6 +434,7 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
         }
     }
     if (fcount > 0) drain(fcount);
+    t_steps.flush(cnt, CF(ph_steps));
 }
 
 // ------------------------------------------------------------- detector

@@ -147,7 +147,7 @@ typedef struct {
     int64_t sample_decays;         /* decays each candidate ran */
     double ms_default, ms_tuned;   /* transport device time of the sample, before and after */
 } gpet_tuning;
-/* Time candidate shapes on the first sample_decays (<= 0: min(total, 2^23))
+/* Time candidate shapes on the first sample_decays (<= 0: min(total, 2^24))
  * decays of this context's own workload, coordinate descent over the fields
  * of gpet_tuning, and keep the fastest in the context. Discards the context's
  * previous results. Option autotune=1 runs it on the first gpet_run. */
