@@ -119,7 +119,7 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2])
 // simulation's descriptor; otherwise the one descriptor is staged in shared
 // memory.
 template <bool kMulti>
-__global__ void __launch_bounds__(256) k_source(const Wave* waves, int wi, PairBuf pb, Counters* cnt)
+__global__ void __launch_bounds__(256, 4) k_source(const Wave* waves, int wi, PairBuf pb, Counters* cnt)
 {
     const Wave w = waves[wi];
     __shared__ SimDesc sS;
@@ -500,7 +500,7 @@ __device__ __forceinline__ int readout(const SimDesc& S, PEvent* ev, int n)
 
 // kMulti as for k_source: the queue holds photons of several simulations
 template <bool kMulti>
-__global__ void __launch_bounds__(256) k_detector(const SimDesc* sims, QueueDev q, PulseDev P,
+__global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueDev q, PulseDev P,
                                                   HitDev H, int rec_hits, Counters* cnt, EntryRec* entries)
 {
     __shared__ SimDesc sS;
