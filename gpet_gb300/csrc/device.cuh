@@ -160,7 +160,7 @@ __device__ __forceinline__ float lerp1(const float* __restrict__ tab, int n, flo
     int i = (int)x;
     float f = x - (float)i;
     float a = __ldg(tab + i), b = __ldg(tab + i + 1);
-    return a + f * (b - a);
+    return dm_fma(f, b - a, a);
 }
 
 // all four cross sections of material m at energy e
@@ -175,10 +175,10 @@ __device__ __forceinline__ float4 xs_at(const SimDesc& S, int m, float e)
     float f = x - (float)i;
     float4 a = __ldg(t + i), b = __ldg(t + i + 1);
     float4 r;
-    r.x = a.x + f * (b.x - a.x);
-    r.y = a.y + f * (b.y - a.y);
-    r.z = a.z + f * (b.z - a.z);
-    r.w = a.w + f * (b.w - a.w);
+    r.x = dm_fma(f, b.x - a.x, a.x);
+    r.y = dm_fma(f, b.y - a.y, a.y);
+    r.z = dm_fma(f, b.z - a.z, a.z);
+    r.w = dm_fma(f, b.w - a.w, a.w);
     return r;
 }
 
@@ -196,9 +196,9 @@ __device__ __forceinline__ float lerp2(const float* __restrict__ s, int ncp, int
     const float* r0 = s + (size_t)ic * ne;
     const float* r1 = r0 + ne;
     float a00 = __ldg(r0 + ie), a01 = __ldg(r0 + ie + 1), a10 = __ldg(r1 + ie), a11 = __ldg(r1 + ie + 1);
-    float a = a00 + fe * (a01 - a00);
-    float b = a10 + fe * (a11 - a10);
-    return a + fc * (b - a);
+    float a = dm_fma(fe, a01 - a00, a00);
+    float b = dm_fma(fe, a11 - a10, a10);
+    return dm_fma(fc, b - a, a);
 }
 
 __device__ __forceinline__ float wck_at(const float* __restrict__ tab, float e0, float ide, float e)
@@ -459,10 +459,10 @@ __device__ __forceinline__ int phantom_transport(const SimDesc& S, Photon& p, St
         steps++;
         float lammin = wck_at(S.wck_ph, S.wck_e0, S.wck_ide, p.E);
         float s = -lammin * dm_logf(st_u(st));
-        p.x[0] += s * p.u[0];
-        p.x[1] += s * p.u[1];
-        p.x[2] += s * p.u[2];
-        p.tf += s * DM_INV_SPEED;
+        p.x[0] = dm_fma(s, p.u[0], p.x[0]);
+        p.x[1] = dm_fma(s, p.u[1], p.x[1]);
+        p.x[2] = dm_fma(s, p.u[2], p.x[2]);
+        p.tf = dm_fma(s, DM_INV_SPEED, p.tf);
         int ix, iy, iz;
         if (!abs_vox(S, p.x[0], p.x[1], p.x[2], ix, iy, iz)) return 1;
         uint2 vv = voxel(S, ix, iy, iz);
@@ -470,10 +470,10 @@ __device__ __forceinline__ int phantom_transport(const SimDesc& S, Photon& p, St
         int m = (int)vv.y;
         float lamden = lammin * voxden;
         float4 xs = xs_at(S, m, p.E);
-        float prob = 1.0f - lamden * xs.x;
+        float prob = dm_fma(-lamden, xs.x, 1.0f);
         float rn = st_u(st);
         if (rn < prob) continue;
-        prob += lamden * xs.y;
+        prob = dm_fma(lamden, xs.y, prob);
         if (rn < prob) {
             float efrac, cost;
             compton_surface(S, p.E, m, st, efrac, cost);
@@ -484,7 +484,7 @@ __device__ __forceinline__ int phantom_transport(const SimDesc& S, Photon& p, St
             rotate(p.u[0], p.u[1], p.u[2], cost, phi);
             continue;
         }
-        prob += lamden * xs.z;
+        prob = dm_fma(lamden, xs.z, prob);
         if (rn < prob) {
             float cost = rayleigh_surface(S, p.E, m, st);
             float phi = st_u(st);

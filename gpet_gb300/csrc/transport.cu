@@ -341,10 +341,10 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
             steps++;
             float lammin = wck_at(S.wck_ph, S.wck_e0, S.wck_ide, ph.E);
             float s = -lammin * dm_logf(st_u(st));
-            ph.x[0] += s * ph.u[0];
-            ph.x[1] += s * ph.u[1];
-            ph.x[2] += s * ph.u[2];
-            ph.tf += s * DM_INV_SPEED;
+            ph.x[0] = dm_fma(s, ph.u[0], ph.x[0]);
+            ph.x[1] = dm_fma(s, ph.u[1], ph.x[1]);
+            ph.x[2] = dm_fma(s, ph.u[2], ph.x[2]);
+            ph.tf = dm_fma(s, DM_INV_SPEED, ph.tf);
             int ix, iy, iz;
             if (!abs_vox(S, ph.x[0], ph.x[1], ph.x[2], ix, iy, iz)) {
                 status = 1;
@@ -354,11 +354,11 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
                 int m = (int)vv.y;
                 float lamden = lammin * voxden;
                 float4 xs = xs_at(S, m, ph.E);
-                float prob = 1.0f - lamden * xs.x;
+                float prob = dm_fma(-lamden, xs.x, 1.0f);
                 float rn = st_u(st);
                 if (rn < prob) {
                 } else {
-                    prob += lamden * xs.y;
+                    prob = dm_fma(lamden, xs.y, prob);
                     if (rn < prob) {
                         float efrac, cost;
                         compton_surface(S, ph.E, m, st, efrac, cost);
@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
                         if (ph.E < S.eabsph) status = 1;
                         else rotate(ph.u[0], ph.u[1], ph.u[2], cost, phi);
                     } else {
-                        prob += lamden * xs.z;
+                        prob = dm_fma(lamden, xs.z, prob);
                         if (rn < prob) {
                             float cost = rayleigh_surface(S, ph.E, m, st);
                             float phi = st_u(st);
@@ -557,10 +557,10 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                 nsteps++;
                 float lammin = wck_at(S.wck_det, S.wck_e0, S.wck_ide, L.E);
                 float s = -lammin * dm_logf(st_u(st));
-                L.x[0] += s * L.u[0];
-                L.x[1] += s * L.u[1];
-                L.x[2] += s * L.u[2];
-                L.tf += s * DM_INV_SPEED;
+                L.x[0] = dm_fma(s, L.u[0], L.x[0]);
+                L.x[1] = dm_fma(s, L.u[1], L.x[1]);
+                L.x[2] = dm_fma(s, L.u[2], L.x[2]);
+                L.tf = dm_fma(s, DM_INV_SPEED, L.tf);
                 if (fabsf(L.x[1]) > Pn[1] * 0.5f || fabsf(L.x[2]) > Pn[2] * 0.5f || L.x[0] * Pn[18] < 0.0f ||
                     L.x[0] * Pn[18] > Pn[0])
                     break;
@@ -570,11 +570,11 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                 int mat = S.det_mat[m_id];
                 float lamden = lammin * den;
                 float4 xs = xs_at(S, mat, L.E);
-                float prob = 1.0f - lamden * xs.x;
+                float prob = dm_fma(-lamden, xs.x, 1.0f);
                 if (prob < 0.0f) prob = 0.0f;
                 float rn = st_u(st);
                 if (rn < prob) continue;
-                prob += lamden * xs.y;
+                prob = dm_fma(lamden, xs.y, prob);
                 int type = 0;
                 float dep = 0.0f;
                 if (rn < prob) {
@@ -607,7 +607,7 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                         continue;
                     }
                 } else {
-                    prob += lamden * xs.z;
+                    prob = dm_fma(lamden, xs.z, prob);
                     if (rn < prob) {
                         float cost = rayleigh_surface(S, L.E, mat, st);
                         float phi = st_u(st);

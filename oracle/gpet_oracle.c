@@ -23,6 +23,7 @@ typedef float real;
 #define R_CBRT(x) dm_cbrtf(x)
 #define R_FLOOR(x) floorf(x)
 #define R_FABS(x) fabsf(x)
+#define R_FMA(a, b, c) dm_fma(a, b, c)
 static inline void r_sincos_turns(real u, real* s, real* c) { dm_sincos_turns(u, s, c); }
 #else
 typedef double real;
@@ -32,6 +33,7 @@ typedef double real;
 #define R_CBRT(x) cbrt(x)
 #define R_FLOOR(x) floor(x)
 #define R_FABS(x) fabs(x)
+#define R_FMA(a, b, c) fma(a, b, c)
 static inline void r_sincos_turns(real u, real* s, real* c)
 {
     double a = 6.283185307179586476925 * u;
@@ -48,7 +50,7 @@ static inline void r_sincos_turns(real u, real* s, real* c)
  * stamp once; the FP64 build accumulates in double at every step, as the
  * reference does (gPET_kernals.cu:283, 1025). */
 #ifdef ORACLE_FP32
-#define TIME_STEP(p, s) ((p)->tf += (s) * DM_INV_SPEED)
+#define TIME_STEP(p, s) ((p)->tf = dm_fma((s), DM_INV_SPEED, (p)->tf))
 #else
 #define TIME_STEP(p, s) ((p)->t += (double)(s) / C_SPE)
 #endif
@@ -150,7 +152,7 @@ static inline real lerp1(const float* tab, int n, real x)
     int i = (int)x;
     real f = x - (real)i;
     real a = (real)tab[i], b = (real)tab[i + 1];
-    return a + f * (b - a);
+    return R_FMA(f, b - a, a);
 }
 
 /* bilinear lookup of an inverse-CDF surface [ncp][ne] at (energy index xe,
@@ -166,9 +168,9 @@ static inline real lerp2(const float* s, int ncp, int ne, real xe, real ycp)
     real fe = xe - (real)ie, fc = ycp - (real)ic;
     const float* r0 = s + (size_t)ic * ne;
     const float* r1 = r0 + ne;
-    real a = (real)r0[ie] + fe * ((real)r0[ie + 1] - (real)r0[ie]);
-    real b = (real)r1[ie] + fe * ((real)r1[ie + 1] - (real)r1[ie]);
-    return a + fc * (b - a);
+    real a = R_FMA(fe, (real)r0[ie + 1] - (real)r0[ie], (real)r0[ie]);
+    real b = R_FMA(fe, (real)r1[ie + 1] - (real)r1[ie], (real)r1[ie]);
+    return R_FMA(fc, b - a, a);
 }
 
 static inline real xs_at(const or_scene* sc, const float* tab, int m, real e)
@@ -444,9 +446,9 @@ static int phantom_transport(const or_scene* sc, const wck_t* wck, photon_t* p, 
     for (int step = 0; step < MAX_STEPS; ++step) {
         real lammin = wck_at(wck, p->E);
         real s = -lammin * R_LOG(st_u(st));
-        p->x[0] += s * p->u[0];
-        p->x[1] += s * p->u[1];
-        p->x[2] += s * p->u[2];
+        p->x[0] = R_FMA(s, p->u[0], p->x[0]);
+        p->x[1] = R_FMA(s, p->u[1], p->x[1]);
+        p->x[2] = R_FMA(s, p->u[2], p->x[2]);
         TIME_STEP(p, s);
         int ix, iy, iz;
         if (!abs_vox(sc, idx, idy, idz, p->x[0], p->x[1], p->x[2], &ix, &iy, &iz)) return 1;
@@ -454,10 +456,10 @@ static int phantom_transport(const or_scene* sc, const wck_t* wck, photon_t* p, 
         real voxden = (real)sc->den[v];
         int m = sc->mat[v];
         real lamden = lammin * voxden;
-        real prob = (real)1.0 - lamden * xs_at(sc, sc->lamph, m, p->E);
+        real prob = R_FMA(-lamden, xs_at(sc, sc->lamph, m, p->E), (real)1.0);
         real rn = st_u(st);
         if (rn < prob) continue;
-        prob += lamden * xs_at(sc, sc->compt, m, p->E);
+        prob = R_FMA(lamden, xs_at(sc, sc->compt, m, p->E), prob);
         if (rn < prob) {
             real efrac, cost;
             compton_surface(sc, p->E, m, st, &efrac, &cost);
@@ -468,7 +470,7 @@ static int phantom_transport(const or_scene* sc, const wck_t* wck, photon_t* p, 
             rotate(&p->u[0], &p->u[1], &p->u[2], cost, phi);
             continue;
         }
-        prob += lamden * xs_at(sc, sc->rayle, m, p->E);
+        prob = R_FMA(lamden, xs_at(sc, sc->rayle, m, p->E), prob);
         if (rn < prob) {
             real cost = rayleigh_surface(sc, p->E, m, st);
             real phi = st_u(st);
@@ -682,9 +684,9 @@ static void detector_transport(const or_scene* sc, const wck_t* wck, local_t* q,
     for (step = 0; step < MAX_STEPS; ++step) {
         real lammin = wck_at(wck, q->E);
         real s = -lammin * R_LOG(st_u(st));
-        q->x[0] += s * q->u[0];
-        q->x[1] += s * q->u[1];
-        q->x[2] += s * q->u[2];
+        q->x[0] = R_FMA(s, q->u[0], q->x[0]);
+        q->x[1] = R_FMA(s, q->u[1], q->x[1]);
+        q->x[2] = R_FMA(s, q->u[2], q->x[2]);
         TIME_STEP(q, s);
         if (R_FABS(q->x[1]) > (real)P[1] * (real)0.5 || R_FABS(q->x[2]) > (real)P[2] * (real)0.5 ||
             q->x[0] * (real)P[18] < (real)0.0 || q->x[0] * (real)P[18] > (real)P[0])
@@ -694,11 +696,11 @@ static void detector_transport(const or_scene* sc, const wck_t* wck, local_t* q,
         real den = (real)(m_id < 2 ? sc->det_den[m_id] : sc->xdet_den[m_id - 2]);
         int mat = m_id < 2 ? sc->det_mat[m_id] : sc->xdet_mat[m_id - 2];
         real lamden = lammin * den;
-        real prob = (real)1.0 - lamden * xs_at(sc, sc->lamph, mat, q->E);
+        real prob = R_FMA(-lamden, xs_at(sc, sc->lamph, mat, q->E), (real)1.0);
         if (prob < (real)0.0) prob = (real)0.0;
         real rn = st_u(st);
         if (rn < prob) continue;
-        prob += lamden * xs_at(sc, sc->compt, mat, q->E);
+        prob = R_FMA(lamden, xs_at(sc, sc->compt, mat, q->E), prob);
         int type = 0;
         real dep = (real)0.0;
         int stop = 0;
@@ -729,7 +731,7 @@ static void detector_transport(const or_scene* sc, const wck_t* wck, local_t* q,
                 continue;
             }
         } else {
-            prob += lamden * xs_at(sc, sc->rayle, mat, q->E);
+            prob = R_FMA(lamden, xs_at(sc, sc->rayle, mat, q->E), prob);
             if (rn < prob) {
                 real cost = rayleigh_surface(sc, q->E, mat, st);
                 real phi = st_u(st);
