@@ -41,7 +41,8 @@ struct DevBuf {
 // device work buffers and results of one run; a batch's contexts share the
 // leader's Work and read their own simulation's slice of the results
 struct Work {
-    DevBuf q_f, q_t, q_i;                 // detector queue
+    DevBuf q_f, q_t, q_i;                 // detector queues: two, used by alternate chunks
+    DevBuf qb_f, qb_t, qb_i;
     int64_t q_cap = 0;
     DevBuf q2_f, q2_t, q2_i, sidx;        // with a surrogate: the Monte Carlo part of the queue, the surrogate's list
     DevBuf ent;                           // entry records of one chunk
@@ -64,8 +65,9 @@ struct Work {
     DevBuf d_waves, d_work;               // wave table and photon counters of one chunk
     Wave* h_waves = nullptr;              // pinned staging of the wave table
     size_t h_waves_cap = 0;
-    cudaGraphExec_t gexec = nullptr;      // the chunk's launches, replayed while their arguments stay put
-    std::vector<unsigned char> gkey;
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};   // per queue: the chunk's launches, replayed while
+    std::vector<unsigned char> gkey[2];              // their arguments stay put
+    std::vector<cudaEvent_t> dev;         // per chunk: detector stage start, end, surrogate start, end
     // results
     int nsims = 0;
     int64_t n_pulses = 0, n_hits = 0, n_singles = 0, n_coinc = 0;
@@ -76,7 +78,8 @@ struct Work {
     ~Work()
     {
         for (auto& e : tev) cudaEventDestroy(e);
-        if (gexec) cudaGraphExecDestroy(gexec);
+        for (auto& e : dev) cudaEventDestroy(e);
+        for (auto& g : gexec) if (g) cudaGraphExecDestroy(g);
         if (h_waves) cudaFreeHost(h_waves);
         if (dg.coinc_pairs) cudaFree(dg.coinc_pairs);
         if (dg.coinc_class) cudaFree(dg.coinc_class);
@@ -86,6 +89,8 @@ struct Work {
 struct gpet_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;       // detector stage, overlapping the next chunk's transport
+    cudaEvent_t qev[4] = {};              // per queue: transport done [0, 1], detector done [2, 3]
     std::string err;
     // options
     uint64_t seed = 20261203ull;
@@ -217,6 +222,12 @@ int gpet_create(int device, gpet_ctx** out)
         return GPET_ERR_CUDA;
     }
     for (auto& e : c->ev) cudaEventCreate(&e);
+    for (auto& e : c->qev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return GPET_ERR_CUDA;
+    }
     *out = c;
     return GPET_OK;
 }
@@ -226,9 +237,12 @@ void gpet_destroy(gpet_ctx* c)
     if (!c) return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    cudaStreamSynchronize(c->stream2);
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+    for (auto& e : c->qev) if (e) cudaEventDestroy(e);
     c->work.reset();
     cudaStreamDestroy(c->stream);
+    cudaStreamDestroy(c->stream2);
     delete c;
 }
 
@@ -881,33 +895,35 @@ static cudaError_t enqueue_chunk(const ChunkLaunch& L, cudaStream_t s)
 
 // the chunk's launches: replayed from the cached graph when nothing they
 // depend on changed, captured and instantiated again otherwise
-static int launch_chunk(gpet_ctx* c, Work& W, const ChunkLaunch& L)
+static int launch_chunk(gpet_ctx* c, Work& W, const ChunkLaunch& L, int slot)
 {
     if (!L.graph) {
         CK(enqueue_chunk(L, c->stream));
         return GPET_OK;
     }
     const unsigned char* key = reinterpret_cast<const unsigned char*>(&L);
-    if (!W.gexec || W.gkey.size() != sizeof(L) || std::memcmp(W.gkey.data(), key, sizeof(L)) != 0) {
-        if (W.gexec) {
-            cudaGraphExecDestroy(W.gexec);
-            W.gexec = nullptr;
+    cudaGraphExec_t& gexec = W.gexec[slot];
+    std::vector<unsigned char>& gkey = W.gkey[slot];
+    if (!gexec || gkey.size() != sizeof(L) || std::memcmp(gkey.data(), key, sizeof(L)) != 0) {
+        if (gexec) {
+            cudaGraphExecDestroy(gexec);
+            gexec = nullptr;
         }
-        W.gkey.clear();
+        gkey.clear();
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         cudaError_t e = enqueue_chunk(L, c->stream);
         cudaGraph_t g = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
         if (e == cudaSuccess) e = e2;
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&W.gexec, g, 0);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&gexec, g, 0);
         if (g) cudaGraphDestroy(g);
         if (e != cudaSuccess) {
-            W.gexec = nullptr;
+            gexec = nullptr;
             return cuda_fail(c, e, "capture of the chunk's launches");
         }
-        W.gkey.assign(key, key + sizeof(L));
+        gkey.assign(key, key + sizeof(L));
     }
-    CK(cudaGraphLaunch(W.gexec, c->stream));
+    CK(cudaGraphLaunch(gexec, c->stream));
     return GPET_OK;
 }
 
@@ -941,6 +957,8 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
             if (cs[s]->sur != c->sur) return fail(c, GPET_ERR_ARG, "the simulations of a batch share one surrogate or none");
         }
     CK(cudaSetDevice(c->device));
+    // nothing of an earlier run may still use the work buffers
+    CK(cudaStreamSynchronize(c->stream2));
     std::vector<int64_t> nd(nsim);
     int64_t ND = 0, max_site = 1;
     bool rec_hits = false;
@@ -1024,6 +1042,9 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         CK(W.q_f.ensure((size_t)2 * chunk * 7 * 4));
         CK(W.q_t.ensure((size_t)2 * chunk * 8));
         CK(W.q_i.ensure((size_t)2 * chunk * 5 * 4));
+        CK(W.qb_f.ensure((size_t)2 * chunk * 7 * 4));
+        CK(W.qb_t.ensure((size_t)2 * chunk * 8));
+        CK(W.qb_i.ensure((size_t)2 * chunk * 5 * 4));
         W.q_cap = 2 * chunk;
     }
     if (c->sur) {
@@ -1075,7 +1096,6 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     PairBuf pb;
     pb.f = W.pb_f.as<float>(); pb.t = W.pb_t.as<double>(); pb.nph = W.pb_n.as<uint8_t>(); pb.cap = W.pb_cap;
     Counters* dcnt = W.cnt.as<Counters>();
-    unsigned long long* qcount = W.aux.as<unsigned long long>() + 0;
     unsigned long long* pcount = W.aux.as<unsigned long long>() + 1;
     unsigned long long* hcount = W.aux.as<unsigned long long>() + 2;
     const bool multi = nsim > 1;
@@ -1114,9 +1134,18 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     gpet_run_stats tot{};
     float ms_det = 0, ms_src = 0, ms_ph = 0, ms_sur = 0;
     cudaEventRecord(c->ev[0], c->stream);
+    // Chunks alternate between two queues. Chunk k's detector stage runs on
+    // stream2 while chunk k+1's source and phantom waves run on the main
+    // stream; chunk k+2's transport waits until that detector stage is done
+    // with the queue. Pulse and hit buffers are checked against an upper
+    // bound (their count so far plus the worst case of the chunks in flight),
+    // and grown only with stream2 idle.
     int64_t pulses_used = 0, hits_used = 0;
+    int64_t inflight = 0;        // queue length of the detector stage that may still run
     size_t wi = 0;
+    int ci = 0;
     while (wi < waves.size()) {
+        const int b = ci & 1;
         // one chunk: waves until `chunk` decays
         const int64_t cg0 = waves[wi].g;
         size_t we = wi;
@@ -1137,9 +1166,12 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
             wave.source = rec_source ? W.source.as<SrcRec>() + 2 * (waves[w].g - cg0) : nullptr;
         }
         CK(cudaMemcpyAsync(W.d_waves.p, W.h_waves, K * sizeof(Wave), cudaMemcpyHostToDevice, c->stream));
+        unsigned long long* qcount = W.aux.as<unsigned long long>() + (b ? 6 : 0);
         QueueDev q;
-        q.f = W.q_f.as<float>(); q.t = W.q_t.as<double>(); q.i = W.q_i.as<int32_t>();
+        q.f = (b ? W.qb_f : W.q_f).as<float>(); q.t = (b ? W.qb_t : W.q_t).as<double>();
+        q.i = (b ? W.qb_i : W.q_i).as<int32_t>();
         q.count = qcount; q.cap = W.q_cap;
+        if (ci >= 2) CK(cudaStreamWaitEvent(c->stream, c->qev[2 + b], 0));   // the queue is free again
         ChunkLaunch L;
         std::memset(&L, 0, sizeof(L));
         L.d_waves = W.d_waves.as<Wave>();
@@ -1158,19 +1190,22 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         L.ph_blocks = (uint32_t)(bps * nsm);
         L.period = c->drain_period;
         L.graph = c->use_graphs ? 1 : 0;
-        rc = launch_chunk(c, W, L);
+        rc = launch_chunk(c, W, L, b);
         if (rc) return rc;
         tot.kernel_launches += 2 * K;
-        unsigned long long hq = 0;
-        CK(cudaMemcpyAsync(&hq, qcount, 8, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaEventRecord(c->qev[b], c->stream));
+        unsigned long long hq3[3] = {0, 0, 0};   // queue, pulses and hits so far (lower bounds)
+        CK(cudaMemcpyAsync(&hq3[0], qcount, 8, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(&hq3[1], pcount, 16, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         CK(cudaGetLastError());
+        const unsigned long long hq = hq3[0];
         for (int e = 0; e < 3 * K; e += 3) {
-            float a = 0, b = 0;
+            float a = 0, bb = 0;
             cudaEventElapsedTime(&a, W.tev[e], W.tev[e + 1]);
-            cudaEventElapsedTime(&b, W.tev[e + 1], W.tev[e + 2]);
+            cudaEventElapsedTime(&bb, W.tev[e + 1], W.tev[e + 2]);
             ms_src += a;
-            ms_ph += b;
+            ms_ph += bb;
         }
         const int64_t cn = waves[we - 1].g + waves[we - 1].n - cg0;
         if (rec_exits)
@@ -1179,10 +1214,26 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         if (rec_source)
             CK(cudaMemcpy(c->host_source.data() + 2 * cg0, W.source.p, (size_t)2 * cn * sizeof(SrcRec),
                           cudaMemcpyDeviceToHost));
-        // room for the worst case of this chunk's queue
-        rc = grow_pulses(c, W, pulses_used + (int64_t)hq * kMaxPulse, pulses_used);
-        if (rc) return rc;
-        if (rec_hits) { rc = grow_hits(c, W, hits_used + (int64_t)hq * kMaxHits, hits_used); if (rc) return rc; }
+        // room for the worst case of this chunk and of the one still in flight
+        pulses_used = std::max<int64_t>(pulses_used, std::min<int64_t>((int64_t)hq3[1], W.p_cap));
+        hits_used = std::max<int64_t>(hits_used, std::min<int64_t>((int64_t)hq3[2], W.h_cap));
+        const int64_t need_p = pulses_used + (inflight + (int64_t)hq) * kMaxPulse;
+        const int64_t need_h = hits_used + (inflight + (int64_t)hq) * kMaxHits;
+        if (need_p > W.p_cap || (rec_hits && need_h > W.h_cap)) {
+            CK(cudaStreamSynchronize(c->stream2));
+            unsigned long long hp[2] = {0, 0};
+            CK(cudaMemcpy(hp, pcount, 16, cudaMemcpyDeviceToHost));
+            pulses_used = (int64_t)std::min<unsigned long long>(hp[0], (unsigned long long)W.p_cap);
+            hits_used = (int64_t)std::min<unsigned long long>(hp[1], (unsigned long long)W.h_cap);
+            inflight = 0;
+            // leave room for two more chunks like this one
+            rc = grow_pulses(c, W, pulses_used + 3 * (int64_t)hq * kMaxPulse, pulses_used);
+            if (rc) return rc;
+            if (rec_hits) {
+                rc = grow_hits(c, W, hits_used + 3 * (int64_t)hq * kMaxHits, hits_used);
+                if (rc) return rc;
+            }
+        }
         PulseDev P = pulse_view(W);
         P.sim = multi ? W.p_sim.as<int32_t>() : nullptr;
         HitDev H;
@@ -1191,7 +1242,14 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         const int dt = c->det_threads;
         int64_t dblocks = std::min<int64_t>(((int64_t)hq + dt - 1) / dt, (int64_t)nsm * 8 * (256 / dt));
         EntryRec* ent = rec_entries ? W.ent.as<EntryRec>() : nullptr;
-        cudaEventRecord(c->ev[1], c->stream);
+        while (W.dev.size() < 4 * (size_t)(ci + 1)) {
+            cudaEvent_t e;
+            CK(cudaEventCreate(&e));
+            W.dev.push_back(e);
+        }
+        cudaStream_t s2 = c->stream2;
+        CK(cudaStreamWaitEvent(s2, c->qev[b], 0));
+        cudaEventRecord(W.dev[4 * ci], s2);
         if (hq > 0 && use_sur) {
             // photons in the surrogate's domain take the learned response, the
             // others the Monte Carlo; the kernels read their counts on the device
@@ -1199,33 +1257,24 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
             q2.f = W.q2_f.as<float>(); q2.t = W.q2_t.as<double>(); q2.i = W.q2_i.as<int32_t>();
             q2.count = W.aux.as<unsigned long long>() + 4; q2.cap = W.q_cap;
             unsigned long long* scount = W.aux.as<unsigned long long>() + 5;
-            CK(cudaMemsetAsync(q2.count, 0, 16, c->stream));
-            CK(launch_route(sdev, q, (int64_t)hq, q2, W.sidx.as<uint32_t>(), scount, c->stream));
-            CK(launch_detector(multi, (unsigned)std::max<int64_t>(dblocks, 1), (unsigned)dt, smem, c->stream, d_sims,
-                               q2, P, H, rec_hits ? 1 : 0, dcnt, ent));
-            cudaEventRecord(c->ev[6], c->stream);
+            CK(cudaMemsetAsync(q2.count, 0, 16, s2));
+            CK(launch_route(sdev, q, (int64_t)hq, q2, W.sidx.as<uint32_t>(), scount, s2));
+            CK(launch_detector(multi, (unsigned)std::max<int64_t>(dblocks, 1), (unsigned)dt, smem, s2, d_sims, q2, P,
+                               H, rec_hits ? 1 : 0, dcnt, ent));
+            cudaEventRecord(W.dev[4 * ci + 2], s2);
             CK(launch_surrogate(sdev, d_sims, q, W.sidx.as<uint32_t>(), scount, (int64_t)hq, P, dcnt,
-                                W.serr.as<int>(), c->stream));
-            cudaEventRecord(c->ev[7], c->stream);
+                                W.serr.as<int>(), s2));
+            cudaEventRecord(W.dev[4 * ci + 3], s2);
             tot.kernel_launches += 3;
         } else if (hq > 0) {
-            CK(launch_detector(multi, (unsigned)std::max<int64_t>(dblocks, 1), (unsigned)dt, smem, c->stream, d_sims,
-                               q, P, H, rec_hits ? 1 : 0, dcnt, ent));
+            CK(launch_detector(multi, (unsigned)std::max<int64_t>(dblocks, 1), (unsigned)dt, smem, s2, d_sims, q, P,
+                               H, rec_hits ? 1 : 0, dcnt, ent));
             tot.kernel_launches++;
         }
-        cudaEventRecord(c->ev[2], c->stream);
-        unsigned long long hp[2] = {0, 0};
-        CK(cudaMemcpyAsync(hp, pcount, 16, cudaMemcpyDeviceToHost, c->stream));
-        CK(cudaStreamSynchronize(c->stream));
-        CK(cudaGetLastError());
-        float ms = 0;
-        cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]);
-        ms_det += ms;
-        if (hq > 0 && use_sur) {
-            cudaEventElapsedTime(&ms, c->ev[6], c->ev[7]);
-            ms_sur += ms;
-        }
+        cudaEventRecord(W.dev[4 * ci + 1], s2);
+        CK(cudaEventRecord(c->qev[2 + b], s2));
         if (rec_entries && hq > 0) {
+            CK(cudaStreamSynchronize(s2));
             unsigned long long ne = hq;
             if (use_sur) CK(cudaMemcpy(&ne, W.aux.as<unsigned long long>() + 4, 8, cudaMemcpyDeviceToHost));
             const size_t old = c->host_entries.size();
@@ -1233,9 +1282,27 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
             CK(cudaMemcpy(c->host_entries.data() + old, W.ent.p, (size_t)ne * sizeof(EntryRec),
                           cudaMemcpyDeviceToHost));
         }
+        inflight = (int64_t)hq;
+        wi = we;
+        ci++;
+    }
+    // join the detector stream
+    CK(cudaStreamSynchronize(c->stream2));
+    CK(cudaGetLastError());
+    {
+        unsigned long long hp[2] = {0, 0};
+        CK(cudaMemcpy(hp, pcount, 16, cudaMemcpyDeviceToHost));
         pulses_used = (int64_t)std::min<unsigned long long>(hp[0], (unsigned long long)W.p_cap);
         hits_used = (int64_t)std::min<unsigned long long>(hp[1], (unsigned long long)W.h_cap);
-        wi = we;
+    }
+    for (int k = 0; k < ci; ++k) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, W.dev[4 * k], W.dev[4 * k + 1]);
+        ms_det += ms;
+        if (use_sur) {
+            cudaEventElapsedTime(&ms, W.dev[4 * k + 2], W.dev[4 * k + 3]);
+            ms_sur += ms;
+        }
     }
     Counters h0{};
     CK(cudaMemcpy(&h0, dcnt, sizeof(Counters), cudaMemcpyDeviceToHost));
@@ -1251,8 +1318,13 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     if (transport_only) {
         // results of this partial run are not kept
         for (int s = 0; s < nsim; ++s) cs[s]->have_results = false;
+        cudaEventRecord(c->ev[3], c->stream);
+        CK(cudaEventSynchronize(c->ev[3]));
+        float ms_wall = 0;
+        cudaEventElapsedTime(&ms_wall, c->ev[0], c->ev[3]);
         if (stats) {
             stats[0] = tot;
+            stats[0].ms_total = ms_wall;
             stats[0].ms_source = ms_src;
             stats[0].ms_phantom = ms_ph;
             stats[0].ms_source_phantom = ms_src + ms_ph;
@@ -1323,7 +1395,7 @@ static int time_transport(gpet_ctx* c, int64_t sample, int reps, double* ms)
         gpet_run_stats st{};
         int rc = run_batch(one, 1, &st, sample, true);
         if (rc) return rc;
-        best = std::min(best, st.ms_source + st.ms_phantom + st.ms_detector);
+        best = std::min(best, st.ms_total);
     }
     *ms = best;
     return GPET_OK;
@@ -1451,6 +1523,7 @@ int gpet_digitize(gpet_ctx* c, const gpet_event* ev, const uint8_t* scat, const 
     if (!c || n < 0 || (n > 0 && (!ev || !scat || !slot))) return GPET_ERR_ARG;
     if (!c->have_geo) return fail(c, GPET_ERR_ARG, "load the geometry first (site numbering)");
     CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream2));
     gpet_run_stats local{};
     if (!st) st = &local;
     std::memset(st, 0, sizeof(*st));
