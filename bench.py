@@ -46,9 +46,9 @@ def algorithmic_bytes_phantom(n_photons, ph_steps, entered):
 
 
 # DRAM bytes per photon slot of k_phantom measured by ncu (dram__bytes_read.sum
-# + dram__bytes_write.sum of one 2^21-decay launch of this workload, 4,194,304
-# photon slots: 146.4 MB + 14.8 MB; the tuned launch shape of the headline run)
-MEASURED_DRAM_BYTES_PER_PHOTON = (146.420224e6 + 14.797312e6) / 4194304
+# + dram__bytes_write.sum of one launch of 4,194,304 decays of this workload,
+# 8,388,608 photon slots: 276.8 MB + 36.3 MB)
+MEASURED_DRAM_BYTES_PER_PHOTON = (276.7552e6 + 36.292608e6) / 8388608
 
 
 def _peaks():
