@@ -340,6 +340,11 @@ __global__ void k_count_by_sim(const uint32_t* __restrict__ order, int64_t m, co
     }
 }
 
+__global__ void k_add_count(Counters* cnt, int field, unsigned long long v)
+{
+    reinterpret_cast<unsigned long long*>(cnt)[field] += v;
+}
+
 // dead time (deadtime, gPET_kernals.cu:657-698, sequential semantics, FP64):
 // sorder is the (simulation, site, t, parn, slot) order
 __global__ void k_deadtime(const uint32_t* __restrict__ sorder, int64_t m, const int32_t* __restrict__ site,
@@ -729,7 +734,11 @@ int digitize_device(const PulseDev& P, int64_t n, const DigiParams* d_prms, int 
             radix_sort(ka, va, kb, vb, m, sim_bits, D.hist, D.scan_aux, total, s, launches);
         }
         cudaMemcpyAsync(D.torder, va, sizeof(uint32_t) * m, cudaMemcpyDeviceToDevice, s);
-        k_count_by_sim<<<grid_for(m, 256), 256, 0, s>>>(D.torder, m, psim, d_cnt, CF(n_thr));
+        if (psim) {
+            k_count_by_sim<<<grid_for(m, 256), 256, 0, s>>>(D.torder, m, psim, d_cnt, CF(n_thr));
+        } else {   // one simulation: its count is m
+            k_add_count<<<1, 1, 0, s>>>(d_cnt, CF(n_thr), (unsigned long long)m);
+        }
         // site order
         int site_bits = 8;
         while (site_bits < 32 && (1ll << site_bits) <= max_site) site_bits += 8;

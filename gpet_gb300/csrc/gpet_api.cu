@@ -50,6 +50,7 @@ struct Work {
     DevBuf pb_f, pb_t, pb_n;              // emitted pairs of one wave
     int64_t pb_cap = 0;
     DevBuf aux;                           // [0] queue count [1] pulses [2] hits [4] Monte Carlo queue [5] surrogate list
+                                          // [6] second queue count [8] detector lanes' next entry
     DevBuf cnt;                           // Counters per simulation
     DevBuf sims, prms, segs;              // batch descriptors
     DevBuf p_int, p_t, p_f, p_meta, p_sim;  // pulses: 6 int32, double, 4 float, byte, simulation
@@ -1105,6 +1106,10 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
     int bps = 0;
     CK(phantom_blocks_per_sm(multi, smem, &bps));
+    int det_bps = 0;
+    CK(detector_blocks_per_sm(multi, (unsigned)c->det_threads, smem, &det_bps));
+    det_bps = std::max(det_bps, 1);
+    unsigned long long* dtake = W.aux.as<unsigned long long>() + 8;
     bps = std::max(1, bps);
     if (c->phantom_bps > 0) bps = std::min(bps, c->phantom_bps);
     const SimDesc* d_sims = W.sims.as<SimDesc>();
@@ -1240,7 +1245,8 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         H.id = W.h_id.as<int32_t>(); H.f = W.h_f.as<float>(); H.count = hcount; H.cap = W.h_cap;
         H.sim = multi ? W.h_sim.as<int32_t>() : nullptr;
         const int dt = c->det_threads;
-        int64_t dblocks = std::min<int64_t>(((int64_t)hq + dt - 1) / dt, (int64_t)nsm * 8 * (256 / dt));
+        // persistent: at most the resident blocks, whose lanes take photons as they finish
+        int64_t dblocks = std::min<int64_t>(((int64_t)hq + dt - 1) / dt, (int64_t)nsm * det_bps);
         EntryRec* ent = rec_entries ? W.ent.as<EntryRec>() : nullptr;
         while (W.dev.size() < 4 * (size_t)(ci + 1)) {
             cudaEvent_t e;
@@ -1249,6 +1255,8 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         }
         cudaStream_t s2 = c->stream2;
         CK(cudaStreamWaitEvent(s2, c->qev[b], 0));
+        CK(cudaMemsetAsync(dtake, 0, 8, s2));
+        q.take = dtake;
         cudaEventRecord(W.dev[4 * ci], s2);
         if (hq > 0 && use_sur) {
             // photons in the surrogate's domain take the learned response, the
@@ -1258,6 +1266,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
             q2.count = W.aux.as<unsigned long long>() + 4; q2.cap = W.q_cap;
             unsigned long long* scount = W.aux.as<unsigned long long>() + 5;
             CK(cudaMemsetAsync(q2.count, 0, 16, s2));
+            q2.take = dtake;
             CK(launch_route(sdev, q, (int64_t)hq, q2, W.sidx.as<uint32_t>(), scount, s2));
             CK(launch_detector(multi, (unsigned)std::max<int64_t>(dblocks, 1), (unsigned)dt, smem, s2, d_sims, q2, P,
                                H, rec_hits ? 1 : 0, dcnt, ent));

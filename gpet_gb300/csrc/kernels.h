@@ -48,6 +48,7 @@ struct QueueDev {
     int32_t* i;                   // [5][cap]: panel index, parn, event id, phantom scatters, simulation
     unsigned long long* count;
     int64_t cap;
+    unsigned long long* take = nullptr;   // next entry for the detector stage's lanes (zero before it)
 };
 
 // pulses after adder + readout, structure of arrays
@@ -168,6 +169,7 @@ cudaError_t launch_detector(bool multi, unsigned blocks, unsigned threads, size_
                             Counters* cnt, EntryRec* entries);
 // resident k_phantom blocks per SM at 256 threads and `smem` bytes
 cudaError_t phantom_blocks_per_sm(bool multi, size_t smem, int* blocks);
+cudaError_t detector_blocks_per_sm(bool multi, unsigned threads, size_t smem, int* blocks);
 // cudaSuccess when the transport kernels have an image for the current device
 cudaError_t transport_kernels_loadable();
 

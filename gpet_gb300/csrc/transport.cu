@@ -498,7 +498,11 @@ __device__ __forceinline__ int readout(const SimDesc& S, PEvent* ev, int n)
     return k;
 }
 
-// kMulti as for k_source: the queue holds photons of several simulations
+// Detector stage: persistent warps; a lane whose photon has finished takes
+// the next queued photon at once (one atomic per warp), so the lanes stay busy
+// while photons need different numbers of steps; pulses and hits of the
+// photons that finished in an iteration are appended with one atomic per warp.
+// kMulti as for k_source: the queue holds photons of several simulations.
 template <bool kMulti>
 __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueDev q, PulseDev P,
                                                   HitDev H, int rec_hits, Counters* cnt, EntryRec* entries)
@@ -512,49 +516,73 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
     unsigned long long nq = *q.count;
     if (nq > (unsigned long long)q.cap) nq = (unsigned long long)q.cap;
     const int64_t n = (int64_t)nq;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
+    const unsigned lt = lanemask_lt();
     unsigned long long n_pdrop = 0, n_hdrop = 0;
     SimTally t_steps, t_cap, t_over, t_pulse, t_hit;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
-        const int64_t j = base + threadIdx.x;
-        const bool valid = j < n;
-        PEvent ev[kMaxPulse];
-        int nev = 0;
-        int nh = 0;
-        int32_t hid[kMaxHits][4];
-        float hf[kMaxHits][5];
-        int32_t parn = 0, eid = 0, scat = 0, sim = 0;
-        bool overflow = false;
-        unsigned nsteps = 0, capped = 0;
-        if (valid) {
-            sim = q.i[4 * q.cap + j];
-            const SimDesc& S = kMulti ? sims[sim] : sS;
-            Local L;
-            L.x[0] = q.f[0 * q.cap + j]; L.x[1] = q.f[1 * q.cap + j]; L.x[2] = q.f[2 * q.cap + j];
-            L.u[0] = q.f[3 * q.cap + j]; L.u[1] = q.f[4 * q.cap + j]; L.u[2] = q.f[5 * q.cap + j];
-            L.E = q.f[6 * q.cap + j];
-            L.t = q.t[j];
-            L.tf = 0.0f;
-            L.panel = q.i[0 * q.cap + j];
-            parn = q.i[1 * q.cap + j];
-            eid = q.i[2 * q.cap + j];
-            scat = q.i[3 * q.cap + j];
-            const float* Pn = kMulti ? S.panels + L.panel * kPanelStride : sP + L.panel * kPanelStride;
-            const int32_t pann = (int32_t)Pn[30];
-            EntryRec er;
-            if (entries) {
-                er.panel = L.panel;
-                er.y = L.x[1]; er.z = L.x[2];
-                er.ux = L.u[0]; er.uy = L.u[1]; er.uz = L.u[2];
-                er.E = L.E;
+    // the lane's photon
+    bool active = false, exhausted = false;
+    int64_t j = 0;
+    Local L;
+    const float* Pn = nullptr;
+    int32_t pann = 0;
+    Stream st;
+    PEvent ev[kMaxPulse];
+    int nev = 0, nh = 0, step = 0;
+    int32_t hid[kMaxHits][4];
+    float hf[kMaxHits][5];
+    int32_t parn = 0, eid = 0, scat = 0, sim = 0;
+    bool overflow = false;
+    unsigned nsteps = 0;
+    EntryRec er;
+    for (;;) {
+        // refill idle lanes
+        const bool need = !active && !exhausted;
+        const unsigned mneed = __ballot_sync(0xffffffffu, need);
+        if (mneed) {
+            unsigned long long b = 0;
+            const int leader = __ffs(mneed) - 1;
+            if (lane == leader) b = atomicAdd(q.take, (unsigned long long)__popc(mneed));
+            b = __shfl_sync(0xffffffffu, b, leader);
+            if (need) {
+                j = (int64_t)(b + __popc(mneed & lt));
+                if (j >= n) {
+                    exhausted = true;
+                } else {
+                    sim = q.i[4 * q.cap + j];
+                    const SimDesc& S = kMulti ? sims[sim] : sS;
+                    L.x[0] = q.f[0 * q.cap + j]; L.x[1] = q.f[1 * q.cap + j]; L.x[2] = q.f[2 * q.cap + j];
+                    L.u[0] = q.f[3 * q.cap + j]; L.u[1] = q.f[4 * q.cap + j]; L.u[2] = q.f[5 * q.cap + j];
+                    L.E = q.f[6 * q.cap + j];
+                    L.t = q.t[j];
+                    L.tf = 0.0f;
+                    L.panel = q.i[0 * q.cap + j];
+                    parn = q.i[1 * q.cap + j];
+                    eid = q.i[2 * q.cap + j];
+                    scat = q.i[3 * q.cap + j];
+                    Pn = kMulti ? S.panels + L.panel * kPanelStride : sP + L.panel * kPanelStride;
+                    pann = (int32_t)Pn[30];
+                    if (entries) {
+                        er.panel = L.panel;
+                        er.y = L.x[1]; er.z = L.x[2];
+                        er.ux = L.u[0]; er.uy = L.u[1]; er.uz = L.u[2];
+                        er.E = L.E;
+                    }
+                    st_init(st, S.key0, S.key1, kTagDet + (parn & 1), (uint64_t)(uint32_t)eid);
+                    nev = 0; nh = 0; step = 0; nsteps = 0;
+                    overflow = false;
+                    active = true;
+                }
             }
-            Stream st;
-            st_init(st, S.key0, S.key1, kTagDet + (parn & 1), (uint64_t)(uint32_t)eid);
-            // photonde transport loop, gPET_kernals.cu:1013-1193
-            int step;
-            for (step = 0; step < kMaxSteps; ++step) {
-                nsteps++;
+        }
+        if (__all_sync(0xffffffffu, !active && exhausted)) break;
+        // one Woodcock step in the panel (photonde, gPET_kernals.cu:1013-1193)
+        bool done = false;
+        unsigned capped = 0;
+        if (active) {
+            const SimDesc& S = kMulti ? sims[sim] : sS;
+            nsteps++;
+            do {   // a single pass: `break` ends the step
                 float lammin = wck_at(S.wck_det, S.wck_e0, S.wck_ide, L.E);
                 float s = -lammin * dm_logf(st_u(st));
                 L.x[0] = dm_fma(s, L.u[0], L.x[0]);
@@ -562,8 +590,10 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                 L.x[2] = dm_fma(s, L.u[2], L.x[2]);
                 L.tf = dm_fma(s, DM_INV_SPEED, L.tf);
                 if (fabsf(L.x[1]) > Pn[1] * 0.5f || fabsf(L.x[2]) > Pn[2] * 0.5f || L.x[0] * Pn[18] < 0.0f ||
-                    L.x[0] * Pn[18] > Pn[0])
+                    L.x[0] * Pn[18] > Pn[0]) {
+                    done = true;
                     break;
+                }
                 int m_id = -1, M_id = -1, L_id = -1;
                 crystal_search(S, Pn, L.x, m_id, M_id, L_id);
                 float den = S.det_den[m_id];
@@ -573,7 +603,7 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                 float prob = dm_fma(-lamden, xs.x, 1.0f);
                 if (prob < 0.0f) prob = 0.0f;
                 float rn = st_u(st);
-                if (rn < prob) continue;
+                if (rn < prob) break;   // virtual
                 prob = dm_fma(lamden, xs.y, prob);
                 int type = 0;
                 float dep = 0.0f;
@@ -604,7 +634,7 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                         type = 2; dep = L.E;
                     } else {
                         rotate(L.u[0], L.u[1], L.u[2], cost, phi);
-                        continue;
+                        break;
                     }
                 } else {
                     prob = dm_fma(lamden, xs.z, prob);
@@ -612,7 +642,7 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                         float cost = rayleigh_surface(S, L.E, mat, st);
                         float phi = st_u(st);
                         rotate(L.u[0], L.u[1], L.u[2], cost, phi);
-                        continue;
+                        break;
                     }
                     type = 4; dep = L.E;
                 }
@@ -633,24 +663,31 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                     }
                     if (!adder(ev, nev, e)) overflow = true;
                 }
-                break;
+                done = true;
+            } while (false);
+            step++;
+            if (!done && step >= kMaxSteps) {
+                done = true;
+                capped = 1;
             }
-            if (step == kMaxSteps) capped = 1;
-            if (nev) nev = readout(S, ev, nev);
-            if (entries) {
-                er.crystal = nev ? ev[0].cryn : -1;
-                er.depth = nev ? ev[0].x * Pn[18] : 0.0f;
-                er.Edep = nev ? ev[0].E : 0.0f;
-                entries[j] = er;
+            if (done) {
+                if (nev) nev = readout(S, ev, nev);
+                if (entries) {
+                    er.crystal = nev ? ev[0].cryn : -1;
+                    er.depth = nev ? ev[0].x * Pn[18] : 0.0f;
+                    er.Edep = nev ? ev[0].E : 0.0f;
+                    entries[j] = er;
+                }
+                t_steps.add(cnt, CF(det_steps), sim, nsteps);
+                t_cap.add(cnt, CF(stepcap), sim, capped);
+                t_over.add(cnt, CF(overflow), sim, overflow ? 1u : 0u);
+                t_pulse.add(cnt, CF(n_pulse), sim, (unsigned)nev);
+                t_hit.add(cnt, CF(n_hit), sim, rec_hits ? (unsigned)nh : 0u);
             }
-            t_steps.add(cnt, CF(det_steps), sim, nsteps);
-            t_cap.add(cnt, CF(stepcap), sim, capped);
-            t_over.add(cnt, CF(overflow), sim, overflow ? 1u : 0u);
-            t_pulse.add(cnt, CF(n_pulse), sim, (unsigned)nev);
-            t_hit.add(cnt, CF(n_hit), sim, rec_hits ? (unsigned)nh : 0u);
         }
-        // append pulses and hits, one atomic per warp
-        int inc = nev;
+        // append the pulses and hits of the photons that finished, one atomic per warp
+        const int my_ev = done ? nev : 0;
+        int inc = my_ev;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             int v = __shfl_up_sync(0xffffffffu, inc, o);
@@ -661,8 +698,8 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
             unsigned long long b = 0;
             if (lane == 31) b = atomicAdd(P.count, (unsigned long long)tot);
             b = __shfl_sync(0xffffffffu, b, 31);
-            unsigned long long o = b + (unsigned long long)(inc - nev);
-            for (int i = 0; i < nev; ++i, ++o) {
+            unsigned long long o = b + (unsigned long long)(inc - my_ev);
+            for (int i = 0; i < my_ev; ++i, ++o) {
                 if (o >= (unsigned long long)P.cap) { n_pdrop++; continue; }
                 P.parn[o] = parn; P.pann[o] = ev[i].pann; P.modn[o] = ev[i].modn; P.cryn[o] = ev[i].cryn;
                 P.siten[o] = ev[i].siten; P.eventid[o] = eid; P.t[o] = ev[i].t;
@@ -672,7 +709,8 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
             }
         }
         if (rec_hits) {
-            int hinc = nh;
+            const int my_h = done ? nh : 0;
+            int hinc = my_h;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 int v = __shfl_up_sync(0xffffffffu, hinc, o);
@@ -683,8 +721,8 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                 unsigned long long b = 0;
                 if (lane == 31) b = atomicAdd(H.count, (unsigned long long)htot);
                 b = __shfl_sync(0xffffffffu, b, 31);
-                unsigned long long o = b + (unsigned long long)(hinc - nh);
-                for (int i = 0; i < nh; ++i, ++o) {
+                unsigned long long o = b + (unsigned long long)(hinc - my_h);
+                for (int i = 0; i < my_h; ++i, ++o) {
                     if (o >= (unsigned long long)H.cap) { n_hdrop++; continue; }
                     H.id[5 * o + 0] = parn;
                     H.id[5 * o + 1] = hid[i][0]; H.id[5 * o + 2] = hid[i][1]; H.id[5 * o + 3] = hid[i][2];
@@ -694,6 +732,7 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                 }
             }
         }
+        if (done) active = false;
     }
     t_steps.flush(cnt, CF(det_steps));
     t_cap.flush(cnt, CF(stepcap));
@@ -741,6 +780,13 @@ cudaError_t phantom_blocks_per_sm(bool multi, size_t smem, int* blocks)
 {
     return multi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_phantom<true>, 256, smem)
                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_phantom<false>, 256, smem);
+}
+
+cudaError_t detector_blocks_per_sm(bool multi, unsigned threads, size_t smem, int* blocks)
+{
+    if (!valid_threads(threads)) return cudaErrorInvalidValue;
+    return multi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_detector<true>, (int)threads, smem)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_detector<false>, (int)threads, smem);
 }
 
 cudaError_t transport_kernels_loadable()
