@@ -44,10 +44,12 @@ struct SimDesc {
     float wck_e0, wck_ide;
     const float* wck_ph;          // [4096]
     const float* wck_det;         // [4096]
-    // phantom: vox[i] = (density bits, material), x fastest
+    // phantom: vox[i] = (density bits, material), x fastest; or, with vox16
+    // set, vox[vox16[i]] (a palette of the distinct pairs)
     int32_t nx, ny, nz;
     float dx, dy, dz, idx, idy, idz, offx, offy, offz;
     const uint2* vox;
+    const uint16_t* vox16;
     // detector
     int32_t npanels;
     const float* panels;          // [npanels][32]
@@ -247,7 +249,9 @@ __device__ __forceinline__ bool abs_vox(const SimDesc& S, float x, float y, floa
 
 __device__ __forceinline__ uint2 voxel(const SimDesc& S, int ix, int iy, int iz)
 {
-    return __ldg(S.vox + ((size_t)ix + (size_t)S.nx * ((size_t)iy + (size_t)S.ny * iz)));
+    const size_t i = (size_t)ix + (size_t)S.nx * ((size_t)iy + (size_t)S.ny * iz);
+    if (S.vox16) return __ldg(S.vox + __ldg(S.vox16 + i));
+    return __ldg(S.vox + i);
 }
 
 __device__ __forceinline__ float den_clamped(const SimDesc& S, int ix, int iy, int iz)

@@ -115,6 +115,9 @@ struct gpet_ctx {
     float noise_emean = 511000.0f, noise_sigma = 0.0f;
     double noise_interval_us = 1000.0;
     int psf_sphere = 0;                   // phantom phase space projected onto the record sphere
+    int voxel_palette = 1;                // 16-bit voxel indices into a (density, material) palette
+                                          // when the distinct pairs fit (1), or 8-byte pairs (0)
+    bool vox_pal = false;                 // the phantom on the device is in palette form
     gpet_surrogate* sur = nullptr;        // learned detector response (not owned)
     std::string base_dir = ".";
     std::string data_dir;
@@ -137,6 +140,7 @@ struct gpet_ctx {
     // device scene
     SimDesc sim{};
     DevBuf d_sim, d_xs4, d_cmpsf, d_rayff, d_wck_ph, d_wck_det, d_vox, d_panels, d_psf;
+    DevBuf d_vox16, d_pal;                // palette form: per-voxel index, palette (hash table of pairs)
     DevBuf d_mat_stage, d_den_stage, d_maxden;   // phantom upload
     // results of the last run this context took part in
     std::shared_ptr<Work> work;
@@ -194,6 +198,57 @@ __global__ void k_pack_phantom(const int32_t* __restrict__ mat, const float* __r
         vox[v] = make_uint2(__float_as_uint(d), (unsigned)m);
     }
     if (nbad) atomicAdd(bad, nbad);
+    __syncthreads();
+    if ((int)threadIdx.x < nmat && threadIdx.x < 16 && smax[threadIdx.x]) atomicMax(&maxden_bits[threadIdx.x], smax[threadIdx.x]);
+}
+
+// Palette form of the phantom: each voxel's (density bits, material) pair is
+// entered in an open-addressing hash table of kPalSlots 64-bit keys (material
+// in the high word, density bits in the low word, so a key read as uint2 is
+// the voxel record), and the voxel stores its slot. A slot goes from empty to
+// its key once, so a plain (cached) read that sees a key sees the final one;
+// one that sees an empty slot goes on to the compare-and-swap. Slot numbers
+// depend on insertion order, the values they hold do not. Pairs that find no
+// slot within kPalProbes probes are counted in bad[1] (the caller falls back
+// to the uint2 form).
+constexpr int kPalBits = 16;
+constexpr uint32_t kPalSlots = 1u << kPalBits;
+constexpr int kPalProbes = 256;
+constexpr unsigned long long kPalEmpty = ~0ull;
+
+__global__ void k_pack_palette(const int32_t* __restrict__ mat, const float* __restrict__ den, int64_t n, int nmat,
+                               uint16_t* __restrict__ vox16, unsigned long long* keys, unsigned* maxden_bits,
+                               unsigned* bad)
+{
+    __shared__ unsigned smax[16];
+    if (threadIdx.x < 16) smax[threadIdx.x] = 0;
+    __syncthreads();
+    unsigned nbad = 0, novf = 0;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int m = mat[v];
+        const float d = den[v];
+        if (m < 0 || m >= nmat) {
+            nbad++;
+            continue;
+        }
+        if (d > 0.0f) atomicMax(&smax[m], __float_as_uint(d));
+        const unsigned long long key = ((unsigned long long)(unsigned)m << 32) | __float_as_uint(d);
+        uint32_t h = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - kPalBits));
+        int slot = -1;
+        for (int p = 0; p < kPalProbes; ++p) {
+            const unsigned long long cur = keys[h];
+            if (cur == key) { slot = (int)h; break; }
+            if (cur == kPalEmpty) {
+                const unsigned long long prev = atomicCAS(&keys[h], kPalEmpty, key);
+                if (prev == kPalEmpty || prev == key) { slot = (int)h; break; }
+            }
+            h = (h + 1) & (kPalSlots - 1);
+        }
+        if (slot < 0) novf++;
+        else vox16[v] = (uint16_t)slot;
+    }
+    if (nbad) atomicAdd(bad, nbad);
+    if (novf) atomicAdd(bad + 1, novf);
     __syncthreads();
     if ((int)threadIdx.x < nmat && threadIdx.x < 16 && smax[threadIdx.x]) atomicMax(&maxden_bits[threadIdx.x], smax[threadIdx.x]);
 }
@@ -275,6 +330,7 @@ int gpet_set_option(gpet_ctx* c, const char* key, const char* value)
     else if (k == "record_entries") c->record_entries = (int)std::strtol(value, &end, 10);
     else if (k == "record_source") c->record_source = (int)std::strtol(value, &end, 10);
     else if (k == "psf_sphere") c->psf_sphere = (int)std::strtol(value, &end, 10);
+    else if (k == "voxel_palette") c->voxel_palette = (int)std::strtol(value, &end, 10);
     else if (k == "noise_lambda_us") c->noise_lambda_us = std::strtof(value, &end);
     else if (k == "noise_emean_ev") c->noise_emean = std::strtof(value, &end);
     else if (k == "noise_sigma_ev") c->noise_sigma = std::strtof(value, &end);
@@ -292,6 +348,7 @@ int gpet_set_option(gpet_ctx* c, const char* key, const char* value)
     if (c->noise_lambda_us > 0.0f && c->noise_interval_us > 1024.0 * c->noise_lambda_us)
         return fail(c, GPET_ERR_ARG, "noise_interval_us may hold at most 1024 mean gaps");
     if (c->drain_period < 1 || c->drain_period > 32) return fail(c, GPET_ERR_ARG, "drain_period must be 1..32");
+    if (c->voxel_palette < 0 || c->voxel_palette > 1) return fail(c, GPET_ERR_ARG, "voxel_palette must be 0 or 1");
     for (int t : {c->det_threads, c->src_threads})
         if (t < 32 || t > 256 || t % 32) return fail(c, GPET_ERR_ARG, "threads per block must be 32..256, a multiple of 32");
     return GPET_OK;
@@ -381,19 +438,41 @@ int gpet_set_phantom(gpet_ctx* c, const int32_t* mat, const float* den, const in
     c->have_phantom = false;
     CK(c->d_mat_stage.ensure((size_t)n * 4));
     CK(c->d_den_stage.ensure((size_t)n * 4));
-    CK(c->d_vox.ensure((size_t)n * sizeof(uint2)));
     CK(c->d_maxden.ensure(32 * 4));
     CK(cudaMemsetAsync(c->d_maxden.p, 0, 32 * 4, c->stream));
     CK(cudaMemcpyAsync(c->d_mat_stage.p, mat, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->d_den_stage.p, den, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
     const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 16);
-    k_pack_phantom<<<(unsigned)blocks, 256, 0, c->stream>>>(c->d_mat_stage.as<int32_t>(), c->d_den_stage.as<float>(),
-                                                             n, c->tab.nmat, c->d_vox.as<uint2>(),
-                                                             c->d_maxden.as<unsigned>(), c->d_maxden.as<unsigned>() + 16);
-    CK(cudaGetLastError());
-    unsigned h[17] = {0};
-    CK(cudaMemcpyAsync(h, c->d_maxden.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
+    unsigned h[18] = {0};
+    // palette form (2 B per voxel: a 256 x 256 x 512 phantom stays in L2)
+    // unless switched off or the distinct pairs do not fit
+    bool pal = c->voxel_palette == 1;
+    if (pal) {
+        CK(c->d_vox16.ensure((size_t)n * 2));
+        CK(c->d_pal.ensure((size_t)kPalSlots * 8));
+        CK(cudaMemsetAsync(c->d_pal.p, 0xFF, (size_t)kPalSlots * 8, c->stream));
+        k_pack_palette<<<(unsigned)blocks, 256, 0, c->stream>>>(
+            c->d_mat_stage.as<int32_t>(), c->d_den_stage.as<float>(), n, c->tab.nmat, c->d_vox16.as<uint16_t>(),
+            c->d_pal.as<unsigned long long>(), c->d_maxden.as<unsigned>(), c->d_maxden.as<unsigned>() + 16);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(h, c->d_maxden.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (h[17]) {   // too many distinct pairs: the uint2 form
+            pal = false;
+            CK(cudaMemsetAsync(c->d_maxden.p, 0, 32 * 4, c->stream));
+        }
+    }
+    if (!pal) {
+        CK(c->d_vox.ensure((size_t)n * sizeof(uint2)));
+        k_pack_phantom<<<(unsigned)blocks, 256, 0, c->stream>>>(c->d_mat_stage.as<int32_t>(),
+                                                                 c->d_den_stage.as<float>(), n, c->tab.nmat,
+                                                                 c->d_vox.as<uint2>(), c->d_maxden.as<unsigned>(),
+                                                                 c->d_maxden.as<unsigned>() + 16);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(h, c->d_maxden.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    c->vox_pal = pal;
     if (h[16]) return fail(c, GPET_ERR_ARG, "phantom material index out of range");
     float maxden[10] = {0};
     for (int m = 0; m < 10 && m < c->tab.nmat; ++m) std::memcpy(&maxden[m], &h[m], 4);
@@ -579,7 +658,8 @@ static int build_sim(gpet_ctx* c)
     S.dx = c->psz[0] / (float)c->pdim[0]; S.dy = c->psz[1] / (float)c->pdim[1]; S.dz = c->psz[2] / (float)c->pdim[2];
     S.idx = 1.0f / S.dx; S.idy = 1.0f / S.dy; S.idz = 1.0f / S.dz;
     S.offx = c->poff[0]; S.offy = c->poff[1]; S.offz = c->poff[2];
-    S.vox = c->d_vox.as<uint2>();
+    S.vox = c->vox_pal ? c->d_pal.as<uint2>() : c->d_vox.as<uint2>();
+    S.vox16 = c->vox_pal ? c->d_vox16.as<uint16_t>() : nullptr;
     S.npanels = c->geo.npanels;
     S.panels = c->d_panels.as<float>();
     S.ndetmat = c->geo.ndetmat;
@@ -1102,6 +1182,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     const bool multi = nsim > 1;
     // one simulation: its panels are staged in shared memory
     if (multi) smem = 0;
+    else CK(transport_set_smem(smem));
     int nsm = 0;
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
     int bps = 0;

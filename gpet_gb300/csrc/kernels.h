@@ -169,6 +169,7 @@ cudaError_t launch_detector(bool multi, unsigned blocks, unsigned threads, size_
                             Counters* cnt, EntryRec* entries);
 // resident k_phantom blocks per SM at 256 threads and `smem` bytes
 cudaError_t phantom_blocks_per_sm(bool multi, size_t smem, int* blocks);
+cudaError_t transport_set_smem(size_t smem);
 cudaError_t detector_blocks_per_sm(bool multi, unsigned threads, size_t smem, int* blocks);
 // cudaSuccess when the transport kernels have an image for the current device
 cudaError_t transport_kernels_loadable();

@@ -789,6 +789,19 @@ cudaError_t detector_blocks_per_sm(bool multi, unsigned threads, size_t smem, in
                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_detector<false>, (int)threads, smem);
 }
 
+// the panels staged in shared memory (single-simulation launches) can take
+// the source, phantom and detector kernels above the 48 KB that need no opt-in
+cudaError_t transport_set_smem(size_t smem)
+{
+    const int v = (int)smem;
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_source<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v)) != cudaSuccess)
+        return e;
+    if ((e = cudaFuncSetAttribute(k_phantom<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v)) != cudaSuccess)
+        return e;
+    return cudaFuncSetAttribute(k_detector<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+}
+
 cudaError_t transport_kernels_loadable()
 {
     cudaFuncAttributes fa;

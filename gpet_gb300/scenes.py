@@ -141,10 +141,14 @@ def positron(directory, n_decays=100_000_000, nvox=128, seed=DEFAULT_SEED):
                  "F-18 cylinder r=3 cm, %d^3 water/bone/lung, 8-panel ring at 8 cm" % nvox)
 
 
-def large(directory, n_decays=1_000_000_000, dims=(256, 256, 512), seed=DEFAULT_SEED):
+def large(directory, n_decays=1_000_000_000, dims=(256, 256, 512), seed=DEFAULT_SEED, voxel_cm=0.2):
+    """Whole-body acquisition: F-18 cylinder r=10 cm, h=60 cm in a 30 x 20 cm
+    elliptic water body with lungs (rho 0.3) and a spine (bone), 48-panel
+    ring of 16 x 16 LYSO crystals (4 x 4 x 20 mm). voxel_cm coarsens the grid
+    (the body keeps its size) for cases the oracle finishes in seconds."""
     os.makedirs(directory, exist_ok=True)
     nx, ny, nz = dims
-    sx, sy, sz = 0.2 * nx, 0.2 * ny, 0.2 * nz
+    sx, sy, sz = voxel_cm * nx, voxel_cm * ny, voxel_cm * nz
     c = _base_config(directory, dims, (sx, sy, sz), (-sx / 2, -sy / 2, -sz / 2))
     c.useprange = 1
     c.dlevel, c.dtype, c.dtime = 2, 0, 0.3

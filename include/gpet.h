@@ -88,7 +88,11 @@ const char* gpet_last_error(gpet_ctx* ctx);
  *   (results do not depend on it): sub_decays, chunk_decays,
  *   phantom_blocks_per_sm, drain_period, detector_threads, source_threads,
  *   use_graphs (1: each chunk's wave launches replay as one CUDA graph),
- *   autotune (1: gpet_autotune on the first gpet_run); background singles
+ *   autotune (1: gpet_autotune on the first gpet_run), voxel_palette (read
+ *   by gpet_set_phantom: 1 (default) stores the phantom as 16-bit indices
+ *   into a palette of its distinct (density, material) pairs, 0 as 8-byte
+ *   pairs; more distinct pairs than the palette holds (about 32k or more)
+ *   fall back to pairs); background singles
  *   (addnoise, gPET_kernals.cu:699-735): noise_lambda_us (mean gap, 0 = off),
  *   noise_emean_ev, noise_sigma_ev, noise_interval_us (1000; each interval
  *   has its own random stream). */

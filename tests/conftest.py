@@ -59,6 +59,15 @@ def scene_positron(tmp_path_factory, data_dir):
     return scenes.positron(str(d), n_decays=20000, nvox=48)
 
 
+@pytest.fixture(scope="session")
+def scene_large(tmp_path_factory, data_dir):
+    """The whole-body configuration (48 panels at 49 cm, body phantom) on a
+    coarse 64 x 64 x 128 grid of 0.8 cm voxels."""
+    from gpet_gb300 import scenes
+    d = tmp_path_factory.mktemp("large")
+    return scenes.large(str(d), n_decays=300000, dims=(64, 64, 128), voxel_cm=0.8)
+
+
 def make_ctx(scene, data_dir, **extra):
     from gpet_gb300 import api
     ctx = api.Context(0)

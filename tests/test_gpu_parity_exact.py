@@ -4,6 +4,8 @@ The CUDA kernels and the oracle's FP32 build perform the same IEEE operations
 in the same order on the same Philox streams, so every photon's phantom exit
 state, every hit, every pulse, every single and every coincidence must agree
 bit for bit. Sizes are ones the oracle finishes in about a second."""
+import os
+
 import numpy as np
 import pytest
 
@@ -29,9 +31,9 @@ def _run_both(scene, data_dir, **extra):
     return ctx, st, r
 
 
-@pytest.mark.parametrize("which", ["small", "positron"])
-def test_histories_bit_exact(which, scene_small, scene_positron, data_dir, gpet_lib, oracle_mod):
-    scene = scene_small if which == "small" else scene_positron
+@pytest.mark.parametrize("which", ["small", "positron", "large"])
+def test_histories_bit_exact(which, scene_small, scene_positron, scene_large, data_dir, gpet_lib, oracle_mod):
+    scene = {"small": scene_small, "positron": scene_positron, "large": scene_large}[which]
     ctx, st, r = _run_both(scene, data_dir)
     gx = ctx.exits()
     ox = r["exits"]
@@ -56,9 +58,9 @@ def test_histories_bit_exact(which, scene_small, scene_positron, data_dir, gpet_
     assert np.array_equal(canon(gid, gf), canon(r["hit_id"], r["hit_f"]))
 
 
-@pytest.mark.parametrize("which", ["small", "positron"])
-def test_singles_and_coincidences_bit_exact(which, scene_small, scene_positron, data_dir, gpet_lib, oracle_mod):
-    scene = scene_small if which == "small" else scene_positron
+@pytest.mark.parametrize("which", ["small", "positron", "large"])
+def test_singles_and_coincidences_bit_exact(which, scene_small, scene_positron, scene_large, data_dir, gpet_lib, oracle_mod):
+    scene = {"small": scene_small, "positron": scene_positron, "large": scene_large}[which]
     ctx, st, r = _run_both(scene, data_dir)
     gs, gsc = ctx.singles()
     assert st["n_threshold"] == r["n_threshold"]
@@ -227,3 +229,40 @@ def test_multi_material_detector_bit_exact(scene_small, data_dir, gpet_lib, orac
     ctx2.run()
     _, gf2 = ctx2.hits()
     assert (gf2[:, 2] >= -0.5 - 1e-6).all()
+
+
+@pytest.mark.parametrize("which", ["positron", "large"])
+def test_voxel_pairs_bit_exact(which, scene_positron, scene_large, data_dir, gpet_lib, oracle_mod):
+    """The phantom stored as 8-byte (density, material) pairs instead of the
+    default palette form (16-bit indices into the distinct pairs): histories,
+    singles and coincidences bit for bit against the oracle."""
+    scene = scene_positron if which == "positron" else scene_large
+    ctx = make_ctx(scene, data_dir, record_exits=1, voxel_palette=0)
+    st = ctx.run()
+    r = oracle_for(scene, data_dir, panels=ctx.panels()).run(precision="fp32", exits=True, hits=True)
+    msg = _first_diff(ctx.exits(), r["exits"], ["status", "panel", "nscat", "E", "x", "y", "z", "ux", "uy", "uz", "t"])
+    assert msg is None, msg
+    gs, _ = ctx.singles()
+    assert np.array_equal(gs.view(np.uint8), r["singles"].view(np.uint8))
+    pr, cl = ctx.coincidences()
+    assert np.array_equal(pr, r["coinc"]) and np.array_equal(cl, r["coinc_class"])
+
+
+def test_voxel_palette_falls_back_to_pairs(scene_positron, data_dir, gpet_lib):
+    """More distinct (density, material) pairs than the palette holds: the
+    phantom is stored as pairs and the run equals the one without a palette."""
+    from gpet_gb300 import formats as F
+    cfg = F.read_config(scene_positron.config_path)
+    d = scene_positron.directory
+    mat, den = F.read_phantom(os.path.join(d, "phantom_mat.dat"), os.path.join(d, "phantom_den.dat"),
+                              tuple(cfg.pdim))
+    rng = np.random.default_rng(11)
+    den = (den * rng.uniform(0.98, 1.02, den.shape)).astype(np.float32)   # ~110k distinct values
+    assert len(np.unique(den)) > 70000
+    out = []
+    for pal in (1, 0):   # 1 falls back to pairs here
+        ctx = make_ctx(scene_positron, data_dir, voxel_palette=pal)
+        ctx.set_phantom(mat, den, cfg.pdim, cfg.poffset, cfg.psize)
+        st = ctx.run()
+        out.append((st["n_singles"], st["n_coinc"], ctx.singles()[0].tobytes(), ctx.coincidences()[0].tobytes()))
+    assert out[0] == out[1] and out[0][1] > 0
