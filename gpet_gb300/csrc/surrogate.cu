@@ -175,107 +175,146 @@ struct FwdInfer {
 // a warp's 32 TMEM lanes, columns [c0, c0 + 32): all lanes must call it
 __device__ __forceinline__ void ld_cols(uint32_t taddr, int c0, float (&v)[32]) { umma::tmem_ld32(taddr + c0, v); }
 
-// sample a photon's response from the head's outputs (in TMEM) and append
-// its pulse; all 128 threads call it (the TMEM loads are warp-collective)
-__device__ __noinline__ void sample_and_append(const SurrogateDev& sd, const FwdInfer& in, uint32_t taddr, bool valid,
-                                               int sim, int panel, int parn, int eid, int scat, float E, float ux,
-                                               double t0, int lane)
+__device__ __forceinline__ float tanh_approx(float x)
+{
+    float r;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// The response of a photon is sampled from the head's outputs in TMEM by
+// three warp groups at once (each thread: one row of the tile): the deposited
+// energy bin, the crystal, the depth. Each draws from the photon's own Philox
+// stream (tag 6, id = parn) in the fixed order ue, uw, uc, um, zn, skipping
+// the draws of the others. hb: the head's bias.
+
+// deposited-energy fraction bin: softmax over columns [76, 140)
+__device__ __forceinline__ int sample_energy(uint32_t taddr, const float* hb, float ue)
 {
     using namespace sg;
-    const float* bias = sd.params + b_off(kLayers - 1);
-    const SimDesc& S = in.sims[valid ? sim : 0];
-    Stream st;
-    st_init(st, S.key0, S.key1, kTagSurrogate, (uint64_t)(uint32_t)parn);
-    const float ue = st_u(st), uw = st_u(st), uc = st_u(st), um = st_u(st);
-    const float zn = st_normal(st);
-    // deposited-energy fraction: columns [76, 140)
+    uint32_t a[32], b[32], c[16];
+    umma::tmem_ld32_nowait(taddr + 64, a);
+    umma::tmem_ld32_nowait(taddr + 96, b);
+    umma::tmem_ld16_nowait(taddr + 128, c);
+    umma::tmem_wait_ld();
+    float e[kBins];
+#pragma unroll
+    for (int k = 0; k < kBins; ++k) {
+        const int col = kColE + k;
+        const uint32_t raw = col < 96 ? a[col - 64] : (col < 128 ? b[col - 96] : c[col - 128]);
+        e[k] = __uint_as_float(raw) + hb[col];
+    }
     float mx = -1e30f;
-    for (int c = 64; c < 160; c += 32) {
-        float v[32];
-        ld_cols(taddr, c, v);
-        for (int j = 0; j < 32; ++j) {
-            const int col = c + j;
-            if (col >= kColE && col < kColE + kBins) mx = fmaxf(mx, v[j] + bias[col]);
-        }
-    }
+#pragma unroll
+    for (int k = 0; k < kBins; ++k) mx = fmaxf(mx, e[k]);
     float sum = 0.0f;
-    for (int c = 64; c < 160; c += 32) {
-        float v[32];
-        ld_cols(taddr, c, v);
-        for (int j = 0; j < 32; ++j) {
-            const int col = c + j;
-            if (col >= kColE && col < kColE + kBins) sum += __expf(v[j] + bias[col] - mx);
-        }
+#pragma unroll
+    for (int k = 0; k < kBins; ++k) {
+        e[k] = __expf(e[k] - mx);
+        sum += e[k];
     }
+    const float target = ue * sum;
+    float acc = 0.0f;
     int bin = kBins - 1;
-    {
-        const float target = ue * sum;
-        float acc = 0.0f;
-        bool found = false;
-        for (int c = 64; c < 160; c += 32) {
-            float v[32];
-            ld_cols(taddr, c, v);
-            for (int j = 0; j < 32; ++j) {
-                const int col = c + j;
-                if (col >= kColE && col < kColE + kBins && !found) {
-                    acc += __expf(v[j] + bias[col] - mx);
-                    if (acc >= target) { bin = col - kColE; found = true; }
-                }
-            }
+    bool found = false;
+#pragma unroll
+    for (int k = 0; k < kBins; ++k) {
+        if (!found) {
+            acc += e[k];
+            if (acc >= target) { bin = k; found = true; }
         }
     }
-    // crystal: columns [0, crystalN)
-    float cm = -1e30f;
-    for (int c = 0; c < 64; c += 32) {
-        float v[32];
-        ld_cols(taddr, c, v);
-        for (int j = 0; j < 32; ++j)
-            if (c + j < sd.crystalN) cm = fmaxf(cm, v[j] + bias[c + j]);
-    }
-    float cs = 0.0f;
-    for (int c = 0; c < 64; c += 32) {
-        float v[32];
-        ld_cols(taddr, c, v);
-        for (int j = 0; j < 32; ++j)
-            if (c + j < sd.crystalN) cs += __expf(v[j] + bias[c + j] - cm);
-    }
-    int cry = sd.crystalN - 1;
-    {
-        const float target = uc * cs;
-        float acc = 0.0f;
-        bool found = false;
-        for (int c = 0; c < 64; c += 32) {
-            float v[32];
-            ld_cols(taddr, c, v);
-            for (int j = 0; j < 32; ++j)
-                if (c + j < sd.crystalN && !found) {
-                    acc += __expf(v[j] + bias[c + j] - cm);
-                    if (acc >= target) { cry = c + j; found = true; }
-                }
+    return bin;
+}
+
+// crystal: softmax over columns [0, ncry)
+__device__ __forceinline__ int sample_crystal(uint32_t taddr, const float* hb, int ncry, float uc)
+{
+    using namespace sg;
+    uint32_t a[32], b[32];
+    umma::tmem_ld32_nowait(taddr, a);
+    umma::tmem_ld32_nowait(taddr + 32, b);
+    umma::tmem_wait_ld();
+    float e[kCry];
+#pragma unroll
+    for (int k = 0; k < kCry; ++k) e[k] = __uint_as_float(k < 32 ? a[k] : b[k - 32]) + hb[k];
+    float mx = -1e30f;
+#pragma unroll
+    for (int k = 0; k < kCry; ++k)
+        if (k < ncry) mx = fmaxf(mx, e[k]);
+    float sum = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kCry; ++k) {
+        if (k < ncry) {
+            e[k] = __expf(e[k] - mx);
+            sum += e[k];
         }
     }
-    // depth: mixture columns [64, 76)
-    float depth_n;
-    {
-        float v[32];
-        ld_cols(taddr, 64, v);
-        float wm = -1e30f;
-        for (int k = 0; k < kMix; ++k) wm = fmaxf(wm, v[k] + bias[kColW + k]);
-        float ws = 0.0f;
-        for (int k = 0; k < kMix; ++k) ws += __expf(v[k] + bias[kColW + k] - wm);
-        int comp = kMix - 1;
-        float acc = 0.0f;
-        for (int k = 0; k < kMix; ++k) {
-            acc += __expf(v[k] + bias[kColW + k] - wm);
-            if (acc >= um * ws) { comp = k; break; }
+    const float target = uc * sum;
+    float acc = 0.0f;
+    int cry = ncry - 1;
+    bool found = false;
+#pragma unroll
+    for (int k = 0; k < kCry; ++k) {
+        if (k < ncry && !found) {
+            acc += e[k];
+            if (acc >= target) { cry = k; found = true; }
         }
-        const float mu = v[kColMu - 64 + comp] + bias[kColMu + comp];
-        const float ls = fminf(fmaxf(v[kColLs - 64 + comp] + bias[kColLs + comp], kLsMin), kLsMax);
-        depth_n = fminf(fmaxf(mu + __expf(ls) * zn, 0.0f), 1.0f);
     }
+    return cry;
+}
+
+// depth below the entry face over the panel depth: one component of the
+// Gaussian mixture in columns [64, 76), clamped to [0, 1]
+__device__ __forceinline__ float sample_depth(uint32_t taddr, const float* hb, float um, float zn)
+{
+    using namespace sg;
+    uint32_t a[16];
+    umma::tmem_ld16_nowait(taddr + 64, a);
+    umma::tmem_wait_ld();
+    float w[kMix];
+    float wm = -1e30f;
+#pragma unroll
+    for (int k = 0; k < kMix; ++k) {
+        w[k] = __uint_as_float(a[kColW - 64 + k]) + hb[kColW + k];
+        wm = fmaxf(wm, w[k]);
+    }
+    float ws = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kMix; ++k) {
+        w[k] = __expf(w[k] - wm);
+        ws += w[k];
+    }
+    int comp = kMix - 1;
+    float acc = 0.0f;
+    bool found = false;
+#pragma unroll
+    for (int k = 0; k < kMix; ++k) {
+        if (!found) {
+            acc += w[k];
+            if (acc >= um * ws) { comp = k; found = true; }
+        }
+    }
+    float mu = 0.0f, ls = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kMix; ++k)
+        if (k == comp) {
+            mu = __uint_as_float(a[kColMu - 64 + k]) + hb[kColMu + k];
+            ls = __uint_as_float(a[kColLs - 64 + k]) + hb[kColLs + k];
+        }
+    ls = fminf(fmaxf(ls, kLsMin), kLsMax);
+    return fminf(fmaxf(mu + __expf(ls) * zn, 0.0f), 1.0f);
+}
+
+// append the photon's pulse (deposit bin > 0), one atomic per warp
+__device__ __forceinline__ void append_pulse(const SurrogateDev& sd, const FwdInfer& in, bool valid, int sim,
+                                             int panel, int parn, int eid, int scat, float E, float ux, double t0,
+                                             int bin, int cry, float depth_n, float uw, int lane)
+{
+    using namespace sg;
+    const SimDesc& S = in.sims[valid ? sim : 0];
     const bool pulse = valid && bin > 0;
     const float Edep = bin == kBins - 1 ? E : ((float)bin + uw) * (1.0f / kBins) * E;
-    // append, one atomic per warp
     const unsigned m = __ballot_sync(0xffffffffu, pulse);
     unsigned long long base = 0;
     if (m) {
@@ -328,6 +367,11 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd(SurrogateDev sd, Fwd
     unsigned char* sB = sm + kSmemA;
     __shared__ __align__(8) uint64_t bar_ld, bar_mma;
     __shared__ uint32_t tbase;
+    // biases: hidden layers (halved for the tanh form of SiLU in inference), then the head
+    __shared__ float sbias[(kLayers - 1) * kHid + kOut];
+    // per tile (inference): the photon's stream and simulation, its sampled response
+    __shared__ int32_t s_parn[128], s_sim[128], s_bin[128], s_cry[128];
+    __shared__ float s_depth[128];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int64_t n;
     if (kTrain) {
@@ -345,6 +389,12 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd(SurrogateDev sd, Fwd
     if (warp == 0) {
         umma::tmem_alloc(&tbase, 256);
         umma::tmem_relinquish();
+    }
+    for (int i = threadIdx.x; i < (kLayers - 1) * kHid + kOut; i += blockDim.x) {
+        const int l = i < (kLayers - 1) * kHid ? i / kHid : kLayers - 1;
+        const int col = i - l * kHid;
+        const float b = sd.params[b_off(l) + col];
+        sbias[i] = (!kTrain && l < kLayers - 1) ? 0.5f * b : b;
     }
     umma::fence_before_sync();
     __syncthreads();
@@ -396,6 +446,10 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd(SurrogateDev sd, Fwd
             sim = in.q.i[4 * cap + j];
             features(sd, sd.params + kEmbOff, panel, y, z, ux, uy, uz, E, f);
         }
+        if (!kTrain && cq == 0) {
+            s_parn[rloc] = parn;
+            s_sim[rloc] = sim;
+        }
         if (cq == 0) {
             uint4 a, b;
             a.x = pack_bf16(f[0], f[1]); a.y = pack_bf16(f[2], f[3]); a.z = pack_bf16(f[4], f[5]);
@@ -437,31 +491,49 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd(SurrogateDev sd, Fwd
                     umma::bulk_g2s(sB + o, sd.img + img_off(l + 1) + o, bytes - o < 32768u ? bytes - o : 32768u,
                                    &bar_ld);
             }
-            const float* bias = sd.params + b_off(l);
+            const float* bias = sbias + l * kHid;
             if (l + 1 < kLayers) {
-                for (int c = 64 * cq; c < 64 * cq + 64; c += 32) {
-                    float v[32];
-                    ld_cols(taddr, c, v);
+                // this thread's 64 columns of its row: bias, SiLU, bf16, into the next layer's operand
+                const int c0 = 64 * cq;
+                uint32_t r0[32], r1[32];
+                umma::tmem_ld32_nowait(taddr + c0, r0);
+                umma::tmem_ld32_nowait(taddr + c0 + 32, r1);
+                umma::tmem_wait_ld();
+                auto chunk = [&](const uint32_t (&rr)[32], int c) {
                     uint32_t hp[16];
 #pragma unroll
                     for (int j = 0; j < 32; j += 2) {
-                        const float z0 = v[j] + bias[c + j], z1 = v[j + 1] + bias[c + j + 1];
-                        if (kTrain && valid) {
-                            float* zr = tr.Z + ((int64_t)l * tr.n + row) * kHid + c + j;
-                            zr[0] = z0;
-                            zr[1] = z1;
+                        const float v0 = __uint_as_float(rr[j]), v1 = __uint_as_float(rr[j + 1]);
+                        float a0, a1;
+                        if (kTrain) {
+                            const float z0 = v0 + bias[c + j], z1 = v1 + bias[c + j + 1];
+                            if (valid) {
+                                float* zr = tr.Z + ((int64_t)l * tr.n + row) * kHid + c + j;
+                                zr[0] = z0;
+                                zr[1] = z1;
+                            }
+                            a0 = silu(z0);
+                            a1 = silu(z1);
+                        } else {
+                            // z silu(z) = h + h tanh(h), h = z / 2 (bias already halved)
+                            const float h0 = fmaf(v0, 0.5f, bias[c + j]), h1 = fmaf(v1, 0.5f, bias[c + j + 1]);
+                            a0 = fmaf(h0, tanh_approx(h0), h0);
+                            a1 = fmaf(h1, tanh_approx(h1), h1);
                         }
-                        hp[j / 2] = pack_bf16(silu(z0), silu(z1));
+                        hp[j / 2] = pack_bf16(a0, a1);
                     }
                     if (kTrain && valid) {
                         uint4* dst = reinterpret_cast<uint4*>(tr.H + ((int64_t)l * tr.n + row) * kHid + c);
                         for (int q = 0; q < 4; ++q)
                             dst[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
                     }
+#pragma unroll
                     for (int q = 0; q < 4; ++q)
                         *reinterpret_cast<uint4*>(sA + umma::img_offset(rloc, c + 8 * q, 128)) =
                             make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
-                }
+                };
+                chunk(r0, c0);
+                chunk(r1, c0 + 32);
             } else if (kTrain) {
                 // chunks of 32 columns: quarter cq takes chunk cq, quarter 0 also chunk 4
                 for (int c = 32 * cq; c < kOut; c += 128) {
@@ -476,8 +548,29 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd(SurrogateDev sd, Fwd
             __syncthreads();
             umma::fence_after_sync();
         }
-        if (!kTrain && ok && cq == 0)
-            sample_and_append(sd, in, taddr, valid, sim, panel, parn, eid, scat, E, ux, t0, lane);
+        if (!kTrain && ok) {
+            // three warp groups sample the response of the tile's photons at once
+            const int prn = s_parn[rloc];
+            const SimDesc& S = in.sims[valid ? s_sim[rloc] : 0];
+            const float* hb = sbias + (kLayers - 1) * kHid;
+            Stream st;
+            st_init(st, S.key0, S.key1, kTagSurrogate, (uint64_t)(uint32_t)prn);
+            const float ue = st_u(st), uw = st_u(st), uc = st_u(st), um = st_u(st);
+            if (cq == 0) {
+                s_bin[rloc] = sample_energy(taddr, hb, ue);
+            } else if (cq == 1) {
+                s_cry[rloc] = sample_crystal(taddr, hb, sd.crystalN, uc);
+            } else if (cq == 2) {
+                const float zn = st_normal(st);
+                s_depth[rloc] = sample_depth(taddr, hb, um, zn);
+            }
+            umma::fence_before_sync();
+            __syncthreads();
+            umma::fence_after_sync();
+            if (cq == 0)
+                append_pulse(sd, in, valid, sim, panel, parn, eid, scat, E, ux, t0, s_bin[rloc], s_cry[rloc],
+                             s_depth[rloc], uw, lane);
+        }
         umma::fence_before_sync();
         __syncthreads();
         umma::fence_after_sync();
