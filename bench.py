@@ -446,9 +446,10 @@ def _chi2(a, b):
 
 def run_surrogate_workload(args):
     """The headline workload with the learned detector response: training on
-    entry records of independent Monte Carlo runs (untimed), then the same
-    acquisitions with and without the surrogate, timed like the headline,
-    and the two-sample chi-square of their singles spectra and crystal maps."""
+    entry records of independent Monte Carlo runs (untimed), then acquisitions
+    with and without the surrogate (independent seeds), timed like the
+    headline, and the two-sample chi-square of their singles spectra and
+    crystal maps."""
     import numpy as np
     import torch
     from gpet_gb300 import api
@@ -494,7 +495,7 @@ def run_surrogate_workload(args):
             for k in range(args.steps):
                 flush.zero_()
                 torch.cuda.synchronize()
-                ctx.set_option("seed", 20261203 + k)
+                ctx.set_option("seed", (20261203 if mode == "mc" else 40261203) + k)
                 st = ctx.run()
                 tot["ms"] += st["ms_total"]; tot["det"] += st["ms_detector"]; tot["sur"] += st["ms_surrogate"]
                 tot["coinc"] += st["n_coinc"]; tot["nsur"] += st["n_surrogate"]; tot["entered"] += st["n_entered"]
@@ -504,7 +505,7 @@ def run_surrogate_workload(args):
             res[mode] = (tot, hist_e, hist_c)
             ctx.close()
     mc, su = res["mc"][0], res["surrogate"][0]
-    flops = 2 * 236032 * su["nsur"]
+    flops = 2 * 252928 * su["nsur"]
     ach = flops / max(su["sur"] * 1e-3, 1e-12) / 1e12
     line = {"metric": METRIC.replace("(plain MC)", "(surrogate detector response)"),
             "value": su["coinc"] / (su["ms"] * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
@@ -523,7 +524,7 @@ def run_surrogate_workload(args):
                           "fraction_of_entered": su["nsur"] / max(1, su["entered"])},
             "roofline_mlp": {"kernel": "k_mlp_fwd<false>", "bound": "tensor", "achieved": ach, "peak": peak_t,
                              "unit": "TFLOP/s", "frac": ach / peak_t,
-                             "flops_per_photon": 2 * 236032},
+                             "flops_per_photon": 2 * 252928},
             "parity": {"singles_energy_350_650keV": _chi2(res["mc"][1], res["surrogate"][1]),
                        "singles_per_crystal": _chi2(res["mc"][2], res["surrogate"][2]),
                        "singles_mc": float(res["mc"][1].sum()), "singles_surrogate": float(res["surrogate"][1].sum()),
@@ -554,8 +555,8 @@ def main():
                     help="positron: the headline workload; batched64: 64 uneven simulations in one job; "
                          "surrogate: the headline workload with the learned detector response; "
                          "large: the whole-body configuration (48 panels, 256x256x512 phantom)")
-    ap.add_argument("--train-decays", type=int, default=20_000_000, help=argparse.SUPPRESS)
-    ap.add_argument("--train-epochs", type=int, default=3, help=argparse.SUPPRESS)
+    ap.add_argument("--train-decays", type=int, default=200_000_000, help=argparse.SUPPRESS)
+    ap.add_argument("--train-epochs", type=int, default=12, help=argparse.SUPPRESS)
     ap.add_argument("--batch-sims", type=int, default=64, help=argparse.SUPPRESS)
     args = ap.parse_args()
     args.set = dict(kv.split("=", 1) for kv in args.set)

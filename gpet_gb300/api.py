@@ -425,7 +425,7 @@ class Surrogate:
 
     def forward(self, rec):
         rec = np.ascontiguousarray(rec, ENTRY_DTYPE)
-        out = np.zeros((len(rec), 144), np.float32)
+        out = np.zeros((len(rec), 208), np.float32)
         self._ck(self.L.gpet_surrogate_forward(self.h, _ptr(rec), len(rec), _ptr(out)))
         return out
 

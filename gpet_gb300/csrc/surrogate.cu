@@ -1,10 +1,13 @@
 // surrogate.cu - the learned detector response (a new stage; the reference
 // always transports photons through the panels, gPET_kernals.cu:839-1233).
 //
-// Model: 14 inputs (entry point y, z in the panel, direction, energy, an
-// 8-wide learned panel embedding; padded to 16) -> 4 x 256 SiLU -> 140
-// outputs (64 crystal logits, a 4-component Gaussian mixture over the depth of
-// the pulse, 64 logits of the deposited-energy fraction; padded to 144).
+// Model: 16 inputs (entry point y, z in the panel, direction, energy, an
+// 8-wide learned panel embedding, the entry point's offset from the centre of
+// its crystal in y and z in pitches) -> 4 x 256 SiLU -> 204
+// outputs (two sets of 64 crystal logits, one per class of deposited energy,
+// a 4-component Gaussian mixture over the depth of the pulse, 64 logits of the
+// deposited-energy fraction; padded to 208). The crystal is drawn given the
+// energy bin: from the first set below bin kClassBin, else from the second.
 // BF16 weights and activations, FP32 accumulation in tensor memory.
 //
 //   k_mlp_fwd<train>  fused forward: one CTA of 512 threads per 128 samples
@@ -39,9 +42,10 @@ constexpr uint32_t kWaitLimit = 1u << 24;   // mbarrier polls before a wait give
 constexpr uint32_t kTagSurrogate = 6;       // Philox stream tag of the surrogate's draws
 
 namespace sg {
-constexpr int kIn = 16, kFeat = 14, kHid = 256, kOut = 144, kOutUsed = 140, kEmb = 8;
+constexpr int kIn = 16, kFeat = 16, kHid = 256, kOut = 208, kOutUsed = 204, kEmb = 8;
 constexpr int kCry = 64, kMix = 4, kBins = 64;
-constexpr int kColW = 64, kColMu = 68, kColLs = 72, kColE = 76;
+constexpr int kClassBin = 40;   // energy bins >= this (deposit >= 62.5 % of E) take the second crystal set
+constexpr int kColW = 128, kColMu = 132, kColLs = 136, kColE = 140;
 constexpr int kLayers = 5;
 constexpr float kLsMin = -7.0f, kLsMax = 3.0f;   // log sigma of a mixture component, clamped
 __host__ __device__ constexpr int fan_in(int l) { return l == 0 ? kIn : kHid; }
@@ -81,7 +85,9 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b)
     return (uint32_t)__bfloat16_as_ushort(x) | ((uint32_t)__bfloat16_as_ushort(y) << 16);
 }
 
-// 16 features of a photon entering a panel (the last two are zero)
+// 16 features of a photon entering a panel; the last two place the entry
+// point within its crystal (-0.5 .. 0.5 pitch from the crystal's centre), which
+// makes the entry crystal a linear function of the inputs
 __device__ __forceinline__ void features(const SurrogateDev& sd, const float* __restrict__ emb, int panel, float y,
                                          float z, float ux, float uy, float uz, float E, float f[16])
 {
@@ -92,8 +98,9 @@ __device__ __forceinline__ void features(const SurrogateDev& sd, const float* __
     f[4] = uz;
     f[5] = E * (1.0f / 511000.0f);
     for (int k = 0; k < sg::kEmb; ++k) f[6 + k] = emb[panel * sg::kEmb + k];
-    f[14] = 0.0f;
-    f[15] = 0.0f;
+    const float ty = (y + sd.half_y) / sd.cry_pitch_y, tz = (z + sd.half_z) / sd.cry_pitch_z;
+    f[14] = ty - floorf(ty) - 0.5f;
+    f[15] = tz - floorf(tz) - 0.5f;
 }
 
 // ---------------------------------------------------------------- self-test
@@ -188,20 +195,21 @@ __device__ __forceinline__ float tanh_approx(float x)
 // stream (tag 6, id = parn) in the fixed order ue, uw, uc, um, zn, skipping
 // the draws of the others. hb: the head's bias.
 
-// deposited-energy fraction bin: softmax over columns [76, 140)
+// deposited-energy fraction bin: softmax over columns [140, 204)
 __device__ __forceinline__ int sample_energy(uint32_t taddr, const float* hb, float ue)
 {
     using namespace sg;
+    static_assert(kColE >= 128 && kColE + kBins <= 208, "energy columns within the three loads");
     uint32_t a[32], b[32], c[16];
-    umma::tmem_ld32_nowait(taddr + 64, a);
-    umma::tmem_ld32_nowait(taddr + 96, b);
-    umma::tmem_ld16_nowait(taddr + 128, c);
+    umma::tmem_ld32_nowait(taddr + 128, a);
+    umma::tmem_ld32_nowait(taddr + 160, b);
+    umma::tmem_ld16_nowait(taddr + 192, c);
     umma::tmem_wait_ld();
     float e[kBins];
 #pragma unroll
     for (int k = 0; k < kBins; ++k) {
         const int col = kColE + k;
-        const uint32_t raw = col < 96 ? a[col - 64] : (col < 128 ? b[col - 96] : c[col - 128]);
+        const uint32_t raw = col < 160 ? a[col - 128] : (col < 192 ? b[col - 160] : c[col - 192]);
         e[k] = __uint_as_float(raw) + hb[col];
     }
     float mx = -1e30f;
@@ -227,17 +235,18 @@ __device__ __forceinline__ int sample_energy(uint32_t taddr, const float* hb, fl
     return bin;
 }
 
-// crystal: softmax over columns [0, ncry)
-__device__ __forceinline__ int sample_crystal(uint32_t taddr, const float* hb, int ncry, float uc)
+// crystal: softmax over the ncry columns of crystal set `set` ([64 set, 64 set + ncry))
+__device__ __forceinline__ int sample_crystal(uint32_t taddr, const float* hb, int set, int ncry, float uc)
 {
     using namespace sg;
+    const int c0 = kCry * set;
     uint32_t a[32], b[32];
-    umma::tmem_ld32_nowait(taddr, a);
-    umma::tmem_ld32_nowait(taddr + 32, b);
+    umma::tmem_ld32_nowait(taddr + c0, a);
+    umma::tmem_ld32_nowait(taddr + c0 + 32, b);
     umma::tmem_wait_ld();
     float e[kCry];
 #pragma unroll
-    for (int k = 0; k < kCry; ++k) e[k] = __uint_as_float(k < 32 ? a[k] : b[k - 32]) + hb[k];
+    for (int k = 0; k < kCry; ++k) e[k] = __uint_as_float(k < 32 ? a[k] : b[k - 32]) + hb[c0 + k];
     float mx = -1e30f;
 #pragma unroll
     for (int k = 0; k < kCry; ++k)
@@ -265,18 +274,19 @@ __device__ __forceinline__ int sample_crystal(uint32_t taddr, const float* hb, i
 }
 
 // depth below the entry face over the panel depth: one component of the
-// Gaussian mixture in columns [64, 76), clamped to [0, 1]
+// Gaussian mixture in columns [128, 140), clamped to [0, 1]
 __device__ __forceinline__ float sample_depth(uint32_t taddr, const float* hb, float um, float zn)
 {
     using namespace sg;
+    static_assert(kColW == 128 && kColLs + kMix <= 144, "mixture columns within one load");
     uint32_t a[16];
-    umma::tmem_ld16_nowait(taddr + 64, a);
+    umma::tmem_ld16_nowait(taddr + 128, a);
     umma::tmem_wait_ld();
     float w[kMix];
     float wm = -1e30f;
 #pragma unroll
     for (int k = 0; k < kMix; ++k) {
-        w[k] = __uint_as_float(a[kColW - 64 + k]) + hb[kColW + k];
+        w[k] = __uint_as_float(a[kColW - 128 + k]) + hb[kColW + k];
         wm = fmaxf(wm, w[k]);
     }
     float ws = 0.0f;
@@ -299,8 +309,8 @@ __device__ __forceinline__ float sample_depth(uint32_t taddr, const float* hb, f
 #pragma unroll
     for (int k = 0; k < kMix; ++k)
         if (k == comp) {
-            mu = __uint_as_float(a[kColMu - 64 + k]) + hb[kColMu + k];
-            ls = __uint_as_float(a[kColLs - 64 + k]) + hb[kColLs + k];
+            mu = __uint_as_float(a[kColMu - 128 + k]) + hb[kColMu + k];
+            ls = __uint_as_float(a[kColLs - 128 + k]) + hb[kColLs + k];
         }
     ls = fminf(fmaxf(ls, kLsMin), kLsMax);
     return fminf(fmaxf(mu + __expf(ls) * zn, 0.0f), 1.0f);
@@ -370,7 +380,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd(SurrogateDev sd, Fwd
     // biases: hidden layers (halved for the tanh form of SiLU in inference), then the head
     __shared__ float sbias[(kLayers - 1) * kHid + kOut];
     // per tile (inference): the photon's stream and simulation, its sampled response
-    __shared__ int32_t s_parn[128], s_sim[128], s_bin[128], s_cry[128];
+    __shared__ int32_t s_parn[128], s_sim[128], s_bin[128], s_cry[2][128];
     __shared__ float s_depth[128];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int64_t n;
@@ -535,7 +545,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd(SurrogateDev sd, Fwd
                 chunk(r0, c0);
                 chunk(r1, c0 + 32);
             } else if (kTrain) {
-                // chunks of 32 columns: quarter cq takes chunk cq, quarter 0 also chunk 4
+                // chunks of 32 columns: quarter cq takes chunks cq and cq + 4 (7 chunks)
                 for (int c = 32 * cq; c < kOut; c += 128) {
                     float v[32];
                     ld_cols(taddr, c, v);
@@ -549,7 +559,8 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd(SurrogateDev sd, Fwd
             umma::fence_after_sync();
         }
         if (!kTrain && ok) {
-            // three warp groups sample the response of the tile's photons at once
+            // the four warp groups sample the response of the tile's photons at
+            // once: energy bin, the crystal of each set, depth
             const int prn = s_parn[rloc];
             const SimDesc& S = in.sims[valid ? s_sim[rloc] : 0];
             const float* hb = sbias + (kLayers - 1) * kHid;
@@ -558,18 +569,20 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd(SurrogateDev sd, Fwd
             const float ue = st_u(st), uw = st_u(st), uc = st_u(st), um = st_u(st);
             if (cq == 0) {
                 s_bin[rloc] = sample_energy(taddr, hb, ue);
-            } else if (cq == 1) {
-                s_cry[rloc] = sample_crystal(taddr, hb, sd.crystalN, uc);
-            } else if (cq == 2) {
+            } else if (cq == 1 || cq == 3) {
+                s_cry[cq >> 1][rloc] = sample_crystal(taddr, hb, cq >> 1, sd.crystalN, uc);
+            } else {
                 const float zn = st_normal(st);
                 s_depth[rloc] = sample_depth(taddr, hb, um, zn);
             }
             umma::fence_before_sync();
             __syncthreads();
             umma::fence_after_sync();
-            if (cq == 0)
-                append_pulse(sd, in, valid, sim, panel, parn, eid, scat, E, ux, t0, s_bin[rloc], s_cry[rloc],
-                             s_depth[rloc], uw, lane);
+            if (cq == 0) {
+                const int bin = s_bin[rloc];
+                append_pulse(sd, in, valid, sim, panel, parn, eid, scat, E, ux, t0, bin,
+                             s_cry[bin >= kClassBin ? 1 : 0][rloc], s_depth[rloc], uw, lane);
+            }
         }
         umma::fence_before_sync();
         __syncthreads();
@@ -731,13 +744,16 @@ __global__ void k_loss(const float* __restrict__ out, int64_t n, const int32_t* 
                 d[kColE + k] = (expf(o[kColE + k] - lse) - (k == bin[i] ? 1.0f : 0.0f)) * scale;
         }
         if (cry[i] >= 0) {
+            // the crystal set of the sample's energy class
+            const int c0 = bin[i] >= kClassBin ? kCry : 0;
             float mx = -1e30f;
-            for (int k = 0; k < crystalN; ++k) mx = fmaxf(mx, o[k]);
+            for (int k = 0; k < crystalN; ++k) mx = fmaxf(mx, o[c0 + k]);
             float s = 0.0f;
-            for (int k = 0; k < crystalN; ++k) s += expf(o[k] - mx);
+            for (int k = 0; k < crystalN; ++k) s += expf(o[c0 + k] - mx);
             const float lse = mx + logf(s);
-            lsum += lse - o[cry[i]];
-            for (int k = 0; k < crystalN; ++k) d[k] = (expf(o[k] - lse) - (k == cry[i] ? 1.0f : 0.0f)) * scale;
+            lsum += lse - o[c0 + cry[i]];
+            for (int k = 0; k < crystalN; ++k)
+                d[c0 + k] = (expf(o[c0 + k] - lse) - (k == cry[i] ? 1.0f : 0.0f)) * scale;
             // depth: Gaussian mixture negative log likelihood
             const float x = dep[i];
             float lw[kMix], lp[kMix], ls[kMix], mu[kMix];
@@ -782,6 +798,14 @@ __global__ void k_loss(const float* __restrict__ out, int64_t n, const int32_t* 
 }
 
 // dZ = dH * SiLU'(Z), in place on dH
+// the batch's records, in the epoch's order, from the training set on the device
+__global__ void k_gather_records(const EntryRec* __restrict__ all, const uint32_t* __restrict__ order, int64_t n,
+                                 EntryRec* out)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = all[order[i]];
+}
+
 __global__ void k_silu_back(float* dH, const float* __restrict__ Z, int64_t count)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
@@ -816,8 +840,8 @@ __global__ void k_emb_grad(const float* __restrict__ dX, const int32_t* __restri
     }
 }
 
-// padding entries of the parameter vector (inputs 14, 15 of the first layer,
-// outputs 140..143 of the head) stay zero
+// padding entries of the parameter vector (first-layer inputs from kFeat on,
+// head outputs from kOutUsed on) stay zero
 __device__ __forceinline__ bool is_pad(int64_t i)
 {
     using namespace sg;
@@ -992,6 +1016,8 @@ struct gpet_surrogate {
     // training batch scratch
     int64_t cap = 0;
     Buf X, Z, H, out, dout, dA, dB, cry, dep, bin, pan, rec;
+    // training set on the device and the epoch's visiting order
+    Buf all, perm, epoch_loss;
 };
 
 namespace {
@@ -1089,7 +1115,10 @@ int gemm(gpet_surrogate* s, const Opnd& A, int64_t m_rows, const Opnd& B, int N,
 
 // forward + loss + backward of n samples already in s->rec; gradients into
 // s->grads (zeroed here), mean loss into *loss
-int loss_and_grad(gpet_surrogate* s, int64_t n, float* loss)
+// Loss and gradient of the n records in s->rec. loss != NULL: the batch mean
+// is returned and the stream synchronised; else the mean is added to
+// *acc_dev on the device and nothing waits (a training step).
+int loss_and_grad(gpet_surrogate* s, int64_t n, float* loss, float* acc_dev = nullptr)
 {
     using namespace sg;
     int rc = ensure_batch(s, n);
@@ -1107,10 +1136,10 @@ int loss_and_grad(gpet_surrogate* s, int64_t n, float* loss)
     SCK(cudaFuncSetAttribute(k_umma_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem));
     k_mlp_fwd<true><<<grid_cap(n, 128, 152), kFwdThreads, smem, st>>>(sd, tr, in, s->errflag.as<int>());
     SCK(cudaGetLastError());
-    SCK(cudaMemsetAsync(s->loss.p, 0, 4, st));
+    if (!acc_dev) SCK(cudaMemsetAsync(s->loss.p, 0, 4, st));
     SCK(cudaMemsetAsync(s->grads.p, 0, (size_t)s->nparam * 4, st));
     k_loss<<<g1, 256, 0, st>>>(s->out.as<float>(), n, s->cry.as<int32_t>(), s->dep.as<float>(), s->bin.as<int32_t>(),
-                               s->geom.crystalN, s->dout.as<float>(), s->loss.as<float>());
+                               s->geom.crystalN, s->dout.as<float>(), acc_dev ? acc_dev : s->loss.as<float>());
     SCK(cudaGetLastError());
     float* G = s->grads.as<float>();
     const __nv_bfloat16* Wb = s->wrow.as<__nv_bfloat16>();
@@ -1144,6 +1173,7 @@ int loss_and_grad(gpet_surrogate* s, int64_t n, float* loss)
             SCK(cudaGetLastError());
         }
     }
+    if (acc_dev) return GPET_OK;
     int herr = 0;
     SCK(cudaMemcpyAsync(&herr, s->errflag.p, 4, cudaMemcpyDeviceToHost, st));
     if (loss) SCK(cudaMemcpyAsync(loss, s->loss.p, 4, cudaMemcpyDeviceToHost, st));
@@ -1329,14 +1359,14 @@ int gpet_surrogate_grad(gpet_surrogate* s, const gpet_entry* rec, int64_t n, flo
     return GPET_OK;
 }
 
-int gpet_surrogate_forward(gpet_surrogate* s, const gpet_entry* rec, int64_t n, float* out144)
+int gpet_surrogate_forward(gpet_surrogate* s, const gpet_entry* rec, int64_t n, float* out208)
 {
-    if (!s || !rec || n < 1 || !out144) return GPET_ERR_ARG;
+    if (!s || !rec || n < 1 || !out208) return GPET_ERR_ARG;
     SCK(cudaSetDevice(s->device));
     float loss = 0.0f;
     int rc = gpet_surrogate_grad(s, rec, n, &loss, nullptr);
     if (rc) return rc;
-    SCK(cudaMemcpy(out144, s->out.p, (size_t)n * sg::kOut * 4, cudaMemcpyDeviceToHost));
+    SCK(cudaMemcpy(out208, s->out.p, (size_t)n * sg::kOut * 4, cudaMemcpyDeviceToHost));
     return GPET_OK;
 }
 
@@ -1344,38 +1374,58 @@ int gpet_surrogate_train(gpet_surrogate* s, const gpet_entry* rec, int64_t n, in
                          float lr, uint64_t seed, float* epoch_loss)
 {
     if (!s || !rec || n < 1 || epochs < 1 || batch < 128 || !(lr > 0.0f)) return GPET_ERR_ARG;
+    if (n > (int64_t)UINT32_MAX) return sfail(s, GPET_ERR_ARG, "at most 2^32 - 1 training records");
     SCK(cudaSetDevice(s->device));
     const int64_t B = std::min<int64_t>(batch, n);
     int rc = ensure_batch(s, B);
     if (rc) return rc;
-    // each epoch visits the records in a new shuffled order, in batches of B
-    std::vector<int64_t> order((size_t)n);
-    for (int64_t i = 0; i < n; ++i) order[(size_t)i] = i;
+    // the training set goes to the device once; each epoch uploads a new
+    // shuffled visiting order and the batches are gathered there
+    SCK(s->all.ensure((size_t)n * sizeof(EntryRec)));
+    SCK(s->perm.ensure((size_t)n * 4));
+    SCK(s->epoch_loss.ensure(4));
+    SCK(cudaMemcpyAsync(s->all.p, rec, (size_t)n * sizeof(EntryRec), cudaMemcpyHostToDevice, s->stream));
+    std::vector<uint32_t> order((size_t)n);
+    for (int64_t i = 0; i < n; ++i) order[(size_t)i] = (uint32_t)i;
     uint64_t st = seed;
-    std::vector<EntryRec> hb((size_t)B);
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    // learning rate: cosine from lr down to lr / 50 over the run's steps
+    const int64_t steps = (int64_t)epochs * (n / B);
+    int64_t step = 0;
+    const unsigned gb = (unsigned)std::min<int64_t>((B + 255) / 256, 152 * 8);
     for (int ep = 0; ep < epochs; ++ep) {
         for (int64_t i = n - 1; i > 0; --i) std::swap(order[(size_t)i], order[(size_t)(splitmix(st) % (uint64_t)(i + 1))]);
-        double lsum = 0.0;
+        // the previous epoch's batches read the order buffer until they are done
+        SCK(cudaStreamSynchronize(s->stream));
+        SCK(cudaMemcpyAsync(s->perm.p, order.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s->stream));
+        SCK(cudaMemsetAsync(s->epoch_loss.p, 0, 4, s->stream));
         int64_t nb = 0;
         for (int64_t b0 = 0; b0 + B <= n; b0 += B) {
-            for (int64_t k = 0; k < B; ++k) hb[(size_t)k] = reinterpret_cast<const EntryRec*>(rec)[order[(size_t)(b0 + k)]];
-            SCK(cudaMemcpyAsync(s->rec.p, hb.data(), (size_t)B * sizeof(EntryRec), cudaMemcpyHostToDevice, s->stream));
-            float l = 0.0f;
-            rc = loss_and_grad(s, B, &l);
+            k_gather_records<<<gb, 256, 0, s->stream>>>(s->all.as<EntryRec>(), s->perm.as<uint32_t>() + b0, B,
+                                                       s->rec.as<EntryRec>());
+            SCK(cudaGetLastError());
+            rc = loss_and_grad(s, B, nullptr, s->epoch_loss.as<float>());
             if (rc) return rc;
             s->adam_t++;
             const float c1 = 1.0f / (1.0f - std::pow(b1, (float)s->adam_t));
             const float c2 = 1.0f / (1.0f - std::pow(b2, (float)s->adam_t));
+            const double frac = steps > 1 ? (double)step / (double)(steps - 1) : 1.0;
+            const float lr_t = (float)(lr * (0.02 + 0.49 * (1.0 + std::cos(3.14159265358979 * frac))));
+            step++;
             k_adam<<<152 * 4, 256, 0, s->stream>>>(s->params.as<float>(), s->grads.as<float>(), s->adam_m.as<float>(),
-                                                   s->adam_v.as<float>(), s->nparam, lr, b1, b2, eps, c1, c2);
+                                                   s->adam_v.as<float>(), s->nparam, lr_t, b1, b2, eps, c1, c2);
             SCK(cudaGetLastError());
             rc = refresh_weights(s);
             if (rc) return rc;
-            lsum += l;
             nb++;
         }
-        if (epoch_loss) epoch_loss[ep] = nb ? (float)(lsum / nb) : 0.0f;
+        float lsum = 0.0f;
+        int herr = 0;
+        SCK(cudaMemcpyAsync(&lsum, s->epoch_loss.p, 4, cudaMemcpyDeviceToHost, s->stream));
+        SCK(cudaMemcpyAsync(&herr, s->errflag.p, 4, cudaMemcpyDeviceToHost, s->stream));
+        SCK(cudaStreamSynchronize(s->stream));
+        if (herr) return sfail(s, GPET_ERR_CUDA, "a tensor-core wait gave up");
+        if (epoch_loss) epoch_loss[ep] = nb ? lsum / (float)nb : 0.0f;
     }
     SCK(cudaStreamSynchronize(s->stream));
     return GPET_OK;

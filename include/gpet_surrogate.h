@@ -2,7 +2,7 @@
  *
  * No counterpart in the reference, which always transports each photon
  * through the panel crystals (photonde, gPET_kernals.cu:839-1233). An MLP
- * (14 inputs -> 4 x 256 SiLU -> 140 outputs, BF16 weights, FP32
+ * (16 inputs -> 4 x 256 SiLU -> 204 outputs, BF16 weights, FP32
  * accumulation on the tcgen05 tensor cores) maps a photon entering a panel to
  * its detector response; photons outside the domain it was validated on are
  * transported by the plain Monte Carlo. */
@@ -43,7 +43,7 @@ void gpet_surrogate_destroy(gpet_surrogate* s);
 const char* gpet_surrogate_last_error(gpet_surrogate* s);
 /* Parameters, fp32, in this order: for each layer l = 0..4 its weights
  * [out][in] then biases [out] (in: 16, 256, 256, 256, 256; out: 256, 256,
- * 256, 256, 144; input columns 14-15 and output rows 140-143 are padding
+ * 256, 256, 208; output rows 204-207 are padding
  * and stay zero), then the panel embedding [npanels][8]. */
 int64_t gpet_surrogate_param_count(gpet_surrogate* s);
 int gpet_surrogate_get_params(gpet_surrogate* s, float* out, int64_t n);
@@ -56,10 +56,15 @@ int gpet_surrogate_set_domain(gpet_surrogate* s, float e_lo, float e_hi, float m
 /* Mean loss of n records and its gradient (param_count floats, NULL: none)
  * at the current parameters; no update. */
 int gpet_surrogate_grad(gpet_surrogate* s, const gpet_entry* rec, int64_t n, float* loss, float* grad);
-/* Raw head outputs [n][144] of n records (for checks). */
-int gpet_surrogate_forward(gpet_surrogate* s, const gpet_entry* rec, int64_t n, float* out144);
+/* Raw head outputs [n][208] of n records (for checks): crystal logits of the
+ * partial-deposit class [0, 64) and of the near-full class [64, 128) (energy
+ * bin >= 40 of 64), mixture weights [128, 132), means [132, 136), log sigmas
+ * [136, 140), energy-fraction logits [140, 204). */
+int gpet_surrogate_forward(gpet_surrogate* s, const gpet_entry* rec, int64_t n, float* out208);
 /* Adam (beta 0.9, 0.999) over `epochs` shuffled passes in batches of
- * `batch`; epoch_loss[epochs] (may be NULL) receives each pass's mean loss. */
+ * `batch`, the learning rate falling from lr to lr / 50 along a cosine over
+ * the call's steps; epoch_loss[epochs] (may be NULL) receives each pass's
+ * mean loss. */
 int gpet_surrogate_train(gpet_surrogate* s, const gpet_entry* rec, int64_t n, int32_t epochs, int32_t batch,
                          float lr, uint64_t seed, float* epoch_loss);
 /* Use (s) or stop using (NULL) the surrogate in this context's runs; s must

@@ -13,9 +13,10 @@ Only tests import it.
 """
 import numpy as np
 
-IN, FEAT, HID, OUT, OUT_USED, EMB = 16, 14, 256, 144, 140, 8
+IN, FEAT, HID, OUT, OUT_USED, EMB = 16, 16, 256, 208, 204, 8
 CRY, MIX, BINS = 64, 4, 64
-COL_W, COL_MU, COL_LS, COL_E = 64, 68, 72, 76
+CLASS_BIN = 40          # energy bins >= this take the second crystal set (columns 64-127)
+COL_W, COL_MU, COL_LS, COL_E = 128, 132, 136, 140
 LAYERS = 5
 LS_MIN, LS_MAX = -7.0, 3.0
 
@@ -60,16 +61,31 @@ def bf16(x):
     return (((u + r) >> 16) << 16).astype(np.uint32).view(np.float32)
 
 
-def features(rec, emb, half_y, half_z):
+def default_pitch(half_y, half_z, crystal_n):
+    """Crystal pitch of a square module of crystal_n crystals without edge gaps."""
+    side = int(round(np.sqrt(crystal_n)))
+    return 2.0 * half_y / side, 2.0 * half_z / side
+
+
+def features(rec, emb, half_y, half_z, pitch):
+    """The 16 inputs: y, z over the half-widths, direction, E / 511 keV, the
+    panel embedding, the entry point's offset from its crystal's centre in
+    pitches (float32 arithmetic, as on the GPU)."""
     n = len(rec)
     f = np.zeros((n, IN), np.float64)
-    f[:, 0] = rec["y"].astype(np.float32) / np.float32(half_y)
-    f[:, 1] = rec["z"].astype(np.float32) / np.float32(half_z)
+    y = rec["y"].astype(np.float32)
+    z = rec["z"].astype(np.float32)
+    f[:, 0] = y / np.float32(half_y)
+    f[:, 1] = z / np.float32(half_z)
     f[:, 2] = rec["ux"]
     f[:, 3] = rec["uy"]
     f[:, 4] = rec["uz"]
     f[:, 5] = rec["E"].astype(np.float32) * np.float32(1.0 / 511000.0)
     f[:, 6:14] = emb[rec["panel"]]
+    ty = (y + np.float32(half_y)) / np.float32(pitch[0])
+    tz = (z + np.float32(half_z)) / np.float32(pitch[1])
+    f[:, 14] = ty - np.floor(ty) - np.float32(0.5)
+    f[:, 15] = tz - np.floor(tz) - np.float32(0.5)
     return f
 
 
@@ -109,12 +125,14 @@ def loss_and_dout(out, cry, dep, b, crystal_n):
     has = cry >= 0
     if has.any():
         i = np.nonzero(has)[0]
-        c = out[i, :crystal_n]
+        # the crystal set of each sample's energy class
+        cols = np.where(b[i] >= CLASS_BIN, CRY, 0)[:, None] + np.arange(crystal_n)[None, :]
+        c = out[i[:, None], cols]
         cl = _lse(c)
         loss += (cl[:, 0] - c[np.arange(len(i)), cry[i]]).sum()
         pc = np.exp(c - cl)
         pc[np.arange(len(i)), cry[i]] -= 1.0
-        d[i, :crystal_n] = pc
+        d[i[:, None], cols] = pc
         w = out[i, COL_W:COL_W + MIX]
         lw = w - _lse(w)
         mu = out[i, COL_MU:COL_MU + MIX]
@@ -134,12 +152,15 @@ def loss_and_dout(out, cry, dep, b, crystal_n):
     return loss / n, d / n
 
 
-def forward_backward(params, rec, npanels, half_y, half_z, depth_len, crystal_n, rounding=True):
-    """Loss, gradient (flat, like params) and head outputs of the records."""
+def forward_backward(params, rec, npanels, half_y, half_z, depth_len, crystal_n, rounding=True, pitch=None):
+    """Loss, gradient (flat, like params) and head outputs of the records;
+    pitch: the crystal pitch (y, z), default_pitch when None."""
     p = np.asarray(params, np.float64)
     Ws, bs, emb = unpack(p, npanels)
     r = bf16 if rounding else (lambda x: np.asarray(x, np.float64))
-    f = features(rec, emb, half_y, half_z)
+    if pitch is None:
+        pitch = default_pitch(half_y, half_z, crystal_n)
+    f = features(rec, emb, half_y, half_z, pitch)
     x = r(f).astype(np.float64)
     ins, Zs = [x], []
     h = x

@@ -21,10 +21,10 @@ def _loss(p, rec):
 def test_layout():
     lay, emb_off, total = S.offsets(NP)
     assert lay[0] == (0, 16 * 256)
-    assert emb_off == 238736
-    assert total == 238736 + NP * 8
-    macs = 14 * 256 + 3 * 256 * 256 + 256 * 140
-    assert macs == 236032
+    assert emb_off == 255184
+    assert total == 255184 + NP * 8
+    macs = 16 * 256 + 3 * 256 * 256 + 256 * 204
+    assert macs == 252928
 
 
 def test_backward_matches_finite_differences():
@@ -44,7 +44,7 @@ def test_backward_matches_finite_differences():
     picks += [emb_off + int(i) for i in rng.integers(0, NP * 8, 4)]
     # head columns of each kind: crystal, mixture weight / mean / log sigma, energy
     w4, b4 = lay[-1]
-    picks += [b4 + 3, b4 + S.COL_W + 1, b4 + S.COL_MU + 2, b4 + S.COL_LS + 3, b4 + S.COL_E + 5]
+    picks += [b4 + 3, b4 + S.CRY + 9, b4 + S.COL_W + 1, b4 + S.COL_MU + 2, b4 + S.COL_LS + 3, b4 + S.COL_E + 5]
     eps = 1e-6
     for i in picks:
         q = p.copy()
@@ -61,10 +61,22 @@ def test_padding_has_no_gradient():
     _, g, _ = S.forward_backward(p, rec, NP, HY, HZ, DEPTH, NCRY, rounding=False)
     lay, _, _ = S.offsets(NP)
     w0, b0 = lay[0]
-    assert not g[w0:b0].reshape(256, 16)[:, 14:].any()
+    assert not g[w0:b0].reshape(256, 16)[:, S.FEAT:].any()
     w4, b4 = lay[-1]
-    assert not g[w4:b4].reshape(144, 256)[140:].any()
-    assert not g[b4 + 140:b4 + 144].any()
+    assert not g[w4:b4].reshape(S.OUT, 256)[S.OUT_USED:].any()
+    assert not g[b4 + S.OUT_USED:b4 + S.OUT].any()
+
+
+def test_in_crystal_offset_features():
+    """Inputs 14, 15: the entry point's offset from its crystal's centre, in
+    pitches (crystal 0 starts at the panel edge)."""
+    rec = np.zeros(4, S.ENTRY_DTYPE)
+    rec["y"] = [-1.2, -1.05, 0.0, 1.1]
+    rec["z"] = [0.15, -0.6, 0.299, -1.2]
+    f = S.features(rec, np.zeros((1, S.EMB)), 1.2, 1.2, (0.3, 0.3))
+    assert np.allclose(f[:, 14], [-0.5, 0.0, -0.5, 0.1666667], atol=1e-5)
+    assert np.allclose(f[:, 15], [0.0, -0.5, 0.4966667, -0.5], atol=1e-5)
+    assert (np.abs(f[:, 14:]) <= 0.5).all()
 
 
 def test_bf16_rounding():
