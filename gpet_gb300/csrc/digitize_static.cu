@@ -96,15 +96,8 @@ void scan(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* aux, uint32_t*
 void sort(uint64_t*& ka, uint32_t*& va, uint64_t*& kb, uint32_t*& vb, int64_t n, int nbits, uint32_t* hist,
           uint32_t* aux, uint32_t* total, cudaStream_t s)
 {
-    if (n <= 1) return;
-    int64_t nb = (n + kDigiTile - 1) / kDigiTile;
-    for (int shift = 0; shift < nbits; shift += 8) {
-        k_radix_hist<<<(unsigned)nb, 256, 0, s>>>(ka, n, shift, hist, nb);
-        scan(hist, hist, 256 * nb, aux, total, s);
-        k_radix_scatter<<<(unsigned)nb, 256, 0, s>>>(ka, va, n, shift, hist, nb, kb, vb);
-        std::swap(ka, kb);
-        std::swap(va, vb);
-    }
+    int64_t launches = 0;
+    radix_sort(ka, va, kb, vb, n, nbits, hist, aux, total, s, &launches);
 }
 
 int set_err(char* err, int32_t len, int code, const char* msg)
@@ -182,27 +175,27 @@ extern "C" int gpet_digitize_static(const gpet_digi_params* prm, const gpet_even
 
     // the arena keeps the last call's contents: clear the counters
     cudaMemsetAsync(D.dcount, 0, 16 * sizeof(unsigned long long), s);
+    cudaMemsetAsync(D.dcount + 8, 0xFF, sizeof(unsigned long long), s);
     cudaMemsetAsync(d_cnt, 0, sizeof(Counters), s);
     cudaMemcpyAsync(d_prm, &dp, sizeof(DigiParams), cudaMemcpyHostToDevice, s);
-    unsigned long long hc[8] = {0};
+    unsigned long long hc[11] = {0};
     if (n > 0) {
         k_events_to_soa<<<grid256(n), 256, 0, s>>>(reinterpret_cast<const EventRec*>(d_pulses), d_scat, d_slot, n, P);
-        k_blur_threshold<<<grid256(n), 256, 0, s>>>(P, n, d_prm, D.Eb, D.xb, D.yb, D.zb, D.site, D.sel, D.dcount + 0);
+        k_blur_threshold<<<grid256(n), 256, 0, s>>>(P, n, d_prm, D.Eb, D.xb, D.yb, D.zb, D.site, D.sel, D.dcount + 0,
+                                                    D.dcount + 8);
     }
-    cudaMemcpyAsync(hc, D.dcount, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hc, D.dcount, sizeof(hc), cudaMemcpyDeviceToHost, s);
     if ((ce = cudaStreamSynchronize(s)) != cudaSuccess) return set_err(err, err_len, GPET_ERR_CUDA, cudaGetErrorString(ce));
     const int64_t m = (int64_t)hc[0];
     uint32_t* total = reinterpret_cast<uint32_t*>(D.dcount + 4);
     uint64_t *ka = D.key_a, *kb = D.key_b;
     uint32_t *va = D.idx_a, *vb = D.idx_b;
     if (m > 0) {
-        k_time_keys<<<grid256(m), 256, 0, s>>>(D.sel, m, P.t, ka, va);
-        sort(ka, va, kb, vb, m, 64, D.hist, D.scan_aux, total, s);
-        k_tie_fix<<<grid256(m), 256, 0, s>>>(ka, va, m, P.parn, P.meta);
+        const int tbits = launch_time_keys(D.sel, m, P.t, hc + 8, ka, va, s);
+        sort(ka, va, kb, vb, m, tbits, D.hist, D.scan_aux, total, s);
+        k_tie_fix<<<grid256(m), 256, 0, s>>>(ka, va, m, P.t, P.parn, P.meta);
         cudaMemcpyAsync(D.torder, va, sizeof(uint32_t) * m, cudaMemcpyDeviceToDevice, s);
-        int site_bits = 8;
-        const int64_t maxsite = (int64_t)prm->moduleN * prm->crystalN * kMaxPanels;
-        while (site_bits < 32 && (1ll << site_bits) <= maxsite) site_bits += 8;
+        const int site_bits = site_key_bits(hc[10]);
         k_site_keys<<<grid256(m), 256, 0, s>>>(D.torder, m, D.site, nullptr, ka, va);
         sort(ka, va, kb, vb, m, site_bits, D.hist, D.scan_aux, total, s);
         k_deadtime<<<grid256(m), 256, 0, s>>>(va, m, D.site, nullptr, P.t, d_prm, D.flags, d_cnt);

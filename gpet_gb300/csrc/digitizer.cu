@@ -15,6 +15,8 @@
 //   coincidences          one thread per cluster of singles closer than the
 //                         window; pair counts, scan, write
 #include <algorithm>
+#include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "kernels.h"
@@ -23,6 +25,12 @@
 namespace gpet {
 
 constexpr int kTile = 4096;      // items per block in radix / scan kernels
+// time keys: (t - tmin) quantised to 48 bits over the survivors' time span
+// (6 radix passes instead of 8); runs of equal keys are ordered by t after
+constexpr int kTimeKeyBits = 48;
+constexpr uint64_t kTimeKeyMax = (1ull << kTimeKeyBits) - 1;
+
+static unsigned grid_for(int64_t n, int threads);
 constexpr int kScanThreads = 1024;
 
 // ---------------------------------------------------------------- scan
@@ -149,67 +157,115 @@ __global__ void __launch_bounds__(256) k_radix_hist(const uint64_t* __restrict__
     hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
 }
 
-// stable scatter: items of a tile keep their order within a digit
+// stable scatter: items of a tile keep their order within a digit. The tile
+// is first reordered by digit in shared memory, then written out in that
+// order, so the threads of a warp write consecutive addresses of a digit's
+// run instead of 32 scattered ones.
+constexpr int kScatterSmem = kTile * (8 + 4);   // the tile's keys and values
+
 __global__ void __launch_bounds__(256) k_radix_scatter(const uint64_t* __restrict__ kin,
                                                        const uint32_t* __restrict__ vin, int64_t n, int shift,
                                                        const uint32_t* __restrict__ off, int64_t nblocks,
                                                        uint64_t* __restrict__ kout, uint32_t* __restrict__ vout)
 {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    uint64_t* sk = reinterpret_cast<uint64_t*>(dsm);
+    uint32_t* sv = reinterpret_cast<uint32_t*>(dsm + kTile * 8);
     __shared__ uint32_t run[256];
     __shared__ uint32_t wc[8][256];
+    __shared__ uint32_t soff[256];   // where this tile's run of digit d starts in the output
+    __shared__ uint32_t toff[256];   // where it starts within the tile
+    __shared__ uint32_t wsum[8];
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     unsigned lt;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
-    run[tid] = 0;
     const int64_t base = (int64_t)blockIdx.x * kTile;
-    const uint32_t goff = off[(int64_t)tid * nblocks + blockIdx.x];
-    __shared__ uint32_t soff[256];
-    soff[tid] = goff;
+    const int ntile = (int)(n - base < kTile ? n - base : kTile);
+    // the tile's count of digit tid: the scanned histogram is digit-major, so
+    // its next entry is this one plus that count (n after the last)
+    const int64_t fi = (int64_t)tid * nblocks + blockIdx.x;
+    const uint32_t g0 = off[fi];
+    const uint32_t cnt = (fi + 1 < 256 * nblocks ? off[fi + 1] : (uint32_t)n) - g0;
+    soff[tid] = g0;
+    run[tid] = 0;
+    uint32_t v = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) wsum[w] = v;
+    __syncthreads();
+    uint32_t add0 = 0;
+    for (int ww = 0; ww < w; ++ww) add0 += wsum[ww];
+    toff[tid] = v - cnt + add0;
     for (int r = 0; r < kTile / 256; ++r) {
 #pragma unroll
         for (int ww = 0; ww < 8; ++ww) wc[ww][tid] = 0;
         __syncthreads();
-        const int64_t i = base + (int64_t)r * 256 + tid;
-        const bool valid = i < n;
-        uint64_t key = valid ? kin[i] : 0ull;
-        uint32_t val = valid ? vin[i] : 0u;
-        uint32_t dig = valid ? (uint32_t)((key >> shift) & 255u) : 256u;
-        unsigned peers = __match_any_sync(0xffffffffu, dig);
-        uint32_t rank = __popc(peers & lt);
+        const int li = r * 256 + tid;
+        const bool valid = li < ntile;
+        const uint64_t key = valid ? kin[base + li] : 0ull;
+        const uint32_t val = valid ? vin[base + li] : 0u;
+        const uint32_t dig = valid ? (uint32_t)((key >> shift) & 255u) : 256u;
+        const unsigned peers = __match_any_sync(0xffffffffu, dig);
+        const uint32_t rank = __popc(peers & lt);
         if (valid && rank == 0) wc[w][dig] = __popc(peers);
         __syncthreads();
         if (valid) {
             uint32_t pre = run[dig] + rank;
             for (int ww = 0; ww < w; ++ww) pre += wc[ww][dig];
-            const uint32_t pos = soff[dig] + pre;
-            kout[pos] = key;
-            vout[pos] = val;
+            const uint32_t lp = toff[dig] + pre;
+            sk[lp] = key;
+            sv[lp] = val;
         }
         __syncthreads();
         uint32_t add = 0;
 #pragma unroll
         for (int ww = 0; ww < 8; ++ww) add += wc[ww][tid];
         run[tid] += add;
-        __syncthreads();
-        (void)lane;
+    }
+    __syncthreads();
+    for (int li = tid; li < ntile; li += 256) {
+        const uint64_t key = sk[li];
+        const uint32_t dig = (uint32_t)((key >> shift) & 255u);
+        const uint32_t pos = soff[dig] + ((uint32_t)li - toff[dig]);
+        kout[pos] = key;
+        vout[pos] = sv[li];
     }
 }
 
 // sort (keys, vals) of length n by bits [0, nbits) of key, stably; result in
-// (ka, va) on return (the buffers are ping-ponged an even number of times)
-static void radix_sort(uint64_t*& ka, uint32_t*& va, uint64_t*& kb, uint32_t*& vb, int64_t n, int nbits,
-                       uint32_t* hist, uint32_t* aux, uint32_t* total, cudaStream_t s, int64_t* launches)
+// (ka, va) on return (the buffers are ping-ponged)
+void radix_sort(uint64_t*& ka, uint32_t*& va, uint64_t*& kb, uint32_t*& vb, int64_t n, int nbits, uint32_t* hist,
+                uint32_t* aux, uint32_t* total, cudaStream_t s, int64_t* launches)
 {
     if (n <= 1) return;
+    cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, kScatterSmem);
     int64_t nb = (n + kTile - 1) / kTile;
     for (int shift = 0; shift < nbits; shift += 8) {
         k_radix_hist<<<(unsigned)nb, 256, 0, s>>>(ka, n, shift, hist, nb);
         scan_exclusive(hist, hist, 256 * nb, aux, total, s, launches);
-        k_radix_scatter<<<(unsigned)nb, 256, 0, s>>>(ka, va, n, shift, hist, nb, kb, vb);
+        k_radix_scatter<<<(unsigned)nb, 256, kScatterSmem, s>>>(ka, va, n, shift, hist, nb, kb, vb);
         *launches += 2;
         std::swap(ka, kb);
         std::swap(va, vb);
     }
+}
+
+// order-preserving unsigned image of a double (negative values included)
+__device__ __forceinline__ unsigned long long ordered_bits(double t)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(t);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+static double from_ordered_bits(unsigned long long o)
+{
+    const unsigned long long u = (o >> 63) ? (o & 0x7fffffffffffffffull) : ~o;
+    double t;
+    std::memcpy(&t, &u, 8);
+    return t;
 }
 
 // ---------------------------------------------------------------- stages
@@ -218,13 +274,17 @@ __device__ __forceinline__ int pulse_sim(const PulseDev& P, int64_t i) { return 
 // blur (gPET_kernals.cu:814-837) + threshold (energywindow :641-656 with
 // [Eth, 2 MeV]); survivors' pulse indices appended to sel, site stored.
 // Parameters per simulation: prms[sim].
+// range[0], range[1]: smallest and largest ordered_bits of the survivors'
+// times, range[2]: their largest site (as unsigned); one atomic per block each
 __global__ void k_blur_threshold(PulseDev P, int64_t n, const DigiParams* __restrict__ prms, float* Eb, float* xb,
-                                 float* yb, float* zb, int32_t* site, uint32_t* sel, unsigned long long* nsel)
+                                 float* yb, float* zb, int32_t* site, uint32_t* sel, unsigned long long* nsel,
+                                 unsigned long long* range)
 {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
     unsigned lt;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    unsigned long long tlo = ~0ull, thi = 0ull, smax = 0ull;
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
         const int64_t i = base + threadIdx.x;
         bool keep = false;
@@ -259,6 +319,12 @@ __global__ void k_blur_threshold(PulseDev P, int64_t n, const DigiParams* __rest
             default: sv = P.siten[i]; break;
             }
             site[i] = sv;
+            if (keep) {
+                const unsigned long long o = ordered_bits(P.t[i]);
+                tlo = o < tlo ? o : tlo;
+                thi = o > thi ? o : thi;
+                smax = (unsigned long long)(uint32_t)sv > smax ? (unsigned long long)(uint32_t)sv : smax;
+            }
         }
         unsigned m = __ballot_sync(0xffffffffu, keep);
         if (m) {
@@ -269,21 +335,60 @@ __global__ void k_blur_threshold(PulseDev P, int64_t n, const DigiParams* __rest
             if (keep) sel[b + __popc(m & lt)] = (uint32_t)i;
         }
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long x = __shfl_xor_sync(0xffffffffu, tlo, o);
+        const unsigned long long y = __shfl_xor_sync(0xffffffffu, thi, o);
+        const unsigned long long z = __shfl_xor_sync(0xffffffffu, smax, o);
+        tlo = x < tlo ? x : tlo;
+        thi = y > thi ? y : thi;
+        smax = z > smax ? z : smax;
+    }
+    __shared__ unsigned long long red[3][32];
+    const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) {
+        red[0][w] = tlo;
+        red[1][w] = thi;
+        red[2][w] = smax;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < nw; ++k) {
+            tlo = red[0][k] < tlo ? red[0][k] : tlo;
+            thi = red[1][k] > thi ? red[1][k] : thi;
+            smax = red[2][k] > smax ? red[2][k] : smax;
+        }
+        if (thi) {
+            atomicMin(&range[0], tlo);
+            atomicMax(&range[1], thi);
+            atomicMax(&range[2], smax);
+        }
+    }
 }
 
-__global__ void k_time_keys(const uint32_t* __restrict__ sel, int64_t m, const double* __restrict__ t,
-                            uint64_t* key, uint32_t* val)
+// time keys: with quant, floor((t - tmin) * scale) (at most 48 bits; t >=
+// tmin for every selected pulse, and the key is monotone in t), else the
+// IEEE bits of t (non-negative times order like their bits)
+__global__ void k_time_keys(const uint32_t* __restrict__ sel, int64_t m, const double* __restrict__ t, int quant,
+                            double tmin, double scale, uint64_t* key, uint32_t* val)
 {
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
-        uint32_t p = sel[j];
-        key[j] = (uint64_t)__double_as_longlong(t[p]);
+        const uint32_t p = sel[j];
+        if (quant) {
+            const double x = (t[p] - tmin) * scale;
+            uint64_t q = x > 0.0 ? (uint64_t)x : 0ull;
+            key[j] = q > kTimeKeyMax ? kTimeKeyMax : q;
+        } else {
+            key[j] = (uint64_t)__double_as_longlong(t[p]);
+        }
         val[j] = p;
     }
 }
 
-// order runs of equal t by (parn, slot)
-__global__ void k_tie_fix(const uint64_t* __restrict__ key, uint32_t* idx, int64_t m, const int32_t* __restrict__ parn,
-                          const uint8_t* __restrict__ meta)
+// order each run of equal keys by (t, parn, slot) (quantised keys can join
+// different times; equal IEEE keys are equal times)
+__global__ void k_tie_fix(const uint64_t* __restrict__ key, uint32_t* idx, int64_t m, const double* __restrict__ t,
+                          const int32_t* __restrict__ parn, const uint8_t* __restrict__ meta)
 {
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
         if (j > 0 && key[j] == key[j - 1]) continue;
@@ -291,19 +396,42 @@ __global__ void k_tie_fix(const uint64_t* __restrict__ key, uint32_t* idx, int64
         int64_t e = j + 1;
         while (e < m && key[e] == key[j]) e++;
         for (int64_t a = j + 1; a < e; ++a) {
-            uint32_t v = idx[a];
-            uint64_t kv = ((uint64_t)(uint32_t)parn[v] << 8) | (meta[v] & 0x7fu);
+            const uint32_t v = idx[a];
+            const double tv = t[v];
+            const uint64_t kv = ((uint64_t)(uint32_t)parn[v] << 8) | (meta[v] & 0x7fu);
             int64_t b = a - 1;
             while (b >= j) {
-                uint32_t u = idx[b];
-                uint64_t ku = ((uint64_t)(uint32_t)parn[u] << 8) | (meta[u] & 0x7fu);
-                if (ku <= kv) break;
+                const uint32_t u = idx[b];
+                const double tu = t[u];
+                const uint64_t ku = ((uint64_t)(uint32_t)parn[u] << 8) | (meta[u] & 0x7fu);
+                if (tu < tv || (tu == tv && ku <= kv)) break;
                 idx[b + 1] = u;
                 b--;
             }
             idx[b + 1] = v;
         }
     }
+}
+
+// keys of the time order of the m selected pulses from the survivors' time
+// range (host copy of k_blur_threshold's range[0..1]); returns the key bits
+int launch_time_keys(const uint32_t* sel, int64_t m, const double* t, const unsigned long long* range,
+                     uint64_t* key, uint32_t* val, cudaStream_t s)
+{
+    const double tmin = from_ordered_bits(range[0]), tmax = from_ordered_bits(range[1]);
+    const double span = tmax - tmin;
+    const double scale = (double)kTimeKeyMax / span;
+    const bool quant = m > 1 && span > 0.0 && std::isfinite(span) && std::isfinite(scale);
+    k_time_keys<<<grid_for(m, 256), 256, 0, s>>>(sel, m, t, quant ? 1 : 0, tmin, quant ? scale : 0.0, key, val);
+    return quant ? kTimeKeyBits : 64;
+}
+
+// bits of the site keys for sites up to smax
+int site_key_bits(unsigned long long smax)
+{
+    int bits = 8;
+    while (bits < 32 && (1ull << bits) <= smax) bits += 8;
+    return bits;
 }
 
 // keys for the stable sort of the time order by simulation
@@ -697,22 +825,23 @@ int sinogram_device(const int64_t* pairs, const uint8_t* klass, int64_t c0, int6
     return cudaGetLastError() == cudaSuccess ? 0 : GPET_ERR_CUDA;
 }
 
-int digitize_device(const PulseDev& P, int64_t n, const DigiParams* d_prms, int nsims, int64_t max_site,
-                    DigiScratch& D, Counters* d_cnt, cudaStream_t s, int64_t* launches, int64_t* n_singles_out,
-                    int64_t* n_coinc_out)
+int digitize_device(const PulseDev& P, int64_t n, const DigiParams* d_prms, int nsims, DigiScratch& D,
+                    Counters* d_cnt, cudaStream_t s, int64_t* launches, int64_t* n_singles_out, int64_t* n_coinc_out)
 {
     // dcount: [0] selected [2] singles (uint32, scan total) [4] scratch scan total
-    unsigned long long hc[4] = {0, 0, 0, 0};
-    cudaMemsetAsync(D.dcount, 0, 8 * sizeof(unsigned long long), s);
+    // [8], [9] survivors' time range (ordered bits) [10] their largest site
+    unsigned long long hc[11] = {0};
+    cudaMemsetAsync(D.dcount, 0, 16 * sizeof(unsigned long long), s);
+    cudaMemsetAsync(D.dcount + 8, 0xFF, sizeof(unsigned long long), s);
     const int32_t* psim = nsims > 1 ? P.sim : nullptr;
     PulseDev Pv = P;
     Pv.sim = const_cast<int32_t*>(psim);
     if (n > 0) {
         k_blur_threshold<<<grid_for(n, 256), 256, 0, s>>>(Pv, n, d_prms, D.Eb, D.xb, D.yb, D.zb, D.site, D.sel,
-                                                          D.dcount + 0);
+                                                          D.dcount + 0, D.dcount + 8);
         ++*launches;
     }
-    cudaMemcpyAsync(hc, D.dcount, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hc, D.dcount, sizeof(hc), cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return GPET_ERR_CUDA;
     const int64_t m = (int64_t)hc[0];
     uint32_t* total = reinterpret_cast<uint32_t*>(D.dcount + 4);
@@ -723,10 +852,10 @@ int digitize_device(const PulseDev& P, int64_t n, const DigiParams* d_prms, int 
     uint64_t *ka = D.key_a, *kb = D.key_b;
     uint32_t *va = D.idx_a, *vb = D.idx_b;
     if (m > 0) {
-        k_time_keys<<<grid_for(m, 256), 256, 0, s>>>(D.sel, m, P.t, ka, va);
+        const int tbits = launch_time_keys(D.sel, m, P.t, hc + 8, ka, va, s);
         ++*launches;
-        radix_sort(ka, va, kb, vb, m, 64, D.hist, D.scan_aux, total, s, launches);
-        k_tie_fix<<<grid_for(m, 256), 256, 0, s>>>(ka, va, m, P.parn, P.meta);
+        radix_sort(ka, va, kb, vb, m, tbits, D.hist, D.scan_aux, total, s, launches);
+        k_tie_fix<<<grid_for(m, 256), 256, 0, s>>>(ka, va, m, P.t, P.parn, P.meta);
         ++*launches;
         if (psim) {   // (simulation, t, parn, slot)
             k_sim_keys<<<grid_for(m, 256), 256, 0, s>>>(va, m, psim, ka, va);
@@ -740,9 +869,7 @@ int digitize_device(const PulseDev& P, int64_t n, const DigiParams* d_prms, int 
             k_add_count<<<1, 1, 0, s>>>(d_cnt, CF(n_thr), (unsigned long long)m);
         }
         // site order
-        int site_bits = 8;
-        while (site_bits < 32 && (1ll << site_bits) <= max_site) site_bits += 8;
-        if (psim) site_bits = 32 + sim_bits;
+        const int site_bits = psim ? 32 + sim_bits : site_key_bits(hc[10]);
         k_site_keys<<<grid_for(m, 256), 256, 0, s>>>(D.torder, m, D.site, psim, ka, va);
         *launches += 2;
         radix_sort(ka, va, kb, vb, m, site_bits, D.hist, D.scan_aux, total, s, launches);

@@ -903,7 +903,7 @@ static int add_noise(gpet_ctx* c, Work& W, gpet_ctx* const* cs, int nsim, int64_
 
 // digitize W's pulses for nsims simulations with parameters prms (host),
 // leaving per-simulation counts in W.hcnt and result offsets in W.s_off/c_off
-static int digitize_work(gpet_ctx* c, Work& W, const std::vector<DigiParams>& prms, int64_t max_site,
+static int digitize_work(gpet_ctx* c, Work& W, const std::vector<DigiParams>& prms,
                          gpet_run_stats* st, float* ms_digi)
 {
     const int n = (int)prms.size();
@@ -914,7 +914,7 @@ static int digitize_work(gpet_ctx* c, Work& W, const std::vector<DigiParams>& pr
     PulseDev P = pulse_view(W);
     cudaEventRecord(c->ev[4], c->stream);
     int64_t ns = 0, nc = 0;
-    rc = digitize_device(P, W.n_digi, W.prms.as<DigiParams>(), n, max_site, W.dg, W.cnt.as<Counters>(), c->stream,
+    rc = digitize_device(P, W.n_digi, W.prms.as<DigiParams>(), n, W.dg, W.cnt.as<Counters>(), c->stream,
                          &st->kernel_launches, &ns, &nc);
     if (rc) return fail(c, rc, std::string("digitizer failed: ") + cudaGetErrorString(cudaGetLastError()));
     cudaEventRecord(c->ev[5], c->stream);
@@ -1041,7 +1041,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     // nothing of an earlier run may still use the work buffers
     CK(cudaStreamSynchronize(c->stream2));
     std::vector<int64_t> nd(nsim);
-    int64_t ND = 0, max_site = 1;
+    int64_t ND = 0;
     bool rec_hits = false;
     size_t smem = 0;
     for (int s = 0; s < nsim; ++s) {
@@ -1051,7 +1051,6 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         if (limit >= 0) nd[s] = std::min(nd[s], limit);
         ND += nd[s];
         rec_hits = rec_hits || cs[s]->record_hits;
-        max_site = std::max<int64_t>(max_site, (int64_t)cs[s]->geo.npanels * cs[s]->geo.moduleN * cs[s]->geo.crystalN);
         smem = std::max(smem, (size_t)cs[s]->geo.npanels * kPanelStride * 4);
     }
     Work& W = fresh_work(c);
@@ -1426,7 +1425,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     rc = add_noise(c, W, cs, nsim, &tot.kernel_launches);
     if (rc) return rc;
     float ms_digi = 0;
-    rc = digitize_work(c, W, prms, max_site, &tot, &ms_digi);
+    rc = digitize_work(c, W, prms, &tot, &ms_digi);
     if (rc) return rc;
     cudaEventRecord(c->ev[3], c->stream);
     CK(cudaEventSynchronize(c->ev[3]));
@@ -1651,9 +1650,8 @@ int gpet_digitize(gpet_ctx* c, const gpet_event* ev, const uint8_t* scat, const 
     rc = add_noise(c, W, one, 1, &st->kernel_launches);
     if (rc) return rc;
     std::vector<DigiParams> prms(1, digi_params(c));
-    int64_t max_site = std::max<int64_t>(1, (int64_t)c->geo.npanels * c->geo.moduleN * c->geo.crystalN);
     float ms_digi = 0;
-    rc = digitize_work(c, W, prms, max_site, st, &ms_digi);
+    rc = digitize_work(c, W, prms, st, &ms_digi);
     if (rc) return rc;
     fill_stats(W.hcnt[0], st);
     st->n_pulses = n;

@@ -218,9 +218,18 @@ __global__ void k_radix_hist(const uint64_t* keys, int64_t n, int shift, uint32_
 __global__ void k_radix_scatter(const uint64_t* kin, const uint32_t* vin, int64_t n, int shift, const uint32_t* off,
                                 int64_t nblocks, uint64_t* kout, uint32_t* vout);
 __global__ void k_blur_threshold(PulseDev P, int64_t n, const DigiParams* prms, float* Eb, float* xb, float* yb,
-                                 float* zb, int32_t* site, uint32_t* sel, unsigned long long* nsel);
-__global__ void k_time_keys(const uint32_t* sel, int64_t m, const double* t, uint64_t* key, uint32_t* val);
-__global__ void k_tie_fix(const uint64_t* key, uint32_t* idx, int64_t m, const int32_t* parn, const uint8_t* meta);
+                                 float* zb, int32_t* site, uint32_t* sel, unsigned long long* nsel,
+                                 unsigned long long* range);
+__global__ void k_tie_fix(const uint64_t* key, uint32_t* idx, int64_t m, const double* t, const int32_t* parn,
+                          const uint8_t* meta);
+// host side of the sorts: stable LSD radix sort by bits [0, nbits) (8 per
+// pass; result in ka, va), the time keys of the selected pulses (returns the
+// key width), the site key width for sites up to smax
+void radix_sort(uint64_t*& ka, uint32_t*& va, uint64_t*& kb, uint32_t*& vb, int64_t n, int nbits, uint32_t* hist,
+                uint32_t* aux, uint32_t* total, cudaStream_t s, int64_t* launches);
+int launch_time_keys(const uint32_t* sel, int64_t m, const double* t, const unsigned long long* range,
+                     uint64_t* key, uint32_t* val, cudaStream_t s);
+int site_key_bits(unsigned long long smax);
 __global__ void k_site_keys(const uint32_t* torder, int64_t m, const int32_t* site, const int32_t* psim,
                             uint64_t* key, uint32_t* val);
 __global__ void k_deadtime(const uint32_t* sorder, int64_t m, const int32_t* site, const int32_t* psim,
@@ -280,9 +289,8 @@ int sinogram_device(const int64_t* pairs, const uint8_t* klass, int64_t c0, int6
 // digitized in one pass with parameters d_prms[sim] (device); singles come out
 // in (simulation, t) order in D.single_idx, coincidences in D.coinc_*,
 // per-simulation counts in d_cnt[sim]. `launches` accumulates kernel launches.
-// max_site bounds every site number (panels x modules x crystals).
-int digitize_device(const PulseDev& P, int64_t n, const DigiParams* d_prms, int nsims, int64_t max_site,
-                    DigiScratch& D, Counters* d_cnt, cudaStream_t s, int64_t* launches, int64_t* n_singles_out,
-                    int64_t* n_coinc_out);
+// D.dcount needs 16 entries.
+int digitize_device(const PulseDev& P, int64_t n, const DigiParams* d_prms, int nsims, DigiScratch& D,
+                    Counters* d_cnt, cudaStream_t s, int64_t* launches, int64_t* n_singles_out, int64_t* n_coinc_out);
 
 }  // namespace gpet
