@@ -93,6 +93,34 @@ def test_positron_spectrum_mean(oracle_mod, data_dir):
     assert KAT["positron_mean_kinetic_MeV"][0] == pytest.approx(0.2756, abs=2e-3)
 
 
+def test_positron_sampler_matches_reference_density(oracle_mod, data_dir):
+    """The positron kinetic energies follow the reference's density
+    min(polynomial, nmax) on [0.511, emax] MeV (its rejection against nmax,
+    gPET_kernals.cu:420-443; for F-18 the fitted polynomial peaks slightly
+    above nmax, so the top is clipped): chi-square of 400k draws."""
+    from scipy import stats
+    from gpet_gb300 import formats as F
+    iso = F.read_isotopes(os.path.join(data_dir, "isotopes.txt"))
+    L = oracle_mod.lib("fp64")
+    L.oracle_sample_ek.argtypes = [C.c_void_p, C.c_uint64, C.c_int64, C.c_void_p]
+    for row in range(len(iso.halftime)):
+        cf32 = np.ascontiguousarray(iso.coef[row], np.float32)
+        cf = cf32.astype(np.float64)
+        emax, nmax = cf[0], cf[1]
+        E = np.linspace(0.511, emax, 100001)
+        target = np.clip(np.minimum(sum(cf[2 + i] * E ** (5 - i) for i in range(6)), nmax), 0.0, None)
+        out = np.zeros(400000)
+        L.oracle_sample_ek(cf32.ctypes.data, 99 + row, len(out), out.ctypes.data)
+        edges = np.linspace(0.511, emax, 51)
+        h, _ = np.histogram(out / 1e6 + 0.511, bins=edges)
+        cdf = np.concatenate([[0.0], np.cumsum((target[1:] + target[:-1]) * 0.5 * np.diff(E))])
+        p = np.diff(np.interp(edges, E, cdf))
+        exp = p / p.sum() * len(out)
+        keep = exp > 20
+        chi2 = float((((h - exp) ** 2) / exp)[keep].sum())
+        assert stats.chi2.sf(chi2, int(keep.sum()) - 1) > 1e-3, (row, chi2, int(keep.sum()))
+
+
 @pytest.mark.parametrize("energy", [511e3, 300e3, 100e3])
 def test_klein_nishina_chi2(oracle_mod, energy):
     from scipy import stats
