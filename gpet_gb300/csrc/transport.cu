@@ -686,6 +686,7 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
             }
         }
         // append the pulses and hits of the photons that finished, one atomic per warp
+        if (!__any_sync(0xffffffffu, done)) continue;
         const int my_ev = done ? nev : 0;
         int inc = my_ev;
 #pragma unroll
