@@ -346,9 +346,13 @@ BATCH_WORKLOAD = ("batched64: 64 simulations of uneven size in one job - phantom
                   "and digitizer")
 
 
-def run_batched_workload(args):
+def run_batched_workload(args, surrogate=False):
     """The 64-simulation job, once batched (gpet_run_batched) and once as 64
-    separate runs, on the same contexts."""
+    separate runs, on the same contexts. surrogate: instead, the batched job
+    with and without a learned detector response (trained, untimed, on entry
+    records of the positron workload, whose ring the 64 simulations share),
+    on independent seeds, with the two-sample chi-square of the pooled
+    singles spectra and crystal maps."""
     import numpy as np
     import torch
     from gpet_gb300 import api, scenes
@@ -369,61 +373,107 @@ def run_batched_workload(args):
             ctxs.append(ctx)
         setup_s = time.perf_counter() - t0
         seeds = [bs.options["seed"] for bs in sims]
+        sur, train = None, None
+        if surrogate:
+            t0 = time.perf_counter()
+            ps = scenes.positron(os.path.join(d, "train"), n_decays=args.train_decays)
+            gen = api.Context(0)
+            gen.set_options(dict(ps.options, data_dir=data, base_dir=ps.directory, record_entries=1, seed=555))
+            gen.load_config(ps.config_path)
+            gen.run()
+            rec = gen.entries()
+            sur = api.Surrogate(gen, seed=9)
+            losses = sur.train(rec, epochs=args.train_epochs, batch=8192, lr=2e-3)
+            sur.set_domain(1.0e5, 5.2e5, 0.3)
+            gen.close()
+            train = {"decays": args.train_decays, "records": int(len(rec)), "epochs": args.train_epochs,
+                     "loss_last_epoch": float(losses[-1]), "seconds": time.perf_counter() - t0}
 
         def reseed(k):
             for c, sd in zip(ctxs, seeds):
                 c.set_option("seed", sd + 1000003 * k)
 
-        for w in range(args.warmup):
-            reseed(100 + w)
-            api.run_batched(ctxs)
-        # the same simulations one after another need the tuner no more than
-        # the batch: both use the library defaults
-        sampler = ClockSampler(0)
-        torch.cuda.synchronize()
-        sampler.start()
-        ms_b, coinc_b, decays_b, launches_b, wall_b = 0.0, 0, 0, 0, 0.0
-        for k in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            reseed(k)
-            t0 = time.perf_counter()
-            st = api.run_batched(ctxs)
-            wall_b += time.perf_counter() - t0
-            ms_b += st[0]["ms_total"]
-            coinc_b += sum(x["n_coinc"] for x in st)
-            decays_b += sum(x["n_decays"] for x in st)
-            launches_b += st[0]["kernel_launches"]
-        clocks = sampler.stop()
-        # the same simulations one after another
-        ms_s, coinc_s, wall_s, launches_s = 0.0, 0, 0.0, 0
-        for k in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            reseed(k)
+        def batched_arm(k0, with_sur):
             for c in ctxs:
+                c.set_surrogate(sur if with_sur else None)
+            for w in range(args.warmup):
+                reseed(k0 + 100 + w)
+                api.run_batched(ctxs)
+            sampler = ClockSampler(0)
+            torch.cuda.synchronize()
+            sampler.start()
+            tot = {"ms": 0.0, "coinc": 0, "decays": 0, "launches": 0, "wall": 0.0, "nsur": 0, "entered": 0,
+                   "det": 0.0}
+            hist_e, hist_c = np.zeros(60), np.zeros(64)
+            for k in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                reseed(k0 + k)
                 t0 = time.perf_counter()
-                st = c.run()
-                wall_s += time.perf_counter() - t0
-                ms_s += st["ms_total"]
-                coinc_s += st["n_coinc"]
-                launches_s += st["kernel_launches"]
+                st = api.run_batched(ctxs)
+                tot["wall"] += time.perf_counter() - t0
+                tot["ms"] += st[0]["ms_total"]
+                tot["det"] += st[0]["ms_detector"]
+                tot["coinc"] += sum(x["n_coinc"] for x in st)
+                tot["decays"] += sum(x["n_decays"] for x in st)
+                tot["nsur"] += sum(x["n_surrogate"] for x in st)
+                tot["entered"] += sum(x["n_entered"] for x in st)
+                tot["launches"] += st[0]["kernel_launches"]
+                if surrogate:
+                    for c in ctxs:
+                        s_ev, _ = c.singles()
+                        hist_e += np.histogram(s_ev["E"], bins=60, range=(3.5e5, 6.5e5))[0]
+                        hist_c += np.bincount(s_ev["cryn"], minlength=64)[:64]
+            return tot, sampler.stop(), hist_e, hist_c
+
+        mc, clocks, mc_e, mc_c = batched_arm(0, False)
+        if surrogate:
+            su, clocks, su_e, su_c = batched_arm(50000, True)
+        else:
+            # the same simulations one after another
+            ms_s, coinc_s, wall_s, launches_s = 0.0, 0, 0.0, 0
+            for k in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                reseed(k)
+                for c in ctxs:
+                    t0 = time.perf_counter()
+                    st = c.run()
+                    wall_s += time.perf_counter() - t0
+                    ms_s += st["ms_total"]
+                    coinc_s += st["n_coinc"]
+                    launches_s += st["kernel_launches"]
         for c in ctxs:
             c.close()
-    line = {"metric": METRIC.replace("(plain MC)", "(plain MC, batched simulations)"),
-            "value": coinc_b / (ms_b * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_b / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+    base = {"unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "data": "synthetic (seeded)",
             "config": {"workload": BATCH_WORKLOAD, "simulations": len(sims),
-                       "decays_per_step": decays_b // max(1, args.steps),
+                       "decays_per_step": mc["decays"] // max(1, args.steps),
                        "l2": "flushed between steps (512 MB write)"},
-            "gpu_launches": launches_b,
-            "decays_per_s": decays_b / (ms_b * 1e-3),
-            "host_wall_per_step_s": wall_b / args.steps,
-            "separate_runs": {"value": coinc_s / (ms_s * 1e-3), "ms_per_step": ms_s / args.steps,
-                              "host_wall_per_step_s": wall_s / args.steps,
-                              "gpu_launches": launches_s, "same_coincidences": coinc_s == coinc_b},
             "setup_s": setup_s, "clocks": clocks}
+    if surrogate:
+        line = dict(base, metric=METRIC.replace("(plain MC)", "(surrogate detector response, batched simulations)"),
+                    value=su["coinc"] / (su["ms"] * 1e-3), ms_per_step=su["ms"] / args.steps,
+                    dtype="bf16 (MLP), f32 (transport)", gpu_launches=su["launches"],
+                    decays_per_s=su["decays"] / (su["ms"] * 1e-3))
+        line["config"] = dict(base["config"], training=train,
+                              domain="entry energy 100-520 keV, >= 3 mm inside the panel edges, all panels")
+        line["plain_mc_batched"] = {"value": mc["coinc"] / (mc["ms"] * 1e-3), "ms_per_step": mc["ms"] / args.steps,
+                                    "detector_ms_per_step": mc["det"] / args.steps}
+        line["surrogate"] = {"detector_ms_per_step": su["det"] / args.steps,
+                             "photons_per_step": su["nsur"] / args.steps,
+                             "fraction_of_entered": su["nsur"] / max(1, su["entered"])}
+        line["parity"] = {"singles_energy_350_650keV": _chi2(mc_e, su_e), "singles_per_crystal": _chi2(mc_c, su_c),
+                          "singles_mc": float(mc_e.sum()), "singles_surrogate": float(su_e.sum()),
+                          "coincidences_mc": mc["coinc"], "coincidences_surrogate": su["coinc"]}
+    else:
+        line = dict(base, metric=METRIC.replace("(plain MC)", "(plain MC, batched simulations)"),
+                    value=mc["coinc"] / (mc["ms"] * 1e-3), ms_per_step=mc["ms"] / args.steps, dtype="f32",
+                    gpu_launches=mc["launches"], decays_per_s=mc["decays"] / (mc["ms"] * 1e-3),
+                    host_wall_per_step_s=mc["wall"] / args.steps,
+                    separate_runs={"value": coinc_s / (ms_s * 1e-3), "ms_per_step": ms_s / args.steps,
+                                   "host_wall_per_step_s": wall_s / args.steps,
+                                   "gpu_launches": launches_s, "same_coincidences": coinc_s == mc["coinc"]})
     print(json.dumps(line), flush=True)
 
 
@@ -551,9 +601,11 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=-1,
                     help="steps of the end-to-end leg (default max(2, steps/2); 0 skips it: profiling only)")
     ap.add_argument("--gloo", action="store_true", help=argparse.SUPPRESS)
-    ap.add_argument("--workload", choices=["positron", "batched64", "surrogate", "large"], default="positron",
+    ap.add_argument("--workload", choices=["positron", "batched64", "surrogate", "surrogate_batched64", "large"],
+                    default="positron",
                     help="positron: the headline workload; batched64: 64 uneven simulations in one job; "
                          "surrogate: the headline workload with the learned detector response; "
+                         "surrogate_batched64: the 64-simulation job with and without it; "
                          "large: the whole-body configuration (48 panels, 256x256x512 phantom)")
     ap.add_argument("--train-decays", type=int, default=200_000_000, help=argparse.SUPPRESS)
     ap.add_argument("--train-epochs", type=int, default=12, help=argparse.SUPPRESS)
@@ -568,6 +620,8 @@ def main():
         run_reference(args)
     elif args.workload == "batched64":
         run_batched_workload(args)
+    elif args.workload == "surrogate_batched64":
+        run_batched_workload(args, surrogate=True)
     elif args.workload == "surrogate":
         run_surrogate_workload(args)
     else:

@@ -115,3 +115,35 @@ def test_batch_argument_errors(scene_small, data_dir, gpet_lib):
     c = api.Context(0)
     with pytest.raises(api.GpetError):
         api.run_batched([a, c])
+
+
+def test_batch_with_surrogate_equals_individual_runs(scene_positron, data_dir, gpet_lib):
+    """The learned detector response inside a batched job: the surrogate's
+    draws are keyed by each simulation's own streams, so every simulation's
+    pulses, singles and coincidences equal those of its run alone with the
+    same surrogate."""
+    from gpet_gb300 import api
+    gen = make_ctx(scene_positron, data_dir, seed=101, n_decays=300000, record_entries=1)
+    gen.run()
+    rec = gen.entries()
+    sur = api.Surrogate(gen, seed=5)
+    sur.train(rec, epochs=2, batch=4096, lr=2e-3)
+    sur.set_domain(1.0e5, 5.2e5, 0.3)
+    specs = [dict(seed=301, n_decays=60000), dict(seed=302, sim_id=4, n_decays=25000), dict(seed=303, n_decays=90000)]
+    alone, alone_st = [], []
+    for opts in specs:
+        ctx = make_ctx(scene_positron, data_dir, sub_decays=8192, **opts)
+        ctx.set_surrogate(sur)
+        alone_st.append(ctx.run())
+        alone.append(_results(ctx))
+        ctx.close()
+    ctxs = [make_ctx(scene_positron, data_dir, sub_decays=8192, chunk_decays=32768, **opts) for opts in specs]
+    for c in ctxs:
+        c.set_surrogate(sur)
+    stats = api.run_batched(ctxs)
+    for i, ctx in enumerate(ctxs):
+        what = "simulation %d" % i
+        assert stats[i]["n_surrogate"] == alone_st[i]["n_surrogate"] > 0, what
+        for k in ("n_entered", "n_pulses", "n_singles", "n_coinc", "n_true", "n_scatter", "n_random"):
+            assert stats[i][k] == alone_st[i][k], "%s %s: batch %r alone %r" % (what, k, stats[i][k], alone_st[i][k])
+        _same(_results(ctx), alone[i], what)
