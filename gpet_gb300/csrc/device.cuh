@@ -412,9 +412,11 @@ __device__ __forceinline__ void make_pair(const SimDesc& S, Stream& st, const fl
 }
 
 // comsam(matid), gPET_kernals.cu:66-88
-__device__ __forceinline__ void compton_surface(const SimDesc& S, float e, int m, Stream& st, float& efrac, float& cost)
+template <class U>
+__device__ __forceinline__ void compton_surface_u(const SimDesc& S, float e, int m, U&& unif, float& efrac,
+                                                  float& cost)
 {
-    float indcp = st_u(st) * S.idcp_c;
+    float indcp = unif() * S.idcp_c;
     float inde = e * S.ide_c;
     float c = lerp2(S.cmpsf + (size_t)m * S.ncp_c * S.ne_c, S.ncp_c, S.ne_c, inde, indcp);
     if (c > 1.0f) c = 1.0f;
@@ -423,10 +425,16 @@ __device__ __forceinline__ void compton_surface(const SimDesc& S, float e, int m
     efrac = 1.0f / (1.0f + e * kIMC2 * (1.0f - c));
 }
 
-// rylsam, gPET_kernals.cu:128-146
-__device__ __forceinline__ float rayleigh_surface(const SimDesc& S, float e, int m, Stream& st)
+__device__ __forceinline__ void compton_surface(const SimDesc& S, float e, int m, Stream& st, float& efrac, float& cost)
 {
-    float indcp = st_u(st) * S.idcp_r;
+    compton_surface_u(S, e, m, [&]() { return st_u(st); }, efrac, cost);
+}
+
+// rylsam, gPET_kernals.cu:128-146
+template <class U>
+__device__ __forceinline__ float rayleigh_surface_u(const SimDesc& S, float e, int m, U&& unif)
+{
+    float indcp = unif() * S.idcp_r;
     float inde = e * S.ide_r;
     float c = lerp2(S.rayff + (size_t)m * S.ncp_r * S.ne_r, S.ncp_r, S.ne_r, inde, indcp);
     if (c > 1.0f) c = 1.0f;
@@ -434,8 +442,14 @@ __device__ __forceinline__ float rayleigh_surface(const SimDesc& S, float e, int
     return c;
 }
 
+__device__ __forceinline__ float rayleigh_surface(const SimDesc& S, float e, int m, Stream& st)
+{
+    return rayleigh_surface_u(S, e, m, [&]() { return st_u(st); });
+}
+
 // comsam, free-electron Klein-Nishina, gPET_kernals.cu:90-126
-__device__ __forceinline__ void kn_sample(float e, Stream& st, float& efrac, float& cost)
+template <class U>
+__device__ __forceinline__ void kn_sample_u(float e, U&& unif, float& efrac, float& cost)
 {
     float e0 = e * kIMC2;
     float twoe = 2.0f * e0;
@@ -443,15 +457,20 @@ __device__ __forceinline__ void kn_sample(float e, Stream& st, float& efrac, flo
     float loge = dm_logf(1.0f + twoe);
     float ef = 1.0f;
     for (int it = 0; it < 100000; ++it) {
-        if (st_u(st) * (loge + twoe * (1.0f + e0) * kmin2) < loge)
-            ef = dm_expf(-st_u(st) * loge);
+        if (unif() * (loge + twoe * (1.0f + e0) * kmin2) < loge)
+            ef = dm_expf(-unif() * loge);
         else
-            ef = dm_sqrt(kmin2 + st_u(st) * (1.0f - kmin2));
+            ef = dm_sqrt(kmin2 + unif() * (1.0f - kmin2));
         float mess = e0 * e0 * ef * (1.0f + ef * ef);
-        if (st_u(st) * mess <= mess - (1.0f - ef) * ((1.0f + twoe) * ef - 1.0f)) break;
+        if (unif() * mess <= mess - (1.0f - ef) * ((1.0f + twoe) * ef - 1.0f)) break;
     }
     efrac = ef;
     cost = 1.0f - (1.0f - ef) / (ef * e0);
+}
+
+__device__ __forceinline__ void kn_sample(float e, Stream& st, float& efrac, float& cost)
+{
+    kn_sample_u(e, [&]() { return st_u(st); }, efrac, cost);
 }
 
 // photon(), gPET_kernals.cu:256-345 - Woodcock tracking to the phantom exit.

@@ -274,7 +274,29 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
     int steps = 0;
     SimTally t_steps;
     Photon ph;
-    Stream st;
+    // the photon's Philox stream (tag kTagPhantom + (p & 1), id d, the
+    // simulation's key): only the block counter, position and current block
+    // are held; key and id are re-read when a block is generated
+    uint32_t rblk = 0, rbuf[4] = {0u, 0u, 0u, 0u};
+    int rpos = 4;
+    auto unif = [&]() -> float {
+        if (rpos == 4) {
+            const SimDesc& S = kMulti ? w.sims[sim] : sS;
+            philox10(rblk, kTagPhantom + (uint32_t)(p & 1), (uint32_t)d, (uint32_t)((uint64_t)d >> 32), S.key0,
+                     S.key1, rbuf);
+            rblk++;
+            rpos = 0;
+        }
+        uint32_t v;
+        switch (rpos) {   // keeps the block in registers
+        case 0: v = rbuf[0]; break;
+        case 1: v = rbuf[1]; break;
+        case 2: v = rbuf[2]; break;
+        default: v = rbuf[3]; break;
+        }
+        rpos++;
+        return dm_u01(v);
+    };
     for (;;) {
         // refill idle lanes, one atomic per warp
         const bool need = !active && !exhausted;
@@ -306,8 +328,8 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
                         ph.t = pb.t[j];
                         ph.tf = 0.0f;
                         ph.nscat = 0;
-                        const SimDesc& S = kMulti ? w.sims[sim] : sS;
-                        st_init(st, S.key0, S.key1, kTagPhantom + k, (uint64_t)d);
+                        rblk = 0;
+                        rpos = 4;
                         steps = 0;
                         active = true;
                         if (w.source) {
@@ -340,7 +362,7 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
             const SimDesc& S = kMulti ? w.sims[sim] : sS;
             steps++;
             float lammin = wck_at(S.wck_ph, S.wck_e0, S.wck_ide, ph.E);
-            float s = -lammin * dm_logf(st_u(st));
+            float s = -lammin * dm_logf(unif());
             ph.x[0] = dm_fma(s, ph.u[0], ph.x[0]);
             ph.x[1] = dm_fma(s, ph.u[1], ph.x[1]);
             ph.x[2] = dm_fma(s, ph.u[2], ph.x[2]);
@@ -355,14 +377,14 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
                 float lamden = lammin * voxden;
                 float4 xs = xs_at(S, m, ph.E);
                 float prob = dm_fma(-lamden, xs.x, 1.0f);
-                float rn = st_u(st);
+                float rn = unif();
                 if (rn < prob) {
                 } else {
                     prob = dm_fma(lamden, xs.y, prob);
                     if (rn < prob) {
                         float efrac, cost;
-                        compton_surface(S, ph.E, m, st, efrac, cost);
-                        float phi = st_u(st);
+                        compton_surface_u(S, ph.E, m, unif, efrac, cost);
+                        float phi = unif();
                         ph.E *= efrac;
                         ph.nscat++;
                         if (ph.E < S.eabsph) status = 1;
@@ -370,8 +392,8 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
                     } else {
                         prob = dm_fma(lamden, xs.z, prob);
                         if (rn < prob) {
-                            float cost = rayleigh_surface(S, ph.E, m, st);
-                            float phi = st_u(st);
+                            float cost = rayleigh_surface_u(S, ph.E, m, unif);
+                            float phi = unif();
                             rotate(ph.u[0], ph.u[1], ph.u[2], cost, phi);
                             ph.nscat++;
                         } else {
@@ -526,7 +548,6 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
     Local L;
     const float* Pn = nullptr;
     int32_t pann = 0;
-    Stream st;
     PEvent ev[kMaxPulse];
     int nev = 0, nh = 0, step = 0;
     int32_t hid[kMaxHits][4];
@@ -535,6 +556,27 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
     bool overflow = false;
     unsigned nsteps = 0;
     EntryRec er;
+    // the photon's Philox stream (tag kTagDet + (parn & 1), id eid, the
+    // simulation's key): key and id are re-read when a block is generated
+    uint32_t rblk = 0, rbuf[4] = {0u, 0u, 0u, 0u};
+    int rpos = 4;
+    auto unif = [&]() -> float {
+        if (rpos == 4) {
+            const SimDesc& S = kMulti ? sims[sim] : sS;
+            philox10(rblk, kTagDet + (uint32_t)(parn & 1), (uint32_t)eid, 0u, S.key0, S.key1, rbuf);
+            rblk++;
+            rpos = 0;
+        }
+        uint32_t v;
+        switch (rpos) {   // keeps the block in registers
+        case 0: v = rbuf[0]; break;
+        case 1: v = rbuf[1]; break;
+        case 2: v = rbuf[2]; break;
+        default: v = rbuf[3]; break;
+        }
+        rpos++;
+        return dm_u01(v);
+    };
     for (;;) {
         // refill idle lanes
         const bool need = !active && !exhausted;
@@ -568,7 +610,8 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                         er.ux = L.u[0]; er.uy = L.u[1]; er.uz = L.u[2];
                         er.E = L.E;
                     }
-                    st_init(st, S.key0, S.key1, kTagDet + (parn & 1), (uint64_t)(uint32_t)eid);
+                    rblk = 0;
+                    rpos = 4;
                     nev = 0; nh = 0; step = 0; nsteps = 0;
                     overflow = false;
                     active = true;
@@ -584,7 +627,7 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
             nsteps++;
             do {   // a single pass: `break` ends the step
                 float lammin = wck_at(S.wck_det, S.wck_e0, S.wck_ide, L.E);
-                float s = -lammin * dm_logf(st_u(st));
+                float s = -lammin * dm_logf(unif());
                 L.x[0] = dm_fma(s, L.u[0], L.x[0]);
                 L.x[1] = dm_fma(s, L.u[1], L.x[1]);
                 L.x[2] = dm_fma(s, L.u[2], L.x[2]);
@@ -602,16 +645,16 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                 float4 xs = xs_at(S, mat, L.E);
                 float prob = dm_fma(-lamden, xs.x, 1.0f);
                 if (prob < 0.0f) prob = 0.0f;
-                float rn = st_u(st);
+                float rn = unif();
                 if (rn < prob) break;   // virtual
                 prob = dm_fma(lamden, xs.y, prob);
                 int type = 0;
                 float dep = 0.0f;
                 if (rn < prob) {
                     float efrac, cost;
-                    kn_sample(L.E, st, efrac, cost);
+                    kn_sample_u(L.E, unif, efrac, cost);
                     float de = L.E * (1.0f - efrac);
-                    float phi = st_u(st);
+                    float phi = unif();
                     if (m_id != 1) {   // a crystal (not the gap)
                         PEvent e;
                         e.pann = pann; e.modn = M_id; e.cryn = L_id;
@@ -639,8 +682,8 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                 } else {
                     prob = dm_fma(lamden, xs.z, prob);
                     if (rn < prob) {
-                        float cost = rayleigh_surface(S, L.E, mat, st);
-                        float phi = st_u(st);
+                        float cost = rayleigh_surface_u(S, L.E, mat, unif);
+                        float phi = unif();
                         rotate(L.u[0], L.u[1], L.u[2], cost, phi);
                         break;
                     }
