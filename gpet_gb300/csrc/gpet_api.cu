@@ -341,7 +341,8 @@ int gpet_set_option(gpet_ctx* c, const char* key, const char* value)
     if (end == value || (end && *end)) return fail(c, GPET_ERR_ARG, "bad value for " + k + ": " + v);
     if (c->coinc_policy < 0 || c->coinc_policy > 1) return fail(c, GPET_ERR_ARG, "coinc_policy must be 0 or 1");
     if (c->chunk_decays < 1024) return fail(c, GPET_ERR_ARG, "chunk_decays must be >= 1024");
-    if (c->sub_decays < 1024) return fail(c, GPET_ERR_ARG, "sub_decays must be >= 1024");
+    if (c->sub_decays < 1024 || c->sub_decays > (1ll << 28))
+        return fail(c, GPET_ERR_ARG, "sub_decays must be 1024 .. 2^28");
     if (c->phantom_bps < 0 || c->phantom_bps > 32) return fail(c, GPET_ERR_ARG, "phantom_blocks_per_sm must be 0..32");
     if (!(c->noise_lambda_us >= 0.0f) || !(c->noise_interval_us > 0.0) || !(c->noise_sigma >= 0.0f))
         return fail(c, GPET_ERR_ARG, "noise_lambda_us >= 0, noise_interval_us > 0, noise_sigma_ev >= 0");

@@ -269,7 +269,8 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
     };
 
     bool active = false, exhausted = false;
-    int64_t p = 0, d = 0;
+    int32_t p = 0;   // photon index within the wave (< 2^25)
+    int64_t d = 0;
     int sim = 0;
     int steps = 0;
     SimTally t_steps;
@@ -307,14 +308,15 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
             if (lane == leader) b = atomicAdd(work, (unsigned long long)__popc(mneed));
             b = __shfl_sync(0xffffffffu, b, leader);
             if (need) {
-                p = (int64_t)(b + __popc(mneed & lt));
-                if (p >= nphot) {
+                const unsigned long long pw = b + __popc(mneed & lt);
+                if (pw >= (unsigned long long)nphot) {
                     exhausted = true;
                 } else {
+                    p = (int32_t)pw;
                     const int64_t j = p >> 1;
                     const int k = (int)(p & 1);
                     const int sgi = seg_of(sg, j);
-                    sim = sg.sim[sgi];
+                    sim = kMulti ? sg.sim[sgi] : 0;
                     d = sg.d0[sgi] + (j - sg.g0[sgi]);
                     const int nph = pb.nph[j];
                     if (k < nph) {
@@ -325,7 +327,7 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
                         ph.u[1] = pb.f[(4 + 3 * k) * pb.cap + j];
                         ph.u[2] = pb.f[(5 + 3 * k) * pb.cap + j];
                         ph.E = pb.f[(9 + k) * pb.cap + j];
-                        ph.t = pb.t[j];
+                        ph.t = 0.0;   // the emission time stays in the pair buffer (pb.t[p >> 1])
                         ph.tf = 0.0f;
                         ph.nscat = 0;
                         rblk = 0;
@@ -336,7 +338,7 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
                             SrcRec r;
                             r.x = ph.x[0]; r.y = ph.x[1]; r.z = ph.x[2];
                             r.ux = ph.u[0]; r.uy = ph.u[1]; r.uz = ph.u[2];
-                            r.E = ph.E; r.eventid = (int32_t)d; r.t = ph.t;
+                            r.E = ph.E; r.eventid = (int32_t)d; r.t = pb.t[j];
                             w.source[p] = r;
                         }
                     } else {
@@ -419,7 +421,7 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
                     ExitRec e;
                     e.x = ph.x[0]; e.y = ph.x[1]; e.z = ph.x[2];
                     e.ux = ph.u[0]; e.uy = ph.u[1]; e.uz = ph.u[2];
-                    e.E = ph.E; e.nscat = ph.nscat; e.t = ph.t + (double)ph.tf;
+                    e.E = ph.E; e.nscat = ph.nscat; e.t = pb.t[p >> 1] + (double)ph.tf;
                     e.status = status;
                     e.panel = -1;
                     exits[p] = e;
@@ -433,7 +435,7 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
                 FinRec r;
                 r.x = ph.x[0]; r.y = ph.x[1]; r.z = ph.x[2];
                 r.ux = ph.u[0]; r.uy = ph.u[1]; r.uz = ph.u[2];
-                r.E = ph.E; r.nscat = ph.nscat; r.t = ph.t; r.p = p; r.d = d; r.status = status; r.tf = ph.tf;
+                r.E = ph.E; r.nscat = ph.nscat; r.t = pb.t[p >> 1]; r.p = p; r.d = d; r.status = status; r.tf = ph.tf;
                 r.sim = sim; r.steps = steps;
                 fb[fcount + __popc(mf & lt)] = r;
                 active = false;
