@@ -154,6 +154,26 @@ def cpu_baseline(scene, seconds, threads=0, max_decays=200_000_000):
             "decays_per_s": n / dt, "coincidences": r["n_coinc"]}
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), or None."""
+    import subprocess
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return None
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -216,11 +236,14 @@ def run_ours(args):
     with tempfile.TemporaryDirectory() as d:
         sc = make_scene(d, args.decays, args.workload)
         data = os.path.join(ROOT, "data")
+        t_setup = time.perf_counter()
         ctx = api.Context(local)
         opts = dict(sc.options, data_dir=data, base_dir=d, sim_id=rank)
         opts.update(args.set)
         ctx.set_options(opts)
         ctx.load_config(sc.config_path)
+        torch.cuda.synchronize()
+        setup_s = time.perf_counter() - t_setup
         tuning = ctx.autotune(args.tune_decays) if args.autotune else None
         # decays per k_source / k_phantom launch of this run
         sub_decays = int(tuning["sub_decays"]) if tuning else int(args.set.get("sub_decays", SUB_DECAYS))
@@ -326,10 +349,15 @@ def run_ours(args):
         "clocks": clocks,
         "wall_s_timed_region": wall,
         "launch_shape": tuning if tuning else "library defaults",
+        "setup_s": setup_s,
     }
     if world == 1 and not args.no_cpu_baseline:
         with tempfile.TemporaryDirectory() as d2:
-            line["cpu_baseline"] = cpu_baseline(make_scene(d2, args.decays, args.workload), args.cpu_seconds)
+            sc2 = make_scene(d2, args.decays, args.workload)
+            line["cpu_baseline"] = cpu_baseline(sc2, args.cpu_seconds)
+            line["cpu_baseline"]["cpu_model"] = cpu_model()
+            one = cpu_baseline(sc2, args.cpu_seconds / 4, threads=1)
+            line["cpu_baseline_1core"] = {k: one[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
