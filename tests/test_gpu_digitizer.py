@@ -111,3 +111,27 @@ def test_digitizer_with_background_singles(scene_positron, data_dir, gpet_lib, o
     pr, cl = ctx.coincidences()
     with_noise = noise[pr[:, 0]] | noise[pr[:, 1]]
     assert with_noise.any() and (cl[with_noise] == 2).all()
+
+
+@pytest.mark.parametrize("case", ["one_instant", "ulp_apart_wide_span", "negative_times"])
+def test_time_order_keys_edge_cases(scene_positron, data_dir, gpet_lib, oracle_mod, case):
+    """The time order sorts 48-bit keys of (t - t_min) over the survivors'
+    time span and puts runs of equal keys in (t, parn, slot) order: pulses
+    at one instant (zero span: the IEEE bits of t are the keys), pulses a few
+    ulps apart within a span of 1e12 us (many share a quantised key), and
+    negative times; singles and coincidences bit for bit against the oracle."""
+    ctx = make_ctx(scene_positron, data_dir)
+    o = oracle_for(scene_positron, data_dir)
+    n = 4000
+    ev, scat, slot = synthetic_pulses(n, seed=99, ties=False)
+    rng = np.random.default_rng(5)
+    if case == "one_instant":
+        ev["t"] = 1234.5
+    elif case == "ulp_apart_wide_span":
+        base = rng.uniform(0, 1e12, n // 8)
+        t = np.repeat(base, 8)
+        t = t + np.tile(np.arange(8), n // 8) * np.spacing(t)       # 8 times a few ulps apart
+        ev["t"] = rng.permutation(t)
+    else:
+        ev["t"] = rng.uniform(-50.0, 50.0, n)
+    _check(ctx, o, ev, scat, slot)

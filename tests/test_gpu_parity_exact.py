@@ -266,3 +266,21 @@ def test_voxel_palette_falls_back_to_pairs(scene_positron, data_dir, gpet_lib):
         st = ctx.run()
         out.append((st["n_singles"], st["n_coinc"], ctx.singles()[0].tobytes(), ctx.coincidences()[0].tobytes()))
     assert out[0] == out[1] and out[0][1] > 0
+
+
+@pytest.mark.parametrize("n", [0, 1, 7])
+def test_tiny_runs_bit_exact(n, scene_positron, data_dir, gpet_lib, oracle_mod):
+    """No decays, one decay, a handful: histories and singles against the
+    oracle, and empty results read back as empty arrays."""
+    ctx, st, r = _run_both(scene_positron, data_dir, n_decays=n)
+    assert st["n_decays"] == n
+    gx = ctx.exits()
+    assert len(gx) == len(r["exits"]) == 2 * n
+    if n:
+        msg = _first_diff(gx, r["exits"], ["status", "panel", "nscat", "E", "x", "y", "z", "ux", "uy", "uz", "t"])
+        assert msg is None, msg
+    gs, gsc = ctx.singles()
+    assert len(gs) == r["n_singles"]
+    assert np.array_equal(gs.view(np.uint8), r["singles"].view(np.uint8))
+    pr, cl = ctx.coincidences()
+    assert len(pr) == r["n_coinc"]
