@@ -1,7 +1,10 @@
 // gpet_api.cu - host runtime behind the C ABI of include/gpet.h: context,
 // options, scene upload, run orchestration (the role of main.cu, init and
 // sampleParticle/simulateParticle in gPET.cu), output copy-out and writers.
+#include <sys/stat.h>
+
 #include <algorithm>
+#include <cerrno>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1874,6 +1877,13 @@ int gpet_write_outputs(gpet_ctx* c, const char* dir)
     if (!c || !dir) return GPET_ERR_ARG;
     if (!results(c)) return fail(c, GPET_ERR_ARG, "no results to write");
     std::string d(dir);
+    // the directory and its parents are made when missing
+    for (size_t i = 1; i <= d.size(); ++i) {
+        if (i < d.size() && d[i] != '/') continue;
+        const std::string part = d.substr(0, i);
+        if (mkdir(part.c_str(), 0755) != 0 && errno != EEXIST)
+            return fail(c, GPET_ERR_IO, "cannot make the output directory " + part);
+    }
     int64_t n = 0;
     int rc;
     // adder.dat: pulses after adder + readout (gPET.cu:383)

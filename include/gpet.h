@@ -212,7 +212,8 @@ int gpet_sinogram(gpet_ctx* ctx, const gpet_sino_params* params, uint32_t* out);
  * coincidences.dat (+ coincidences_class.dat); with record_source=1
  * outsource.dat / idsource.dat / timesource.dat, with record_exits=1
  * outphantom.dat / idphantom.dat / timephantom.dat (28-byte state, int32 id,
- * double time per photon, the reference's layouts). */
+ * double time per photon, the reference's layouts). out_dir and its parents
+ * are made when missing. */
 int gpet_write_outputs(gpet_ctx* ctx, const char* out_dir);
 
 /* ------------------------------------------------------------ introspection */

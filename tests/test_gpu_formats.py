@@ -119,3 +119,36 @@ def test_sinogram_matches_list_mode(scene_positron, data_dir, gpet_lib):
     # the source is a cylinder of radius 3 cm: true lines of response have |s| <~ 3 cm
     t = ctx.sinogram(64, 48, 1, 6.0, 3.2, (0,)).sum(axis=(0, 1))
     assert t[16:48].sum() > 0.9 * t.sum()
+
+
+def test_cli_writes_the_library_records(scene_positron, data_dir, gpet_lib, tmp_path):
+    """`gpet input_PET.in key=value ...` (the drop-in for `./gPET
+    input_PET.in`) writes the same records as the library API on the same
+    scene and options: adder, singles and coincidence files byte for byte,
+    hits as the same multiset (their order across photons is not defined)."""
+    import subprocess
+    from gpet_gb300 import build as B
+    cli = os.path.join(B.OUT, "gpet")
+    assert os.path.exists(cli)
+    opts = dict(scene_positron.options, seed=4242, n_decays=30000)
+    args = ["%s=%s" % (k, v) for k, v in opts.items()] + ["data_dir=" + data_dir, "base_dir=" + scene_positron.directory,
+                                                          "out_dir=" + str(tmp_path / "cli")]
+    r = subprocess.run([cli, scene_positron.config_path] + args, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "coincidences" in r.stdout
+    ctx = make_ctx(scene_positron, data_dir, seed=4242, n_decays=30000)
+    ctx.run()
+    ctx.write_outputs(str(tmp_path / "lib"))
+    for name in ("adder.dat", "singles.dat", "coincidences.dat", "coincidences_class.dat"):
+        a = (tmp_path / "cli" / name).read_bytes()
+        b = (tmp_path / "lib" / name).read_bytes()
+        assert a == b, name
+    assert os.path.getsize(tmp_path / "cli" / "singles.dat") % 48 == 0
+    assert os.path.getsize(tmp_path / "cli" / "singles.dat") > 0
+
+    def hits(d):
+        ids = np.fromfile(d / "HitsID.dat", np.int32).reshape(-1, 5)
+        f = np.fromfile(d / "Hits.dat", np.float32).reshape(-1, 5)
+        rec = np.concatenate([ids.view(np.uint32), f.view(np.uint32)], axis=1)
+        return rec[np.lexsort(rec.T[::-1])]
+    assert np.array_equal(hits(tmp_path / "cli"), hits(tmp_path / "lib"))
