@@ -313,7 +313,10 @@ __device__ __forceinline__ float sample_ek(const float* cf, Stream& st)
 
 // setPositronRange, gPET_kernals.cu:347-418 (density read from the voxel being
 // entered; outside the phantom the remaining range is walked in air)
-inline __device__ void positron_range(const SimDesc& S, float x[3], float ek, const float* dir, Stream& st)
+// spare (may be null): the second normal of the last Box-Muller pair, which
+// the pair emission uses for its non-collinearity angle
+inline __device__ void positron_range(const SimDesc& S, float x[3], float ek, const float* dir, Stream& st,
+                                      float* spare = nullptr)
 {
     float ekin = ek / 1.0e6f;
     const float b1 = 5.44040782f, b2 = 0.369516529f;
@@ -325,7 +328,10 @@ inline __device__ void positron_range(const SimDesc& S, float x[3], float ek, co
         st_normal2(st, n1, n2);
         d[0] = sigma * n1;
         d[1] = sigma * n2;
-        d[2] = sigma * st_normal(st);
+        float n3, n4;
+        st_normal2(st, n3, n4);
+        d[2] = sigma * n3;
+        if (spare) *spare = n4;
     }
     float r = dm_sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     if (dir) {
@@ -387,7 +393,10 @@ struct Photon {
 
 // annihilation pair, setPosition gPET_kernals.cu:536-555 (non-collinearity
 // with the +-theta*MC2/2 energy shift of the reference)
-__device__ __forceinline__ void make_pair(const SimDesc& S, Stream& st, const float pos[3], double t_us, Photon ph[2])
+// spare: a standard normal already drawn (the positron range's second
+// normal of its last pair) for the non-collinearity angle, or null
+__device__ __forceinline__ void make_pair(const SimDesc& S, Stream& st, const float pos[3], double t_us, Photon ph[2],
+                                          const float* spare = nullptr)
 {
     float cost = -1.0f + 2.0f * st_u(st);
     float phi = st_u(st);
@@ -396,7 +405,7 @@ __device__ __forceinline__ void make_pair(const SimDesc& S, Stream& st, const fl
     float sint = dm_sqrt(1.0f - cost * cost);
     float u0 = sint * c, u1 = sint * s, u2 = cost;
     float phi2 = st_u(st);
-    float theta = st_normal(st) * S.noncol_sigma;
+    float theta = (spare ? *spare : st_normal(st)) * S.noncol_sigma;
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         ph[k].x[0] = pos[0]; ph[k].x[1] = pos[1]; ph[k].x[2] = pos[2];

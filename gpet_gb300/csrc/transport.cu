@@ -89,8 +89,9 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2])
         }
         float pos[3] = {(float)r[0], (float)r[1], (float)r[2]};
         float dir[3] = {(float)r[4], (float)r[5], (float)r[6]};
-        if (S.useprange) positron_range(S, pos, (float)r[7], dir, st);
-        make_pair(S, st, pos, r[3], ph);
+        float spare = 0.0f;
+        if (S.useprange) positron_range(S, pos, (float)r[7], dir, st, &spare);
+        make_pair(S, st, pos, r[3], ph, S.useprange ? &spare : nullptr);
         return 2;
     }
     int si = 0;
@@ -105,11 +106,12 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2])
     if (!(br < S.iso_ratio[si])) return 0;
     float pos[3];
     shape_position(S, si, st, pos);
+    float spare = 0.0f;
     if (S.useprange) {
         float ek = sample_ek(S.iso_coef[si], st);
-        positron_range(S, pos, ek, nullptr, st);
+        positron_range(S, pos, ek, nullptr, st, &spare);
     }
-    make_pair(S, st, pos, t_us, ph);
+    make_pair(S, st, pos, t_us, ph, S.useprange ? &spare : nullptr);
     return 2;
 }
 

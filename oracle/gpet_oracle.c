@@ -339,7 +339,9 @@ static real sample_ek(const or_scene* sc, int type, stream_t* st)
  * entered (as the reference does). A positron that reaches outside the phantom
  * finishes its remaining range in air (0.0012905 g/cm^3); the reference adds a
  * spurious 1000 cm there (:383,405). */
-static void positron_range(const or_scene* sc, real x[3], real ek, const real* dir, stream_t* st)
+/* spare (may be NULL): the second normal of the last Box-Muller pair, which
+ * the pair emission uses for its non-collinearity angle */
+static void positron_range(const or_scene* sc, real x[3], real ek, const real* dir, stream_t* st, real* spare)
 {
     real ekin = ek / (real)1.0e6;
     real b1 = (real)5.44040782, b2 = (real)0.369516529;
@@ -351,7 +353,10 @@ static void positron_range(const or_scene* sc, real x[3], real ek, const real* d
         st_normal2(st, &n1, &n2);
         d[0] = sigma * n1;
         d[1] = sigma * n2;
-        d[2] = sigma * st_normal(st);
+        real n3, n4;
+        st_normal2(st, &n3, &n4);
+        d[2] = sigma * n3;
+        if (spare) *spare = n4;
     }
     real r = R_SQRT(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     if (dir) {
@@ -773,7 +778,10 @@ typedef struct {
     double ntau_us[64], cfac[64];   /* per source: -lifetime (us), 1 - exp(-dt/lifetime) */
 } prep_t;
 
-static void make_pair(const or_scene* sc, stream_t* st, const real pos[3], photon_t ph[2], double t_us)
+/* spare: a standard normal already drawn (the positron range's second
+ * normal of its last pair) for the non-collinearity angle, or NULL */
+static void make_pair(const or_scene* sc, stream_t* st, const real pos[3], photon_t ph[2], double t_us,
+                      const real* spare)
 {
     /* setPosition, gPET_kernals.cu:536-555 */
     real cost = (real)-1.0 + (real)2.0 * st_u(st);
@@ -783,7 +791,7 @@ static void make_pair(const or_scene* sc, stream_t* st, const real pos[3], photo
     real sint = R_SQRT((real)1.0 - cost * cost);
     real u0 = sint * c, u1 = sint * s, u2 = cost;
     real phi2 = st_u(st);
-    real theta = st_normal(st) * (real)sc->noncol_sigma;
+    real theta = (spare ? *spare : st_normal(st)) * (real)sc->noncol_sigma;
     for (int k = 0; k < 2; ++k) {
         ph[k].x[0] = pos[0]; ph[k].x[1] = pos[1]; ph[k].x[2] = pos[2];
         ph[k].t = t_us; ph[k].tf = (real)0.0; ph[k].nscat = 0;
@@ -884,8 +892,9 @@ static void simulate_decay(const or_scene* sc, const prep_t* pp, int64_t d, or_e
         }
         real pos[3] = {(real)(float)r[0], (real)(float)r[1], (real)(float)r[2]};
         real dir[3] = {(real)(float)r[4], (real)(float)r[5], (real)(float)r[6]};
-        if (sc->useprange) positron_range(sc, pos, (real)(float)r[7], dir, &st);
-        make_pair(sc, &st, pos, ph, r[3]);
+        real spare = (real)0.0;
+        if (sc->useprange) positron_range(sc, pos, (real)(float)r[7], dir, &st, &spare);
+        make_pair(sc, &st, pos, ph, r[3], sc->useprange ? &spare : NULL);
         have = 1;
         tb->n_pairs++;
         transport_pair(sc, pp, d, ph, have, exits, src, tb, flags);
@@ -910,11 +919,12 @@ static void simulate_decay(const or_scene* sc, const prep_t* pp, int64_t d, or_e
     if (br < (real)sc->iso_ratio[type]) {
         real pos[3];
         shape_position(sc, si, &st, pos);
+        real spare = (real)0.0;
         if (sc->useprange) {
             real ek = sample_ek(sc, type, &st);
-            positron_range(sc, pos, ek, NULL, &st);
+            positron_range(sc, pos, ek, NULL, &st, &spare);
         }
-        make_pair(sc, &st, pos, ph, t_us);
+        make_pair(sc, &st, pos, ph, t_us, sc->useprange ? &spare : NULL);
         have = 1;
         tb->n_pairs++;
     }
@@ -1309,7 +1319,7 @@ void oracle_pair_angles(float sigma, uint64_t seed, int64_t n, double* angle, do
         stream_t st;
         st_init(&st, &sc, TAG_DECAY, (uint64_t)i);
         photon_t ph[2];
-        make_pair(&sc, &st, pos, ph, 0.0);
+        make_pair(&sc, &st, pos, ph, 0.0, NULL);
         double d = (double)ph[0].u[0] * ph[1].u[0] + (double)ph[0].u[1] * ph[1].u[1] + (double)ph[0].u[2] * ph[1].u[2];
         double n0 = sqrt((double)ph[0].u[0] * ph[0].u[0] + (double)ph[0].u[1] * ph[0].u[1] + (double)ph[0].u[2] * ph[0].u[2]);
         double n1 = sqrt((double)ph[1].u[0] * ph[1].u[0] + (double)ph[1].u[1] * ph[1].u[1] + (double)ph[1].u[2] * ph[1].u[2]);
