@@ -284,3 +284,46 @@ def test_tiny_runs_bit_exact(n, scene_positron, data_dir, gpet_lib, oracle_mod):
     assert np.array_equal(gs.view(np.uint8), r["singles"].view(np.uint8))
     pr, cl = ctx.coincidences()
     assert len(pr) == r["n_coinc"]
+
+
+@pytest.mark.parametrize("ptype,prange", [(0, 1), (0, 0), (1, 0)])
+def test_phase_space_source_bit_exact(ptype, prange, scene_positron, data_dir, gpet_lib, oracle_mod, tmp_path):
+    """A phase-space file as the source (initialize.cu:76-115; setPosition-
+    ForPhoton, gPET_kernals.cu:563-604): positron records (ptype 0, with and
+    without positron range: each makes a pair, the second photon with its
+    time set) and photon records (ptype 1: one photon each, records with
+    t <= 0 dropped); histories, singles and coincidences against the oracle."""
+    import copy
+    from gpet_gb300 import formats as F
+    rng = np.random.default_rng(21 + 3 * ptype + prange)
+    n = 20000
+    rec = np.zeros((n, 8))
+    rec[:, 0:3] = rng.uniform(-1.0, 1.0, (n, 3))
+    rec[:, 3] = rng.uniform(0.0, 1.0e6, n)
+    if ptype == 1:
+        rec[::50, 3] = 0.0                           # dropped by the reference's t > 0 test
+    u = rng.standard_normal((n, 3))
+    rec[:, 4:7] = u / np.linalg.norm(u, axis=1, keepdims=True)
+    rec[:, 7] = rng.uniform(1.0e5, 6.0e5, n) if ptype == 0 else rng.choice([511.0e3, 350.0e3], n)
+    psf_path = tmp_path / "psf.dat"
+    rec.tofile(psf_path)
+    cfg = F.read_config(scene_positron.config_path)
+    cfg.usepsf, cfg.sourcefile, cfg.ptype, cfg.useprange, cfg.nparticle = 1, str(psf_path), ptype, prange, n
+    path = tmp_path / "input_PET.in"
+    F.write_config(str(path), cfg)
+    sc = copy.copy(scene_positron)
+    sc.config_path = str(path)
+    ctx, st, r = _run_both(sc, data_dir)
+    assert st["n_decays"] == n
+    gx = ctx.exits()
+    assert len(gx) == len(r["exits"]) == 2 * n
+    msg = _first_diff(gx, r["exits"], ["status", "panel", "nscat", "E", "x", "y", "z", "ux", "uy", "uz", "t"])
+    assert msg is None, msg
+    if ptype == 1:
+        assert (gx["status"][1::2] == 2).all()        # no second photon
+        assert (gx["status"][0::2][::50] == 2).all()  # t = 0 records emit nothing
+    gs, _ = ctx.singles()
+    assert len(gs) == r["n_singles"] > 0
+    assert np.array_equal(gs.view(np.uint8), r["singles"].view(np.uint8))
+    pr, cl = ctx.coincidences()
+    assert np.array_equal(pr, r["coinc"]) and np.array_equal(cl, r["coinc_class"])
