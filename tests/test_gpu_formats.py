@@ -152,3 +152,36 @@ def test_cli_writes_the_library_records(scene_positron, data_dir, gpet_lib, tmp_
         rec = np.concatenate([ids.view(np.uint32), f.view(np.uint32)], axis=1)
         return rec[np.lexsort(rec.T[::-1])]
     assert np.array_equal(hits(tmp_path / "cli"), hits(tmp_path / "lib"))
+
+
+def test_phantom_majorant_bounds_every_material(scene_positron, data_dir, gpet_lib):
+    """The Woodcock majorant (quirk Q1 fixed): node i holds 1 / the largest
+    mu rho_max over [E_(i-1), E_(i+1)] of the interpolated tables, so on every
+    energy the kernels can meet, the interpolated majorant times every
+    material's interpolated mu at its largest density stays <= 1 (a real
+    interaction probability never exceeds 1, prob never goes below 0)."""
+    from gpet_gb300 import formats as F
+    ctx = make_ctx(scene_positron, data_dir)
+    tab, e0, ide = ctx.majorant(0)
+    T = F.read_tables(data_dir)
+    cfg = F.read_config(scene_positron.config_path)
+    mat, den = F.read_phantom(cfg.matfile, cfg.denfile, tuple(cfg.pdim))
+    f32 = np.float32
+    E = np.linspace(T.eminph, T.emax * 0.9999, 200001).astype(f32)
+
+    def lerp(t, x):
+        x = np.clip(x, f32(0), f32(len(t) - 1))
+        i = np.minimum(x.astype(np.int64), len(t) - 2)
+        fr = (x - i.astype(f32)).astype(f32)
+        return (t[i] + fr * (t[i + 1] - t[i])).astype(f32)
+
+    lam = lerp(tab.astype(f32), (f32(ide) * (E - f32(e0))).astype(f32))
+    idle = f32((len(T.energy) - 1) / (float(T.energy[-1]) - float(T.energy[0])))
+    xe = (idle * (E - f32(T.energy[0]))).astype(f32)
+    worst = 0.0
+    for m in np.unique(mat):
+        rho = f32(den[mat == m].max())
+        mu = lerp(np.asarray(T.lamph[m], f32), xe)
+        worst = max(worst, float((lam.astype(np.float64) * float(rho) * mu.astype(np.float64)).max()))
+    assert worst <= 1.0 + 1e-5
+    assert worst > 0.9                                # and it is tight where the densest material dominates

@@ -327,3 +327,10 @@ def test_phase_space_source_bit_exact(ptype, prange, scene_positron, data_dir, g
     assert np.array_equal(gs.view(np.uint8), r["singles"].view(np.uint8))
     pr, cl = ctx.coincidences()
     assert np.array_equal(pr, r["coinc"]) and np.array_equal(cl, r["coinc_class"])
+    if prange:
+        # the same records through gpet_set_source_psf on a context loaded
+        # with its decay source: the same run
+        api_ctx = make_ctx(scene_positron, data_dir, record_exits=1)
+        api_ctx.set_source_psf(rec, ptype)
+        api_ctx.run()
+        assert np.array_equal(api_ctx.singles()[0].view(np.uint8), gs.view(np.uint8))
