@@ -140,7 +140,7 @@ def cpu_baseline(scene, seconds, threads=0, max_decays=200_000_000):
     import bridge
     bridge.build()
     o = bridge.OracleScene(scene.config_path, scene.options, os.path.join(ROOT, "data"), base_dir=scene.directory)
-    n0 = 200_000
+    n0 = min(200_000, o.n_decays)
     t0 = time.perf_counter()
     o.run(0, n0, precision="fp64", threads=threads)
     rate = n0 / max(time.perf_counter() - t0, 1e-6)
@@ -184,13 +184,13 @@ def run_reference(args):
         import bridge
         bridge.build()
         o = bridge.OracleScene(sc.config_path, sc.options, os.path.join(ROOT, "data"), base_dir=d)
-        n0 = 200_000
+        n0 = min(200_000, o.n_decays)
         t0 = time.perf_counter()
         o.run(0, n0, precision="fp64")
         rate = n0 / max(time.perf_counter() - t0, 1e-6)
         n = int(min(o.n_decays, max(n0, rate * args.ref_step_seconds)))
         for w in range(args.warmup):
-            o.run(0, min(n, 200_000), precision="fp64")
+            o.run(0, min(n, n0), precision="fp64")
         tot_c, tot_t, tot_d = 0, 0.0, 0
         for k in range(args.steps):
             b = (k * n) % max(1, o.n_decays - n + 1)

@@ -52,3 +52,24 @@ def test_ranks_draw_disjoint_streams(scene_small, data_dir, oracle_mod):
     b = oracle_for(scene_small, data_dir, sim_id=1).run(0, 4000, exits=True)["exits"]
     esc = (a["status"] == 1) & (b["status"] == 1)
     assert np.mean(a["x"][esc] == b["x"][esc]) < 0.01
+
+
+def test_bench_reference_arm_json_line():
+    """`bench.py --impl reference` (the CPU arm the GPU arm is compared
+    with) prints one JSON line with the contract's keys, on a small sample."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--steps", "2",
+                        "--warmup", "1", "--decays", "30000", "--ref-step-seconds", "0.2"],
+                       capture_output=True, text=True, timeout=600, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    j = json.loads(lines[0])
+    assert j["impl"] == "reference" and j["value"] > 0 and j["steps"] == 2 and j["warmup"] == 1
+    for k in ("metric", "unit", "ms_per_step", "higher_is_better", "config", "cpu_baseline", "e2e"):
+        assert k in j, k
+    assert j["e2e"]["h2d_bytes_per_step"] == 0 and j["e2e"]["d2h_bytes_per_step"] == 0
+    assert j["cpu_baseline"]["kind"] == "port"
