@@ -117,7 +117,7 @@ def test_positron_sampler_matches_reference_density(oracle_mod, data_dir):
         p = np.diff(np.interp(edges, E, cdf))
         exp = p / p.sum() * len(out)
         keep = exp > 20
-        chi2 = float((((h - exp) ** 2) / exp)[keep].sum())
+        chi2 = float((((h[keep] - exp[keep]) ** 2) / exp[keep]).sum())
         assert stats.chi2.sf(chi2, int(keep.sum()) - 1) > 1e-3, (row, chi2, int(keep.sum()))
 
 
