@@ -42,7 +42,8 @@ constexpr uint32_t kWaitLimit = 1u << 24;   // mbarrier polls before a wait give
 constexpr uint32_t kTagSurrogate = 6;       // Philox stream tag of the surrogate's draws
 
 namespace sg {
-constexpr int kIn = 16, kFeat = 16, kHid = 256, kOut = 208, kOutUsed = 204, kEmb = 8;
+constexpr int kIn = 16, kFeat = 16, kHid = 256, kOut = 208, kOutUsed = 204, kEmb = 6;
+constexpr int kEmbCol = 8;   // first input column of the panel embedding
 constexpr int kCry = 64, kMix = 4, kBins = 64;
 constexpr int kClassBin = 40;   // energy bins >= this (deposit >= 62.5 % of E) take the second crystal set
 constexpr int kColW = 128, kColMu = 132, kColLs = 136, kColE = 140;
@@ -85,9 +86,11 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b)
     return (uint32_t)__bfloat16_as_ushort(x) | ((uint32_t)__bfloat16_as_ushort(y) << 16);
 }
 
-// 16 features of a photon entering a panel; the last two place the entry
-// point within its crystal (-0.5 .. 0.5 pitch from the crystal's centre), which
-// makes the entry crystal a linear function of the inputs
+// 16 features of a photon entering a panel: y, z over the half-widths,
+// direction, E / 511 keV; where its straight path is at half the panel depth
+// and where it enters, each as the offset from the centre of the crystal it is
+// in (-0.5 .. 0.5 pitch: the crystal becomes a linear function of the inputs);
+// the panel's learned embedding
 __device__ __forceinline__ void features(const SurrogateDev& sd, const float* __restrict__ emb, int panel, float y,
                                          float z, float ux, float uy, float uz, float E, float f[16])
 {
@@ -97,7 +100,12 @@ __device__ __forceinline__ void features(const SurrogateDev& sd, const float* __
     f[3] = uy;
     f[4] = uz;
     f[5] = E * (1.0f / 511000.0f);
-    for (int k = 0; k < sg::kEmb; ++k) f[6 + k] = emb[panel * sg::kEmb + k];
+    const float a = fmaxf(fabsf(ux), 0.05f), hd = 0.5f * sd.depth;
+    const float ym = y + uy / a * hd, zm = z + uz / a * hd;
+    const float tym = (ym + sd.half_y) / sd.cry_pitch_y, tzm = (zm + sd.half_z) / sd.cry_pitch_z;
+    f[6] = tym - floorf(tym) - 0.5f;
+    f[7] = tzm - floorf(tzm) - 0.5f;
+    for (int k = 0; k < sg::kEmb; ++k) f[sg::kEmbCol + k] = emb[panel * sg::kEmb + k];
     const float ty = (y + sd.half_y) / sd.cry_pitch_y, tz = (z + sd.half_z) / sd.cry_pitch_z;
     f[14] = ty - floorf(ty) - 0.5f;
     f[15] = tz - floorf(tz) - 0.5f;
@@ -836,7 +844,7 @@ __global__ void k_emb_grad(const float* __restrict__ dX, const int32_t* __restri
          i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t s = i / sg::kEmb;
         const int k = (int)(i % sg::kEmb);
-        atomicAdd(&gemb[panel[s] * sg::kEmb + k], dX[s * sg::kIn + 6 + k]);
+        atomicAdd(&gemb[panel[s] * sg::kEmb + k], dX[s * sg::kIn + sg::kEmbCol + k]);
     }
 }
 

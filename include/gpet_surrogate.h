@@ -44,7 +44,7 @@ const char* gpet_surrogate_last_error(gpet_surrogate* s);
 /* Parameters, fp32, in this order: for each layer l = 0..4 its weights
  * [out][in] then biases [out] (in: 16, 256, 256, 256, 256; out: 256, 256,
  * 256, 256, 208; output rows 204-207 are padding
- * and stay zero), then the panel embedding [npanels][8]. */
+ * and stay zero), then the panel embedding [npanels][6]. */
 int64_t gpet_surrogate_param_count(gpet_surrogate* s);
 int gpet_surrogate_get_params(gpet_surrogate* s, float* out, int64_t n);
 int gpet_surrogate_set_params(gpet_surrogate* s, const float* in, int64_t n);

@@ -13,7 +13,8 @@ Only tests import it.
 """
 import numpy as np
 
-IN, FEAT, HID, OUT, OUT_USED, EMB = 16, 16, 256, 208, 204, 8
+IN, FEAT, HID, OUT, OUT_USED, EMB = 16, 16, 256, 208, 204, 6
+EMB_COL = 8             # first input column of the panel embedding
 CRY, MIX, BINS = 64, 4, 64
 CLASS_BIN = 40          # energy bins >= this take the second crystal set (columns 64-127)
 COL_W, COL_MU, COL_LS, COL_E = 128, 132, 136, 140
@@ -67,10 +68,11 @@ def default_pitch(half_y, half_z, crystal_n):
     return 2.0 * half_y / side, 2.0 * half_z / side
 
 
-def features(rec, emb, half_y, half_z, pitch):
+def features(rec, emb, half_y, half_z, pitch, depth_len):
     """The 16 inputs: y, z over the half-widths, direction, E / 511 keV, the
-    panel embedding, the entry point's offset from its crystal's centre in
-    pitches (float32 arithmetic, as on the GPU)."""
+    offsets (in pitches, from the crystal centre) of the straight path at half
+    the panel depth, the panel embedding, the entry point's offsets (float32
+    arithmetic, as on the GPU)."""
     n = len(rec)
     f = np.zeros((n, IN), np.float64)
     y = rec["y"].astype(np.float32)
@@ -81,7 +83,16 @@ def features(rec, emb, half_y, half_z, pitch):
     f[:, 3] = rec["uy"]
     f[:, 4] = rec["uz"]
     f[:, 5] = rec["E"].astype(np.float32) * np.float32(1.0 / 511000.0)
-    f[:, 6:14] = emb[rec["panel"]]
+    ux = rec["ux"].astype(np.float32)
+    a = np.maximum(np.abs(ux), np.float32(0.05))
+    hd = np.float32(0.5) * np.float32(depth_len)
+    ym = y + rec["uy"].astype(np.float32) / a * hd
+    zm = z + rec["uz"].astype(np.float32) / a * hd
+    tym = (ym + np.float32(half_y)) / np.float32(pitch[0])
+    tzm = (zm + np.float32(half_z)) / np.float32(pitch[1])
+    f[:, 6] = tym - np.floor(tym) - np.float32(0.5)
+    f[:, 7] = tzm - np.floor(tzm) - np.float32(0.5)
+    f[:, EMB_COL:EMB_COL + EMB] = emb[rec["panel"]]
     ty = (y + np.float32(half_y)) / np.float32(pitch[0])
     tz = (z + np.float32(half_z)) / np.float32(pitch[1])
     f[:, 14] = ty - np.floor(ty) - np.float32(0.5)
@@ -160,7 +171,7 @@ def forward_backward(params, rec, npanels, half_y, half_z, depth_len, crystal_n,
     r = bf16 if rounding else (lambda x: np.asarray(x, np.float64))
     if pitch is None:
         pitch = default_pitch(half_y, half_z, crystal_n)
-    f = features(rec, emb, half_y, half_z, pitch)
+    f = features(rec, emb, half_y, half_z, pitch, depth_len)
     x = r(f).astype(np.float64)
     ins, Zs = [x], []
     h = x
@@ -188,7 +199,7 @@ def forward_backward(params, rec, npanels, half_y, half_z, depth_len, crystal_n,
             dz = dinp * silu_grad(Zs[l - 1])
         else:
             ge = np.zeros((npanels, EMB))
-            np.add.at(ge, rec["panel"], dinp[:, 6:14])
+            np.add.at(ge, rec["panel"], dinp[:, EMB_COL:EMB_COL + EMB])
             g[emb_off:] = ge.ravel()
     # padding entries carry no gradient
     w0, _ = lay[0]

@@ -22,7 +22,7 @@ def test_layout():
     lay, emb_off, total = S.offsets(NP)
     assert lay[0] == (0, 16 * 256)
     assert emb_off == 255184
-    assert total == 255184 + NP * 8
+    assert total == 255184 + NP * S.EMB
     macs = 16 * 256 + 3 * 256 * 256 + 256 * 204
     assert macs == 252928
 
@@ -41,7 +41,7 @@ def test_backward_matches_finite_differences():
         for _ in range(4):
             picks.append(w + int(rng.integers(rows)) * K + int(rng.integers(cols)))
         picks.append(b + int(rng.integers(rows)))
-    picks += [emb_off + int(i) for i in rng.integers(0, NP * 8, 4)]
+    picks += [emb_off + int(i) for i in rng.integers(0, NP * S.EMB, 4)]
     # head columns of each kind: crystal, mixture weight / mean / log sigma, energy
     w4, b4 = lay[-1]
     picks += [b4 + 3, b4 + S.CRY + 9, b4 + S.COL_W + 1, b4 + S.COL_MU + 2, b4 + S.COL_LS + 3, b4 + S.COL_E + 5]
@@ -73,7 +73,9 @@ def test_in_crystal_offset_features():
     rec = np.zeros(4, S.ENTRY_DTYPE)
     rec["y"] = [-1.2, -1.05, 0.0, 1.1]
     rec["z"] = [0.15, -0.6, 0.299, -1.2]
-    f = S.features(rec, np.zeros((1, S.EMB)), 1.2, 1.2, (0.3, 0.3))
+    rec["ux"] = -1.0                                  # normal incidence: the mid-depth point is the entry point
+    f = S.features(rec, np.zeros((1, S.EMB)), 1.2, 1.2, (0.3, 0.3), 2.0)
+    assert np.array_equal(f[:, 6:8], f[:, 14:16])
     assert np.allclose(f[:, 14], [-0.5, 0.0, -0.5, 0.1666667], atol=1e-5)
     assert np.allclose(f[:, 15], [0.0, -0.5, 0.4966667, -0.5], atol=1e-5)
     assert (np.abs(f[:, 14:]) <= 0.5).all()
