@@ -554,8 +554,6 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
     int32_t pann = 0;
     PEvent ev[kMaxPulse];
     int nev = 0, nh = 0, step = 0;
-    int32_t hid[kMaxHits][4];
-    float hf[kMaxHits][5];
     int32_t parn = 0, eid = 0, scat = 0, sim = 0;
     bool overflow = false;
     unsigned nsteps = 0;
@@ -564,6 +562,30 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
     // simulation's key): key and id are re-read when a block is generated
     uint32_t rblk = 0, rbuf[4] = {0u, 0u, 0u, 0u};
     int rpos = 4;
+    // a deposit goes to the hit list at once (at most kMaxHits per photon),
+    // the lanes that record one at the same point sharing one atomic
+    auto put_hit = [&](int32_t M_id, int32_t L_id, int32_t type, float Ed, double t) {
+        if (nh >= kMaxHits) {
+            overflow = true;
+            return;
+        }
+        nh++;
+        const unsigned act = __activemask();
+        const int leader = __ffs(act) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(H.count, (unsigned long long)__popc(act));
+        base = __shfl_sync(act, base, leader);
+        const unsigned long long o = base + __popc(act & lt);
+        if (o >= (unsigned long long)H.cap) {
+            n_hdrop++;
+            return;
+        }
+        H.id[5 * o + 0] = parn;
+        H.id[5 * o + 1] = pann; H.id[5 * o + 2] = M_id; H.id[5 * o + 3] = L_id; H.id[5 * o + 4] = type;
+        H.f[5 * o + 0] = Ed; H.f[5 * o + 1] = (float)t;
+        H.f[5 * o + 2] = L.x[0]; H.f[5 * o + 3] = L.x[1]; H.f[5 * o + 4] = L.x[2];
+        if (H.sim) H.sim[o] = sim;
+    };
     auto unif = [&]() -> float {
         if (rpos == 4) {
             const SimDesc& S = kMulti ? sims[sim] : sS;
@@ -664,16 +686,7 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                         e.pann = pann; e.modn = M_id; e.cryn = L_id;
                         e.siten = pann * S.moduleN * S.crystalN + M_id * S.crystalN + L_id;
                         e.E = de; e.t = L.t + (double)L.tf; e.x = L.x[0]; e.y = L.x[1]; e.z = L.x[2];
-                        if (rec_hits) {
-                            if (nh < kMaxHits) {
-                                hid[nh][0] = pann; hid[nh][1] = M_id; hid[nh][2] = L_id; hid[nh][3] = 1;
-                                hf[nh][0] = de; hf[nh][1] = (float)e.t; hf[nh][2] = L.x[0]; hf[nh][3] = L.x[1];
-                                hf[nh][4] = L.x[2];
-                                nh++;
-                            } else {
-                                overflow = true;
-                            }
-                        }
+                        if (rec_hits) put_hit(M_id, L_id, 1, de, e.t);
                         if (!adder(ev, nev, e)) overflow = true;
                     }
                     L.E -= de;
@@ -698,16 +711,7 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                     e.pann = pann; e.modn = M_id; e.cryn = L_id;
                     e.siten = pann * S.moduleN * S.crystalN + M_id * S.crystalN + L_id;
                     e.E = dep; e.t = L.t + (double)L.tf; e.x = L.x[0]; e.y = L.x[1]; e.z = L.x[2];
-                    if (rec_hits) {
-                        if (nh < kMaxHits) {
-                            hid[nh][0] = pann; hid[nh][1] = M_id; hid[nh][2] = L_id; hid[nh][3] = type;
-                            hf[nh][0] = dep; hf[nh][1] = (float)e.t; hf[nh][2] = L.x[0]; hf[nh][3] = L.x[1];
-                            hf[nh][4] = L.x[2];
-                            nh++;
-                        } else {
-                            overflow = true;
-                        }
-                    }
+                    if (rec_hits) put_hit(M_id, L_id, type, dep, e.t);
                     if (!adder(ev, nev, e)) overflow = true;
                 }
                 done = true;
@@ -754,30 +758,6 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                 P.E[o] = ev[i].E; P.x[o] = ev[i].x; P.y[o] = ev[i].y; P.z[o] = ev[i].z;
                 P.meta[o] = (uint8_t)(i | (scat ? 0x80 : 0));
                 if (P.sim) P.sim[o] = sim;
-            }
-        }
-        if (rec_hits) {
-            const int my_h = done ? nh : 0;
-            int hinc = my_h;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                int v = __shfl_up_sync(0xffffffffu, hinc, o);
-                if (lane >= o) hinc += v;
-            }
-            int htot = __shfl_sync(0xffffffffu, hinc, 31);
-            if (htot) {
-                unsigned long long b = 0;
-                if (lane == 31) b = atomicAdd(H.count, (unsigned long long)htot);
-                b = __shfl_sync(0xffffffffu, b, 31);
-                unsigned long long o = b + (unsigned long long)(hinc - my_h);
-                for (int i = 0; i < my_h; ++i, ++o) {
-                    if (o >= (unsigned long long)H.cap) { n_hdrop++; continue; }
-                    H.id[5 * o + 0] = parn;
-                    H.id[5 * o + 1] = hid[i][0]; H.id[5 * o + 2] = hid[i][1]; H.id[5 * o + 3] = hid[i][2];
-                    H.id[5 * o + 4] = hid[i][3];
-                    for (int c = 0; c < 5; ++c) H.f[5 * o + c] = hf[i][c];
-                    if (H.sim) H.sim[o] = sim;
-                }
             }
         }
         if (done) active = false;
