@@ -464,17 +464,30 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
 }
 
 // ------------------------------------------------------------- detector
+// a deposit of one photon: all of them lie in the photon's panel, so module
+// and crystal identify the crystal (the site number follows from them)
 struct PEvent {
-    int32_t pann, modn, cryn, siten;
+    int32_t modn, cryn;
     double t;
     float E, x, y, z;
 };
 
-// adder, gPET_kernals.cu:737-755
+// the pulse's site number after readout at the configured depth
+// (setSitenum levels of gPET_kernals.cu:778-808: depth 3 and up keep the crystal)
+__device__ __forceinline__ int32_t site_of(const SimDesc& S, int32_t pann, int32_t modn, int32_t cryn)
+{
+    const int depth = S.rdepth == 3 ? 3 : (S.rpolicy == 1 ? 2 : S.rdepth);
+    if (depth == 0) return 0;
+    if (depth == 1) return pann;
+    if (depth == 2) return pann * S.moduleN + modn;
+    return pann * S.moduleN * S.crystalN + modn * S.crystalN + cryn;
+}
+
+// adder, gPET_kernals.cu:737-755 (same crystal: same module and crystal)
 __device__ __forceinline__ bool adder(PEvent* ev, int& n, const PEvent& e)
 {
     for (int i = 0; i < n; ++i) {
-        if (e.siten == ev[i].siten) {
+        if (e.modn == ev[i].modn && e.cryn == ev[i].cryn) {
             float s = ev[i].E + e.E;
             ev[i].x = (ev[i].x * ev[i].E + e.x * e.E) / s;
             ev[i].y = (ev[i].y * ev[i].E + e.y * e.E) / s;
@@ -494,11 +507,11 @@ __device__ __forceinline__ int readout(const SimDesc& S, PEvent* ev, int n)
     int depth = S.rdepth, policy = S.rpolicy;
     if (depth == 3) return n;
     if (policy == 1) depth = 2;
-    for (int i = 0; i < n; ++i) {
-        if (depth == 0) ev[i].siten = 0;
-        else if (depth == 1) ev[i].siten = ev[i].pann;
-        else if (depth == 2) ev[i].siten = ev[i].pann * S.moduleN + ev[i].modn;
-    }
+    // the site at this depth within the photon's panel: all one site at
+    // depths 0 and 1, the module at 2, the crystal above
+    auto key = [&](const PEvent& e) -> int32_t {
+        return depth <= 1 ? 0 : (depth == 2 ? e.modn : e.modn * S.crystalN + e.cryn);
+    };
     unsigned dead = 0;
     int k = 0;
     for (int i = 0; i < n; ++i) {
@@ -506,7 +519,7 @@ __device__ __forceinline__ int readout(const SimDesc& S, PEvent* ev, int n)
         PEvent e0 = ev[i];
         for (int j = i + 1; j < n; ++j) {
             const PEvent e = ev[j];
-            if (e.siten == e0.siten) {   // one photon: parn always equal
+            if (key(e) == key(e0)) {   // one photon: parn always equal
                 if (policy == 1) {
                     float s = e0.E + e.E;
                     e0.x = (e0.x * e0.E + e.x * e.E) / s;
@@ -683,8 +696,7 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                     float phi = unif();
                     if (m_id != 1) {   // a crystal (not the gap)
                         PEvent e;
-                        e.pann = pann; e.modn = M_id; e.cryn = L_id;
-                        e.siten = pann * S.moduleN * S.crystalN + M_id * S.crystalN + L_id;
+                        e.modn = M_id; e.cryn = L_id;
                         e.E = de; e.t = L.t + (double)L.tf; e.x = L.x[0]; e.y = L.x[1]; e.z = L.x[2];
                         if (rec_hits) put_hit(M_id, L_id, 1, de, e.t);
                         if (!adder(ev, nev, e)) overflow = true;
@@ -708,8 +720,7 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                 }
                 if (m_id != 1) {   // a crystal (not the gap)
                     PEvent e;
-                    e.pann = pann; e.modn = M_id; e.cryn = L_id;
-                    e.siten = pann * S.moduleN * S.crystalN + M_id * S.crystalN + L_id;
+                    e.modn = M_id; e.cryn = L_id;
                     e.E = dep; e.t = L.t + (double)L.tf; e.x = L.x[0]; e.y = L.x[1]; e.z = L.x[2];
                     if (rec_hits) put_hit(M_id, L_id, type, dep, e.t);
                     if (!adder(ev, nev, e)) overflow = true;
@@ -753,8 +764,9 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
             unsigned long long o = b + (unsigned long long)(inc - my_ev);
             for (int i = 0; i < my_ev; ++i, ++o) {
                 if (o >= (unsigned long long)P.cap) { n_pdrop++; continue; }
-                P.parn[o] = parn; P.pann[o] = ev[i].pann; P.modn[o] = ev[i].modn; P.cryn[o] = ev[i].cryn;
-                P.siten[o] = ev[i].siten; P.eventid[o] = eid; P.t[o] = ev[i].t;
+                P.parn[o] = parn; P.pann[o] = pann; P.modn[o] = ev[i].modn; P.cryn[o] = ev[i].cryn;
+                P.siten[o] = site_of(kMulti ? sims[sim] : sS, pann, ev[i].modn, ev[i].cryn);
+                P.eventid[o] = eid; P.t[o] = ev[i].t;
                 P.E[o] = ev[i].E; P.x[o] = ev[i].x; P.y[o] = ev[i].y; P.z[o] = ev[i].z;
                 P.meta[o] = (uint8_t)(i | (scat ? 0x80 : 0));
                 if (P.sim) P.sim[o] = sim;
