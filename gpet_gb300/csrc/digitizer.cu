@@ -717,6 +717,53 @@ __global__ void k_gather_events(PulseDev P, const uint32_t* __restrict__ idx, in
     }
 }
 
+// the same records for a destination in mapped (pinned) host memory: a block
+// builds 256 records in shared memory and stores them as consecutive 16-byte
+// words, so every store that crosses the host link is a whole, aligned word;
+// flags[j] = 1 for a record whose photon scattered in the phantom (meta bit 7).
+// out must be 16-byte aligned.
+__global__ void __launch_bounds__(256) k_gather_events_mapped(PulseDev P, const uint32_t* __restrict__ idx, int64_t n,
+                                                              const float* __restrict__ Eb,
+                                                              const float* __restrict__ xb,
+                                                              const float* __restrict__ yb,
+                                                              const float* __restrict__ zb,
+                                                              const int32_t* __restrict__ site, uint4* out,
+                                                              uint8_t* flags)
+{
+    __shared__ EventRec st[256];
+    static_assert(sizeof(st) % 16 == 0, "the staged tile is whole 16-byte words");
+    for (int64_t t0 = (int64_t)blockIdx.x * 256; t0 < n; t0 += (int64_t)gridDim.x * 256) {
+        const int64_t j = t0 + threadIdx.x;
+        if (j < n) {
+            const int64_t p = idx ? (int64_t)idx[j] : j;
+            EventRec e;
+            e.parn = P.parn[p]; e.pann = P.pann[p]; e.modn = P.modn[p]; e.cryn = P.cryn[p];
+            e.siten = site[p];
+            e.eventid = P.eventid[p];
+            e.t = P.t[p];
+            e.E = Eb[p]; e.x = xb[p]; e.y = yb[p]; e.z = zb[p];
+            st[threadIdx.x] = e;
+            if (flags) flags[j] = (P.meta[p] & 0x80u) ? 1 : 0;
+        }
+        __syncthreads();
+        const int64_t cnt = n - t0 < 256 ? n - t0 : 256;
+        const int words = (int)cnt * (int)(sizeof(EventRec) / 16);
+        const uint4* w = reinterpret_cast<const uint4*>(st);
+        for (int k = threadIdx.x; k < words; k += 256) out[t0 * (int64_t)(sizeof(EventRec) / 16) + k] = w[k];
+        __syncthreads();
+    }
+}
+
+int gather_events_mapped(const PulseDev& P, const uint32_t* idx, int64_t n, const DigiScratch& D, EventRec* out,
+                         uint8_t* flags, cudaStream_t s)
+{
+    if (n <= 0) return 0;
+    if (reinterpret_cast<uintptr_t>(out) & 15) return GPET_ERR_ARG;
+    k_gather_events_mapped<<<grid_for_g(n), 256, 0, s>>>(P, idx, n, D.Eb, D.xb, D.yb, D.zb, D.site,
+                                                         reinterpret_cast<uint4*>(out), flags);
+    return cudaGetLastError() == cudaSuccess ? 0 : GPET_ERR_CUDA;
+}
+
 int gather_events(const PulseDev& P, const uint32_t* idx, int64_t n, bool blurred, const DigiScratch& D,
                   EventRec* out, uint8_t* meta, cudaStream_t s)
 {

@@ -1691,6 +1691,19 @@ static int gather(gpet_ctx* c, Work& W, const uint32_t* d_idx, int64_t n, bool b
 
 static bool results(gpet_ctx* c) { return c->have_results && c->work; }
 
+// the device address of pinned (page-locked, mapped) host memory, or null for
+// any other memory (pageable, device, unknown)
+static void* mapped_host(const void* p)
+{
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 extern "C" {
 
 int gpet_get_singles(gpet_ctx* c, gpet_event* buf, uint8_t* scat, int64_t cap, int64_t* n)
@@ -1702,10 +1715,21 @@ int gpet_get_singles(gpet_ctx* c, gpet_event* buf, uint8_t* scat, int64_t cap, i
     *n = W.s_off[c->res_sim + 1] - off;
     if (!buf || *n == 0) return GPET_OK;
     if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the singles");
-    // gathered on the device and copied straight into the caller's buffers
+    PulseDev P = pulse_view(W);
+    // into pinned caller memory the gather kernel stores the records itself
+    // (whole 16-byte words across the host link, no staging copy)
+    void* dbuf = mapped_host(buf);
+    void* dscat = mapped_host(scat);
+    if (dbuf && !(reinterpret_cast<uintptr_t>(dbuf) & 15) && (!scat || dscat)) {
+        if (gather_events_mapped(P, W.dg.single_idx + off, *n, W.dg, static_cast<EventRec*>(dbuf),
+                                 static_cast<uint8_t*>(dscat), c->stream))
+            return fail(c, GPET_ERR_CUDA, "gather of event records failed");
+        CK(cudaStreamSynchronize(c->stream));
+        return GPET_OK;
+    }
+    // otherwise gathered on the device and copied into the caller's buffers
     CK(W.g_ev.ensure((size_t)*n * sizeof(EventRec)));
     CK(W.g_meta.ensure((size_t)*n));
-    PulseDev P = pulse_view(W);
     if (gather_events(P, W.dg.single_idx + off, *n, true, W.dg, W.g_ev.as<EventRec>(), W.g_meta.as<uint8_t>(),
                       c->stream))
         return fail(c, GPET_ERR_CUDA, "gather of event records failed");

@@ -207,6 +207,11 @@ static_assert(sizeof(EventRec) == 48, "Event record is 48 bytes");
 
 int gather_events(const PulseDev& P, const uint32_t* idx, int64_t n, bool blurred, const DigiScratch& D,
                   EventRec* out, uint8_t* meta, cudaStream_t s);
+// the blurred records written straight into mapped (pinned) host memory seen
+// through its device address (16-byte aligned), flags[j] = scattered in the
+// phantom (may be null)
+int gather_events_mapped(const PulseDev& P, const uint32_t* idx, int64_t n, const DigiScratch& D, EventRec* out,
+                         uint8_t* flags, cudaStream_t s);
 
 // digitizer kernels (digitizer.cu), for callers that orchestrate them with
 // their own working memory

@@ -163,7 +163,10 @@ int gpet_digitize(gpet_ctx* ctx, const gpet_event* pulses, const uint8_t* scat, 
                   gpet_run_stats* stats);
 
 /* ------------------------------------------------------------ outputs */
-/* Each copies into caller memory; with buf == NULL only *n is set. */
+/* Each copies into caller memory; with buf == NULL only *n is set.
+ * gpet_get_singles: when buf (16-byte aligned) and scat (or scat == NULL) are
+ * pinned host memory, the gather kernel writes the records there itself
+ * instead of staging them on the device and copying. */
 int gpet_get_singles(gpet_ctx* ctx, gpet_event* buf, uint8_t* scat, int64_t cap, int64_t* n);
 /* Pulses after adder + readout, ordered by (parn, slot) (adder.dat content). */
 int gpet_get_pulses(gpet_ctx* ctx, gpet_event* buf, uint8_t* scat, uint8_t* slot, int64_t cap, int64_t* n);

@@ -1,5 +1,6 @@
 """The native loaders (C++) and the Python readers are independent
 implementations of gPET's parsers; both must see the same numbers."""
+import ctypes
 import os
 
 import numpy as np
@@ -185,3 +186,39 @@ def test_phantom_majorant_bounds_every_material(scene_positron, data_dir, gpet_l
         worst = max(worst, float((lam.astype(np.float64) * float(rho) * mu.astype(np.float64)).max()))
     assert worst <= 1.0 + 1e-5
     assert worst > 0.9                                # and it is tight where the densest material dominates
+
+
+def test_singles_into_pinned_memory_match_the_copy(scene_positron, data_dir, gpet_lib):
+    """gpet_get_singles writes straight into pinned buffers (the gather kernel's
+    own stores); the records and flags equal those of the staged copy into
+    pageable memory, also for an unaligned pinned buffer (the copy path) and
+    without flags."""
+    import torch
+    from gpet_gb300 import formats as F
+    ctx = make_ctx(scene_positron, data_dir, seed=91, n_decays=2000000)
+    ctx.run()
+    ev0, sc0 = ctx.singles()
+    n = len(ev0)
+    assert n > 1000
+
+    def pinned(nbytes):
+        return torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+
+    for shift in (0, 8):
+        raw_ev = pinned(n * 48 + 64)
+        raw_sc = pinned(n + 64)
+        base = (-raw_ev.ctypes.data) % 16 + shift
+        ev_buf = raw_ev[base:base + n * 48].view(F.EVENT_DTYPE)
+        sc_buf = raw_sc[:n]
+        ev_buf[:] = np.zeros(1, F.EVENT_DTYPE)
+        sc_buf[:] = 7
+        ev, sc = ctx.singles(out=(ev_buf, sc_buf))
+        assert ev.tobytes() == ev0.tobytes(), shift
+        assert np.array_equal(sc, sc0), shift
+    # pinned records without flags
+    raw_ev = pinned(n * 48 + 64)
+    base = (-raw_ev.ctypes.data) % 16
+    ev_buf = raw_ev[base:base + n * 48].view(F.EVENT_DTYPE)
+    m = ctypes.c_int64()
+    assert ctx.L.gpet_get_singles(ctx.h, ev_buf.ctypes.data, None, n, ctypes.byref(m)) == 0
+    assert m.value == n and ev_buf.tobytes() == ev0.tobytes()
