@@ -137,6 +137,7 @@ struct gpet_ctx {
     int pdim[3] = {0, 0, 0};
     float poff[3] = {0, 0, 0}, psz[3] = {0, 0, 0};
     float maxden_ph[10] = {0};
+    bool wck_ph_valid = false;   // wck_ph is built from the loaded tables and maxden_ph
     std::vector<float> wck_ph, wck_det;
     float wck_e0 = 0, wck_ide = 0;
     std::vector<int64_t> src_first, src_count;
@@ -426,6 +427,7 @@ int gpet_load_tables(gpet_ctx* c, const char* data_dir)
     CK(c->d_rayff.ensure(T.rayff.size() * 4));
     CK(cudaMemcpy(c->d_rayff.p, T.rayff.data(), T.rayff.size() * 4, cudaMemcpyHostToDevice));
     c->have_tables = true;
+    c->wck_ph_valid = false;
     return GPET_OK;
 }
 
@@ -481,10 +483,16 @@ int gpet_set_phantom(gpet_ctx* c, const int32_t* mat, const float* den, const in
     float maxden[10] = {0};
     for (int m = 0; m < 10 && m < c->tab.nmat; ++m) std::memcpy(&maxden[m], &h[m], 4);
     for (int k = 0; k < 3; ++k) { c->pdim[k] = dims[k]; c->poff[k] = offset[k]; c->psz[k] = size[k]; }
-    std::memcpy(c->maxden_ph, maxden, sizeof(maxden));
-    build_wck(c->tab, table_idle(c->tab), maxden, c->wck_ph, c->wck_e0, c->wck_ide);
-    CK(c->d_wck_ph.ensure(kNwck * 4));
-    CK(cudaMemcpy(c->d_wck_ph.p, c->wck_ph.data(), kNwck * 4, cudaMemcpyHostToDevice));
+    // the majorant depends on the tables and the densest voxel of each
+    // material only: a phantom with the same maxima keeps it
+    if (!c->wck_ph_valid || std::memcmp(c->maxden_ph, maxden, sizeof(maxden)) != 0) {
+        c->wck_ph_valid = false;
+        std::memcpy(c->maxden_ph, maxden, sizeof(maxden));
+        build_wck(c->tab, table_idle(c->tab), maxden, c->wck_ph, c->wck_e0, c->wck_ide);
+        CK(c->d_wck_ph.ensure(kNwck * 4));
+        CK(cudaMemcpy(c->d_wck_ph.p, c->wck_ph.data(), kNwck * 4, cudaMemcpyHostToDevice));
+        c->wck_ph_valid = true;
+    }
     c->have_phantom = true;
     return GPET_OK;
 }
