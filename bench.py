@@ -610,6 +610,119 @@ def run_surrogate_workload(args):
     print(json.dumps(line), flush=True)
 
 
+WIDEN_WORKLOAD = ("widen: the positron workload with one optional feature at a time - phase-space records of "
+                  "the emitted and escaped photons, a quadric exclusion (cylinder r=6 mm along each crystal "
+                  "block's depth axis), two-material crystals (back 10 mm LSO), background singles (Poisson, "
+                  "mean gap 270 us, 511 +- 60 keV), and the sinogram of the run's coincidences")
+
+
+def run_widen_workload(args):
+    """Cost of each widened feature on the positron workload: per variant W
+    untimed and K timed acquisitions (device time of the run's CUDA events,
+    host wall time beside it, L2 flushed before each), with the launch shape
+    the tuner picks for the plain run. Phase-space records are kept for
+    args.psf_decays decays per step (host memory: 80 B per decay)."""
+    import numpy as np
+    import torch
+    from gpet_gb300 import api, formats as F, scenes
+    torch.cuda.set_device(0)
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda:0")
+    data = os.path.join(ROOT, "data")
+    res = {}
+    with tempfile.TemporaryDirectory() as d:
+        sc = make_scene(d, args.decays, "positron")
+
+        def variant_config(name, surfaces=None, geo=None):
+            cfg = F.read_config(sc.config_path)
+            if surfaces is not None:
+                cfg.surfaces = surfaces
+            if geo is not None:
+                cfg.geofile = geo
+            path = os.path.join(d, "input_%s.in" % name)
+            F.write_config(path, cfg)
+            return path
+
+        geo3 = os.path.join(d, "ring3.geo")
+        F.write_geo(geo3, 8, (0, 0, 1), 45.0, (scenes.MAT_LYSO, scenes.MAT_AIR, 9), (7.1, 0.001025, 7.4),
+                    scenes.ring_panel0(8.0, 8, 8, 0.298, 0.002, 2.0))
+        variants = [
+            ("plain", sc.config_path, {}, args.decays),
+            ("phase_space", sc.config_path, {"record_source": 1, "record_exits": 1}, args.psf_decays),
+            ("quadric_exclusion", variant_config("quadric", [[0, 1, 1, 0, 0, 0, 0, 0, 0, -0.6 ** 2]]), {},
+             args.decays),
+            ("two_material_crystals", variant_config("lso", [[0, 0, 0, 0, 0, 0, 1, 0, 0, 1.0]], geo3), {},
+             args.decays),
+            ("background_singles", sc.config_path,
+             {"noise_lambda_us": 270.0, "noise_emean_ev": 511000.0, "noise_sigma_ev": 60000.0}, args.decays),
+        ]
+        shape = None
+        for name, cfg_path, extra, nd in variants:
+            ctx = api.Context(0)
+            opts = dict(sc.options, data_dir=data, base_dir=d, n_decays=nd)
+            opts.update(args.set)
+            opts.update(extra)
+            ctx.set_options(opts)
+            ctx.load_config(cfg_path)
+            if shape is None:
+                shape = ctx.autotune(args.tune_decays) if args.autotune else None
+            elif shape:
+                ctx.set_options({"sub_decays": shape["sub_decays"], "chunk_decays": shape["chunk_decays"],
+                                 "source_threads": shape["source_threads"],
+                                 "detector_threads": shape["detector_threads"],
+                                 "drain_period": shape["drain_period"]})
+            for w in range(args.warmup):
+                ctx.set_option("seed", 1000 + w)
+                ctx.run()
+            tot = {"ms": 0.0, "wall": 0.0, "src": 0.0, "ph": 0.0, "det": 0.0, "dig": 0.0, "coinc": 0, "singles": 0,
+                   "hits": 0, "noise": 0, "records": 0}
+            for k in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                ctx.set_option("seed", 20261203 + k)
+                t0 = time.perf_counter()
+                st = ctx.run()
+                tot["wall"] += time.perf_counter() - t0
+                tot["ms"] += st["ms_total"]; tot["src"] += st["ms_source"]; tot["ph"] += st["ms_phantom"]
+                tot["det"] += st["ms_detector"]; tot["dig"] += st["ms_digitizer"] + st["ms_coincidence"]
+                tot["coinc"] += st["n_coinc"]; tot["singles"] += st["n_singles"]; tot["hits"] += st["n_hits"]
+                tot["noise"] += st["n_noise"]
+                if name == "phase_space":
+                    tot["records"] += ctx._count(ctx.L.gpet_get_source_records, None)
+                    tot["records"] += ctx._count(ctx.L.gpet_get_phantom_records, None)
+            K = args.steps
+            r = {"decays_per_step": nd, "ms_per_step": tot["ms"] / K, "wall_ms_per_step": 1e3 * tot["wall"] / K,
+                 "decays_per_s": nd / (tot["ms"] / K * 1e-3),
+                 "stage_ms": {"source": tot["src"] / K, "phantom": tot["ph"] / K, "detector": tot["det"] / K,
+                              "digitizer_and_coincidences": tot["dig"] / K},
+                 "coincidences_per_step": tot["coinc"] / K, "singles_per_step": tot["singles"] / K,
+                 "coincidences_per_s": tot["coinc"] / (tot["ms"] * 1e-3)}
+            if name == "phase_space":
+                r["records_per_step"] = tot["records"] / K
+                r["records_per_s_wall"] = tot["records"] / tot["wall"]
+            if name == "background_singles":
+                r["background_singles_per_step"] = tot["noise"] / K
+            if name == "plain":
+                # sinogram of the last run's coincidences (host clock: launch, binning, copy-back)
+                ts = []
+                for _ in range(5):
+                    t0 = time.perf_counter()
+                    sino = ctx.sinogram(128, 96, 8, 6.0, 1.2)
+                    ts.append(time.perf_counter() - t0)
+                t_s = statistics.median(ts)
+                r["sinogram"] = {"bins": [8, 96, 128], "ms": 1e3 * t_s, "coincidences": int(st["n_coinc"]),
+                                 "binned": int(sino.sum()), "coincidences_per_s": st["n_coinc"] / t_s}
+            res[name] = r
+            ctx.close()
+    base = res["plain"]["ms_per_step"]
+    for name, r in res.items():
+        r["ms_vs_plain"] = r["ms_per_step"] / base * (res["plain"]["decays_per_step"] / r["decays_per_step"])
+    line = {"metric": "cost of the widened features (device ms per acquisition)", "workload": "widen",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WIDEN_WORKLOAD, "base": WORKLOAD, "l2": "flushed before each acquisition"},
+            "launch_shape": shape if shape else "library defaults", "variants": res}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -629,7 +742,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=-1,
                     help="steps of the end-to-end leg (default max(2, steps/2); 0 skips it: profiling only)")
     ap.add_argument("--gloo", action="store_true", help=argparse.SUPPRESS)
-    ap.add_argument("--workload", choices=["positron", "batched64", "surrogate", "surrogate_batched64", "large"],
+    ap.add_argument("--workload", choices=["positron", "batched64", "surrogate", "surrogate_batched64", "large", "widen"],
                     default="positron",
                     help="positron: the headline workload; batched64: 64 uneven simulations in one job; "
                          "surrogate: the headline workload with the learned detector response; "
@@ -638,6 +751,7 @@ def main():
     ap.add_argument("--train-decays", type=int, default=200_000_000, help=argparse.SUPPRESS)
     ap.add_argument("--train-epochs", type=int, default=12, help=argparse.SUPPRESS)
     ap.add_argument("--batch-sims", type=int, default=64, help=argparse.SUPPRESS)
+    ap.add_argument("--psf-decays", type=int, default=10_000_000, help=argparse.SUPPRESS)
     args = ap.parse_args()
     args.set = dict(kv.split("=", 1) for kv in args.set)
     if args.decays is None:
@@ -652,6 +766,8 @@ def main():
         run_batched_workload(args, surrogate=True)
     elif args.workload == "surrogate":
         run_surrogate_workload(args)
+    elif args.workload == "widen":
+        run_widen_workload(args)
     else:
         run_ours(args)
 

@@ -39,6 +39,42 @@ struct DevBuf {
     template <class T> T* as() const { return reinterpret_cast<T*>(p); }
 };
 
+// grow-only page-locked host array: device-to-host copies into it run at the
+// host link's rate and asynchronously; resize() leaves the contents unset
+template <class T>
+struct PinnedVec {
+    T* p = nullptr;
+    size_t n = 0, cap = 0;
+    PinnedVec() = default;
+    PinnedVec(const PinnedVec&) = delete;
+    PinnedVec& operator=(const PinnedVec&) = delete;
+    ~PinnedVec() { if (p) cudaFreeHost(p); }
+    cudaError_t resize(size_t m)
+    {
+        if (m > cap) {
+            if (p) cudaFreeHost(p);
+            p = nullptr;
+            cap = n = 0;
+            cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&p), m * sizeof(T), cudaHostAllocDefault);
+            if (e != cudaSuccess) {
+                p = nullptr;
+                return e;
+            }
+            cap = m;
+        }
+        n = m;
+        return cudaSuccess;
+    }
+    void clear() { n = 0; }
+    size_t size() const { return n; }
+    bool empty() const { return n == 0; }
+    T* data() { return p; }
+    const T* data() const { return p; }
+    const T& operator[](size_t i) const { return p[i]; }
+    const T* begin() const { return p; }
+    const T* end() const { return p + n; }
+};
+
 }  // namespace
 
 // device work buffers and results of one run; a batch's contexts share the
@@ -149,9 +185,9 @@ struct gpet_ctx {
     // results of the last run this context took part in
     std::shared_ptr<Work> work;
     int res_sim = 0;
-    std::vector<ExitRec> host_exits;
+    PinnedVec<ExitRec> host_exits;       // every photon slot of the run (record_exits)
     std::vector<EntryRec> host_entries;
-    std::vector<SrcRec> host_source;
+    PinnedVec<SrcRec> host_source;       // every photon slot of the run (record_source)
     gpet_run_stats last{};
     bool have_results = false;
     cudaEvent_t ev[8] = {};
@@ -1050,6 +1086,8 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
             if (cs[s]->sur != c->sur) return fail(c, GPET_ERR_ARG, "the simulations of a batch share one surrogate or none");
         }
     CK(cudaSetDevice(c->device));
+    // a run that fails leaves no results (the record arrays are then partly written)
+    for (int s = 0; s < nsim; ++s) cs[s]->have_results = false;
     // nothing of an earlier run may still use the work buffers
     CK(cudaStreamSynchronize(c->stream2));
     std::vector<int64_t> nd(nsim);
@@ -1161,7 +1199,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     const bool rec_source = c->record_source && !transport_only;
     if (rec_source) {
         CK(W.source.ensure((size_t)2 * chunk * sizeof(SrcRec)));
-        c->host_source.assign((size_t)2 * ND, SrcRec{});
+        CK(c->host_source.resize((size_t)2 * ND));   // every slot is copied from the device
     } else {
         c->host_source.clear();
     }
@@ -1181,7 +1219,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     }
     if (rec_exits) {
         CK(W.exits.ensure((size_t)2 * chunk * sizeof(ExitRec)));
-        c->host_exits.assign((size_t)2 * ND, ExitRec{});
+        CK(c->host_exits.resize((size_t)2 * ND));   // every slot is copied from the device
     } else {
         c->host_exits.clear();
     }
@@ -1306,11 +1344,11 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         }
         const int64_t cn = waves[we - 1].g + waves[we - 1].n - cg0;
         if (rec_exits)
-            CK(cudaMemcpy(c->host_exits.data() + 2 * cg0, W.exits.p, (size_t)2 * cn * sizeof(ExitRec),
-                          cudaMemcpyDeviceToHost));
+            CK(cudaMemcpyAsync(c->host_exits.data() + 2 * cg0, W.exits.p, (size_t)2 * cn * sizeof(ExitRec),
+                               cudaMemcpyDeviceToHost, c->stream));
         if (rec_source)
-            CK(cudaMemcpy(c->host_source.data() + 2 * cg0, W.source.p, (size_t)2 * cn * sizeof(SrcRec),
-                          cudaMemcpyDeviceToHost));
+            CK(cudaMemcpyAsync(c->host_source.data() + 2 * cg0, W.source.p, (size_t)2 * cn * sizeof(SrcRec),
+                               cudaMemcpyDeviceToHost, c->stream));
         // room for the worst case of this chunk and of the one still in flight
         pulses_used = std::max<int64_t>(pulses_used, std::min<int64_t>((int64_t)hq3[1], W.p_cap));
         hits_used = std::max<int64_t>(hits_used, std::min<int64_t>((int64_t)hq3[2], W.h_cap));
@@ -1841,7 +1879,7 @@ int gpet_get_hits(gpet_ctx* c, int32_t* ids, float* f, int64_t cap, int64_t* n)
 int gpet_get_exits(gpet_ctx* c, void* buf, int64_t cap, int64_t* n)
 {
     if (!c || !n) return GPET_ERR_ARG;
-    *n = (int64_t)c->host_exits.size();
+    *n = results(c) ? (int64_t)c->host_exits.size() : 0;
     if (!buf || *n == 0) return GPET_OK;
     if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the exits");
     std::memcpy(buf, c->host_exits.data(), sizeof(ExitRec) * (size_t)*n);
@@ -2012,6 +2050,7 @@ int gpet_sinogram(gpet_ctx* c, const gpet_sino_params* sp, uint32_t* out)
 int gpet_get_source_records(gpet_ctx* c, gpet_psf_record* buf, int64_t cap, int64_t* n)
 {
     if (!c || !n) return GPET_ERR_ARG;
+    if (!results(c)) { *n = 0; return GPET_OK; }
     std::vector<SrcRec> v;
     source_records(c, v);
     *n = (int64_t)v.size();
@@ -2024,6 +2063,7 @@ int gpet_get_source_records(gpet_ctx* c, gpet_psf_record* buf, int64_t cap, int6
 int gpet_get_phantom_records(gpet_ctx* c, gpet_psf_record* buf, int64_t cap, int64_t* n)
 {
     if (!c || !n) return GPET_ERR_ARG;
+    if (!results(c)) { *n = 0; return GPET_OK; }
     std::vector<SrcRec> v;
     phantom_records(c, v);
     *n = (int64_t)v.size();

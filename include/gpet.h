@@ -124,7 +124,9 @@ int gpet_set_source_psf(gpet_ctx* ctx, const double* rec8, int64_t n, int ptype)
 
 /* ------------------------------------------------------------ run */
 /* Simulate the configured source and digitize: sampleParticle (gPET.cu:201-437)
- * or simulateParticle (gPET.cu:13-199) followed by the coincidence sorter. */
+ * or simulateParticle (gPET.cu:13-199) followed by the coincidence sorter.
+ * The previous run's results are dropped when a run starts; a run that fails
+ * leaves none (the gpet_get_* calls then report 0 records). */
 int gpet_run(gpet_ctx* ctx, gpet_run_stats* stats);
 /* No counterpart in the reference (one simulation per process there).
  * Runs n independent simulations (contexts on one device, each fully loaded;
