@@ -413,9 +413,11 @@ def run_batched_workload(args, surrogate=False):
             sur = api.Surrogate(gen, seed=9)
             losses = sur.train(rec, epochs=args.train_epochs, batch=8192, lr=2e-3)
             sur.set_domain(1.0e5, 5.2e5, 0.3)
+            calib = sur.calibrate(rec, iters=args.calib_iters) if args.calib_iters > 0 else None
             gen.close()
             train = {"decays": args.train_decays, "records": int(len(rec)), "epochs": args.train_epochs,
-                     "loss_last_epoch": float(losses[-1]), "seconds": time.perf_counter() - t0}
+                     "loss_last_epoch": float(losses[-1]), "calibration_passes": args.calib_iters,
+                     "calibration_last_max_log_ratio": calib, "seconds": time.perf_counter() - t0}
 
         def reseed(k):
             for c, sd in zip(ctxs, seeds):
@@ -556,6 +558,7 @@ def run_surrogate_workload(args):
         sur = api.Surrogate(gen, seed=9)
         losses = sur.train(rec, epochs=args.train_epochs, batch=8192, lr=2e-3)
         sur.set_domain(1.0e5, 5.2e5, 0.3)
+        calib = sur.calibrate(rec, iters=args.calib_iters) if args.calib_iters > 0 else None
         train_s = time.perf_counter() - t0
         gen.close()
         res = {}
@@ -592,7 +595,8 @@ def run_surrogate_workload(args):
             "config": {"workload": WORKLOAD, "decays_per_step": args.decays,
                        "training": {"decays": args.train_decays, "records": int(len(rec)),
                                     "epochs": args.train_epochs, "loss_per_epoch": [float(x) for x in losses],
-                                    "seconds": train_s},
+                                    "calibration_passes": args.calib_iters,
+                                    "calibration_last_max_log_ratio": calib, "seconds": train_s},
                        "domain": "entry energy 100-520 keV, >= 3 mm inside the panel edges, all panels"},
             "plain_mc": {"value": mc["coinc"] / (mc["ms"] * 1e-3), "ms_per_step": mc["ms"] / args.steps,
                          "detector_ms_per_step": mc["det"] / args.steps},
@@ -752,6 +756,7 @@ def main():
     ap.add_argument("--train-epochs", type=int, default=12, help=argparse.SUPPRESS)
     ap.add_argument("--batch-sims", type=int, default=64, help=argparse.SUPPRESS)
     ap.add_argument("--psf-decays", type=int, default=10_000_000, help=argparse.SUPPRESS)
+    ap.add_argument("--calib-iters", type=int, default=4, help=argparse.SUPPRESS)
     args = ap.parse_args()
     args.set = dict(kv.split("=", 1) for kv in args.set)
     if args.decays is None:

@@ -109,6 +109,7 @@ def load_library(path=None):
     L.gpet_surrogate_grad.argtypes = [vp, vp, i64, f32p, vp]
     L.gpet_surrogate_forward.argtypes = [vp, vp, i64, vp]
     L.gpet_surrogate_train.argtypes = [vp, vp, i64, i32, i32, C.c_float, C.c_uint64, vp]
+    L.gpet_surrogate_calibrate.argtypes = [vp, vp, i64, i32, C.POINTER(C.c_float)]
     L.gpet_set_surrogate.argtypes = [vp, vp]
     L.gpet_umma_selftest.argtypes = [C.c_int, vp, vp, i32, i32, vp]
     L.gpet_digitize.argtypes = [vp, vp, vp, vp, i64, C.POINTER(RunStats)]
@@ -428,6 +429,15 @@ class Surrogate:
         out = np.zeros((len(rec), 208), np.float32)
         self._ck(self.L.gpet_surrogate_forward(self.h, _ptr(rec), len(rec), _ptr(out)))
         return out
+
+    def calibrate(self, rec, iters=3):
+        """Match the expected (energy class, crystal) and energy-bin counts of
+        the records in the current domain (gpet_surrogate_calibrate); returns
+        the last pass's largest |log(observed / expected)|."""
+        rec = np.ascontiguousarray(rec, ENTRY_DTYPE)
+        adj = C.c_float()
+        self._ck(self.L.gpet_surrogate_calibrate(self.h, _ptr(rec), len(rec), int(iters), C.byref(adj)))
+        return adj.value
 
     def train(self, rec, epochs=1, batch=8192, lr=1e-3, seed=7):
         rec = np.ascontiguousarray(rec, ENTRY_DTYPE)

@@ -805,7 +805,6 @@ __global__ void k_loss(const float* __restrict__ out, int64_t n, const int32_t* 
     }
 }
 
-// dZ = dH * SiLU'(Z), in place on dH
 // the batch's records, in the epoch's order, from the training set on the device
 __global__ void k_gather_records(const EntryRec* __restrict__ all, const uint32_t* __restrict__ order, int64_t n,
                                  EntryRec* out)
@@ -814,6 +813,63 @@ __global__ void k_gather_records(const EntryRec* __restrict__ all, const uint32_
         out[i] = all[order[i]];
 }
 
+// expected counts of a batch under the model: acc[set * kCry + crystal] of
+// each (energy class, crystal) — per record the probability of the class (its
+// energy-bin probabilities summed over the class's bins; bin 0 = no pulse
+// belongs to neither) times the class's crystal probability — and
+// acc[2 * kCry + bin] of each energy bin. One warp per record, two bins and
+// two crystals per lane.
+__global__ void __launch_bounds__(256) k_calib_accum(const float* __restrict__ out, int64_t n, int crystalN,
+                                                     double* acc)
+{
+    using namespace sg;
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    float a[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+    float ea[2] = {0.0f, 0.0f};
+    for (int64_t i = w0; i < n; i += nw) {
+        const float* o = out + i * kOut;
+        const float e0 = o[kColE + lane], e1 = o[kColE + 32 + lane];
+        float mx = fmaxf(e0, e1);
+        for (int d = 16; d > 0; d >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+        const float x0 = expf(e0 - mx), x1 = expf(e1 - mx);
+        const int b0 = lane, b1 = 32 + lane;
+        float s = x0 + x1;
+        float c0 = (b0 >= 1 && b0 < kClassBin ? x0 : 0.0f) + (b1 >= 1 && b1 < kClassBin ? x1 : 0.0f);
+        float c1 = (b0 >= kClassBin ? x0 : 0.0f) + (b1 >= kClassBin ? x1 : 0.0f);
+        for (int d = 16; d > 0; d >>= 1) {
+            s += __shfl_xor_sync(0xffffffffu, s, d);
+            c0 += __shfl_xor_sync(0xffffffffu, c0, d);
+            c1 += __shfl_xor_sync(0xffffffffu, c1, d);
+        }
+        ea[0] += x0 / s;
+        ea[1] += x1 / s;
+#pragma unroll
+        for (int set = 0; set < 2; ++set) {
+            const float* l = o + set * kCry;
+            const bool v0 = lane < crystalN, v1 = 32 + lane < crystalN;
+            const float l0 = v0 ? l[lane] : -1e30f, l1 = v1 ? l[32 + lane] : -1e30f;
+            float m2 = fmaxf(l0, l1);
+            for (int d = 16; d > 0; d >>= 1) m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, d));
+            const float y0 = v0 ? expf(l0 - m2) : 0.0f, y1 = v1 ? expf(l1 - m2) : 0.0f;
+            float t = y0 + y1;
+            for (int d = 16; d > 0; d >>= 1) t += __shfl_xor_sync(0xffffffffu, t, d);
+            const float w = (set ? c1 : c0) / (s * t);
+            a[set][0] += w * y0;
+            a[set][1] += w * y1;
+        }
+    }
+#pragma unroll
+    for (int set = 0; set < 2; ++set) {
+        atomicAdd(&acc[set * kCry + lane], (double)a[set][0]);
+        atomicAdd(&acc[set * kCry + 32 + lane], (double)a[set][1]);
+    }
+    atomicAdd(&acc[2 * kCry + lane], (double)ea[0]);
+    atomicAdd(&acc[2 * kCry + 32 + lane], (double)ea[1]);
+}
+
+// dZ = dH * SiLU'(Z), in place on dH
 __global__ void k_silu_back(float* dH, const float* __restrict__ Z, int64_t count)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
@@ -1026,6 +1082,7 @@ struct gpet_surrogate {
     Buf X, Z, H, out, dout, dA, dB, cry, dep, bin, pan, rec;
     // training set on the device and the epoch's visiting order
     Buf all, perm, epoch_loss;
+    Buf calib;   // expected (energy class, crystal) counts of a calibration pass
 };
 
 namespace {
@@ -1436,6 +1493,95 @@ int gpet_surrogate_train(gpet_surrogate* s, const gpet_entry* rec, int64_t n, in
         if (epoch_loss) epoch_loss[ep] = nb ? lsum / (float)nb : 0.0f;
     }
     SCK(cudaStreamSynchronize(s->stream));
+    return GPET_OK;
+}
+
+int gpet_surrogate_calibrate(gpet_surrogate* s, const gpet_entry* rec, int64_t n, int32_t iters, float* max_adjust)
+{
+    using namespace sg;
+    if (!s || !rec || n < 1 || iters < 1) return GPET_ERR_ARG;
+    SCK(cudaSetDevice(s->device));
+    const SurrogateDev sd = make_view(s);
+    const int ncry = s->geom.crystalN;
+    // the records of the surrogate's domain (the test of k_route) and their
+    // observed (energy class, crystal) and energy-bin counts, the bin as in
+    // training (0: no pulse)
+    constexpr int kAcc = 2 * kCry + kBins;
+    const EntryRec* r = reinterpret_cast<const EntryRec*>(rec);
+    std::vector<EntryRec> dom;
+    std::vector<double> obs(kAcc, 0.0);
+    for (int64_t i = 0; i < n; ++i) {
+        const EntryRec& e = r[i];
+        const bool in = e.E >= s->e_lo && e.E <= s->e_hi && std::fabs(e.y) <= sd.half_y - s->margin &&
+                        std::fabs(e.z) <= sd.half_z - s->margin && e.panel >= 0 && e.panel < s->geom.npanels &&
+                        (s->panel_ok.empty() || s->panel_ok[(size_t)e.panel]);
+        if (!in) continue;
+        dom.push_back(e);
+        int b = 0;
+        if (e.crystal >= 0 && e.Edep > 0.0f) {
+            b = (int)(e.Edep / e.E * (float)kBins);
+            b = b < 1 ? 1 : (b > kBins - 1 ? kBins - 1 : b);
+            if (e.crystal < ncry) obs[(size_t)((b >= kClassBin ? kCry : 0) + e.crystal)] += 1.0;
+        }
+        obs[(size_t)(2 * kCry + b)] += 1.0;
+    }
+    const int64_t m = (int64_t)dom.size();
+    if (m == 0) return sfail(s, GPET_ERR_ARG, "no record in the surrogate's domain");
+    const int64_t B = std::min<int64_t>(m, 1 << 16);
+    int rc = ensure_batch(s, B);
+    if (rc) return rc;
+    SCK(s->all.ensure((size_t)m * sizeof(EntryRec)));
+    SCK(s->calib.ensure(kAcc * sizeof(double)));
+    SCK(cudaMemcpyAsync(s->all.p, dom.data(), (size_t)m * sizeof(EntryRec), cudaMemcpyHostToDevice, s->stream));
+    const int smem = (int)(kSmemA + kSmemB);
+    SCK(cudaFuncSetAttribute(k_mlp_fwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    float last = 0.0f;
+    for (int it = 0; it < iters; ++it) {
+        SCK(cudaMemsetAsync(s->calib.p, 0, kAcc * sizeof(double), s->stream));
+        for (int64_t b0 = 0; b0 < m; b0 += B) {
+            const int64_t nb = std::min<int64_t>(B, m - b0);
+            SCK(cudaMemcpyAsync(s->rec.p, s->all.as<EntryRec>() + b0, (size_t)nb * sizeof(EntryRec),
+                                cudaMemcpyDeviceToDevice, s->stream));
+            const unsigned g1 = (unsigned)std::min<int64_t>((nb + 255) / 256, 152 * 8);
+            k_entry_features<<<g1, 256, 0, s->stream>>>(s->rec.as<EntryRec>(), nb, sd, s->params.as<float>(),
+                                                        s->X.as<__nv_bfloat16>(), s->cry.as<int32_t>(),
+                                                        s->dep.as<float>(), s->bin.as<int32_t>(),
+                                                        s->pan.as<int32_t>());
+            FwdTrain tr{s->X.as<__nv_bfloat16>(), nb, s->Z.as<float>(), s->H.as<__nv_bfloat16>(), s->out.as<float>()};
+            FwdInfer in{};
+            k_mlp_fwd<true><<<grid_cap(nb, 128, 152), kFwdThreads, smem, s->stream>>>(sd, tr, in,
+                                                                                     s->errflag.as<int>());
+            k_calib_accum<<<(unsigned)std::min<int64_t>((nb + 7) / 8, 152 * 8), 256, 0, s->stream>>>(
+                s->out.as<float>(), nb, ncry, s->calib.as<double>());
+            SCK(cudaGetLastError());
+        }
+        std::vector<double> expd(kAcc);
+        std::vector<float> bias(kOut);
+        int herr = 0;
+        float* const pb = s->params.as<float>() + b_off(kLayers - 1);
+        SCK(cudaMemcpyAsync(expd.data(), s->calib.p, expd.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        SCK(cudaMemcpyAsync(bias.data(), pb, bias.size() * 4, cudaMemcpyDeviceToHost, s->stream));
+        SCK(cudaMemcpyAsync(&herr, s->errflag.p, 4, cudaMemcpyDeviceToHost, s->stream));
+        SCK(cudaStreamSynchronize(s->stream));
+        if (herr) return sfail(s, GPET_ERR_CUDA, "a tensor-core wait gave up");
+        // the crystal logits of each class and the energy-bin logits move by
+        // log(observed / expected)
+        last = 0.0f;
+        auto nudge = [&](size_t j, size_t col) {
+            if (!(obs[j] > 0.0) || !(expd[j] > 0.0)) return;
+            const float d = (float)std::log(obs[j] / expd[j]);
+            bias[col] += d;
+            last = std::max(last, std::fabs(d));
+        };
+        for (int set = 0; set < 2; ++set)
+            for (int k = 0; k < ncry; ++k) nudge((size_t)(set * kCry + k), (size_t)(set * kCry + k));
+        for (int b = 0; b < kBins; ++b) nudge((size_t)(2 * kCry + b), (size_t)(kColE + b));
+        SCK(cudaMemcpyAsync(pb, bias.data(), bias.size() * 4, cudaMemcpyHostToDevice, s->stream));
+        rc = refresh_weights(s);
+        if (rc) return rc;
+        SCK(cudaStreamSynchronize(s->stream));
+    }
+    if (max_adjust) *max_adjust = last;
     return GPET_OK;
 }
 

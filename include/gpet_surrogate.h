@@ -67,6 +67,14 @@ int gpet_surrogate_forward(gpet_surrogate* s, const gpet_entry* rec, int64_t n, 
  * mean loss. */
 int gpet_surrogate_train(gpet_surrogate* s, const gpet_entry* rec, int64_t n, int32_t epochs, int32_t batch,
                          float lr, uint64_t seed, float* epoch_loss);
+/* Calibration on the records of the surrogate's current domain: `iters`
+ * passes each move the biases of the crystal logits of each energy class and
+ * of the energy-bin logits by log(observed / expected) of that (class,
+ * crystal) or energy-bin count over the records, so that the model's expected
+ * counts match the Monte Carlo ones (iterative proportional fitting; the
+ * other parameters stay). *max_adjust (may be NULL) receives the last pass's
+ * largest |log ratio|. Call after gpet_surrogate_set_domain. */
+int gpet_surrogate_calibrate(gpet_surrogate* s, const gpet_entry* rec, int64_t n, int32_t iters, float* max_adjust);
 /* Use (s) or stop using (NULL) the surrogate in this context's runs; s must
  * outlive its use. Its photons produce pulses but no hits. */
 int gpet_set_surrogate(gpet_ctx* ctx, gpet_surrogate* s);

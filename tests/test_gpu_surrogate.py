@@ -125,3 +125,53 @@ def test_entries_train_and_run_with_surrogate(scene_positron, data_dir, gpet_lib
     sc.set_surrogate(None)
     st_b = sc.run()
     assert st_b["n_surrogate"] == 0 and st_b["n_singles"] == st_mc["n_singles"]
+
+
+def test_crystal_calibration_matches_observed_counts(scene_positron, data_dir, gpet_lib):
+    """gpet_surrogate_calibrate moves only the head's crystal and energy-bin
+    biases, and afterwards the model's expected counts over the records of its
+    domain — per energy bin, and per (energy class, crystal): class
+    probability from the energy-bin softmax times the class's crystal
+    softmax, computed here in float64 from the raw head outputs — equal the
+    observed counts of those records."""
+    from gpet_gb300 import api
+    gen = make_ctx(scene_positron, data_dir, seed=303, n_decays=600000, record_entries=1)
+    gen.run()
+    rec = gen.entries()
+    sur = api.Surrogate(gen, seed=6)
+    sur.train(rec, epochs=2, batch=4096, lr=2e-3)
+    sur.set_domain(1.0e5, 5.2e5, 0.3)
+    npan, hy, hz, _, ncry, _ = _geom(gen)
+    p0 = sur.params()
+    adj = sur.calibrate(rec, iters=8)
+    p1 = sur.params()
+    b_head = len(p0) - npan * 6 - 208   # the head's bias sits before the embedding
+    changed = np.nonzero(p0 != p1)[0]
+    assert len(changed) > 0
+    assert changed.min() >= b_head and changed.max() < b_head + 204, (changed.min(), changed.max())
+    assert not np.isin(changed - b_head, np.arange(128, 140)).any()   # depth mixture untouched
+    dom = rec[(rec["E"] >= 1.0e5) & (rec["E"] <= 5.2e5) & (np.abs(rec["y"]) <= hy - 0.3) &
+              (np.abs(rec["z"]) <= hz - 0.3)]
+    out = sur.forward(dom).astype(np.float64)
+    eb = out[:, 140:204]
+    pe = np.exp(eb - eb.max(axis=1, keepdims=True))
+    pe /= pe.sum(axis=1, keepdims=True)
+    pc = [pe[:, 1:40].sum(axis=1), pe[:, 40:64].sum(axis=1)]
+    has = (dom["crystal"] >= 0) & (dom["Edep"] > 0)
+    b = np.clip((dom["Edep"][has] / dom["E"][has] * np.float32(64)).astype(np.int64), 1, 63)
+    ob = np.bincount(b, minlength=64).astype(np.float64)
+    ob[0] = (~has).sum()
+    ok = ob >= 20
+    assert ok.sum() > 32
+    assert np.abs(pe.sum(axis=0)[ok] / ob[ok] - 1.0).max() < 0.01, adj
+    for s in range(2):
+        lg = out[:, 64 * s:64 * s + ncry]
+        pk = np.exp(lg - lg.max(axis=1, keepdims=True))
+        pk /= pk.sum(axis=1, keepdims=True)
+        expected = (pc[s][:, None] * pk).sum(axis=0)
+        sel = (b >= 40) if s else (b < 40)
+        observed = np.bincount(dom["crystal"][has][sel], minlength=ncry)[:ncry].astype(np.float64)
+        big = observed >= 20    # fitted to these very records: equal up to convergence, not statistics
+        assert big.sum() > ncry // 2, (s, observed)
+        rel = np.abs(expected[big] / observed[big] - 1.0)
+        assert rel.max() < 0.01, (s, rel.max(), adj)
