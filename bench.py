@@ -756,7 +756,7 @@ def main():
     ap.add_argument("--train-epochs", type=int, default=12, help=argparse.SUPPRESS)
     ap.add_argument("--batch-sims", type=int, default=64, help=argparse.SUPPRESS)
     ap.add_argument("--psf-decays", type=int, default=10_000_000, help=argparse.SUPPRESS)
-    ap.add_argument("--calib-iters", type=int, default=4, help=argparse.SUPPRESS)
+    ap.add_argument("--calib-iters", type=int, default=10, help=argparse.SUPPRESS)
     args = ap.parse_args()
     args.set = dict(kv.split("=", 1) for kv in args.set)
     if args.decays is None:
