@@ -730,13 +730,13 @@ def run_widen_workload(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--decays", type=int, default=None,
                     help="decays per step (default 1e8; 1e9 for the large workload)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--ref-step-seconds", type=float, default=4.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=2.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
                     help="time launch shapes on a sample before the warm-up (results do not depend on the shape)")
