@@ -76,7 +76,8 @@ struct SimDesc {
     int32_t rdepth, rpolicy;
     // bound of the panel entry faces for a quick rejection (see
     // may_reach_panels): faces parallel to the z axis, none closer to it than
-    // sqrt(ring_rin2), all within [ring_zmin, ring_zmax] (padded)
+    // sqrt(ring_rin2), all within [ring_zmin, ring_zmax] (padded); 0 none,
+    // 1 the bound, 2 the bound and every face entered only from the axis side
     int32_t ring_test;
     float ring_zmin, ring_zmax, ring_rin2;
     int32_t pad_;
@@ -552,8 +553,18 @@ __device__ __forceinline__ bool may_reach_panels(const SimDesc& S, const Photon&
     if (uz == 0.0f) return p.x[2] >= S.ring_zmin && p.x[2] <= S.ring_zmax;
     const float iu = 1.0f / uz;
     const float t1 = (S.ring_zmin - p.x[2]) * iu, t2 = (S.ring_zmax - p.x[2]) * iu;
-    const float x1 = p.x[0] + t1 * p.u[0], y1 = p.x[1] + t1 * p.u[1];
-    const float x2 = p.x[0] + t2 * p.u[0], y2 = p.x[1] + t2 * p.u[1];
+    const float tb = fmaxf(t1, t2);
+    float ta = fminf(t1, t2);
+    // ring_test 2: every face takes only photons moving toward it from the
+    // axis side, so for a photon inside the faces' cylinder only the part of
+    // the ray ahead of it counts (a photon leaving the z band never reaches a
+    // face)
+    if (S.ring_test == 2 && p.x[0] * p.x[0] + p.x[1] * p.x[1] < S.ring_rin2) {
+        if (tb < 0.0f) return false;
+        ta = fmaxf(ta, 0.0f);
+    }
+    const float x1 = p.x[0] + ta * p.u[0], y1 = p.x[1] + ta * p.u[1];
+    const float x2 = p.x[0] + tb * p.u[0], y2 = p.x[1] + tb * p.u[1];
     return fmaxf(x1 * x1 + y1 * y1, x2 * x2 + y2 * y2) >= S.ring_rin2;
 }
 

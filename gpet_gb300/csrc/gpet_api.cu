@@ -664,6 +664,10 @@ static void ring_bound(const Geometry& g, SimDesc& S)
 {
     S.ring_test = 0;
     double zmin = 1e30, zmax = -1e30, rin = 1e30;
+    // whether every face takes only photons moving toward it from the axis
+    // side: enter_panel's direction test (u . n) * dir_x >= 0 with the sign of
+    // dir_x equal to that of n . o (the plane's side as seen from the axis)
+    bool toward = true;
     for (int i = 0; i < g.npanels; ++i) {
         const float* P = &g.panels[(size_t)i * kPanelStride];
         const double nx = P[21], ny = P[22], nz = P[23];
@@ -671,6 +675,8 @@ static void ring_bound(const Geometry& g, SimDesc& S)
         if (std::fabs(nz) > 1e-6 || !(nxy > 0.5)) return;
         const double d = std::fabs(nx * P[15] + ny * P[16]) / nxy;
         rin = std::min(rin, d);
+        const double no = nx * P[15] + ny * P[16] + nz * P[17];
+        if (!(P[18] != 0.0f) || !(no != 0.0) || (P[18] > 0.0f) != (no > 0.0)) toward = false;
         for (int sy = -1; sy <= 1; sy += 2)
             for (int sz = -1; sz <= 1; sz += 2) {
                 const double z = (double)P[17] + sy * 0.5 * P[1] * P[26] + sz * 0.5 * P[2] * P[29];
@@ -684,7 +690,7 @@ static void ring_bound(const Geometry& g, SimDesc& S)
     S.ring_zmin = (float)(zmin - pad - 1e-4 * std::fabs(zmin));
     S.ring_zmax = (float)(zmax + pad + 1e-4 * std::fabs(zmax));
     S.ring_rin2 = (float)(r * r);
-    S.ring_test = 1;
+    S.ring_test = toward ? 2 : 1;
 }
 
 static int build_sim(gpet_ctx* c)
