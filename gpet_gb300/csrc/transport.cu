@@ -167,16 +167,16 @@ __global__ void __launch_bounds__(256, 4) k_source(const Wave* waves, int wi, Pa
 }
 
 // a photon that has left the phantom (or stopped), waiting for the panel search
+// (always escaped: status 1; the emission time stays in the pair buffer and
+// is read in the drain, only for the photons that need it)
 struct FinRec {
     float x, y, z, ux, uy, uz, E;
     int32_t nscat;
-    double t;
-    long long p;      // photon index within the wave
     long long d;      // decay index within its simulation
-    int32_t status;
+    int32_t p;        // photon index within the wave
     float tf;
     int32_t sim;
-    int32_t steps;    // Woodcock steps of this photon
+    int32_t pad_;
 };
 
 constexpr int kPhWarps = 8;      // warps per k_phantom block (256 threads)
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
         if (has) {
             ph.x[0] = r.x; ph.x[1] = r.y; ph.x[2] = r.z;
             ph.u[0] = r.ux; ph.u[1] = r.uy; ph.u[2] = r.uz;
-            ph.E = r.E; ph.t = r.t; ph.tf = r.tf; ph.nscat = r.nscat;
+            ph.E = r.E; ph.t = 0.0; ph.tf = r.tf; ph.nscat = r.nscat;   // L.t: flight time alone
             if (kMulti) {
                 const SimDesc& S = w.sims[r.sim];
                 entered = enter_panel(S.panels, S.npanels, ph, L);
@@ -229,6 +229,9 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
                 entered = enter_panel(sP, sS.npanels, ph, L);
             }
         }
+        // the emission time, loaded by all lanes that need it at once
+        const double te = (entered || (has && exits)) ? pb.t[r.p >> 1] : 0.0;
+        if (entered) L.t = te + L.t;
         const unsigned m = __ballot_sync(0xffffffffu, entered);
         if (m) {
             unsigned long long b = 0;
@@ -262,8 +265,8 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
         if (has && exits) {
             ExitRec e;
             e.x = r.x; e.y = r.y; e.z = r.z; e.ux = r.ux; e.uy = r.uy; e.uz = r.uz;
-            e.E = r.E; e.nscat = r.nscat; e.t = r.t + (double)r.tf;
-            e.status = r.status;
+            e.E = r.E; e.nscat = r.nscat; e.t = te + (double)r.tf;
+            e.status = 1;
             e.panel = entered ? L.panel : -1;
             exits[r.p] = e;
         }
@@ -437,8 +440,8 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
                 FinRec r;
                 r.x = ph.x[0]; r.y = ph.x[1]; r.z = ph.x[2];
                 r.ux = ph.u[0]; r.uy = ph.u[1]; r.uz = ph.u[2];
-                r.E = ph.E; r.nscat = ph.nscat; r.t = pb.t[p >> 1]; r.p = p; r.d = d; r.status = status; r.tf = ph.tf;
-                r.sim = sim; r.steps = steps;
+                r.E = ph.E; r.nscat = ph.nscat; r.p = p; r.d = d; r.tf = ph.tf;
+                r.sim = sim; r.pad_ = 0;
                 fb[fcount + __popc(mf & lt)] = r;
                 active = false;
             }
