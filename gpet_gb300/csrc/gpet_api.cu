@@ -7,6 +7,7 @@
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -39,26 +40,39 @@ struct DevBuf {
     template <class T> T* as() const { return reinterpret_cast<T*>(p); }
 };
 
-// grow-only page-locked host array: device-to-host copies into it run at the
-// host link's rate and asynchronously; resize() leaves the contents unset
+// grow-only host array, page-locked when the system grants it (device-to-host
+// copies into it then run at the host link's rate and asynchronously), else
+// ordinary memory (the copies are then staged by the driver); resize() leaves
+// the contents unset
 template <class T>
 struct PinnedVec {
     T* p = nullptr;
     size_t n = 0, cap = 0;
+    bool pinned = false;
     PinnedVec() = default;
     PinnedVec(const PinnedVec&) = delete;
     PinnedVec& operator=(const PinnedVec&) = delete;
-    ~PinnedVec() { if (p) cudaFreeHost(p); }
+    ~PinnedVec() { release(); }
+    void release()
+    {
+        if (p) {
+            if (pinned) cudaFreeHost(p);
+            else std::free(p);
+        }
+        p = nullptr;
+        cap = n = 0;
+        pinned = false;
+    }
     cudaError_t resize(size_t m)
     {
         if (m > cap) {
-            if (p) cudaFreeHost(p);
-            p = nullptr;
-            cap = n = 0;
-            cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&p), m * sizeof(T), cudaHostAllocDefault);
-            if (e != cudaSuccess) {
-                p = nullptr;
-                return e;
+            release();
+            if (cudaHostAlloc(reinterpret_cast<void**>(&p), m * sizeof(T), cudaHostAllocDefault) == cudaSuccess) {
+                pinned = true;
+            } else {
+                cudaGetLastError();   // not sticky; fall back to pageable memory
+                p = static_cast<T*>(std::malloc(m * sizeof(T)));
+                if (!p) return cudaErrorMemoryAllocation;
             }
             cap = m;
         }
