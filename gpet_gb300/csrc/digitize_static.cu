@@ -6,11 +6,13 @@
 // must not pass `g_digi_arena` itself to a kernel: on the host that name is a
 // stand-in, not a device address (a kernel given it would fault, or on a
 // system where the GPU can reach host memory, silently use the wrong memory).
-// The device address is looked up once per device with cudaGetSymbolAddress,
-// on the first call made with that device current, and reused afterwards.
+// Its device address belongs to the CUDA context that loaded the module, not
+// to the device number, so every call looks it up again with
+// cudaGetSymbolAddress in the context current at that moment (after a
+// cudaDeviceReset, or under a non-primary context, a cached address would be
+// stale).
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 
 #include "kernels.h"
 #include "../../include/gpet.h"
@@ -21,27 +23,18 @@ static __device__ __align__(256) unsigned char g_digi_arena[GPET_STATIC_ARENA_BY
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-std::mutex g_arena_mu;
-unsigned char* g_arena_ptr[kMaxDevices] = {};
-
-// device address of g_digi_arena for the current device (set-up on first use)
-cudaError_t arena_for_current_device(unsigned char** out)
+// device address of g_digi_arena in the current context (looked up on every call)
+cudaError_t arena_for_current_context(unsigned char** out)
 {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_digi_arena);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lk(g_arena_mu);
-    if (!g_arena_ptr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_digi_arena);
-        if (e != cudaSuccess) return e;
-        g_arena_ptr[dev] = static_cast<unsigned char*>(p);
-    }
-    *out = g_arena_ptr[dev];
+    *out = static_cast<unsigned char*>(p);
     return cudaSuccess;
 }
+
+// word of DigiScratch::dcount that k_events_to_soa sets when a slot is >= 128
+constexpr int kBadSlotWord = 12;
 
 // bump allocator over the arena, 256-byte aligned pieces
 struct Carve {
@@ -57,15 +50,20 @@ struct Carve {
     }
 };
 
+// slots of 128 or more cannot be packed beside the scatter flag: they are
+// counted in *bad_slot and the call is refused, as gpet_digitize refuses them
 __global__ void k_events_to_soa(const EventRec* __restrict__ ev, const uint8_t* __restrict__ scat,
-                                const uint8_t* __restrict__ slot, int64_t n, PulseDev P)
+                                const uint8_t* __restrict__ slot, int64_t n, PulseDev P,
+                                unsigned long long* bad_slot)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const EventRec e = ev[i];
+        const uint8_t sl = slot[i];
+        if (sl > 0x7fu) atomicAdd(bad_slot, 1ull);
         P.parn[i] = e.parn; P.pann[i] = e.pann; P.modn[i] = e.modn; P.cryn[i] = e.cryn;
         P.siten[i] = e.siten; P.eventid[i] = e.eventid; P.t[i] = e.t;
         P.E[i] = e.E; P.x[i] = e.x; P.y[i] = e.y; P.z[i] = e.z;
-        P.meta[i] = (uint8_t)((slot[i] & 0x7fu) | (scat[i] ? 0x80u : 0u));
+        P.meta[i] = (uint8_t)((sl & 0x7fu) | (scat[i] ? 0x80u : 0u));
     }
 }
 
@@ -127,8 +125,16 @@ extern "C" int gpet_digitize_static(const gpet_digi_params* prm, const gpet_even
     if (prm->coinc_policy < 0 || prm->coinc_policy > 1)
         return set_err(err, err_len, GPET_ERR_ARG, "coinc_policy must be 0 or 1");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // an error left by the caller's earlier work is reported as such and left pending for the caller
+    cudaError_t ce = cudaPeekAtLastError();
+    if (ce != cudaSuccess) {
+        char msg[200];
+        std::snprintf(msg, sizeof(msg), "a CUDA error from earlier work is pending (not cleared): %s",
+                      cudaGetErrorString(ce));
+        return set_err(err, err_len, GPET_ERR_CUDA, msg);
+    }
     unsigned char* arena = nullptr;
-    cudaError_t ce = arena_for_current_device(&arena);
+    ce = arena_for_current_context(&arena);
     if (ce != cudaSuccess) return set_err(err, err_len, GPET_ERR_CUDA, cudaGetErrorString(ce));
     for (int k = 0; k < 8; ++k) counts[k] = 0;
 
@@ -178,14 +184,22 @@ extern "C" int gpet_digitize_static(const gpet_digi_params* prm, const gpet_even
     cudaMemsetAsync(D.dcount + 8, 0xFF, sizeof(unsigned long long), s);
     cudaMemsetAsync(d_cnt, 0, sizeof(Counters), s);
     cudaMemcpyAsync(d_prm, &dp, sizeof(DigiParams), cudaMemcpyHostToDevice, s);
-    unsigned long long hc[11] = {0};
+    unsigned long long hc[kBadSlotWord + 1] = {0};
     if (n > 0) {
-        k_events_to_soa<<<grid256(n), 256, 0, s>>>(reinterpret_cast<const EventRec*>(d_pulses), d_scat, d_slot, n, P);
+        k_events_to_soa<<<grid256(n), 256, 0, s>>>(reinterpret_cast<const EventRec*>(d_pulses), d_scat, d_slot, n, P,
+                                                   D.dcount + kBadSlotWord);
         k_blur_threshold<<<grid256(n), 256, 0, s>>>(P, n, d_prm, D.Eb, D.xb, D.yb, D.zb, D.site, D.sel, D.dcount + 0,
                                                     D.dcount + 8);
     }
     cudaMemcpyAsync(hc, D.dcount, sizeof(hc), cudaMemcpyDeviceToHost, s);
+    if ((ce = cudaGetLastError()) != cudaSuccess) return set_err(err, err_len, GPET_ERR_CUDA, cudaGetErrorString(ce));
     if ((ce = cudaStreamSynchronize(s)) != cudaSuccess) return set_err(err, err_len, GPET_ERR_CUDA, cudaGetErrorString(ce));
+    if (hc[kBadSlotWord] != 0) {
+        char msg[160];
+        std::snprintf(msg, sizeof(msg), "gpet_digitize_static: %llu pulses have a readout slot of 128 or more",
+                      hc[kBadSlotWord]);
+        return set_err(err, err_len, GPET_ERR_ARG, msg);
+    }
     const int64_t m = (int64_t)hc[0];
     uint32_t* total = reinterpret_cast<uint32_t*>(D.dcount + 4);
     uint64_t *ka = D.key_a, *kb = D.key_b;

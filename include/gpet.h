@@ -248,8 +248,12 @@ int gpet_get_table(gpet_ctx* ctx, int which, float* out, int64_t cap, int64_t* n
  *  - n <= GPET_STATIC_MAX_PULSES; larger inputs are rejected (GPET_ERR_ARG,
  *    message in err when err != NULL); more singles or pairs than the caller's
  *    capacities -> GPET_ERR_CAPACITY, nothing written past them.
- *  - The first call on a device looks up the array's device address (for the
- *    current device); make that first call before any stream capture.
+ *  - Every call looks up the array's device address in the CUDA context
+ *    current at that moment (the address belongs to the context, not the
+ *    device number, so nothing is cached across calls).
+ *  - A CUDA error already pending from the caller's earlier work is reported
+ *    (GPET_ERR_CUDA) and left pending; a readout slot of 128 or more is
+ *    refused with GPET_ERR_ARG, as gpet_digitize refuses it.
  *  - All calls share the one array, which keeps the last call's contents:
  *    calls whose work overlaps on the GPU (two host threads, or two streams of
  *    one device) race and must be serialised by the caller.

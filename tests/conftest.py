@@ -87,6 +87,25 @@ def oracle_for(scene, data_dir, panels=None, **extra):
     return bridge.OracleScene(scene.config_path, opts, data_dir, panels=panels, base_dir=scene.directory)
 
 
+def two_sample_chi2(a, b):
+    """p-value of the two-sample chi-square of histograms a and b (same bins,
+    empty bins of both dropped)."""
+    from scipy import stats
+    a = np.asarray(a, float)
+    b = np.asarray(b, float)
+    m = (a + b) > 0
+    a, b = a[m], b[m]
+    ka = np.sqrt(b.sum() / a.sum())
+    kb = np.sqrt(a.sum() / b.sum())
+    chi2 = np.sum((ka * a - kb * b) ** 2 / (a + b))
+    return stats.chi2.sf(chi2, max(len(a) - 1, 1))
+
+
+def within_sigma(x, y, k=3.0):
+    """Two Poisson counts agree within k standard deviations of their difference."""
+    return abs(x - y) <= k * np.sqrt(x + y + 1.0)
+
+
 def event_key_sort(ev, slot):
     order = np.lexsort((slot, ev["parn"]))
     return ev[order], slot[order], order

@@ -4,26 +4,10 @@ singles energy spectrum, per-crystal singles, coincidence classes and the
 scatter fraction (chi-square p > 0.01, totals within 3 sigma)."""
 import numpy as np
 import pytest
-from scipy import stats
 
-from conftest import make_ctx, oracle_for
+from conftest import make_ctx, oracle_for, two_sample_chi2, within_sigma
 
 pytestmark = pytest.mark.gpu
-
-
-def two_sample_chi2(a, b):
-    a = np.asarray(a, float)
-    b = np.asarray(b, float)
-    m = (a + b) > 0
-    a, b = a[m], b[m]
-    ka = np.sqrt(b.sum() / a.sum())
-    kb = np.sqrt(a.sum() / b.sum())
-    chi2 = np.sum((ka * a - kb * b) ** 2 / (a + b))
-    return stats.chi2.sf(chi2, max(len(a) - 1, 1))
-
-
-def within_sigma(x, y, k=3.0):
-    return abs(x - y) <= k * np.sqrt(x + y + 1.0)
 
 
 @pytest.fixture(scope="module")
