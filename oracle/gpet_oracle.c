@@ -78,7 +78,14 @@ void oracle_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], ui
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-typedef struct { uint32_t key[2], ctr[4], buf[4]; int pos; } stream_t;
+typedef struct {
+    uint32_t key[2], ctr[4], buf[4];
+    int pos;
+#ifdef ORACLE_TAPE
+    const uint32_t* tape;   /* words to draw instead of Philox (pins against the reference) */
+    int64_t tape_n, tape_pos;
+#endif
+} stream_t;
 
 static void st_init(stream_t* s, const or_scene* sc, uint32_t tag, uint64_t id)
 {
@@ -86,10 +93,20 @@ static void st_init(stream_t* s, const or_scene* sc, uint32_t tag, uint64_t id)
     s->key[1] = (uint32_t)(sc->seed >> 32) + sc->sim_id;
     s->ctr[0] = 0; s->ctr[1] = tag; s->ctr[2] = (uint32_t)id; s->ctr[3] = (uint32_t)(id >> 32);
     s->pos = 4;
+#ifdef ORACLE_TAPE
+    s->tape = NULL;
+#endif
 }
 
 static inline uint32_t st_next(stream_t* s)
 {
+#ifdef ORACLE_TAPE
+    if (s->tape) {
+        const uint32_t w = s->tape_pos < s->tape_n ? s->tape[s->tape_pos] : 0x80000000u;
+        s->tape_pos++;
+        return w;
+    }
+#endif
     if (s->pos == 4) {
         oracle_philox4x32_10(s->ctr, s->key, s->buf);
         s->ctr[0]++;
@@ -966,22 +983,27 @@ static int cmp_parn_slot(const void* a, const void* b)
 /* blur, gPET_kernals.cu:814-837, with the normal deviates drawn from the
  * pulse's own Philox stream (key (parn, slot)) so the result does not depend
  * on the order pulses are processed in */
+static void blur_event(const or_scene* sc, or_event* e, stream_t* st)
+{
+    float R = 0.0f;
+    if (sc->blurpolicy == 0) R = dm_sqrt(sc->Eref / e->E) * sc->Rref;
+    if (sc->blurpolicy == 1) R = sc->Rref + sc->Eslope * (e->E - sc->Eref) / 1.0e6f;
+    if (R < 0.0f) R = 0.0f;
+    float z = st_normal_f(st);
+    e->E += z * R * e->E / 2.35482f;
+    if (sc->Sblur > 0.0f) {
+        e->x += sc->Sblur * st_normal_f(st);
+        e->y += sc->Sblur * st_normal_f(st);
+        e->z += sc->Sblur * st_normal_f(st);
+    }
+}
+
 static void blur_pulse(const or_scene* sc, dpulse_t* p)
 {
     if (p->e.parn < 0) return;   /* background singles carry their own energy spread */
     stream_t st;
     st_init(&st, sc, TAG_BLUR, ((uint64_t)(uint32_t)p->e.parn << 4) | p->slot);
-    float R = 0.0f;
-    if (sc->blurpolicy == 0) R = dm_sqrt(sc->Eref / p->e.E) * sc->Rref;
-    if (sc->blurpolicy == 1) R = sc->Rref + sc->Eslope * (p->e.E - sc->Eref) / 1.0e6f;
-    if (R < 0.0f) R = 0.0f;
-    float z = st_normal_f(&st);
-    p->e.E += z * R * p->e.E / 2.35482f;
-    if (sc->Sblur > 0.0f) {
-        p->e.x += sc->Sblur * st_normal_f(&st);
-        p->e.y += sc->Sblur * st_normal_f(&st);
-        p->e.z += sc->Sblur * st_normal_f(&st);
-    }
+    blur_event(sc, &p->e, &st);
 }
 
 /* setSitenum, gPET_kernals.cu:607-640 (applied only when dlevel != 3,
@@ -1365,3 +1387,207 @@ void oracle_detmath_d(int which, int64_t n, const double* x, double* y)
         }
     }
 }
+
+#ifdef ORACLE_TAPE
+/* ------------------------------------------------------------------------
+ * Tape-driven entry points: each runs one step of the oracle on random words
+ * given by the caller instead of its Philox streams, so the pins in tests/
+ * can feed the oracle and the reference's own functions (built for the CPU)
+ * exactly the same words and compare what they compute. */
+static void st_tape(stream_t* s, const uint32_t* tape, int64_t n)
+{
+    memset(s, 0, sizeof(*s));
+    s->tape = tape;
+    s->tape_n = n;
+    s->tape_pos = 0;
+}
+
+static void photon_from(photon_t* p, const float in[7], double t_us)
+{
+    memset(p, 0, sizeof(*p));
+    for (int k = 0; k < 3; ++k) { p->x[k] = (real)in[k]; p->u[k] = (real)in[3 + k]; }
+    p->E = (real)in[6];
+    p->t = t_us;
+}
+
+/* photon(), gPET_kernals.cu:256-345, with the majorant table given */
+int oracle_tape_phantom(const or_scene* sc, const float* wtab, float e0, float ide, const float in[7], double t_us,
+                        const uint32_t* tape, int64_t n, double out[7], double* t_out, int32_t* nscat, int64_t* used)
+{
+    static wck_t w;
+    w.e0 = e0; w.ide = ide;
+    memcpy(w.tab, wtab, sizeof(w.tab));
+    photon_t p;
+    photon_from(&p, in, t_us);
+    stream_t st;
+    st_tape(&st, tape, n);
+    int status = phantom_transport(sc, &w, &p, &st);
+    for (int k = 0; k < 3; ++k) { out[k] = (double)p.x[k]; out[3 + k] = (double)p.u[k]; }
+    out[6] = (double)p.E;
+    *t_out = p.t + (double)p.tf;
+    *nscat = p.nscat;
+    *used = st.tape_pos;
+    return status;
+}
+
+/* photonde per photon, gPET_kernals.cu:839-1233: panel search, detector
+ * transport with the detector majorant given, adder, readout; pulses (parn 0)
+ * into out[cap]; returns the pulse count, *panel the entered panel or -1 */
+int oracle_tape_detector(const or_scene* sc, const float* wtab, float e0, float ide, const float in[7], double t_us,
+                         int32_t eventid, const uint32_t* tape, int64_t n, or_event* out, int cap, int32_t* panel,
+                         int64_t* used)
+{
+    static wck_t w;
+    w.e0 = e0; w.ide = ide;
+    memcpy(w.tab, wtab, sizeof(w.tab));
+    photon_t p;
+    photon_from(&p, in, t_us);
+    local_t q;
+    *panel = -1;
+    *used = 0;
+    if (!enter_panel(sc, &p, &q)) return 0;
+    *panel = q.panel;
+    stream_t st;
+    st_tape(&st, tape, n);
+    tbuf_t tb;
+    memset(&tb, 0, sizeof(tb));
+    detector_transport(sc, &w, &q, 0, eventid, 0, &st, &tb, 0);
+    *used = st.tape_pos;
+    int k = (int)tb.n;
+    for (int i = 0; i < k && i < cap; ++i) out[i] = tb.ev[i];
+    free(tb.ev); free(tb.scat); free(tb.slot); free(tb.hid); free(tb.hf);
+    return k;
+}
+
+/* comsam, free-electron Klein-Nishina (gPET_kernals.cu:90-126) */
+void oracle_tape_kn(double e, const uint32_t* tape, int64_t n, double* efrac, double* cost, int64_t* used)
+{
+    stream_t st;
+    st_tape(&st, tape, n);
+    real ef, c;
+    kn_sample((real)e, &st, &ef, &c);
+    *efrac = (double)ef; *cost = (double)c; *used = st.tape_pos;
+}
+
+/* comsam from the surface (which 0) and rylsam (which 1), gPET_kernals.cu:66-88, 128-146 */
+void oracle_tape_surface(const or_scene* sc, int which, double e, int m, const uint32_t* tape, int64_t n,
+                         double* efrac, double* cost, int64_t* used)
+{
+    stream_t st;
+    st_tape(&st, tape, n);
+    real ef = (real)1.0, c;
+    if (which == 0) compton_surface(sc, (real)e, m, &st, &ef, &c);
+    else c = rayleigh_surface(sc, (real)e, m, &st);
+    *efrac = (double)ef; *cost = (double)c; *used = st.tape_pos;
+}
+
+/* sampleEkPositron (gPET_kernals.cu:420-443) for one isotope's coefficients */
+double oracle_tape_sample_ek(const float coef8[8], const uint32_t* tape, int64_t n, int64_t* used)
+{
+    or_scene sc;
+    memset(&sc, 0, sizeof(sc));
+    sc.iso_coef = coef8;
+    stream_t st;
+    st_tape(&st, tape, n);
+    double ek = (double)sample_ek(&sc, 0, &st);
+    *used = st.tape_pos;
+    return ek;
+}
+
+/* getPositionFromShape (gPET_kernals.cu:445-482) */
+void oracle_tape_shape(int shape, const float coef6[6], const uint32_t* tape, int64_t n, double p[3], int64_t* used)
+{
+    or_scene sc;
+    memset(&sc, 0, sizeof(sc));
+    int32_t sh = shape;
+    sc.src_coef = coef6;
+    sc.src_shape = &sh;
+    stream_t st;
+    st_tape(&st, tape, n);
+    real r[3];
+    shape_position(&sc, 0, &st, r);
+    p[0] = (double)r[0]; p[1] = (double)r[1]; p[2] = (double)r[2];
+    *used = st.tape_pos;
+}
+
+/* setPositronRange (gPET_kernals.cu:347-418) in the scene's phantom; dir NULL:
+ * the sampled direction (usedirection 0) */
+void oracle_tape_positron_range(const or_scene* sc, const float x[3], double ek, const float* dir,
+                                const uint32_t* tape, int64_t n, double out[3], int64_t* used)
+{
+    stream_t st;
+    st_tape(&st, tape, n);
+    real p[3] = {(real)x[0], (real)x[1], (real)x[2]};
+    real d[3];
+    if (dir) { d[0] = (real)dir[0]; d[1] = (real)dir[1]; d[2] = (real)dir[2]; }
+    positron_range(sc, p, (real)ek, dir ? d : NULL, &st, NULL);
+    out[0] = (double)p[0]; out[1] = (double)p[1]; out[2] = (double)p[2];
+    *used = st.tape_pos;
+}
+
+/* setPositionForPhoton (gPET_kernals.cu:563-604) for one positron record:
+ * out = position (3), photon 0 direction and energy (4), photon 1 (4) */
+void oracle_tape_psf_pair(const or_scene* sc, const float x[3], const float v4[4], int useprange,
+                          const uint32_t* tape, int64_t n, double out[11], int64_t* used)
+{
+    stream_t st;
+    st_tape(&st, tape, n);
+    real pos[3] = {(real)x[0], (real)x[1], (real)x[2]};
+    real dir[3] = {(real)v4[0], (real)v4[1], (real)v4[2]};
+    real spare = (real)0.0;
+    if (useprange) positron_range(sc, pos, (real)v4[3], dir, &st, &spare);
+    photon_t ph[2];
+    make_pair(sc, &st, pos, ph, 1.0, useprange ? &spare : NULL);
+    for (int k = 0; k < 3; ++k) out[k] = (double)pos[k];
+    for (int j = 0; j < 2; ++j) {
+        for (int k = 0; k < 3; ++k) out[3 + 4 * j + k] = (double)ph[j].u[k];
+        out[6 + 4 * j] = (double)ph[j].E;
+    }
+    *used = st.tape_pos;
+}
+
+/* crystalSearch (gPET_kernals.cu:1236-1279) in panel p of the scene */
+void oracle_crystal_search_at(const or_scene* sc, int p, const double x[3], int32_t ids[3])
+{
+    real r[3] = {(real)x[0], (real)x[1], (real)x[2]};
+    int m = -1, M = -1, L = -1;
+    crystal_search(sc, sc->panels + (size_t)p * OR_PANEL_STRIDE, r, &m, &M, &L);
+    ids[0] = m; ids[1] = M; ids[2] = L;
+}
+
+/* adder over n deposits of one photon, then readout (gPET_kernals.cu:737-813) */
+int oracle_adder_readout(const or_scene* sc, const or_event* dep, int n, or_event* out, int cap)
+{
+    or_event ev[MAX_PULSE];
+    int nev = 0;
+    for (int i = 0; i < n; ++i)
+        if (!adder(ev, &nev, &dep[i])) return -1;
+    or_event tmp[MAX_PULSE];
+    int k = readout(sc, ev, nev, tmp);
+    for (int i = 0; i < k && i < cap; ++i) out[i] = tmp[i];
+    return k;
+}
+
+/* the Woodcock majorant the oracle builds for the scene (which 0 phantom,
+ * 1 detector): 4096 mean free paths, first energy, inverse spacing */
+int oracle_majorant(const or_scene* sc, int which, float* tab, float* e0, float* ide)
+{
+    static prep_t pp;
+    int rc = prepare(sc, &pp);
+    if (rc) return rc;
+    const wck_t* w = which == 0 ? &pp.wph : &pp.wdet;
+    memcpy(tab, w->tab, sizeof(w->tab));
+    *e0 = w->e0;
+    *ide = w->ide;
+    return 0;
+}
+
+/* blur (gPET_kernals.cu:814-837) of one pulse */
+void oracle_tape_blur(const or_scene* sc, or_event* e, const uint32_t* tape, int64_t n, int64_t* used)
+{
+    stream_t st;
+    st_tape(&st, tape, n);
+    blur_event(sc, e, &st);
+    *used = st.tape_pos;
+}
+#endif /* ORACLE_TAPE */
