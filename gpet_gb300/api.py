@@ -439,6 +439,43 @@ class Surrogate:
         self._ck(self.L.gpet_surrogate_calibrate(self.h, _ptr(rec), len(rec), int(iters), C.byref(adj)))
         return adj.value
 
+    # layer shapes of the parameter vector (gpet_surrogate.h): weights [out][in], then biases
+    LAYERS = ((16, 256), (256, 256), (256, 256), (256, 256), (256, 208))
+
+    def save(self, path, domain, **meta):
+        """Write the parameters for inference: the weight matrices rounded to
+        bf16 (the precision the tensor-core forward uses, so inference is
+        unchanged) as 16-bit patterns, biases and the panel embedding in
+        float32, the validated domain (e_lo, e_hi, margin) and `meta`."""
+        p = self.params()
+        w_bits, rest, off = [], [], 0
+        for fin, fout in self.LAYERS:
+            w = np.ascontiguousarray(p[off:off + fin * fout], np.float32).view(np.uint32)
+            w_bits.append(((w + 0x7FFF + ((w >> 16) & 1)) >> 16).astype(np.uint16))
+            off += fin * fout
+            rest.append(p[off:off + fout])
+            off += fout
+        np.savez_compressed(path, weights_bf16=np.concatenate(w_bits), biases=np.concatenate(rest),
+                            embedding=p[off:], domain=np.array(domain, np.float32),
+                            meta=np.array(repr(meta)))
+
+    def load(self, path):
+        """Set the parameters and domain saved by save(); returns its meta."""
+        import ast
+        z = np.load(path)
+        wb, b, emb = z["weights_bf16"], z["biases"], z["embedding"]
+        parts, wo, bo = [], 0, 0
+        for fin, fout in self.LAYERS:
+            parts.append((wb[wo:wo + fin * fout].astype(np.uint32) << 16).view(np.float32))
+            parts.append(b[bo:bo + fout])
+            wo += fin * fout
+            bo += fout
+        parts.append(emb)
+        self.set_params(np.concatenate(parts).astype(np.float32))
+        d = z["domain"]
+        self.set_domain(float(d[0]), float(d[1]), float(d[2]))
+        return ast.literal_eval(str(z["meta"]))
+
     def train(self, rec, epochs=1, batch=8192, lr=1e-3, seed=7):
         rec = np.ascontiguousarray(rec, ENTRY_DTYPE)
         losses = np.zeros(epochs, np.float32)
