@@ -12,7 +12,11 @@ Workload (one step = one full acquisition, simulated and digitized):
 Prints one JSON line (rank 0). `value` = coincidences / device time with the
 scene resident on the GPU (CUDA events on the library's stream); `e2e` = the
 same metric through the C ABI with host buffers (phantom upload, run, singles
-and coincidence copy-out) timed on the host clock. The reference arm
+and coincidence copy-out) timed on the host clock. `surrogate_batched` = the
+metric's second form: 64 uneven simulations batched in one job with the
+learned detector response (committed model), against the plain form (each
+simulation its own plain Monte Carlo run) and plain batched, with the
+chi-square of the singles spectrum and crystal map. The reference arm
 (--impl reference) times the CPU oracle, the restatement of the reference's
 algorithm, on all host cores (the reference's own GPU build does not compile
 with CUDA 13).
@@ -188,12 +192,14 @@ def run_reference(args):
         t0 = time.perf_counter()
         o.run(0, n0, precision="fp64")
         rate = n0 / max(time.perf_counter() - t0, 1e-6)
-        n = int(min(o.n_decays, max(n0, rate * args.ref_step_seconds)))
+        # each timed step is the whole acquisition unless a bounded sample is asked for
+        n = o.n_decays if args.ref_step_seconds <= 0 else int(min(o.n_decays, max(n0, rate * args.ref_step_seconds)))
         for w in range(args.warmup):
             o.run(0, min(n, n0), precision="fp64")
         tot_c, tot_t, tot_d = 0, 0.0, 0
         for k in range(args.steps):
             b = (k * n) % max(1, o.n_decays - n + 1)
+            o.s.seed = 20261203 + k      # the seeds of the GPU arm's timed steps
             t0 = time.perf_counter()
             r = o.run(b, b + n, precision="fp64")
             tot_t += time.perf_counter() - t0
@@ -257,11 +263,16 @@ def run_ours(args):
         tot = {"coinc": 0, "ms": 0.0, "ms_sp": 0.0, "ms_src": 0.0, "ms_ph": 0.0, "ms_det": 0.0, "ms_dig": 0.0, "launches": 0, "ph_steps": 0,
                "entered": 0, "decays": 0, "singles": 0, "true": 0, "scatter": 0, "random": 0, "chunks": 0,
                "pairs": 0}
+        t_flush, t_run = 0.0, 0.0
         for k in range(args.steps):
+            t0 = time.perf_counter()
             flush.zero_()
             torch.cuda.synchronize()
+            t1 = time.perf_counter()
             ctx.set_option("seed", 20261203 + k)
             st = ctx.run()
+            t_run += time.perf_counter() - t1
+            t_flush += t1 - t0
             tot["coinc"] += st["n_coinc"]; tot["ms"] += st["ms_total"]; tot["ms_sp"] += st["ms_source_phantom"]
             tot["ms_src"] += st["ms_source"]; tot["ms_ph"] += st["ms_phantom"]
             tot["ms_det"] += st["ms_detector"]; tot["ms_dig"] += st["ms_digitizer"]
@@ -348,9 +359,14 @@ def run_ours(args):
                 "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps} if e2e_steps > 0 else None,
         "clocks": clocks,
         "wall_s_timed_region": wall,
+        # host clock per step: the L2 flush (512 MB write + sync) and gpet_run
+        # (device time plus the host's per-chunk count reads and launches)
+        "wall_ms_per_step": {"l2_flush": 1e3 * t_flush / args.steps, "gpet_run": 1e3 * t_run / args.steps},
         "launch_shape": tuning if tuning else "library defaults",
         "setup_s": setup_s,
     }
+    if world == 1 and args.surrogate_steps > 0 and args.workload == "positron":
+        line["surrogate_batched"] = measure_surrogate_batched(args.surrogate_steps, 2)
     if world == 1 and not args.no_cpu_baseline:
         with tempfile.TemporaryDirectory() as d2:
             sc2 = make_scene(d2, args.decays, args.workload)
@@ -372,6 +388,112 @@ BATCH_WORKLOAD = ("batched64: 64 simulations of uneven size in one job - phantom
                   "over a 6.4 cm cube of seeded water/bone/air ellipsoids, 1e5-1e7 F-18 decays each "
                   "(log-uniform, positron range on), point or cylinder sources, the positron workload's ring "
                   "and digitizer")
+
+
+SURROGATE_MODEL = os.path.join(ROOT, "data", "surrogate_positron_ring.npz")
+
+
+def measure_surrogate_batched(steps, warmup, model_path=SURROGATE_MODEL):
+    """The metric's second form: the 64-simulation job (BATCH_WORKLOAD) with
+    the learned detector response (the committed model, trained by
+    data/make_surrogate.py with the library's kernels), batched in one job,
+    against the plain form (plain Monte Carlo, each simulation its own run)
+    and plain Monte Carlo batched; device time (CUDA events) per job, L2
+    flushed before each; the singles of the plain batched and surrogate
+    batched arms (independent seeds) compared by two-sample chi-square."""
+    import numpy as np
+    import torch
+    from gpet_gb300 import api, scenes
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda:0")
+    data = os.path.join(ROOT, "data")
+    with tempfile.TemporaryDirectory() as d:
+        sims = scenes.batched(d)
+        ctxs = []
+        for bs in sims:
+            c = api.Context(0)
+            c.set_options(dict(bs.options, data_dir=data, base_dir=d))
+            c.load_config(bs.config_path)
+            mat, den = bs.phantom()
+            c.set_phantom(mat, den, (bs.nvox,) * 3, (-3.2,) * 3, (6.4,) * 3)
+            c.set_source_file(bs.source_path, 0.0, 120.0)
+            ctxs.append(c)
+        seeds = [bs.options["seed"] for bs in sims]
+        sur = api.Surrogate(ctxs[0], seed=1)
+        meta = sur.load(model_path)
+
+        def reseed(k):
+            for c, sd in zip(ctxs, seeds):
+                c.set_option("seed", sd + 1000003 * k)
+
+        def arm(kind, k0):
+            for c in ctxs:
+                c.set_surrogate(sur if kind == "surrogate_batched" else None)
+            tot = {"ms": 0.0, "det": 0.0, "coinc": 0, "decays": 0, "nsur": 0, "entered": 0, "launches": 0,
+                   "true": 0, "scatter": 0, "random": 0, "singles": 0}
+            he, hc = np.zeros(60), np.zeros(64)
+            for k in range(-warmup, steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                reseed(k0 + k)
+                if kind == "plain_separate":
+                    st = [c.run() for c in ctxs]
+                    ms = sum(x["ms_total"] for x in st)
+                    det = sum(x["ms_detector"] for x in st)
+                    launches = sum(x["kernel_launches"] for x in st)
+                else:
+                    st = api.run_batched(ctxs)
+                    ms, det, launches = st[0]["ms_total"], st[0]["ms_detector"], st[0]["kernel_launches"]
+                if k < 0:
+                    continue
+                tot["ms"] += ms; tot["det"] += det; tot["launches"] += launches
+                for key, f in (("coinc", "n_coinc"), ("decays", "n_decays"), ("nsur", "n_surrogate"),
+                               ("entered", "n_entered"), ("true", "n_true"), ("scatter", "n_scatter"),
+                               ("random", "n_random"), ("singles", "n_singles")):
+                    tot[key] += sum(x[f] for x in st)
+                if kind != "plain_separate":
+                    for c in ctxs:
+                        s_ev, _ = c.singles()
+                        he += np.histogram(s_ev["E"], bins=60, range=(3.5e5, 6.5e5))[0]
+                        hc += np.bincount(s_ev["cryn"], minlength=64)[:64]
+            r = {"value": tot["coinc"] / (tot["ms"] * 1e-3), "unit": UNIT, "ms_per_job": tot["ms"] / steps,
+                 "detector_ms_per_job": tot["det"] / steps, "coincidences_per_job": tot["coinc"] / steps,
+                 "singles_per_job": tot["singles"] / steps, "gpu_launches_per_job": tot["launches"] / steps,
+                 "classes_per_job": {"true": tot["true"] / steps, "scatter": tot["scatter"] / steps,
+                                     "random": tot["random"] / steps}}
+            if kind == "surrogate_batched":
+                r["fraction_of_entered_photons"] = tot["nsur"] / max(1, tot["entered"])
+            return r, he, hc, tot
+
+        plain_sep, _, _, t_sep = arm("plain_separate", 0)
+        plain_bat, mc_e, mc_c, t_bat = arm("plain_batched", 0)
+        sur_bat, su_e, su_c, t_sur = arm("surrogate_batched", 50000)
+        for c in ctxs:
+            c.set_surrogate(None)
+            c.close()
+        sur.close()
+    rel = (su_c / su_c.sum()) / (mc_c / mc_c.sum()) - 1.0
+    det_share = plain_bat["detector_ms_per_job"] / plain_bat["ms_per_job"]
+    return {
+        "workload": BATCH_WORKLOAD, "simulations": len(sims), "decays_per_job": t_bat["decays"] / steps,
+        "steps": steps, "warmup": warmup, "l2": "flushed before each job (512 MB write)",
+        "plain_separate": plain_sep, "plain_batched": plain_bat, "surrogate_batched": sur_bat,
+        "speedup_vs_plain_separate": sur_bat["value"] / plain_sep["value"],
+        "speedup_vs_plain_batched": sur_bat["value"] / plain_bat["value"],
+        "batching_speedup_plain": plain_bat["value"] / plain_sep["value"],
+        "parity_vs_plain_batched": {"singles_energy_350_650keV": _chi2(mc_e, su_e),
+                                    "singles_per_crystal": _chi2(mc_c, su_c),
+                                    "per_crystal_max_rel_dev": float(np.abs(rel).max()),
+                                    "per_crystal_within_2pct": bool(np.abs(rel).max() < 0.02),
+                                    "singles_plain": float(mc_c.sum()), "singles_surrogate": float(su_c.sum())},
+        "amdahl": {"detector_share_of_plain_batched_job": det_share,
+                   "bound_free_detector_vs_plain_batched": 1.0 / max(1e-9, 1.0 - det_share),
+                   "bound_free_detector_vs_plain_separate":
+                       plain_bat["value"] / plain_sep["value"] / max(1e-9, 1.0 - det_share)},
+        "model": {"file": "data/surrogate_positron_ring.npz", "train_records": meta.get("train_records"),
+                  "epochs": meta.get("train", {}).get("epochs"),
+                  "calibration_records": meta.get("calibration_records"),
+                  "domain": "entry energy 100-520 keV, >= 3 mm inside the panel edges, all panels"},
+    }
 
 
 def run_batched_workload(args, surrogate=False):
@@ -519,9 +641,12 @@ def _chi2(a, b):
     kb = 1.0 / ka
     chi2 = float((((ka * a - kb * b) ** 2) / (a + b)).sum())
     ndf = int(keep.sum()) - 1
-    rel = np.abs(b / b.sum() - a / a.sum()) / np.maximum(a / a.sum(), 1e-12)
-    return {"chi2": chi2, "ndf": ndf, "p": float(stats.chi2.sf(chi2, ndf)), "max_rel_dev": float(rel.max()),
-            "mean_rel_dev": float(rel.mean())}
+    # relative deviations over the bins holding at least 1000 counts in each
+    big = (a >= 1000) & (b >= 1000)
+    rel = np.abs(b[big] / b.sum() - a[big] / a.sum()) / (a[big] / a.sum())
+    return {"chi2": chi2, "ndf": ndf, "p": float(stats.chi2.sf(chi2, ndf)),
+            "max_rel_dev": float(rel.max()) if big.any() else None,
+            "mean_rel_dev": float(rel.mean()) if big.any() else None}
 
 
 def run_surrogate_workload(args):
@@ -552,15 +677,23 @@ def run_surrogate_workload(args):
             return c
 
         t0 = time.perf_counter()
-        gen = ctx_for(record_entries=1, n_decays=args.train_decays, seed=555)
-        gen.run()
-        rec = gen.entries()
-        sur = api.Surrogate(gen, seed=9)
-        losses = sur.train(rec, epochs=args.train_epochs, batch=8192, lr=2e-3)
-        sur.set_domain(1.0e5, 5.2e5, 0.3)
-        calib = sur.calibrate(rec, iters=args.calib_iters) if args.calib_iters > 0 else None
+        if args.model:
+            # the committed model (data/make_surrogate.py)
+            gen = ctx_for(n_decays=1000)
+            sur = api.Surrogate(gen, seed=9)
+            meta = sur.load(args.model)
+            rec, losses, calib = np.zeros(meta["train_records"]), meta["loss_per_epoch"], \
+                meta["calibration_last_max_log_ratio"]
+        else:
+            gen = ctx_for(record_entries=1, n_decays=args.train_decays, seed=555)
+            gen.run()
+            rec = gen.entries()
+            sur = api.Surrogate(gen, seed=9)
+            losses = sur.train(rec, epochs=args.train_epochs, batch=8192, lr=2e-3)
+            sur.set_domain(1.0e5, 5.2e5, 0.3)
+            calib = sur.calibrate(rec, iters=args.calib_iters) if args.calib_iters > 0 else None
+            gen.close()
         train_s = time.perf_counter() - t0
-        gen.close()
         res = {}
         for mode in ("mc", "surrogate"):
             ctx = ctx_for()
@@ -736,7 +869,8 @@ def main():
     ap.add_argument("--decays", type=int, default=None,
                     help="decays per step (default 1e8; 1e9 for the large workload)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--ref-step-seconds", type=float, default=2.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=0.0,
+                    help="reference arm: decays per step sized to about this many seconds (0: the whole workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
                     help="time launch shapes on a sample before the warm-up (results do not depend on the shape)")
@@ -745,6 +879,8 @@ def main():
                     help="context option for the headline workload (e.g. a fixed launch shape for profiling)")
     ap.add_argument("--e2e-steps", type=int, default=-1,
                     help="steps of the end-to-end leg (default max(2, steps/2); 0 skips it: profiling only)")
+    ap.add_argument("--surrogate-steps", type=int, default=3,
+                    help="jobs per arm of the surrogate+batched measurement in the default line (0: skip)")
     ap.add_argument("--gloo", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--workload", choices=["positron", "batched64", "surrogate", "surrogate_batched64", "large", "widen"],
                     default="positron",
@@ -757,6 +893,9 @@ def main():
     ap.add_argument("--batch-sims", type=int, default=64, help=argparse.SUPPRESS)
     ap.add_argument("--psf-decays", type=int, default=10_000_000, help=argparse.SUPPRESS)
     ap.add_argument("--calib-iters", type=int, default=10, help=argparse.SUPPRESS)
+    ap.add_argument("--model", default=None,
+                    help="surrogate workload: load this model (e.g. data/surrogate_positron_ring.npz) instead of "
+                         "training one")
     args = ap.parse_args()
     args.set = dict(kv.split("=", 1) for kv in args.set)
     if args.decays is None:
