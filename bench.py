@@ -393,89 +393,71 @@ BATCH_WORKLOAD = ("batched64: 64 simulations of uneven size in one job - phantom
 SURROGATE_MODEL = os.path.join(ROOT, "data", "surrogate_positron_ring.npz")
 
 
-def measure_surrogate_batched(steps, warmup, model_path=SURROGATE_MODEL):
-    """The metric's second form: the 64-simulation job (BATCH_WORKLOAD) with
-    the learned detector response (the committed model, trained by
-    data/make_surrogate.py with the library's kernels), batched in one job,
-    against the plain form (plain Monte Carlo, each simulation its own run)
-    and plain Monte Carlo batched; device time (CUDA events) per job, L2
-    flushed before each; the singles of the plain batched and surrogate
-    batched arms (independent seeds) compared by two-sample chi-square."""
+def _three_arms(ctxs, seeds, sur, steps, warmup, ncry):
+    """One job of several loaded contexts in three forms: each its own plain
+    Monte Carlo run (the plain form), plain Monte Carlo batched, and batched
+    with the surrogate `sur`; device time per job (CUDA events), L2 flushed
+    before each; the pooled singles of the two batched arms (independent
+    seeds) compared by two-sample chi-square."""
     import numpy as np
     import torch
-    from gpet_gb300 import api, scenes
+    from gpet_gb300 import api
     flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda:0")
-    data = os.path.join(ROOT, "data")
-    with tempfile.TemporaryDirectory() as d:
-        sims = scenes.batched(d)
-        ctxs = []
-        for bs in sims:
-            c = api.Context(0)
-            c.set_options(dict(bs.options, data_dir=data, base_dir=d))
-            c.load_config(bs.config_path)
-            mat, den = bs.phantom()
-            c.set_phantom(mat, den, (bs.nvox,) * 3, (-3.2,) * 3, (6.4,) * 3)
-            c.set_source_file(bs.source_path, 0.0, 120.0)
-            ctxs.append(c)
-        seeds = [bs.options["seed"] for bs in sims]
-        sur = api.Surrogate(ctxs[0], seed=1)
-        meta = sur.load(model_path)
 
-        def reseed(k):
-            for c, sd in zip(ctxs, seeds):
-                c.set_option("seed", sd + 1000003 * k)
+    def reseed(k):
+        for c, sd in zip(ctxs, seeds):
+            c.set_option("seed", sd + 1000003 * k)
 
-        def arm(kind, k0):
-            for c in ctxs:
-                c.set_surrogate(sur if kind == "surrogate_batched" else None)
-            tot = {"ms": 0.0, "det": 0.0, "coinc": 0, "decays": 0, "nsur": 0, "entered": 0, "launches": 0,
-                   "true": 0, "scatter": 0, "random": 0, "singles": 0}
-            he, hc = np.zeros(60), np.zeros(64)
-            for k in range(-warmup, steps):
-                flush.zero_()
-                torch.cuda.synchronize()
-                reseed(k0 + k)
-                if kind == "plain_separate":
-                    st = [c.run() for c in ctxs]
-                    ms = sum(x["ms_total"] for x in st)
-                    det = sum(x["ms_detector"] for x in st)
-                    launches = sum(x["kernel_launches"] for x in st)
-                else:
-                    st = api.run_batched(ctxs)
-                    ms, det, launches = st[0]["ms_total"], st[0]["ms_detector"], st[0]["kernel_launches"]
-                if k < 0:
-                    continue
-                tot["ms"] += ms; tot["det"] += det; tot["launches"] += launches
-                for key, f in (("coinc", "n_coinc"), ("decays", "n_decays"), ("nsur", "n_surrogate"),
-                               ("entered", "n_entered"), ("true", "n_true"), ("scatter", "n_scatter"),
-                               ("random", "n_random"), ("singles", "n_singles")):
-                    tot[key] += sum(x[f] for x in st)
-                if kind != "plain_separate":
-                    for c in ctxs:
-                        s_ev, _ = c.singles()
-                        he += np.histogram(s_ev["E"], bins=60, range=(3.5e5, 6.5e5))[0]
-                        hc += np.bincount(s_ev["cryn"], minlength=64)[:64]
-            r = {"value": tot["coinc"] / (tot["ms"] * 1e-3), "unit": UNIT, "ms_per_job": tot["ms"] / steps,
-                 "detector_ms_per_job": tot["det"] / steps, "coincidences_per_job": tot["coinc"] / steps,
-                 "singles_per_job": tot["singles"] / steps, "gpu_launches_per_job": tot["launches"] / steps,
-                 "classes_per_job": {"true": tot["true"] / steps, "scatter": tot["scatter"] / steps,
-                                     "random": tot["random"] / steps}}
-            if kind == "surrogate_batched":
-                r["fraction_of_entered_photons"] = tot["nsur"] / max(1, tot["entered"])
-            return r, he, hc, tot
-
-        plain_sep, _, _, t_sep = arm("plain_separate", 0)
-        plain_bat, mc_e, mc_c, t_bat = arm("plain_batched", 0)
-        sur_bat, su_e, su_c, t_sur = arm("surrogate_batched", 50000)
+    def arm(kind, k0):
         for c in ctxs:
-            c.set_surrogate(None)
-            c.close()
-        sur.close()
-    rel = (su_c / su_c.sum()) / (mc_c / mc_c.sum()) - 1.0
+            c.set_surrogate(sur if kind == "surrogate_batched" else None)
+        tot = {"ms": 0.0, "det": 0.0, "coinc": 0, "decays": 0, "nsur": 0, "entered": 0, "launches": 0,
+               "true": 0, "scatter": 0, "random": 0, "singles": 0}
+        he, hc = np.zeros(60), np.zeros(ncry)
+        for k in range(-warmup, steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            reseed(k0 + k)
+            if kind == "plain_separate":
+                st = [c.run() for c in ctxs]
+                ms = sum(x["ms_total"] for x in st)
+                det = sum(x["ms_detector"] for x in st)
+                launches = sum(x["kernel_launches"] for x in st)
+            else:
+                st = api.run_batched(ctxs)
+                ms, det, launches = st[0]["ms_total"], st[0]["ms_detector"], st[0]["kernel_launches"]
+            if k < 0:
+                continue
+            tot["ms"] += ms; tot["det"] += det; tot["launches"] += launches
+            for key, f in (("coinc", "n_coinc"), ("decays", "n_decays"), ("nsur", "n_surrogate"),
+                           ("entered", "n_entered"), ("true", "n_true"), ("scatter", "n_scatter"),
+                           ("random", "n_random"), ("singles", "n_singles")):
+                tot[key] += sum(x[f] for x in st)
+            if kind != "plain_separate":
+                for c in ctxs:
+                    s_ev, _ = c.singles()
+                    he += np.histogram(s_ev["E"], bins=60, range=(3.5e5, 6.5e5))[0]
+                    hc += np.bincount(s_ev["cryn"], minlength=ncry)[:ncry]
+        r = {"value": tot["coinc"] / (tot["ms"] * 1e-3), "unit": UNIT, "ms_per_job": tot["ms"] / steps,
+             "detector_ms_per_job": tot["det"] / steps, "coincidences_per_job": tot["coinc"] / steps,
+             "singles_per_job": tot["singles"] / steps, "gpu_launches_per_job": tot["launches"] / steps,
+             "classes_per_job": {"true": tot["true"] / steps, "scatter": tot["scatter"] / steps,
+                                 "random": tot["random"] / steps}}
+        if kind == "surrogate_batched":
+            r["fraction_of_entered_photons"] = tot["nsur"] / max(1, tot["entered"])
+        return r, he, hc, tot
+
+    plain_sep, _, _, _ = arm("plain_separate", 0)
+    plain_bat, mc_e, mc_c, t_bat = arm("plain_batched", 0)
+    sur_bat, su_e, su_c, _ = arm("surrogate_batched", 50000)
+    for c in ctxs:
+        c.set_surrogate(None)
+    big = mc_c >= 1000
+    rel = (su_c[big] / su_c.sum()) / (mc_c[big] / mc_c.sum()) - 1.0
     det_share = plain_bat["detector_ms_per_job"] / plain_bat["ms_per_job"]
     return {
-        "workload": BATCH_WORKLOAD, "simulations": len(sims), "decays_per_job": t_bat["decays"] / steps,
-        "steps": steps, "warmup": warmup, "l2": "flushed before each job (512 MB write)",
+        "decays_per_job": t_bat["decays"] / steps, "steps": steps, "warmup": warmup,
+        "l2": "flushed before each job (512 MB write)",
         "plain_separate": plain_sep, "plain_batched": plain_bat, "surrogate_batched": sur_bat,
         "speedup_vs_plain_separate": sur_bat["value"] / plain_sep["value"],
         "speedup_vs_plain_batched": sur_bat["value"] / plain_bat["value"],
@@ -489,11 +471,92 @@ def measure_surrogate_batched(steps, warmup, model_path=SURROGATE_MODEL):
                    "bound_free_detector_vs_plain_batched": 1.0 / max(1e-9, 1.0 - det_share),
                    "bound_free_detector_vs_plain_separate":
                        plain_bat["value"] / plain_sep["value"] / max(1e-9, 1.0 - det_share)},
-        "model": {"file": "data/surrogate_positron_ring.npz", "train_records": meta.get("train_records"),
-                  "epochs": meta.get("train", {}).get("epochs"),
-                  "calibration_records": meta.get("calibration_records"),
-                  "domain": "entry energy 100-520 keV, >= 3 mm inside the panel edges, all panels"},
     }
+
+
+def _model_meta(path, meta, domain="entry energy 100-520 keV, >= 3 mm inside the panel edges, all panels"):
+    return {"file": os.path.relpath(path, ROOT), "train_records": meta.get("train_records"),
+            "epochs": meta.get("train", {}).get("epochs"), "calibration_records": meta.get("calibration_records"),
+            "domain": domain}
+
+
+def measure_surrogate_batched(steps, warmup, model_path=SURROGATE_MODEL):
+    """The metric's second form: the 64-simulation job (BATCH_WORKLOAD) with
+    the learned detector response (the committed model, trained by
+    data/make_surrogate.py with the library's kernels), batched in one job,
+    against the plain form and plain batched (_three_arms)."""
+    from gpet_gb300 import api, scenes
+    data = os.path.join(ROOT, "data")
+    with tempfile.TemporaryDirectory() as d:
+        sims = scenes.batched(d)
+        ctxs = []
+        for bs in sims:
+            c = api.Context(0)
+            c.set_options(dict(bs.options, data_dir=data, base_dir=d))
+            c.load_config(bs.config_path)
+            mat, den = bs.phantom()
+            c.set_phantom(mat, den, (bs.nvox,) * 3, (-3.2,) * 3, (6.4,) * 3)
+            c.set_source_file(bs.source_path, 0.0, 120.0)
+            ctxs.append(c)
+        sur = api.Surrogate(ctxs[0], seed=1)
+        meta = sur.load(model_path)
+        res = _three_arms(ctxs, [bs.options["seed"] for bs in sims], sur, steps, warmup, 64)
+        for c in ctxs:
+            c.close()
+        sur.close()
+    return dict({"workload": BATCH_WORKLOAD, "simulations": len(sims)}, **res,
+                model=_model_meta(model_path, meta))
+
+
+WHOLEBODY_MODEL = os.path.join(ROOT, "data", "surrogate_wholebody_ring.npz")
+BEDS_WORKLOAD = ("whole-body in 8 bed positions: the large workload's body (256x256x512 x 2 mm) and source "
+                 "shifted along z in 6.4 cm steps through the 48-panel ring (16x16 crystals 4x4x20 mm), "
+                 "1e9 F-18 decays in all (1.25e8 per bed), one simulation per bed")
+
+
+def run_beds_workload(args):
+    """BASELINE's whole-body configuration as plain Monte Carlo and as
+    surrogate + batched (8 bed positions batched): the three arms of
+    _three_arms with the committed whole-body model."""
+    import torch
+    from gpet_gb300 import api, formats as F, scenes
+    torch.cuda.set_device(0)
+    data = os.path.join(ROOT, "data")
+    with tempfile.TemporaryDirectory() as d:
+        t0 = time.perf_counter()
+        beds = scenes.large_beds(d, decays_per_bed=args.decays // 8)
+        cfg = F.read_config(beds[0].config_path)
+        mat, den = F.read_phantom(cfg.matfile, cfg.denfile, tuple(cfg.pdim))
+        ctxs = []
+        for b in beds:
+            c = api.Context(0)
+            c.set_options(dict(b.options, data_dir=data, base_dir=d))
+            c.load_config(b.config_path)
+            c.set_phantom(mat, den, b.dims, b.offset, b.size)
+            c.set_source_file(b.source_path, 0.0, 120.0)
+            ctxs.append(c)
+        setup_s = time.perf_counter() - t0
+        sur = api.Surrogate(ctxs[0], seed=1)
+        meta = sur.load(args.model or WHOLEBODY_MODEL)
+        sampler = ClockSampler(0)
+        sampler.start()
+        res = _three_arms(ctxs, [b.options["seed"] for b in beds], sur, args.steps, args.warmup, 256)
+        clocks = sampler.stop()
+        for c in ctxs:
+            c.close()
+        sur.close()
+    sb = res["surrogate_batched"]
+    line = {"metric": METRIC.replace("(plain MC)", "(whole-body: surrogate detector response, 8 bed positions "
+                                                   "batched)"),
+            "value": sb["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": sb["ms_per_job"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 (MLP), f32 (transport)", "data": "synthetic (seeded)",
+            "config": {"workload": BEDS_WORKLOAD, "decays_per_step": args.decays, "beds": len(beds),
+                       "l2": "flushed between steps (512 MB write)"},
+            "setup_s": setup_s, "clocks": clocks,
+            "model": _model_meta(args.model or WHOLEBODY_MODEL, meta)}
+    line.update(res)
+    print(json.dumps(line), flush=True)
 
 
 def run_batched_workload(args, surrogate=False):
@@ -882,12 +945,14 @@ def main():
     ap.add_argument("--surrogate-steps", type=int, default=3,
                     help="jobs per arm of the surrogate+batched measurement in the default line (0: skip)")
     ap.add_argument("--gloo", action="store_true", help=argparse.SUPPRESS)
-    ap.add_argument("--workload", choices=["positron", "batched64", "surrogate", "surrogate_batched64", "large", "widen"],
+    ap.add_argument("--workload", choices=["positron", "batched64", "surrogate", "surrogate_batched64", "large", "widen",
+                                           "beds"],
                     default="positron",
                     help="positron: the headline workload; batched64: 64 uneven simulations in one job; "
                          "surrogate: the headline workload with the learned detector response; "
                          "surrogate_batched64: the 64-simulation job with and without it; "
-                         "large: the whole-body configuration (48 panels, 256x256x512 phantom)")
+                         "large: the whole-body configuration (48 panels, 256x256x512 phantom); "
+                         "beds: the whole-body configuration in 8 bed positions, plain and surrogate + batched")
     ap.add_argument("--train-decays", type=int, default=200_000_000, help=argparse.SUPPRESS)
     ap.add_argument("--train-epochs", type=int, default=12, help=argparse.SUPPRESS)
     ap.add_argument("--batch-sims", type=int, default=64, help=argparse.SUPPRESS)
@@ -899,7 +964,7 @@ def main():
     args = ap.parse_args()
     args.set = dict(kv.split("=", 1) for kv in args.set)
     if args.decays is None:
-        args.decays = 1_000_000_000 if args.workload == "large" else 100_000_000
+        args.decays = 1_000_000_000 if args.workload in ("large", "beds") else 100_000_000
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
@@ -912,6 +977,8 @@ def main():
         run_surrogate_workload(args)
     elif args.workload == "widen":
         run_widen_workload(args)
+    elif args.workload == "beds":
+        run_beds_workload(args)
     else:
         run_ours(args)
 

@@ -243,8 +243,42 @@ __device__ __forceinline__ int sample_energy(uint32_t taddr, const float* hb, fl
     return bin;
 }
 
-// crystal: softmax over the ncry columns of crystal set `set` ([64 set, 64 set + ncry))
-__device__ __forceinline__ int sample_crystal(uint32_t taddr, const float* hb, int set, int ncry, float uc)
+// index drawn with probability softmax(v[0..n)) at uniform u (first index
+// whose running sum reaches u times the total)
+template <int N>
+__device__ __forceinline__ int softmax_draw(float (&v)[N], int n, float u)
+{
+    float mx = -1e30f;
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+        if (k < n) mx = fmaxf(mx, v[k]);
+    float sum = 0.0f;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        if (k < n) {
+            v[k] = __expf(v[k] - mx);
+            sum += v[k];
+        }
+    }
+    const float target = u * sum;
+    float acc = 0.0f;
+    int pick = n - 1;
+    bool found = false;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        if (k < n && !found) {
+            acc += v[k];
+            if (acc >= target) { pick = k; found = true; }
+        }
+    }
+    return pick;
+}
+
+// crystal of set `set` (columns [64 set, 64 set + 64)): one softmax over the
+// ncry crystals, or (fact) a row from the first 32 columns (ny rows, uniform
+// uc) and a column from the last 32 (nz columns, uniform uc2)
+__device__ __forceinline__ int sample_crystal(uint32_t taddr, const float* hb, int set, int ncry, int fact, int ny,
+                                              int nz, float uc, float uc2)
 {
     using namespace sg;
     const int c0 = kCry * set;
@@ -252,33 +286,21 @@ __device__ __forceinline__ int sample_crystal(uint32_t taddr, const float* hb, i
     umma::tmem_ld32_nowait(taddr + c0, a);
     umma::tmem_ld32_nowait(taddr + c0 + 32, b);
     umma::tmem_wait_ld();
+    if (fact) {
+        float r[32], c[32];
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+            r[k] = __uint_as_float(a[k]) + hb[c0 + k];
+            c[k] = __uint_as_float(b[k]) + hb[c0 + 32 + k];
+        }
+        const int ly = softmax_draw(r, ny, uc);
+        const int lz = softmax_draw(c, nz, uc2);
+        return ly + ny * lz;
+    }
     float e[kCry];
 #pragma unroll
     for (int k = 0; k < kCry; ++k) e[k] = __uint_as_float(k < 32 ? a[k] : b[k - 32]) + hb[c0 + k];
-    float mx = -1e30f;
-#pragma unroll
-    for (int k = 0; k < kCry; ++k)
-        if (k < ncry) mx = fmaxf(mx, e[k]);
-    float sum = 0.0f;
-#pragma unroll
-    for (int k = 0; k < kCry; ++k) {
-        if (k < ncry) {
-            e[k] = __expf(e[k] - mx);
-            sum += e[k];
-        }
-    }
-    const float target = uc * sum;
-    float acc = 0.0f;
-    int cry = ncry - 1;
-    bool found = false;
-#pragma unroll
-    for (int k = 0; k < kCry; ++k) {
-        if (k < ncry && !found) {
-            acc += e[k];
-            if (acc >= target) { cry = k; found = true; }
-        }
-    }
-    return cry;
+    return softmax_draw(e, ncry, uc);
 }
 
 // depth below the entry face over the panel depth: one component of the
@@ -578,7 +600,13 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd(SurrogateDev sd, Fwd
             if (cq == 0) {
                 s_bin[rloc] = sample_energy(taddr, hb, ue);
             } else if (cq == 1 || cq == 3) {
-                s_cry[cq >> 1][rloc] = sample_crystal(taddr, hb, cq >> 1, sd.crystalN, uc);
+                // the column of a factorised head takes the stream's seventh
+                // word (the depth group's normal takes the fifth and sixth)
+                st_next(st);
+                st_next(st);
+                const float uc2 = st_u(st);
+                s_cry[cq >> 1][rloc] = sample_crystal(taddr, hb, cq >> 1, sd.crystalN, sd.fact, sd.crystalNy,
+                                                      sd.crystalNz, uc, uc2);
             } else {
                 const float zn = st_normal(st);
                 s_depth[rloc] = sample_depth(taddr, hb, um, zn);
@@ -728,9 +756,22 @@ __global__ void k_entry_features(const EntryRec* __restrict__ rec, int64_t n, Su
 }
 
 // loss of each sample and d loss / d output (mean over the n samples)
+// cross entropy of the logits o[0..n) against class t; d[0..n) = its gradient times scale
+__device__ __forceinline__ float xent(const float* o, int n, int t, float scale, float* d)
+{
+    float mx = -1e30f;
+    for (int k = 0; k < n; ++k) mx = fmaxf(mx, o[k]);
+    float s = 0.0f;
+    for (int k = 0; k < n; ++k) s += expf(o[k] - mx);
+    const float lse = mx + logf(s);
+    for (int k = 0; k < n; ++k) d[k] = (expf(o[k] - lse) - (k == t ? 1.0f : 0.0f)) * scale;
+    return lse - o[t];
+}
+
+// fact: the crystal head is a row softmax (ny) and a column softmax (nz)
 __global__ void k_loss(const float* __restrict__ out, int64_t n, const int32_t* __restrict__ cry,
-                       const float* __restrict__ dep, const int32_t* __restrict__ bin, int crystalN, float* dout,
-                       float* loss_sum)
+                       const float* __restrict__ dep, const int32_t* __restrict__ bin, int crystalN, int fact,
+                       int ny, int nz, float* dout, float* loss_sum)
 {
     using namespace sg;
     __shared__ float red[8];
@@ -754,14 +795,12 @@ __global__ void k_loss(const float* __restrict__ out, int64_t n, const int32_t* 
         if (cry[i] >= 0) {
             // the crystal set of the sample's energy class
             const int c0 = bin[i] >= kClassBin ? kCry : 0;
-            float mx = -1e30f;
-            for (int k = 0; k < crystalN; ++k) mx = fmaxf(mx, o[c0 + k]);
-            float s = 0.0f;
-            for (int k = 0; k < crystalN; ++k) s += expf(o[c0 + k] - mx);
-            const float lse = mx + logf(s);
-            lsum += lse - o[c0 + cry[i]];
-            for (int k = 0; k < crystalN; ++k)
-                d[c0 + k] = (expf(o[c0 + k] - lse) - (k == cry[i] ? 1.0f : 0.0f)) * scale;
+            if (fact) {
+                lsum += xent(o + c0, ny, cry[i] % ny, scale, d + c0);
+                lsum += xent(o + c0 + 32, nz, cry[i] / ny, scale, d + c0 + 32);
+            } else {
+                lsum += xent(o + c0, crystalN, cry[i], scale, d + c0);
+            }
             // depth: Gaussian mixture negative log likelihood
             const float x = dep[i];
             float lw[kMix], lp[kMix], ls[kMix], mu[kMix];
@@ -819,8 +858,10 @@ __global__ void k_gather_records(const EntryRec* __restrict__ all, const uint32_
 // belongs to neither) times the class's crystal probability — and
 // acc[2 * kCry + bin] of each energy bin. One warp per record, two bins and
 // two crystals per lane.
+// fact: acc[set * kCry + row] and acc[set * kCry + 32 + column] of the
+// factorised head's row and column softmaxes instead.
 __global__ void __launch_bounds__(256) k_calib_accum(const float* __restrict__ out, int64_t n, int crystalN,
-                                                     double* acc)
+                                                     int fact, int ny, int nz, double* acc)
 {
     using namespace sg;
     const int lane = threadIdx.x & 31;
@@ -848,6 +889,26 @@ __global__ void __launch_bounds__(256) k_calib_accum(const float* __restrict__ o
 #pragma unroll
         for (int set = 0; set < 2; ++set) {
             const float* l = o + set * kCry;
+            if (fact) {
+                // rows in the first 32 columns, columns in the last 32
+                const bool v0 = lane < ny, v1 = lane < nz;
+                const float l0 = v0 ? l[lane] : -1e30f, l1 = v1 ? l[32 + lane] : -1e30f;
+                float m0 = l0, m1 = l1;
+                for (int d = 16; d > 0; d >>= 1) {
+                    m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, d));
+                    m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, d));
+                }
+                const float y0 = v0 ? expf(l0 - m0) : 0.0f, y1 = v1 ? expf(l1 - m1) : 0.0f;
+                float t0 = y0, t1 = y1;
+                for (int d = 16; d > 0; d >>= 1) {
+                    t0 += __shfl_xor_sync(0xffffffffu, t0, d);
+                    t1 += __shfl_xor_sync(0xffffffffu, t1, d);
+                }
+                const float w = (set ? c1 : c0) / s;
+                a[set][0] += w * y0 / t0;
+                a[set][1] += w * y1 / t1;
+                continue;
+            }
             const bool v0 = lane < crystalN, v1 = 32 + lane < crystalN;
             const float l0 = v0 ? l[lane] : -1e30f, l1 = v1 ? l[32 + lane] : -1e30f;
             float m2 = fmaxf(l0, l1);
@@ -1116,6 +1177,8 @@ SurrogateDev make_view(const gpet_surrogate* s)
     d.margin = s->margin;
     d.crystalN = g.crystalN;
     d.crystalNy = g.crystalNy;
+    d.fact = g.crystalN > sg::kCry ? 1 : 0;
+    d.crystalNz = g.crystalNy > 0 ? g.crystalN / g.crystalNy : 0;
     d.rdepth = g.rdepth;
     d.rpolicy = g.rpolicy;
     d.moduleN = g.moduleN;
@@ -1204,7 +1267,8 @@ int loss_and_grad(gpet_surrogate* s, int64_t n, float* loss, float* acc_dev = nu
     if (!acc_dev) SCK(cudaMemsetAsync(s->loss.p, 0, 4, st));
     SCK(cudaMemsetAsync(s->grads.p, 0, (size_t)s->nparam * 4, st));
     k_loss<<<g1, 256, 0, st>>>(s->out.as<float>(), n, s->cry.as<int32_t>(), s->dep.as<float>(), s->bin.as<int32_t>(),
-                               s->geom.crystalN, s->dout.as<float>(), acc_dev ? acc_dev : s->loss.as<float>());
+                               s->geom.crystalN, sd.fact, sd.crystalNy, sd.crystalNz, s->dout.as<float>(),
+                               acc_dev ? acc_dev : s->loss.as<float>());
     SCK(cudaGetLastError());
     float* G = s->grads.as<float>();
     const __nv_bfloat16* Wb = s->wrow.as<__nv_bfloat16>();
@@ -1312,8 +1376,13 @@ int gpet_surrogate_create(gpet_ctx* ctx, uint64_t seed, gpet_surrogate** out)
     SurGeom g{};
     int rc = ctx_geometry(ctx, &g);
     if (rc) return rc;
-    if (g.moduleN != 1 || g.crystalN > sg::kCry || g.crystalN < 1 || g.rdepth > 2 || g.npanels < 1)
-        return GPET_ERR_ARG;   // more than one pulse per photon possible, or too many crystals
+    // one pulse per photon (one module, readout depth <= 2) and a crystal head
+    // that holds the crystals: up to 64 in one softmax, else a grid of up to
+    // 32 x 32 as rows and columns
+    const bool joint = g.crystalN >= 1 && g.crystalN <= sg::kCry;
+    const bool grid = g.crystalNy >= 1 && g.crystalNy <= 32 && g.crystalN % g.crystalNy == 0 &&
+                      g.crystalN / g.crystalNy <= 32;
+    if (g.moduleN != 1 || !(joint || grid) || g.rdepth > 2 || g.npanels < 1) return GPET_ERR_ARG;
     if (cudaSetDevice(g.device) != cudaSuccess) return GPET_ERR_NOGPU;
     auto* s = new gpet_surrogate();
     s->device = g.device;
@@ -1521,7 +1590,15 @@ int gpet_surrogate_calibrate(gpet_surrogate* s, const gpet_entry* rec, int64_t n
         if (e.crystal >= 0 && e.Edep > 0.0f) {
             b = (int)(e.Edep / e.E * (float)kBins);
             b = b < 1 ? 1 : (b > kBins - 1 ? kBins - 1 : b);
-            if (e.crystal < ncry) obs[(size_t)((b >= kClassBin ? kCry : 0) + e.crystal)] += 1.0;
+            const size_t c0 = b >= kClassBin ? kCry : 0;
+            if (e.crystal < ncry) {
+                if (sd.fact) {
+                    obs[c0 + (size_t)(e.crystal % sd.crystalNy)] += 1.0;
+                    obs[c0 + 32 + (size_t)(e.crystal / sd.crystalNy)] += 1.0;
+                } else {
+                    obs[c0 + (size_t)e.crystal] += 1.0;
+                }
+            }
         }
         obs[(size_t)(2 * kCry + b)] += 1.0;
     }
@@ -1552,7 +1629,7 @@ int gpet_surrogate_calibrate(gpet_surrogate* s, const gpet_entry* rec, int64_t n
             k_mlp_fwd<true><<<grid_cap(nb, 128, 152), kFwdThreads, smem, s->stream>>>(sd, tr, in,
                                                                                      s->errflag.as<int>());
             k_calib_accum<<<(unsigned)std::min<int64_t>((nb + 7) / 8, 152 * 8), 256, 0, s->stream>>>(
-                s->out.as<float>(), nb, ncry, s->calib.as<double>());
+                s->out.as<float>(), nb, ncry, sd.fact, sd.crystalNy, sd.crystalNz, s->calib.as<double>());
             SCK(cudaGetLastError());
         }
         std::vector<double> expd(kAcc);
@@ -1573,8 +1650,15 @@ int gpet_surrogate_calibrate(gpet_surrogate* s, const gpet_entry* rec, int64_t n
             bias[col] += d;
             last = std::max(last, std::fabs(d));
         };
-        for (int set = 0; set < 2; ++set)
-            for (int k = 0; k < ncry; ++k) nudge((size_t)(set * kCry + k), (size_t)(set * kCry + k));
+        for (int set = 0; set < 2; ++set) {
+            if (sd.fact) {
+                for (int k = 0; k < sd.crystalNy; ++k) nudge((size_t)(set * kCry + k), (size_t)(set * kCry + k));
+                for (int k = 0; k < sd.crystalNz; ++k)
+                    nudge((size_t)(set * kCry + 32 + k), (size_t)(set * kCry + 32 + k));
+            } else {
+                for (int k = 0; k < ncry; ++k) nudge((size_t)(set * kCry + k), (size_t)(set * kCry + k));
+            }
+        }
         for (int b = 0; b < kBins; ++b) nudge((size_t)(2 * kCry + b), (size_t)(kColE + b));
         SCK(cudaMemcpyAsync(pb, bias.data(), bias.size() * 4, cudaMemcpyHostToDevice, s->stream));
         rc = refresh_weights(s);

@@ -32,6 +32,10 @@ struct SurrogateDev {
     float dirsign;
     float e_lo, e_hi, margin;     // validated domain: entry energy (eV), distance from the panel edges (cm)
     int32_t crystalN, crystalNy, rdepth, rpolicy, moduleN;
+    // crystal head: 0 one softmax over the crystals of a set (at most 64);
+    // 1 a row softmax (columns [0, 32) of the set) and a column softmax
+    // ([32, 64)), for grids of up to 32 x 32 crystals
+    int32_t fact, crystalNz;
     float cry_pitch_y, cry_pitch_z, cry_y, cry_z;   // crystal pitch and size in y, z (module 0)
 };
 

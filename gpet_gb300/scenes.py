@@ -20,6 +20,9 @@ Workloads (materials are row indices of data/input4gPET.matter):
              ellipse, lungs, spine); 48 panels of 16x16 4x4x20 mm crystals.
   batched  : 64 simulations of uneven size for one batched job (phantoms
              64^3-256^3, 1e5-1e7 decays each, point or cylinder sources).
+  beds     : the large acquisition in 8 bed positions (the body shifted
+             along z by 6.4 cm steps), one simulation each, for one batched
+             job.
 """
 import os
 from dataclasses import dataclass, field
@@ -174,6 +177,43 @@ def large(directory, n_decays=1_000_000_000, dims=(256, 256, 512), seed=DEFAULT_
     return Scene(directory, os.path.join(directory, "input_PET.in"),
                  {"n_decays": n_decays, "seed": seed, "coinc_window_ns": 4.0},
                  "F-18 body phantom 256x256x512, 48-panel ring")
+
+
+@dataclass
+class BedPosition:
+    """One bed position of the whole-body acquisition: the body and its
+    source moved along z by `shift` cm through the ring (the configuration
+    and phantom of `large`, offset), with its own decays and seed."""
+    config_path: str
+    directory: str
+    source_path: str
+    shift: float
+    offset: tuple
+    size: tuple
+    dims: tuple
+    options: dict
+
+
+def large_beds(directory, n_beds=8, decays_per_bed=125_000_000, dims=(256, 256, 512), voxel_cm=0.2,
+               seed=DEFAULT_SEED):
+    """Whole-body acquisition in n_beds bed positions: the body of `large`
+    (its source, a cylinder r=10 cm h=60 cm, moving with it) shifted along z
+    so that consecutive positions put adjacent 6.4 cm slabs (the ring's axial
+    extent) in the ring. Returns the BedPosition list; the phantom is
+    written once (phantom_mat.dat / phantom_den.dat of the `large` scene)."""
+    sc = large(directory, n_decays=decays_per_bed, dims=dims, seed=seed, voxel_cm=voxel_cm)
+    nx, ny, nz = dims
+    size = (voxel_cm * nx, voxel_cm * ny, voxel_cm * nz)
+    beds = []
+    for k in range(n_beds):
+        shift = (k - 0.5 * (n_beds - 1)) * 6.4
+        src = os.path.join(directory, "source_bed%d.txt" % k)
+        F.write_sources(src, [4_000_000_000], [0], [1], [(0, 0, shift, 10.0, 60.0, 0)])
+        off = (-size[0] / 2, -size[1] / 2, -size[2] / 2 + shift)
+        beds.append(BedPosition(sc.config_path, directory, src, shift, off, size, dims,
+                                {"n_decays": decays_per_bed, "seed": seed + 7919 * (k + 1), "sim_id": k,
+                                 "coinc_window_ns": 4.0}))
+    return beds
 
 
 @dataclass

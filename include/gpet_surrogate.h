@@ -36,8 +36,12 @@ int gpet_get_entries(gpet_ctx* ctx, gpet_entry* buf, int64_t cap, int64_t* n);
 
 /* A surrogate for the detector of `ctx` (its panel geometry, materials and
  * readout, which must give at most one pulse per photon: one module per
- * panel, readout depth <= 2, at most 64 crystals), with seeded random
- * initial weights, on ctx's device. */
+ * panel, readout depth <= 2), with seeded random initial weights, on ctx's
+ * device. Up to 64 crystals per panel, each energy class's crystal set is one
+ * softmax over the crystals; a grid of up to 32 x 32 crystals (the
+ * whole-body ring's 16 x 16) is factorised: the set's first 32 columns are
+ * row logits, its last 32 column logits, the crystal row + crystalNy x
+ * column. */
 int gpet_surrogate_create(gpet_ctx* ctx, uint64_t seed, gpet_surrogate** out);
 void gpet_surrogate_destroy(gpet_surrogate* s);
 const char* gpet_surrogate_last_error(gpet_surrogate* s);
@@ -58,7 +62,7 @@ int gpet_surrogate_set_domain(gpet_surrogate* s, float e_lo, float e_hi, float m
 int gpet_surrogate_grad(gpet_surrogate* s, const gpet_entry* rec, int64_t n, float* loss, float* grad);
 /* Raw head outputs [n][208] of n records (for checks): crystal logits of the
  * partial-deposit class [0, 64) and of the near-full class [64, 128) (energy
- * bin >= 40 of 64), mixture weights [128, 132), means [132, 136), log sigmas
+ * bin >= 40 of 64; factorised: rows then columns in each), mixture weights [128, 132), means [132, 136), log sigmas
  * [136, 140), energy-fraction logits [140, 204). */
 int gpet_surrogate_forward(gpet_surrogate* s, const gpet_entry* rec, int64_t n, float* out208);
 /* Adam (beta 0.9, 0.999) over `epochs` shuffled passes in batches of

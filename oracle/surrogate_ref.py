@@ -123,8 +123,23 @@ def _lse(x, axis=-1):
     return (m + np.log(np.exp(x - m).sum(axis=axis, keepdims=True)))
 
 
-def loss_and_dout(out, cry, dep, b, crystal_n):
-    """Mean loss and d loss / d out (float64)."""
+def _xent(out, d, rows, cols, target):
+    """Cross entropy of out[rows, cols] against target columns; adds the
+    gradient into d and returns the summed loss."""
+    c = out[rows[:, None], cols]
+    cl = _lse(c)
+    loss = (cl[:, 0] - c[np.arange(len(rows)), target]).sum()
+    pc = np.exp(c - cl)
+    pc[np.arange(len(rows)), target] -= 1.0
+    d[rows[:, None], cols] = pc
+    return loss
+
+
+def loss_and_dout(out, cry, dep, b, crystal_n, crystal_ny=None):
+    """Mean loss and d loss / d out (float64). A head of more than 64
+    crystals is factorised: the first 32 columns of each energy class's set
+    are row logits (crystal_ny rows), the last 32 column logits (crystal_n /
+    crystal_ny columns), the crystal being row + crystal_ny * column."""
     n = len(out)
     d = np.zeros_like(out)
     e = out[:, COL_E:COL_E + BINS]
@@ -137,13 +152,14 @@ def loss_and_dout(out, cry, dep, b, crystal_n):
     if has.any():
         i = np.nonzero(has)[0]
         # the crystal set of each sample's energy class
-        cols = np.where(b[i] >= CLASS_BIN, CRY, 0)[:, None] + np.arange(crystal_n)[None, :]
-        c = out[i[:, None], cols]
-        cl = _lse(c)
-        loss += (cl[:, 0] - c[np.arange(len(i)), cry[i]]).sum()
-        pc = np.exp(c - cl)
-        pc[np.arange(len(i)), cry[i]] -= 1.0
-        d[i[:, None], cols] = pc
+        c0 = np.where(b[i] >= CLASS_BIN, CRY, 0)[:, None]
+        if crystal_n > CRY:
+            ny = crystal_ny
+            nz = crystal_n // ny
+            loss += _xent(out, d, i, c0 + np.arange(ny)[None, :], cry[i] % ny)
+            loss += _xent(out, d, i, c0 + 32 + np.arange(nz)[None, :], cry[i] // ny)
+        else:
+            loss += _xent(out, d, i, c0 + np.arange(crystal_n)[None, :], cry[i])
         w = out[i, COL_W:COL_W + MIX]
         lw = w - _lse(w)
         mu = out[i, COL_MU:COL_MU + MIX]
@@ -163,9 +179,11 @@ def loss_and_dout(out, cry, dep, b, crystal_n):
     return loss / n, d / n
 
 
-def forward_backward(params, rec, npanels, half_y, half_z, depth_len, crystal_n, rounding=True, pitch=None):
+def forward_backward(params, rec, npanels, half_y, half_z, depth_len, crystal_n, rounding=True, pitch=None,
+                     crystal_ny=None):
     """Loss, gradient (flat, like params) and head outputs of the records;
-    pitch: the crystal pitch (y, z), default_pitch when None."""
+    pitch: the crystal pitch (y, z), default_pitch when None; crystal_ny:
+    crystals per row (square grid when None)."""
     p = np.asarray(params, np.float64)
     Ws, bs, emb = unpack(p, npanels)
     r = bf16 if rounding else (lambda x: np.asarray(x, np.float64))
@@ -186,7 +204,9 @@ def forward_backward(params, rec, npanels, half_y, half_z, depth_len, crystal_n,
         else:
             out = z
     cry, dep, b = targets(rec, depth_len)
-    loss, dz = loss_and_dout(out, cry, dep, b, crystal_n)
+    if crystal_ny is None:
+        crystal_ny = int(round(np.sqrt(crystal_n)))
+    loss, dz = loss_and_dout(out, cry, dep, b, crystal_n, crystal_ny)
     lay, emb_off, total = offsets(npanels)
     g = np.zeros(total, np.float64)
     for l in range(LAYERS - 1, -1, -1):

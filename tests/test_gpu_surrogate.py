@@ -94,6 +94,32 @@ def test_forward_and_gradients_match_oracle(scene_positron, data_dir, gpet_lib):
     assert loss2 < loss
 
 
+def test_factorised_head_forward_and_gradients_match_oracle(scene_large, data_dir, gpet_lib):
+    """The whole-body ring (48 panels of 16 x 16 crystals): the factorised
+    crystal head (row and column logits per energy class) through the fused
+    forward and the backward products, against the oracle."""
+    from gpet_gb300 import api
+    ctx = make_ctx(scene_large, data_dir)
+    sur = api.Surrogate(ctx, seed=4)
+    npan, hy, hz, dl, ncry, pitch = _geom(ctx)
+    _, _, cny, _ = ctx.counts()
+    assert npan == 48 and ncry == 256 and cny == 16
+    p = S.init_params(npan, 12)
+    sur.set_params(p)
+    rec = S.random_records(1000, npan, hy, hz, dl, ncry, 6)
+    loss_ref, g_ref, out_ref = S.forward_backward(p, rec, npan, hy, hz, dl, ncry, rounding=True, pitch=pitch,
+                                                  crystal_ny=cny)
+    out = sur.forward(rec)
+    assert _rel(out[:, :S.OUT_USED], out_ref[:, :S.OUT_USED]) < 5e-3
+    loss, g = sur.grad(rec)
+    assert abs(loss - loss_ref) <= 2e-4 * abs(loss_ref)
+    lay, emb_off, total = S.offsets(npan)
+    w4, b4 = lay[-1]
+    assert _rel(g[w4:b4], g_ref[w4:b4]) < 2e-2
+    assert _rel(g[b4:b4 + S.OUT], g_ref[b4:b4 + S.OUT]) < 1e-2
+    assert _rel(g[emb_off:], g_ref[emb_off:]) < 2e-2
+
+
 def test_entries_train_and_run_with_surrogate(scene_positron, data_dir, gpet_lib):
     from gpet_gb300 import api
     gen = make_ctx(scene_positron, data_dir, seed=101, n_decays=300000, record_entries=1)

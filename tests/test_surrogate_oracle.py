@@ -88,3 +88,30 @@ def test_bf16_rounding():
     assert r[2] == np.float32(1.0078125)
     assert abs(r[3] + 3.140625) < 1e-6
     assert (r.view(np.uint32) & 0xFFFF == 0).all()
+
+
+def test_factorised_head_backward_matches_finite_differences():
+    """A ring of 16 x 16 crystals (more than the 64 one softmax holds): each
+    energy class's set holds 16 row logits (columns 0-15 of the set) and 16
+    column logits (32-47); its gradient against finite differences, and no
+    gradient on the set's unused columns."""
+    npan, ncry, ny = 4, 256, 16
+    p = S.init_params(npan, 9).astype(np.float64)
+    rec = S.random_records(32, npan, 3.2, 3.2, DEPTH, ncry, 10)
+    pitch = (0.4, 0.4)
+    loss, g, _ = S.forward_backward(p, rec, npan, 3.2, 3.2, DEPTH, ncry, rounding=False, pitch=pitch,
+                                    crystal_ny=ny)
+    assert np.isfinite(loss) and loss > 0
+    lay, _, _ = S.offsets(npan)
+    w4, b4 = lay[-1]
+    eps = 1e-6
+    for col in (2, 15, 32 + 3, 32 + 15, S.CRY + 7, S.CRY + 32 + 11):
+        q = p.copy()
+        q[b4 + col] += eps
+        lp = S.forward_backward(q, rec, npan, 3.2, 3.2, DEPTH, ncry, rounding=False, pitch=pitch, crystal_ny=ny)[0]
+        q[b4 + col] -= 2 * eps
+        lm = S.forward_backward(q, rec, npan, 3.2, 3.2, DEPTH, ncry, rounding=False, pitch=pitch, crystal_ny=ny)[0]
+        fd = (lp - lm) / (2 * eps)
+        assert abs(fd - g[b4 + col]) <= 1e-6 + 1e-4 * abs(fd), (col, fd, g[b4 + col])
+    unused = [c for s in (0, S.CRY) for c in list(range(s + 16, s + 32)) + list(range(s + 48, s + 64))]
+    assert not g[[b4 + c for c in unused]].any()
