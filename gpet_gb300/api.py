@@ -110,6 +110,8 @@ def load_library(path=None):
     L.gpet_surrogate_forward.argtypes = [vp, vp, i64, vp]
     L.gpet_surrogate_train.argtypes = [vp, vp, i64, i32, i32, C.c_float, C.c_uint64, vp]
     L.gpet_surrogate_calibrate.argtypes = [vp, vp, i64, i32, C.POINTER(C.c_float)]
+    L.gpet_surrogate_get_cell_weights.argtypes = [vp, vp, i64]
+    L.gpet_surrogate_set_cell_weights.argtypes = [vp, vp, i64]
     L.gpet_set_surrogate.argtypes = [vp, vp]
     L.gpet_umma_selftest.argtypes = [C.c_int, vp, vp, i32, i32, vp]
     L.gpet_digitize.argtypes = [vp, vp, vp, vp, i64, C.POINTER(RunStats)]
@@ -430,6 +432,16 @@ class Surrogate:
         self._ck(self.L.gpet_surrogate_forward(self.h, _ptr(rec), len(rec), _ptr(out)))
         return out
 
+    def cell_weights(self):
+        """Factorised head: the (energy class, row, column) cell weights [2, 32, 32]."""
+        w = np.zeros(2048, np.float32)
+        self._ck(self.L.gpet_surrogate_get_cell_weights(self.h, _ptr(w), 2048))
+        return w.reshape(2, 32, 32)
+
+    def set_cell_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32).reshape(-1)
+        self._ck(self.L.gpet_surrogate_set_cell_weights(self.h, _ptr(w), len(w)))
+
     def calibrate(self, rec, iters=3):
         """Match the expected (energy class, crystal) and energy-bin counts of
         the records in the current domain (gpet_surrogate_calibrate); returns
@@ -446,7 +458,8 @@ class Surrogate:
         """Write the parameters for inference: the weight matrices rounded to
         bf16 (the precision the tensor-core forward uses, so inference is
         unchanged) as 16-bit patterns, biases and the panel embedding in
-        float32, the validated domain (e_lo, e_hi, margin) and `meta`."""
+        float32, the cell weights of a factorised head, the validated domain
+        (e_lo, e_hi, margin) and `meta`."""
         p = self.params()
         w_bits, rest, off = [], [], 0
         for fin, fout in self.LAYERS:
@@ -457,7 +470,7 @@ class Surrogate:
             off += fout
         np.savez_compressed(path, weights_bf16=np.concatenate(w_bits), biases=np.concatenate(rest),
                             embedding=p[off:], domain=np.array(domain, np.float32),
-                            meta=np.array(repr(meta)))
+                            cell_weights=self.cell_weights(), meta=np.array(repr(meta)))
 
     def load(self, path):
         """Set the parameters and domain saved by save(); returns its meta."""
@@ -474,6 +487,8 @@ class Surrogate:
         self.set_params(np.concatenate(parts).astype(np.float32))
         d = z["domain"]
         self.set_domain(float(d[0]), float(d[1]), float(d[2]))
+        if "cell_weights" in z.files:
+            self.set_cell_weights(z["cell_weights"])
         return ast.literal_eval(str(z["meta"]))
 
     def train(self, rec, epochs=1, batch=8192, lr=1e-3, seed=7):

@@ -275,10 +275,12 @@ __device__ __forceinline__ int softmax_draw(float (&v)[N], int n, float u)
 }
 
 // crystal of set `set` (columns [64 set, 64 set + 64)): one softmax over the
-// ncry crystals, or (fact) a row from the first 32 columns (ny rows, uniform
-// uc) and a column from the last 32 (nz columns, uniform uc2)
+// ncry crystals, or (fact) from the joint of a row softmax (the first 32
+// columns, ny rows) and a column softmax (the last 32, nz columns) weighted
+// per cell by W[row * 32 + column]: the row first (uniform uc) from its
+// marginal, then the column given the row (uc2)
 __device__ __forceinline__ int sample_crystal(uint32_t taddr, const float* hb, int set, int ncry, int fact, int ny,
-                                              int nz, float uc, float uc2)
+                                              int nz, const float* __restrict__ W, float uc, float uc2)
 {
     using namespace sg;
     const int c0 = kCry * set;
@@ -288,13 +290,66 @@ __device__ __forceinline__ int sample_crystal(uint32_t taddr, const float* hb, i
     umma::tmem_wait_ld();
     if (fact) {
         float r[32], c[32];
+        float mr = -1e30f, mc = -1e30f;
 #pragma unroll
         for (int k = 0; k < 32; ++k) {
             r[k] = __uint_as_float(a[k]) + hb[c0 + k];
             c[k] = __uint_as_float(b[k]) + hb[c0 + 32 + k];
+            if (k < ny) mr = fmaxf(mr, r[k]);
+            if (k < nz) mc = fmaxf(mc, c[k]);
         }
-        const int ly = softmax_draw(r, ny, uc);
-        const int lz = softmax_draw(c, nz, uc2);
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+            c[k] = k < nz ? __expf(c[k] - mc) : 0.0f;
+            r[k] = k < ny ? __expf(r[k] - mr) : 0.0f;
+        }
+        const float* w = W + set * 1024;
+        // row marginal: p(row) sum over columns of p(column) W
+        float tot = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+            if (k < ny) {
+                float srow = 0.0f;
+                for (int j = 0; j < nz; ++j) srow = fmaf(c[j], __ldg(w + k * 32 + j), srow);
+                r[k] *= srow;
+                tot += r[k];
+            }
+        }
+        int ly = ny - 1;
+        {
+            const float target = uc * tot;
+            float acc = 0.0f;
+            bool found = false;
+#pragma unroll
+            for (int k = 0; k < 32; ++k) {
+                if (k < ny && !found) {
+                    acc += r[k];
+                    if (acc >= target) { ly = k; found = true; }
+                }
+            }
+        }
+        // the column given the row
+        float ct = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+            if (k < nz) {
+                c[k] *= __ldg(w + ly * 32 + k);
+                ct += c[k];
+            }
+        }
+        int lz = nz - 1;
+        {
+            const float target = uc2 * ct;
+            float acc = 0.0f;
+            bool found = false;
+#pragma unroll
+            for (int k = 0; k < 32; ++k) {
+                if (k < nz && !found) {
+                    acc += c[k];
+                    if (acc >= target) { lz = k; found = true; }
+                }
+            }
+        }
         return ly + ny * lz;
     }
     float e[kCry];
@@ -606,7 +661,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd(SurrogateDev sd, Fwd
                 st_next(st);
                 const float uc2 = st_u(st);
                 s_cry[cq >> 1][rloc] = sample_crystal(taddr, hb, cq >> 1, sd.crystalN, sd.fact, sd.crystalNy,
-                                                      sd.crystalNz, uc, uc2);
+                                                      sd.crystalNz, sd.corr, uc, uc2);
             } else {
                 const float zn = st_normal(st);
                 s_depth[rloc] = sample_depth(taddr, hb, um, zn);
@@ -858,10 +913,8 @@ __global__ void k_gather_records(const EntryRec* __restrict__ all, const uint32_
 // belongs to neither) times the class's crystal probability — and
 // acc[2 * kCry + bin] of each energy bin. One warp per record, two bins and
 // two crystals per lane.
-// fact: acc[set * kCry + row] and acc[set * kCry + 32 + column] of the
-// factorised head's row and column softmaxes instead.
 __global__ void __launch_bounds__(256) k_calib_accum(const float* __restrict__ out, int64_t n, int crystalN,
-                                                     int fact, int ny, int nz, double* acc)
+                                                     double* acc)
 {
     using namespace sg;
     const int lane = threadIdx.x & 31;
@@ -889,26 +942,6 @@ __global__ void __launch_bounds__(256) k_calib_accum(const float* __restrict__ o
 #pragma unroll
         for (int set = 0; set < 2; ++set) {
             const float* l = o + set * kCry;
-            if (fact) {
-                // rows in the first 32 columns, columns in the last 32
-                const bool v0 = lane < ny, v1 = lane < nz;
-                const float l0 = v0 ? l[lane] : -1e30f, l1 = v1 ? l[32 + lane] : -1e30f;
-                float m0 = l0, m1 = l1;
-                for (int d = 16; d > 0; d >>= 1) {
-                    m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, d));
-                    m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, d));
-                }
-                const float y0 = v0 ? expf(l0 - m0) : 0.0f, y1 = v1 ? expf(l1 - m1) : 0.0f;
-                float t0 = y0, t1 = y1;
-                for (int d = 16; d > 0; d >>= 1) {
-                    t0 += __shfl_xor_sync(0xffffffffu, t0, d);
-                    t1 += __shfl_xor_sync(0xffffffffu, t1, d);
-                }
-                const float w = (set ? c1 : c0) / s;
-                a[set][0] += w * y0 / t0;
-                a[set][1] += w * y1 / t1;
-                continue;
-            }
             const bool v0 = lane < crystalN, v1 = 32 + lane < crystalN;
             const float l0 = v0 ? l[lane] : -1e30f, l1 = v1 ? l[32 + lane] : -1e30f;
             float m2 = fmaxf(l0, l1);
@@ -928,6 +961,78 @@ __global__ void __launch_bounds__(256) k_calib_accum(const float* __restrict__ o
     }
     atomicAdd(&acc[2 * kCry + lane], (double)ea[0]);
     atomicAdd(&acc[2 * kCry + 32 + lane], (double)ea[1]);
+}
+
+// expected counts of a batch under a factorised head: acc[set * 1024 + row *
+// 32 + column] of each (energy class, row, column) cell — the class
+// probability times the cell's share of the class's joint, p(row) p(column)
+// W[set][row][column] normalised — and acc[2048 + bin] of each energy bin.
+// One warp per record; lane j holds column j and sums over the rows.
+__global__ void __launch_bounds__(256) k_calib_accum_grid(const float* __restrict__ out, int64_t n, int ny, int nz,
+                                                          const float* __restrict__ W, double* acc)
+{
+    using namespace sg;
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    float a[2][32];
+#pragma unroll
+    for (int set = 0; set < 2; ++set)
+#pragma unroll
+        for (int k = 0; k < 32; ++k) a[set][k] = 0.0f;
+    float ea[2] = {0.0f, 0.0f};
+    for (int64_t i = w0; i < n; i += nw) {
+        const float* o = out + i * kOut;
+        const float e0 = o[kColE + lane], e1 = o[kColE + 32 + lane];
+        float mx = fmaxf(e0, e1);
+        for (int d = 16; d > 0; d >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, d));
+        const float x0 = expf(e0 - mx), x1 = expf(e1 - mx);
+        const int b0 = lane, b1 = 32 + lane;
+        float s = x0 + x1;
+        float c0 = (b0 >= 1 && b0 < kClassBin ? x0 : 0.0f) + (b1 >= 1 && b1 < kClassBin ? x1 : 0.0f);
+        float c1 = (b0 >= kClassBin ? x0 : 0.0f) + (b1 >= kClassBin ? x1 : 0.0f);
+        for (int d = 16; d > 0; d >>= 1) {
+            s += __shfl_xor_sync(0xffffffffu, s, d);
+            c0 += __shfl_xor_sync(0xffffffffu, c0, d);
+            c1 += __shfl_xor_sync(0xffffffffu, c1, d);
+        }
+        ea[0] += x0 / s;
+        ea[1] += x1 / s;
+#pragma unroll
+        for (int set = 0; set < 2; ++set) {
+            const float* l = o + set * kCry;
+            const bool vr = lane < ny, vc = lane < nz;
+            const float lr = vr ? l[lane] : -1e30f, lc = vc ? l[32 + lane] : -1e30f;
+            float mr = lr, mc = lc;
+            for (int d = 16; d > 0; d >>= 1) {
+                mr = fmaxf(mr, __shfl_xor_sync(0xffffffffu, mr, d));
+                mc = fmaxf(mc, __shfl_xor_sync(0xffffffffu, mc, d));
+            }
+            const float pr = vr ? expf(lr - mr) : 0.0f;   // this lane's row weight
+            const float pc = vc ? expf(lc - mc) : 0.0f;   // this lane's column weight
+            const float* w = W + set * 1024;
+            // cell (row k, column lane): p(row k) p(column lane) W
+            float cell[32];
+            float part = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 32; ++k) {
+                const float prk = __shfl_sync(0xffffffffu, pr, k);
+                cell[k] = (k < ny && vc) ? prk * pc * __ldg(w + k * 32 + lane) : 0.0f;
+                part += cell[k];
+            }
+            for (int d = 16; d > 0; d >>= 1) part += __shfl_xor_sync(0xffffffffu, part, d);
+            const float f = (set ? c1 : c0) / (s * part);
+#pragma unroll
+            for (int k = 0; k < 32; ++k) a[set][k] += f * cell[k];
+        }
+    }
+#pragma unroll
+    for (int set = 0; set < 2; ++set)
+#pragma unroll
+        for (int k = 0; k < 32; ++k)
+            if (k < ny && lane < nz) atomicAdd(&acc[set * 1024 + k * 32 + lane], (double)a[set][k]);
+    atomicAdd(&acc[2048 + lane], (double)ea[0]);
+    atomicAdd(&acc[2048 + 32 + lane], (double)ea[1]);
 }
 
 // dZ = dH * SiLU'(Z), in place on dH
@@ -1144,6 +1249,7 @@ struct gpet_surrogate {
     // training set on the device and the epoch's visiting order
     Buf all, perm, epoch_loss;
     Buf calib;   // expected (energy class, crystal) counts of a calibration pass
+    Buf corr;    // factorised head: cell weights [2][32][32] (1 until calibrated)
 };
 
 namespace {
@@ -1179,6 +1285,7 @@ SurrogateDev make_view(const gpet_surrogate* s)
     d.crystalNy = g.crystalNy;
     d.fact = g.crystalN > sg::kCry ? 1 : 0;
     d.crystalNz = g.crystalNy > 0 ? g.crystalN / g.crystalNy : 0;
+    d.corr = s->corr.as<float>();
     d.rdepth = g.rdepth;
     d.rpolicy = g.rpolicy;
     d.moduleN = g.moduleN;
@@ -1412,9 +1519,12 @@ int gpet_surrogate_create(gpet_ctx* ctx, uint64_t seed, gpet_surrogate** out)
     if (s->params.ensure((size_t)s->nparam * 4) || s->grads.ensure((size_t)s->nparam * 4) ||
         s->adam_m.ensure((size_t)s->nparam * 4) || s->adam_v.ensure((size_t)s->nparam * 4) ||
         s->wrow.ensure((size_t)s->nparam * 2) || s->img.ensure(sg::kImgBytes) ||
-        s->panel_ok_d.ensure((size_t)g.npanels) || s->errflag.ensure(4) || s->loss.ensure(4))
+        s->panel_ok_d.ensure((size_t)g.npanels) || s->errflag.ensure(4) || s->loss.ensure(4) ||
+        s->corr.ensure(2048 * 4))
         rc = GPET_ERR_CUDA;
     if (!rc) {
+        const std::vector<float> ones(2048, 1.0f);
+        cudaMemcpy(s->corr.p, ones.data(), ones.size() * 4, cudaMemcpyHostToDevice);
         cudaMemcpy(s->params.p, p.data(), p.size() * 4, cudaMemcpyHostToDevice);
         cudaMemset(s->adam_m.p, 0, (size_t)s->nparam * 4);
         cudaMemset(s->adam_v.p, 0, (size_t)s->nparam * 4);
@@ -1461,6 +1571,24 @@ int gpet_surrogate_set_params(gpet_surrogate* s, const float* in, int64_t n)
     int rc = refresh_weights(s);
     if (rc) return rc;
     SCK(cudaStreamSynchronize(s->stream));
+    return GPET_OK;
+}
+
+int gpet_surrogate_get_cell_weights(gpet_surrogate* s, float* out, int64_t n)
+{
+    if (!s || !out || n != 2048) return GPET_ERR_ARG;
+    SCK(cudaSetDevice(s->device));
+    SCK(cudaMemcpy(out, s->corr.p, 2048 * 4, cudaMemcpyDeviceToHost));
+    return GPET_OK;
+}
+
+int gpet_surrogate_set_cell_weights(gpet_surrogate* s, const float* in, int64_t n)
+{
+    if (!s || !in || n != 2048) return GPET_ERR_ARG;
+    for (int64_t i = 0; i < n; ++i)
+        if (!(in[i] >= 0.0f) || !std::isfinite(in[i])) return sfail(s, GPET_ERR_ARG, "cell weights must be finite, >= 0");
+    SCK(cudaSetDevice(s->device));
+    SCK(cudaMemcpy(s->corr.p, in, 2048 * 4, cudaMemcpyHostToDevice));
     return GPET_OK;
 }
 
@@ -1575,7 +1703,10 @@ int gpet_surrogate_calibrate(gpet_surrogate* s, const gpet_entry* rec, int64_t n
     // the records of the surrogate's domain (the test of k_route) and their
     // observed (energy class, crystal) and energy-bin counts, the bin as in
     // training (0: no pulse)
-    constexpr int kAcc = 2 * kCry + kBins;
+    // joint head: (class, crystal) cells then the bins; factorised head: the
+    // 2 x 32 x 32 (class, row, column) cells then the bins
+    const int ebin0 = sd.fact ? 2048 : 2 * kCry;
+    const int kAcc = ebin0 + kBins;
     const EntryRec* r = reinterpret_cast<const EntryRec*>(rec);
     std::vector<EntryRec> dom;
     std::vector<double> obs(kAcc, 0.0);
@@ -1590,17 +1721,15 @@ int gpet_surrogate_calibrate(gpet_surrogate* s, const gpet_entry* rec, int64_t n
         if (e.crystal >= 0 && e.Edep > 0.0f) {
             b = (int)(e.Edep / e.E * (float)kBins);
             b = b < 1 ? 1 : (b > kBins - 1 ? kBins - 1 : b);
-            const size_t c0 = b >= kClassBin ? kCry : 0;
+            const int set = b >= kClassBin ? 1 : 0;
             if (e.crystal < ncry) {
-                if (sd.fact) {
-                    obs[c0 + (size_t)(e.crystal % sd.crystalNy)] += 1.0;
-                    obs[c0 + 32 + (size_t)(e.crystal / sd.crystalNy)] += 1.0;
-                } else {
-                    obs[c0 + (size_t)e.crystal] += 1.0;
-                }
+                if (sd.fact)
+                    obs[(size_t)(set * 1024 + (e.crystal % sd.crystalNy) * 32 + e.crystal / sd.crystalNy)] += 1.0;
+                else
+                    obs[(size_t)(set * kCry + e.crystal)] += 1.0;
             }
         }
-        obs[(size_t)(2 * kCry + b)] += 1.0;
+        obs[(size_t)(ebin0 + b)] += 1.0;
     }
     const int64_t m = (int64_t)dom.size();
     if (m == 0) return sfail(s, GPET_ERR_ARG, "no record in the surrogate's domain");
@@ -1628,8 +1757,12 @@ int gpet_surrogate_calibrate(gpet_surrogate* s, const gpet_entry* rec, int64_t n
             FwdInfer in{};
             k_mlp_fwd<true><<<grid_cap(nb, 128, 152), kFwdThreads, smem, s->stream>>>(sd, tr, in,
                                                                                      s->errflag.as<int>());
-            k_calib_accum<<<(unsigned)std::min<int64_t>((nb + 7) / 8, 152 * 8), 256, 0, s->stream>>>(
-                s->out.as<float>(), nb, ncry, sd.fact, sd.crystalNy, sd.crystalNz, s->calib.as<double>());
+            if (sd.fact)
+                k_calib_accum_grid<<<(unsigned)std::min<int64_t>((nb + 7) / 8, 152 * 8), 256, 0, s->stream>>>(
+                    s->out.as<float>(), nb, sd.crystalNy, sd.crystalNz, sd.corr, s->calib.as<double>());
+            else
+                k_calib_accum<<<(unsigned)std::min<int64_t>((nb + 7) / 8, 152 * 8), 256, 0, s->stream>>>(
+                    s->out.as<float>(), nb, ncry, s->calib.as<double>());
             SCK(cudaGetLastError());
         }
         std::vector<double> expd(kAcc);
@@ -1641,25 +1774,34 @@ int gpet_surrogate_calibrate(gpet_surrogate* s, const gpet_entry* rec, int64_t n
         SCK(cudaMemcpyAsync(&herr, s->errflag.p, 4, cudaMemcpyDeviceToHost, s->stream));
         SCK(cudaStreamSynchronize(s->stream));
         if (herr) return sfail(s, GPET_ERR_CUDA, "a tensor-core wait gave up");
-        // the crystal logits of each class and the energy-bin logits move by
-        // log(observed / expected)
+        // the crystal logits of each class (factorised head: the cell
+        // weights) and the energy-bin logits move by log(observed / expected)
         last = 0.0f;
-        auto nudge = [&](size_t j, size_t col) {
-            if (!(obs[j] > 0.0) || !(expd[j] > 0.0)) return;
-            const float d = (float)std::log(obs[j] / expd[j]);
-            bias[col] += d;
-            last = std::max(last, std::fabs(d));
+        auto ratio = [&](size_t j, float* d) {
+            if (!(obs[j] > 0.0) || !(expd[j] > 0.0)) return false;
+            *d = (float)std::log(obs[j] / expd[j]);
+            last = std::max(last, std::fabs(*d));
+            return true;
         };
-        for (int set = 0; set < 2; ++set) {
-            if (sd.fact) {
-                for (int k = 0; k < sd.crystalNy; ++k) nudge((size_t)(set * kCry + k), (size_t)(set * kCry + k));
-                for (int k = 0; k < sd.crystalNz; ++k)
-                    nudge((size_t)(set * kCry + 32 + k), (size_t)(set * kCry + 32 + k));
-            } else {
-                for (int k = 0; k < ncry; ++k) nudge((size_t)(set * kCry + k), (size_t)(set * kCry + k));
-            }
+        float d = 0.0f;
+        if (sd.fact) {
+            std::vector<float> w(2048);
+            SCK(cudaMemcpyAsync(w.data(), s->corr.p, w.size() * 4, cudaMemcpyDeviceToHost, s->stream));
+            SCK(cudaStreamSynchronize(s->stream));
+            for (int set = 0; set < 2; ++set)
+                for (int ky = 0; ky < sd.crystalNy; ++ky)
+                    for (int kz = 0; kz < sd.crystalNz; ++kz) {
+                        const size_t j = (size_t)(set * 1024 + ky * 32 + kz);
+                        if (ratio(j, &d)) w[j] *= std::exp(d);
+                    }
+            SCK(cudaMemcpyAsync(s->corr.p, w.data(), w.size() * 4, cudaMemcpyHostToDevice, s->stream));
+        } else {
+            for (int set = 0; set < 2; ++set)
+                for (int k = 0; k < ncry; ++k)
+                    if (ratio((size_t)(set * kCry + k), &d)) bias[(size_t)(set * kCry + k)] += d;
         }
-        for (int b = 0; b < kBins; ++b) nudge((size_t)(2 * kCry + b), (size_t)(kColE + b));
+        for (int b = 0; b < kBins; ++b)
+            if (ratio((size_t)(ebin0 + b), &d)) bias[(size_t)(kColE + b)] += d;
         SCK(cudaMemcpyAsync(pb, bias.data(), bias.size() * 4, cudaMemcpyHostToDevice, s->stream));
         rc = refresh_weights(s);
         if (rc) return rc;

@@ -36,6 +36,10 @@ struct SurrogateDev {
     // 1 a row softmax (columns [0, 32) of the set) and a column softmax
     // ([32, 64)), for grids of up to 32 x 32 crystals
     int32_t fact, crystalNz;
+    // factorised head: multiplicative weights of each (energy class, row,
+    // column) cell on the product of the row and column probabilities,
+    // [2][32][32], fitted by the calibration (1 before it)
+    const float* corr;
     float cry_pitch_y, cry_pitch_z, cry_y, cry_z;   // crystal pitch and size in y, z (module 0)
 };
 

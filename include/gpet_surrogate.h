@@ -72,13 +72,21 @@ int gpet_surrogate_forward(gpet_surrogate* s, const gpet_entry* rec, int64_t n, 
 int gpet_surrogate_train(gpet_surrogate* s, const gpet_entry* rec, int64_t n, int32_t epochs, int32_t batch,
                          float lr, uint64_t seed, float* epoch_loss);
 /* Calibration on the records of the surrogate's current domain: `iters`
- * passes each move the biases of the crystal logits of each energy class and
- * of the energy-bin logits by log(observed / expected) of that (class,
- * crystal) or energy-bin count over the records, so that the model's expected
+ * passes each move the biases of the crystal logits of each energy class
+ * (factorised head: the cell weights of each (class, row, column)) and of the
+ * energy-bin logits by log(observed / expected) of that (class, crystal) or
+ * energy-bin count over the records, so that the model's expected
  * counts match the Monte Carlo ones (iterative proportional fitting; the
  * other parameters stay). *max_adjust (may be NULL) receives the last pass's
  * largest |log ratio|. Call after gpet_surrogate_set_domain. */
 int gpet_surrogate_calibrate(gpet_surrogate* s, const gpet_entry* rec, int64_t n, int32_t iters, float* max_adjust);
+/* Factorised head only: the weight of each (energy class, row, column) cell
+ * on the product of the row and column probabilities, float[2][32][32]
+ * (class, row, column; n = 2048), 1 after create, fitted by
+ * gpet_surrogate_calibrate so that the model's expected (class, crystal)
+ * counts match the records'. Saved and restored beside the parameters. */
+int gpet_surrogate_get_cell_weights(gpet_surrogate* s, float* out, int64_t n);
+int gpet_surrogate_set_cell_weights(gpet_surrogate* s, const float* in, int64_t n);
 /* Use (s) or stop using (NULL) the surrogate in this context's runs; s must
  * outlive its use. Its photons produce pulses but no hits. */
 int gpet_set_surrogate(gpet_ctx* ctx, gpet_surrogate* s);
