@@ -474,10 +474,16 @@ def _three_arms(ctxs, seeds, sur, steps, warmup, ncry):
     }
 
 
+SURROGATE_ARCH = ("16 inputs (entry y, z; direction; E; 6-wide panel embedding; 4 in-crystal offsets) -> "
+                  "4 x 256 SiLU -> 204 outputs (two crystal sets of 64 logits by energy class, factorised into "
+                  "32 row + 32 column logits above 64 crystals; MoG-4 depth; 64 energy bins); BASELINE's "
+                  "surrogate configuration names 14 inputs with an 8-wide embedding and 140 outputs")
+
+
 def _model_meta(path, meta, domain="entry energy 100-520 keV, >= 3 mm inside the panel edges, all panels"):
-    return {"file": os.path.relpath(path, ROOT), "train_records": meta.get("train_records"),
-            "epochs": meta.get("train", {}).get("epochs"), "calibration_records": meta.get("calibration_records"),
-            "domain": domain}
+    return {"file": os.path.relpath(path, ROOT), "architecture": SURROGATE_ARCH,
+            "train_records": meta.get("train_records"), "epochs": meta.get("train", {}).get("epochs"),
+            "calibration_records": meta.get("calibration_records"), "domain": domain}
 
 
 def measure_surrogate_batched(steps, warmup, model_path=SURROGATE_MODEL):
