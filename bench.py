@@ -12,7 +12,8 @@ Workload (one step = one full acquisition, simulated and digitized):
 Prints one JSON line (rank 0). `value` = coincidences / device time with the
 scene resident on the GPU (CUDA events on the library's stream); `e2e` = the
 same metric through the C ABI with host buffers (phantom upload, run, singles
-and coincidence copy-out) timed on the host clock. `surrogate_batched` = the
+and coincidence copy-out, the copy-out of one step overlapping the next step)
+timed on the host clock. `surrogate_batched` = the
 metric's second form: 64 uneven simulations batched in one job with the
 learned detector response (committed model), against the plain form (each
 simulation its own plain Monte Carlo run) and plain batched, with the
@@ -254,6 +255,7 @@ def run_ours(args):
         # decays per k_source / k_phantom launch of this run
         sub_decays = int(tuning["sub_decays"]) if tuning else int(args.set.get("sub_decays", SUB_DECAYS))
         for w in range(args.warmup):
+            flush.zero_()
             ctx.set_option("seed", 1000 + w)
             ctx.run()
         sampler = ClockSampler(local)
@@ -304,23 +306,60 @@ def run_ours(args):
         den[...] = den0
         cap_s = int(2 * tot["singles"] / max(1, args.steps)) + 1024
         cap_c = int(2 * tot["coinc"] / max(1, args.steps)) + 1024
-        out_s = (pinned((cap_s,), F.EVENT_DTYPE), pinned((cap_s,), np.uint8))
-        out_c = (pinned((cap_c, 2), np.int64), pinned((cap_c,), np.uint8))
+        # two sets of host buffers: a step's records are copied (on the
+        # library's copy stream) while the next step's phantom upload and run
+        # proceed, and read on the host once the next run has returned
+        outs = [((pinned((cap_s,), F.EVENT_DTYPE), pinned((cap_s,), np.uint8)),
+                 (pinned((cap_c, 2), np.int64), pinned((cap_c,), np.uint8))) for _ in range(2)]
         e2e_steps = max(2, args.steps // 2) if args.e2e_steps < 0 else args.e2e_steps
+
+        def host_read(singles, pairs):
+            # the step's result read on the host: time order of its first and
+            # last single, its last pair's indices within the singles
+            ok = len(singles) == 0 or singles["t"][-1] >= singles["t"][0]
+            return ok and (len(pairs) == 0 or int(pairs[-1].max()) < len(singles))
+
+        # one untimed step first: the library's staging buffers and copy
+        # stream are set up there, as in a stream of acquisitions
+        if e2e_steps > 0:
+            ctx.set_option("seed", 776)
+            ctx.set_phantom(mat, den, cfg.pdim, cfg.poffset, cfg.psize)
+            ctx.run()
+            ctx.singles_async(outs[1][0])
+            ctx.coincidences_async(outs[1][1])
+            ctx.wait_copies()
         barrier()
         t0 = time.perf_counter()
-        e_coinc, h2d, d2h = 0, 0, 0
+        e_coinc, h2d, d2h, e_ok, pend = 0, 0, 0, True, None
+        e_host = {"set_phantom": 0.0, "gpet_run": 0.0, "wait_and_read": 0.0, "singles_async": 0.0,
+                  "coincidences_async": 0.0}
         for k in range(e2e_steps):
+            ta = time.perf_counter()
             ctx.set_option("seed", 777 + k)
             ctx.set_phantom(mat, den, cfg.pdim, cfg.poffset, cfg.psize)
+            tb = time.perf_counter()
             st = ctx.run()
-            singles, scat = ctx.singles(out=out_s)
-            pairs, cls = ctx.coincidences(out=out_c)
+            tc = time.perf_counter()
+            ctx.wait_copies()
+            if pend is not None:
+                e_ok = e_ok and host_read(*pend)
+            td = time.perf_counter()
+            singles, scat = ctx.singles_async(outs[k % 2][0])
+            te = time.perf_counter()
+            pairs, cls = ctx.coincidences_async(outs[k % 2][1])
+            tf = time.perf_counter()
+            for key, dt in zip(e_host, (tb - ta, tc - tb, td - tc, te - td, tf - te)):
+                e_host[key] += dt
+            pend = (singles, pairs)
             e_coinc += len(pairs)
             h2d += mat.nbytes + den.nbytes
             d2h += singles.nbytes + scat.nbytes + pairs.nbytes + cls.nbytes
+        ctx.wait_copies()
+        e_ok = e_ok and (pend is None or host_read(*pend))
         barrier()
         e_wall = time.perf_counter() - t0
+        if not e_ok:
+            raise RuntimeError("end-to-end results read back inconsistent")
         ctx.close()
     if rank != 0:
         if dist:
@@ -356,7 +395,12 @@ def run_ours(args):
                      "note": "issue/latency-bound (RNG, transcendental math, dependent L2 gathers); "
                              "HBM per the path's byte model"},
         "e2e": {"value": e_coinc / e_wall, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
-                "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps} if e2e_steps > 0 else None,
+                "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps,
+                "host_ms_per_step": {k: 1e3 * v / e2e_steps for k, v in e_host.items()},
+                "copies": "each step's singles and coincidences are gathered on the device and copied into "
+                          "pinned host memory on the library's copy stream while the next step's phantom "
+                          "upload and run proceed (gpet_get_*_async); the timed region ends after the last "
+                          "step's copies have landed"} if e2e_steps > 0 else None,
         "clocks": clocks,
         "wall_s_timed_region": wall,
         # host clock per step: the L2 flush (512 MB write + sync) and gpet_run

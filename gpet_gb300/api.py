@@ -118,6 +118,9 @@ def load_library(path=None):
     L.gpet_get_singles.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
     L.gpet_get_pulses.argtypes = [vp, vp, vp, vp, i64, C.POINTER(i64)]
     L.gpet_get_coincidences.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
+    L.gpet_get_singles_async.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
+    L.gpet_get_coincidences_async.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
+    L.gpet_wait_copies.argtypes = [vp]
     L.gpet_get_hits.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
     L.gpet_get_exits.argtypes = [vp, vp, i64, C.POINTER(i64)]
     L.gpet_write_outputs.argtypes = [vp, C.c_char_p]
@@ -263,6 +266,35 @@ class Context:
         if n:
             self._ck(self.L.gpet_get_coincidences(self.h, _ptr(pr), _ptr(cl), n, C.byref(m)))
         return pr, cl
+
+    def singles_async(self, out):
+        """As singles(out=...), but the records reach `out` (page-locked
+        arrays, e.g. views of pinned memory, large enough) on the context's
+        copy stream while the next run proceeds: the returned views hold them
+        after wait_copies()."""
+        n = self._count(self.L.gpet_get_singles_async, None, None)
+        if len(out[0]) < n or len(out[1]) < n:
+            raise ValueError("output arrays too small for %d singles" % n)
+        ev, sc = out[0][:n], out[1][:n]
+        m = C.c_int64()
+        if n:
+            self._ck(self.L.gpet_get_singles_async(self.h, _ptr(ev), _ptr(sc), n, C.byref(m)))
+        return ev, sc
+
+    def coincidences_async(self, out):
+        """As coincidences(out=...), asynchronously as singles_async()."""
+        n = self._count(self.L.gpet_get_coincidences_async, None, None)
+        if len(out[0]) < n or len(out[1]) < n:
+            raise ValueError("output arrays too small for %d coincidences" % n)
+        pr, cl = out[0][:n], out[1][:n]
+        m = C.c_int64()
+        if n:
+            self._ck(self.L.gpet_get_coincidences_async(self.h, _ptr(pr), _ptr(cl), n, C.byref(m)))
+        return pr, cl
+
+    def wait_copies(self):
+        """Waits for the copies of singles_async / coincidences_async."""
+        self._ck(self.L.gpet_wait_copies(self.h))
 
     def hits(self):
         n = self._count(self.L.gpet_get_hits, None, None)

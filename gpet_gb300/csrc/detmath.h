@@ -224,10 +224,13 @@ DM_FN double dm_log1p_small(double x)
  * times that are added to a double-precision time stamp once */
 #define DM_INV_SPEED 3.3356409519815204e-05f
 
-/* uniform (0,1) float from 24 random bits: (k + 0.5) 2^-24, exact */
+/* uniform (0,1) float from the top 23 random bits: (k + 1/2) 2^-23, exact
+ * (k + 1/2 < 2^23 fits the 24-bit significand), so never 0 or 1: the values
+ * run from 2^-24 to 1 - 2^-24. (With 24 bits, k + 1/2 would round to an even
+ * integer for k >= 2^23 and k = 2^24 - 1 would give exactly 1.) */
 DM_FN float dm_u01(uint32_t x)
 {
-    return ((float)(x >> 8) + 0.5f) * 5.9604644775390625e-08f;
+    return ((float)(x >> 9) + 0.5f) * 1.1920928955078125e-07f;
 }
 
 /* uniform (0,1) double from 52 random bits: (k + 1/2) 2^-52, made as

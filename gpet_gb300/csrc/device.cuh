@@ -84,12 +84,15 @@ struct SimDesc {
 };
 
 // ------------------------------------------------------------------ RNG
-// Philox4x32-10 (Salmon et al., SC'11). Stream = (key, tag, 64-bit id); the
-// first counter word counts blocks of four 32-bit outputs.
+// A stream is keyed by (key, tag, 64-bit id): its state is the Philox4x32-10
+// block (Salmon et al., SC'11) of counter (0, tag, id) under the key, and its
+// words come from xoshiro128** (Blackman & Vigna, "Scrambled linear
+// pseudorandom number generators", ACM TOMS 2021) run from that state. The
+// counter-based seed keeps every decay's, photon's and pulse's draws
+// independent of which thread takes it and when; the sequential generator
+// costs a fraction of a Philox block per word.
 struct Stream {
-    uint32_t k0, k1, tag, idlo, idhi, blk;
-    uint32_t buf[4];
-    int pos;
+    uint32_t s[4];
 };
 
 __device__ __forceinline__ void philox10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
@@ -106,29 +109,36 @@ __device__ __forceinline__ void philox10(uint32_t c0, uint32_t c1, uint32_t c2, 
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-__device__ __forceinline__ void st_init(Stream& s, uint32_t k0, uint32_t k1, uint32_t tag, uint64_t id)
+// state of stream (key k0 k1, tag, id hi:lo); the all-zero state, which
+// xoshiro never leaves, is replaced by a fixed one
+__device__ __forceinline__ void st_seed(uint32_t (&s)[4], uint32_t k0, uint32_t k1, uint32_t tag, uint32_t idlo,
+                                        uint32_t idhi)
 {
-    s.k0 = k0; s.k1 = k1; s.tag = tag; s.idlo = (uint32_t)id; s.idhi = (uint32_t)(id >> 32);
-    s.blk = 0; s.pos = 4;
+    philox10(0u, tag, idlo, idhi, k0, k1, s);
+    if ((s[0] | s[1] | s[2] | s[3]) == 0u) s[0] = 0x9E3779B9u;
 }
 
-__device__ __forceinline__ uint32_t st_next(Stream& s)
+// next word of xoshiro128**: rotl(s1 * 5, 7) * 9, then the linear step
+__device__ __forceinline__ uint32_t xo_next(uint32_t (&s)[4])
 {
-    if (s.pos == 4) {
-        philox10(s.blk, s.tag, s.idlo, s.idhi, s.k0, s.k1, s.buf);
-        s.blk++;
-        s.pos = 0;
-    }
-    uint32_t v;
-    switch (s.pos) {              // keeps buf in registers
-    case 0: v = s.buf[0]; break;
-    case 1: v = s.buf[1]; break;
-    case 2: v = s.buf[2]; break;
-    default: v = s.buf[3]; break;
-    }
-    s.pos++;
+    const uint32_t m = s[1] * 5u;
+    const uint32_t v = __funnelshift_l(m, m, 7) * 9u;
+    const uint32_t t = s[1] << 9;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = __funnelshift_l(s[3], s[3], 11);
     return v;
 }
+
+__device__ __forceinline__ void st_init(Stream& s, uint32_t k0, uint32_t k1, uint32_t tag, uint64_t id)
+{
+    st_seed(s.s, k0, k1, tag, (uint32_t)id, (uint32_t)(id >> 32));
+}
+
+__device__ __forceinline__ uint32_t st_next(Stream& s) { return xo_next(s.s); }
 
 __device__ __forceinline__ float st_u(Stream& s) { return dm_u01(st_next(s)); }
 

@@ -717,9 +717,10 @@ __global__ void k_gather_events(PulseDev P, const uint32_t* __restrict__ idx, in
     }
 }
 
-// the same records for a destination in mapped (pinned) host memory: a block
-// builds 256 records in shared memory and stores them as consecutive 16-byte
-// words, so every store that crosses the host link is a whole, aligned word;
+// the same records for a destination in mapped (pinned) host memory or a
+// device buffer: a block builds 256 records in shared memory and stores them
+// as consecutive 16-byte words, so every store (across the host link, or to
+// device memory) is a whole, aligned word and a warp's stores are coalesced;
 // flags[j] = 1 for a record whose photon scattered in the phantom (meta bit 7).
 // out must be 16-byte aligned.
 __global__ void __launch_bounds__(256) k_gather_events_mapped(PulseDev P, const uint32_t* __restrict__ idx, int64_t n,
@@ -755,11 +756,13 @@ __global__ void __launch_bounds__(256) k_gather_events_mapped(PulseDev P, const 
 }
 
 int gather_events_mapped(const PulseDev& P, const uint32_t* idx, int64_t n, const DigiScratch& D, EventRec* out,
-                         uint8_t* flags, cudaStream_t s)
+                         uint8_t* flags, cudaStream_t s, unsigned max_blocks)
 {
     if (n <= 0) return 0;
     if (reinterpret_cast<uintptr_t>(out) & 15) return GPET_ERR_ARG;
-    k_gather_events_mapped<<<grid_for_g(n), 256, 0, s>>>(P, idx, n, D.Eb, D.xb, D.yb, D.zb, D.site,
+    unsigned g = grid_for_g(n);
+    if (max_blocks && g > max_blocks) g = max_blocks;
+    k_gather_events_mapped<<<g, 256, 0, s>>>(P, idx, n, D.Eb, D.xb, D.yb, D.zb, D.site,
                                                          reinterpret_cast<uint4*>(out), flags);
     return cudaGetLastError() == cudaSuccess ? 0 : GPET_ERR_CUDA;
 }

@@ -140,6 +140,14 @@ struct Work {
     }
 };
 
+// device buffers of one kind of result on their way to the caller, and the
+// end of the last copy out of them
+struct Staged {
+    DevBuf a, b;
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+};
+
 struct gpet_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -198,6 +206,12 @@ struct gpet_ctx {
     DevBuf d_mat_stage, d_den_stage, d_maxden;   // phantom upload
     // results of the last run this context took part in
     std::shared_ptr<Work> work;
+    // gpet_get_*_async: results gathered into context-owned device buffers
+    // (one group for singles, one for coincidences) on `stream`, copied to the
+    // caller on `cstream` while the next run proceeds
+    cudaStream_t cstream = nullptr;
+    cudaEvent_t cready = nullptr;
+    Staged st_singles, st_coinc;
     int res_sim = 0;
     PinnedVec<ExitRec> host_exits;       // every photon slot of the run (record_exits)
     std::vector<EntryRec> host_entries;
@@ -314,6 +328,19 @@ __global__ void k_scat_flags(uint8_t* meta, int64_t n)
         meta[i] = (meta[i] & 0x80u) ? 1 : 0;
 }
 
+// coincidences of one simulation, pairs as indices into its own singles, into
+// device or mapped host memory (cls may be null)
+__global__ void k_coinc_out(const int64_t* __restrict__ pairs, const uint8_t* __restrict__ klass, int64_t n,
+                            int64_t soff, int64_t* dst, uint8_t* cls)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const longlong2 v = reinterpret_cast<const longlong2*>(pairs)[i];
+        dst[2 * i] = v.x - soff;
+        dst[2 * i + 1] = v.y - soff;
+        if (cls) cls[i] = klass[i];
+    }
+}
+
 extern "C" {
 
 int gpet_create(int device, gpet_ctx** out)
@@ -338,6 +365,15 @@ int gpet_create(int device, gpet_ctx** out)
         delete c;
         return GPET_ERR_CUDA;
     }
+    if (cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamDestroy(c->stream);
+        cudaStreamDestroy(c->stream2);
+        delete c;
+        return GPET_ERR_CUDA;
+    }
+    cudaEventCreateWithFlags(&c->cready, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->st_singles.done, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c->st_coinc.done, cudaEventDisableTiming);
     *out = c;
     return GPET_OK;
 }
@@ -348,11 +384,15 @@ void gpet_destroy(gpet_ctx* c)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     cudaStreamSynchronize(c->stream2);
+    cudaStreamSynchronize(c->cstream);
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     for (auto& e : c->qev) if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {c->cready, c->st_singles.done, c->st_coinc.done})
+        if (e) cudaEventDestroy(e);
     c->work.reset();
     cudaStreamDestroy(c->stream);
     cudaStreamDestroy(c->stream2);
+    cudaStreamDestroy(c->cstream);
     delete c;
 }
 
@@ -925,6 +965,18 @@ static void fill_stats(const Counters& h, gpet_run_stats* st)
 
 // the leader's Work for a new run: reused unless other contexts still hold
 // results in it
+// stream s waits for the asynchronous copies of c, which read c's results:
+// launches that rewrite those buffers go after them
+static cudaError_t join_copies(gpet_ctx* c, cudaStream_t s)
+{
+    for (Staged* g : {&c->st_singles, &c->st_coinc})
+        if (g->pending) {
+            cudaError_t e = cudaStreamWaitEvent(s, g->done, 0);
+            if (e != cudaSuccess) return e;
+        }
+    return cudaSuccess;
+}
+
 static Work& fresh_work(gpet_ctx* c)
 {
     if (!c->work || c->work.use_count() > 1) c->work = std::make_shared<Work>();
@@ -1124,6 +1176,9 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         smem = std::max(smem, (size_t)cs[s]->geo.npanels * kPanelStride * 4);
     }
     Work& W = fresh_work(c);
+    // the detector stage rewrites the pulses that copies of the last results
+    // may still be reading (the transport before it overlaps those copies)
+    CK(join_copies(c, c->stream2));
     W.nsims = nsim;
     W.n_pulses = W.n_hits = W.n_singles = W.n_coinc = 0;
     W.sim_hits.assign(nsim, 0);
@@ -1448,6 +1503,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     // join the detector stream
     CK(cudaStreamSynchronize(c->stream2));
     CK(cudaGetLastError());
+    CK(join_copies(c, c->stream));
     {
         unsigned long long hp[2] = {0, 0};
         CK(cudaMemcpy(hp, pcount, 16, cudaMemcpyDeviceToHost));
@@ -1687,6 +1743,7 @@ int gpet_digitize(gpet_ctx* c, const gpet_event* ev, const uint8_t* scat, const 
     if (!st) st = &local;
     std::memset(st, 0, sizeof(*st));
     Work& W = fresh_work(c);
+    CK(join_copies(c, c->stream));
     W.nsims = 1;
     W.sim_hits.assign(1, 0);
     int rc = grow_pulses(c, W, std::max<int64_t>(n, 1), 0);
@@ -1807,6 +1864,109 @@ int gpet_get_singles(gpet_ctx* c, gpet_event* buf, uint8_t* scat, int64_t cap, i
         CK(cudaMemcpyAsync(scat, W.g_meta.p, (size_t)*n, cudaMemcpyDeviceToHost, c->stream));
     }
     CK(cudaStreamSynchronize(c->stream));
+    return GPET_OK;
+}
+
+// staging buffer b of group g holding at least n bytes (a growth takes a
+// quarter more, so that runs of slightly varying size do not reallocate, and
+// first waits for the copies in flight, which may still read the old buffer)
+static cudaError_t stage_ensure(gpet_ctx* c, Staged& g, DevBuf& b, size_t n)
+{
+    if (n <= b.bytes && b.p) return cudaSuccess;
+    if (g.pending) {
+        cudaError_t e = cudaStreamSynchronize(c->cstream);
+        if (e != cudaSuccess) return e;
+        c->st_singles.pending = c->st_coinc.pending = false;
+    }
+    return b.ensure(n + n / 4);
+}
+
+// blocks of the kernels of the asynchronous copies: they run beside the next
+// run's kernels and are bound by the host link, not by the SMs
+constexpr unsigned kCopyBlocks = 64;
+
+// the copy stream starts after everything enqueued on the main stream so far
+// (the run whose results are copied)
+static cudaError_t copies_after_main(gpet_ctx* c)
+{
+    cudaError_t e = cudaEventRecord(c->cready, c->stream);
+    return e == cudaSuccess ? cudaStreamWaitEvent(c->cstream, c->cready, 0) : e;
+}
+
+int gpet_get_singles_async(gpet_ctx* c, gpet_event* buf, uint8_t* scat, int64_t cap, int64_t* n)
+{
+    if (!c || !n) return GPET_ERR_ARG;
+    if (!results(c)) { *n = 0; return GPET_OK; }
+    Work& W = *c->work;
+    const int64_t off = W.s_off[c->res_sim];
+    *n = W.s_off[c->res_sim + 1] - off;
+    if (!buf || *n == 0) return GPET_OK;
+    if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the singles");
+    Staged& g = c->st_singles;
+    const PulseDev P = pulse_view(W);
+    void* dbuf = mapped_host(buf);
+    void* dscat = mapped_host(scat);
+    CK(copies_after_main(c));
+    if (dbuf && !(reinterpret_cast<uintptr_t>(dbuf) & 15) && (!scat || dscat)) {
+        // pinned caller memory: the tile-staged gather stores the records there
+        // itself, across the host link, on the copy stream
+        if (gather_events_mapped(P, W.dg.single_idx + off, *n, W.dg, static_cast<EventRec*>(dbuf),
+                                 static_cast<uint8_t*>(dscat), c->cstream, kCopyBlocks))
+            return fail(c, GPET_ERR_CUDA, "gather of event records failed");
+    } else {
+        // otherwise gathered into the context's device buffers and copied
+        CK(stage_ensure(c, g, g.a, (size_t)*n * sizeof(EventRec)));
+        CK(stage_ensure(c, g, g.b, (size_t)*n));
+        if (gather_events_mapped(P, W.dg.single_idx + off, *n, W.dg, g.a.as<EventRec>(),
+                                 scat ? g.b.as<uint8_t>() : nullptr, c->cstream, kCopyBlocks))
+            return fail(c, GPET_ERR_CUDA, "gather of event records failed");
+        CK(cudaMemcpyAsync(buf, g.a.p, (size_t)*n * sizeof(EventRec), cudaMemcpyDeviceToHost, c->cstream));
+        if (scat) CK(cudaMemcpyAsync(scat, g.b.p, (size_t)*n, cudaMemcpyDeviceToHost, c->cstream));
+    }
+    CK(cudaEventRecord(g.done, c->cstream));
+    g.pending = true;
+    return GPET_OK;
+}
+
+int gpet_get_coincidences_async(gpet_ctx* c, int64_t* pairs, uint8_t* klass, int64_t cap, int64_t* n)
+{
+    if (!c || !n) return GPET_ERR_ARG;
+    if (!results(c)) { *n = 0; return GPET_OK; }
+    Work& W = *c->work;
+    const int64_t off = W.c_off[c->res_sim];
+    *n = W.c_off[c->res_sim + 1] - off;
+    if (!pairs || *n == 0) return GPET_OK;
+    if (cap < *n) return fail(c, GPET_ERR_ARG, "buffer too small for the coincidences");
+    Staged& g = c->st_coinc;
+    void* dpairs = mapped_host(pairs);
+    void* dcls = mapped_host(klass);
+    const bool direct = dpairs && (!klass || dcls);
+    if (!direct) {
+        CK(stage_ensure(c, g, g.a, sizeof(int64_t) * 2 * (size_t)*n));
+        CK(stage_ensure(c, g, g.b, (size_t)*n));
+    }
+    CK(copies_after_main(c));
+    int64_t* dp = direct ? static_cast<int64_t*>(dpairs) : g.a.as<int64_t>();
+    uint8_t* dc = klass ? (direct ? static_cast<uint8_t*>(dcls) : g.b.as<uint8_t>()) : nullptr;
+    const int64_t blocks = std::min<int64_t>((*n + 255) / 256, kCopyBlocks);
+    k_coinc_out<<<(unsigned)blocks, 256, 0, c->cstream>>>(W.dg.coinc_pairs + 2 * off, W.dg.coinc_class + off, *n,
+                                                          W.s_off[c->res_sim], dp, dc);
+    CK(cudaGetLastError());
+    if (!direct) {
+        CK(cudaMemcpyAsync(pairs, g.a.p, sizeof(int64_t) * 2 * (size_t)*n, cudaMemcpyDeviceToHost, c->cstream));
+        if (klass) CK(cudaMemcpyAsync(klass, g.b.p, (size_t)*n, cudaMemcpyDeviceToHost, c->cstream));
+    }
+    CK(cudaEventRecord(g.done, c->cstream));
+    g.pending = true;
+    return GPET_OK;
+}
+
+int gpet_wait_copies(gpet_ctx* c)
+{
+    if (!c) return GPET_ERR_ARG;
+    if (!c->st_singles.pending && !c->st_coinc.pending) return GPET_OK;
+    CK(cudaStreamSynchronize(c->cstream));
+    c->st_singles.pending = c->st_coinc.pending = false;
     return GPET_OK;
 }
 

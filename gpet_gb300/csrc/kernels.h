@@ -189,7 +189,7 @@ struct DigiScratch {
     int64_t cap, hist_cap;
     // outputs
     uint32_t* single_idx;         // pulse index of each single, time order
-    int64_t* coinc_pairs;         // [2][coinc_cap] single indices
+    int64_t* coinc_pairs;         // [coinc_cap][2] single indices
     uint8_t* coinc_class;
     uint32_t* wcount;             // per-single pair count / offsets
     uint32_t* wend;               // per window start: one past its last single
@@ -210,8 +210,9 @@ int gather_events(const PulseDev& P, const uint32_t* idx, int64_t n, bool blurre
 // the blurred records written straight into mapped (pinned) host memory seen
 // through its device address (16-byte aligned), flags[j] = scattered in the
 // phantom (may be null)
+// max_blocks > 0 caps the grid (a gather that runs beside other kernels)
 int gather_events_mapped(const PulseDev& P, const uint32_t* idx, int64_t n, const DigiScratch& D, EventRec* out,
-                         uint8_t* flags, cudaStream_t s);
+                         uint8_t* flags, cudaStream_t s, unsigned max_blocks = 0);
 
 // digitizer kernels (digitizer.cu), for callers that orchestrate them with
 // their own working memory

@@ -39,7 +39,7 @@
 namespace gpet {
 
 constexpr uint32_t kWaitLimit = 1u << 24;   // mbarrier polls before a wait gives up
-constexpr uint32_t kTagSurrogate = 6;       // Philox stream tag of the surrogate's draws
+constexpr uint32_t kTagSurrogate = 6;       // stream tag of the surrogate's draws
 
 namespace sg {
 constexpr int kIn = 16, kFeat = 16, kHid = 256, kOut = 208, kOutUsed = 204, kEmb = 6;
@@ -199,8 +199,8 @@ __device__ __forceinline__ float tanh_approx(float x)
 
 // The response of a photon is sampled from the head's outputs in TMEM by
 // three warp groups at once (each thread: one row of the tile): the deposited
-// energy bin, the crystal, the depth. Each draws from the photon's own Philox
-// stream (tag 6, id = parn) in the fixed order ue, uw, uc, um, zn, skipping
+// energy bin, the crystal, the depth. Each draws from the photon's own stream
+// (tag 6, id = parn) in the fixed order ue, uw, uc, um, zn, skipping
 // the draws of the others. hb: the head's bias.
 
 // deposited-energy fraction bin: softmax over columns [140, 204)

@@ -280,29 +280,10 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
     int steps = 0;
     SimTally t_steps;
     Photon ph;
-    // the photon's Philox stream (tag kTagPhantom + (p & 1), id d, the
-    // simulation's key): only the block counter, position and current block
-    // are held; key and id are re-read when a block is generated
-    uint32_t rblk = 0, rbuf[4] = {0u, 0u, 0u, 0u};
-    int rpos = 4;
-    auto unif = [&]() -> float {
-        if (rpos == 4) {
-            const SimDesc& S = kMulti ? w.sims[sim] : sS;
-            philox10(rblk, kTagPhantom + (uint32_t)(p & 1), (uint32_t)d, (uint32_t)((uint64_t)d >> 32), S.key0,
-                     S.key1, rbuf);
-            rblk++;
-            rpos = 0;
-        }
-        uint32_t v;
-        switch (rpos) {   // keeps the block in registers
-        case 0: v = rbuf[0]; break;
-        case 1: v = rbuf[1]; break;
-        case 2: v = rbuf[2]; break;
-        default: v = rbuf[3]; break;
-        }
-        rpos++;
-        return dm_u01(v);
-    };
+    // the photon's stream (tag kTagPhantom + (p & 1), id d, the simulation's
+    // key), seeded when the lane takes the photon
+    uint32_t rst[4] = {0u, 0u, 0u, 0u};
+    auto unif = [&]() -> float { return dm_u01(xo_next(rst)); };
     for (;;) {
         // refill idle lanes, one atomic per warp
         const bool need = !active && !exhausted;
@@ -335,8 +316,11 @@ __global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, P
                         ph.t = 0.0;   // the emission time stays in the pair buffer (pb.t[p >> 1])
                         ph.tf = 0.0f;
                         ph.nscat = 0;
-                        rblk = 0;
-                        rpos = 4;
+                        {
+                            const SimDesc& S = kMulti ? w.sims[sim] : sS;
+                            st_seed(rst, S.key0, S.key1, kTagPhantom + (uint32_t)(p & 1), (uint32_t)d,
+                                    (uint32_t)((uint64_t)d >> 32));
+                        }
                         steps = 0;
                         active = true;
                         if (w.source) {
@@ -574,10 +558,9 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
     bool overflow = false;
     unsigned nsteps = 0;
     EntryRec er;
-    // the photon's Philox stream (tag kTagDet + (parn & 1), id eid, the
-    // simulation's key): key and id are re-read when a block is generated
-    uint32_t rblk = 0, rbuf[4] = {0u, 0u, 0u, 0u};
-    int rpos = 4;
+    // the photon's stream (tag kTagDet + (parn & 1), id eid, the simulation's
+    // key), seeded when the lane takes the photon
+    uint32_t rst[4] = {0u, 0u, 0u, 0u};
     // a deposit goes to the hit list at once (at most kMaxHits per photon),
     // the lanes that record one at the same point sharing one atomic
     auto put_hit = [&](int32_t M_id, int32_t L_id, int32_t type, float Ed, double t) {
@@ -602,23 +585,7 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
         H.f[5 * o + 2] = L.x[0]; H.f[5 * o + 3] = L.x[1]; H.f[5 * o + 4] = L.x[2];
         if (H.sim) H.sim[o] = sim;
     };
-    auto unif = [&]() -> float {
-        if (rpos == 4) {
-            const SimDesc& S = kMulti ? sims[sim] : sS;
-            philox10(rblk, kTagDet + (uint32_t)(parn & 1), (uint32_t)eid, 0u, S.key0, S.key1, rbuf);
-            rblk++;
-            rpos = 0;
-        }
-        uint32_t v;
-        switch (rpos) {   // keeps the block in registers
-        case 0: v = rbuf[0]; break;
-        case 1: v = rbuf[1]; break;
-        case 2: v = rbuf[2]; break;
-        default: v = rbuf[3]; break;
-        }
-        rpos++;
-        return dm_u01(v);
-    };
+    auto unif = [&]() -> float { return dm_u01(xo_next(rst)); };
     for (;;) {
         // refill idle lanes
         const bool need = !active && !exhausted;
@@ -652,8 +619,7 @@ __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueD
                         er.ux = L.u[0]; er.uy = L.u[1]; er.uz = L.u[2];
                         er.E = L.E;
                     }
-                    rblk = 0;
-                    rpos = 4;
+                    st_seed(rst, S.key0, S.key1, kTagDet + (uint32_t)(parn & 1), (uint32_t)eid, 0u);
                     nev = 0; nh = 0; step = 0; nsteps = 0;
                     overflow = false;
                     active = true;

@@ -175,6 +175,19 @@ int gpet_get_pulses(gpet_ctx* ctx, gpet_event* buf, uint8_t* scat, uint8_t* slot
 /* Coincidences: index pairs into the singles list and class (0 true,
  * 1 scatter, 2 random). */
 int gpet_get_coincidences(gpet_ctx* ctx, int64_t* pairs, uint8_t* klass, int64_t cap, int64_t* n);
+/* Asynchronous forms of gpet_get_singles / gpet_get_coincidences (the
+ * writeSingles / writeCoinc outputs of the reference's main loop, main.cu,
+ * for callers that stream acquisitions): the records are gathered on the
+ * device (the call waits for that, a fraction of a millisecond) and copied
+ * into the caller's buffers on the context's copy stream, which overlaps the
+ * context's next gpet_set_phantom / gpet_run. *n is set at once; the buffers
+ * (page-locked host memory for the copy to be asynchronous) hold the records
+ * only after gpet_wait_copies, and must not be reused or freed before it.
+ * Results are identical to the synchronous calls. */
+int gpet_get_singles_async(gpet_ctx* ctx, gpet_event* buf, uint8_t* scat, int64_t cap, int64_t* n);
+int gpet_get_coincidences_async(gpet_ctx* ctx, int64_t* pairs, uint8_t* klass, int64_t cap, int64_t* n);
+/* Waits for the copies of the asynchronous calls above. */
+int gpet_wait_copies(gpet_ctx* ctx);
 /* Hits (HitsID.dat / Hits.dat records, gPET.cu:367-379): ids [n][5] = parn,
  * panel, module, crystal, type (1/2 Compton, 4 photoelectric); f [n][5] = E,
  * t, local x, y, z. Order within a photon is deposit order. */

@@ -109,6 +109,8 @@ def lib(precision="fp64"):
                                       C.POINTER(C.c_uint8), C.c_int64, C.POINTER(_Result)]
         L.oracle_free_result.argtypes = [C.POINTER(_Result)]
         L.oracle_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.oracle_stream_words.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_int64,
+                                          C.POINTER(C.c_uint32)]
         _LIBS[precision] = L
     return _LIBS[precision]
 
@@ -118,6 +120,13 @@ def philox(ctr, key):
     k = (C.c_uint32 * 2)(*key)
     o = (C.c_uint32 * 4)()
     lib().oracle_philox4x32_10(c, k, o)
+    return list(o)
+
+
+def stream_words(key, tag, ident, n):
+    """The first n words of the oracle's random stream (key, tag, id)."""
+    o = (C.c_uint32 * n)()
+    lib().oracle_stream_words(key[0], key[1], tag, ident, n, o)
     return list(o)
 
 

@@ -78,25 +78,36 @@ void oracle_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], ui
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
+/* A stream (key, tag, 64-bit id): its state is the Philox4x32-10 block of
+ * counter (0, tag, id) under the key (the all-zero state, which xoshiro never
+ * leaves, replaced by a fixed one); its words come from xoshiro128**
+ * (Blackman & Vigna, "Scrambled linear pseudorandom number generators", ACM
+ * TOMS 2021), restated from the paper. */
 typedef struct {
-    uint32_t key[2], ctr[4], buf[4];
-    int pos;
+    uint32_t s[4];
 #ifdef ORACLE_TAPE
-    const uint32_t* tape;   /* words to draw instead of Philox (pins against the reference) */
+    const uint32_t* tape;   /* words to draw instead of the stream's (pins against the reference) */
     int64_t tape_n, tape_pos;
 #endif
 } stream_t;
 
-static void st_init(stream_t* s, const or_scene* sc, uint32_t tag, uint64_t id)
+static void st_seed_words(stream_t* s, uint32_t k0, uint32_t k1, uint32_t tag, uint64_t id)
 {
-    s->key[0] = (uint32_t)sc->seed;
-    s->key[1] = (uint32_t)(sc->seed >> 32) + sc->sim_id;
-    s->ctr[0] = 0; s->ctr[1] = tag; s->ctr[2] = (uint32_t)id; s->ctr[3] = (uint32_t)(id >> 32);
-    s->pos = 4;
+    const uint32_t key[2] = {k0, k1};
+    const uint32_t ctr[4] = {0u, tag, (uint32_t)id, (uint32_t)(id >> 32)};
+    oracle_philox4x32_10(ctr, key, s->s);
+    if ((s->s[0] | s->s[1] | s->s[2] | s->s[3]) == 0u) s->s[0] = 0x9E3779B9u;
 #ifdef ORACLE_TAPE
     s->tape = NULL;
 #endif
 }
+
+static void st_init(stream_t* s, const or_scene* sc, uint32_t tag, uint64_t id)
+{
+    st_seed_words(s, (uint32_t)sc->seed, (uint32_t)(sc->seed >> 32) + sc->sim_id, tag, id);
+}
+
+static inline uint32_t rotl32(uint32_t x, int k) { return (x << k) | (x >> (32 - k)); }
 
 static inline uint32_t st_next(stream_t* s)
 {
@@ -107,12 +118,30 @@ static inline uint32_t st_next(stream_t* s)
         return w;
     }
 #endif
-    if (s->pos == 4) {
-        oracle_philox4x32_10(s->ctr, s->key, s->buf);
-        s->ctr[0]++;
-        s->pos = 0;
-    }
-    return s->buf[s->pos++];
+    uint32_t* q = s->s;
+    const uint32_t v = rotl32(q[1] * 5u, 7) * 9u;
+    const uint32_t t = q[1] << 9;
+    q[2] ^= q[0];
+    q[3] ^= q[1];
+    q[1] ^= q[2];
+    q[0] ^= q[3];
+    q[2] ^= t;
+    q[3] = rotl32(q[3], 11);
+    return v;
+}
+
+/* uniforms the samplers make of words w (dm_u01), for known-answer tests */
+void oracle_u01(int64_t n, const uint32_t* w, float* out)
+{
+    for (int64_t i = 0; i < n; ++i) out[i] = dm_u01(w[i]);
+}
+
+/* the first n words of stream (key, tag, id), for known-answer tests */
+void oracle_stream_words(uint32_t k0, uint32_t k1, uint32_t tag, uint64_t id, int64_t n, uint32_t* out)
+{
+    stream_t s;
+    st_seed_words(&s, k0, k1, tag, id);
+    for (int64_t i = 0; i < n; ++i) out[i] = st_next(&s);
 }
 
 static inline real st_u(stream_t* s) { return (real)dm_u01(st_next(s)); }

@@ -141,6 +141,11 @@ int oracle_digitize(const or_scene* sc, const or_event* pulses, const uint8_t* s
 void oracle_free_result(or_result* r);
 /* Philox4x32-10 block, for known-answer tests. */
 void oracle_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* The uniforms the samplers make of words w. */
+void oracle_u01(int64_t n, const uint32_t* w, float* out);
+/* The first n words of the stream (key k0 k1, tag, id): xoshiro128** from the
+ * Philox4x32-10 block of counter (0, tag, id), for known-answer tests. */
+void oracle_stream_words(uint32_t k0, uint32_t k1, uint32_t tag, uint64_t id, int64_t n, uint32_t* out);
 int oracle_real_bytes(void);
 
 #endif

@@ -222,3 +222,52 @@ def test_singles_into_pinned_memory_match_the_copy(scene_positron, data_dir, gpe
     m = ctypes.c_int64()
     assert ctx.L.gpet_get_singles(ctx.h, ev_buf.ctypes.data, None, n, ctypes.byref(m)) == 0
     assert m.value == n and ev_buf.tobytes() == ev0.tobytes()
+
+
+def test_async_copies_equal_the_synchronous_calls(scene_positron, scene_small, data_dir, gpet_lib):
+    """gpet_get_singles_async / gpet_get_coincidences_async: the records of a
+    run reach pinned buffers while the next run (larger, so the staging
+    buffers grow under a pending copy) proceeds, and equal what the
+    synchronous calls give for that run; in a batched job each simulation's
+    pairs index its own singles."""
+    import torch
+    from gpet_gb300 import api, formats as F
+
+    def pinned(n, dtype, shape=None):
+        nb = int(np.prod(shape or (n,))) * np.dtype(dtype).itemsize
+        return torch.empty(nb, dtype=torch.uint8, pin_memory=True).numpy().view(dtype).reshape(shape or (n,))
+
+    ref = make_ctx(scene_positron, data_dir, seed=31, n_decays=1500000)
+    ref.run()
+    want_a = (ref.singles(), ref.coincidences())
+    ref.close()
+    ctx = make_ctx(scene_positron, data_dir, seed=31, n_decays=1500000)
+    ctx.run()
+    cap = 4 * len(want_a[0][0]) + 1024
+    outs = [((pinned(cap, F.EVENT_DTYPE), pinned(cap, np.uint8)),
+             (pinned(cap, np.int64, (cap, 2)), pinned(cap, np.uint8))) for _ in range(2)]
+    s_a = ctx.singles_async(outs[0][0])
+    c_a = ctx.coincidences_async(outs[0][1])
+    ctx.set_options({"seed": 32, "n_decays": 3000000})
+    ctx.run()                                   # overlaps the copies above
+    s_b = ctx.singles_async(outs[1][0])
+    c_b = ctx.coincidences_async(outs[1][1])
+    ctx.wait_copies()
+    assert len(s_b[0]) > len(s_a[0]) > 1000 and len(c_a[0]) > 100
+    for got, want in zip(s_a + c_a, want_a[0] + want_a[1]):
+        assert got.tobytes() == want.tobytes()
+    for got, want in zip(s_b + c_b, ctx.singles() + ctx.coincidences()):
+        assert got.tobytes() == want.tobytes()
+    ctx.close()
+    # batched: the second simulation's pairs are rebased onto its own singles
+    ctxs = [make_ctx(scene_small, data_dir, seed=41 + i, n_decays=20000) for i in range(2)]
+    api.run_batched(ctxs)
+    for c in ctxs:
+        o = ((pinned(cap, F.EVENT_DTYPE), pinned(cap, np.uint8)), (pinned(cap, np.int64, (cap, 2)), pinned(cap, np.uint8)))
+        s = c.singles_async(o[0])
+        p = c.coincidences_async(o[1])
+        c.wait_copies()
+        for got, want in zip(s + p, c.singles() + c.coincidences()):
+            assert got.tobytes() == want.tobytes()
+        assert len(p[0]) == 0 or p[0].max() < len(s[0])
+        c.close()

@@ -1,6 +1,7 @@
 """Pins of the CPU oracle against known answers: Random123's Philox vectors,
-the reference's own data files (tables at 511 keV, isotope spectra, the
-example detector), and the physics the samplers must reproduce."""
+the random streams seeded from them, the reference's own data files (tables
+at 511 keV, isotope spectra, the example detector), and the physics the
+samplers must reproduce."""
 import ctypes as C
 import json
 import os
@@ -19,6 +20,58 @@ def test_philox_random123_vectors(oracle_mod):
     assert ph([0xffffffff] * 4, [0xffffffff] * 2) == [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
     assert ph([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0]) == \
         [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+def _xoshiro128ss(state, n):
+    # xoshiro128** (Blackman & Vigna), restated from the paper in Python
+    s = list(state)
+    rotl = lambda x, k: ((x << k) | (x >> (32 - k))) & 0xFFFFFFFF
+    out = []
+    for _ in range(n):
+        out.append(rotl((s[1] * 5) & 0xFFFFFFFF, 7) * 9 & 0xFFFFFFFF)
+        t = (s[1] << 9) & 0xFFFFFFFF
+        s[2] ^= s[0]
+        s[3] ^= s[1]
+        s[1] ^= s[2]
+        s[0] ^= s[3]
+        s[2] ^= t
+        s[3] = rotl(s[3], 11)
+    return out
+
+
+def test_stream_is_xoshiro_from_a_philox_block(oracle_mod):
+    """A stream's words: xoshiro128** from the Philox4x32-10 block of counter
+    (0, tag, id) under the key. The generator's first words from state
+    (1, 2, 3, 4) worked by hand: 11520, 0, 5927040."""
+    assert _xoshiro128ss([1, 2, 3, 4], 3) == [11520, 0, 5927040]
+    for key, tag, ident in (([0, 0], 0, 0), ([20261203, 7], 2, 123456789), ([0xFFFFFFFF, 1], 9, (5 << 32) + 17)):
+        seed = oracle_mod.philox([0, tag, ident & 0xFFFFFFFF, ident >> 32], key)
+        assert oracle_mod.stream_words(key, tag, ident, 64) == _xoshiro128ss(seed, 64)
+    # streams of neighbouring ids and tags share no words
+    a = oracle_mod.stream_words([1, 2], 2, 1000, 4096)
+    b = oracle_mod.stream_words([1, 2], 2, 1001, 4096)
+    c = oracle_mod.stream_words([1, 2], 3, 1000, 4096)
+    assert not (set(a) & set(b)) and not (set(a) & set(c))
+    # the top 24 bits (what a uniform uses) are uniform: chi-square over 256 bins
+    w = np.array(oracle_mod.stream_words([3, 4], 1, 42, 1 << 18), np.uint32) >> 24
+    h = np.bincount(w, minlength=256)
+    chi2 = float(((h - h.mean()) ** 2 / h.mean()).sum())
+    assert 150 < chi2 < 380
+
+
+def test_uniforms_stay_inside_the_unit_interval(oracle_mod):
+    """Every word gives (k + 1/2) 2^-23 from its top 23 bits, exactly, never 0
+    or 1 (a uniform of 1 made a Box-Muller normal exactly 0, and the
+    positron-range walk's reciprocal of that displacement component a NaN
+    position)."""
+    L = oracle_mod.lib("fp32")
+    L.oracle_u01.argtypes = [C.c_int64, C.c_void_p, C.c_void_p]
+    w = np.concatenate([np.arange(0, 1 << 12, dtype=np.uint64), (1 << 32) - 1 - np.arange(1 << 12, dtype=np.uint64),
+                        np.random.default_rng(3).integers(0, 1 << 32, 1 << 16, dtype=np.uint64)]).astype(np.uint32)
+    u = np.zeros(len(w), np.float32)
+    L.oracle_u01(len(w), w.ctypes.data, u.ctypes.data)
+    assert u.min() == np.float32(2.0 ** -24) and u.max() == np.float32(1 - 2.0 ** -24)
+    assert np.array_equal(u.astype(np.float64), ((w >> 9).astype(np.float64) + 0.5) * 2.0 ** -23)
 
 
 def _dm(oracle_mod, which, x):
