@@ -121,7 +121,7 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2])
 // simulation's descriptor; otherwise the one descriptor is staged in shared
 // memory.
 template <bool kMulti>
-__global__ void __launch_bounds__(256, 4) k_source(const Wave* waves, int wi, PairBuf pb, Counters* cnt)
+__global__ void __launch_bounds__(256, 5) k_source(const Wave* waves, int wi, PairBuf pb, Counters* cnt)
 {
     const Wave w = waves[wi];
     __shared__ SimDesc sS;
@@ -189,7 +189,7 @@ constexpr int kFinCap = 64;      // finished photons staged per warp
 // at a time, one per lane. Photon p of the wave is photon (p & 1) of the
 // wave's decay p >> 1. kMulti as for k_source.
 template <bool kMulti>
-__global__ void __launch_bounds__(256, 4) k_phantom(const Wave* waves, int wi, PairBuf pb, QueueDev q, Counters* cnt,
+__global__ void __launch_bounds__(256, 5) k_phantom(const Wave* waves, int wi, PairBuf pb, QueueDev q, Counters* cnt,
                                                     int period)
 {
     const Wave w = waves[wi];
