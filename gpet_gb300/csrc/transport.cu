@@ -168,16 +168,15 @@ __global__ void __launch_bounds__(256, 5) k_source(const Wave* waves, int wi, Pa
 
 // a photon that has left the phantom (or stopped), waiting for the panel search
 // (always escaped: status 1; the emission time stays in the pair buffer and
-// is read in the drain, only for the photons that need it)
+// is read in the drain, only for the photons that need it; the decay index
+// and simulation follow from the photon index through the wave's segments)
 struct FinRec {
     float x, y, z, ux, uy, uz, E;
     int32_t nscat;
-    long long d;      // decay index within its simulation
     int32_t p;        // photon index within the wave
     float tf;
-    int32_t sim;
-    int32_t pad_;
 };
+static_assert(sizeof(FinRec) == 40, "staged record");
 
 constexpr int kPhWarps = 8;      // warps per k_phantom block (256 threads)
 constexpr int kFinCap = 64;      // finished photons staged per warp
@@ -213,8 +212,15 @@ __global__ void __launch_bounds__(256, 5) k_phantom(const Wave* waves, int wi, P
     auto drain = [&](int k) {
         const bool has = lane < k;
         FinRec r;
-        r.sim = 0;
-        if (has) r = fb[lane];
+        int rsim = 0;
+        int64_t rd = 0;
+        if (has) {
+            r = fb[lane];
+            const int64_t j = r.p >> 1;
+            const int sgi = seg_of(sg, j);
+            rsim = kMulti ? sg.sim[sgi] : 0;
+            rd = sg.d0[sgi] + (j - sg.g0[sgi]);
+        }
         Photon ph;
         Local L;
         bool entered = false;
@@ -223,7 +229,7 @@ __global__ void __launch_bounds__(256, 5) k_phantom(const Wave* waves, int wi, P
             ph.u[0] = r.ux; ph.u[1] = r.uy; ph.u[2] = r.uz;
             ph.E = r.E; ph.t = 0.0; ph.tf = r.tf; ph.nscat = r.nscat;   // L.t: flight time alone
             if (kMulti) {
-                const SimDesc& S = w.sims[r.sim];
+                const SimDesc& S = w.sims[rsim];
                 entered = enter_panel(S.panels, S.npanels, ph, L);
             } else {
                 entered = enter_panel(sP, sS.npanels, ph, L);
@@ -241,7 +247,7 @@ __global__ void __launch_bounds__(256, 5) k_phantom(const Wave* waves, int wi, P
             if (entered) {
                 const unsigned long long jq = b + __popc(m & lt);
                 if (jq < (unsigned long long)q.cap) {
-                    const int64_t d = r.d;
+                    const int64_t d = rd;
                     q.f[0 * q.cap + jq] = L.x[0];
                     q.f[1 * q.cap + jq] = L.x[1];
                     q.f[2 * q.cap + jq] = L.x[2];
@@ -254,14 +260,14 @@ __global__ void __launch_bounds__(256, 5) k_phantom(const Wave* waves, int wi, P
                     q.i[1 * q.cap + jq] = (int32_t)(2 * d + (r.p & 1));
                     q.i[2 * q.cap + jq] = (int32_t)d;
                     q.i[3 * q.cap + jq] = r.nscat;
-                    q.i[4 * q.cap + jq] = r.sim;
+                    q.i[4 * q.cap + jq] = rsim;
                 } else {
                     entered = false;
                     atomicAdd(&cnt->queue_drop, 1ull);
                 }
             }
         }
-        add_by_sim(cnt, r.sim, CF(entered), entered ? 1u : 0u);
+        add_by_sim(cnt, rsim, CF(entered), entered ? 1u : 0u);
         if (has && exits) {
             ExitRec e;
             e.x = r.x; e.y = r.y; e.z = r.z; e.ux = r.ux; e.uy = r.uy; e.uz = r.uz;
@@ -424,8 +430,7 @@ __global__ void __launch_bounds__(256, 5) k_phantom(const Wave* waves, int wi, P
                 FinRec r;
                 r.x = ph.x[0]; r.y = ph.x[1]; r.z = ph.x[2];
                 r.ux = ph.u[0]; r.uy = ph.u[1]; r.uz = ph.u[2];
-                r.E = ph.E; r.nscat = ph.nscat; r.p = p; r.d = d; r.tf = ph.tf;
-                r.sim = sim; r.pad_ = 0;
+                r.E = ph.E; r.nscat = ph.nscat; r.p = p; r.tf = ph.tf;
                 fb[fcount + __popc(mf & lt)] = r;
                 active = false;
             }
