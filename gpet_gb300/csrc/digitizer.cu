@@ -25,9 +25,12 @@
 namespace gpet {
 
 constexpr int kTile = 4096;      // items per block in radix / scan kernels
-// time keys: (t - tmin) quantised to 48 bits over the survivors' time span
-// (6 radix passes instead of 8); runs of equal keys are ordered by t after
-constexpr int kTimeKeyBits = 48;
+// time keys: (t - tmin) quantised to 32 bits over the survivors' time span
+// (4 radix passes instead of 8 on the IEEE bits); runs of equal keys are
+// ordered by (t, parn, slot) after the sort. m pulses spread over the span
+// share a key with m / 2^32 others on average (about 1e-3 for a 1e8-decay
+// acquisition), so the runs are the few pulses of one instant.
+constexpr int kTimeKeyBits = 32;
 constexpr uint64_t kTimeKeyMax = (1ull << kTimeKeyBits) - 1;
 
 static unsigned grid_for(int64_t n, int threads);
@@ -366,7 +369,7 @@ __global__ void k_blur_threshold(PulseDev P, int64_t n, const DigiParams* __rest
     }
 }
 
-// time keys: with quant, floor((t - tmin) * scale) (at most 48 bits; t >=
+// time keys: with quant, floor((t - tmin) * scale) (at most 32 bits; t >=
 // tmin for every selected pulse, and the key is monotone in t), else the
 // IEEE bits of t (non-negative times order like their bits)
 __global__ void k_time_keys(const uint32_t* __restrict__ sel, int64_t m, const double* __restrict__ t, int quant,

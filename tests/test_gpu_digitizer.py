@@ -115,7 +115,7 @@ def test_digitizer_with_background_singles(scene_positron, data_dir, gpet_lib, o
 
 @pytest.mark.parametrize("case", ["one_instant", "ulp_apart_wide_span", "negative_times"])
 def test_time_order_keys_edge_cases(scene_positron, data_dir, gpet_lib, oracle_mod, case):
-    """The time order sorts 48-bit keys of (t - t_min) over the survivors'
+    """The time order sorts 32-bit keys of (t - t_min) over the survivors'
     time span and puts runs of equal keys in (t, parn, slot) order: pulses
     at one instant (zero span: the IEEE bits of t are the keys), pulses a few
     ulps apart within a span of 1e12 us (many share a quantised key), and
