@@ -50,6 +50,9 @@ struct SimDesc {
     float dx, dy, dz, idx, idy, idz, offx, offy, offz;
     const uint2* vox;
     const uint16_t* vox16;
+    // radius of uniform density around each voxel (prange_uniform), or null
+    const int8_t* prmap;
+    float prdmin;                 // min(dx, dy, dz)
     // detector
     int32_t npanels;
     const float* panels;          // [npanels][32]
@@ -322,18 +325,23 @@ __device__ __forceinline__ float sample_ek(const float* cf, Stream& st)
     return (e - 0.511f) * 1.0e6f;
 }
 
-// setPositronRange, gPET_kernals.cu:347-418 (density read from the voxel being
-// entered; outside the phantom the remaining range is walked in air)
-// spare (may be null): the second normal of the last Box-Muller pair, which
-// the pair emission uses for its non-collinearity angle
-inline __device__ void positron_range(const SimDesc& S, float x[3], float ek, const float* dir, Stream& st,
-                                      float* spare = nullptr)
+// setPositronRange, gPET_kernals.cu:347-418, in three parts: the Gaussian
+// displacement (prange_draw), the closed form for a walk that stays in voxels
+// of one density (prange_uniform) and the voxel walk itself (prange_walk_*,
+// density read from the voxel being entered; outside the phantom the
+// remaining range is walked in air). The walk draws no random numbers, so
+// k_source can leave it to k_walk and go on with the pair emission.
+constexpr int kPrMax = 6;        // largest radius the uniform-density map holds
+
+// displacement d (length r, returned) of a positron of kinetic energy ek (eV);
+// along dir when given. spare (may be null): the second normal of the last
+// Box-Muller pair, which the pair emission uses for its non-collinearity angle
+__device__ __forceinline__ float prange_draw(float ek, const float* dir, Stream& st, float d[3], float* spare)
 {
     float ekin = ek / 1.0e6f;
     const float b1 = 5.44040782f, b2 = 0.369516529f;
     float rex = 0.1f * b1 * ekin * ekin / (b2 + ekin);
     float sigma = rex / 2.0f;
-    float d[3];
     {
         float n1, n2;
         st_normal2(st, n1, n2);
@@ -349,45 +357,100 @@ inline __device__ void positron_range(const SimDesc& S, float x[3], float ek, co
         float tmp = dm_sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
         d[0] = r * dir[0] / tmp; d[1] = r * dir[1] / tmp; d[2] = r * dir[2] / tmp;
     }
-    // reciprocals once: the voxel walk multiplies instead of dividing
-    const float id0 = 1.0f / d[0], id1 = 1.0f / d[1], id2 = 1.0f / d[2];
+    return r;
+}
+
+// The walk ends where the density-weighted path length reaches r. Where every
+// voxel it reads has the density rho, that is x + (r / rho) * d / r exactly.
+// The voxels it reads lie within floor(L / dmin) + 2 voxels (Chebyshev) of the
+// start voxel, L = r / rho (the end voxel, plus the voxel entered beyond it);
+// prmap[v] = R says that all voxels within R of v have v's density and lie in
+// [1, n-2] on every axis, so L < (R - 1.5) * dmin (half a voxel of margin)
+// keeps the walk inside. Returns false (x unchanged) where the walk is needed.
+// A zero displacement moves nothing, as in the walk.
+__device__ __forceinline__ bool prange_uniform(const SimDesc& S, float x[3], const float d[3], float r)
+{
+    if (!(r > 0.0f)) return true;
+    if (!S.prmap) return false;
+    int ix, iy, iz;
+    if (!abs_vox(S, x[0], x[1], x[2], ix, iy, iz)) return false;
+    const size_t i = (size_t)ix + (size_t)S.nx * ((size_t)iy + (size_t)S.ny * iz);
+    const int R = __ldg(S.prmap + i);
+    if (R < 2) return false;
+    const float rho = __uint_as_float(voxel(S, ix, iy, iz).x);
+    if (!(rho > 0.0f)) return false;
+    const float L = r / rho;
+    if (!(L < ((float)R - 1.5f) * S.prdmin)) return false;
     const float ir = 1.0f / r;
     const float dn0 = d[0] * ir, dn1 = d[1] * ir, dn2 = d[2] * ir;
-    int vx = 0, vy = 0, vz = 0;
-    bool inside = abs_vox(S, x[0], x[1], x[2], vx, vy, vz);
-    if (!inside) { vx = vy = vz = 0; }
-    float s = 0.0f, step;
+    x[0] = x[0] + L * dn0;
+    x[1] = x[1] + L * dn1;
+    x[2] = x[2] + L * dn2;
+    return true;
+}
+
+// state of one voxel walk
+struct PWalk {
+    float x[3], id[3], dn[3], r, s;
+    int v[3];
+    int guard;
+    int pos;                      // bit k: d[k] > 0
+    bool inside;
+};
+
+// set up the walk of displacement d (length r) from x; false if it has no step
+__device__ __forceinline__ bool prange_walk_init(const SimDesc& S, PWalk& w, const float x[3], const float d[3],
+                                                 float r)
+{
+    // reciprocals once: the walk multiplies instead of dividing
+    w.id[0] = 1.0f / d[0]; w.id[1] = 1.0f / d[1]; w.id[2] = 1.0f / d[2];
+    const float ir = 1.0f / r;
+    w.dn[0] = d[0] * ir; w.dn[1] = d[1] * ir; w.dn[2] = d[2] * ir;
+    w.pos = (d[0] > 0.0f ? 1 : 0) | (d[1] > 0.0f ? 2 : 0) | (d[2] > 0.0f ? 4 : 0);
+    w.x[0] = x[0]; w.x[1] = x[1]; w.x[2] = x[2];
+    w.inside = abs_vox(S, x[0], x[1], x[2], w.v[0], w.v[1], w.v[2]);
+    if (!w.inside) { w.v[0] = w.v[1] = w.v[2] = 0; }
+    w.r = r;
+    w.s = 0.0f;
+    w.guard = 0;
+    return w.s < w.r;
+}
+
+// one step of the walk; false once it has ended
+__device__ __forceinline__ bool prange_walk_step(const SimDesc& S, PWalk& w)
+{
+    float step = 1000.0f;
+    if (w.inside) {
+        int ax = 0;
+        const int px = w.pos & 1, py = (w.pos >> 1) & 1, pz = (w.pos >> 2) & 1;
+        float bb = (S.offx + (float)(w.v[0] + px) * S.dx - w.x[0]) * w.id[0];
+        if (step > bb) { step = bb; ax = 1; }
+        bb = (S.offy + (float)(w.v[1] + py) * S.dy - w.x[1]) * w.id[1];
+        if (step > bb) { step = bb; ax = 2; }
+        bb = (S.offz + (float)(w.v[2] + pz) * S.dz - w.x[2]) * w.id[2];
+        if (step > bb) { step = bb; ax = 3; }
+        if (ax == 1) w.v[0] += px ? 1 : -1;
+        else if (ax == 2) w.v[1] += py ? 1 : -1;
+        else w.v[2] += pz ? 1 : -1;
+        float rho = den_clamped(S, w.v[0], w.v[1], w.v[2]);
+        step = step * w.r;
+        w.s += step * rho;
+        if (w.s > w.r) step += (w.r - w.s) / rho;
+    } else {
+        step = (w.r - w.s) / 0.0012905f;
+        w.s = w.r + 100.0f;
+    }
+    w.x[0] += step * w.dn[0];
+    w.x[1] += step * w.dn[1];
+    w.x[2] += step * w.dn[2];
     const float xmax = S.offx + (float)S.nx * S.dx;
     const float ymax = S.offy + (float)S.ny * S.dy;
     const float zmax = S.offz + (float)S.nz * S.dz;
-    for (int guard = 0; s < r && guard < 100000; ++guard) {
-        step = 1000.0f;
-        if (inside) {
-            int ax = 0;
-            float bb = (S.offx + (float)(vx + (d[0] > 0.0f)) * S.dx - x[0]) * id0;
-            if (step > bb) { step = bb; ax = 1; }
-            bb = (S.offy + (float)(vy + (d[1] > 0.0f)) * S.dy - x[1]) * id1;
-            if (step > bb) { step = bb; ax = 2; }
-            bb = (S.offz + (float)(vz + (d[2] > 0.0f)) * S.dz - x[2]) * id2;
-            if (step > bb) { step = bb; ax = 3; }
-            if (ax == 1) vx += d[0] > 0.0f ? 1 : -1;
-            else if (ax == 2) vy += d[1] > 0.0f ? 1 : -1;
-            else vz += d[2] > 0.0f ? 1 : -1;
-            float rho = den_clamped(S, vx, vy, vz);
-            step = step * r;
-            s += step * rho;
-            if (s > r) step += (r - s) / rho;
-        } else {
-            step = (r - s) / 0.0012905f;
-            s = r + 100.0f;
-        }
-        x[0] += step * dn0;
-        x[1] += step * dn1;
-        x[2] += step * dn2;
-        if (x[0] < S.offx || x[0] > xmax) inside = false;
-        if (x[1] < S.offy || x[1] > ymax) inside = false;
-        if (x[2] < S.offz || x[2] > zmax) inside = false;
-    }
+    if (w.x[0] < S.offx || w.x[0] > xmax) w.inside = false;
+    if (w.x[1] < S.offy || w.x[1] > ymax) w.inside = false;
+    if (w.x[2] < S.offz || w.x[2] > zmax) w.inside = false;
+    ++w.guard;
+    return w.s < w.r && w.guard < 100000;
 }
 
 // ---------------------------------------------------------------- photons

@@ -101,6 +101,7 @@ struct Work {
     DevBuf ent;                           // entry records of one chunk
     DevBuf serr;                          // surrogate kernel error flag
     DevBuf pb_f, pb_t, pb_n;              // emitted pairs of one wave
+    DevBuf pb_wf, pb_wj;                  // the wave's positron walk list
     int64_t pb_cap = 0;
     DevBuf aux;                           // [0] queue count [1] pulses [2] hits [4] Monte Carlo queue [5] surrogate list
                                           // [6] second queue count [8] detector lanes' next entry
@@ -204,6 +205,7 @@ struct gpet_ctx {
     DevBuf d_sim, d_xs4, d_cmpsf, d_rayff, d_wck_ph, d_wck_det, d_vox, d_panels, d_psf;
     DevBuf d_vox16, d_pal;                // palette form: per-voxel index, palette (hash table of pairs)
     DevBuf d_mat_stage, d_den_stage, d_maxden;   // phantom upload
+    DevBuf d_prmap, d_prmap2;             // uniform-density map of the positron range (and a pass buffer)
     // results of the last run this context took part in
     std::shared_ptr<Work> work;
     // gpet_get_*_async: results gathered into context-owned device buffers
@@ -242,6 +244,68 @@ static std::string resolve(const gpet_ctx* c, const std::string& p)
 {
     if (p.empty() || p[0] == '/') return p;
     return c->base_dir + "/" + p;
+}
+
+// Uniform-density map of the positron-range closed form (prange_uniform):
+// m[v] = the largest R <= kPrMax such that every voxel within Chebyshev
+// distance R of v has v's density (the same float bits) and lies in
+// [1, n-2] on every axis; -1 where v itself is outside that range. The ball
+// of radius R around v is the union of the balls of radius R-1 around v's
+// 26 neighbours, so m = 1 + min over the neighbours of m where all 26 have
+// v's density and lie in the range, else 0; kPrMax Jacobi passes from
+// m = min(m, 1) give min(R, kPrMax) exactly.
+__device__ __forceinline__ bool pr_interior(int x, int y, int z, int nx, int ny, int nz)
+{
+    return x >= 1 && x <= nx - 2 && y >= 1 && y <= ny - 2 && z >= 1 && z <= nz - 2;
+}
+
+// one thread per voxel on a (32, 8, 1) block grid over (x, y, z); planes
+// beyond the grid's z extent (65535) loop
+__global__ void k_prmap_init(const float* __restrict__ den, int nx, int ny, int nz, int8_t* __restrict__ m)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= nx || y >= ny) return;
+    for (int z = blockIdx.z; z < nz; z += gridDim.z) {
+        const int64_t v = (int64_t)x + (int64_t)nx * (y + (int64_t)ny * z);
+        int8_t r = -1;
+        if (pr_interior(x, y, z, nx, ny, nz)) {
+            r = 1;
+            const unsigned b = __float_as_uint(den[v]);
+            for (int dz = -1; dz <= 1 && r; ++dz)
+                for (int dy = -1; dy <= 1 && r; ++dy)
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        if (!pr_interior(x + dx, y + dy, z + dz, nx, ny, nz) ||
+                            __float_as_uint(den[v + dx + (int64_t)nx * (dy + (int64_t)ny * dz)]) != b) {
+                            r = 0;
+                            break;
+                        }
+                    }
+        }
+        m[v] = r;
+    }
+}
+
+__global__ void k_prmap_pass(const int8_t* __restrict__ m0, int nx, int ny, int nz, int8_t* __restrict__ m1)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= nx || y >= ny) return;
+    for (int z = blockIdx.z; z < nz; z += gridDim.z) {
+        const int64_t v = (int64_t)x + (int64_t)nx * (y + (int64_t)ny * z);
+        int r = m0[v];
+        if (r >= 1) {
+            // v and all its neighbours are in the range and of one density
+            int mn = kPrMax;
+            for (int dz = -1; dz <= 1; ++dz)
+                for (int dy = -1; dy <= 1; ++dy)
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        if ((dx | dy | dz) == 0) continue;
+                        const int q = __ldg(m0 + v + dx + (int64_t)nx * (dy + (int64_t)ny * dz));
+                        mn = q < mn ? q : mn;
+                    }
+            r = mn + 1 < kPrMax ? mn + 1 : kPrMax;
+        }
+        m1[v] = (int8_t)r;
+    }
 }
 
 // pack (density, material) into the phantom's 8-byte voxels and take each
@@ -570,6 +634,21 @@ int gpet_set_phantom(gpet_ctx* c, const int32_t* mat, const float* den, const in
     }
     c->vox_pal = pal;
     if (h[16]) return fail(c, GPET_ERR_ARG, "phantom material index out of range");
+    {
+        CK(c->d_prmap.ensure((size_t)n));
+        CK(c->d_prmap2.ensure((size_t)n));
+        int8_t* m[2] = {c->d_prmap.as<int8_t>(), c->d_prmap2.as<int8_t>()};
+        // kPrMax - 1 passes after the first: the last one lands in d_prmap
+        int cur = (kPrMax - 1) % 2;
+        const dim3 pb(32, 8, 1), pg((dims[0] + 31) / 32, (dims[1] + 7) / 8, std::min(dims[2], 65535));
+        k_prmap_init<<<pg, pb, 0, c->stream>>>(c->d_den_stage.as<float>(), dims[0], dims[1], dims[2], m[cur]);
+        CK(cudaGetLastError());
+        for (int p = 1; p < kPrMax; ++p) {
+            k_prmap_pass<<<pg, pb, 0, c->stream>>>(m[cur], dims[0], dims[1], dims[2], m[cur ^ 1]);
+            CK(cudaGetLastError());
+            cur ^= 1;
+        }
+    }
     float maxden[10] = {0};
     for (int m = 0; m < 10 && m < c->tab.nmat; ++m) std::memcpy(&maxden[m], &h[m], 4);
     for (int k = 0; k < 3; ++k) { c->pdim[k] = dims[k]; c->poff[k] = offset[k]; c->psz[k] = size[k]; }
@@ -768,6 +847,8 @@ static int build_sim(gpet_ctx* c)
     S.offx = c->poff[0]; S.offy = c->poff[1]; S.offz = c->poff[2];
     S.vox = c->vox_pal ? c->d_pal.as<uint2>() : c->d_vox.as<uint2>();
     S.vox16 = c->vox_pal ? c->d_vox16.as<uint16_t>() : nullptr;
+    S.prmap = c->d_prmap.as<int8_t>();
+    S.prdmin = std::fmin(S.dx, std::fmin(S.dy, S.dz));
     S.npanels = c->geo.npanels;
     S.panels = c->d_panels.as<float>();
     S.ndetmat = c->geo.ndetmat;
@@ -1069,7 +1150,7 @@ struct ChunkLaunch {
     size_t smem;
     int32_t nwaves;
     int32_t multi;
-    uint32_t src_blocks, src_threads, ph_blocks;
+    uint32_t src_blocks, src_threads, ph_blocks, walk_blocks;
     int32_t period;
     int32_t graph;
 };
@@ -1079,12 +1160,13 @@ static cudaError_t enqueue_chunk(const ChunkLaunch& L, cudaStream_t s)
     const unsigned flag = L.graph ? cudaEventRecordExternal : cudaEventRecordDefault;
     cudaError_t e;
     if ((e = cudaMemsetAsync(L.qcount, 0, 8, s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(L.d_work, 0, 8 * (size_t)L.nwaves, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(L.d_work, 0, 16 * (size_t)L.nwaves, s)) != cudaSuccess) return e;
     for (int k = 0; k < L.nwaves; ++k) {
         if ((e = cudaEventRecordWithFlags(L.ev[3 * k], s, flag)) != cudaSuccess) return e;
         if ((e = launch_source(L.multi != 0, L.src_blocks, L.src_threads, L.smem, s, L.d_waves, k, L.pb, L.dcnt)) !=
             cudaSuccess)
             return e;
+        if ((e = launch_walk(L.multi != 0, L.walk_blocks, s, L.d_waves, k, L.pb)) != cudaSuccess) return e;
         if ((e = cudaEventRecordWithFlags(L.ev[3 * k + 1], s, flag)) != cudaSuccess) return e;
         if ((e = launch_phantom(L.multi != 0, L.ph_blocks, L.smem, s, L.d_waves, k, L.pb, L.q, L.dcnt, L.period)) !=
             cudaSuccess)
@@ -1263,6 +1345,8 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         CK(W.pb_f.ensure((size_t)sub * 11 * 4));
         CK(W.pb_t.ensure((size_t)sub * 8));
         CK(W.pb_n.ensure((size_t)sub));
+        CK(W.pb_wf.ensure((size_t)sub * 7 * 4));
+        CK(W.pb_wj.ensure((size_t)sub * 4));
         W.pb_cap = sub;
     }
     int rc = grow_pulses(c, W, 1 << 20, 0);
@@ -1300,6 +1384,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     }
     PairBuf pb;
     pb.f = W.pb_f.as<float>(); pb.t = W.pb_t.as<double>(); pb.nph = W.pb_n.as<uint8_t>(); pb.cap = W.pb_cap;
+    pb.wf = W.pb_wf.as<float>(); pb.wj = W.pb_wj.as<int32_t>();
     Counters* dcnt = W.cnt.as<Counters>();
     unsigned long long* pcount = W.aux.as<unsigned long long>() + 1;
     unsigned long long* hcount = W.aux.as<unsigned long long>() + 2;
@@ -1317,6 +1402,9 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
     unsigned long long* dtake = W.aux.as<unsigned long long>() + 8;
     bps = std::max(1, bps);
     if (c->phantom_bps > 0) bps = std::min(bps, c->phantom_bps);
+    int walk_bps = 0;
+    CK(walk_blocks_per_sm(multi, &walk_bps));
+    walk_bps = std::max(walk_bps, 1);
     const SimDesc* d_sims = W.sims.as<SimDesc>();
     // wave table and counters for the largest chunk
     size_t max_k = 1;
@@ -1328,7 +1416,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         w0 = w1;
     }
     CK(W.d_waves.ensure(max_k * sizeof(Wave)));
-    CK(W.d_work.ensure(max_k * 8));
+    CK(W.d_work.ensure(max_k * 16));
     if (W.h_waves_cap < max_k) {
         if (W.h_waves) cudaFreeHost(W.h_waves);
         W.h_waves = nullptr;
@@ -1371,7 +1459,8 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
             wave.sim = d_sim + woff_d0[w];
             wave.nseg = waves[w].nseg;
             wave.n = waves[w].n;
-            wave.work = W.d_work.as<unsigned long long>() + k;
+            wave.work = W.d_work.as<unsigned long long>() + 2 * k;
+            wave.walkn = W.d_work.as<unsigned long long>() + 2 * k + 1;
             wave.exits = rec_exits ? W.exits.as<ExitRec>() + 2 * (waves[w].g - cg0) : nullptr;
             wave.source = rec_source ? W.source.as<SrcRec>() + 2 * (waves[w].g - cg0) : nullptr;
         }
@@ -1398,11 +1487,12 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         L.src_blocks = (uint32_t)std::max<int64_t>(1, std::min<int64_t>((sub + c->src_threads - 1) / c->src_threads,
                                                                       (int64_t)nsm * 32));
         L.ph_blocks = (uint32_t)(bps * nsm);
+        L.walk_blocks = (uint32_t)(walk_bps * nsm);
         L.period = c->drain_period;
         L.graph = c->use_graphs ? 1 : 0;
         rc = launch_chunk(c, W, L, b);
         if (rc) return rc;
-        tot.kernel_launches += 2 * K;
+        tot.kernel_launches += 3 * K;
         CK(cudaEventRecord(c->qev[b], c->stream));
         unsigned long long hq3[3] = {0, 0, 0};   // queue, pulses and hits so far (lower bounds)
         CK(cudaMemcpyAsync(&hq3[0], qcount, 8, cudaMemcpyDeviceToHost, c->stream));

@@ -37,6 +37,7 @@ struct Wave {
     int32_t nseg;
     int64_t n;                    // decays in the wave
     unsigned long long* work;     // photon counter of k_phantom, zero at launch
+    unsigned long long* walkn;    // entries of the positron walk list, zero at launch
     ExitRec* exits;               // per photon of the wave, or NULL
     SrcRec* source;               // per photon of the wave, or NULL
 };
@@ -141,6 +142,8 @@ struct PairBuf {
     float* f;                     // [11][cap]: x, y, z, u0 (3), u1 (3), E0, E1
     double* t;                    // [cap]
     uint8_t* nph;                 // [cap]: photons emitted (0, 1 or 2)
+    float* wf;                    // walk list [7][cap]: start x, y, z, displacement (3), its length
+    int32_t* wj;                  // walk list [cap]: the decay's index within the wave
     int64_t cap;
 };
 
@@ -161,6 +164,9 @@ __global__ void k_detector(const SimDesc* sims, QueueDev q, PulseDev P, HitDev H
 // threads per block: a multiple of 32 up to 256 (k_phantom: 256)
 cudaError_t launch_source(bool multi, unsigned blocks, unsigned threads, size_t smem, cudaStream_t s,
                           const Wave* waves, int wi, const PairBuf& pb, Counters* cnt);
+// the wave's deferred positron-range walks (after k_source, before k_phantom)
+cudaError_t launch_walk(bool multi, unsigned blocks, cudaStream_t s, const Wave* waves, int wi, const PairBuf& pb);
+cudaError_t walk_blocks_per_sm(bool multi, int* blocks);
 cudaError_t launch_phantom(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const Wave* waves, int wi,
                            const PairBuf& pb, const QueueDev& q, Counters* cnt, int period);
 // entries: one record per queue entry (or NULL)

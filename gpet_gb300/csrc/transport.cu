@@ -74,11 +74,15 @@ __device__ __forceinline__ int seg_of(const SegSmem& sg, int64_t g)
 // in the H3 form: the decay's source is fixed by its index, its time is a
 // truncated exponential on [0, dt)); PSF records (setPositionForPhoton
 // :563-604, with the second photon's time set) when npsf > 0.
-// Returns how many photons of the pair exist (0, 1 or 2).
-__device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2])
+// Returns how many photons of the pair exist (0, 1 or 2). walk: the positron
+// range needs the voxel walk, which starts at the pair's position with
+// displacement wd[0..2] of length wd[3] (the pair's position is then its
+// start, and k_walk moves it).
+__device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2], bool& walk, float wd[4])
 {
     Stream st;
     st_init(st, S.key0, S.key1, kTagDecay, (uint64_t)d);
+    walk = false;
     if (S.npsf > 0) {
         const double* r = S.psf + 8 * d;
         if (S.psf_ptype == 1) {
@@ -90,7 +94,10 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2])
         float pos[3] = {(float)r[0], (float)r[1], (float)r[2]};
         float dir[3] = {(float)r[4], (float)r[5], (float)r[6]};
         float spare = 0.0f;
-        if (S.useprange) positron_range(S, pos, (float)r[7], dir, st, &spare);
+        if (S.useprange) {
+            wd[3] = prange_draw((float)r[7], dir, st, wd, &spare);
+            walk = !prange_uniform(S, pos, wd, wd[3]);
+        }
         make_pair(S, st, pos, r[3], ph, S.useprange ? &spare : nullptr);
         return 2;
     }
@@ -109,17 +116,19 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2])
     float spare = 0.0f;
     if (S.useprange) {
         float ek = sample_ek(S.iso_coef[si], st);
-        positron_range(S, pos, ek, nullptr, st, &spare);
+        wd[3] = prange_draw(ek, nullptr, st, wd, &spare);
+        walk = !prange_uniform(S, pos, wd, wd[3]);
     }
     make_pair(S, st, pos, t_us, ph, S.useprange ? &spare : nullptr);
     return 2;
 }
 
 // source stage: one thread per decay, the emitted pair (or PSF photon) goes
-// to a structure-of-arrays buffer sized to stay in L2. kMulti: the decays of a
-// wave belong to several simulations and each thread reads its own
-// simulation's descriptor; otherwise the one descriptor is staged in shared
-// memory.
+// to a structure-of-arrays buffer. kMulti: the decays of a wave belong to
+// several simulations and each thread reads its own simulation's descriptor;
+// otherwise the one descriptor is staged in shared memory. Decays whose
+// positron range needs the voxel walk are appended to the wave's walk list
+// (one atomic per warp) and their position is written by k_walk.
 template <bool kMulti>
 __global__ void __launch_bounds__(256, 5) k_source(const Wave* waves, int wi, PairBuf pb, Counters* cnt)
 {
@@ -130,24 +139,31 @@ __global__ void __launch_bounds__(256, 5) k_source(const Wave* waves, int wi, Pa
     if (!kMulti) load_sim(w.sims, sS, sP);
     load_segs(w, sg);
     __syncthreads();
+    const unsigned lt = lanemask_lt();
+    const int lane = threadIdx.x & 31;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     SimTally pairs;
+    // every lane of a warp runs the same iterations (base is block-uniform)
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < w.n; base += stride) {
         const int64_t j = base + threadIdx.x;
         int nph = 0;
         int sim = 0;
+        bool walk = false;
+        float wd[4];
+        Photon ph[2];
         if (j < w.n) {
             const int sgi = seg_of(sg, j);
             sim = sg.sim[sgi];
             const int64_t d = sg.d0[sgi] + (j - sg.g0[sgi]);
             const SimDesc& S = kMulti ? w.sims[sim] : sS;
-            Photon ph[2];
-            nph = sample_decay(S, d, ph);
+            nph = sample_decay(S, d, ph, walk, wd);
             pb.nph[j] = (uint8_t)nph;
             if (nph > 0) {
-                pb.f[0 * pb.cap + j] = ph[0].x[0];
-                pb.f[1 * pb.cap + j] = ph[0].x[1];
-                pb.f[2 * pb.cap + j] = ph[0].x[2];
+                if (!walk) {
+                    pb.f[0 * pb.cap + j] = ph[0].x[0];
+                    pb.f[1 * pb.cap + j] = ph[0].x[1];
+                    pb.f[2 * pb.cap + j] = ph[0].x[2];
+                }
                 pb.f[3 * pb.cap + j] = ph[0].u[0];
                 pb.f[4 * pb.cap + j] = ph[0].u[1];
                 pb.f[5 * pb.cap + j] = ph[0].u[2];
@@ -162,8 +178,90 @@ __global__ void __launch_bounds__(256, 5) k_source(const Wave* waves, int wi, Pa
             }
             pairs.add(cnt, CF(pairs), sim, nph == 2 ? 1u : 0u);
         }
+        const unsigned mw = __ballot_sync(0xffffffffu, walk);
+        if (mw) {
+            unsigned long long b = 0;
+            const int leader = __ffs(mw) - 1;
+            if (lane == leader) b = atomicAdd(w.walkn, (unsigned long long)__popc(mw));
+            b = __shfl_sync(0xffffffffu, b, leader);
+            if (walk) {
+                const unsigned long long k = b + __popc(mw & lt);
+                pb.wf[0 * pb.cap + k] = ph[0].x[0];
+                pb.wf[1 * pb.cap + k] = ph[0].x[1];
+                pb.wf[2 * pb.cap + k] = ph[0].x[2];
+                pb.wf[3 * pb.cap + k] = wd[0];
+                pb.wf[4 * pb.cap + k] = wd[1];
+                pb.wf[5 * pb.cap + k] = wd[2];
+                pb.wf[6 * pb.cap + k] = wd[3];
+                pb.wj[k] = (int32_t)j;
+            }
+        }
     }
     pairs.flush(cnt, CF(pairs));
+}
+
+// the positron-range walks k_source left (prange_walk_*): each lane walks one
+// positron at a time and takes the next of its stride as soon as its walk
+// ends, so a warp does not wait for its longest walk; the end point is the
+// pair's position in the pair buffer. Each lane holds the record of its next
+// walk, loaded while the current one runs: the list comes from DRAM, and a
+// refill that waited for it would stall the warp's other lanes on nearly
+// every step. At most one entry per decay of the wave, so the list never
+// overflows.
+template <bool kMulti>
+__global__ void __launch_bounds__(256) k_walk(const Wave* waves, int wi, PairBuf pb)
+{
+    const Wave w = waves[wi];
+    __shared__ SimDesc sS;
+    __shared__ SegSmem sg;
+    if (kMulti) {
+        load_segs(w, sg);
+    } else {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(w.sims);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(&sS);
+        for (int i = threadIdx.x; i < (int)(sizeof(SimDesc) / 4); i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const int64_t n = (int64_t)*w.walkn;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // the next walk's record
+    float nx[3], nd[3], nr = 0.0f;
+    int32_t nj = 0;
+    bool has_next = k < n;
+    auto fetch = [&]() {
+        nx[0] = pb.wf[0 * pb.cap + k]; nx[1] = pb.wf[1 * pb.cap + k]; nx[2] = pb.wf[2 * pb.cap + k];
+        nd[0] = pb.wf[3 * pb.cap + k]; nd[1] = pb.wf[4 * pb.cap + k]; nd[2] = pb.wf[5 * pb.cap + k];
+        nr = pb.wf[6 * pb.cap + k];
+        nj = pb.wj[k];
+    };
+    if (has_next) fetch();
+    k += stride;
+    const SimDesc* S = kMulti ? w.sims : &sS;
+    PWalk pw;
+    int32_t j = 0;
+    bool active = false;
+    for (;;) {
+        if (!active) {
+            if (!has_next) break;
+            j = nj;
+            const float x[3] = {nx[0], nx[1], nx[2]};
+            const float d[3] = {nd[0], nd[1], nd[2]};
+            const float r = nr;
+            has_next = k < n;
+            if (has_next) fetch();
+            k += stride;
+            if (kMulti) S = w.sims + sg.sim[seg_of(sg, j)];
+            active = prange_walk_init(*S, pw, x, d, r);
+        } else {
+            active = prange_walk_step(*S, pw);
+        }
+        if (!active) {
+            pb.f[0 * pb.cap + j] = pw.x[0];
+            pb.f[1 * pb.cap + j] = pw.x[1];
+            pb.f[2 * pb.cap + j] = pw.x[2];
+        }
+    }
 }
 
 // a photon that has left the phantom (or stopped), waiting for the panel search
@@ -771,6 +869,19 @@ cudaError_t launch_source(bool multi, unsigned blocks, unsigned threads, size_t 
     return cudaGetLastError();
 }
 
+cudaError_t launch_walk(bool multi, unsigned blocks, cudaStream_t s, const Wave* waves, int wi, const PairBuf& pb)
+{
+    if (multi) k_walk<true><<<blocks, 256, 0, s>>>(waves, wi, pb);
+    else k_walk<false><<<blocks, 256, 0, s>>>(waves, wi, pb);
+    return cudaGetLastError();
+}
+
+cudaError_t walk_blocks_per_sm(bool multi, int* blocks)
+{
+    return multi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_walk<true>, 256, 0)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_walk<false>, 256, 0);
+}
+
 cudaError_t launch_phantom(bool multi, unsigned blocks, size_t smem, cudaStream_t s, const Wave* waves, int wi,
                            const PairBuf& pb, const QueueDev& q, Counters* cnt, int period)
 {
@@ -824,6 +935,8 @@ cudaError_t transport_kernels_loadable()
 
 template __global__ void k_source<false>(const Wave*, int, PairBuf, Counters*);
 template __global__ void k_source<true>(const Wave*, int, PairBuf, Counters*);
+template __global__ void k_walk<false>(const Wave*, int, PairBuf);
+template __global__ void k_walk<true>(const Wave*, int, PairBuf);
 template __global__ void k_phantom<false>(const Wave*, int, PairBuf, QueueDev, Counters*, int);
 template __global__ void k_phantom<true>(const Wave*, int, PairBuf, QueueDev, Counters*, int);
 template __global__ void k_detector<false>(const SimDesc*, QueueDev, PulseDev, HitDev, int, Counters*, EntryRec*);

@@ -80,6 +80,7 @@ class _Scene(C.Structure):
         ("noise_lambda_us", C.c_float), ("noise_emean", C.c_float), ("noise_sigma", C.c_float),
         ("noise_interval_us", C.c_double), ("noise_t0_us", C.c_double), ("noise_t1_us", C.c_double),
         ("nxdet", C.c_int32), ("xdet_mat", C.c_int32 * 6), ("xdet_den", C.c_float * 6),
+        ("prmap", C.POINTER(C.c_int8)),
     ]
 
 
@@ -108,6 +109,7 @@ def lib(precision="fp64"):
         L.oracle_digitize.argtypes = [C.POINTER(_Scene), C.POINTER(_Event), C.POINTER(C.c_uint8),
                                       C.POINTER(C.c_uint8), C.c_int64, C.POINTER(_Result)]
         L.oracle_free_result.argtypes = [C.POINTER(_Result)]
+        L.oracle_build_prmap.argtypes = [C.POINTER(_Scene), C.POINTER(C.c_int8)]
         L.oracle_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.oracle_stream_words.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_int64,
                                           C.POINTER(C.c_uint32)]
@@ -198,6 +200,11 @@ class OracleScene:
         s.dz = F.f32(np.float32(cfg.psize[2]) / np.float32(cfg.pdim[2]))
         s.offx, s.offy, s.offz = cfg.poffset
         s.mat = self.mat.ctypes.data_as(_IP); s.den = self.den.ctypes.data_as(_FP)
+        # the uniform-density map of the positron range's closed form (the
+        # same map the library builds at phantom upload)
+        self.prmap = np.empty(int(np.prod(cfg.pdim)), np.int8)
+        lib().oracle_build_prmap(C.byref(s), self.prmap.ctypes.data_as(C.POINTER(C.c_int8)))
+        s.prmap = self.prmap.ctypes.data_as(C.POINTER(C.c_int8))
         s.npanels = geo.npanels; s.panels = self.panels.ctypes.data_as(_FP)
         s.det_mat[0], s.det_mat[1] = geo.det_mat[:2]
         s.det_den[0], s.det_den[1] = geo.det_den[:2]

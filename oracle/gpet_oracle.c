@@ -379,6 +379,104 @@ static real sample_ek(const or_scene* sc, int type, stream_t* st)
     return (e - (real)0.511) * (real)1.0e6;
 }
 
+/* The positron-range walk below ends where the density-weighted path length
+ * reaches r. Where every voxel it reads has one density rho, that end point
+ * is x + (r / rho) * d / r exactly; the walk reads voxels within
+ * floor(L / dmin) + 2 (Chebyshev) of its start voxel, L = r / rho (the end
+ * voxel and the one entered beyond it). The map holds, per voxel, the largest
+ * R <= OR_PRMAX such that all voxels within R have its density (same float
+ * bits) and lie in [1, n-2] on every axis (-1 where the voxel itself does
+ * not), so with L < (R - 1.5) * dmin the closed form replaces the walk. The
+ * CUDA kernels take the same closed form under the same test, so both give
+ * the same end point bit for bit; against the reference's walk it differs by
+ * rounding only. */
+#define OR_PRMAX 6
+
+static inline int pr_interior(int x, int y, int z, int nx, int ny, int nz)
+{
+    return x >= 1 && x <= nx - 2 && y >= 1 && y <= ny - 2 && z >= 1 && z <= nz - 2;
+}
+
+/* the map of the scene's phantom into out[nx*ny*nz]: Jacobi passes of
+ * m(v) = 1 + min over the 26 neighbours, valid where v and its neighbours
+ * are in range and of one density (the ball of radius R around v is the union
+ * of the balls of radius R-1 around its neighbours) */
+void oracle_build_prmap(const or_scene* sc, int8_t* out)
+{
+    const int nx = sc->nx, ny = sc->ny, nz = sc->nz;
+    const int64_t n = (int64_t)nx * ny * nz;
+    int8_t* tmp = (int8_t*)malloc((size_t)n);
+    int8_t* m[2] = {out, tmp};
+    int cur = (OR_PRMAX - 1) % 2;
+    #pragma omp parallel for schedule(static)
+    for (int64_t v = 0; v < n; ++v) {
+        const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / ((int64_t)nx * ny));
+        int8_t r = -1;
+        if (pr_interior(x, y, z, nx, ny, nz)) {
+            uint32_t b;
+            memcpy(&b, sc->den + v, 4);
+            r = 1;
+            for (int dz = -1; dz <= 1 && r; ++dz)
+                for (int dy = -1; dy <= 1 && r; ++dy)
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        uint32_t q;
+                        memcpy(&q, sc->den + v + dx + (int64_t)nx * (dy + (int64_t)ny * dz), 4);
+                        if (!pr_interior(x + dx, y + dy, z + dz, nx, ny, nz) || q != b) { r = 0; break; }
+                    }
+        }
+        m[cur][v] = r;
+    }
+    for (int pass = 1; pass < OR_PRMAX; ++pass) {
+        const int8_t* m0 = m[cur];
+        int8_t* m1 = m[cur ^ 1];
+        #pragma omp parallel for schedule(static)
+        for (int64_t v = 0; v < n; ++v) {
+            int r = m0[v];
+            if (r >= 1) {
+                const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / ((int64_t)nx * ny));
+                int mn = OR_PRMAX;
+                for (int dz = -1; dz <= 1; ++dz)
+                    for (int dy = -1; dy <= 1; ++dy)
+                        for (int dx = -1; dx <= 1; ++dx) {
+                            if ((dx | dy | dz) == 0) continue;
+                            int q = m0[(int64_t)(x + dx) + (int64_t)nx * ((y + dy) + (int64_t)ny * (z + dz))];
+                            if (q < mn) mn = q;
+                        }
+                r = mn + 1 < OR_PRMAX ? mn + 1 : OR_PRMAX;
+            }
+            m1[v] = (int8_t)r;
+        }
+        cur ^= 1;
+    }
+    free(tmp);
+}
+
+/* the closed form above; returns 0 (x unchanged) where the walk is needed.
+ * A zero displacement moves nothing, as in the walk. */
+static int prange_uniform(const or_scene* sc, real x[3], const real d[3], real r)
+{
+    if (!(r > (real)0.0)) return 1;
+    if (!sc->prmap) return 0;
+    int ix, iy, iz;
+    if (!abs_vox(sc, (real)(1.0f / sc->dx), (real)(1.0f / sc->dy), (real)(1.0f / sc->dz), x[0], x[1], x[2],
+                 &ix, &iy, &iz))
+        return 0;
+    const size_t i = (size_t)ix + (size_t)sc->nx * ((size_t)iy + (size_t)sc->ny * iz);
+    const int R = sc->prmap[i];
+    if (R < 2) return 0;
+    const real rho = (real)sc->den[i];
+    if (!(rho > (real)0.0)) return 0;
+    const real L = r / rho;
+    const real dmin = (real)fminf(sc->dx, fminf(sc->dy, sc->dz));
+    if (!(L < ((real)R - (real)1.5) * dmin)) return 0;
+    const real ir = (real)1.0 / r;
+    const real dn0 = d[0] * ir, dn1 = d[1] * ir, dn2 = d[2] * ir;
+    x[0] = x[0] + L * dn0;
+    x[1] = x[1] + L * dn1;
+    x[2] = x[2] + L * dn2;
+    return 1;
+}
+
 /* setPositronRange, gPET_kernals.cu:347-418: Gaussian displacement with
  * sigma = Rex/2 (Rex from a water fit), walked through voxels so that the
  * density-weighted length equals r. The density is read from the voxel being
@@ -409,6 +507,7 @@ static void positron_range(const or_scene* sc, real x[3], real ek, const real* d
         real tmp = R_SQRT(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
         d[0] = r * dir[0] / tmp; d[1] = r * dir[1] / tmp; d[2] = r * dir[2] / tmp;
     }
+    if (prange_uniform(sc, x, d, r)) return;
     /* the walk multiplies by reciprocals computed once */
     const real id0 = (real)1.0 / d[0], id1 = (real)1.0 / d[1], id2 = (real)1.0 / d[2];
     const real ir = (real)1.0 / r;

@@ -92,6 +92,9 @@ typedef struct {
     int32_t nxdet;
     int32_t xdet_mat[6];
     float xdet_den[6];
+    /* uniform-density map of the positron range (oracle_build_prmap), or
+     * NULL: every positron walks */
+    const int8_t* prmap;
 } or_scene;
 
 typedef struct {

@@ -1,0 +1,105 @@
+"""The positron range's closed form for walks in voxels of one density.
+
+setPositronRange (gPET_kernals.cu:347-418) walks a positron through the
+voxels until the density-weighted path length reaches the sampled range r.
+Where every voxel the walk reads has one density rho, its end point is
+x + (r / rho) * d / r, and both the oracle and the CUDA kernels take that
+closed form instead of the walk when a per-voxel map says the voxels within
+reach are uniform. These CPU tests check the map against its definition by
+brute force and the closed form against the full walk on the same random
+words (the oracle's FP32 build, which the kernels match bit for bit)."""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "oracle", "ref"))
+
+PRMAX = 6
+
+
+def _map_by_definition(den):
+    """R = the largest radius <= PRMAX such that every voxel within that
+    Chebyshev distance has the voxel's density bits and lies in [1, n-2] on
+    every axis; -1 where the voxel itself is outside that range."""
+    nz, ny, nx = den.shape
+    bits = den.view(np.uint32)
+    out = np.full(den.shape, -1, np.int8)
+    for z in range(1, nz - 1):
+        for y in range(1, ny - 1):
+            for x in range(1, nx - 1):
+                r = 0
+                for k in range(1, PRMAX + 1):
+                    if x - k < 1 or y - k < 1 or z - k < 1 or x + k > nx - 2 or y + k > ny - 2 or z + k > nz - 2:
+                        break
+                    cube = bits[z - k:z + k + 1, y - k:y + k + 1, x - k:x + k + 1]
+                    if not np.all(cube == bits[z, y, x]):
+                        break
+                    r = k
+                out[z, y, x] = r
+    return out
+
+
+def test_map_matches_its_definition(oracle_mod):
+    rng = np.random.default_rng(7)
+    nz, ny, nx = 17, 19, 23
+    den = np.ones((nz, ny, nx), np.float32)
+    for _ in range(5):   # boxes of other densities
+        z0, y0, x0 = rng.integers(0, [nz, ny, nx])
+        dz, dy, dx = rng.integers(1, 7, 3)
+        den[z0:z0 + dz, y0:y0 + dy, x0:x0 + dx] = rng.choice([0.3, 1.85, 1.0000001])
+    den[3, 17, 5] = -0.0   # same value as 0.0, other bits: not uniform with a 0.0 neighbour
+    s = oracle_mod._Scene()
+    s.nx, s.ny, s.nz = nx, ny, nz
+    s.den = den.ctypes.data_as(C.POINTER(C.c_float))
+    got = np.empty(den.size, np.int8)
+    oracle_mod.lib().oracle_build_prmap(C.byref(s), got.ctypes.data_as(C.POINTER(C.c_int8)))
+    want = _map_by_definition(den)
+    assert np.array_equal(got.reshape(den.shape), want)
+    assert (want >= 2).sum() > 100 and (want == 0).sum() > 100
+
+
+@pytest.mark.parametrize("nvox", [48, 128])
+def test_closed_form_equals_walk(oracle_mod, data_dir, tmp_path, nvox):
+    """On the positron workload's phantom (water, bone rods, lung sphere),
+    positrons of the F-18 range started all over the source cylinder end where
+    the full walk ends them, to the rounding of the walk's steps, with the
+    same random words; most of them take the closed form."""
+    import pins
+    from gpet_gb300 import scenes
+    sc = scenes.positron(str(tmp_path), n_decays=1000, nvox=nvox)
+    o = oracle_mod.OracleScene(sc.config_path, sc.options, data_dir, base_dir=sc.directory)
+    with_map = o.s
+    without = oracle_mod._Scene.from_buffer_copy(o.s)
+    without.prmap = C.POINTER(C.c_int8)()
+    L = pins.oracle_lib()
+    rng = np.random.default_rng(11)
+    n = 4000
+    rr = 3.0 * np.sqrt(rng.random(n))
+    ph = 2 * np.pi * rng.random(n)
+    x = np.stack([rr * np.cos(ph), rr * np.sin(ph), 6.0 * (rng.random(n) - 0.5)], 1).astype(np.float32)
+    ek = rng.random(n) * 633e3
+    tape = rng.integers(1, 2 ** 32 - 1, size=(n, pins.TAPE), dtype=np.uint64).astype(np.uint32)
+    ends = {}
+    for name, S in (("map", with_map), ("walk", without)):
+        out = np.zeros((n, 3))
+        used = np.zeros(n, np.int64)
+        u = C.c_int64()
+        for i in range(n):
+            L.oracle_tape_positron_range(C.byref(S), pins._p(np.ascontiguousarray(x[i]), pins._FP), float(ek[i]),
+                                         None, pins._p(np.ascontiguousarray(tape[i]), pins._UP), pins.TAPE,
+                                         pins._p(out[i], pins._DP), C.byref(u))
+            used[i] = u.value
+        ends[name] = (out, used)
+    assert np.array_equal(ends["map"][1], ends["walk"][1])
+    dist = np.linalg.norm(ends["map"][0] - ends["walk"][0], axis=1)
+    assert dist.max() < 2e-6
+    moved = np.linalg.norm(ends["walk"][0] - x, axis=1)
+    assert np.median(moved) > 0.01                    # ranges of a fraction of a millimetre
+    exact = dist == 0.0
+    assert exact.mean() < 0.9                          # most positrons took the closed form (not bit-equal)
+    prmap = o.prmap.reshape(nvox, nvox, nvox)
+    assert (prmap >= 2).mean() > 0.5
