@@ -261,9 +261,10 @@ __device__ __forceinline__ bool abs_vox(const SimDesc& S, float x, float y, floa
     return in;
 }
 
+// (ix, iy, iz) in range; a phantom holds fewer than 2^31 voxels
 __device__ __forceinline__ uint2 voxel(const SimDesc& S, int ix, int iy, int iz)
 {
-    const size_t i = (size_t)ix + (size_t)S.nx * ((size_t)iy + (size_t)S.ny * iz);
+    const uint32_t i = (uint32_t)ix + (uint32_t)S.nx * ((uint32_t)iy + (uint32_t)S.ny * (uint32_t)iz);
     if (S.vox16) return __ldg(S.vox + __ldg(S.vox16 + i));
     return __ldg(S.vox + i);
 }
@@ -366,21 +367,28 @@ __device__ __forceinline__ float prange_draw(float ek, const float* dir, Stream&
 // start voxel, L = r / rho (the end voxel, plus the voxel entered beyond it);
 // prmap[v] = R says that all voxels within R of v have v's density and lie in
 // [1, n-2] on every axis, so L < (R - 1.5) * dmin (half a voxel of margin)
-// keeps the walk inside. Returns false (x unchanged) where the walk is needed.
-// A zero displacement moves nothing, as in the walk.
-__device__ __forceinline__ bool prange_uniform(const SimDesc& S, float x[3], const float d[3], float r)
+// keeps the walk inside. Returns false (x unchanged) where the walk is needed,
+// with est = sum |d_k| / (rho * dmin), about the number of voxel faces the walk
+// crosses at the start voxel's density (0 outside the phantom, where it takes
+// one step). A zero displacement moves nothing, as in the walk.
+__device__ __forceinline__ bool prange_uniform(const SimDesc& S, float x[3], const float d[3], float r, float& est)
 {
+    est = 0.0f;
     if (!(r > 0.0f)) return true;
-    if (!S.prmap) return false;
     int ix, iy, iz;
     if (!abs_vox(S, x[0], x[1], x[2], ix, iy, iz)) return false;
-    const size_t i = (size_t)ix + (size_t)S.nx * ((size_t)iy + (size_t)S.ny * iz);
-    const int R = __ldg(S.prmap + i);
-    if (R < 2) return false;
+    const uint32_t i = (uint32_t)ix + (uint32_t)S.nx * ((uint32_t)iy + (uint32_t)S.ny * (uint32_t)iz);
+    const int R = S.prmap ? __ldg(S.prmap + i) : 0;
     const float rho = __uint_as_float(voxel(S, ix, iy, iz).x);
-    if (!(rho > 0.0f)) return false;
+    if (!(rho > 0.0f)) {
+        est = 1.0e30f;
+        return false;
+    }
     const float L = r / rho;
-    if (!(L < ((float)R - 1.5f) * S.prdmin)) return false;
+    if (R < 2 || !(L < ((float)R - 1.5f) * S.prdmin)) {
+        est = (fabsf(d[0]) + fabsf(d[1]) + fabsf(d[2])) / (rho * S.prdmin);
+        return false;
+    }
     const float ir = 1.0f / r;
     const float dn0 = d[0] * ir, dn1 = d[1] * ir, dn2 = d[2] * ir;
     x[0] = x[0] + L * dn0;
@@ -392,6 +400,7 @@ __device__ __forceinline__ bool prange_uniform(const SimDesc& S, float x[3], con
 // state of one voxel walk
 struct PWalk {
     float x[3], id[3], dn[3], r, s;
+    float xmax, ymax, zmax;       // far faces of the phantom
     int v[3];
     int guard;
     int pos;                      // bit k: d[k] > 0
@@ -408,6 +417,9 @@ __device__ __forceinline__ bool prange_walk_init(const SimDesc& S, PWalk& w, con
     w.dn[0] = d[0] * ir; w.dn[1] = d[1] * ir; w.dn[2] = d[2] * ir;
     w.pos = (d[0] > 0.0f ? 1 : 0) | (d[1] > 0.0f ? 2 : 0) | (d[2] > 0.0f ? 4 : 0);
     w.x[0] = x[0]; w.x[1] = x[1]; w.x[2] = x[2];
+    w.xmax = S.offx + (float)S.nx * S.dx;
+    w.ymax = S.offy + (float)S.ny * S.dy;
+    w.zmax = S.offz + (float)S.nz * S.dz;
     w.inside = abs_vox(S, x[0], x[1], x[2], w.v[0], w.v[1], w.v[2]);
     if (!w.inside) { w.v[0] = w.v[1] = w.v[2] = 0; }
     w.r = r;
@@ -443,12 +455,9 @@ __device__ __forceinline__ bool prange_walk_step(const SimDesc& S, PWalk& w)
     w.x[0] += step * w.dn[0];
     w.x[1] += step * w.dn[1];
     w.x[2] += step * w.dn[2];
-    const float xmax = S.offx + (float)S.nx * S.dx;
-    const float ymax = S.offy + (float)S.ny * S.dy;
-    const float zmax = S.offz + (float)S.nz * S.dz;
-    if (w.x[0] < S.offx || w.x[0] > xmax) w.inside = false;
-    if (w.x[1] < S.offy || w.x[1] > ymax) w.inside = false;
-    if (w.x[2] < S.offz || w.x[2] > zmax) w.inside = false;
+    if (w.x[0] < S.offx || w.x[0] > w.xmax) w.inside = false;
+    if (w.x[1] < S.offy || w.x[1] > w.ymax) w.inside = false;
+    if (w.x[2] < S.offz || w.x[2] > w.zmax) w.inside = false;
     ++w.guard;
     return w.s < w.r && w.guard < 100000;
 }

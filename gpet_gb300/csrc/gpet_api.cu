@@ -591,6 +591,8 @@ int gpet_set_phantom(gpet_ctx* c, const int32_t* mat, const float* den, const in
     if (!c || !mat || !den || !dims || !offset || !size) return GPET_ERR_ARG;
     if (!c->have_tables) return fail(c, GPET_ERR_ARG, "load the tables before the phantom");
     if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1) return fail(c, GPET_ERR_ARG, "phantom dimensions must be >= 1");
+    if ((int64_t)dims[0] * dims[1] * dims[2] > INT32_MAX)
+        return fail(c, GPET_ERR_ARG, "a phantom holds at most 2^31 - 1 voxels");
     CK(cudaSetDevice(c->device));
     const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
     // the caller's arrays go to the device as they are (a DMA when the caller's
@@ -1160,7 +1162,7 @@ static cudaError_t enqueue_chunk(const ChunkLaunch& L, cudaStream_t s)
     const unsigned flag = L.graph ? cudaEventRecordExternal : cudaEventRecordDefault;
     cudaError_t e;
     if ((e = cudaMemsetAsync(L.qcount, 0, 8, s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(L.d_work, 0, 16 * (size_t)L.nwaves, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(L.d_work, 0, 64 * (size_t)L.nwaves, s)) != cudaSuccess) return e;
     for (int k = 0; k < L.nwaves; ++k) {
         if ((e = cudaEventRecordWithFlags(L.ev[3 * k], s, flag)) != cudaSuccess) return e;
         if ((e = launch_source(L.multi != 0, L.src_blocks, L.src_threads, L.smem, s, L.d_waves, k, L.pb, L.dcnt)) !=
@@ -1345,8 +1347,8 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         CK(W.pb_f.ensure((size_t)sub * 11 * 4));
         CK(W.pb_t.ensure((size_t)sub * 8));
         CK(W.pb_n.ensure((size_t)sub));
-        CK(W.pb_wf.ensure((size_t)sub * 7 * 4));
-        CK(W.pb_wj.ensure((size_t)sub * 4));
+        CK(W.pb_wf.ensure((size_t)sub * kWalkLists * 7 * 4));
+        CK(W.pb_wj.ensure((size_t)sub * kWalkLists * 4));
         W.pb_cap = sub;
     }
     int rc = grow_pulses(c, W, 1 << 20, 0);
@@ -1416,7 +1418,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         w0 = w1;
     }
     CK(W.d_waves.ensure(max_k * sizeof(Wave)));
-    CK(W.d_work.ensure(max_k * 16));
+    CK(W.d_work.ensure(max_k * 64));
     if (W.h_waves_cap < max_k) {
         if (W.h_waves) cudaFreeHost(W.h_waves);
         W.h_waves = nullptr;
@@ -1459,8 +1461,8 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
             wave.sim = d_sim + woff_d0[w];
             wave.nseg = waves[w].nseg;
             wave.n = waves[w].n;
-            wave.work = W.d_work.as<unsigned long long>() + 2 * k;
-            wave.walkn = W.d_work.as<unsigned long long>() + 2 * k + 1;
+            wave.work = W.d_work.as<unsigned long long>() + 8 * k;          // 8 counters per wave:
+            wave.walkn = W.d_work.as<unsigned long long>() + 8 * k + 1;     // photons, walk lists
             wave.exits = rec_exits ? W.exits.as<ExitRec>() + 2 * (waves[w].g - cg0) : nullptr;
             wave.source = rec_source ? W.source.as<SrcRec>() + 2 * (waves[w].g - cg0) : nullptr;
         }

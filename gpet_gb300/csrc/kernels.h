@@ -37,7 +37,7 @@ struct Wave {
     int32_t nseg;
     int64_t n;                    // decays in the wave
     unsigned long long* work;     // photon counter of k_phantom, zero at launch
-    unsigned long long* walkn;    // entries of the positron walk list, zero at launch
+    unsigned long long* walkn;    // [kWalkLists] entries of the positron walk lists, zero at launch
     ExitRec* exits;               // per photon of the wave, or NULL
     SrcRec* source;               // per photon of the wave, or NULL
 };
@@ -138,12 +138,14 @@ struct DigiParams {
 };
 
 // emitted pairs of a sub-chunk of decays, structure of arrays
+constexpr int kWalkLists = 4;    // positron walk lists by estimated length
+
 struct PairBuf {
     float* f;                     // [11][cap]: x, y, z, u0 (3), u1 (3), E0, E1
     double* t;                    // [cap]
     uint8_t* nph;                 // [cap]: photons emitted (0, 1 or 2)
-    float* wf;                    // walk list [7][cap]: start x, y, z, displacement (3), its length
-    int32_t* wj;                  // walk list [cap]: the decay's index within the wave
+    float* wf;                    // walk lists [kWalkLists][7][cap]: start x, y, z, displacement (3), its length
+    int32_t* wj;                  // walk lists [kWalkLists][cap]: the decay's index within the wave
     int64_t cap;
 };
 

@@ -76,9 +76,9 @@ __device__ __forceinline__ int seg_of(const SegSmem& sg, int64_t g)
 // :563-604, with the second photon's time set) when npsf > 0.
 // Returns how many photons of the pair exist (0, 1 or 2). walk: the positron
 // range needs the voxel walk, which starts at the pair's position with
-// displacement wd[0..2] of length wd[3] (the pair's position is then its
-// start, and k_walk moves it).
-__device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2], bool& walk, float wd[4])
+// displacement wd[0..2] of length wd[3] and about wd[4] steps (the pair's
+// position is then its start, and k_walk moves it).
+__device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2], bool& walk, float wd[5])
 {
     Stream st;
     st_init(st, S.key0, S.key1, kTagDecay, (uint64_t)d);
@@ -96,7 +96,7 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2], bool& wal
         float spare = 0.0f;
         if (S.useprange) {
             wd[3] = prange_draw((float)r[7], dir, st, wd, &spare);
-            walk = !prange_uniform(S, pos, wd, wd[3]);
+            walk = !prange_uniform(S, pos, wd, wd[3], wd[4]);
         }
         make_pair(S, st, pos, r[3], ph, S.useprange ? &spare : nullptr);
         return 2;
@@ -117,7 +117,7 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2], bool& wal
     if (S.useprange) {
         float ek = sample_ek(S.iso_coef[si], st);
         wd[3] = prange_draw(ek, nullptr, st, wd, &spare);
-        walk = !prange_uniform(S, pos, wd, wd[3]);
+        walk = !prange_uniform(S, pos, wd, wd[3], wd[4]);
     }
     make_pair(S, st, pos, t_us, ph, S.useprange ? &spare : nullptr);
     return 2;
@@ -127,8 +127,14 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2], bool& wal
 // to a structure-of-arrays buffer. kMulti: the decays of a wave belong to
 // several simulations and each thread reads its own simulation's descriptor;
 // otherwise the one descriptor is staged in shared memory. Decays whose
-// positron range needs the voxel walk are appended to the wave's walk list
-// (one atomic per warp) and their position is written by k_walk.
+// positron range needs the voxel walk are appended to one of the wave's
+// kWalkLists walk lists by their estimated number of steps (one atomic per
+// warp and list), and their position is written by k_walk.
+__device__ __forceinline__ int walk_list(float est)
+{
+    return est < 1.5f ? 0 : (est < 3.0f ? 1 : (est < 6.0f ? 2 : 3));
+}
+
 template <bool kMulti>
 __global__ void __launch_bounds__(256, 5) k_source(const Wave* waves, int wi, PairBuf pb, Counters* cnt)
 {
@@ -149,7 +155,7 @@ __global__ void __launch_bounds__(256, 5) k_source(const Wave* waves, int wi, Pa
         int nph = 0;
         int sim = 0;
         bool walk = false;
-        float wd[4];
+        float wd[5];
         Photon ph[2];
         if (j < w.n) {
             const int sgi = seg_of(sg, j);
@@ -178,36 +184,38 @@ __global__ void __launch_bounds__(256, 5) k_source(const Wave* waves, int wi, Pa
             }
             pairs.add(cnt, CF(pairs), sim, nph == 2 ? 1u : 0u);
         }
-        const unsigned mw = __ballot_sync(0xffffffffu, walk);
-        if (mw) {
-            unsigned long long b = 0;
-            const int leader = __ffs(mw) - 1;
-            if (lane == leader) b = atomicAdd(w.walkn, (unsigned long long)__popc(mw));
-            b = __shfl_sync(0xffffffffu, b, leader);
+        if (__any_sync(0xffffffffu, walk)) {
+            // lanes of one list take consecutive entries (one atomic per list)
+            const int wl = walk ? walk_list(wd[4]) : -1;
+            const unsigned grp = __match_any_sync(0xffffffffu, wl);
             if (walk) {
-                const unsigned long long k = b + __popc(mw & lt);
-                pb.wf[0 * pb.cap + k] = ph[0].x[0];
-                pb.wf[1 * pb.cap + k] = ph[0].x[1];
-                pb.wf[2 * pb.cap + k] = ph[0].x[2];
-                pb.wf[3 * pb.cap + k] = wd[0];
-                pb.wf[4 * pb.cap + k] = wd[1];
-                pb.wf[5 * pb.cap + k] = wd[2];
-                pb.wf[6 * pb.cap + k] = wd[3];
-                pb.wj[k] = (int32_t)j;
+                const int leader = __ffs(grp) - 1;
+                unsigned long long base_k = 0;
+                if (lane == leader) base_k = atomicAdd(w.walkn + wl, (unsigned long long)__popc(grp));
+                base_k = __shfl_sync(grp, base_k, leader);
+                const unsigned long long k = base_k + __popc(grp & lt);
+                float* wf = pb.wf + (size_t)wl * 7 * pb.cap;
+                wf[0 * pb.cap + k] = ph[0].x[0];
+                wf[1 * pb.cap + k] = ph[0].x[1];
+                wf[2 * pb.cap + k] = ph[0].x[2];
+                wf[3 * pb.cap + k] = wd[0];
+                wf[4 * pb.cap + k] = wd[1];
+                wf[5 * pb.cap + k] = wd[2];
+                wf[6 * pb.cap + k] = wd[3];
+                pb.wj[(size_t)wl * pb.cap + k] = (int32_t)j;
             }
         }
     }
     pairs.flush(cnt, CF(pairs));
 }
 
-// the positron-range walks k_source left (prange_walk_*): each lane walks one
-// positron at a time and takes the next of its stride as soon as its walk
-// ends, so a warp does not wait for its longest walk; the end point is the
-// pair's position in the pair buffer. Each lane holds the record of its next
-// walk, loaded while the current one runs: the list comes from DRAM, and a
-// refill that waited for it would stall the warp's other lanes on nearly
-// every step. At most one entry per decay of the wave, so the list never
-// overflows.
+// the positron-range walks k_source left (prange_walk_*), list by list: a
+// lane walks one positron to its end; the lists hold walks of similar
+// estimated length, so the lanes of a warp finish at about the same step
+// (a refill as soon as a lane's walk ends put the refill and the step on
+// separate paths of the warp at nearly every step). The end point is the
+// pair's position in the pair buffer. At most one entry per decay of the
+// wave in each list, so no list overflows.
 template <bool kMulti>
 __global__ void __launch_bounds__(256) k_walk(const Wave* waves, int wi, PairBuf pb)
 {
@@ -222,41 +230,21 @@ __global__ void __launch_bounds__(256) k_walk(const Wave* waves, int wi, PairBuf
         for (int i = threadIdx.x; i < (int)(sizeof(SimDesc) / 4); i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
-    const int64_t n = (int64_t)*w.walkn;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    // the next walk's record
-    float nx[3], nd[3], nr = 0.0f;
-    int32_t nj = 0;
-    bool has_next = k < n;
-    auto fetch = [&]() {
-        nx[0] = pb.wf[0 * pb.cap + k]; nx[1] = pb.wf[1 * pb.cap + k]; nx[2] = pb.wf[2 * pb.cap + k];
-        nd[0] = pb.wf[3 * pb.cap + k]; nd[1] = pb.wf[4 * pb.cap + k]; nd[2] = pb.wf[5 * pb.cap + k];
-        nr = pb.wf[6 * pb.cap + k];
-        nj = pb.wj[k];
-    };
-    if (has_next) fetch();
-    k += stride;
-    const SimDesc* S = kMulti ? w.sims : &sS;
-    PWalk pw;
-    int32_t j = 0;
-    bool active = false;
-    for (;;) {
-        if (!active) {
-            if (!has_next) break;
-            j = nj;
-            const float x[3] = {nx[0], nx[1], nx[2]};
-            const float d[3] = {nd[0], nd[1], nd[2]};
-            const float r = nr;
-            has_next = k < n;
-            if (has_next) fetch();
-            k += stride;
-            if (kMulti) S = w.sims + sg.sim[seg_of(sg, j)];
-            active = prange_walk_init(*S, pw, x, d, r);
-        } else {
-            active = prange_walk_step(*S, pw);
-        }
-        if (!active) {
+    for (int b = 0; b < kWalkLists; ++b) {
+        const int64_t n = (int64_t)w.walkn[b];
+        const float* wf = pb.wf + (size_t)b * 7 * pb.cap;
+        const int32_t* wj = pb.wj + (size_t)b * pb.cap;
+        for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+            const int32_t j = wj[k];
+            const float x[3] = {wf[0 * pb.cap + k], wf[1 * pb.cap + k], wf[2 * pb.cap + k]};
+            const float d[3] = {wf[3 * pb.cap + k], wf[4 * pb.cap + k], wf[5 * pb.cap + k]};
+            const float r = wf[6 * pb.cap + k];
+            const SimDesc* S = kMulti ? w.sims + sg.sim[seg_of(sg, j)] : &sS;
+            PWalk pw;
+            if (prange_walk_init(*S, pw, x, d, r))
+                while (prange_walk_step(*S, pw)) {
+                }
             pb.f[0 * pb.cap + j] = pw.x[0];
             pb.f[1 * pb.cap + j] = pw.x[1];
             pb.f[2 * pb.cap + j] = pw.x[2];
