@@ -265,6 +265,7 @@ struct FinRec {
 static_assert(sizeof(FinRec) == 40, "staged record");
 
 constexpr int kPhWarps = 8;      // warps per k_phantom block (256 threads)
+constexpr uint32_t kClaim = 64;  // photons a k_phantom warp claims at a time
 constexpr int kFinCap = 64;      // finished photons staged per warp
 
 // phantom stage: persistent warps; a lane whose photon has left the phantom
@@ -376,18 +377,49 @@ __global__ void __launch_bounds__(256, 5) k_phantom(const Wave* waves, int wi, P
     // key), seeded when the lane takes the photon
     uint32_t rst[4] = {0u, 0u, 0u, 0u};
     auto unif = [&]() -> float { return dm_u01(xo_next(rst)); };
+    // The warp claims photons kClaim at a time, one block ahead of the lanes
+    // that take them, and has the next block's pair-buffer lines fetched
+    // into L2 when it claims it: a lane's refill then reads L2 instead of
+    // waiting for DRAM while its warp's other lanes wait for it.
+    // [cb, ce): the block lanes take photons from; nb: the next block.
+    auto claim = [&]() -> uint32_t {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(work, (unsigned long long)kClaim);
+        const uint32_t b = (uint32_t)__shfl_sync(0xffffffffu, t, 0);
+        if (b < (uint32_t)nphot && lane < 16) {
+            // decays [b/2, b/2 + kClaim/2) of the 11 float arrays, the
+            // emission times and the photon counts; both ends of each range
+            const int64_t j0 = b >> 1;
+            const int64_t j1 = min(j0 + kClaim / 2 - 1, w.n - 1);
+            const int a = lane < 11 ? lane : 0;
+            const void* p0 = lane < 11 ? (const void*)(pb.f + a * pb.cap + j0)
+                                       : (lane < 13 ? (const void*)(pb.t + j0) : (const void*)(pb.nph + j0));
+            const void* p1 = lane < 11 ? (const void*)(pb.f + a * pb.cap + j1)
+                                       : (lane < 13 ? (const void*)(pb.t + j1) : (const void*)(pb.nph + j1));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(lane == 11 || lane >= 13 ? p0 : p1));
+            if (lane < 11) asm volatile("prefetch.global.L2 [%0];" ::"l"(p0));
+        }
+        return b;
+    };
+    uint32_t cb = claim();
+    uint32_t ce = cb + kClaim;
+    uint32_t nb = claim();
     for (;;) {
-        // refill idle lanes, one atomic per warp
+        // refill idle lanes from the claimed blocks
         const bool need = !active && !exhausted;
         const unsigned mneed = __ballot_sync(0xffffffffu, need);
         if (mneed) {
-            unsigned long long b = 0;
-            const int leader = __ffs(mneed) - 1;
-            if (lane == leader) b = atomicAdd(work, (unsigned long long)__popc(mneed));
-            b = __shfl_sync(0xffffffffu, b, leader);
+            const uint32_t k = __popc(mneed), r = __popc(mneed & lt), avail = ce - cb;
+            const uint32_t pw = r < avail ? cb + r : nb + (r - avail);
+            if (k >= avail) {   // into the next block (k <= 32 <= kClaim): claim the one after it
+                cb = nb + (k - avail);
+                ce = nb + kClaim;
+                nb = claim();
+            } else {
+                cb += k;
+            }
             if (need) {
-                const unsigned long long pw = b + __popc(mneed & lt);
-                if (pw >= (unsigned long long)nphot) {
+                if (pw >= (uint32_t)nphot) {
                     exhausted = true;
                 } else {
                     p = (int32_t)pw;
