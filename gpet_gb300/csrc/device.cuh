@@ -7,6 +7,7 @@
 // FP32 build bit for bit (fused steps appear only as explicit fma in
 // detmath.h). Reference: gPET_kernals.cu (file:line at each function).
 #pragma once
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "detmath.h"
@@ -62,7 +63,16 @@ struct SimDesc {
     int32_t moduleN, crystalN, moduleNy, crystalNy;
     int32_t nsurface;
     float surface[10 * kMaxSurf];
-    // sources
+    float eabsph;
+    int32_t rdepth, rpolicy;
+    // bound of the panel entry faces for a quick rejection (see
+    // may_reach_panels): faces parallel to the z axis, none closer to it than
+    // sqrt(ring_rin2), all within [ring_zmin, ring_zmax] (padded); 0 none,
+    // 1 the bound, 2 the bound and every face entered only from the axis side
+    int32_t ring_test;
+    float ring_zmin, ring_zmax, ring_rin2;
+    // sources (last: the transport kernels stage only the fields before
+    // them, kSimTransportBytes, in shared memory)
     int32_t nsrc;
     int64_t src_end[kMaxSrc];     // exclusive end of each source's decay range
     int32_t src_type[kMaxSrc], src_shape[kMaxSrc];
@@ -72,19 +82,17 @@ struct SimDesc {
     float iso_coef[kMaxSrc][8];   // indexed by source
     double tstart_us;
     int32_t useprange;
-    float noncol_sigma, eabsph;
+    float noncol_sigma;
     int64_t npsf;
     const double* psf;            // [npsf][8]
     int32_t psf_ptype;
-    int32_t rdepth, rpolicy;
-    // bound of the panel entry faces for a quick rejection (see
-    // may_reach_panels): faces parallel to the z axis, none closer to it than
-    // sqrt(ring_rin2), all within [ring_zmin, ring_zmax] (padded); 0 none,
-    // 1 the bound, 2 the bound and every face entered only from the axis side
-    int32_t ring_test;
-    float ring_zmin, ring_zmax, ring_rin2;
     int32_t pad_;
 };
+
+// bytes of a SimDesc the phantom and detector kernels use (everything before
+// the sources)
+constexpr size_t kSimTransportBytes = offsetof(SimDesc, nsrc);
+static_assert(kSimTransportBytes % 4 == 0, "staged as 32-bit words");
 
 // ------------------------------------------------------------------ RNG
 // A stream is keyed by (key, tag, 64-bit id): its state is the Philox4x32-10

@@ -15,11 +15,14 @@
 
 namespace gpet {
 
-__device__ __forceinline__ void load_sim(const SimDesc* __restrict__ g, SimDesc& s, float* sP)
+// the simulation's descriptor (its first `bytes` bytes) and panels into
+// shared memory
+__device__ __forceinline__ void load_sim(const SimDesc* __restrict__ g, SimDesc& s, float* sP,
+                                         size_t bytes = sizeof(SimDesc))
 {
     const uint32_t* src = reinterpret_cast<const uint32_t*>(g);
     uint32_t* dst = reinterpret_cast<uint32_t*>(&s);
-    for (int i = threadIdx.x; i < (int)(sizeof(SimDesc) / 4); i += blockDim.x) dst[i] = src[i];
+    for (int i = threadIdx.x; i < (int)(bytes / 4); i += blockDim.x) dst[i] = src[i];
     __syncthreads();
     int np = s.npanels * kPanelStride;
     for (int i = threadIdx.x; i < np; i += blockDim.x) sP[i] = __ldg(s.panels + i);
@@ -220,14 +223,14 @@ template <bool kMulti>
 __global__ void __launch_bounds__(256) k_walk(const Wave* waves, int wi, PairBuf pb)
 {
     const Wave w = waves[wi];
-    __shared__ SimDesc sS;
+    __shared__ __align__(16) uint32_t sSw[kSimTransportBytes / 4];
+    SimDesc& sS = *reinterpret_cast<SimDesc*>(sSw);
     __shared__ SegSmem sg;
     if (kMulti) {
         load_segs(w, sg);
     } else {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(w.sims);
-        uint32_t* dst = reinterpret_cast<uint32_t*>(&sS);
-        for (int i = threadIdx.x; i < (int)(sizeof(SimDesc) / 4); i += blockDim.x) dst[i] = src[i];
+        for (int i = threadIdx.x; i < (int)(kSimTransportBytes / 4); i += blockDim.x) sSw[i] = src[i];
     }
     __syncthreads();
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -281,11 +284,13 @@ __global__ void __launch_bounds__(256, 5) k_phantom(const Wave* waves, int wi, P
     const Wave w = waves[wi];
     unsigned long long* const work = w.work;
     ExitRec* const exits = w.exits;
-    __shared__ SimDesc sS;
+    // the descriptor's transport part only (the sources are k_source's)
+    __shared__ __align__(16) uint32_t sSw[kSimTransportBytes / 4];
+    SimDesc& sS = *reinterpret_cast<SimDesc*>(sSw);
     __shared__ SegSmem sg;
     __shared__ FinRec fbuf[kPhWarps][kFinCap];
     extern __shared__ float sP[];
-    if (!kMulti) load_sim(w.sims, sS, sP);
+    if (!kMulti) load_sim(w.sims, sS, sP, kSimTransportBytes);
     load_segs(w, sg);
     __syncthreads();
     const unsigned lt = lanemask_lt();
@@ -656,10 +661,11 @@ template <bool kMulti>
 __global__ void __launch_bounds__(256, 3) k_detector(const SimDesc* sims, QueueDev q, PulseDev P,
                                                   HitDev H, int rec_hits, Counters* cnt, EntryRec* entries)
 {
-    __shared__ SimDesc sS;
+    __shared__ __align__(16) uint32_t sSw[kSimTransportBytes / 4];
+    SimDesc& sS = *reinterpret_cast<SimDesc*>(sSw);
     extern __shared__ float sP[];
     if (!kMulti) {
-        load_sim(sims, sS, sP);
+        load_sim(sims, sS, sP, kSimTransportBytes);
         __syncthreads();
     }
     unsigned long long nq = *q.count;
@@ -934,12 +940,33 @@ cudaError_t detector_blocks_per_sm(bool multi, unsigned threads, size_t smem, in
                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_detector<false>, (int)threads, smem);
 }
 
+// shared-memory carveout of `f` just large enough for `blocks` resident
+// blocks with `smem` dynamic bytes each, so that the rest of the SM's unified
+// L1 / shared memory serves as L1 (k_phantom's spill reloads and table
+// gathers); a hint the driver may round up
+template <class F>
+static cudaError_t set_carveout(F* f, int blocks, size_t smem)
+{
+    int dev = 0, per_sm = 0, reserved = 0;
+    cudaError_t e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess) return e;
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, f)) != cudaSuccess) return e;
+    const size_t need = (size_t)blocks * (fa.sharedSizeBytes + smem + (size_t)reserved);
+    int pct = per_sm > 0 ? (int)((100 * need + per_sm - 1) / (size_t)per_sm) : 100;
+    pct = pct < 1 ? 1 : (pct > 100 ? 100 : pct);
+    return cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+}
+
 // the panels staged in shared memory (single-simulation launches) can take
 // the source, phantom and detector kernels above the 48 KB that need no opt-in
 cudaError_t transport_set_smem(size_t smem)
 {
     const int v = (int)smem;
     cudaError_t e;
+    if ((e = set_carveout(k_phantom<false>, 5, smem)) != cudaSuccess) return e;
     if ((e = cudaFuncSetAttribute(k_source<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v)) != cudaSuccess)
         return e;
     if ((e = cudaFuncSetAttribute(k_phantom<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v)) != cudaSuccess)
