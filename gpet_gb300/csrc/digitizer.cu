@@ -284,9 +284,13 @@ __global__ void k_blur_threshold(PulseDev P, int64_t n, const DigiParams* __rest
                                  unsigned long long* range)
 {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarps = (blockDim.x + 31) >> 5;
     unsigned lt;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    // survivors are appended with one atomic per block and iteration (one
+    // per warp, all on one counter, made the kernel wait on the atomics)
+    __shared__ unsigned s_woff[32];
+    __shared__ unsigned long long s_base;
     unsigned long long tlo = ~0ull, thi = 0ull, smax = 0ull;
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
         const int64_t i = base + threadIdx.x;
@@ -329,14 +333,20 @@ __global__ void k_blur_threshold(PulseDev P, int64_t n, const DigiParams* __rest
                 smax = (unsigned long long)(uint32_t)sv > smax ? (unsigned long long)(uint32_t)sv : smax;
             }
         }
-        unsigned m = __ballot_sync(0xffffffffu, keep);
-        if (m) {
-            unsigned long long b = 0;
-            int leader = __ffs(m) - 1;
-            if (lane == leader) b = atomicAdd(nsel, (unsigned long long)__popc(m));
-            b = __shfl_sync(0xffffffffu, b, leader);
-            if (keep) sel[b + __popc(m & lt)] = (uint32_t)i;
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) s_woff[wid] = __popc(m);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned tot = 0;
+            for (int k = 0; k < nwarps; ++k) {
+                const unsigned c = s_woff[k];
+                s_woff[k] = tot;
+                tot += c;
+            }
+            s_base = tot ? atomicAdd(nsel, (unsigned long long)tot) : 0ull;
         }
+        __syncthreads();
+        if (keep) sel[s_base + s_woff[wid] + __popc(m & lt)] = (uint32_t)i;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -464,11 +474,10 @@ __global__ void k_site_keys(const uint32_t* __restrict__ torder, int64_t m, cons
 __global__ void k_count_by_sim(const uint32_t* __restrict__ order, int64_t m, const int32_t* __restrict__ psim,
                                Counters* cnt, int field)
 {
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m; base += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = base + threadIdx.x;
-        const int sim = (j < m && psim) ? psim[order[j]] : 0;
-        add_by_sim(cnt, sim, field, j < m ? 1u : 0u);
-    }
+    SimTally t;   // per thread, flushed once
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x)
+        t.add(cnt, field, psim ? psim[order[j]] : 0, 1u);
+    t.flush(cnt, field);
 }
 
 __global__ void k_add_count(Counters* cnt, int field, unsigned long long v)
@@ -482,6 +491,7 @@ __global__ void k_deadtime(const uint32_t* __restrict__ sorder, int64_t m, const
                            const int32_t* __restrict__ psim, const double* __restrict__ t,
                            const DigiParams* __restrict__ prms, uint32_t* flags, Counters* cnt)
 {
+    SimTally t_alive;   // per thread, flushed once (an atomic per warp and iteration queued on one counter)
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m; base += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = base + threadIdx.x;
         unsigned alive = 0;
@@ -526,8 +536,9 @@ __global__ void k_deadtime(const uint32_t* __restrict__ sorder, int64_t m, const
                 }
             }
         }
-        add_by_sim(cnt, sim, CF(n_dead), alive);
+        if (j < m) t_alive.add(cnt, CF(n_dead), sim, alive);
     }
+    t_alive.flush(cnt, CF(n_dead));
 }
 
 // energy window (gPET.cu:418) predicate over the (simulation, t) order
@@ -535,19 +546,19 @@ __global__ void k_window_pred(const uint32_t* __restrict__ torder, int64_t m, co
                               const float* __restrict__ Eb, const int32_t* __restrict__ psim,
                               const DigiParams* __restrict__ prms, uint32_t* pred, Counters* cnt)
 {
+    SimTally t_single;   // per thread, flushed once
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m; base += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = base + threadIdx.x;
-        bool ok = false;
-        int sim = 0;
         if (j < m) {
             const uint32_t p = torder[j];
-            sim = psim ? psim[p] : 0;
+            const int sim = psim ? psim[p] : 0;
             const float E = Eb[p];
-            ok = flags[p] && !(E < prms[sim].ewin_lo || E > prms[sim].ewin_hi);
+            const bool ok = flags[p] && !(E < prms[sim].ewin_lo || E > prms[sim].ewin_hi);
             pred[j] = ok ? 1u : 0u;
+            t_single.add(cnt, CF(n_single), sim, ok ? 1u : 0u);
         }
-        add_by_sim(cnt, sim, CF(n_single), ok ? 1u : 0u);
     }
+    t_single.flush(cnt, CF(n_single));
 }
 
 __global__ void k_compact(const uint32_t* __restrict__ torder, const uint32_t* __restrict__ pred,
