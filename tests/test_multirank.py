@@ -73,3 +73,23 @@ def test_bench_reference_arm_json_line():
         assert k in j, k
     assert j["e2e"]["h2d_bytes_per_step"] == 0 and j["e2e"]["d2h_bytes_per_step"] == 0
     assert j["cpu_baseline"]["kind"] == "port"
+
+
+def test_bench_reference_arm_under_torchrun_two_ranks():
+    """Launched as the two-rank job of the bench contract (torchrun, one
+    process per rank), the reference arm prints exactly one JSON line, from
+    rank 0, and every rank exits 0."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), os.path.join(root, "bench.py"),
+           "--impl", "reference", "--gpus", "2", "--steps", "2", "--warmup", "1", "--decays", "30000",
+           "--ref-step-seconds", "0.2"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    j = json.loads(lines[0])
+    assert j["impl"] == "reference" and j["n_gpus"] == 2 and j["value"] > 0
