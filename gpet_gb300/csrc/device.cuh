@@ -375,13 +375,21 @@ __device__ __forceinline__ float prange_draw(float ek, const float* dir, Stream&
 // start voxel, L = r / rho (the end voxel, plus the voxel entered beyond it);
 // prmap[v] = R says that all voxels within R of v have v's density and lie in
 // [1, n-2] on every axis, so L < (R - 1.5) * dmin (half a voxel of margin)
-// keeps the walk inside. Returns false (x unchanged) where the walk is needed,
-// with est = sum |d_k| / (rho * dmin), about the number of voxel faces the walk
-// crosses at the start voxel's density (0 outside the phantom, where it takes
-// one step). A zero displacement moves nothing, as in the walk.
-__device__ __forceinline__ bool prange_uniform(const SimDesc& S, float x[3], const float d[3], float r, float& est)
+// keeps the walk inside. Returns false where the walk is needed. A walk that
+// reaches beyond the uniform cube (R >= 2) starts where its first
+// lim = (R - 1.5) * dmin of path would take it: x moves by lim along d / r and
+// *s0 = lim * rho is the density-weighted length already covered (the walk
+// would read only voxels of density rho up to there: the voxel holding that
+// point lies within R - 1 of the start voxel, and the one entered after it
+// within R); otherwise x is unchanged and *s0 = 0. est = about the number of
+// voxel faces the rest of the walk crosses at the start voxel's density (0
+// outside the phantom, where it takes one step). A zero displacement moves
+// nothing, as in the walk.
+__device__ __forceinline__ bool prange_uniform(const SimDesc& S, float x[3], const float d[3], float r, float& est,
+                                               float& s0)
 {
     est = 0.0f;
+    s0 = 0.0f;
     if (!(r > 0.0f)) return true;
     int ix, iy, iz;
     if (!abs_vox(S, x[0], x[1], x[2], ix, iy, iz)) return false;
@@ -393,16 +401,26 @@ __device__ __forceinline__ bool prange_uniform(const SimDesc& S, float x[3], con
         return false;
     }
     const float L = r / rho;
-    if (R < 2 || !(L < ((float)R - 1.5f) * S.prdmin)) {
-        est = (fabsf(d[0]) + fabsf(d[1]) + fabsf(d[2])) / (rho * S.prdmin);
+    const float sum_d = fabsf(d[0]) + fabsf(d[1]) + fabsf(d[2]);
+    if (R < 2) {
+        est = sum_d / (rho * S.prdmin);
         return false;
     }
+    const float lim = ((float)R - 1.5f) * S.prdmin;
     const float ir = 1.0f / r;
     const float dn0 = d[0] * ir, dn1 = d[1] * ir, dn2 = d[2] * ir;
-    x[0] = x[0] + L * dn0;
-    x[1] = x[1] + L * dn1;
-    x[2] = x[2] + L * dn2;
-    return true;
+    if (L < lim) {
+        x[0] = x[0] + L * dn0;
+        x[1] = x[1] + L * dn1;
+        x[2] = x[2] + L * dn2;
+        return true;
+    }
+    x[0] = x[0] + lim * dn0;
+    x[1] = x[1] + lim * dn1;
+    x[2] = x[2] + lim * dn2;
+    s0 = lim * rho;
+    est = (L - lim) * ir * sum_d / S.prdmin;
+    return false;
 }
 
 // state of one voxel walk
@@ -415,9 +433,10 @@ struct PWalk {
     bool inside;
 };
 
-// set up the walk of displacement d (length r) from x; false if it has no step
+// set up the walk of displacement d (length r) from x, with the
+// density-weighted length s0 already covered; false if it has no step
 __device__ __forceinline__ bool prange_walk_init(const SimDesc& S, PWalk& w, const float x[3], const float d[3],
-                                                 float r)
+                                                 float r, float s0)
 {
     // reciprocals once: the walk multiplies instead of dividing
     w.id[0] = 1.0f / d[0]; w.id[1] = 1.0f / d[1]; w.id[2] = 1.0f / d[2];
@@ -431,7 +450,7 @@ __device__ __forceinline__ bool prange_walk_init(const SimDesc& S, PWalk& w, con
     w.inside = abs_vox(S, x[0], x[1], x[2], w.v[0], w.v[1], w.v[2]);
     if (!w.inside) { w.v[0] = w.v[1] = w.v[2] = 0; }
     w.r = r;
-    w.s = 0.0f;
+    w.s = s0;
     w.guard = 0;
     return w.s < w.r;
 }

@@ -1347,7 +1347,7 @@ static int run_batch(gpet_ctx* const* cs, int nsim, gpet_run_stats* stats, int64
         CK(W.pb_f.ensure((size_t)sub * 11 * 4));
         CK(W.pb_t.ensure((size_t)sub * 8));
         CK(W.pb_n.ensure((size_t)sub));
-        CK(W.pb_wf.ensure((size_t)sub * kWalkLists * 7 * 4));
+        CK(W.pb_wf.ensure((size_t)sub * kWalkLists * kWalkFields * 4));
         CK(W.pb_wj.ensure((size_t)sub * kWalkLists * 4));
         W.pb_cap = sub;
     }

@@ -139,12 +139,13 @@ struct DigiParams {
 
 // emitted pairs of a sub-chunk of decays, structure of arrays
 constexpr int kWalkLists = 4;    // positron walk lists by estimated length
+constexpr int kWalkFields = 8;   // floats per walk: start (3), displacement (3), its length, length covered
 
 struct PairBuf {
     float* f;                     // [11][cap]: x, y, z, u0 (3), u1 (3), E0, E1
     double* t;                    // [cap]
     uint8_t* nph;                 // [cap]: photons emitted (0, 1 or 2)
-    float* wf;                    // walk lists [kWalkLists][7][cap]: start x, y, z, displacement (3), its length
+    float* wf;                    // walk lists [kWalkLists][kWalkFields][cap]
     int32_t* wj;                  // walk lists [kWalkLists][cap]: the decay's index within the wave
     int64_t cap;
 };

@@ -79,9 +79,10 @@ __device__ __forceinline__ int seg_of(const SegSmem& sg, int64_t g)
 // :563-604, with the second photon's time set) when npsf > 0.
 // Returns how many photons of the pair exist (0, 1 or 2). walk: the positron
 // range needs the voxel walk, which starts at the pair's position with
-// displacement wd[0..2] of length wd[3] and about wd[4] steps (the pair's
-// position is then its start, and k_walk moves it).
-__device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2], bool& walk, float wd[5])
+// displacement wd[0..2] of length wd[3], density-weighted length wd[5]
+// already covered and about wd[4] steps to go (the pair's position is then
+// the walk's start, and k_walk moves it).
+__device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2], bool& walk, float wd[6])
 {
     Stream st;
     st_init(st, S.key0, S.key1, kTagDecay, (uint64_t)d);
@@ -99,7 +100,7 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2], bool& wal
         float spare = 0.0f;
         if (S.useprange) {
             wd[3] = prange_draw((float)r[7], dir, st, wd, &spare);
-            walk = !prange_uniform(S, pos, wd, wd[3], wd[4]);
+            walk = !prange_uniform(S, pos, wd, wd[3], wd[4], wd[5]);
         }
         make_pair(S, st, pos, r[3], ph, S.useprange ? &spare : nullptr);
         return 2;
@@ -120,7 +121,7 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2], bool& wal
     if (S.useprange) {
         float ek = sample_ek(S.iso_coef[si], st);
         wd[3] = prange_draw(ek, nullptr, st, wd, &spare);
-        walk = !prange_uniform(S, pos, wd, wd[3], wd[4]);
+        walk = !prange_uniform(S, pos, wd, wd[3], wd[4], wd[5]);
     }
     make_pair(S, st, pos, t_us, ph, S.useprange ? &spare : nullptr);
     return 2;
@@ -158,7 +159,7 @@ __global__ void __launch_bounds__(256, 5) k_source(const Wave* waves, int wi, Pa
         int nph = 0;
         int sim = 0;
         bool walk = false;
-        float wd[5];
+        float wd[6];
         Photon ph[2];
         if (j < w.n) {
             const int sgi = seg_of(sg, j);
@@ -197,7 +198,7 @@ __global__ void __launch_bounds__(256, 5) k_source(const Wave* waves, int wi, Pa
                 if (lane == leader) base_k = atomicAdd(w.walkn + wl, (unsigned long long)__popc(grp));
                 base_k = __shfl_sync(grp, base_k, leader);
                 const unsigned long long k = base_k + __popc(grp & lt);
-                float* wf = pb.wf + (size_t)wl * 7 * pb.cap;
+                float* wf = pb.wf + (size_t)wl * kWalkFields * pb.cap;
                 wf[0 * pb.cap + k] = ph[0].x[0];
                 wf[1 * pb.cap + k] = ph[0].x[1];
                 wf[2 * pb.cap + k] = ph[0].x[2];
@@ -205,6 +206,7 @@ __global__ void __launch_bounds__(256, 5) k_source(const Wave* waves, int wi, Pa
                 wf[4 * pb.cap + k] = wd[1];
                 wf[5 * pb.cap + k] = wd[2];
                 wf[6 * pb.cap + k] = wd[3];
+                wf[7 * pb.cap + k] = wd[5];
                 pb.wj[(size_t)wl * pb.cap + k] = (int32_t)j;
             }
         }
@@ -236,16 +238,16 @@ __global__ void __launch_bounds__(256) k_walk(const Wave* waves, int wi, PairBuf
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int b = 0; b < kWalkLists; ++b) {
         const int64_t n = (int64_t)w.walkn[b];
-        const float* wf = pb.wf + (size_t)b * 7 * pb.cap;
+        const float* wf = pb.wf + (size_t)b * kWalkFields * pb.cap;
         const int32_t* wj = pb.wj + (size_t)b * pb.cap;
         for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
             const int32_t j = wj[k];
             const float x[3] = {wf[0 * pb.cap + k], wf[1 * pb.cap + k], wf[2 * pb.cap + k]};
             const float d[3] = {wf[3 * pb.cap + k], wf[4 * pb.cap + k], wf[5 * pb.cap + k]};
-            const float r = wf[6 * pb.cap + k];
+            const float r = wf[6 * pb.cap + k], s0 = wf[7 * pb.cap + k];
             const SimDesc* S = kMulti ? w.sims + sg.sim[seg_of(sg, j)] : &sS;
             PWalk pw;
-            if (prange_walk_init(*S, pw, x, d, r))
+            if (prange_walk_init(*S, pw, x, d, r, s0))
                 while (prange_walk_step(*S, pw)) {
                 }
             pb.f[0 * pb.cap + j] = pw.x[0];

@@ -451,10 +451,17 @@ void oracle_build_prmap(const or_scene* sc, int8_t* out)
     free(tmp);
 }
 
-/* the closed form above; returns 0 (x unchanged) where the walk is needed.
- * A zero displacement moves nothing, as in the walk. */
-static int prange_uniform(const or_scene* sc, real x[3], const real d[3], real r)
+/* the closed form above; returns 0 where the walk is needed. A walk that
+ * reaches beyond the uniform cube (R >= 2) starts where its first
+ * lim = (R - 1.5) * dmin of path takes it: x moves by lim along d / r and *s0 =
+ * lim * rho is the density-weighted length already covered (up to there the
+ * walk reads only voxels of density rho: the voxel holding that point lies
+ * within R - 1 of the start voxel, the one entered after it within R);
+ * otherwise x is unchanged and *s0 = 0. A zero displacement moves nothing, as
+ * in the walk. */
+static int prange_uniform(const or_scene* sc, real x[3], const real d[3], real r, real* s0)
 {
+    *s0 = (real)0.0;
     if (!(r > (real)0.0)) return 1;
     if (!sc->prmap) return 0;
     int ix, iy, iz;
@@ -463,18 +470,24 @@ static int prange_uniform(const or_scene* sc, real x[3], const real d[3], real r
         return 0;
     const size_t i = (size_t)ix + (size_t)sc->nx * ((size_t)iy + (size_t)sc->ny * iz);
     const int R = sc->prmap[i];
-    if (R < 2) return 0;
     const real rho = (real)sc->den[i];
-    if (!(rho > (real)0.0)) return 0;
+    if (!(rho > (real)0.0) || R < 2) return 0;
     const real L = r / rho;
     const real dmin = (real)fminf(sc->dx, fminf(sc->dy, sc->dz));
-    if (!(L < ((real)R - (real)1.5) * dmin)) return 0;
+    const real lim = ((real)R - (real)1.5) * dmin;
     const real ir = (real)1.0 / r;
     const real dn0 = d[0] * ir, dn1 = d[1] * ir, dn2 = d[2] * ir;
-    x[0] = x[0] + L * dn0;
-    x[1] = x[1] + L * dn1;
-    x[2] = x[2] + L * dn2;
-    return 1;
+    if (L < lim) {
+        x[0] = x[0] + L * dn0;
+        x[1] = x[1] + L * dn1;
+        x[2] = x[2] + L * dn2;
+        return 1;
+    }
+    x[0] = x[0] + lim * dn0;
+    x[1] = x[1] + lim * dn1;
+    x[2] = x[2] + lim * dn2;
+    *s0 = lim * rho;
+    return 0;
 }
 
 /* setPositronRange, gPET_kernals.cu:347-418: Gaussian displacement with
@@ -507,7 +520,8 @@ static void positron_range(const or_scene* sc, real x[3], real ek, const real* d
         real tmp = R_SQRT(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
         d[0] = r * dir[0] / tmp; d[1] = r * dir[1] / tmp; d[2] = r * dir[2] / tmp;
     }
-    if (prange_uniform(sc, x, d, r)) return;
+    real s0;
+    if (prange_uniform(sc, x, d, r, &s0)) return;
     /* the walk multiplies by reciprocals computed once */
     const real id0 = (real)1.0 / d[0], id1 = (real)1.0 / d[1], id2 = (real)1.0 / d[2];
     const real ir = (real)1.0 / r;
@@ -522,7 +536,7 @@ static void positron_range(const or_scene* sc, real x[3], real ek, const real* d
          * are only used while inside, so any value will do */
         vx = vy = vz = 0;
     }
-    real s = (real)0.0, step;
+    real s = s0, step;
     const real xmax = (real)sc->offx + (real)sc->nx * (real)sc->dx;
     const real ymax = (real)sc->offy + (real)sc->ny * (real)sc->dy;
     const real zmax = (real)sc->offz + (real)sc->nz * (real)sc->dz;
