@@ -270,7 +270,7 @@ struct FinRec {
 static_assert(sizeof(FinRec) == 40, "staged record");
 
 constexpr int kPhWarps = 8;      // warps per k_phantom block (256 threads)
-constexpr uint32_t kClaim = 64;  // photons a k_phantom warp claims at a time
+constexpr uint32_t kClaim = 128; // photons a k_phantom warp claims at a time
 constexpr int kFinCap = 64;      // finished photons staged per warp
 
 // phantom stage: persistent warps; a lane whose photon has left the phantom
@@ -393,18 +393,26 @@ __global__ void __launch_bounds__(256, 5) k_phantom(const Wave* waves, int wi, P
         unsigned long long t = 0;
         if (lane == 0) t = atomicAdd(work, (unsigned long long)kClaim);
         const uint32_t b = (uint32_t)__shfl_sync(0xffffffffu, t, 0);
-        if (b < (uint32_t)nphot && lane < 16) {
-            // decays [b/2, b/2 + kClaim/2) of the 11 float arrays, the
-            // emission times and the photon counts; both ends of each range
+        if (b < (uint32_t)nphot) {
+            // every 128-byte line of decays [b/2, b/2 + kClaim/2) in the 11
+            // float arrays, the emission times and the photon counts: the
+            // lanes take the (array, line) pairs in turn; the range's last
+            // element is prefetched too (the range need not start on a line)
             const int64_t j0 = b >> 1;
-            const int64_t j1 = min(j0 + kClaim / 2 - 1, w.n - 1);
-            const int a = lane < 11 ? lane : 0;
-            const void* p0 = lane < 11 ? (const void*)(pb.f + a * pb.cap + j0)
-                                       : (lane < 13 ? (const void*)(pb.t + j0) : (const void*)(pb.nph + j0));
-            const void* p1 = lane < 11 ? (const void*)(pb.f + a * pb.cap + j1)
-                                       : (lane < 13 ? (const void*)(pb.t + j1) : (const void*)(pb.nph + j1));
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(lane == 11 || lane >= 13 ? p0 : p1));
-            if (lane < 11) asm volatile("prefetch.global.L2 [%0];" ::"l"(p0));
+            const int64_t nd = min((int64_t)(kClaim / 2), w.n - j0);
+            constexpr int kFl = kClaim / 64 + 1, kTl = kClaim / 32 + 1;   // lines per float / time array
+            for (int q = lane; q < 11 * kFl + kTl + 1; q += 32) {
+                const void* ptr;
+                if (q < 11 * kFl) {
+                    const int64_t o = min((int64_t)(q % kFl) * 32, nd - 1);
+                    ptr = pb.f + (q / kFl) * pb.cap + j0 + o;
+                } else if (q < 11 * kFl + kTl) {
+                    ptr = pb.t + j0 + min((int64_t)(q - 11 * kFl) * 16, nd - 1);
+                } else {
+                    ptr = pb.nph + j0;
+                }
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
+            }
         }
         return b;
     };
