@@ -140,7 +140,7 @@ __device__ __forceinline__ int walk_list(float est)
 }
 
 template <bool kMulti>
-__global__ void __launch_bounds__(256, 5) k_source(const Wave* waves, int wi, PairBuf pb, Counters* cnt)
+__global__ void __launch_bounds__(256, 6) k_source(const Wave* waves, int wi, PairBuf pb, Counters* cnt)
 {
     const Wave w = waves[wi];
     __shared__ SimDesc sS;
