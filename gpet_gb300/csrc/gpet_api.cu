@@ -355,29 +355,42 @@ __global__ void k_pack_palette(const int32_t* __restrict__ mat, const float* __r
     __shared__ unsigned smax[16];
     if (threadIdx.x < 16) smax[threadIdx.x] = 0;
     __syncthreads();
+    const int lane = threadIdx.x & 31;
     unsigned nbad = 0, novf = 0;
-    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-        const int m = mat[v];
-        const float d = den[v];
-        if (m < 0 || m >= nmat) {
-            nbad++;
-            continue;
-        }
-        if (d > 0.0f) atomicMax(&smax[m], __float_as_uint(d));
-        const unsigned long long key = ((unsigned long long)(unsigned)m << 32) | __float_as_uint(d);
-        uint32_t h = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - kPalBits));
+    // all lanes of a warp run the same iterations (base is block-uniform)
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = base + threadIdx.x;
+        const bool in = v < n;
+        const int m = in ? mat[v] : 0;
+        const float d = in ? den[v] : 0.0f;
+        const bool good = in && m >= 0 && m < nmat;
+        if (in && !good) nbad++;
+        if (good && d > 0.0f) atomicMax(&smax[m], __float_as_uint(d));
+        // one probe per distinct pair of the warp (a phantom has few): the
+        // lanes holding the same key share their leader's slot; the table is
+        // read through L2, where the insertions of other SMs are visible
+        const unsigned long long key = good ? (((unsigned long long)(unsigned)m << 32) | __float_as_uint(d))
+                                            : kPalEmpty;
+        const unsigned grp = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(grp) - 1;
         int slot = -1;
-        for (int p = 0; p < kPalProbes; ++p) {
-            const unsigned long long cur = keys[h];
-            if (cur == key) { slot = (int)h; break; }
-            if (cur == kPalEmpty) {
-                const unsigned long long prev = atomicCAS(&keys[h], kPalEmpty, key);
-                if (prev == kPalEmpty || prev == key) { slot = (int)h; break; }
+        if (good && lane == leader) {
+            uint32_t h = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - kPalBits));
+            for (int p = 0; p < kPalProbes; ++p) {
+                const unsigned long long cur = __ldcg(&keys[h]);
+                if (cur == key) { slot = (int)h; break; }
+                if (cur == kPalEmpty) {
+                    const unsigned long long prev = atomicCAS(&keys[h], kPalEmpty, key);
+                    if (prev == kPalEmpty || prev == key) { slot = (int)h; break; }
+                }
+                h = (h + 1) & (kPalSlots - 1);
             }
-            h = (h + 1) & (kPalSlots - 1);
         }
-        if (slot < 0) novf++;
-        else vox16[v] = (uint16_t)slot;
+        slot = __shfl_sync(0xffffffffu, slot, leader);
+        if (good) {
+            if (slot < 0) novf++;
+            else vox16[v] = (uint16_t)slot;
+        }
     }
     if (nbad) atomicAdd(bad, nbad);
     if (novf) atomicAdd(bad + 1, novf);
