@@ -139,12 +139,15 @@ def make_scene(directory, n_decays, workload="positron"):
     return scenes.positron(directory, n_decays=n_decays)
 
 
-def cpu_baseline(scene, seconds, threads=0, max_decays=200_000_000):
-    """The oracle (FP64, OpenMP over decays) on a bounded sample of the workload."""
+def cpu_baseline(scene, seconds, threads=0, max_decays=200_000_000, with_hists=False):
+    """The oracle (FP64, OpenMP over decays) on a bounded sample of the workload
+    (with_hists: also its singles histograms and counts, for the parity check)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import bridge
     bridge.build()
     o = bridge.OracleScene(scene.config_path, scene.options, os.path.join(ROOT, "data"), base_dir=scene.directory)
+    if with_hists:
+        o.s.seed = 4242   # a key no GPU step of the bench uses: independent samples
     n0 = min(200_000, o.n_decays)
     t0 = time.perf_counter()
     o.run(0, n0, precision="fp64", threads=threads)
@@ -154,9 +157,47 @@ def cpu_baseline(scene, seconds, threads=0, max_decays=200_000_000):
     r = o.run(0, n, precision="fp64", threads=threads)
     dt = time.perf_counter() - t0
     cores = threads if threads > 0 else (os.cpu_count() or 1)
-    return {"value": r["n_coinc"] / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d of the %d decays (oracle FP64, %d threads, %.1f s)" % (n, o.n_decays, cores, dt),
-            "decays_per_s": n / dt, "coincidences": r["n_coinc"]}
+    out = {"value": r["n_coinc"] / dt, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": "%d of the %d decays (oracle FP64, %d threads, %.1f s)" % (n, o.n_decays, cores, dt),
+           "decays_per_s": n / dt, "coincidences": r["n_coinc"]}
+    if with_hists:
+        out["_parity"] = (_singles_hists(r["singles"]),
+                          {"n_decays": n, "n_singles": r["n_singles"], "n_coinc": r["n_coinc"],
+                           "n_true": r["n_true"], "n_scatter": r["n_scatter"], "n_random": r["n_random"]},
+                          int(o.s.seed))
+    return out
+
+
+def _singles_hists(ev):
+    """Singles energy spectrum (60 bins over the 350-650 keV window) and
+    singles per crystal (pooled over panels and modules)."""
+    import numpy as np
+    he = np.histogram(ev["E"], bins=60, range=(3.5e5, 6.5e5))[0]
+    hc = np.bincount(ev["cryn"], minlength=64) if len(ev) else np.zeros(64, np.int64)
+    return he, hc
+
+
+def _parity_vs_oracle(gpu_hist, gpu_counts, gpu_seed, oracle_part):
+    """Plain Monte Carlo on the GPU against the FP64 oracle on the same
+    workload with independent seeds: two-sample chi-square of the singles
+    spectrum and crystal map, and per-decay rates with the difference in
+    standard deviations of the two Poisson counts."""
+    import numpy as np
+    (oe, oc), ocounts, oseed = oracle_part
+    ge, gc = gpu_hist
+    nc = max(len(gc), len(oc))
+    gc = np.pad(gc, (0, nc - len(gc)))
+    oc = np.pad(oc, (0, nc - len(oc)))
+    rates = {}
+    for k in ("n_singles", "n_coinc", "n_true", "n_scatter", "n_random"):
+        a, na = float(gpu_counts[k]), float(gpu_counts["n_decays"])
+        b, nb = float(ocounts[k]), float(ocounts["n_decays"])
+        ra, rb = a / na, b / nb
+        sd = np.sqrt(a / na ** 2 + b / nb ** 2)
+        rates[k[2:]] = {"gpu_per_decay": ra, "oracle_per_decay": rb, "sigma": (ra - rb) / sd if sd > 0 else 0.0}
+    return {"gpu": {"seed": gpu_seed, "decays": int(gpu_counts["n_decays"])},
+            "oracle": {"seed": oseed, "decays": int(ocounts["n_decays"]), "precision": "fp64"},
+            "singles_energy_350_650keV": _chi2(ge, oe), "singles_per_crystal": _chi2(gc, oc), "rates": rates}
 
 
 def cpu_model():
@@ -286,6 +327,12 @@ def run_ours(args):
         barrier()
         wall = time.perf_counter() - t_wall0
         clocks = sampler.stop()
+        # the last timed acquisition's singles, for the parity check against
+        # the oracle's own acquisition (independent seeds) below
+        last_seed = 20261203 + args.steps - 1
+        last_ev, _ = ctx.singles()
+        last_hist = _singles_hists(last_ev)
+        last_counts = {k: st[k] for k in ("n_decays", "n_singles", "n_coinc", "n_true", "n_scatter", "n_random")}
         ms_max, coinc_all = combine_ranks(tot["ms"], tot["coinc"], dist,
                                           "cpu" if args.gloo else "cuda:%d" % local)
         value = coinc_all / (ms_max * 1e-3)
@@ -414,8 +461,10 @@ def run_ours(args):
     if world == 1 and not args.no_cpu_baseline:
         with tempfile.TemporaryDirectory() as d2:
             sc2 = make_scene(d2, args.decays, args.workload)
-            line["cpu_baseline"] = cpu_baseline(sc2, args.cpu_seconds)
+            line["cpu_baseline"] = cpu_baseline(sc2, args.cpu_seconds, with_hists=True)
             line["cpu_baseline"]["cpu_model"] = cpu_model()
+            line["parity_vs_oracle"] = _parity_vs_oracle(last_hist, last_counts, last_seed,
+                                                         line["cpu_baseline"].pop("_parity"))
             one = cpu_baseline(sc2, args.cpu_seconds / 4, threads=1)
             line["cpu_baseline_1core"] = {k: one[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line), flush=True)
