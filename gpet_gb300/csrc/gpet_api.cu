@@ -42,7 +42,7 @@ struct DevBuf {
 
 // grow-only host array, page-locked when the system grants it (device-to-host
 // copies into it then run at the host link's rate and asynchronously), else
-// ordinary memory (the copies are then staged by the driver); resize() leaves
+// ordinary memory (the copies are then staged by the CUDA driver); resize() leaves
 // the contents unset
 template <class T>
 struct PinnedVec {

@@ -953,7 +953,7 @@ cudaError_t detector_blocks_per_sm(bool multi, unsigned threads, size_t smem, in
 // shared-memory carveout of `f` just large enough for `blocks` resident
 // blocks with `smem` dynamic bytes each, so that the rest of the SM's unified
 // L1 / shared memory serves as L1 (k_phantom's spill reloads and table
-// gathers); a hint the driver may round up
+// gathers); a hint the CUDA driver may round up
 template <class F>
 static cudaError_t set_carveout(F* f, int blocks, size_t smem)
 {
