@@ -212,7 +212,7 @@ extern "C" int gpet_digitize_static(const gpet_digi_params* prm, const gpet_even
         const int site_bits = site_key_bits(hc[10]);
         k_site_keys<<<grid256(m), 256, 0, s>>>(D.torder, m, D.site, nullptr, ka, va);
         sort(ka, va, kb, vb, m, site_bits, D.hist, D.scan_aux, total, s);
-        k_deadtime<<<grid256(m), 256, 0, s>>>(va, m, D.site, nullptr, P.t, d_prm, D.flags, d_cnt);
+        k_deadtime<<<grid256(m), 256, 0, s>>>(va, ka, m, P.t, d_prm, 0, D.flags, d_cnt);
         k_window_pred<<<grid256(m), 256, 0, s>>>(D.torder, m, D.flags, D.Eb, nullptr, d_prm, D.sel, d_cnt);
         scan(D.sel, D.wcount, m, D.scan_aux, reinterpret_cast<uint32_t*>(D.dcount + 2), s);
         k_compact<<<grid256(m), 256, 0, s>>>(D.torder, D.sel, D.wcount, m, D.single_idx);

@@ -487,56 +487,60 @@ __global__ void k_add_count(Counters* cnt, int field, unsigned long long v)
 
 // dead time (deadtime, gPET_kernals.cu:657-698, sequential semantics, FP64):
 // sorder is the (simulation, site, t, parn, slot) order
-__global__ void k_deadtime(const uint32_t* __restrict__ sorder, int64_t m, const int32_t* __restrict__ site,
-                           const int32_t* __restrict__ psim, const double* __restrict__ t,
-                           const DigiParams* __restrict__ prms, uint32_t* flags, Counters* cnt)
+// skey: the sorted (simulation, site) keys beside sorder (equal keys: the
+// same site of the same simulation); multi: the key's high word is the
+// simulation. A pulse's predecessor in this order comes from the lane below
+// (key and time), so a pulse costs one gather of its time.
+__global__ void k_deadtime(const uint32_t* __restrict__ sorder, const uint64_t* __restrict__ skey, int64_t m,
+                           const double* __restrict__ t, const DigiParams* __restrict__ prms, int multi,
+                           uint32_t* flags, Counters* cnt)
 {
+    const int lane = threadIdx.x & 31;
     SimTally t_alive;   // per thread, flushed once (an atomic per warp and iteration queued on one counter)
+    // all lanes of a warp run the same iterations (base is block-uniform)
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m; base += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = base + threadIdx.x;
+        const bool in = j < m;
+        const uint32_t p = in ? sorder[j] : 0u;
+        const uint64_t kp = in ? skey[j] : 0ull;
+        const double tp = in ? t[p] : 0.0;
+        uint64_t kq = __shfl_up_sync(0xffffffffu, kp, 1);
+        double tq = __shfl_up_sync(0xffffffffu, tp, 1);
+        if (lane == 0 && in && j > 0) {
+            kq = skey[j - 1];
+            tq = t[sorder[j - 1]];
+        }
+        if (!in) continue;
         unsigned alive = 0;
-        int sim = 0;
-        if (j < m) {
-            const uint32_t p = sorder[j];
-            sim = psim ? psim[p] : 0;
-            const double tau = prms[sim].tau;
-            auto same_site = [&](uint32_t a, uint32_t b) {
-                return site[a] == site[b] && (!psim || psim[a] == psim[b]);
-            };
-            if (prms[sim].dtype == 0) {
-                bool keep = true;
-                if (j > 0) {
-                    const uint32_t q = sorder[j - 1];
-                    keep = !(same_site(q, p) && t[p] < t[q] + tau);
-                }
-                flags[p] = keep ? 1u : 0u;
-                alive += keep;
-            } else {
-                // anchors: first pulse of a site or >= tau after its predecessor
-                bool anchor = j == 0;
-                if (!anchor) {
-                    const uint32_t q = sorder[j - 1];
-                    anchor = !same_site(q, p) || !(t[p] < t[q] + tau);
-                }
-                if (anchor) {
-                    double tdead = t[p];
-                    flags[p] = 1u;
-                    alive++;
-                    for (int64_t i = j + 1; i < m; ++i) {
-                        const uint32_t a = sorder[i], b = sorder[i - 1];
-                        if (!same_site(b, a) || !(t[a] < t[b] + tau)) break;   // next anchor
-                        if (t[a] < tdead + tau) {
-                            flags[a] = 0u;
-                        } else {
-                            flags[a] = 1u;
-                            alive++;
-                            tdead = t[a];
-                        }
+        const int sim = multi ? (int)(kp >> 32) : 0;
+        const double tau = prms[sim].tau;
+        if (prms[sim].dtype == 0) {
+            const bool keep = !(j > 0 && kq == kp && tp < tq + tau);
+            flags[p] = keep ? 1u : 0u;
+            alive += keep;
+        } else {
+            // anchors: first pulse of a site or >= tau after its predecessor
+            const bool anchor = j == 0 || kq != kp || !(tp < tq + tau);
+            if (anchor) {
+                double tdead = tp, tprev = tp;
+                flags[p] = 1u;
+                alive++;
+                for (int64_t i = j + 1; i < m; ++i) {
+                    const uint32_t a = sorder[i];
+                    const double ta = t[a];
+                    if (skey[i] != kp || !(ta < tprev + tau)) break;   // next anchor
+                    if (ta < tdead + tau) {
+                        flags[a] = 0u;
+                    } else {
+                        flags[a] = 1u;
+                        alive++;
+                        tdead = ta;
                     }
+                    tprev = ta;
                 }
             }
         }
-        if (j < m) t_alive.add(cnt, CF(n_dead), sim, alive);
+        t_alive.add(cnt, CF(n_dead), sim, alive);
     }
     t_alive.flush(cnt, CF(n_dead));
 }
@@ -938,7 +942,7 @@ int digitize_device(const PulseDev& P, int64_t n, const DigiParams* d_prms, int 
         *launches += 2;
         radix_sort(ka, va, kb, vb, m, site_bits, D.hist, D.scan_aux, total, s, launches);
         // dead time on the site order
-        k_deadtime<<<grid_for(m, 256), 256, 0, s>>>(va, m, D.site, psim, P.t, d_prms, D.flags, d_cnt);
+        k_deadtime<<<grid_for(m, 256), 256, 0, s>>>(va, ka, m, P.t, d_prms, psim ? 1 : 0, D.flags, d_cnt);
         // energy window over the time order, ordered compaction
         k_window_pred<<<grid_for(m, 256), 256, 0, s>>>(D.torder, m, D.flags, D.Eb, psim, d_prms, D.sel, d_cnt);
         *launches += 2;

@@ -247,8 +247,8 @@ int launch_time_keys(const uint32_t* sel, int64_t m, const double* t, const unsi
 int site_key_bits(unsigned long long smax);
 __global__ void k_site_keys(const uint32_t* torder, int64_t m, const int32_t* site, const int32_t* psim,
                             uint64_t* key, uint32_t* val);
-__global__ void k_deadtime(const uint32_t* sorder, int64_t m, const int32_t* site, const int32_t* psim,
-                           const double* t, const DigiParams* prms, uint32_t* flags, Counters* cnt);
+__global__ void k_deadtime(const uint32_t* sorder, const uint64_t* skey, int64_t m, const double* t,
+                           const DigiParams* prms, int multi, uint32_t* flags, Counters* cnt);
 __global__ void k_window_pred(const uint32_t* torder, int64_t m, const uint32_t* flags, const float* Eb,
                               const int32_t* psim, const DigiParams* prms, uint32_t* pred, Counters* cnt);
 __global__ void k_count_by_sim(const uint32_t* order, int64_t m, const int32_t* psim, Counters* cnt, int field);
