@@ -330,9 +330,11 @@ def run_ours(args):
         # the last timed acquisition's singles, for the parity check against
         # the oracle's own acquisition (independent seeds) below
         last_seed = 20261203 + args.steps - 1
-        last_ev, _ = ctx.singles()
-        last_hist = _singles_hists(last_ev)
-        last_counts = {k: st[k] for k in ("n_decays", "n_singles", "n_coinc", "n_true", "n_scatter", "n_random")}
+        last_hist, last_counts = None, None
+        if world == 1 and not args.no_cpu_baseline:
+            last_ev, _ = ctx.singles()
+            last_hist = _singles_hists(last_ev)
+            last_counts = {k: st[k] for k in ("n_decays", "n_singles", "n_coinc", "n_true", "n_scatter", "n_random")}
         ms_max, coinc_all = combine_ranks(tot["ms"], tot["coinc"], dist,
                                           "cpu" if args.gloo else "cuda:%d" % local)
         value = coinc_all / (ms_max * 1e-3)
