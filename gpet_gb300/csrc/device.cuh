@@ -53,6 +53,9 @@ struct SimDesc {
     const uint16_t* vox16;
     // radius of uniform density around each voxel (prange_uniform), or null
     const int8_t* prmap;
+    // the uploaded densities, one float per voxel (the bits the palette
+    // holds), for the positron range's lookups where they fit in L2; or null
+    const float* den;
     float prdmin;                 // min(dx, dy, dz)
     // detector
     int32_t npanels;
@@ -277,12 +280,20 @@ __device__ __forceinline__ uint2 voxel(const SimDesc& S, int ix, int iy, int iz)
     return __ldg(S.vox + i);
 }
 
+// density of voxel (ix, iy, iz) (in range): one load from the density array
+// where there is one, else through the phantom's voxel records
+__device__ __forceinline__ float den_at(const SimDesc& S, int ix, int iy, int iz)
+{
+    if (S.den) return __ldg(S.den + ((uint32_t)ix + (uint32_t)S.nx * ((uint32_t)iy + (uint32_t)S.ny * (uint32_t)iz)));
+    return __uint_as_float(voxel(S, ix, iy, iz).x);
+}
+
 __device__ __forceinline__ float den_clamped(const SimDesc& S, int ix, int iy, int iz)
 {
     ix = ix < 0 ? 0 : (ix > S.nx - 1 ? S.nx - 1 : ix);
     iy = iy < 0 ? 0 : (iy > S.ny - 1 ? S.ny - 1 : iy);
     iz = iz < 0 ? 0 : (iz > S.nz - 1 ? S.nz - 1 : iz);
-    return __uint_as_float(voxel(S, ix, iy, iz).x);
+    return den_at(S, ix, iy, iz);
 }
 
 // ---------------------------------------------------------------- source
@@ -395,7 +406,7 @@ __device__ __forceinline__ bool prange_uniform(const SimDesc& S, float x[3], con
     if (!abs_vox(S, x[0], x[1], x[2], ix, iy, iz)) return false;
     const uint32_t i = (uint32_t)ix + (uint32_t)S.nx * ((uint32_t)iy + (uint32_t)S.ny * (uint32_t)iz);
     const int R = S.prmap ? __ldg(S.prmap + i) : 0;
-    const float rho = __uint_as_float(voxel(S, ix, iy, iz).x);
+    const float rho = den_at(S, ix, iy, iz);
     if (!(rho > 0.0f)) {
         est = 1.0e30f;
         return false;

@@ -863,6 +863,11 @@ static int build_sim(gpet_ctx* c)
     S.vox = c->vox_pal ? c->d_pal.as<uint2>() : c->d_vox.as<uint2>();
     S.vox16 = c->vox_pal ? c->d_vox16.as<uint16_t>() : nullptr;
     S.prmap = c->d_prmap.as<int8_t>();
+    // the uploaded density array (still on the device) serves the positron
+    // range's lookups while it fits comfortably in L2; larger phantoms use
+    // the 16-bit palette records, which stay in L2 longer
+    const int64_t nvox = (int64_t)c->pdim[0] * c->pdim[1] * c->pdim[2];
+    S.den = nvox * 4 <= ((int64_t)64 << 20) ? c->d_den_stage.as<float>() : nullptr;
     S.prdmin = std::fmin(S.dx, std::fmin(S.dy, S.dz));
     S.npanels = c->geo.npanels;
     S.panels = c->d_panels.as<float>();
