@@ -93,3 +93,26 @@ def test_bench_reference_arm_under_torchrun_two_ranks():
     assert len(lines) == 1
     j = json.loads(lines[0])
     assert j["impl"] == "reference" and j["n_gpus"] == 2 and j["value"] > 0
+
+
+def test_bench_parity_vs_oracle_helper(data_dir, oracle_mod, tmp_path):
+    """The bench line's parity object: two independent acquisitions of one
+    scene agree (spectrum and crystal map chi-square p-values, per-decay
+    rates in standard deviations), and the oracle's seed is none the GPU
+    steps use."""
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    from gpet_gb300 import scenes
+    sc = scenes.positron(str(tmp_path), n_decays=400_000, nvox=48)
+    o = oracle_mod.OracleScene(sc.config_path, dict(sc.options, seed=99), data_dir, base_dir=sc.directory)
+    r = o.run(precision="fp32")
+    counts = {"n_decays": 400_000, **{k: r[k] for k in ("n_singles", "n_coinc", "n_true", "n_scatter", "n_random")}}
+    cb = bench.cpu_baseline(sc, 1.0, with_hists=True)
+    part = cb.pop("_parity")
+    assert part[2] == 4242 and "_parity" not in cb
+    p = bench._parity_vs_oracle(bench._singles_hists(r["singles"]), counts, 99, part)
+    assert p["singles_energy_350_650keV"]["ndf"] > 30 and p["singles_per_crystal"]["ndf"] == 63
+    assert p["singles_energy_350_650keV"]["p"] > 1e-4 and p["singles_per_crystal"]["p"] > 1e-4
+    assert set(p["rates"]) == {"singles", "coinc", "true", "scatter", "random"}
+    assert abs(p["rates"]["singles"]["sigma"]) < 5
