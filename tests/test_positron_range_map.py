@@ -67,15 +67,46 @@ def test_map_matches_its_definition(oracle_mod, shape):
         assert (want == -1).all()   # no voxel in [1, n-2] on every axis
 
 
-@pytest.mark.parametrize("nvox", [48, 128])
+def _anisotropic_scene(d):
+    """Voxels of 0.5 x 0.5 x 2 mm (x, y, z): water with a bone slab across z
+    and a lung ball, so that the closed form's reach bound (in units of the
+    smallest voxel side) is tried where one axis is four times coarser."""
+    import os
+    from gpet_gb300 import formats as F, scenes
+    nx, ny, nz = 96, 96, 24
+    c = scenes._base_config(d, (nx, ny, nz), (4.8, 4.8, 4.8), (-2.4, -2.4, -2.4))
+    c.useprange = 1
+    z = -2.4 + (np.arange(nz) + 0.5) * 0.2
+    y = -2.4 + (np.arange(ny) + 0.5) * 0.05
+    x = -2.4 + (np.arange(nx) + 0.5) * 0.05
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    mat = np.full((nz, ny, nx), scenes.MAT_WATER, np.int32)
+    den = np.full((nz, ny, nx), 1.0, np.float32)
+    slab = np.abs(Z - 0.5) < 0.3
+    mat[slab], den[slab] = scenes.MAT_BONE, 1.85
+    ball = X ** 2 + (Y - 0.6) ** 2 + (Z + 0.8) ** 2 < 0.7 ** 2
+    mat[ball], den[ball] = scenes.MAT_TISSUE, 0.3
+    F.write_phantom(c.matfile, c.denfile, mat, den)
+    F.write_geo(c.geofile, 8, (0, 0, 1), 45.0, (scenes.MAT_LYSO, scenes.MAT_AIR), (7.1, 0.001025),
+                scenes.ring_panel0(8.0, 8, 8, 0.298, 0.002, 2.0))
+    F.write_sources(c.sourcefile, [1_000_000_000], [0], [1], [(0, 0, 0, 2.2, 4.6, 0)])
+    F.write_config(os.path.join(d, "input_PET.in"), c)
+    return scenes.Scene(d, os.path.join(d, "input_PET.in"), {"n_decays": 1000, "seed": 3}, "anisotropic voxels")
+
+
+@pytest.mark.parametrize("nvox", [48, 128, "anisotropic"])
 def test_closed_form_equals_walk(oracle_mod, data_dir, tmp_path, nvox):
     """On the positron workload's phantom (water, bone rods, lung sphere),
-    positrons of the F-18 range started all over the source cylinder end where
-    the full walk ends them, to the rounding of the walk's steps, with the
-    same random words; most of them take the closed form."""
+    and on one of anisotropic voxels, positrons of the F-18 range started all
+    over the source cylinder end where the full walk ends them, to the
+    rounding of the walk's steps, with the same random words; most of them
+    take the closed form."""
     import pins
     from gpet_gb300 import scenes
-    sc = scenes.positron(str(tmp_path), n_decays=1000, nvox=nvox)
+    if nvox == "anisotropic":
+        sc = _anisotropic_scene(str(tmp_path))
+    else:
+        sc = scenes.positron(str(tmp_path), n_decays=1000, nvox=nvox)
     o = oracle_mod.OracleScene(sc.config_path, sc.options, data_dir, base_dir=sc.directory)
     with_map = o.s
     without = oracle_mod._Scene.from_buffer_copy(o.s)
@@ -85,7 +116,7 @@ def test_closed_form_equals_walk(oracle_mod, data_dir, tmp_path, nvox):
     n = 4000
     rr = 3.0 * np.sqrt(rng.random(n))
     ph = 2 * np.pi * rng.random(n)
-    x = np.stack([rr * np.cos(ph), rr * np.sin(ph), 6.0 * (rng.random(n) - 0.5)], 1).astype(np.float32)
+    x = np.stack([rr * np.cos(ph), rr * np.sin(ph), 4.4 * (rng.random(n) - 0.5)], 1).astype(np.float32)
     ek = rng.random(n) * 633e3
     tape = rng.integers(1, 2 ** 32 - 1, size=(n, pins.TAPE), dtype=np.uint64).astype(np.uint32)
     ends = {}
@@ -106,5 +137,4 @@ def test_closed_form_equals_walk(oracle_mod, data_dir, tmp_path, nvox):
     assert np.median(moved) > 0.01                    # ranges of a fraction of a millimetre
     exact = dist == 0.0
     assert exact.mean() < 0.9                          # most positrons took the closed form (not bit-equal)
-    prmap = o.prmap.reshape(nvox, nvox, nvox)
-    assert (prmap >= 2).mean() > 0.5
+    assert (o.prmap >= 2).mean() > 0.3
