@@ -72,3 +72,25 @@ def test_positron_walk_edges_bit_exact(data_dir, gpet_lib, oracle_mod, tmp_path)
     assert zero_slab.sum() > 0
     prange = o.prmap.reshape(32, 32, 32)
     assert (prange >= 2).mean() > 0.15 and (prange == 0).mean() > 0.05
+
+
+def test_positron_walk_anisotropic_voxels_bit_exact(data_dir, gpet_lib, oracle_mod, tmp_path):
+    """Voxels of 0.5 x 0.5 x 2 mm: the uniform-density map's reach bound in
+    units of the smallest side, the closed form, the jump and the walk give
+    the FP32 oracle's end points, singles and coincidences bit for bit."""
+    from test_positron_range_map import _anisotropic_scene
+    scene = _anisotropic_scene(str(tmp_path))
+    scene.options["n_decays"] = 300000
+    ctx = make_ctx(scene, data_dir, record_source=1)
+    st = ctx.run()
+    o = oracle_for(scene, data_dir, panels=ctx.panels())
+    r = o.run(precision="fp32", source=True)
+    src = ctx.source_records()
+    osrc = r["source"][r["source"]["t"] > 0]
+    assert len(src) == len(osrc) > 500000
+    assert np.array_equal(src.view(np.uint8), osrc.view(np.uint8))
+    singles, _ = ctx.singles()
+    pairs, cls = ctx.coincidences()
+    assert np.array_equal(singles.view(np.uint8), r["singles"].view(np.uint8))
+    assert np.array_equal(pairs, r["coinc"]) and np.array_equal(cls, r["coinc_class"])
+    assert st["n_singles"] > 1000
