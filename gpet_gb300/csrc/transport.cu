@@ -127,6 +127,12 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2], bool& wal
     return 2;
 }
 
+// walk list of a positron walk of about `est` voxel steps
+__device__ __forceinline__ int walk_list(float est)
+{
+    return est < 1.5f ? 0 : (est < 3.0f ? 1 : (est < 6.0f ? 2 : 3));
+}
+
 // source stage: one thread per decay, the emitted pair (or PSF photon) goes
 // to a structure-of-arrays buffer. kMulti: the decays of a wave belong to
 // several simulations and each thread reads its own simulation's descriptor;
@@ -134,11 +140,6 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2], bool& wal
 // positron range needs the voxel walk are appended to one of the wave's
 // kWalkLists walk lists by their estimated number of steps (one atomic per
 // warp and list), and their position is written by k_walk.
-__device__ __forceinline__ int walk_list(float est)
-{
-    return est < 1.5f ? 0 : (est < 3.0f ? 1 : (est < 6.0f ? 2 : 3));
-}
-
 template <bool kMulti>
 __global__ void __launch_bounds__(256, 6) k_source(const Wave* waves, int wi, PairBuf pb, Counters* cnt)
 {
