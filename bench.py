@@ -52,8 +52,8 @@ def algorithmic_bytes_phantom(n_photons, ph_steps, entered):
 
 # DRAM bytes per photon slot of k_phantom measured by ncu (dram__bytes_read.sum
 # + dram__bytes_write.sum of one launch of 4,194,304 decays of this workload,
-# 8,388,608 photon slots: 310.9 MB + 36.0 MB; profiles/k_phantom_positron_4M.md)
-MEASURED_DRAM_BYTES_PER_PHOTON = (310.944256e6 + 35.95776e6) / 8388608
+# 8,388,608 photon slots: 311.1 MB + 36.1 MB; profiles/k_phantom_positron_4M.md)
+MEASURED_DRAM_BYTES_PER_PHOTON = (311.065088e6 + 36.134656e6) / 8388608
 
 
 def _peaks():
