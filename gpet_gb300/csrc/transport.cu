@@ -130,7 +130,7 @@ __device__ int sample_decay(const SimDesc& S, int64_t d, Photon ph[2], bool& wal
 // walk list of a positron walk of about `est` voxel steps
 __device__ __forceinline__ int walk_list(float est)
 {
-    return est < 1.5f ? 0 : (est < 3.0f ? 1 : (est < 6.0f ? 2 : 3));
+    return est < 4.0f ? 0 : (est < 8.0f ? 1 : (est < 16.0f ? 2 : 3));
 }
 
 // source stage: one thread per decay, the emitted pair (or PSF photon) goes
